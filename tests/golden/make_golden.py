@@ -1,0 +1,179 @@
+"""Generate the golden fixtures in this folder by running the PYSEQM reference.
+
+This script is the only place that executes the reference.  It needs a PYSEQM
+checkout (default /root/reference) and runs on the CPU in float64.  ``h5py`` is
+only needed by the reference's MD module, so a stub stands in for it.
+
+Each fixture records the inputs (species, coordinates, seqm settings) and the
+reference's outputs: Etot/Eelec/Enuc/Hf/Eiso, autograd forces, the converged
+density (packed per molecule, hydrogen p-slots removed), orbital energies, the
+SCF loop count (calls of ``fock_restricted`` minus the one before and the one
+after the loop), per-molecule loop counts (each molecule run alone), and for the
+"stages" fixtures the hcore blocks and two-electron integrals.
+
+Usage:  python tests/golden/make_golden.py [/path/to/PYSEQM]
+"""
+
+import json
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+
+sys.path.insert(0, REPO)
+sys.path.insert(0, REF)
+h5 = types.ModuleType("h5py")
+h5.Group = h5.File = h5.Dataset = type("Stub", (), {})
+sys.modules.setdefault("h5py", h5)
+
+import torch  # noqa: E402
+
+torch.set_default_dtype(torch.float64)
+
+import seqm.seqm_functions.scf_loop as scf_loop_mod  # noqa: E402
+from seqm.basics import Energy  # noqa: E402
+from seqm.ElectronicStructure import Electronic_Structure  # noqa: E402
+from seqm.Molecule import Molecule  # noqa: E402
+from seqm.seqm_functions.constants import Constants  # noqa: E402
+from seqm.seqm_functions.hcore import hcore as ref_hcore  # noqa: E402
+from seqm.seqm_functions.read_xyz import read_xyz  # noqa: E402
+
+from pyseqm_gb300 import workloads  # noqa: E402
+
+_calls = [0]
+_orig_fock = scf_loop_mod.fock_restricted
+
+
+def _counting_fock(*a, **k):
+    _calls[0] += 1
+    return _orig_fock(*a, **k)
+
+
+scf_loop_mod.fock_restricted = _counting_fock
+
+
+def packed_P(P, species):
+    out = []
+    for m in range(species.shape[0]):
+        nh = int(np.sum(species[m] > 1))
+        ny = int(np.sum(species[m] == 1))
+        idx = np.concatenate([np.arange(4 * nh), 4 * nh + 4 * np.arange(ny)])
+        out.append(P[m][np.ix_(idx, idx)].tolist())
+    return out
+
+
+def run_es(species, coords, settings, learned=None):
+    const = Constants()
+    sp = dict(settings)
+    sp["learned"] = list(learned.keys()) if learned else []
+    sp.pop("elements", None)
+    species_t = torch.as_tensor(species, dtype=torch.int64)
+    coords_t = torch.as_tensor(coords, dtype=torch.float64)
+    mol = Molecule(const, sp, coords_t, species_t)
+    mol.verbose = False
+    _calls[0] = 0
+    if learned:
+        Z = mol.Z
+        lp = {k: torch.as_tensor(np.asarray(v(Z.numpy())), dtype=torch.float64).requires_grad_(True)
+              for k, v in learned.items()}
+        mol.coordinates.requires_grad_(True)
+        out = Energy(sp)(mol, learned_parameters=lp, all_terms=True)
+        Hf, Etot, Eelec, Enuc, Eiso, EnucAB, e_gap, e, P, charge, nc = out
+        Etot.sum().backward()
+        grads = {k: mol.parameters[k].grad.detach().numpy().tolist() for k in learned}
+        res = dict(Hf=Hf.detach().numpy().tolist(), Etot=Etot.detach().numpy().tolist(),
+                   Eelec=Eelec.detach().numpy().tolist(), Enuc=Enuc.detach().numpy().tolist(),
+                   Eiso=Eiso.detach().numpy().tolist(), e=e.detach().numpy().tolist(),
+                   P=packed_P(P.detach().numpy(), species), notconverged=nc.numpy().tolist(),
+                   dEtot_dR=mol.coordinates.grad.detach().numpy().tolist(), param_grads=grads,
+                   loop_count=_calls[0] - 2, Z=Z.numpy().tolist())
+        return res
+    es = Electronic_Structure(sp)
+    es(mol)
+    return dict(Hf=mol.Hf.detach().numpy().tolist(), Etot=mol.Etot.detach().numpy().tolist(),
+                Eelec=mol.Eelec.detach().numpy().tolist(), Enuc=mol.Enuc.detach().numpy().tolist(),
+                Eiso=mol.Eiso.detach().numpy().tolist(), force=mol.force.detach().numpy().tolist(),
+                e=mol.e_mo.detach().numpy().tolist(), P=packed_P(mol.dm.numpy(), species),
+                notconverged=es.notconverged.numpy().tolist(), loop_count=_calls[0] - 2,
+                q=mol.q.detach().numpy().tolist())
+
+
+def stages(species, coords, method):
+    const = Constants()
+    sp = {"method": method, "scf_eps": 1e-6, "scf_converger": [1]}
+    mol = Molecule(const, sp, torch.as_tensor(coords), torch.as_tensor(species, dtype=torch.int64))
+    M, w, *_ = ref_hcore(mol)
+    M = M.detach().numpy()
+    return dict(M_diag=M[mol.maskd.numpy()].tolist(), M_pair=M[mol.mask.numpy()].tolist(),
+                w=w.detach().numpy().tolist(), idxi=mol.idxi.numpy().tolist(), idxj=mol.idxj.numpy().tolist())
+
+
+def write(name, species, coords, settings, per_molecule=False, learned=None, with_stages=False, ref_json=None):
+    species = np.asarray(species)
+    coords = np.asarray(coords, dtype=np.float64)
+    rec = dict(name=name, settings=settings, species=species.tolist(), coords=coords.tolist())
+    rec["ref"] = run_es(species, coords, settings, learned)
+    if per_molecule:
+        counts = []
+        for m in range(species.shape[0]):
+            n = int(np.sum(species[m] > 0))
+            counts.append(run_es(species[m:m + 1, :n], coords[m:m + 1, :n], settings)["loop_count"])
+        rec["ref"]["loop_count_per_molecule"] = counts
+    if with_stages:
+        rec["stages"] = stages(species, coords, settings["method"])
+    if ref_json:
+        with open(os.path.join(REF, "tests", "reference", ref_json)) as f:
+            rec["reference_test_json"] = json.load(f)
+    with open(os.path.join(HERE, f"{name}.json"), "w") as f:
+        json.dump(rec, f)
+    print(name, "loop_count", rec["ref"]["loop_count"])
+
+
+def main():
+    data = os.path.join(REF, "tests", "data")
+    sp_m, c_m = read_xyz([os.path.join(data, "methane.xyz")])
+    for method in ("MNDO", "AM1", "PM3"):
+        write(f"smoke_{method}", sp_m, c_m, {"method": method, "scf_eps": 1e-6, "scf_converger": [1]},
+              ref_json=f"smoke_single_point_{method}.json", with_stages=(method == "AM1"))
+    sp_b, c_b = read_xyz([os.path.join(data, "methane.xyz"), os.path.join(data, "benzene.xyz")])
+    write("batch_am1", sp_b, c_b, {"method": "AM1", "scf_eps": 1e-6, "scf_converger": [1]},
+          ref_json="batch_single_point_am1.json")
+    write("force_mixed_am1", sp_b, c_b, {"method": "AM1", "scf_eps": 1e-7, "scf_converger": [1]},
+          ref_json="ground_force_batch_mixed.json")
+    sp_f, c_f = read_xyz([os.path.join(data, f"methanal.{i}.xyz") for i in (1, 2, 3)])
+    write("force_methanal_am1", sp_f, c_f, {"method": "AM1", "scf_eps": 1e-7, "scf_converger": [1]},
+          ref_json="ground_force_batch_methanal.json")
+
+    sp, c = workloads.pad_batch(workloads.butane_batch(4, seed=1))
+    write("butane_pm3_linear", sp, c, {"method": "PM3", "scf_eps": 1e-8, "scf_converger": [0, 0.1]},
+          per_molecule=True, with_stages=True)
+    mols = workloads.mixed_batch(8, seed=2, alkane_range=(1, 6), water_range=(2, 6))
+    sp, c = workloads.pad_batch(mols)
+    write("mixed_am1", sp, c, {"method": "AM1", "scf_eps": 1e-8, "scf_converger": [1]}, per_molecule=True,
+          with_stages=True)
+    write("mixed_am1_sp2", sp, c, {"method": "AM1", "scf_eps": 1e-8, "scf_converger": [1], "sp2": [True, 1e-7]})
+    mols = workloads.mixed_batch(6, seed=3, alkane_range=(2, 8), water_range=(3, 9))
+    sp, c = workloads.pad_batch(mols)
+    write("mixed_pm3_linear", sp, c, {"method": "PM3", "scf_eps": 1e-8, "scf_converger": [0, 0.1]},
+          per_molecule=True)
+    write("mixed_mndo", sp, c, {"method": "MNDO", "scf_eps": 1e-8, "scf_converger": [1]})
+
+    rng = np.random.default_rng(4)
+    mols = [workloads.alkane(8, rng, 0.05), workloads.water_cluster(4, rng)]
+    sp, c = workloads.pad_batch(mols)
+    import json as _json
+    with open(os.path.join(REPO, "pyseqm_gb300", "data", "params_MNDO.json")) as f:
+        tab = _json.load(f)
+    rows = np.asarray(tab["rows"])
+    fld = tab["fields"]
+    learned = {k: (lambda Z, k=k: rows[Z, fld.index(k)]) for k in ("U_ss", "U_pp", "beta_s", "beta_p")}
+    write("mndo_param_grads", sp, c, {"method": "MNDO", "scf_eps": 1e-8, "scf_converger": [1]}, learned=learned)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,64 @@
+"""The CPU oracle against golden outputs of the reference (pins the oracle)."""
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_NAMES, load_golden
+from oracle import seqm_oracle as O
+
+
+def _packed(out, m):
+    idx = O.packed_index(out["mol"]["nheavy"][m], out["mol"]["nhyd"][m])
+    return out["P"][m][np.ix_(idx, idx)]
+
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_oracle_matches_reference(name):
+    g = load_golden(name)
+    s, ref = g["settings"], g["ref"]
+    out = O.single_point(s["method"], g["species_np"], g["coords_np"], s["scf_eps"], tuple(s["scf_converger"]),
+                         tuple(s.get("sp2", [False])))
+    sp2 = s.get("sp2", [False])[0]
+    # energies 1e-6 eV, density 1e-7 (the eigensolver path agrees to ~1e-12)
+    tolE, tolP = (1e-6, 1e-7)
+    for key in ("Etot", "Eelec", "Enuc", "Hf", "Eiso"):
+        np.testing.assert_allclose(out[key], ref[key], atol=tolE, rtol=0)
+    for m in range(g["species_np"].shape[0]):
+        np.testing.assert_allclose(_packed(out, m), np.asarray(ref["P"][m]), atol=tolP, rtol=0)
+    assert int(np.max(out["iters"])) in (ref["loop_count"], ref["loop_count"] - 1, ref["loop_count"] + 1)
+    if "loop_count_per_molecule" in ref:
+        assert np.all(np.abs(out["iters"] - np.asarray(ref["loop_count_per_molecule"])) <= (1 if sp2 else 0))
+    if not sp2:
+        for m in range(g["species_np"].shape[0]):
+            n = out["mol"]["nheavy"][m] * 4 + out["mol"]["nhyd"][m]
+            np.testing.assert_allclose(out["e"][m][:n], np.asarray(ref["e"][m])[:n], atol=1e-8, rtol=0)
+    if "stages" in g:
+        st = g["stages"]
+        mol = out["mol"]
+        np.testing.assert_allclose(out["ints"]["w"], np.asarray(st["w"]), atol=1e-12, rtol=0)
+        np.testing.assert_allclose(out["M"][mol["maskd"]], np.asarray(st["M_diag"]), atol=1e-12, rtol=0)
+        np.testing.assert_allclose(out["M"][mol["mask"]], np.asarray(st["M_pair"]), atol=1e-12, rtol=0)
+    if "reference_test_json" in g:
+        # the reference's own committed golden values (tests/reference/*.json)
+        rj = g["reference_test_json"]
+        if "Etot" in rj:
+            np.testing.assert_allclose(np.ravel(out["Etot"]), np.ravel(rj["Etot"]), atol=1e-5, rtol=1e-5)
+
+
+@pytest.mark.parametrize("name", ["smoke_MNDO", "smoke_AM1", "smoke_PM3", "force_methanal_am1"])
+def test_oracle_forces_match_reference_autograd(name):
+    g = load_golden(name)
+    s = g["settings"]
+    out = O.single_point(s["method"], g["species_np"], g["coords_np"], s["scf_eps"], tuple(s["scf_converger"]),
+                         forces=True)
+    np.testing.assert_allclose(out["force"], np.asarray(g["ref"]["force"]), atol=1e-6, rtol=0)
+
+
+def test_oracle_rejects_odd_electrons():
+    with pytest.raises(ValueError):
+        O.parse(np.array([[6, 1, 1, 1]]), np.zeros((1, 4, 3)) + np.arange(4)[None, :, None])
+
+
+def test_oracle_rejects_unsorted_species():
+    with pytest.raises(ValueError):
+        O.parse(np.array([[1, 6]]), np.array([[[0, 0, 0], [1.1, 0, 0]]], dtype=float))

@@ -1,0 +1,135 @@
+/*
+ * pyseqm_gb300 — C ABI of the GB300 (sm_103a) batched semi-empirical SCF library.
+ *
+ * Every pointer argument is DEVICE memory unless the name ends in _host.  Every
+ * entry point returns 0 on success or a negative SEQM_E* code, launches its work
+ * on the given CUDA stream (a cudaStream_t passed as void*; NULL = legacy default
+ * stream) and does not synchronise unless it says so.
+ *
+ * Data layout (ragged, unpadded):
+ *   molecules m = 0..nmol-1; atoms of molecule m are atom_off[m] .. atom_off[m+1]-1,
+ *   heavy atoms (Z>1) first, then hydrogens (the seqm API's descending-Z order);
+ *   the molecule's packed AO basis has norb = 4*nheavy + nhyd functions
+ *   (s,px,py,pz per heavy atom, then one s per hydrogen; the order of
+ *   seqm/seqm_functions/pack.py:8-17);
+ *   every per-molecule square matrix (F, P, Hcore, eigenvectors) is a dense
+ *   row-major norb x norb FP64 block starting at mat_off[m] of one flat array;
+ *   atom pairs (i<j inside a molecule) are split in three class segments:
+ *   heavy-heavy [0,nxx), heavy-H [nxx,nxx+nxh), H-H [nxx+nxh, npairs); the
+ *   two-electron integrals of pair p are w_xx[100*p] (10x10, row = atom i's
+ *   orbital product, col = atom j's, product order ss,pxs,pxpx,pys,pypx,pypy,
+ *   pzs,pzpx,pzpy,pzpz), w_xh[10*(p-nxx)] (column 0 only) and w_hh[p-nxx-nxh].
+ */
+#ifndef PYSEQM_GB300_H
+#define PYSEQM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SEQM_OK 0
+#define SEQM_E_ARG (-1)       /* bad argument or size */
+#define SEQM_E_CUDA (-2)      /* a CUDA launch or API call failed */
+#define SEQM_E_UNSUPPORTED (-3) /* element / method not supported (ValueError in the reference) */
+#define SEQM_E_TOO_LARGE (-4) /* molecule larger than the density kernel's limit */
+
+/* methods */
+#define SEQM_MNDO 0
+#define SEQM_AM1 1
+#define SEQM_PM3 2
+
+/* per-atom parameter slots of seqm_batch.atom_par (structure of arrays, natoms each) */
+enum {
+  SEQM_P_USS = 0, SEQM_P_UPP, SEQM_P_ZS, SEQM_P_ZP, SEQM_P_BS, SEQM_P_BP, SEQM_P_GSS, SEQM_P_GSP,
+  SEQM_P_GPP, SEQM_P_GP2, SEQM_P_HSP, SEQM_P_ALPHA,
+  SEQM_P_K1, SEQM_P_K2, SEQM_P_K3, SEQM_P_K4, SEQM_P_L1, SEQM_P_L2, SEQM_P_L3, SEQM_P_L4,
+  SEQM_P_M1, SEQM_P_M2, SEQM_P_M3, SEQM_P_M4,
+  /* derived by seqm_hcore: multipole separations and additive terms, valence charge, n */
+  SEQM_P_DD, SEQM_P_QQ, SEQM_P_RHO0, SEQM_P_RHO1, SEQM_P_RHO2, SEQM_P_TORE, SEQM_P_QN,
+  SEQM_NPAR
+};
+
+typedef struct seqm_batch {
+  int32_t nmol, natoms, nxx, nxh, nhh, method, max_norb, pad_;
+  const int32_t *mol_atom_off;  /* [nmol+1] */
+  const int32_t *mol_nheavy;    /* [nmol] */
+  const int32_t *mol_norb;      /* [nmol] */
+  const int32_t *mol_nocc;      /* [nmol] */
+  const int64_t *mol_mat_off;   /* [nmol+1] element offsets of the dense per-molecule matrices */
+  const int32_t *mol_xx_off;    /* [nmol+1] pair offsets inside the heavy-heavy segment */
+  const int32_t *mol_xh_off;    /* [nmol+1] ... heavy-H segment (relative to nxx) */
+  const int32_t *mol_hh_off;    /* [nmol+1] ... H-H segment (relative to nxx+nxh) */
+  const int32_t *mol_order;     /* [nmol] molecules by descending norb (scheduling order of per-molecule kernels) */
+  const int32_t *atom_Z;        /* [natoms] */
+  const int32_t *atom_mol;      /* [natoms] */
+  const double *atom_xyz;       /* [natoms*3] Angstrom */
+  double *atom_par;             /* [SEQM_NPAR*natoms] parameters (SoA), derived slots written by seqm_hcore */
+  const int32_t *pair_i;        /* [npairs] global index of the first (heavier or equal) atom */
+  const int32_t *pair_j;        /* [npairs] global index of the second atom */
+} seqm_batch;
+
+/* Integrals + core Hamiltonian.  Replaces hcore(molecule) (seqm/seqm_functions/hcore.py:9-179),
+ * which calls two_elec_two_center_int (two_elec_two_center_int.py:98-283) and
+ * diatom_overlap_matrix_PM6_SP (diat_overlap_PM6_SP.py:6-444).  Writes the derived
+ * per-atom slots, w_xx/w_xh/w_hh, the full symmetric Hcore (H, dense per molecule) and
+ * the core-core repulsion of every pair (enuc_pair, energy.py:91-134, needs w[0,0]). */
+int seqm_hcore(const seqm_batch *b, double *w_xx, double *w_xh, double *w_hh, double *H, double *enuc_pair,
+               void *stream);
+
+/* Fock matrix F = H + G(P) for the molecules with active[m] != 0 (all if active == NULL).
+ * Replaces fock(...) (seqm/seqm_functions/fock.py:132-181).  F is full and symmetric. */
+int seqm_fock(const seqm_batch *b, const double *P, const double *H, const double *w_xx, const double *w_xh,
+              const double *w_hh, double *F, const uint8_t *active, void *stream);
+
+/* Batched symmetric eigensolver (cyclic Jacobi, FP64, one CTA per molecule, norb <= 160) and
+ * closed-shell density P = 2 C_occ C_occ^T.  Replaces sym_eig_trunc(F, nHeavy, nHydro, nocc)
+ * (seqm/seqm_functions/diag.py:110-241).  evals[mol_row_off[m]..] receives the ascending
+ * eigenvalues (mol_row_off = prefix sum of norb), evecs (NULL: skip) the eigenvectors as
+ * ROWS of the molecule's norb x norb block (row k <-> evals k), P the density (NULL: skip).
+ * work: scratch of mat_off[nmol] doubles (unsorted eigenvector rows).
+ * status[m]: number of sweeps, or -1 if the sweep cap was hit. */
+int seqm_density_jacobi(const seqm_batch *b, const double *F, double *P, double *evals, double *evecs,
+                        double *work, const int64_t *mol_row_off, const uint8_t *active, int32_t *status,
+                        int max_sweeps, void *stream);
+
+/* SP2 purification (FP64), replaces SP2(a, nocc, eps) (seqm/seqm_functions/SP2.py:9-85)
+ * applied per molecule to its packed Fock matrix (eps clamped to [1e-7, 1e-3] as there).
+ * work: scratch of 2*mat_off[nmol] + 4*nmol doubles.  P = 2 X at convergence.
+ * status[m]: SP2 steps taken, or -1 if max_iter was hit.  Synchronises the stream once per
+ * SP2 step to test convergence. */
+int seqm_density_sp2(const seqm_batch *b, const double *F, double *P, double *work, double eps,
+                     const uint8_t *active, int32_t *status, int max_iter, void *stream);
+
+/* One mixing step for active molecules.  Replaces the P update of scf_forward0 (linear,
+ * scf_loop.py:258-267: P <- alpha P + (1-alpha) Pnew) and scf_forward1 (adaptive,
+ * adaptive_mix, scf_loop.py:360-420).  iters[m] counts the molecule's density steps and is
+ * incremented here (the adaptive mixer keys on the 1-based count), old2 = diagonal of P
+ * from two steps before (at mol_row_off[m]).  Pold receives P before the update. */
+int seqm_mix(const seqm_batch *b, double *P, const double *Pnew, double *Pold, double *old2,
+             const int64_t *mol_row_off, int32_t *iters, int linear, double alpha, const uint8_t *active,
+             void *stream);
+
+/* Electronic energy 1/2 sum P(H+F) per molecule (energy.py:26-49) for active molecules, and
+ * the SCF convergence test of get_error (scf_loop.py:106-147): updates err, dm_err, dm_el,
+ * Eelec (the previous energy), clears active[m] for molecules that converged, and writes
+ * Eout[m] = the new energy.  When Pold == NULL only the energy is computed. */
+int seqm_energy_error(const seqm_batch *b, const double *P, const double *Pold, const double *H,
+                      const double *F, double *Eelec, double *Eout, double *err, double *dm_err,
+                      double *dm_el, uint8_t *active, double eps, void *stream);
+
+/* Diagonal initial density (scf_loop.py:2066-2081): tore/4 on heavy-atom s,p; 1 on H s. */
+int seqm_initial_density(const seqm_batch *b, double *P, void *stream);
+
+/* Per-molecule sums of per-pair core-core energies: Enuc[m] (energy.py:177-192). */
+int seqm_pair_sum(const seqm_batch *b, const double *pair_val, double *mol_sum, void *stream);
+
+/* Library build string (host memory; no GPU needed). */
+const char *seqm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,52 @@
+// Shared definitions of the pyseqm_gb300 CUDA kernels (sm_103a, FP64).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/pyseqm_gb300.h"
+
+namespace seqm {
+
+// seqm/seqm_functions/constants.py:4,9 — MOPAC's eV per hartree and bohr radius
+constexpr double EV = 27.21;
+constexpr double A0 = 0.529167;
+constexpr double OVERLAP_CUTOFF = 40.0;  // bohr, constants.py:23
+
+// packed index (0..9) of the upper-triangle product (row, col) of one atom's s,px,py,pz
+// (fock.py:7-18 order: ss, s-px, px-px, s-py, px-py, py-py, s-pz, px-pz, py-pz, pz-pz)
+__host__ __device__ constexpr int k10_row(int k) {
+  return k == 0 ? 0 : k == 1 ? 0 : k == 2 ? 1 : k == 3 ? 0 : k == 4 ? 1 : k == 5 ? 2 : k == 6 ? 0 : k == 7 ? 1 : k == 8 ? 2 : 3;
+}
+__host__ __device__ constexpr int k10_col(int k) { return k == 0 ? 0 : k <= 2 ? 1 : k <= 5 ? 2 : 3; }
+// kind(mu, nu) -> packed index (fock.py:74-79)
+__host__ __device__ constexpr int kind(int mu, int nu) {
+  return mu >= nu ? (mu * (mu + 1)) / 2 + nu : (nu * (nu + 1)) / 2 + mu;
+}
+
+__device__ __forceinline__ double par(const seqm_batch &b, int slot, int atom) {
+  return b.atom_par[(size_t)slot * b.natoms + atom];
+}
+
+// row-major index of pair (i<j) among n items (0-based i, j)
+__host__ __device__ __forceinline__ int tri_index(int i, int j, int n) { return i * n - (i * (i + 1)) / 2 + (j - i - 1); }
+
+// first atom of the molecule owning global pair index p of a class segment: binary search on offsets
+__device__ __forceinline__ int find_mol(const int32_t *off, int nmol, int p) {
+  int lo = 0, hi = nmol;  // off[lo] <= p < off[hi]
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (off[mid] <= p) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// AO index of local atom la inside its molecule's packed basis (heavy: 4 per atom, H: 1)
+__device__ __forceinline__ int atom_ao(int la, int nheavy) { return la < nheavy ? 4 * la : 3 * nheavy + la; }
+
+inline int launch_check() {
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? SEQM_OK : SEQM_E_CUDA;
+}
+
+}  // namespace seqm

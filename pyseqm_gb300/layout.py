@@ -1,0 +1,185 @@
+"""Ragged, unpadded batch layout of molecules -> atoms -> atom pairs.
+
+``Layout.from_padded`` takes the seqm API's padded input (species sorted by
+descending Z per row, zero padding) and builds, on the host with NumPy:
+
+* per molecule: atom / pair-class / dense-matrix / basis-row offsets, norb, nocc;
+* per atom: Z, owning molecule, coordinates, parameters (structure of arrays);
+* per pair: the two atom indices, in three class segments (heavy-heavy, heavy-H,
+  H-H) each enumerated row-major inside its molecule (the index arithmetic the
+  kernels use to find an atom's pairs).
+
+``to_device`` uploads it once; ``struct`` returns the ``seqm_batch`` C struct
+pointing at the device copies.  ``packed_to_padded`` / ``padded_to_packed``
+convert per-molecule matrices to and from the reference's padded
+``(nmol, 4*molsize, 4*molsize)`` layout (seqm/seqm_functions/pack.py:8-96).
+"""
+
+import numpy as np
+import torch
+
+from . import native, tables
+
+
+def _group_fill(dest, off, counts, key_arrays, maker):
+    """Fill dest[off[m] + k] for molecule groups sharing the same key (sizes)."""
+    keys = np.stack(key_arrays, axis=1) if len(key_arrays) > 1 else key_arrays[0][:, None]
+    uniq, inv = np.unique(keys, axis=0, return_inverse=True)
+    for g, key in enumerate(uniq):
+        ms = np.nonzero(inv.reshape(-1) == g)[0]
+        loc = maker(*key)  # tuple of arrays, each (L,)
+        L = loc[0].size
+        if L == 0:
+            continue
+        idx = off[ms][:, None] + np.arange(L)[None, :]
+        for d, v in zip(dest, loc):
+            d[0][idx] = d[1][ms][:, None] + v[None, :]
+
+
+class Layout:
+    def __init__(self):
+        self.dev = None
+
+    # ------------------------------------------------------------------ build
+    @classmethod
+    def from_padded(cls, species, coords, method, charges=None, learned=None):
+        species = np.ascontiguousarray(np.asarray(species, dtype=np.int64))
+        coords = np.asarray(coords, dtype=np.float64)
+        if species.ndim != 2 or coords.shape != species.shape + (3,):
+            raise ValueError("species must be (nmol, molsize) and coordinates (nmol, molsize, 3)")
+        if not np.all(species[:, :-1] >= species[:, 1:]):
+            bad = np.nonzero(~np.all(species[:, :-1] >= species[:, 1:], axis=1))[0].tolist()
+            raise ValueError(f"species must be non-increasing along each row, but rows {bad} are not sorted.")
+        if method not in tables.METHOD_FIELDS:
+            raise ValueError(f"unsupported method {method!r}; supported: MNDO, AM1, PM3")
+        el = tables.elements()
+        L = cls()
+        L.method = method
+        L.nmol, L.molsize = species.shape
+        real = species > 0
+        L.natoms_m = real.sum(1).astype(np.int64)
+        L.nheavy = (species > 1).sum(1).astype(np.int64)
+        L.nhyd = (species == 1).sum(1).astype(np.int64)
+        L.norb = 4 * L.nheavy + L.nhyd
+        nel = el["tore"][species].sum(1).astype(np.int64)
+        if charges is not None:
+            nel = nel - np.asarray(charges, dtype=np.float64).reshape(-1).astype(np.int64)
+        if np.any(nel % 2 == 1):
+            raise ValueError("RHF setting requires closed shell systems (even number of electrons)")
+        L.nocc = nel // 2
+        L.atom_off = np.concatenate([[0], np.cumsum(L.natoms_m)])
+        L.natoms = int(L.atom_off[-1])
+        L.real_index = np.nonzero(real.reshape(-1))[0]  # flat padded index of every real atom
+        L.Z = species.reshape(-1)[L.real_index]
+        if np.any(el["qn"][L.Z] > 3) or np.any(L.Z == 2):
+            raise ValueError("Error from diat.py, overlap matrix\nSome elements are not supported yet")
+        L.xyz = coords.reshape(-1, 3)[L.real_index]
+        L.atom_mol = np.repeat(np.arange(L.nmol), L.natoms_m)
+        L.mat_off = np.concatenate([[0], np.cumsum(L.norb * L.norb)]).astype(np.int64)
+        L.row_off = np.concatenate([[0], np.cumsum(L.norb)]).astype(np.int64)
+        nh, ny = L.nheavy, L.nhyd
+        L.nxx_m, L.nxh_m, L.nhh_m = nh * (nh - 1) // 2, nh * ny, ny * (ny - 1) // 2
+        L.xx_off = np.concatenate([[0], np.cumsum(L.nxx_m)])
+        L.xh_off = np.concatenate([[0], np.cumsum(L.nxh_m)])
+        L.hh_off = np.concatenate([[0], np.cumsum(L.nhh_m)])
+        L.nxx, L.nxh, L.nhh = int(L.xx_off[-1]), int(L.xh_off[-1]), int(L.hh_off[-1])
+        L.npairs = L.nxx + L.nxh + L.nhh
+        pi = np.empty(L.npairs, dtype=np.int64)
+        pj = np.empty(L.npairs, dtype=np.int64)
+        a0 = L.atom_off[:-1]
+        _group_fill([(pi[: L.nxx], a0), (pj[: L.nxx], a0)], L.xx_off, None, [nh],
+                    lambda n: np.triu_indices(n, 1))
+        _group_fill([(pi[L.nxx: L.nxx + L.nxh], a0), (pj[L.nxx: L.nxx + L.nxh], a0 + nh)], L.xh_off, None, [nh, ny],
+                    lambda a, b: (np.repeat(np.arange(a), b), np.tile(np.arange(b), a)))
+        _group_fill([(pi[L.nxx + L.nxh:], a0 + nh), (pj[L.nxx + L.nxh:], a0 + nh)], L.hh_off, None, [ny],
+                    lambda n: np.triu_indices(n, 1))
+        L.pair_i, L.pair_j = pi, pj
+        L.order = np.argsort(-L.norb, kind="stable")
+        L.max_norb = int(L.norb.max()) if L.nmol else 0
+        # per-atom parameters, structure of arrays
+        fields, rows = tables.method_table(method)
+        par = np.zeros((native.NPAR, L.natoms))
+        for k, f in enumerate(fields):
+            par[native.PAR[f]] = rows[L.Z, k]
+        par[native.PAR["_tore"]] = el["tore"][L.Z]
+        par[native.PAR["_qn"]] = el["qn"][L.Z]
+        if learned:
+            for k, v in learned.items():
+                par[native.PAR[k]] = np.asarray(v, dtype=np.float64).reshape(-1)
+        L.par = par
+        return L
+
+    # ----------------------------------------------------------------- device
+    def to_device(self, device="cuda"):
+        i32 = lambda a: torch.as_tensor(np.asarray(a, dtype=np.int32), device=device)  # noqa: E731
+        i64 = lambda a: torch.as_tensor(np.asarray(a, dtype=np.int64), device=device)  # noqa: E731
+        f64 = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device=device)  # noqa: E731
+        d = {
+            "atom_off": i32(self.atom_off), "nheavy": i32(self.nheavy), "norb": i32(self.norb),
+            "nocc": i32(self.nocc), "mat_off": i64(self.mat_off), "row_off": i64(self.row_off),
+            "xx_off": i32(self.xx_off), "xh_off": i32(self.xh_off), "hh_off": i32(self.hh_off),
+            "order": i32(self.order), "Z": i32(self.Z), "atom_mol": i32(self.atom_mol),
+            "xyz": f64(self.xyz.reshape(-1)), "par": f64(self.par.reshape(-1)),
+            "pair_i": i32(self.pair_i), "pair_j": i32(self.pair_j),
+        }
+        self.dev = d
+        self.device = torch.device(device)
+        self._struct = native.SeqmBatch(
+            nmol=self.nmol, natoms=self.natoms, nxx=self.nxx, nxh=self.nxh, nhh=self.nhh,
+            method=native.METHODS[self.method], max_norb=self.max_norb, pad_=0,
+            mol_atom_off=d["atom_off"].data_ptr(), mol_nheavy=d["nheavy"].data_ptr(), mol_norb=d["norb"].data_ptr(),
+            mol_nocc=d["nocc"].data_ptr(), mol_mat_off=d["mat_off"].data_ptr(), mol_xx_off=d["xx_off"].data_ptr(),
+            mol_xh_off=d["xh_off"].data_ptr(), mol_hh_off=d["hh_off"].data_ptr(), mol_order=d["order"].data_ptr(),
+            atom_Z=d["Z"].data_ptr(), atom_mol=d["atom_mol"].data_ptr(), atom_xyz=d["xyz"].data_ptr(),
+            atom_par=d["par"].data_ptr(), pair_i=d["pair_i"].data_ptr(), pair_j=d["pair_j"].data_ptr(),
+        )
+        return self
+
+    def set_coordinates(self, xyz_real):
+        """Replace the device coordinates (natoms, 3) in place (same molecules, new geometry)."""
+        self.dev["xyz"].copy_(torch.as_tensor(xyz_real, dtype=torch.float64).reshape(-1))
+
+    @property
+    def struct(self):
+        return self._struct
+
+    # ------------------------------------------------------------ conversions
+    def packed_index(self):
+        """For each molecule, flat indices (inside the padded 4ms x 4ms matrix) of its packed basis."""
+        out = []
+        for m in range(self.nmol):
+            nh, ny = int(self.nheavy[m]), int(self.nhyd[m])
+            out.append(np.concatenate([np.arange(4 * nh), 4 * nh + 4 * np.arange(ny)]))
+        return out
+
+    def _scatter_maps(self):
+        if getattr(self, "_maps", None) is None:
+            n4 = 4 * self.molsize
+            src, dst = [], []
+            for m, idx in enumerate(self.packed_index()):
+                n = idx.size
+                src.append(self.mat_off[m] + np.arange(n * n))
+                dst.append(m * n4 * n4 + (idx[:, None] * n4 + idx[None, :]).reshape(-1))
+            dev = self.device if self.dev is not None else "cpu"
+            self._maps = (torch.as_tensor(np.concatenate(src) if src else np.zeros(0, np.int64), device=dev),
+                          torch.as_tensor(np.concatenate(dst) if dst else np.zeros(0, np.int64), device=dev))
+        return self._maps
+
+    def packed_to_padded(self, flat):
+        """Concatenated per-molecule norb x norb blocks -> (nmol, 4ms, 4ms), zeros elsewhere."""
+        src, dst = self._scatter_maps()
+        n4 = 4 * self.molsize
+        out = torch.zeros(self.nmol * n4 * n4, dtype=flat.dtype, device=flat.device)
+        out[dst] = flat[src]
+        return out.view(self.nmol, n4, n4)
+
+    def padded_to_packed(self, full):
+        src, dst = self._scatter_maps()
+        out = torch.empty(int(self.mat_off[-1]), dtype=full.dtype, device=full.device)
+        out[src] = full.reshape(-1)[dst]
+        return out
+
+    def block(self, flat, m):
+        """Molecule m's dense norb x norb matrix view from a concatenated flat array."""
+        n = int(self.norb[m])
+        return flat[int(self.mat_off[m]): int(self.mat_off[m]) + n * n].view(n, n)

@@ -1,0 +1,176 @@
+"""Device-resident batched SCF driver over the native kernels.
+
+``BatchSCF`` owns every device buffer of one ragged batch and runs the
+reference's SCF semantics (seqm/seqm_functions/scf_loop.py:2034-2394):
+
+    hcore -> initial diagonal density -> F(P0), E(P0)
+    repeat for molecules still active:
+        density step (Jacobi eigensolver, or SP2)  -> Pnew
+        mixing (linear scf_forward0 / adaptive scf_forward1) -> P, Pold
+        F(P), Eelec(P) and the get_error test, which retires converged molecules
+    final eigen-decomposition of F (orbital energies and vectors)
+
+Converged molecules are retired on the device (their ``active`` flag drops)
+and every kernel skips them, so a molecule's trajectory does not depend on its
+batch mates.  The host reads one byte count per iteration to stop the loop.
+"""
+
+import time
+
+import numpy as np
+import torch
+
+from . import native
+from .layout import Layout
+
+MAX_ITER = 1000  # scf_loop.py:29
+JACOBI_MAX_N = 160
+
+
+class BatchSCF:
+    def __init__(self, layout: Layout, stream=None):
+        if layout.dev is None:
+            raise ValueError("layout must be uploaded with to_device() first")
+        self.L = layout
+        self.lib = native.load()
+        dev = layout.device
+        f64 = dict(dtype=torch.float64, device=dev)
+        T = int(layout.mat_off[-1])
+        R = int(layout.row_off[-1])
+        nm = layout.nmol
+        self.w_xx = torch.empty(max(1, 100 * layout.nxx), **f64)
+        self.w_xh = torch.empty(max(1, 10 * layout.nxh), **f64)
+        self.w_hh = torch.empty(max(1, layout.nhh), **f64)
+        self.enuc_pair = torch.empty(max(1, layout.npairs), **f64)
+        self.H = torch.empty(max(1, T), **f64)
+        self.F = torch.empty(max(1, T), **f64)
+        self.P = torch.zeros(max(1, T), **f64)
+        self.Pnew = torch.empty(max(1, T), **f64)
+        self.Pold = torch.empty(max(1, T), **f64)
+        self.work = torch.empty(max(1, T), **f64)
+        self.evals = torch.zeros(max(1, R), **f64)
+        self.old2 = torch.zeros(max(1, R), **f64)
+        self.Eelec = torch.zeros(max(1, nm), **f64)
+        self.Eout = torch.zeros(max(1, nm), **f64)
+        self.err = torch.ones(max(1, nm), **f64)
+        self.dm_err = torch.ones(max(1, nm), **f64)
+        self.dm_el = torch.ones(max(1, nm), **f64)
+        self.Enuc = torch.zeros(max(1, nm), **f64)
+        self.active = torch.ones(max(1, nm), dtype=torch.uint8, device=dev)
+        self.iters = torch.zeros(max(1, nm), dtype=torch.int32, device=dev)
+        self.status = torch.zeros(max(1, nm), dtype=torch.int32, device=dev)
+        self.sp2_work = None
+        self.stream = stream
+        self.timing = {}
+
+    # ------------------------------------------------------------------ calls
+    def _s(self):
+        s = self.stream if self.stream is not None else torch.cuda.current_stream(self.L.device)
+        return ctypes_stream(s)
+
+    def hcore(self):
+        b = self.L.struct
+        native.check(self.lib.seqm_hcore(b, native.ptr(self.w_xx), native.ptr(self.w_xh), native.ptr(self.w_hh),
+                                         native.ptr(self.H), native.ptr(self.enuc_pair), self._s()), "seqm_hcore")
+        native.check(self.lib.seqm_pair_sum(b, native.ptr(self.enuc_pair), native.ptr(self.Enuc), self._s()),
+                     "seqm_pair_sum")
+
+    def fock(self, active=None):
+        native.check(self.lib.seqm_fock(self.L.struct, native.ptr(self.P), native.ptr(self.H), native.ptr(self.w_xx),
+                                        native.ptr(self.w_xh), native.ptr(self.w_hh), native.ptr(self.F),
+                                        native.ptr(active), self._s()), "seqm_fock")
+
+    def density(self, out, sp2=(False,), active=None, evecs=None, max_sweeps=50):
+        L = self.L
+        if sp2[0] or L.max_norb > JACOBI_MAX_N:
+            if self.sp2_work is None:
+                self.sp2_work = torch.empty(2 * int(L.mat_off[-1]) + 4 * L.nmol, dtype=torch.float64,
+                                            device=L.device)
+            eps = float(sp2[1]) if sp2[0] else 1.0e-7
+            native.check(self.lib.seqm_density_sp2(L.struct, native.ptr(self.F), native.ptr(out),
+                                                   native.ptr(self.sp2_work), eps, native.ptr(active),
+                                                   native.ptr(self.status), 1000, self._s()), "seqm_density_sp2")
+            return
+        native.check(self.lib.seqm_density_jacobi(L.struct, native.ptr(self.F), native.ptr(out),
+                                                  native.ptr(self.evals), native.ptr(evecs), native.ptr(self.work),
+                                                  native.ptr(L.dev["row_off"]), native.ptr(active),
+                                                  native.ptr(self.status), max_sweeps, self._s()),
+                     "seqm_density_jacobi")
+
+    def energy_error(self, eps, first=False):
+        b = self.L.struct
+        if first:
+            native.check(self.lib.seqm_energy_error(b, native.ptr(self.P), None, native.ptr(self.H),
+                                                    native.ptr(self.F), native.ptr(self.Eelec), native.ptr(self.Eout),
+                                                    native.ptr(self.err), native.ptr(self.dm_err),
+                                                    native.ptr(self.dm_el), None, float(eps), self._s()),
+                         "seqm_energy_error")
+            return
+        native.check(self.lib.seqm_energy_error(b, native.ptr(self.P), native.ptr(self.Pold), native.ptr(self.H),
+                                                native.ptr(self.F), native.ptr(self.Eelec), native.ptr(self.Eout),
+                                                native.ptr(self.err), native.ptr(self.dm_err), native.ptr(self.dm_el),
+                                                native.ptr(self.active), float(eps), self._s()), "seqm_energy_error")
+
+    # --------------------------------------------------------------- drivers
+    def scf(self, eps, converger=(1,), sp2=(False,), P0=None, max_iter=MAX_ITER):
+        """Run the SCF; returns the per-molecule not-converged mask (host numpy)."""
+        L = self.L
+        b = L.struct
+        if P0 is None:
+            self.P.zero_()
+            native.check(self.lib.seqm_initial_density(b, native.ptr(self.P), self._s()), "seqm_initial_density")
+        else:
+            self.P.copy_(P0)
+        self.fock()
+        self.energy_error(eps, first=True)
+        self.Eelec.copy_(self.Eout)
+        self.err.fill_(1.0)
+        self.dm_err.fill_(1.0)
+        self.dm_el.fill_(1.0)
+        self.active.fill_(1)
+        self.iters.zero_()
+        self.old2.zero_()
+        linear = int(converger[0]) == 0
+        if int(converger[0]) not in (0, 1):
+            raise NotImplementedError("scf_converger must be [0, alpha] (linear) or [1] (adaptive)")
+        alpha = float(converger[1]) if linear else 0.0
+        n_loop = max_iter + 1 if linear else max_iter
+        for _ in range(n_loop):
+            self.density(self.Pnew, sp2, active=self.active)
+            native.check(self.lib.seqm_mix(b, native.ptr(self.P), native.ptr(self.Pnew), native.ptr(self.Pold),
+                                           native.ptr(self.old2), native.ptr(L.dev["row_off"]),
+                                           native.ptr(self.iters), int(linear), alpha, native.ptr(self.active),
+                                           self._s()), "seqm_mix")
+            self.fock(self.active)
+            self.energy_error(eps)
+            if int(self.active.sum()) == 0:
+                break
+        return self.active[: L.nmol].bool().cpu().numpy()
+
+    def final(self, want_vectors=True):
+        """Fock matrix of the converged density, orbital energies / vectors, energies."""
+        self.fock()
+        evecs = torch.empty_like(self.work) if want_vectors else None
+        self.density(self.Pnew, (False,), active=None, evecs=evecs)
+        self.energy_error(0.0, first=True)
+        self.evecs = evecs
+        return self.Eout[: self.L.nmol].clone(), self.Enuc[: self.L.nmol].clone()
+
+
+def ctypes_stream(s):
+    import ctypes
+
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def run_energy(species, coords, method, eps=1e-6, converger=(1,), sp2=(False,), charges=None, device="cuda",
+               want_vectors=False):
+    """One batched single point: returns a dict of device tensors and host arrays."""
+    t0 = time.perf_counter()
+    L = Layout.from_padded(species, coords, method, charges).to_device(device)
+    s = BatchSCF(L)
+    s.hcore()
+    nc = s.scf(eps, converger, sp2)
+    Eelec, Enuc = s.final(want_vectors)
+    return dict(layout=L, solver=s, Eelec=Eelec, Enuc=Enuc, Etot=Eelec + Enuc, notconverged=nc,
+                iters=s.iters[: L.nmol].cpu().numpy(), wall=time.perf_counter() - t0)

@@ -1,0 +1,135 @@
+"""CUDA path vs golden reference outputs and the CPU oracle (needs a GB300)."""
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import GOLDEN_NAMES, load_golden
+from oracle import seqm_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+EIG_CASES = [n for n in GOLDEN_NAMES if "sp2" not in n]
+
+
+def _run(g, **kw):
+    from pyseqm_gb300.scf import run_energy
+
+    s = g["settings"]
+    return run_energy(g["species_np"], g["coords_np"], s["method"], eps=s["scf_eps"],
+                      converger=tuple(s["scf_converger"]), sp2=tuple(s.get("sp2", [False])), device="cuda", **kw)
+
+
+def test_library_loaded():
+    from pyseqm_gb300 import native
+
+    lib = native.load()
+    assert b"sm_103a" in lib.seqm_version()
+
+
+@pytest.mark.parametrize("name", [n for n in GOLDEN_NAMES if "stages" in load_golden(n)])
+def test_hcore_and_integrals_match_reference(name):
+    """Stage parity: w (10x10 per pair) and Hcore blocks against the reference's hcore()."""
+    from pyseqm_gb300.layout import Layout
+    from pyseqm_gb300.scf import BatchSCF
+
+    g = load_golden(name)
+    st = g["stages"]
+    L = Layout.from_padded(g["species_np"], g["coords_np"], g["settings"]["method"]).to_device("cuda")
+    s = BatchSCF(L)
+    s.hcore()
+    torch.cuda.synchronize()
+    # reference pair order: (mol, i<j) row-major over all atoms; map to our class segments
+    ref_w = np.asarray(st["w"])
+    idxi, idxj = np.asarray(st["idxi"]), np.asarray(st["idxj"])
+    ours = {}
+    wxx = s.w_xx.cpu().numpy()
+    wxh = s.w_xh.cpu().numpy()
+    whh = s.w_hh.cpu().numpy()
+    for p in range(L.npairs):
+        blk = np.zeros((10, 10))
+        if p < L.nxx:
+            blk[:] = wxx[100 * p: 100 * p + 100].reshape(10, 10)
+        elif p < L.nxx + L.nxh:
+            blk[:, 0] = wxh[10 * (p - L.nxx): 10 * (p - L.nxx) + 10]
+        else:
+            blk[0, 0] = whh[p - L.nxx - L.nxh]
+        ours[(int(L.pair_i[p]), int(L.pair_j[p]))] = blk
+    for k in range(idxi.size):
+        np.testing.assert_allclose(ours[(int(idxi[k]), int(idxj[k]))], ref_w[k], atol=1e-11, rtol=1e-12)
+    # Hcore: compare the full padded matrices built from the reference blocks
+    ref = O.parse(g["species_np"], g["coords_np"])
+    M = np.zeros((ref["nmol"] * ref["molsize"] ** 2, 4, 4))
+    M[ref["maskd"]] = np.asarray(st["M_diag"])
+    M[ref["mask"]] = np.asarray(st["M_pair"])
+    Href = O.symmetrize_upper(O.blocks_to_full(M, ref["nmol"], ref["molsize"]))
+    Hours = L.packed_to_padded(s.H).cpu().numpy()
+    np.testing.assert_allclose(Hours, Href, atol=1e-11, rtol=1e-12)
+
+
+@pytest.mark.parametrize("name", EIG_CASES)
+def test_scf_matches_reference(name):
+    g = load_golden(name)
+    ref = g["ref"]
+    out = _run(g, want_vectors=True)
+    L = out["layout"]
+    # |dE| <= 1e-6 eV, density max-abs <= 1e-7, iterations +-1 (per molecule where known)
+    np.testing.assert_allclose(out["Etot"].cpu().numpy(), ref["Etot"], atol=1e-6, rtol=0)
+    np.testing.assert_allclose(out["Eelec"].cpu().numpy(), ref["Eelec"], atol=1e-6, rtol=0)
+    np.testing.assert_allclose(out["Enuc"].cpu().numpy(), ref["Enuc"], atol=1e-6, rtol=0)
+    P = out["solver"].P
+    for m in range(L.nmol):
+        np.testing.assert_allclose(L.block(P, m).cpu().numpy(), np.asarray(ref["P"][m]), atol=1e-7, rtol=0)
+    assert not out["notconverged"].any()
+    if "loop_count_per_molecule" in ref:
+        assert np.all(np.abs(out["iters"] - np.asarray(ref["loop_count_per_molecule"])) <= 1)
+    assert abs(int(out["iters"].max()) - ref["loop_count"]) <= 1
+    ev = out["solver"].evals.cpu().numpy()
+    for m in range(L.nmol):
+        n = int(L.norb[m])
+        np.testing.assert_allclose(ev[L.row_off[m]: L.row_off[m] + n], np.asarray(ref["e"][m])[:n], atol=1e-8)
+
+
+def test_sp2_path_matches_reference_sp2():
+    g = load_golden("mixed_am1_sp2")
+    ref = g["ref"]
+    out = _run(g)
+    np.testing.assert_allclose(out["Etot"].cpu().numpy(), ref["Etot"], atol=1e-6, rtol=0)
+    L = out["layout"]
+    for m in range(L.nmol):
+        np.testing.assert_allclose(L.block(out["solver"].P, m).cpu().numpy(), np.asarray(ref["P"][m]), atol=1e-7)
+    assert abs(int(out["iters"].max()) - ref["loop_count"]) <= 1
+
+
+@pytest.mark.parametrize("seed", [11, 12])
+def test_mixed_batch_matches_oracle(seed):
+    """Seeded mixed alkanes / water clusters (AM1, adaptive mixing) vs the oracle, molecule by molecule."""
+    from pyseqm_gb300 import workloads
+
+    mols = workloads.mixed_batch(24, seed=seed, alkane_range=(1, 12), water_range=(2, 14))
+    species, coords = workloads.pad_batch(mols)
+    out = _run({"species_np": species, "coords_np": coords,
+                "settings": {"method": "AM1", "scf_eps": 1e-8, "scf_converger": [1]}})
+    ref = O.single_point("AM1", species, coords, 1e-8, (1,))
+    np.testing.assert_allclose(out["Etot"].cpu().numpy(), ref["Etot"], atol=1e-6, rtol=0)
+    assert np.all(np.abs(out["iters"] - ref["iters"]) <= 1)
+    L = out["layout"]
+    for m in range(L.nmol):
+        idx = O.packed_index(ref["mol"]["nheavy"][m], ref["mol"]["nhyd"][m])
+        np.testing.assert_allclose(L.block(out["solver"].P, m).cpu().numpy(), ref["P"][m][np.ix_(idx, idx)],
+                                   atol=1e-7)
+
+
+def test_batch_independence():
+    """A molecule's result is the same alone and inside a batch."""
+    from pyseqm_gb300 import workloads
+
+    mols = workloads.mixed_batch(10, seed=5, alkane_range=(1, 8), water_range=(2, 8))
+    species, coords = workloads.pad_batch(mols)
+    s = {"method": "PM3", "scf_eps": 1e-8, "scf_converger": [1]}
+    full = _run({"species_np": species, "coords_np": coords, "settings": s})
+    for m in (0, 3, 7):
+        n = int((species[m] > 0).sum())
+        one = _run({"species_np": species[m:m + 1, :n], "coords_np": coords[m:m + 1, :n], "settings": s})
+        assert abs(float(one["Etot"][0]) - float(full["Etot"][m])) < 1e-9
+        assert int(one["iters"][0]) == int(full["iters"][m])

@@ -61,7 +61,11 @@ class BatchSCF:
         self.status = torch.zeros(max(1, nm), dtype=torch.int32, device=dev)
         self.sp2_work = None
         self.stream = stream
-        self.timing = {}
+        self.launches = 0  # kernels of this library launched (for reporting)
+        self.profile_density = False  # record CUDA events around every density launch
+        self.density_events = []
+        flops = 9.0 * layout.norb.astype(np.float64) ** 3 + 2.0 * layout.norb.astype(np.float64) ** 2 * layout.nocc
+        self.density_flops = torch.as_tensor(flops, dtype=torch.float64, device=dev)
 
     # ------------------------------------------------------------------ calls
     def _s(self):
@@ -69,6 +73,7 @@ class BatchSCF:
         return ctypes_stream(s)
 
     def hcore(self):
+        self.launches += 4
         b = self.L.struct
         native.check(self.lib.seqm_hcore(b, native.ptr(self.w_xx), native.ptr(self.w_xh), native.ptr(self.w_hh),
                                          native.ptr(self.H), native.ptr(self.enuc_pair), self._s()), "seqm_hcore")
@@ -76,12 +81,27 @@ class BatchSCF:
                      "seqm_pair_sum")
 
     def fock(self, active=None):
+        self.launches += 1
         native.check(self.lib.seqm_fock(self.L.struct, native.ptr(self.P), native.ptr(self.H), native.ptr(self.w_xx),
                                         native.ptr(self.w_xh), native.ptr(self.w_hh), native.ptr(self.F),
                                         native.ptr(active), self._s()), "seqm_fock")
 
     def density(self, out, sp2=(False,), active=None, evecs=None, max_sweeps=50):
+        if self.profile_density:
+            stream = self.stream if self.stream is not None else torch.cuda.current_stream(self.L.device)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            self._density(out, sp2, active, evecs, max_sweeps)
+            e1.record(stream)
+            fl = self.density_flops if active is None else self.density_flops * active[: self.L.nmol].double()
+            self.density_events.append((e0, e1, fl.sum()))
+            return
+        self._density(out, sp2, active, evecs, max_sweeps)
+
+    def _density(self, out, sp2=(False,), active=None, evecs=None, max_sweeps=50):
         L = self.L
+        self.launches += 1
         if sp2[0] or L.max_norb > JACOBI_MAX_N:
             if self.sp2_work is None:
                 self.sp2_work = torch.empty(2 * int(L.mat_off[-1]) + 4 * L.nmol, dtype=torch.float64,
@@ -98,6 +118,7 @@ class BatchSCF:
                      "seqm_density_jacobi")
 
     def energy_error(self, eps, first=False):
+        self.launches += 1
         b = self.L.struct
         if first:
             native.check(self.lib.seqm_energy_error(b, native.ptr(self.P), None, native.ptr(self.H),
@@ -118,6 +139,7 @@ class BatchSCF:
         b = L.struct
         if P0 is None:
             self.P.zero_()
+            self.launches += 1
             native.check(self.lib.seqm_initial_density(b, native.ptr(self.P), self._s()), "seqm_initial_density")
         else:
             self.P.copy_(P0)
@@ -137,6 +159,7 @@ class BatchSCF:
         n_loop = max_iter + 1 if linear else max_iter
         for _ in range(n_loop):
             self.density(self.Pnew, sp2, active=self.active)
+            self.launches += 1
             native.check(self.lib.seqm_mix(b, native.ptr(self.P), native.ptr(self.Pnew), native.ptr(self.Pold),
                                            native.ptr(self.old2), native.ptr(L.dev["row_off"]),
                                            native.ptr(self.iters), int(linear), alpha, native.ptr(self.active),

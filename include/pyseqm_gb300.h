@@ -94,6 +94,21 @@ int seqm_density_jacobi(const seqm_batch *b, const double *F, double *P, double 
                         double *work, const int64_t *mol_row_off, const uint8_t *active, int32_t *status,
                         int max_sweeps, void *stream);
 
+/* Allocation-free seqm_density_jacobi.  No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory (a host that owns a fixed device-memory pool,
+ * or one that must not stall the GPU with cudaMalloc/cudaFree mid-pipeline).  Same inputs
+ * and outputs as seqm_density_jacobi, minus `work`: the eigenvector scratch is a fixed
+ * 16 MiB device array inside the library (held by every GPU that loads it, until exit).
+ * Limit: sum of norb^2 over the batch <= SEQM_NOALLOC_JACOBI_DOUBLES, else SEQM_E_TOO_LARGE
+ * and no launch.  Reads mat_off[nmol] back first, so it synchronises `stream` once.
+ * The first call on a device resolves the array's device address (cudaGetSymbolAddress)
+ * with that device current; make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race. */
+#define SEQM_NOALLOC_JACOBI_DOUBLES (1 << 21)
+int seqm_density_jacobi_noalloc(const seqm_batch *b, const double *F, double *P, double *evals, double *evecs,
+                                const int64_t *mol_row_off, const uint8_t *active, int32_t *status, int max_sweeps,
+                                void *stream);
+
 /* SP2 purification (FP64), replaces SP2(a, nocc, eps) (seqm/seqm_functions/SP2.py:9-85)
  * applied per molecule to its packed Fock matrix (eps clamped to [1e-7, 1e-3] as there).
  * work: scratch of 2*mat_off[nmol] + 4*nmol doubles.  P = 2 X at convergence.

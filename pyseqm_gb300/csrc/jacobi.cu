@@ -228,3 +228,76 @@ extern "C" int seqm_density_jacobi(const seqm_batch *bp, const double *F, double
                                                          max_sweeps);
   return launch_check();
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of seqm_density_jacobi.
+//
+// Some callers cannot call cudaMalloc: a host program that carves the GPU's memory
+// into a fixed pool up front (an MD engine or a long-running serving process that
+// owns every byte it hands out), or one that must not stall the device in the middle
+// of its pipeline (cudaMalloc/cudaFree synchronise).  For them the eigenvector
+// scratch of the Jacobi kernel lives in the fixed device array below instead of a
+// caller-provided `work` buffer.  The array is part of this library's image: every
+// GPU that loads the library holds these 16 MiB until the process exits.
+//
+// Limit: the batch's dense matrices must fit, i.e. sum over molecules of norb^2
+// <= SEQM_NOALLOC_JACOBI_DOUBLES (2^21 doubles = 16 MiB); larger batches get
+// SEQM_E_TOO_LARGE and nothing is launched.
+//
+// The array is shared by every call and keeps the previous call's contents.  The
+// kernel writes every scratch entry it later reads (each molecule's block starts
+// from the identity), so no clearing is needed; but two calls that overlap on the
+// GPU (different streams, or different host threads) use the same memory and race.
+constexpr size_t NOALLOC_DOUBLES = size_t(1) << 21;
+static_assert(NOALLOC_DOUBLES == SEQM_NOALLOC_JACOBI_DOUBLES, "header and library disagree on the scratch size");
+static __device__ __align__(256) double g_jacobi_scratch[NOALLOC_DOUBLES];
+
+#include <mutex>
+
+namespace {
+std::mutex g_scratch_mu;
+double *g_scratch_addr[256] = {};  // device address of g_jacobi_scratch, per device ordinal
+
+// Host code may not use g_jacobi_scratch's name as an address: it is a host-side
+// stand-in.  Resolve the real device address once per device, with that device
+// current, and cache it.
+int jacobi_scratch_address(double **out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return SEQM_E_CUDA;
+  if (dev < 0 || dev >= 256) return SEQM_E_ARG;
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_addr[dev]) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_jacobi_scratch) != cudaSuccess || p == nullptr) return SEQM_E_CUDA;
+    g_scratch_addr[dev] = static_cast<double *>(p);
+  }
+  *out = g_scratch_addr[dev];
+  return SEQM_OK;
+}
+}  // namespace
+
+extern "C" int seqm_density_jacobi_noalloc(const seqm_batch *bp, const double *F, double *P, double *evals,
+                                           double *evecs, const int64_t *mol_row_off, const uint8_t *active,
+                                           int32_t *status, int max_sweeps, void *stream) {
+  if (!bp) return SEQM_E_ARG;
+  seqm_batch b = *bp;
+  if (b.nmol == 0) return SEQM_OK;
+  if (b.max_norb > JMAX_N) return SEQM_E_TOO_LARGE;
+  cudaStream_t s = (cudaStream_t)stream;
+  // total dense-matrix size = mat_off[nmol] (device); one small read, then the size check
+  int64_t total = 0;
+  if (cudaMemcpyAsync(&total, b.mol_mat_off + b.nmol, sizeof(int64_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return SEQM_E_CUDA;
+  if (total < 0 || (size_t)total > NOALLOC_DOUBLES) return SEQM_E_TOO_LARGE;
+  double *work = nullptr;
+  int rc = jacobi_scratch_address(&work);
+  if (rc != SEQM_OK) return rc;
+  int lda = b.max_norb | 1;
+  size_t smem = (size_t)b.max_norb * lda * sizeof(double);
+  if (smem < 8) smem = 8;
+  if (cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return SEQM_E_CUDA;
+  k_jacobi<<<b.nmol, NT_J, smem, s>>>(b, F, P, evals, evecs, work, mol_row_off, active, status, max_sweeps);
+  return launch_check();
+}

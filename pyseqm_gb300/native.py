@@ -26,7 +26,8 @@ PAR_NAMES = ["U_ss", "U_pp", "zeta_s", "zeta_p", "beta_s", "beta_p", "g_ss", "g_
 NPAR = len(PAR_NAMES)
 PAR = {n: i for i, n in enumerate(PAR_NAMES)}
 
-EXPORTS = ["seqm_hcore", "seqm_fock", "seqm_density_jacobi", "seqm_density_sp2", "seqm_mix", "seqm_energy_error",
+EXPORTS = ["seqm_hcore", "seqm_fock", "seqm_density_jacobi", "seqm_density_jacobi_noalloc", "seqm_density_sp2",
+           "seqm_mix", "seqm_energy_error",
            "seqm_initial_density", "seqm_pair_sum", "seqm_version"]
 
 _P = ctypes.c_void_p
@@ -68,6 +69,7 @@ def load(path=None):
         "seqm_hcore": [B, _P, _P, _P, _P, _P, _P],
         "seqm_fock": [B, _P, _P, _P, _P, _P, _P, _P, _P],
         "seqm_density_jacobi": [B, _P, _P, _P, _P, _P, _P, _P, _P, i32, _P],
+        "seqm_density_jacobi_noalloc": [B, _P, _P, _P, _P, _P, _P, _P, i32, _P],
         "seqm_density_sp2": [B, _P, _P, _P, f64, _P, _P, i32, _P],
         "seqm_mix": [B, _P, _P, _P, _P, _P, _P, i32, f64, _P, _P],
         "seqm_energy_error": [B, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, f64, _P],

@@ -89,10 +89,13 @@ int seqm_fock(const seqm_batch *b, const double *P, const double *H, const doubl
  * eigenvalues (mol_row_off = prefix sum of norb), evecs (NULL: skip) the eigenvectors as
  * ROWS of the molecule's norb x norb block (row k <-> evals k), P the density (NULL: skip).
  * work: scratch of mat_off[nmol] doubles (unsorted eigenvector rows).
+ * warm (NULL: cold start for all): molecules with warm[m] != 0 start from the orthonormal
+ * rows already in `work` (the previous call's eigenvectors) and rotate A = V F V^T, which
+ * converges in fewer sweeps when F changed little (successive SCF iterations); needs P.
  * status[m]: number of sweeps, or -1 if the sweep cap was hit. */
 int seqm_density_jacobi(const seqm_batch *b, const double *F, double *P, double *evals, double *evecs,
                         double *work, const int64_t *mol_row_off, const uint8_t *active, int32_t *status,
-                        int max_sweeps, void *stream);
+                        int max_sweeps, const uint8_t *warm, void *stream);
 
 /* Allocation-free seqm_density_jacobi.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory (a host that owns a fixed device-memory pool,

@@ -29,7 +29,7 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
                                                  double *__restrict__ evals, double *__restrict__ evecs,
                                                  double *__restrict__ work, const int64_t *__restrict__ row_off,
                                                  const uint8_t *__restrict__ active, int32_t *__restrict__ status,
-                                                 int max_sweeps) {
+                                                 int max_sweeps, const uint8_t *__restrict__ warm) {
   extern __shared__ double A[];
   __shared__ double rc[JMAX_P], rs[JMAX_P], rt[JMAX_P];
   __shared__ int rp[JMAX_P], rq[JMAX_P], rflag[JMAX_P];
@@ -48,12 +48,14 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
   double *V = work + mo;  // row k = eigenvector k (column k of C)
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
 
+  // warm start: V already holds orthonormal rows (the previous SCF step's eigenvectors)
+  const bool is_warm = warm != nullptr && warm[m] != 0 && P != nullptr;
   double f2 = 0.0;
   for (int idx = tid; idx < n * n; idx += NT_J) {
     int i = idx / n, j = idx - i * n;
     double v = Fm[idx];
     A[i * lda + j] = v;
-    V[idx] = i == j ? 1.0 : 0.0;
+    if (!is_warm) V[idx] = i == j ? 1.0 : 0.0;
     f2 += v * v;
   }
 #pragma unroll
@@ -67,6 +69,63 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
   }
   __syncthreads();
   const double tol = 1.0e-13 * sqrt(red[0]);
+
+  if (is_warm) {
+    // A <- V F V^T in two FP64 products, 4x4 register tiles per thread:
+    //   G = V F   (F in shared memory, V rows from L2) -> the P block as temporary
+    //   A = G V^T (upper-triangle tiles, mirrored)      -> shared memory
+    double *G = P + mo;
+    const int nt = (n + 3) >> 2;
+    for (int t = tid; t < nt * nt; t += NT_J) {
+      const int k0 = (t / nt) * 4, j0 = (t % nt) * 4;
+      double acc[4][4] = {};
+      for (int i = 0; i < n; ++i) {
+        double v[4], f[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) v[r] = (k0 + r < n) ? V[(size_t)(k0 + r) * n + i] : 0.0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) f[c] = (j0 + c < n) ? A[i * lda + j0 + c] : 0.0;
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) acc[r][c] += v[r] * f[c];
+      }
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+          if (k0 + r < n && j0 + c < n) G[(size_t)(k0 + r) * n + j0 + c] = acc[r][c];
+    }
+    __syncthreads();
+    for (int t = tid; t < nt * nt; t += NT_J) {
+      const int kb = t / nt, lb = t % nt;
+      if (kb > lb) continue;
+      const int k0 = kb * 4, l0 = lb * 4;
+      double acc[4][4] = {};
+      for (int j = 0; j < n; ++j) {
+        double g[4], v[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) g[r] = (k0 + r < n) ? G[(size_t)(k0 + r) * n + j] : 0.0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) v[c] = (l0 + c < n) ? V[(size_t)(l0 + c) * n + j] : 0.0;
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) acc[r][c] += g[r] * v[c];
+      }
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const int k = k0 + r, l = l0 + c;
+          if (k < n && l < n && k <= l) {
+            A[k * lda + l] = acc[r][c];
+            A[l * lda + k] = acc[r][c];
+          }
+        }
+    }
+    __syncthreads();
+  }
 
   const int npad = n + (n & 1), np = npad / 2, nsteps = npad - 1;
   int sweeps = -1;
@@ -214,8 +273,9 @@ using namespace seqm;
 
 extern "C" int seqm_density_jacobi(const seqm_batch *bp, const double *F, double *P, double *evals, double *evecs,
                                    double *work, const int64_t *mol_row_off, const uint8_t *active, int32_t *status,
-                                   int max_sweeps, void *stream) {
+                                   int max_sweeps, const uint8_t *warm, void *stream) {
   if (!bp || !work) return SEQM_E_ARG;
+  if (warm && !P) return SEQM_E_ARG;  // a warm start uses P's block as temporary storage
   seqm_batch b = *bp;
   if (b.nmol == 0) return SEQM_OK;
   if (b.max_norb > JMAX_N) return SEQM_E_TOO_LARGE;
@@ -225,7 +285,7 @@ extern "C" int seqm_density_jacobi(const seqm_batch *bp, const double *F, double
   if (cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return SEQM_E_CUDA;
   k_jacobi<<<b.nmol, NT_J, smem, (cudaStream_t)stream>>>(b, F, P, evals, evecs, work, mol_row_off, active, status,
-                                                         max_sweeps);
+                                                         max_sweeps, warm);
   return launch_check();
 }
 
@@ -298,6 +358,7 @@ extern "C" int seqm_density_jacobi_noalloc(const seqm_batch *bp, const double *F
   if (smem < 8) smem = 8;
   if (cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return SEQM_E_CUDA;
-  k_jacobi<<<b.nmol, NT_J, smem, s>>>(b, F, P, evals, evecs, work, mol_row_off, active, status, max_sweeps);
+  k_jacobi<<<b.nmol, NT_J, smem, s>>>(b, F, P, evals, evecs, work, mol_row_off, active, status, max_sweeps,
+                                      nullptr);
   return launch_check();
 }

@@ -59,6 +59,8 @@ class BatchSCF:
         self.active = torch.ones(max(1, nm), dtype=torch.uint8, device=dev)
         self.iters = torch.zeros(max(1, nm), dtype=torch.int32, device=dev)
         self.status = torch.zeros(max(1, nm), dtype=torch.int32, device=dev)
+        # 1 once the molecule's eigenvector rows in `work` are valid (warm-started Jacobi)
+        self.warm = torch.zeros(max(1, nm), dtype=torch.uint8, device=dev)
         self.sp2_work = None
         self.stream = stream
         self.launches = 0  # kernels of this library launched (for reporting)
@@ -114,8 +116,12 @@ class BatchSCF:
         native.check(self.lib.seqm_density_jacobi(L.struct, native.ptr(self.F), native.ptr(out),
                                                   native.ptr(self.evals), native.ptr(evecs), native.ptr(self.work),
                                                   native.ptr(L.dev["row_off"]), native.ptr(active),
-                                                  native.ptr(self.status), max_sweeps, self._s()),
+                                                  native.ptr(self.status), max_sweeps, native.ptr(self.warm), self._s()),
                      "seqm_density_jacobi")
+        if active is None:
+            self.warm.fill_(1)
+        else:
+            self.warm.bitwise_or_(active)
 
     def energy_error(self, eps, first=False):
         self.launches += 1
@@ -151,6 +157,7 @@ class BatchSCF:
         self.dm_el.fill_(1.0)
         self.active.fill_(1)
         self.iters.zero_()
+        self.warm.zero_()
         self.old2.zero_()
         linear = int(converger[0]) == 0
         if int(converger[0]) not in (0, 1):

@@ -143,6 +143,15 @@ int seqm_initial_density(const seqm_batch *b, double *P, void *stream);
 /* Per-molecule sums of per-pair core-core energies: Enuc[m] (energy.py:177-192). */
 int seqm_pair_sum(const seqm_batch *b, const double *pair_val, double *mol_sum, void *stream);
 
+/* Gradient of sum_m gE[m]*Eelec[m] + gN[m]*Enuc[m] at fixed densities P, i.e. what the
+ * reference's autograd gives with the SCF as a constant (SCF0, scf_loop.py:1996-2031;
+ * Force.forward, basics.py:1260-1365): dR[natoms*3] = dE/dR (eV/Angstrom; force = -dR) and
+ * dpar[4*natoms] = dE/d(U_ss, U_pp, beta_s, beta_p) per atom (NULL: skip).  Integrals,
+ * overlaps and core-core terms are recomputed with forward-mode derivatives, not stored.
+ * work: scratch of 7*npairs doubles. */
+int seqm_energy_grad(const seqm_batch *b, const double *P, const double *gE, const double *gN, double *dR,
+                     double *dpar, double *work, void *stream);
+
 /* Library build string (host memory; no GPU needed). */
 const char *seqm_version(void);
 

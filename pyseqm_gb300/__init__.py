@@ -5,3 +5,16 @@ The compute path is hand-written sm_103a CUDA in ``csrc/`` behind the C ABI of
 """
 
 __version__ = "0.1.0"
+
+from .api import single_point  # noqa: E402,F401
+from .basics import (  # noqa: E402,F401
+    Constants,
+    Electronic_Structure,
+    Energy,
+    Force,
+    Hamiltonian,
+    Molecule,
+    Pack_Parameters,
+    Parser,
+    SCFEnergyFunction,
+)

@@ -1,0 +1,551 @@
+"""Drop-in replacements for PYSEQM's seqm API on the SCF path.
+
+Mirrors seqm.Molecule.Molecule (Molecule.py:11-186), seqm.basics.Parser
+(basics.py:199-403), Pack_Parameters (:406-448), Hamiltonian (:451-533),
+Energy (:536-1244), Force (:1247-1365), seqm.ElectronicStructure.Electronic_Structure
+(ElectronicStructure.py:10-127) and seqm.seqm_functions.constants.Constants
+(constants.py:26-224): same constructors, same seqm_parameters keys, same return
+tuples, results in the same padded layout.  The computation runs in the CUDA
+library; autograd reaches the coordinates and the per-atom U_ss, U_pp, beta_s,
+beta_p through ``SCFEnergyFunction``, whose backward is the adjoint kernel
+(seqm_energy_grad) evaluated at the converged density, which is what the
+reference's SCF0 boundary implies (scf_loop.py:1996-2031).
+
+Supported: closed-shell MNDO/AM1/PM3, scf_converger [0, alpha] and [1], sp2,
+learned parameters (values for any parameter; gradients for U_ss, U_pp, beta_s,
+beta_p).  UHF, PM6, excited states, scf_backward >= 1 and a finite
+pair_outer_cutoff raise NotImplementedError.
+"""
+
+import copy
+import time
+
+import numpy as np
+import torch
+
+from . import native, tables
+from .layout import Layout
+from .scf import BatchSCF
+
+TO_DEBYE = 1.60217733e-19 * 1e-10 * 2.99792458e8 / 1e-21  # seqm/seqm_functions/constants.py:13-15
+DEBYE_TO_AU = 0.393456
+GRAD_PARAMS = ("U_ss", "U_pp", "beta_s", "beta_p")
+
+
+def _f64(x, device):
+    return torch.as_tensor(np.asarray(x), dtype=torch.float64, device=device)
+
+
+# ------------------------------------------------------------------ constants
+class Constants(torch.nn.Module):
+    """Element tables (constants.py:26-224) as non-trainable parameters, float64."""
+
+    def __init__(self, do_timing=False, length_conversion_factor=(1.0 / tables.A0), energy_conversion_factor=1.0):
+        super().__init__()
+        el = tables.elements()
+        self.length_conversion_factor = length_conversion_factor
+        self.energy_conversion_factor = energy_conversion_factor
+        for name in ("tore", "qn", "ussc", "uppc", "gssc", "gspc", "hspc", "gp2c", "gppc", "mass"):
+            setattr(self, name, torch.nn.Parameter(torch.as_tensor(el[name], dtype=torch.float64),
+                                                   requires_grad=False))
+        self.qn_int = torch.nn.Parameter(self.qn.data.to(torch.int64), requires_grad=False)
+        self.eheat = torch.nn.Parameter(torch.as_tensor(el["eheat_ev"], dtype=torch.float64), requires_grad=False)
+        self.do_timing = do_timing
+        if do_timing:
+            self.timing = {"Hcore + STO Integrals": [], "SCF": [], "Force": [], "MD": [], "D*": [], "CIS/RPA": []}
+
+    def forward(self):
+        pass
+
+
+# --------------------------------------------------------------------- parser
+def _check_options(seqm_parameters):
+    if seqm_parameters.get("method") not in tables.METHOD_FIELDS:
+        raise NotImplementedError(f"method {seqm_parameters.get('method')!r}: supported are MNDO, AM1, PM3")
+    if seqm_parameters.get("UHF", False):
+        raise NotImplementedError("UHF is not supported by pyseqm_gb300 (closed-shell RHF only)")
+    if seqm_parameters.get("excited_states"):
+        raise NotImplementedError("excited states are not supported by pyseqm_gb300")
+    if seqm_parameters.get("scf_backward", 0) != 0:
+        raise NotImplementedError("scf_backward >= 1 (backpropagation through the SCF) is not supported")
+    if seqm_parameters.get("pair_outer_cutoff", 1e10) < 1e10:
+        raise NotImplementedError("a finite pair_outer_cutoff is not supported (all pairs are kept)")
+    conv = seqm_parameters.get("scf_converger", [1])
+    if conv[0] not in (0, 1):
+        raise NotImplementedError("scf_converger must be [0, alpha] or [1]")
+
+
+class Parser(torch.nn.Module):
+    """Pair list and counts in the reference's order and dtypes (basics.py:199-403)."""
+
+    def __init__(self, seqm_parameters):
+        super().__init__()
+        self.outercutoff = seqm_parameters.get("pair_outer_cutoff", 1e10)
+        if seqm_parameters.get("elements") is None:
+            raise RuntimeError("Please instantiate a Molecule object before instantiating an object of "
+                               "Electronic_structure or Molecular_Dynamics class.Alternately, provide a list called "
+                               "of unique elements in the input molecules under the 'elements' key in seqm_parameters")
+        self.elements = seqm_parameters["elements"]
+
+    def forward(self, molecule, themethod, return_mask_l=False, do_large_tensors=True, *args, **kwargs):
+        species = molecule.species
+        dev = molecule.coordinates.device
+        sp = species.detach().cpu().numpy()
+        nmol, molsize = sp.shape
+        el = tables.elements()
+        real = sp > 0
+        real_atoms = np.nonzero(real.reshape(-1))[0]
+        Z = sp.reshape(-1)[real_atoms]
+        nheavy = (sp > 1).sum(1)
+        nhyd = (sp == 1).sum(1)
+        nsh = np.zeros(nmol, dtype=np.int64)
+        nel = el["tore"][sp].sum(1).astype(np.int64)
+        if torch.is_tensor(molecule.tot_charge):
+            nel = nel - molecule.tot_charge.detach().cpu().numpy().reshape(-1).astype(np.int64)
+        if np.any(nel % 2 == 1):
+            raise ValueError("RHF setting requires closed shell systems (even number of electrons)")
+        nocc = nel // 2
+        maskd = ((np.arange(molsize) * (molsize + 1))[None, :] + (np.arange(nmol) * molsize**2)[:, None]).reshape(-1)
+        maskd = maskd[real_atoms]
+        atom_molid = np.repeat(np.arange(nmol), molsize)[real_atoms]
+        inv = np.zeros(nmol * molsize, dtype=np.int64)
+        inv[real_atoms] = np.arange(real_atoms.size)
+        ii, jj = np.triu_indices(molsize, 1)
+        m_all = np.repeat(np.arange(nmol), ii.size)
+        i_all, j_all = np.tile(ii, nmol), np.tile(jj, nmol)
+        keep = real[m_all, i_all] & real[m_all, j_all]
+        mp, ip, jp = m_all[keep], i_all[keep], j_all[keep]
+        t = lambda a: torch.as_tensor(a, dtype=torch.int64, device=dev)  # noqa: E731
+        idxi, idxj = inv[mp * molsize + ip], inv[mp * molsize + jp]
+        coords = molecule.coordinates.detach()
+        d = coords[t(mp), t(jp)] - coords[t(mp), t(ip)]
+        dist = torch.linalg.norm(d, dim=1)
+        out = [nmol, molsize, t(nsh), t(nheavy), t(nhyd), t(nocc), t(Z), t(maskd), t(atom_molid),
+               t(mp * molsize**2 + ip * molsize + jp)]
+        if return_mask_l:
+            out.append(t(mp * molsize**2 + jp * molsize + ip))
+        out += [t(mp), t(Z[idxi]), t(Z[idxj]), t(idxi), t(idxj), d / dist.unsqueeze(1),
+                dist * molecule.const.length_conversion_factor]
+        return tuple(out)
+
+
+class Pack_Parameters(torch.nn.Module):
+    """Per-atom parameters from the method's table plus learned ones (basics.py:406-448)."""
+
+    def __init__(self, seqm_parameters):
+        super().__init__()
+        self.elements = seqm_parameters["elements"]
+        self.learned_list = seqm_parameters.get("learned", [])
+        self.method = seqm_parameters["method"]
+        self.parameters = list(tables.METHOD_FIELDS[self.method])
+        self.required_list = [p for p in self.parameters if p not in self.learned_list]
+        fields, rows = tables.method_table(self.method)
+        self.p = torch.nn.Parameter(torch.as_tensor(rows[:, [fields.index(f) for f in self.required_list]]),
+                                    requires_grad=False)
+        m = max(self.elements)
+        self.alpha = torch.nn.Parameter(torch.zeros(m + 1, m + 1, dtype=torch.float64), requires_grad=False)
+        self.chi = torch.nn.Parameter(torch.zeros(m + 1, m + 1, dtype=torch.float64), requires_grad=False)
+
+    def forward(self, Z, learned_params=dict()):
+        learned_params = dict(learned_params)
+        for i, name in enumerate(self.required_list):
+            learned_params[name] = self.p[Z, i]
+        return learned_params, self.alpha, self.chi
+
+
+# ------------------------------------------------------------------ molecule
+class Molecule(torch.nn.Module):
+    """Batch of molecules (Molecule.py:11-186): same constructor and attributes."""
+
+    def __init__(self, const, seqm_parameters, coordinates, species, charges=0, mult=1, learned_parameters=dict(),
+                 do_large_tensors=True, *args, **kwargs):
+        super().__init__()
+        self.const = const
+        _check_species(species)
+        self.species = species
+        self.coordinates = torch.nn.Parameter(coordinates)
+        self.coordinates.requires_grad_(do_large_tensors)
+        if not torch.is_tensor(charges):
+            charges = charges * torch.ones(coordinates.shape[0], device=coordinates.device)
+        self.tot_charge = charges
+        if not torch.is_tensor(mult):
+            mult = mult * torch.ones(coordinates.shape[0], device=coordinates.device)
+        self.mult = mult
+        if seqm_parameters.get("elements") is None:
+            seqm_parameters["elements"] = [0] + sorted(set(species.reshape(-1).tolist()))
+        self.seqm_parameters = seqm_parameters
+        self.method = seqm_parameters["method"]
+        _check_options(seqm_parameters)
+        self.parser = Parser(seqm_parameters)
+        self.packpar = Pack_Parameters(seqm_parameters).to(coordinates.device)
+        (self.nmol, self.molsize, self.nSuperHeavy, self.nHeavy, self.nHydro, self.nocc, self.Z, self.maskd,
+         self.atom_molid, self.mask, self.mask_l, self.pair_molid, self.ni, self.nj, self.idxi, self.idxj, self.xij,
+         self.rij) = self.parser(self, self.method, return_mask_l=True)
+        if callable(learned_parameters):
+            learned_parameters = learned_parameters(self.species, self.coordinates)
+        self.parameters, self.alp, self.chi = copy.deepcopy(self.packpar(self.Z, learned_params=learned_parameters))
+        _complete_parameters(self.parameters)
+        self.norb = self.nHydro + 4 * self.nHeavy
+        non_zero = self.species != 0
+        self.num_atoms = torch.sum(non_zero, dim=1).to(coordinates.dtype)
+        self.mass = self.const.mass[self.species].unsqueeze(2)
+        self.mass_inverse = torch.zeros_like(self.mass)
+        self.mass_inverse[non_zero] = 1.0 / self.mass[non_zero]
+        for name in ("force", "velocities", "acc", "dm", "q", "w", "Hf", "Etot", "Eelec", "Enuc", "Eiso", "e_mo",
+                     "e_gap", "molecular_orbitals", "charge", "dipole", "analytical_gradient"):
+            setattr(self, name, None)
+        self.verbose = True
+        self.active_state = seqm_parameters.get("active_state", 0)
+
+
+def _check_species(species):
+    ok = species[:, :-1] >= species[:, 1:]
+    row_ok = ok.all(dim=1)
+    if not row_ok.all():
+        bad = (~row_ok).nonzero(as_tuple=False).squeeze(1).tolist()
+        word, verb = ("row", "is") if len(bad) == 1 else ("rows", "are")
+        raise ValueError(f"species must be non-increasing along each row, but {word} "
+                         f"{', '.join(map(str, bad))} {verb} not sorted.")
+
+
+def _complete_parameters(params):
+    if "beta_s" in params and "beta_p" in params:
+        params["beta"] = torch.cat((params["beta_s"].unsqueeze(1), params["beta_p"].unsqueeze(1)), dim=1)
+    z = torch.zeros_like(params["zeta_s"])
+    for k in ("zeta_d", "s_orb_exp_tail", "p_orb_exp_tail", "d_orb_exp_tail", "U_dd", "F0SD", "G2SD", "rho_core"):
+        params[k] = z
+    params["Kbeta"] = params.get("Kbeta", None)
+
+
+# -------------------------------------------------------------- the SCF core
+class _Solve:
+    """One batched SCF solve on the GPU for a Molecule (layout, solver, options)."""
+
+    def __init__(self, molecule, seqm_parameters, P0=None):
+        _check_options(seqm_parameters)
+        self.dev = molecule.coordinates.device if molecule.coordinates.is_cuda else torch.device("cuda")
+        sp = molecule.species.detach().cpu().numpy()
+        xyz = molecule.coordinates.detach().cpu().numpy()
+        learned = {k: v.detach().cpu().numpy() for k, v in molecule.parameters.items()
+                   if k in native.PAR and torch.is_tensor(v)}
+        charges = molecule.tot_charge.detach().cpu().numpy() if torch.is_tensor(molecule.tot_charge) else None
+        self.L = Layout.from_padded(sp, xyz, molecule.method, charges, learned).to_device(self.dev)
+        self.s = BatchSCF(self.L)
+        self.opts = seqm_parameters
+        self.P0 = P0
+        self.timing = {}
+
+    def run(self, const=None):
+        o = self.opts
+        t0 = time.time()
+        self.s.hcore()
+        if const is not None and const.do_timing:
+            torch.cuda.synchronize()
+            const.timing["Hcore + STO Integrals"].append(time.time() - t0)
+        t0 = time.time()
+        P0 = None
+        if self.P0 is not None:
+            P0 = self.L.padded_to_packed(self.P0.detach().to(self.dev, torch.float64))
+        eps = float(o["scf_eps"]) if not torch.is_tensor(o["scf_eps"]) else float(o["scf_eps"].item())
+        self.notconverged = self.s.scf(eps, tuple(o.get("scf_converger", [1])), tuple(o.get("sp2", [False])), P0)
+        self.Eelec, self.Enuc = self.s.final(want_vectors=o.get("eig", True))
+        if const is not None and const.do_timing:
+            torch.cuda.synchronize()
+            const.timing["SCF"].append(time.time() - t0)
+        return self
+
+    def grad(self, gE, gN):
+        L = self.L
+        dR = torch.empty(3 * max(1, L.natoms), dtype=torch.float64, device=self.dev)
+        dpar = torch.empty(4 * max(1, L.natoms), dtype=torch.float64, device=self.dev)
+        work = torch.empty(7 * max(1, L.npairs), dtype=torch.float64, device=self.dev)
+        lib = native.load()
+        self.s.launches += 2
+        native.check(lib.seqm_energy_grad(L.struct, native.ptr(self.s.P), native.ptr(gE.contiguous()),
+                                          native.ptr(gN.contiguous()), native.ptr(dR), native.ptr(dpar),
+                                          native.ptr(work), self.s._s()), "seqm_energy_grad")
+        return dR[: 3 * L.natoms].view(L.natoms, 3), dpar[: 4 * L.natoms].view(4, L.natoms)
+
+    # ------------------------------------------------------- padded outputs
+    def padded(self, flat):
+        return self.L.packed_to_padded(flat)
+
+    def eigen_padded(self):
+        """e (nmol, 4*molsize) zero-padded and v (nmol, nmax, nmax) with eigenvectors as columns."""
+        L = self.L
+        n4 = 4 * L.molsize
+        nmax = int(L.norb.max())
+        e = torch.zeros(L.nmol, n4, dtype=torch.float64, device=self.dev)
+        v = torch.zeros(L.nmol, nmax, nmax, dtype=torch.float64, device=self.dev)
+        for m in range(L.nmol):
+            n = int(L.norb[m])
+            e[m, :n] = self.s.evals[int(L.row_off[m]): int(L.row_off[m]) + n]
+            v[m, :n, :n] = L.block(self.s.evecs, m).t()
+            if n < nmax:
+                v[m, n:, n:] = torch.eye(nmax - n, dtype=torch.float64, device=self.dev)
+        return e, v
+
+    def w_reference_order(self):
+        L = self.L
+        ref = L.reference_pair_index()
+        w = torch.zeros(L.npairs, 10, 10, dtype=torch.float64, device=self.dev)
+        pos = torch.as_tensor(ref, device=self.dev)
+        if L.nxx:
+            w[pos[: L.nxx]] = self.s.w_xx[: 100 * L.nxx].view(-1, 10, 10)
+        if L.nxh:
+            w[pos[L.nxx: L.nxx + L.nxh], :, 0] = self.s.w_xh[: 10 * L.nxh].view(-1, 10)
+        if L.nhh:
+            w[pos[L.nxx + L.nxh:], 0, 0] = self.s.w_hh[: L.nhh]
+        return w
+
+    def pair_values_reference_order(self, v):
+        pos = torch.as_tensor(self.L.reference_pair_index(), device=self.dev)
+        out = torch.empty(self.L.npairs, dtype=v.dtype, device=self.dev)
+        out[pos] = v[: self.L.npairs]
+        return out
+
+
+class SCFEnergyFunction(torch.autograd.Function):
+    """(coordinates of real atoms, U_ss, U_pp, beta_s, beta_p) -> (Eelec, Enuc) per molecule.
+
+    forward runs the SCF; backward is the adjoint kernel at the converged density
+    (no backpropagation through the SCF iterations, as with the reference's SCF0)."""
+
+    @staticmethod
+    def forward(ctx, xyz, uss, upp, bs, bp, solve):
+        ctx.solve = solve
+        return solve.Eelec.clone(), solve.Enuc.clone()
+
+    @staticmethod
+    def backward(ctx, gE, gN):
+        solve = ctx.solve
+        nm = solve.L.nmol
+        gE = torch.zeros(nm, dtype=torch.float64, device=solve.dev) if gE is None else gE.to(solve.dev, torch.float64)
+        gN = torch.zeros(nm, dtype=torch.float64, device=solve.dev) if gN is None else gN.to(solve.dev, torch.float64)
+        dR, dpar = solve.grad(gE, gN)
+        return dR, dpar[0], dpar[1], dpar[2], dpar[3], None
+
+
+def _isolated_atom_energy(const, Z, p):
+    """energy.py:8-23 (differentiable in the parameters)."""
+    return (p["U_ss"] * const.ussc[Z] + p["U_pp"] * const.uppc[Z] + p["g_ss"] * const.gssc[Z]
+            + p["g_pp"] * const.gppc[Z] + p["g_sp"] * const.gspc[Z] + p["g_p2"] * const.gp2c[Z]
+            + p["h_sp"] * const.hspc[Z])
+
+
+def _dipole(molecule, solve):
+    """Ground-state dipole from the diagonal density blocks (dipole.py:85-107), on the device."""
+    L = solve.L
+    dev = solve.dev
+    P = solve.s.P
+    xyz = torch.as_tensor(L.xyz, device=dev)
+    Z = L.Z
+    el = tables.elements()
+    par = L.dev["par"].view(native.NPAR, -1)
+    dd = par[native.PAR["_dd"]] * tables.A0
+    elec = torch.zeros(L.nmol, 3, dtype=torch.float64, device=dev)
+    atom_off = L.atom_off
+    for m in range(L.nmol):
+        blk = L.block(P, m)
+        nh = int(L.nheavy[m])
+        a0, a1 = int(atom_off[m]), int(atom_off[m + 1])
+        d = torch.diagonal(blk)
+        idx = np.arange(a0, a1)
+        heavy = idx[: nh]
+        hyd = idx[nh:]
+        if nh:
+            occ = d[: 4 * nh].view(nh, 4).sum(1)
+            sp = torch.stack([blk[4 * k, 4 * k + 1: 4 * k + 4] for k in range(nh)])
+            elec[m] += -(occ[:, None] * xyz[heavy]).sum(0) - 2.0 * (dd[heavy][:, None] * sp).sum(0)
+        if hyd.size:
+            elec[m] += -(d[4 * nh:][:, None] * xyz[hyd]).sum(0)
+    nuc = (molecule.const.tore[molecule.species].unsqueeze(-1) * molecule.coordinates.detach()).sum(dim=1)
+    return ((elec.to(nuc.device) + nuc) * TO_DEBYE * DEBYE_TO_AU)
+
+
+def _orbital_charges(molecule, solve, v):
+    """Per-orbital atomic charges as the reference forms them (scf_loop.py:2333-2388)."""
+    L = solve.L
+    nmol, molsize = L.nmol, L.molsize
+    charge = torch.zeros(nmol, molsize * 4, molsize, device=v.device, dtype=v.dtype)
+    v2 = v**2
+    for i in range(nmol):
+        n, nh, ny = int(L.norb[i]), int(L.nheavy[i]), int(L.nhyd[i])
+        if nh:
+            charge[i, :n, :nh] = v2[i][:n, : 4 * nh].reshape(n, 4, nh).sum(dim=1)
+        charge[i, :n, nh: nh + ny] = v2[i][:n, 4 * nh: 4 * nh + ny]
+    return charge
+
+
+# ---------------------------------------------------------------- modules
+class Hamiltonian(torch.nn.Module):
+    """SCF driver module (basics.py:451-533); returns the reference's 12-tuple."""
+
+    def __init__(self, seqm_parameters):
+        super().__init__()
+        self.eps = torch.nn.Parameter(torch.as_tensor(seqm_parameters["scf_eps"]), requires_grad=False)
+        self.sp2 = seqm_parameters.get("sp2", [False])
+        self.scf_converger = seqm_parameters["scf_converger"]
+        self.eig = seqm_parameters.get("eig", True)
+        self.seqm_parameters = seqm_parameters
+
+    def solve(self, molecule, P0=None):
+        return _Solve(molecule, self.seqm_parameters, P0).run(molecule.const)
+
+    def forward(self, molecule, themethod, P0=None):
+        s = self.solve(molecule, P0)
+        return _hamiltonian_outputs(molecule, s, self.eig)
+
+
+def _hamiltonian_outputs(molecule, s, eig=True):
+    F = s.padded(s.s.F)
+    P = s.padded(s.s.P)
+    H = s.padded(s.s.H)
+    w = s.w_reference_order()
+    nc = torch.as_tensor(s.notconverged, device=F.device)
+    if eig:
+        e, v = s.eigen_padded()
+        charge = _orbital_charges(molecule, s, v)
+    else:
+        e = v = charge = None
+    par = s.L.dev["par"].view(native.NPAR, -1)
+    ref_i, ref_j = s.L.reference_pair_atoms()
+    rho0 = par[native.PAR["_rho0"]]
+    rho0xi = rho0[torch.as_tensor(ref_i, device=F.device)]
+    rho0xj = rho0[torch.as_tensor(ref_j, device=F.device)]
+    return F, e, P, H, w, charge, rho0xi, rho0xj, None, None, nc, v
+
+
+class Energy(torch.nn.Module):
+    """Energy terms (basics.py:536-1244, ground state)."""
+
+    def __init__(self, seqm_parameters):
+        super().__init__()
+        self.seqm_parameters = seqm_parameters
+        self.method = seqm_parameters["method"]
+        self.parser = Parser(seqm_parameters) if seqm_parameters.get("elements") is not None else None
+        self.packpar = Pack_Parameters(seqm_parameters) if seqm_parameters.get("elements") is not None else None
+        self.hamiltonian = Hamiltonian(seqm_parameters)
+        self.Hf_flag = seqm_parameters.get("Hf_flag", True)
+        self.eig = seqm_parameters.get("eig", True)
+        _check_options(seqm_parameters)
+
+    def _prepare(self, molecule, learned_parameters):
+        if self.parser is None:
+            self.parser = Parser(self.seqm_parameters)
+            self.packpar = Pack_Parameters(self.seqm_parameters).to(molecule.coordinates.device)
+        (molecule.nmol, molecule.molsize, molecule.nSuperHeavy, molecule.nHeavy, molecule.nHydro, molecule.nocc,
+         molecule.Z, molecule.maskd, molecule.atom_molid, molecule.mask, molecule.pair_molid, molecule.ni,
+         molecule.nj, molecule.idxi, molecule.idxj, molecule.xij, molecule.rij) = self.parser(molecule, self.method)
+        if callable(learned_parameters):
+            learned_parameters = learned_parameters(molecule.species, molecule.coordinates)
+        self.packpar = self.packpar.to(molecule.coordinates.device)
+        molecule.parameters, molecule.alp, molecule.chi = copy.deepcopy(
+            self.packpar(molecule.Z, learned_params=learned_parameters))
+        _complete_parameters(molecule.parameters)
+        for k, v in molecule.parameters.items():
+            if torch.is_tensor(v) and v.requires_grad and k not in GRAD_PARAMS and k not in ("beta",):
+                raise NotImplementedError(f"gradients with respect to {k} are not supported "
+                                          f"(supported: {', '.join(GRAD_PARAMS)})")
+
+    def forward(self, molecule, learned_parameters=dict(), all_terms=False, P0=None, cis_amp=None, *args, **kwargs):
+        self._prepare(molecule, learned_parameters)
+        s = self.hamiltonian.solve(molecule, P0)
+        dev = molecule.coordinates.device
+        L = s.L
+        real = torch.as_tensor(L.real_index, device=dev)
+        xyz = molecule.coordinates.reshape(-1, 3)[real]
+        p = molecule.parameters
+        Eelec, Enuc = SCFEnergyFunction.apply(xyz, p["U_ss"], p["U_pp"], p["beta_s"], p["beta_p"], s)
+        Eelec, Enuc = Eelec.to(dev), Enuc.to(dev)
+        F, e, P, H, w, charge, rho0xi, rho0xj, _, _, nc, v = _hamiltonian_outputs(molecule, s, self.eig)
+        molecule.w = w.to(dev)
+        if self.eig:
+            lumo = molecule.nocc.unsqueeze(0).T.to(e.device)
+            e_gap = (e.gather(1, lumo) - e.gather(1, lumo - 1)).reshape(-1).to(dev)
+            molecule.molecular_orbitals = v.to(dev)
+            e = e.to(dev)
+        else:
+            e_gap = None
+        EnucAB = s.pair_values_reference_order(s.s.enuc_pair).to(dev)
+        molecule._gam = w[..., 0, 0].to(dev)
+        with torch.no_grad():
+            molecule.dipole = _dipole(molecule, s).to(dev)
+        P = P.to(dev)
+        nc = nc.to(dev)
+        charge = charge.to(dev) if charge is not None else None
+        molecule._solve = s
+        if all_terms:
+            Etot = Eelec + Enuc
+            Eiso = _isolated_atom_energy(molecule.const, molecule.Z, p)
+            Eiso_sum = torch.zeros_like(Etot).index_add(0, molecule.atom_molid, Eiso)
+            if self.Hf_flag:
+                eheat = torch.zeros_like(Etot).index_add(0, molecule.atom_molid, molecule.const.eheat[molecule.Z])
+                Hf = Etot - Eiso_sum + eheat
+            else:
+                Hf = Etot - Eiso_sum
+            return Hf, Etot, Eelec, Enuc, Eiso_sum, EnucAB, e_gap, e, P, charge, nc
+        return Eelec, EnucAB, P, nc
+
+
+class Force(torch.nn.Module):
+    """Forces -dHf/dR (basics.py:1247-1365)."""
+
+    def __init__(self, seqm_parameters):
+        super().__init__()
+        self.energy = Energy(seqm_parameters)
+        self.create_graph = seqm_parameters.get("2nd_grad", False)
+        self.eig = seqm_parameters.get("eig", True)
+        self.seqm_parameters = seqm_parameters
+        if self.create_graph:
+            raise NotImplementedError("second derivatives (2nd_grad) are not supported")
+
+    def forward(self, molecule, learned_parameters=dict(), P0=None, cis_amp=None, do_force=True, *args, **kwargs):
+        molecule.coordinates.requires_grad_(do_force)
+        Hf, Etot, Eelec, Enuc, Eiso, _, e_gap, e, D, charge, nc = self.energy(
+            molecule, learned_parameters=learned_parameters, all_terms=True, P0=P0)
+        if self.eig and e is not None:
+            e, e_gap = e.detach(), e_gap.detach()
+        if do_force:
+            t0 = time.time()
+            Hf.sum().backward()
+            force = -molecule.coordinates.grad.detach()
+            molecule.coordinates.grad.zero_()
+            if molecule.const.do_timing:
+                torch.cuda.synchronize()
+                molecule.const.timing["Force"].append(time.time() - t0)
+            if self.seqm_parameters.get("analytical_gradient", [False])[0]:
+                molecule.analytical_gradient = -force
+        else:
+            force = torch.tensor([])
+        return (force.detach(), D.detach(), Hf.detach(), Etot.detach(), Eelec.detach(), Enuc.detach(), Eiso.detach(),
+                e, e_gap, charge, nc)
+
+
+class Electronic_Structure(torch.nn.Module):
+    """Single-point driver (ElectronicStructure.py:10-127): sets force, dm, energies, charges."""
+
+    def __init__(self, seqm_parameters, *args, **kwargs):
+        super().__init__()
+        self.seqm_parameters = seqm_parameters
+        self.conservative_force = Force(seqm_parameters)
+
+    @staticmethod
+    def atomic_charges(P, n_orbital=4):
+        n_molecule = P.shape[0]
+        n_atom = P.shape[1] // n_orbital
+        return P.diagonal(dim1=1, dim2=2).reshape(n_molecule, n_atom, n_orbital).sum(axis=2)
+
+    def forward(self, molecule, learned_parameters=dict(), xl_bomd_params=dict(), P0=None, err_threshold=None,
+                max_rank=None, T_el=None, dm_prop="SCF", *args, **kwargs):
+        if dm_prop != "SCF":
+            raise NotImplementedError("only dm_prop='SCF' is supported")
+        (molecule.force, P, molecule.Hf, molecule.Etot, molecule.Eelec, molecule.Enuc, molecule.Eiso, molecule.e_mo,
+         molecule.e_gap, self.charge, self.notconverged) = self.conservative_force(
+            molecule, P0=P0, learned_parameters=learned_parameters)
+        molecule.dm = P.detach()
+        with torch.no_grad():
+            molecule.q = molecule.const.tore[molecule.species] - self.atomic_charges(molecule.dm)
+
+    def get_force(self):
+        return self.force

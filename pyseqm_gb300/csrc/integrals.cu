@@ -12,6 +12,7 @@
 #include <math.h>
 
 #include "common.cuh"
+#include "pair_math.cuh"
 
 namespace seqm {
 
@@ -34,7 +35,7 @@ __global__ void k_atom_prep(seqm_batch b) {
     qq = sqrt((4.0 * qn * qn + 6.0 * qn + 2.0) / 20.0) / zp;
     // rho1: hsp(d) = d/2 - 1/(2 sqrt(4 D1^2 + 1/d^2)), atomic units
     double hsp = par(b, SEQM_P_HSP, a) / EV;
-    double d1 = cbrt(fabs(hsp) / (dd * dd));
+    double d1 = pow(fabs(hsp) / (dd * dd), 1.0 / 3.0);
     if (hsp < 0.0) d1 = -d1;
     double d2 = d1 + 0.04;
     for (int it = 0; it < 5; ++it) {
@@ -66,292 +67,6 @@ __global__ void k_atom_prep(seqm_batch b) {
   P[SEQM_P_RHO2 * n + a] = rho2;
 }
 
-// --------------------------------------------------------- local integrals
-__device__ __forceinline__ double inv_sqrt_ev(double c, double x) { return c / sqrt(x); }
-
-// heavy-heavy: 22 integrals in the local frame (repp, MOPAC numbering 1..22 -> ri[0..21])
-__device__ void local_xx(double r, double da, double db, double qa0, double qb0, double r0a, double r0b, double r1a,
-                         double r1b, double r2a, double r2b, double *ri) {
-  const double ev1 = EV / 2.0, ev2 = EV / 4.0, ev3 = EV / 8.0, ev4 = EV / 16.0;
-  const double qa = qa0 * 2.0, qb = qb0 * 2.0, qa1 = qa0, qb1 = qb0;
-  const double aee = (r0a + r0b) * (r0a + r0b), ade = (r1a + r0b) * (r1a + r0b), aqe = (r2a + r0b) * (r2a + r0b);
-  const double aed = (r0a + r1b) * (r0a + r1b), aeq = (r0a + r2b) * (r0a + r2b), axx = (r1a + r1b) * (r1a + r1b);
-  const double adq = (r1a + r2b) * (r1a + r2b), aqd = (r2a + r1b) * (r2a + r1b), aqq = (r2a + r2b) * (r2a + r2b);
-  const double r2 = r * r;
-#define SQ(x) ((x) * (x))
-  double ee = EV / sqrt(r2 + aee);
-  double dze = -ev1 / sqrt(SQ(r + da) + ade) + ev1 / sqrt(SQ(r - da) + ade);
-  double e6 = ev1 / sqrt(r2 + aqe);
-  double qzze = ev2 / sqrt(SQ(r - qa) + aqe) + ev2 / sqrt(SQ(r + qa) + aqe) - e6;
-  double qxxe = ev1 / sqrt(r2 + qa * qa + aqe) - e6;
-  double edz = -ev1 / sqrt(SQ(r - db) + aed) + ev1 / sqrt(SQ(r + db) + aed);
-  double e12 = ev1 / sqrt(r2 + aeq);
-  double eqzz = ev2 / sqrt(SQ(r - qb) + aeq) + ev2 / sqrt(SQ(r + qb) + aeq) - e12;
-  double eqxx = ev1 / sqrt(r2 + qb * qb + aeq) - e12;
-  double e20 = ev2 / sqrt(SQ(r + da) + adq), e22 = ev2 / sqrt(SQ(r - da) + adq);
-  double e24 = ev2 / sqrt(SQ(r - db) + aqd), e26 = ev2 / sqrt(SQ(r + db) + aqd);
-  double e36 = ev2 / sqrt(r2 + aqq), e39 = ev2 / sqrt(r2 + qa * qa + aqq), e40 = ev2 / sqrt(r2 + qb * qb + aqq);
-  double e42 = ev3 / sqrt(SQ(r - qb) + aqq), e44 = ev3 / sqrt(SQ(r + qb) + aqq);
-  double e46 = ev3 / sqrt(SQ(r + qa) + aqq), e48 = ev3 / sqrt(SQ(r - qa) + aqq);
-  ri[0] = ee;
-  ri[1] = -dze;
-  ri[2] = ee + qzze;
-  ri[3] = ee + qxxe;
-  ri[4] = -edz;
-  ri[5] = ev2 / sqrt(SQ(r + da - db) + axx) + ev2 / sqrt(SQ(r - da + db) + axx) - ev2 / sqrt(SQ(r - da - db) + axx) -
-          ev2 / sqrt(SQ(r + da + db) + axx);
-  ri[6] = ev1 / sqrt(r2 + SQ(da - db) + axx) - ev1 / sqrt(r2 + SQ(da + db) + axx);
-  ri[7] = -edz + ev3 / sqrt(SQ(r + qa - db) + aqd) - ev3 / sqrt(SQ(r + qa + db) + aqd) +
-          ev3 / sqrt(SQ(r - qa - db) + aqd) - ev3 / sqrt(SQ(r - qa + db) + aqd) - e24 + e26;
-  ri[8] = -edz - e24 + ev2 / sqrt(SQ(r - db) + qa * qa + aqd) + e26 - ev2 / sqrt(SQ(r + db) + qa * qa + aqd);
-  ri[9] = ev2 / sqrt(SQ(qa1 - db) + SQ(r + qa1) + aqd) - ev2 / sqrt(SQ(qa1 - db) + SQ(r - qa1) + aqd) -
-          ev2 / sqrt(SQ(qa1 + db) + SQ(r + qa1) + aqd) + ev2 / sqrt(SQ(qa1 + db) + SQ(r - qa1) + aqd);
-  ri[10] = ee + eqzz;
-  ri[11] = ee + eqxx;
-  ri[12] = -dze + ev3 / sqrt(SQ(r + da - qb) + adq) - ev3 / sqrt(SQ(r - da - qb) + adq) +
-           ev3 / sqrt(SQ(r + da + qb) + adq) - ev3 / sqrt(SQ(r - da + qb) + adq) + e22 - e20;
-  ri[13] = -dze - e20 + ev2 / sqrt(SQ(r + da) + qb * qb + adq) + e22 - ev2 / sqrt(SQ(r - da) + qb * qb + adq);
-  ri[14] = ev2 / sqrt(SQ(da - qb1) + SQ(r - qb1) + adq) - ev2 / sqrt(SQ(da - qb1) + SQ(r + qb1) + adq) -
-           ev2 / sqrt(SQ(da + qb1) + SQ(r - qb1) + adq) + ev2 / sqrt(SQ(da + qb1) + SQ(r + qb1) + adq);
-  ri[15] = ee + eqzz + qzze + ev4 / sqrt(SQ(r + qa - qb) + aqq) + ev4 / sqrt(SQ(r + qa + qb) + aqq) +
-           ev4 / sqrt(SQ(r - qa - qb) + aqq) + ev4 / sqrt(SQ(r - qa + qb) + aqq) - e48 - e46 - e42 - e44 + e36;
-  ri[16] = ee + eqzz + qxxe + ev3 / sqrt(SQ(r - qb) + qa * qa + aqq) + ev3 / sqrt(SQ(r + qb) + qa * qa + aqq) - e42 -
-           e44 - e39 + e36;
-  ri[17] = ee + eqxx + qzze + ev3 / sqrt(SQ(r + qa) + qb * qb + aqq) + ev3 / sqrt(SQ(r - qa) + qb * qb + aqq) - e46 -
-           e48 - e40 + e36;
-  double qxxqxx = ev3 / sqrt(r2 + SQ(qa - qb) + aqq) + ev3 / sqrt(r2 + SQ(qa + qb) + aqq) - e39 - e40 + e36;
-  ri[18] = ee + eqxx + qxxe + qxxqxx;
-  ri[19] = ev3 / sqrt(SQ(r + qa1 - qb1) + SQ(qa1 - qb1) + aqq) - ev3 / sqrt(SQ(r + qa1 + qb1) + SQ(qa1 - qb1) + aqq) -
-           ev3 / sqrt(SQ(r - qa1 - qb1) + SQ(qa1 - qb1) + aqq) + ev3 / sqrt(SQ(r - qa1 + qb1) + SQ(qa1 - qb1) + aqq) -
-           ev3 / sqrt(SQ(r + qa1 - qb1) + SQ(qa1 + qb1) + aqq) + ev3 / sqrt(SQ(r + qa1 + qb1) + SQ(qa1 + qb1) + aqq) +
-           ev3 / sqrt(SQ(r - qa1 - qb1) + SQ(qa1 + qb1) + aqq) - ev3 / sqrt(SQ(r - qa1 + qb1) + SQ(qa1 + qb1) + aqq);
-  double qxxqyy = ev2 / sqrt(r2 + qa * qa + qb * qb + aqq) - e39 - e40 + e36;
-  ri[20] = ee + eqxx + qxxe + qxxqyy;
-  ri[21] = 0.5 * (qxxqxx - qxxqyy);
-}
-
-// heavy-hydrogen: 4 integrals (sigma-type only)
-__device__ void local_xh(double r, double da, double qa0, double r0a, double r0b, double r1a, double r2a, double *ri) {
-  const double ev1 = EV / 2.0, ev2 = EV / 4.0;
-  const double aee = (r0a + r0b) * (r0a + r0b), ade = (r1a + r0b) * (r1a + r0b), aqe = (r2a + r0b) * (r2a + r0b);
-  const double qa = qa0 * 2.0;
-  double e6 = ev1 / sqrt(r * r + aqe);
-  double ee = EV / sqrt(r * r + aee);
-  ri[0] = ee;
-  ri[1] = ev1 / sqrt(SQ(r + da) + ade) - ev1 / sqrt(SQ(r - da) + ade);
-  ri[2] = ee + ev2 / sqrt(SQ(r + qa) + aqe) + ev2 / sqrt(SQ(r - qa) + aqe) - e6;
-  ri[3] = ee + ev1 / sqrt(r * r + qa * qa + aqe) - e6;
-}
-
-// ---------------------------------------------------------------- rotation
-// rotation matrix taking unit vector v onto +x via the quaternion (0, v_z, -v_y, 1+v_x);
-// |1+v_x| < 1e-7 uses a half turn about z (two_elec_two_center_int.py:1576-1631)
-__device__ void quat_rot(double vx, double vy, double vz, double R[3][3]) {
-  double qx = 0.0, qy = vz, qz = -vy, qw = 1.0 + vx;
-  if (fabs(qw) < 1.0e-7) { qx = 0.0; qy = 0.0; qz = 1.0; qw = 0.0; }
-  double nrm = sqrt(qx * qx + qy * qy + qz * qz + qw * qw);
-  qy /= nrm; qz /= nrm; qw /= nrm;
-  R[0][0] = 1 - 2 * (qy * qy + qz * qz);
-  R[0][1] = -2 * (qz * qw);
-  R[0][2] = 2 * (qy * qw);
-  R[1][0] = 2 * (qz * qw);
-  R[1][1] = 1 - 2 * (qz * qz);
-  R[1][2] = 2 * (qy * qz);
-  R[2][0] = -2 * (qy * qw);
-  R[2][1] = 2 * (qy * qz);
-  R[2][2] = 1 - 2 * (qy * qy);
-}
-
-// heavy-heavy rotated block, w[a*10+b]; a = (kk,ll) of atom i, b = (mm,nn) of atom j
-__device__ void rotate_xx(const double *ri, const double R[3][3], double *__restrict__ w) {
-  const double *r0 = R[0], *r1 = R[1], *r2 = R[2];
-  int a = 0;
-#pragma unroll
-  for (int kk = 0; kk < 4; ++kk) {
-#pragma unroll
-    for (int ll = 0; ll <= kk; ++ll, ++a) {
-      int b = 0;
-#pragma unroll
-      for (int mm = 0; mm < 4; ++mm) {
-#pragma unroll
-        for (int nn = 0; nn <= mm; ++nn, ++b) {
-          const int k = kk - 1, l = ll - 1, m = mm - 1, n = nn - 1;
-          double val;
-          if (kk == 0) {
-            if (mm == 0) val = ri[0];
-            else if (nn == 0) val = ri[4] * r0[m];
-            else val = ri[10] * (r0[m] * r0[n]) + ri[11] * (r1[m] * r1[n] + r2[m] * r2[n]);
-          } else if (ll == 0) {
-            if (mm == 0) val = ri[1] * r0[k];
-            else if (nn == 0) val = ri[5] * (r0[k] * r0[m]) + ri[6] * (r1[k] * r1[m] + r2[k] * r2[m]);
-            else {
-              double t0 = r0[k] * r0[m] * r0[n];
-              double t1 = (r1[m] * r1[n] + r2[m] * r2[n]) * r0[k];
-              double mix = r1[k] * (r1[n] * r0[m] + r1[m] * r0[n]) + r2[k] * (r2[m] * r0[n] + r2[n] * r0[m]);
-              val = ri[12] * t0 + ri[13] * t1 + ri[14] * mix;
-            }
-          } else {
-            if (mm == 0) val = ri[2] * (r0[k] * r0[l]) + ri[3] * (r1[k] * r1[l] + r2[k] * r2[l]);
-            else if (nn == 0) {
-              double t0 = r0[k] * r0[l] * r0[m];
-              double t1 = (r1[k] * r1[l] + r2[k] * r2[l]) * r0[m];
-              double t2 = r1[l] * r1[m] + r2[l] * r2[m];
-              val = ri[7] * t0 + ri[8] * t1 + ri[9] * (r0[k] * t2 + r0[l] * (r1[k] * r1[m] + r2[k] * r2[m]));
-            } else {
-              val = ri[15] * (r0[k] * r0[l] * r0[m] * r0[n]);
-              val += ri[16] * ((r1[k] * r1[l] + r2[k] * r2[l]) * r0[m] * r0[n]);
-              val += ri[17] * ((r1[m] * r1[n] + r2[m] * r2[n]) * (r0[k] * r0[l]));
-              val += ri[18] * (r1[k] * r1[l] * r1[m] * r1[n] + r2[k] * r2[l] * r2[m] * r2[n]);
-              double mix1 = r0[m] * (r1[l] * r1[n] + r2[l] * r2[n]);
-              double mix2 = r0[n] * (r1[l] * r1[m] + r2[l] * r2[m]);
-              double val5 = r0[k] * (mix1 + mix2) +
-                            r0[l] * (r0[m] * (r1[k] * r1[n] + r2[k] * r2[n]) + r0[n] * (r1[k] * r1[m] + r2[k] * r2[m]));
-              val += ri[19] * val5;
-              val += ri[20] * (r1[k] * r1[l] * r2[m] * r2[n] + r2[k] * r2[l] * r1[m] * r1[n]);
-              val += ri[21] * ((r1[k] * r2[l] + r2[k] * r1[l]) * (r1[m] * r2[n] + r2[m] * r1[n]));
-            }
-          }
-          w[a * 10 + b] = val;
-        }
-      }
-    }
-  }
-}
-
-__device__ void rotate_xh(const double *ri, const double R[3][3], double *__restrict__ w) {
-  int a = 0;
-#pragma unroll
-  for (int kk = 0; kk < 4; ++kk) {
-#pragma unroll
-    for (int ll = 0; ll <= kk; ++ll, ++a) {
-      const int k = kk - 1, l = ll - 1;
-      double val;
-      if (kk == 0) val = ri[0];
-      else if (ll == 0) val = ri[1] * R[0][k];
-      else val = ri[2] * R[0][k] * R[0][l] + ri[3] * (R[1][k] * R[1][l] + R[2][k] * R[2][l]);
-      w[a] = val;
-    }
-  }
-}
-
-// ----------------------------------------------------------------- overlap
-// auxiliary integrals A_k(x), k = 0..6 (diat_overlap_PM6_SP.py:464-519)
-__device__ void aint(double x, double *a) {
-  double xs = x != 0.0 ? x : INFINITY;
-  a[0] = exp(-xs) / xs;
-  a[1] = a[0] + a[0] / xs;
-#pragma unroll
-  for (int k = 2; k < 7; ++k) a[k] = a[0] + k * a[k - 1] / xs;
-}
-
-// auxiliary integrals B_k(x), k = 0..6 (diat_overlap_PM6_SP.py:522-670)
-__device__ void bint(double x, double *b) {
-  double ax = fabs(x);
-  if (ax > 0.5) {
-    double tx = exp(x) / x, tmx = -exp(-x) / x;
-    b[0] = tx + tmx;
-#pragma unroll
-    for (int k = 1; k < 7; ++k) b[k] = ((k & 1) ? -tx : tx) + tmx + k * b[k - 1] / x;
-  } else if (ax > 1.0e-6) {
-    double x2 = x * x, x3 = x2 * x, x4 = x2 * x2, x5 = x4 * x, x6 = x4 * x2;
-    b[0] = 2.0 + x2 / 3.0 + x4 / 60.0 + x6 / 2520.0;
-    b[2] = 2.0 / 3.0 + x2 / 5.0 + x4 / 84.0 + x6 / 3240.0;
-    b[4] = 2.0 / 5.0 + x2 / 7.0 + x4 / 108.0 + x6 / 3960.0;
-    b[6] = 2.0 / 7.0 + x2 / 9.0 + x4 / 132.0 + x6 / 4680.0;
-    b[1] = -2.0 / 3.0 * x - x3 / 15.0 - x5 / 420.0;
-    b[3] = -2.0 / 5.0 * x - x3 / 21.0 - x5 / 540.0;
-    b[5] = -2.0 / 7.0 * x - x3 / 27.0 - x5 / 660.0;
-  } else {
-    b[0] = 2.0; b[1] = 0.0; b[2] = 2.0 / 3.0; b[3] = 0.0; b[4] = 2.0 / 5.0; b[5] = 0.0; b[6] = 2.0 / 7.0;
-  }
-}
-
-struct Sloc { double s111, s211, s121, s221, s222; };
-
-// local-frame overlaps for the principal-quantum-number classes (diat_overlap_PM6_SP.py:56-312);
-// returns false for an unsupported class (the reference raises ValueError)
-__device__ bool overlap_local(int qni, int qnj, double r, double zsa, double zpa, double zsb, double zpb, Sloc &S) {
-  S.s111 = S.s211 = S.s121 = S.s221 = S.s222 = 0.0;
-  double A[7], B[7];
-  const double s3 = sqrt(3.0), s10 = sqrt(10.0), s30 = sqrt(30.0);
-  auto set = [&](double za, double zb) { aint(0.5 * r * (za + zb), A); bint(0.5 * r * (za - zb), B); };
-  if (qni == 1 && qnj == 1) {
-    set(zsa, zsb);
-    S.s111 = pow(zsa * zsb * r * r, 1.5) * (A[2] * B[0] - B[2] * A[0]) / 4.0;
-  } else if (qni == 2 && qnj == 1) {
-    double r4 = r * r * r * r;
-    set(zsa, zsb);
-    S.s111 = pow(zsb, 1.5) * pow(zsa, 2.5) * r4 * (A[3] * B[0] - B[3] * A[0] + A[2] * B[1] - B[2] * A[1]) / (s3 * 8.0);
-    set(zpa, zsb);
-    S.s211 = pow(zsb, 1.5) * pow(zpa, 2.5) * r4 * (A[2] * B[0] - B[2] * A[0] + A[3] * B[1] - B[3] * A[1]) / 8.0;
-  } else if (qni == 2 && qnj == 2) {
-    double r5 = r * r * r * r * r;
-    set(zsa, zsb);
-    S.s111 = pow(zsb * zsa, 2.5) * r5 * (A[4] * B[0] + B[4] * A[0] - 2.0 * A[2] * B[2]) / 48.0;
-    set(zpa, zsb);
-    S.s211 = pow(zsb * zpa, 2.5) * r5 *
-             (A[3] * (B[0] - B[2]) - A[1] * (B[2] - B[4]) + B[3] * (A[0] - A[2]) - B[1] * (A[2] - A[4])) / (16.0 * s3);
-    set(zsa, zpb);
-    S.s121 = pow(zpb * zsa, 2.5) * r5 *
-             (A[3] * (B[0] - B[2]) - A[1] * (B[2] - B[4]) - B[3] * (A[0] - A[2]) + B[1] * (A[2] - A[4])) / (16.0 * s3);
-    set(zpa, zpb);
-    double w = pow(zpb * zpa, 2.5) * r5 / 16.0;
-    S.s221 = -w * (B[2] * (A[4] + A[0]) - A[2] * (B[4] + B[0]));
-    S.s222 = 0.5 * w * (A[4] * (B[0] - B[2]) - B[4] * (A[0] - A[2]) - A[2] * B[0] + B[2] * A[0]);
-  } else if (qni == 3 && qnj == 1) {
-    double r5 = r * r * r * r * r;
-    set(zsa, zsb);
-    S.s111 = pow(zsb, 1.5) * pow(zsa, 3.5) * r5 * (A[4] * B[0] + 2 * B[1] * A[3] - 2.0 * A[1] * B[3] - B[4] * A[0]) /
-             (s10 * 24.0);
-    set(zpa, zsb);
-    S.s211 = pow(zsb, 1.5) * pow(zpa, 3.5) * r5 *
-             (A[3] * (B[0] + B[2]) - A[1] * (B[4] + B[2]) + B[1] * (A[2] + A[4]) - B[3] * (A[2] + A[0])) / (8.0 * s30);
-  } else if (qni == 3 && qnj == 2) {
-    double r6 = r * r * r * r * r * r;
-    set(zsa, zsb);
-    S.s111 = pow(zsb, 2.5) * pow(zsa, 3.5) * r6 *
-             (A[5] * B[0] + B[1] * A[4] - 2 * B[2] * A[3] - 2.0 * A[2] * B[3] + B[4] * A[1] + B[5] * A[0]) / (s30 * 48.0);
-    set(zpa, zsb);
-    S.s211 = pow(zsb, 2.5) * pow(zpa, 3.5) * r6 *
-             (A[4] * B[0] + B[1] * A[5] - 2.0 * B[3] * A[3] - 2.0 * A[2] * B[2] + A[1] * B[5] + A[0] * B[4]) / (48.0 * s10);
-    set(zsa, zpb);
-    S.s121 = pow(zpb, 2.5) * pow(zsa, 3.5) * r6 *
-             ((A[4] * B[0] - A[5] * B[1]) + 2.0 * (A[3] * B[1] - A[4] * B[2]) - 2.0 * (A[1] * B[3] - A[2] * B[4]) -
-              (A[0] * B[4] - A[1] * B[5])) / (48.0 * s10);
-    set(zpa, zpb);
-    S.s221 = pow(zpb, 2.5) * pow(zpa, 3.5) * r6 *
-             ((A[3] * B[0] - A[5] * B[2]) + (A[2] * B[1] - A[4] * B[3]) - (A[1] * B[2] - A[3] * B[4]) -
-              (A[0] * B[3] - A[2] * B[5])) / (16.0 * s30);
-    S.s222 = pow(zpb, 2.5) * pow(zpa, 3.5) * r6 *
-             ((A[5] - A[3]) * (B[0] - B[2]) + (A[4] - A[2]) * (B[1] - B[3]) - (A[3] - A[1]) * (B[2] - B[4]) -
-              (A[2] - A[0]) * (B[3] - B[5])) / (32.0 * s30);
-  } else if (qni == 3 && qnj == 3) {
-    double r7 = r * r * r * r * r * r * r;
-    set(zsa, zsb);
-    S.s111 = pow(zsb * zsa, 3.5) * r7 * (A[6] * B[0] - 3.0 * B[2] * A[4] + 3.0 * A[2] * B[4] - A[0] * B[6]) / 1440.0;
-    set(zpa, zsb);
-    S.s211 = pow(zsb * zpa, 3.5) * r7 *
-             ((A[5] * B[0] + A[6] * B[1]) + (-A[4] * B[1] - A[5] * B[2]) - 2.0 * (A[3] * B[2] + A[4] * B[3]) -
-              2.0 * (-A[2] * B[3] - A[3] * B[4]) + (A[1] * B[4] + A[2] * B[5]) + (-A[0] * B[5] - A[1] * B[6])) /
-             (480.0 * s3);
-    set(zsa, zpb);
-    S.s121 = pow(zpb * zsa, 3.5) * r7 *
-             ((A[5] * B[0] - A[6] * B[1]) + (A[4] * B[1] - A[5] * B[2]) - 2.0 * (A[3] * B[2] - A[4] * B[3]) -
-              2.0 * (A[2] * B[3] - A[3] * B[4]) + (A[1] * B[4] - A[2] * B[5]) + (A[0] * B[5] - A[1] * B[6])) /
-             (480.0 * s3);
-    set(zpa, zpb);
-    S.s221 = pow(zpb, 3.5) * pow(zpa, 3.5) * r7 *
-             ((A[4] * B[0] - A[6] * B[2]) - 2.0 * (A[2] * B[2] - A[4] * B[4]) + (A[0] * B[4] - A[2] * B[6])) / 480.0;
-    S.s222 = pow(zpb, 3.5) * pow(zpa, 3.5) * r7 *
-             ((A[6] - A[4]) * (B[0] - B[2]) - 2.0 * (A[4] - A[2]) * (B[2] - B[4]) + (A[2] - A[0]) * (B[4] - B[6])) /
-             960.0;
-  } else {
-    return false;
-  }
-  return true;
-}
-#undef SQ
-
 // ------------------------------------------------------------- pair kernel
 __global__ void __launch_bounds__(128) k_pairs(seqm_batch b, double *__restrict__ w_xx, double *__restrict__ w_xh,
                                                double *__restrict__ w_hh, double *__restrict__ H,
@@ -372,87 +87,49 @@ __global__ void __launch_bounds__(128) k_pairs(seqm_batch b, double *__restrict_
   double xv = dx / dist, yv = dy / dist, zv = dz / dist;
   const double r0a = par(b, SEQM_P_RHO0, ia), r0b = par(b, SEQM_P_RHO0, ja);
   double R[3][3];
-  quat_rot(-xv, -yv, -zv, R);
+  quat_rot<double>(-xv, -yv, -zv, R);
   double gam;
   if (cls == 2) {
     double ri[22];
-    local_xx(r, par(b, SEQM_P_DD, ia), par(b, SEQM_P_DD, ja), par(b, SEQM_P_QQ, ia), par(b, SEQM_P_QQ, ja), r0a, r0b,
-             par(b, SEQM_P_RHO1, ia), par(b, SEQM_P_RHO1, ja), par(b, SEQM_P_RHO2, ia), par(b, SEQM_P_RHO2, ja), ri);
-    rotate_xx(ri, R, w_xx + (size_t)100 * p);
+    local_xx<double>(r, par(b, SEQM_P_DD, ia), par(b, SEQM_P_DD, ja), par(b, SEQM_P_QQ, ia), par(b, SEQM_P_QQ, ja),
+                     r0a, r0b, par(b, SEQM_P_RHO1, ia), par(b, SEQM_P_RHO1, ja), par(b, SEQM_P_RHO2, ia),
+                     par(b, SEQM_P_RHO2, ja), ri);
+    double *w = w_xx + (size_t)100 * p;
+    rotate_xx<double>(ri, R, [&](int a, int c, double v) { w[a * 10 + c] = v; });
     gam = ri[0];
   } else if (cls == 1) {
     double ri[4];
-    local_xh(r, par(b, SEQM_P_DD, ia), par(b, SEQM_P_QQ, ia), r0a, r0b, par(b, SEQM_P_RHO1, ia),
-             par(b, SEQM_P_RHO2, ia), ri);
-    rotate_xh(ri, R, w_xh + (size_t)10 * (p - b.nxx));
+    local_xh<double>(r, par(b, SEQM_P_DD, ia), par(b, SEQM_P_QQ, ia), r0a, r0b, par(b, SEQM_P_RHO1, ia),
+                     par(b, SEQM_P_RHO2, ia), ri);
+    double *w = w_xh + (size_t)10 * (p - b.nxx);
+    rotate_xh<double>(ri, R, [&](int a, double v) { w[a] = v; });
     gam = ri[0];
   } else {
     gam = EV / sqrt(r * r + (r0a + r0b) * (r0a + r0b));
     w_hh[p - b.nxx - b.nxh] = gam;
   }
-
-  // core-core repulsion (energy.py:91-134)
-  {
-    const int Zi = b.atom_Z[ia], Zj = b.atom_Z[ja];
-    double rija = r * A0;
-    double ti = par(b, SEQM_P_TORE, ia), tj = par(b, SEQM_P_TORE, ja);
-    double t1 = ti * tj * gam;
-    double tmp = exp(-par(b, SEQM_P_ALPHA, ia) * rija);
-    double t2 = ((Zi == 7 || Zi == 8) && Zj == 1) ? tmp * rija : tmp;
-    double t3 = exp(-par(b, SEQM_P_ALPHA, ja) * rija);
-    double e = t1 * (1.0 + t2 + t3);
-    int ng = b.method == SEQM_AM1 ? 4 : (b.method == SEQM_PM3 ? 2 : 0);
-    if (ng) {
-      double t4 = ti * tj / rija, t5 = 0.0, t6 = 0.0;
-      for (int g = 0; g < ng; ++g) {
-        double Ki = par(b, SEQM_P_K1 + g, ia), Li = par(b, SEQM_P_L1 + g, ia), Mi = par(b, SEQM_P_M1 + g, ia);
-        double Kj = par(b, SEQM_P_K1 + g, ja), Lj = par(b, SEQM_P_L1 + g, ja), Mj = par(b, SEQM_P_M1 + g, ja);
-        t5 += Ki * exp(-Li * (rija - Mi) * (rija - Mi));
-        t6 += Kj * exp(-Lj * (rija - Mj) * (rija - Mj));
-      }
-      e += t4 * (t5 + t6);
-    }
-    enuc[p] = e;
-  }
+  enuc[p] = core_core<double>(b, ia, ja, r, gam);
 
   // overlap * (beta_i + beta_j)/2 -> off-diagonal Hcore block, written with its transpose
-  {
-    double di[4][4] = {};
-    if (r <= OVERLAP_CUTOFF) {
-      Sloc S;
-      if (!overlap_local((int)par(b, SEQM_P_QN, ia), (int)par(b, SEQM_P_QN, ja), r, par(b, SEQM_P_ZS, ia),
-                         par(b, SEQM_P_ZP, ia), par(b, SEQM_P_ZS, ja), par(b, SEQM_P_ZP, ja), S)) {
-        atomicExch(err, SEQM_E_UNSUPPORTED);
-        return;
-      }
-      double Q[3][3];
-      quat_rot(xv, yv, zv, Q);
-      di[0][0] = S.s111;
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        di[1 + a][0] = S.s211 * Q[0][a];
-        di[0][1 + a] = -S.s121 * Q[0][a];
-      }
-      const double Mv[3] = {-S.s221, S.s222, S.s222};
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-          di[1 + a][1 + c] = Q[0][a] * Mv[0] * Q[0][c] + Q[1][a] * Mv[1] * Q[1][c] + Q[2][a] * Mv[2] * Q[2][c];
-    }
-    const int li = ia - a0, lj = ja - a0;
-    const int oi = atom_ao(li, nh), oj = atom_ao(lj, nh);
-    const int ni_ = li < nh ? 4 : 1, nj_ = lj < nh ? 4 : 1;
-    double bi[4] = {par(b, SEQM_P_BS, ia), par(b, SEQM_P_BP, ia), par(b, SEQM_P_BP, ia), par(b, SEQM_P_BP, ia)};
-    double bj[4] = {par(b, SEQM_P_BS, ja), par(b, SEQM_P_BP, ja), par(b, SEQM_P_BP, ja), par(b, SEQM_P_BP, ja)};
-    double *Hm = H + b.mol_mat_off[m];
-    for (int mu = 0; mu < ni_; ++mu)
-      for (int nu = 0; nu < nj_; ++nu) {
-        double v = di[mu][nu] * ((bi[mu] + bj[nu]) * 0.5);
-        Hm[(size_t)(oi + mu) * norb + (oj + nu)] = v;
-        Hm[(size_t)(oj + nu) * norb + (oi + mu)] = v;
-      }
+  double di[4][4];
+  if (!overlap_block<double>((int)par(b, SEQM_P_QN, ia), (int)par(b, SEQM_P_QN, ja), r, xv, yv, zv,
+                             par(b, SEQM_P_ZS, ia), par(b, SEQM_P_ZP, ia), par(b, SEQM_P_ZS, ja),
+                             par(b, SEQM_P_ZP, ja), di)) {
+    atomicExch(err, SEQM_E_UNSUPPORTED);
+    return;
   }
+  const int li = ia - a0, lj = ja - a0;
+  const int oi = atom_ao(li, nh), oj = atom_ao(lj, nh);
+  const int ni_ = li < nh ? 4 : 1, nj_ = lj < nh ? 4 : 1;
+  const double bi[4] = {par(b, SEQM_P_BS, ia), par(b, SEQM_P_BP, ia), par(b, SEQM_P_BP, ia), par(b, SEQM_P_BP, ia)};
+  const double bj[4] = {par(b, SEQM_P_BS, ja), par(b, SEQM_P_BP, ja), par(b, SEQM_P_BP, ja), par(b, SEQM_P_BP, ja)};
+  double *Hm = H + b.mol_mat_off[m];
+  for (int mu = 0; mu < ni_; ++mu)
+    for (int nu = 0; nu < nj_; ++nu) {
+      double v = di[mu][nu] * ((bi[mu] + bj[nu]) * 0.5);
+      Hm[(size_t)(oi + mu) * norb + (oj + nu)] = v;
+      Hm[(size_t)(oj + nu) * norb + (oi + mu)] = v;
+    }
 }
 
 // ------------------------------------------------- diagonal Hcore blocks

@@ -179,6 +179,27 @@ class Layout:
         out[src] = full.reshape(-1)[dst]
         return out
 
+    def reference_pair_index(self):
+        """Position of each of our pairs (class order) in the reference's (molecule, i<j) row-major order."""
+        if getattr(self, "_refpos", None) is None:
+            nat = self.natoms_m
+            ref_off = np.concatenate([[0], np.cumsum(nat * (nat - 1) // 2)])
+            m = self.atom_mol[self.pair_i]
+            i = self.pair_i - self.atom_off[m]
+            j = self.pair_j - self.atom_off[m]
+            n = nat[m]
+            self._refpos = ref_off[m] + i * n - (i * (i + 1)) // 2 + (j - i - 1)
+        return self._refpos
+
+    def reference_pair_atoms(self):
+        """(idxi, idxj) global atom indices of the pairs in the reference's order."""
+        pos = self.reference_pair_index()
+        ri = np.empty(self.npairs, dtype=np.int64)
+        rj = np.empty(self.npairs, dtype=np.int64)
+        ri[pos] = self.pair_i
+        rj[pos] = self.pair_j
+        return ri, rj
+
     def block(self, flat, m):
         """Molecule m's dense norb x norb matrix view from a concatenated flat array."""
         n = int(self.norb[m])

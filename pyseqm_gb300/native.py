@@ -28,7 +28,7 @@ PAR = {n: i for i, n in enumerate(PAR_NAMES)}
 
 EXPORTS = ["seqm_hcore", "seqm_fock", "seqm_density_jacobi", "seqm_density_jacobi_noalloc", "seqm_density_sp2",
            "seqm_mix", "seqm_energy_error",
-           "seqm_initial_density", "seqm_pair_sum", "seqm_version"]
+           "seqm_initial_density", "seqm_pair_sum", "seqm_energy_grad", "seqm_version"]
 
 _P = ctypes.c_void_p
 
@@ -75,6 +75,7 @@ def load(path=None):
         "seqm_energy_error": [B, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, f64, _P],
         "seqm_initial_density": [B, _P, _P],
         "seqm_pair_sum": [B, _P, _P, _P],
+        "seqm_energy_grad": [B, _P, _P, _P, _P, _P, _P, _P],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

@@ -92,10 +92,14 @@ int seqm_fock(const seqm_batch *b, const double *P, const double *H, const doubl
  * warm (NULL: cold start for all): molecules with warm[m] != 0 start from the orthonormal
  * rows already in `work` (the previous call's eigenvectors) and rotate A = V F V^T, which
  * converges in fewer sweeps when F changed little (successive SCF iterations); needs P.
- * status[m]: number of sweeps, or -1 if the sweep cap was hit. */
+ * mixed_threshold > 0 (needs P): molecules starting cold, or whose previous call (status[m]
+ * on entry) took >= mixed_threshold sweeps, first sweep in FP32 (A and the rotation product
+ * in shared memory), then lift the vectors to FP64 (one Newton-Schulz re-orthonormalisation)
+ * and finish with FP64 sweeps; 0 = FP64 sweeps only.  The result is FP64-accurate either way.
+ * status[m]: sweeps taken (FP32 + FP64), or -1 if the FP64 sweep cap was hit. */
 int seqm_density_jacobi(const seqm_batch *b, const double *F, double *P, double *evals, double *evecs,
                         double *work, const int64_t *mol_row_off, const uint8_t *active, int32_t *status,
-                        int max_sweeps, const uint8_t *warm, void *stream);
+                        int max_sweeps, const uint8_t *warm, int mixed_threshold, void *stream);
 
 /* Allocation-free seqm_density_jacobi.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory (a host that owns a fixed device-memory pool,

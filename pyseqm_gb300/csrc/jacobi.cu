@@ -1,4 +1,4 @@
-// Batched symmetric eigensolver + closed-shell density (FP64), one CTA per molecule.
+// Batched symmetric eigensolver + closed-shell density, one CTA per molecule.
 //
 // Replaces sym_eig_trunc (seqm/seqm_functions/diag.py:110-241), which packs F,
 // pads every molecule to the batch's largest basis with shifted diagonal
@@ -6,15 +6,24 @@
 // Here each molecule is solved at its own size, so there is no padding.
 //
 // Algorithm: parallel cyclic Jacobi with the round-robin ("circle") ordering:
-// each step rotates n/2 disjoint (p,q) pairs at once.  The matrix A lives in
-// shared memory (row stride odd to spread banks); a thread owns a 2x2 block
-// (pair i rows) x (pair j cols), applies both one-sided rotations and writes the
-// block and its mirror, so every element is touched once per step.  The
-// eigenvectors are kept as ROWS of a per-molecule scratch block in global
-// memory (L2-resident); warp w rotates rows p,q of pair w with coalesced
-// accesses.  Rotations with |a_pq| <= 1e-13 ||A||_F are skipped; the solve stops
-// after a sweep without rotations.  Eigenvalues are ranked, and P is formed from
-// whichever of the occupied / virtual sets is smaller (P = 2 (I - C_v C_v^T)).
+// each step rotates n/2 disjoint (p,q) pairs at once.  A lives in shared memory
+// (odd row stride); a thread owns a 2x2 block (pair i rows) x (pair j cols),
+// applies both one-sided rotations and writes the block and its mirror, so every
+// element is touched once per step.  Eigenvector ROWS are rotated by one warp per
+// pair with coalesced accesses.  A sweep starts only if max |a_pq| > tol, and
+// rotations with |a_pq| <= tol are skipped.
+//
+// GB300's FP64 rate is ~1/64 of FP32, so the sweeps that only need to bring the
+// off-diagonal down to ~1e-6 run in FP32 when that pays:
+//   warm start (previous SCF step's eigenvector rows V in `work`): A = V F V^T;
+//   cold start: A = F, V = I.
+//   If cold, or the previous call needed >= mixed_threshold sweeps:
+//     FP32 Jacobi on (float)A accumulating W (both in shared memory),
+//     V <- W V in FP64, one Newton-Schulz step V <- 1.5 V - 0.5 (V V^T) V
+//     (restores orthonormality from ~1e-6 to ~1e-12), A = V F V^T again;
+//   FP64 polish sweeps to max |a_pq| <= 1e-13 ||F||_F.
+// Eigenvalues are ranked, and P is formed from whichever of the occupied /
+// virtual sets is smaller (P = 2 (I - C_v C_v^T)).
 #include <math.h>
 
 #include "common.cuh"
@@ -25,18 +34,184 @@ constexpr int NT_J = 256;
 constexpr int JMAX_N = 160;
 constexpr int JMAX_P = JMAX_N / 2;
 
+struct JShared {
+  double rc[JMAX_P], rs[JMAX_P], rt[JMAX_P];
+  int rp[JMAX_P], rq[JMAX_P], rflag[JMAX_P];
+  double red[NT_J / 32];
+};
+
+__device__ double jblock_reduce(double v, double *red, bool is_max) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double u = __shfl_xor_sync(0xffffffffu, v, o);
+    v = is_max ? fmax(v, u) : v + u;
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = red[0];
+  for (int w = 1; w < NT_J / 32; ++w) s = is_max ? fmax(s, red[w]) : s + red[w];
+  __syncthreads();
+  return s;
+}
+
+// 4x4-register-tile product out(k, j) <- sum_l L(k, l) R(l, j), k, j < n (upper tiles only if asked)
+template <class LF, class RF, class OF>
+__device__ void tile_product(int n, bool upper_only, LF L, RF R, OF out) {
+  const int nt = (n + 3) >> 2;
+  for (int t = threadIdx.x; t < nt * nt; t += NT_J) {
+    const int kb = t / nt, jb = t % nt;
+    if (upper_only && kb > jb) continue;
+    const int k0 = kb * 4, j0 = jb * 4;
+    double acc[4][4] = {};
+    for (int l = 0; l < n; ++l) {
+      double a[4], c[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) a[r] = (k0 + r < n) ? L(k0 + r, l) : 0.0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) c[q] = (j0 + q < n) ? R(l, j0 + q) : 0.0;
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[r][q] += a[r] * c[q];
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (k0 + r < n && j0 + q < n) out(k0 + r, j0 + q, acc[r][q]);
+  }
+}
+
+// A (shared, holding F on entry) <- V F V^T; G (global n x n) is scratch
+__device__ void form_vfvt(double *A, int lda, const double *V, double *G, int n) {
+  tile_product(
+      n, false, [&](int k, int l) { return V[(size_t)k * n + l]; }, [&](int l, int j) { return A[l * lda + j]; },
+      [&](int k, int j, double v) { G[(size_t)k * n + j] = v; });
+  __syncthreads();
+  tile_product(
+      n, true, [&](int k, int j) { return G[(size_t)k * n + j]; }, [&](int j, int l) { return V[(size_t)l * n + j]; },
+      [&](int k, int l, double v) {
+        if (k <= l) { A[k * lda + l] = v; A[l * lda + k] = v; }
+      });
+  __syncthreads();
+}
+
+template <class T>
+__device__ double offdiag_max(const T *A, int lda, int n, double *red) {
+  double mx = 0.0;
+  for (int idx = threadIdx.x; idx < n * n; idx += NT_J) {
+    int i = idx / n, j = idx - i * n;
+    if (i != j) mx = fmax(mx, fabs((double)A[i * lda + j]));
+  }
+  return jblock_reduce(mx, red, true);
+}
+
+// Jacobi sweeps on A (shared memory, stride lda) accumulating the rotations into the
+// rows of V (stride n, shared or global).  Returns the sweeps performed, or -1 if
+// max |a_pq| > tol after max_sweeps.
+template <class T>
+__device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_sweeps, JShared &sh) {
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int npad = n + (n & 1), np = npad / 2, nsteps = npad - 1;
+  const T ttol = (T)tol;
+  for (int sweep = 0; sweep <= max_sweeps; ++sweep) {
+    if (offdiag_max(A, lda, n, sh.red) <= tol) return sweep;
+    if (sweep == max_sweeps) break;
+    for (int step = 0; step < nsteps; ++step) {
+      if (tid < np) {
+        int a, c;
+        if (tid == 0) { a = npad - 1; c = step; }
+        else { a = (step + tid) % (npad - 1); c = (step - tid + npad - 1) % (npad - 1); }
+        const int p = min(a, c), q = max(a, c);
+        sh.rp[tid] = p;
+        sh.rq[tid] = q;
+        int fl = 0;
+        T cc = 1, ss = 0, tt = 0;
+        if (q < n) {
+          const T apq = A[p * lda + q];
+          if (fabs(apq) > ttol) {
+            const T app = A[p * lda + p], aqq = A[q * lda + q];
+            const T theta = (aqq - app) / (T(2) * apq);
+            T t = T(1) / (fabs(theta) + sqrt(theta * theta + T(1)));
+            if (theta < T(0)) t = -t;
+            cc = T(1) / sqrt(t * t + T(1));
+            ss = t * cc;
+            tt = t;
+            fl = 1;
+          }
+        }
+        sh.rc[tid] = (double)cc;
+        sh.rs[tid] = (double)ss;
+        sh.rt[tid] = (double)tt;
+        sh.rflag[tid] = fl;
+      }
+      __syncthreads();
+      // A <- J^T A J on 2x2 blocks (i <= j); block and mirror written by one thread
+      for (int it = tid; it < np * np; it += NT_J) {
+        const int i = it / np, j = it - i * np;
+        if (j < i) continue;
+        const int fi = sh.rflag[i], fj = sh.rflag[j];
+        if (!(fi | fj)) continue;
+        const int p = sh.rp[i], q = sh.rq[i];
+        if (i == j) {
+          const T t = (T)sh.rt[i], apq = A[p * lda + q];
+          A[p * lda + p] -= t * apq;
+          A[q * lda + q] += t * apq;
+          A[p * lda + q] = T(0);
+          A[q * lda + p] = T(0);
+          continue;
+        }
+        const int r = sh.rp[j], s = sh.rq[j];
+        const bool qv = q < n, sv = s < n;
+        T x00 = A[p * lda + r];
+        T x01 = sv ? A[p * lda + s] : T(0);
+        T x10 = qv ? A[q * lda + r] : T(0);
+        T x11 = (qv && sv) ? A[q * lda + s] : T(0);
+        if (fi) {
+          const T c = (T)sh.rc[i], sn = (T)sh.rs[i];
+          T y00 = c * x00 - sn * x10, y10 = sn * x00 + c * x10;
+          T y01 = c * x01 - sn * x11, y11 = sn * x01 + c * x11;
+          x00 = y00; x10 = y10; x01 = y01; x11 = y11;
+        }
+        if (fj) {
+          const T c = (T)sh.rc[j], sn = (T)sh.rs[j];
+          T z00 = c * x00 - sn * x01, z01 = sn * x00 + c * x01;
+          T z10 = c * x10 - sn * x11, z11 = sn * x10 + c * x11;
+          x00 = z00; x01 = z01; x10 = z10; x11 = z11;
+        }
+        A[p * lda + r] = x00;
+        A[r * lda + p] = x00;
+        if (sv) { A[p * lda + s] = x01; A[s * lda + p] = x01; }
+        if (qv) { A[q * lda + r] = x10; A[r * lda + q] = x10; }
+        if (qv && sv) { A[q * lda + s] = x11; A[s * lda + q] = x11; }
+      }
+      // eigenvector rows p,q: warp per pair, lanes along the row (coalesced / conflict-free)
+      for (int i = wid; i < np; i += NT_J / 32) {
+        if (!sh.rflag[i]) continue;
+        const T c = (T)sh.rc[i], sn = (T)sh.rs[i];
+        T *vp = V + (size_t)sh.rp[i] * n, *vq = V + (size_t)sh.rq[i] * n;
+        for (int k = lane; k < n; k += 32) {
+          const T a = vp[k], bq = vq[k];
+          vp[k] = c * a - sn * bq;
+          vq[k] = sn * a + c * bq;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  return -1;
+}
+
 __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__restrict__ F, double *__restrict__ P,
                                                  double *__restrict__ evals, double *__restrict__ evecs,
                                                  double *__restrict__ work, const int64_t *__restrict__ row_off,
                                                  const uint8_t *__restrict__ active, int32_t *__restrict__ status,
-                                                 int max_sweeps, const uint8_t *__restrict__ warm) {
+                                                 int max_sweeps, const uint8_t *__restrict__ warm,
+                                                 int mixed_threshold) {
   extern __shared__ double A[];
-  __shared__ double rc[JMAX_P], rs[JMAX_P], rt[JMAX_P];
-  __shared__ int rp[JMAX_P], rq[JMAX_P], rflag[JMAX_P];
+  __shared__ JShared sh;
   __shared__ double dg[JMAX_N];
   __shared__ int rank[JMAX_N];
-  __shared__ double red[NT_J / 32];
-  __shared__ int any_rot;
 
   const int m = b.mol_order[blockIdx.x];
   if (active && !active[m]) return;
@@ -46,10 +221,12 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
   const size_t mo = b.mol_mat_off[m];
   const double *Fm = F + mo;
   double *V = work + mo;  // row k = eigenvector k (column k of C)
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-
-  // warm start: V already holds orthonormal rows (the previous SCF step's eigenvectors)
+  double *G = P ? P + mo : nullptr;  // P's block doubles as product scratch until P is written
+  const int tid = threadIdx.x;
   const bool is_warm = warm != nullptr && warm[m] != 0 && P != nullptr;
+  const int hint = status ? status[m] : 0;
+  const bool mixed = mixed_threshold > 0 && P != nullptr && (!is_warm || hint < 0 || hint >= mixed_threshold);
+
   double f2 = 0.0;
   for (int idx = tid; idx < n * n; idx += NT_J) {
     int i = idx / n, j = idx - i * n;
@@ -58,167 +235,63 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
     if (!is_warm) V[idx] = i == j ? 1.0 : 0.0;
     f2 += v * v;
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) f2 += __shfl_xor_sync(0xffffffffu, f2, o);
-  if (lane == 0) red[wid] = f2;
-  __syncthreads();
-  if (tid == 0) {
-    double s = 0.0;
-    for (int w = 0; w < NT_J / 32; ++w) s += red[w];
-    red[0] = s;
-  }
-  __syncthreads();
-  const double tol = 1.0e-13 * sqrt(red[0]);
+  const double fro = sqrt(jblock_reduce(f2, sh.red, false));
+  const double tol = 1.0e-13 * fro;
+  if (is_warm) form_vfvt(A, lda, V, G, n);
 
-  if (is_warm) {
-    // A <- V F V^T in two FP64 products, 4x4 register tiles per thread:
-    //   G = V F   (F in shared memory, V rows from L2) -> the P block as temporary
-    //   A = G V^T (upper-triangle tiles, mirrored)      -> shared memory
-    double *G = P + mo;
-    const int nt = (n + 3) >> 2;
-    for (int t = tid; t < nt * nt; t += NT_J) {
-      const int k0 = (t / nt) * 4, j0 = (t % nt) * 4;
-      double acc[4][4] = {};
-      for (int i = 0; i < n; ++i) {
-        double v[4], f[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) v[r] = (k0 + r < n) ? V[(size_t)(k0 + r) * n + i] : 0.0;
-#pragma unroll
-        for (int c = 0; c < 4; ++c) f[c] = (j0 + c < n) ? A[i * lda + j0 + c] : 0.0;
-#pragma unroll
-        for (int r = 0; r < 4; ++r)
-#pragma unroll
-          for (int c = 0; c < 4; ++c) acc[r][c] += v[r] * f[c];
-      }
-#pragma unroll
-      for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int c = 0; c < 4; ++c)
-          if (k0 + r < n && j0 + c < n) G[(size_t)(k0 + r) * n + j0 + c] = acc[r][c];
+  int s32 = 0;
+  if (mixed) {
+    // FP32 sweeps on (float)A with W accumulated in shared memory (A32 | W32 overlay A64)
+    for (int idx = tid; idx < n * n; idx += NT_J) {
+      int i = idx / n, j = idx - i * n;
+      G[idx] = A[i * lda + j];
     }
     __syncthreads();
-    for (int t = tid; t < nt * nt; t += NT_J) {
-      const int kb = t / nt, lb = t % nt;
-      if (kb > lb) continue;
-      const int k0 = kb * 4, l0 = lb * 4;
-      double acc[4][4] = {};
-      for (int j = 0; j < n; ++j) {
-        double g[4], v[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) g[r] = (k0 + r < n) ? G[(size_t)(k0 + r) * n + j] : 0.0;
-#pragma unroll
-        for (int c = 0; c < 4; ++c) v[c] = (l0 + c < n) ? V[(size_t)(l0 + c) * n + j] : 0.0;
-#pragma unroll
-        for (int r = 0; r < 4; ++r)
-#pragma unroll
-          for (int c = 0; c < 4; ++c) acc[r][c] += g[r] * v[c];
-      }
-#pragma unroll
-      for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          const int k = k0 + r, l = l0 + c;
-          if (k < n && l < n && k <= l) {
-            A[k * lda + l] = acc[r][c];
-            A[l * lda + k] = acc[r][c];
-          }
-        }
+    float *A32 = reinterpret_cast<float *>(A), *W32 = A32 + (size_t)n * lda;
+    for (int idx = tid; idx < n * n; idx += NT_J) {
+      int i = idx / n, j = idx - i * n;
+      A32[i * lda + j] = (float)G[idx];
+      W32[idx] = i == j ? 1.0f : 0.0f;  // rows of stride n, as jacobi_solve expects
     }
     __syncthreads();
+    s32 = jacobi_solve<float>(A32, lda, W32, n, 3.0e-6 * fro, 20, sh);
+    if (s32 < 0) s32 = 20;
+    __syncthreads();
+    // V <- W V (warm) or W (cold), in FP64
+    if (is_warm) {
+      tile_product(
+          n, false, [&](int k, int l) { return (double)W32[k * n + l]; },
+          [&](int l, int j) { return V[(size_t)l * n + j]; }, [&](int k, int j, double v) { G[(size_t)k * n + j] = v; });
+    } else {
+      for (int idx = tid; idx < n * n; idx += NT_J) G[idx] = (double)W32[idx];
+    }
+    __syncthreads();
+    for (int idx = tid; idx < n * n; idx += NT_J) V[idx] = G[idx];
+    __syncthreads();
+    // one Newton-Schulz step: S = V V^T (shared), V <- 1.5 V - 0.5 S V
+    double *S = A;
+    tile_product(
+        n, true, [&](int k, int j) { return V[(size_t)k * n + j]; }, [&](int j, int l) { return V[(size_t)l * n + j]; },
+        [&](int k, int l, double v) {
+          if (k <= l) { S[k * lda + l] = v; S[l * lda + k] = v; }
+        });
+    __syncthreads();
+    tile_product(
+        n, false, [&](int k, int l) { return S[k * lda + l]; }, [&](int l, int j) { return V[(size_t)l * n + j]; },
+        [&](int k, int j, double v) { G[(size_t)k * n + j] = 1.5 * V[(size_t)k * n + j] - 0.5 * v; });
+    __syncthreads();
+    for (int idx = tid; idx < n * n; idx += NT_J) {
+      int i = idx / n, j = idx - i * n;
+      V[idx] = G[idx];
+      A[i * lda + j] = Fm[idx];
+    }
+    __syncthreads();
+    form_vfvt(A, lda, V, G, n);
   }
 
-  const int npad = n + (n & 1), np = npad / 2, nsteps = npad - 1;
-  int sweeps = -1;
-  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
-    if (tid == 0) any_rot = 0;
-    __syncthreads();
-    for (int step = 0; step < nsteps; ++step) {
-      // ---- rotations of this step's disjoint pairs
-      if (tid < np) {
-        int a, c;
-        if (tid == 0) { a = npad - 1; c = step; }
-        else { a = (step + tid) % (npad - 1); c = (step - tid + npad - 1) % (npad - 1); }
-        int p = min(a, c), q = max(a, c);
-        rp[tid] = p;
-        rq[tid] = q;
-        int fl = 0;
-        double cc = 1.0, ss = 0.0, tt = 0.0;
-        if (q < n) {
-          double apq = A[p * lda + q];
-          if (fabs(apq) > tol) {
-            double app = A[p * lda + p], aqq = A[q * lda + q];
-            double theta = (aqq - app) / (2.0 * apq);
-            double t = 1.0 / (fabs(theta) + sqrt(theta * theta + 1.0));
-            if (theta < 0.0) t = -t;
-            cc = 1.0 / sqrt(t * t + 1.0);
-            ss = t * cc;
-            tt = t;
-            fl = 1;
-            any_rot = 1;
-          }
-        }
-        rc[tid] = cc;
-        rs[tid] = ss;
-        rt[tid] = tt;
-        rflag[tid] = fl;
-      }
-      __syncthreads();
-      // ---- A <- J^T A J on 2x2 blocks (i <= j), block and mirror written by one thread
-      for (int it = tid; it < np * np; it += NT_J) {
-        const int i = it / np, j = it - i * np;
-        if (j < i) continue;
-        const int fi = rflag[i], fj = rflag[j];
-        if (!(fi | fj)) continue;
-        const int p = rp[i], q = rq[i];
-        if (i == j) {
-          const double t = rt[i], apq = A[p * lda + q];
-          A[p * lda + p] -= t * apq;
-          A[q * lda + q] += t * apq;
-          A[p * lda + q] = 0.0;
-          A[q * lda + p] = 0.0;
-          continue;
-        }
-        const int r = rp[j], s = rq[j];
-        const bool qv = q < n, sv = s < n;
-        double x00 = A[p * lda + r];
-        double x01 = sv ? A[p * lda + s] : 0.0;
-        double x10 = qv ? A[q * lda + r] : 0.0;
-        double x11 = (qv && sv) ? A[q * lda + s] : 0.0;
-        if (fi) {
-          const double c = rc[i], sn = rs[i];
-          double y00 = c * x00 - sn * x10, y10 = sn * x00 + c * x10;
-          double y01 = c * x01 - sn * x11, y11 = sn * x01 + c * x11;
-          x00 = y00; x10 = y10; x01 = y01; x11 = y11;
-        }
-        if (fj) {
-          const double c = rc[j], sn = rs[j];
-          double z00 = c * x00 - sn * x01, z01 = sn * x00 + c * x01;
-          double z10 = c * x10 - sn * x11, z11 = sn * x10 + c * x11;
-          x00 = z00; x01 = z01; x10 = z10; x11 = z11;
-        }
-        A[p * lda + r] = x00;
-        A[r * lda + p] = x00;
-        if (sv) { A[p * lda + s] = x01; A[s * lda + p] = x01; }
-        if (qv) { A[q * lda + r] = x10; A[r * lda + q] = x10; }
-        if (qv && sv) { A[q * lda + s] = x11; A[s * lda + q] = x11; }
-      }
-      // ---- eigenvector rows p,q: warp per pair, lanes along the row (coalesced)
-      for (int i = wid; i < np; i += NT_J / 32) {
-        if (!rflag[i]) continue;
-        const double c = rc[i], sn = rs[i];
-        double *vp = V + (size_t)rp[i] * n, *vq = V + (size_t)rq[i] * n;
-        for (int k = lane; k < n; k += 32) {
-          double a = vp[k], bq = vq[k];
-          vp[k] = c * a - sn * bq;
-          vq[k] = sn * a + c * bq;
-        }
-      }
-      __syncthreads();
-    }
-    if (!any_rot) { sweeps = sweep + 1; break; }
-    __syncthreads();
-  }
-  if (tid == 0 && status) status[m] = sweeps;
+  const int s64 = jacobi_solve<double>(A, lda, V, n, tol, max_sweeps, sh);
+  __syncthreads();
+  if (tid == 0 && status) status[m] = s64 < 0 ? -1 : s64 + s32;
 
   // ---- eigenvalues, ranks (ascending; ties by index)
   for (int k = tid; k < n; k += NT_J) dg[k] = A[k * lda + k];
@@ -273,9 +346,9 @@ using namespace seqm;
 
 extern "C" int seqm_density_jacobi(const seqm_batch *bp, const double *F, double *P, double *evals, double *evecs,
                                    double *work, const int64_t *mol_row_off, const uint8_t *active, int32_t *status,
-                                   int max_sweeps, const uint8_t *warm, void *stream) {
+                                   int max_sweeps, const uint8_t *warm, int mixed_threshold, void *stream) {
   if (!bp || !work) return SEQM_E_ARG;
-  if (warm && !P) return SEQM_E_ARG;  // a warm start uses P's block as temporary storage
+  if ((warm || mixed_threshold > 0) && !P) return SEQM_E_ARG;  // P's block is used as product scratch
   seqm_batch b = *bp;
   if (b.nmol == 0) return SEQM_OK;
   if (b.max_norb > JMAX_N) return SEQM_E_TOO_LARGE;
@@ -285,7 +358,7 @@ extern "C" int seqm_density_jacobi(const seqm_batch *bp, const double *F, double
   if (cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return SEQM_E_CUDA;
   k_jacobi<<<b.nmol, NT_J, smem, (cudaStream_t)stream>>>(b, F, P, evals, evecs, work, mol_row_off, active, status,
-                                                         max_sweeps, warm);
+                                                         max_sweeps, warm, mixed_threshold);
   return launch_check();
 }
 
@@ -359,6 +432,6 @@ extern "C" int seqm_density_jacobi_noalloc(const seqm_batch *bp, const double *F
   if (cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return SEQM_E_CUDA;
   k_jacobi<<<b.nmol, NT_J, smem, s>>>(b, F, P, evals, evecs, work, mol_row_off, active, status, max_sweeps,
-                                      nullptr);
+                                      nullptr, 0);
   return launch_check();
 }

@@ -61,6 +61,8 @@ class BatchSCF:
         self.status = torch.zeros(max(1, nm), dtype=torch.int32, device=dev)
         # 1 once the molecule's eigenvector rows in `work` are valid (warm-started Jacobi)
         self.warm = torch.zeros(max(1, nm), dtype=torch.uint8, device=dev)
+        # molecules starting cold or whose last solve took >= this many sweeps presweep in FP32 (0 = never)
+        self.mixed_threshold = 5
         self.sp2_work = None
         self.stream = stream
         self.launches = 0  # kernels of this library launched (for reporting)
@@ -116,7 +118,8 @@ class BatchSCF:
         native.check(self.lib.seqm_density_jacobi(L.struct, native.ptr(self.F), native.ptr(out),
                                                   native.ptr(self.evals), native.ptr(evecs), native.ptr(self.work),
                                                   native.ptr(L.dev["row_off"]), native.ptr(active),
-                                                  native.ptr(self.status), max_sweeps, native.ptr(self.warm), self._s()),
+                                                  native.ptr(self.status), max_sweeps, native.ptr(self.warm), self.mixed_threshold,
+                                                  self._s()),
                      "seqm_density_jacobi")
         if active is None:
             self.warm.fill_(1)

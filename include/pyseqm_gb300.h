@@ -96,7 +96,8 @@ int seqm_fock(const seqm_batch *b, const double *P, const double *H, const doubl
  * on entry) took >= mixed_threshold sweeps, first sweep in FP32 (A and the rotation product
  * in shared memory), then lift the vectors to FP64 (one Newton-Schulz re-orthonormalisation)
  * and finish with FP64 sweeps; 0 = FP64 sweeps only.  The result is FP64-accurate either way.
- * status[m]: sweeps taken (FP32 + FP64), or -1 if the FP64 sweep cap was hit. */
+ * status[m]: sweeps taken (FP32 + FP64), or -1 if the FP64 sweep cap was hit, or -2 for an
+ * active molecule with norb > 160, which is left untouched (give it to an SP2 entry point). */
 int seqm_density_jacobi(const seqm_batch *b, const double *F, double *P, double *evals, double *evecs,
                         double *work, const int64_t *mol_row_off, const uint8_t *active, int32_t *status,
                         int max_sweeps, const uint8_t *warm, int mixed_threshold, void *stream);
@@ -123,6 +124,19 @@ int seqm_density_jacobi_noalloc(const seqm_batch *b, const double *F, double *P,
  * SP2 step to test convergence. */
 int seqm_density_sp2(const seqm_batch *b, const double *F, double *P, double *work, double eps,
                      const uint8_t *active, int32_t *status, int max_iter, void *stream);
+
+/* SP2 with the squarings on the tensor cores (tcgen05, BF16 hi+lo split products, FP32
+ * accumulation in tensor memory), then mcweeny_steps FP64 McWeeny refinements
+ * X <- 3X^2 - 2X^3 of X = P/2.  Same purification and branch test as SP2.py:9-85 (the
+ * trace of X^2 for the test is ||X||_F^2 in FP64); a molecule stops when the trace error
+ * is below eps, or below 1e-2 and no longer improving (SP2.py:76-80).  No counterpart of
+ * the mixed-precision form in the reference.  work: SEQM_SP2_TC_WORK_BYTES(T, nmol) bytes
+ * with T = mat_off[nmol].  status[m] = SP2 steps, -1 at the step cap.  Synchronises the
+ * stream once per SP2 step. */
+#define SEQM_SP2_TC_WORK_BYTES(T, nmol) \
+  (24 * (size_t)(T) + 8 + 56 * (size_t)(nmol) + (((size_t)(nmol) + 15) & ~(size_t)15) + 8)
+int seqm_density_sp2_tc(const seqm_batch *b, const double *F, double *P, void *work, double eps,
+                        const uint8_t *active, int32_t *status, int max_iter, int mcweeny_steps, void *stream);
 
 /* One mixing step for active molecules.  Replaces the P update of scf_forward0 (linear,
  * scf_loop.py:258-267: P <- alpha P + (1-alpha) Pnew) and scf_forward1 (adaptive,

@@ -217,6 +217,10 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
   if (active && !active[m]) return;
   const int n = b.mol_norb[m];
   if (n <= 0) return;
+  if (n > JMAX_N) {  // larger bases go to the SP2 density step
+    if (threadIdx.x == 0 && status) status[m] = -2;
+    return;
+  }
   const int lda = n | 1;
   const size_t mo = b.mol_mat_off[m];
   const double *Fm = F + mo;
@@ -351,9 +355,9 @@ extern "C" int seqm_density_jacobi(const seqm_batch *bp, const double *F, double
   if ((warm || mixed_threshold > 0) && !P) return SEQM_E_ARG;  // P's block is used as product scratch
   seqm_batch b = *bp;
   if (b.nmol == 0) return SEQM_OK;
-  if (b.max_norb > JMAX_N) return SEQM_E_TOO_LARGE;
-  int lda = b.max_norb | 1;
-  size_t smem = (size_t)b.max_norb * lda * sizeof(double);
+  const int cap = b.max_norb > JMAX_N ? JMAX_N : b.max_norb;  // larger molecules are skipped (status -2)
+  int lda = cap | 1;
+  size_t smem = (size_t)cap * lda * sizeof(double);
   if (smem < 8) smem = 8;
   if (cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return SEQM_E_CUDA;

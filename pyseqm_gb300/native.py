@@ -27,7 +27,7 @@ NPAR = len(PAR_NAMES)
 PAR = {n: i for i, n in enumerate(PAR_NAMES)}
 
 EXPORTS = ["seqm_hcore", "seqm_fock", "seqm_density_jacobi", "seqm_density_jacobi_noalloc", "seqm_density_sp2",
-           "seqm_mix", "seqm_energy_error",
+           "seqm_density_sp2_tc", "seqm_mix", "seqm_energy_error",
            "seqm_initial_density", "seqm_pair_sum", "seqm_energy_grad", "seqm_version"]
 
 _P = ctypes.c_void_p
@@ -71,6 +71,7 @@ def load(path=None):
         "seqm_density_jacobi": [B, _P, _P, _P, _P, _P, _P, _P, _P, i32, _P, i32, _P],
         "seqm_density_jacobi_noalloc": [B, _P, _P, _P, _P, _P, _P, _P, i32, _P],
         "seqm_density_sp2": [B, _P, _P, _P, f64, _P, _P, i32, _P],
+        "seqm_density_sp2_tc": [B, _P, _P, _P, f64, _P, _P, i32, i32, _P],
         "seqm_mix": [B, _P, _P, _P, _P, _P, _P, i32, f64, _P, _P],
         "seqm_energy_error": [B, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, f64, _P],
         "seqm_initial_density": [B, _P, _P],

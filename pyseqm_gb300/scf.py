@@ -64,6 +64,14 @@ class BatchSCF:
         # molecules starting cold or whose last solve took >= this many sweeps presweep in FP32 (0 = never)
         self.mixed_threshold = 5
         self.sp2_work = None
+        self.sp2_tc_work = None
+        # molecules above the Jacobi limit take SP2: "tc" (tensor cores + FP64 McWeeny) or "fp64"
+        self.large_density = "tc"
+        self.mcweeny_steps = 2
+        self.large_mask = torch.as_tensor((layout.norb > JACOBI_MAX_N).astype(np.uint8), device=dev)
+        self.n_large = int((layout.norb > JACOBI_MAX_N).sum())
+        self.n_small = layout.nmol - self.n_large
+        self.small_mask = 1 - self.large_mask
         self.stream = stream
         self.launches = 0  # kernels of this library launched (for reporting)
         self.profile_density = False  # record CUDA events around every density launch
@@ -103,28 +111,59 @@ class BatchSCF:
             return
         self._density(out, sp2, active, evecs, max_sweeps)
 
-    def _density(self, out, sp2=(False,), active=None, evecs=None, max_sweeps=50):
+    def _sp2_fp64(self, out, eps, active):
         L = self.L
+        if self.sp2_work is None:
+            self.sp2_work = torch.empty(2 * int(L.mat_off[-1]) + 4 * L.nmol, dtype=torch.float64, device=L.device)
         self.launches += 1
-        if sp2[0] or L.max_norb > JACOBI_MAX_N:
-            if self.sp2_work is None:
-                self.sp2_work = torch.empty(2 * int(L.mat_off[-1]) + 4 * L.nmol, dtype=torch.float64,
-                                            device=L.device)
-            eps = float(sp2[1]) if sp2[0] else 1.0e-7
-            native.check(self.lib.seqm_density_sp2(L.struct, native.ptr(self.F), native.ptr(out),
-                                                   native.ptr(self.sp2_work), eps, native.ptr(active),
-                                                   native.ptr(self.status), 1000, self._s()), "seqm_density_sp2")
+        native.check(self.lib.seqm_density_sp2(L.struct, native.ptr(self.F), native.ptr(out), native.ptr(self.sp2_work),
+                                               eps, native.ptr(active), native.ptr(self.status), 1000, self._s()),
+                     "seqm_density_sp2")
+
+    def _sp2_tc(self, out, eps, active):
+        L = self.L
+        if self.sp2_tc_work is None:
+            T = int(L.mat_off[-1])
+            nbytes = 24 * T + 8 + 56 * L.nmol + ((L.nmol + 15) & ~15) + 8
+            self.sp2_tc_work = torch.empty(nbytes, dtype=torch.uint8, device=L.device)
+        self.launches += 1
+        native.check(self.lib.seqm_density_sp2_tc(L.struct, native.ptr(self.F), native.ptr(out),
+                                                  native.ptr(self.sp2_tc_work), eps, native.ptr(active),
+                                                  native.ptr(self.status), 1000, self.mcweeny_steps, self._s()),
+                     "seqm_density_sp2_tc")
+
+    def _density(self, out, sp2=(False,), active=None, evecs=None, max_sweeps=50):
+        """Density step.  sp2[0] set: the reference's SP2 option for every molecule (plain FP64
+        SP2, or tensor-core SP2 + FP64 McWeeny when sp2[2] == "tc").  Otherwise the Jacobi
+        eigensolver for norb <= 160 and, for larger molecules, the SP2 form chosen by
+        ``large_density`` ("tc" by default, "fp64")."""
+        L = self.L
+        if sp2[0]:
+            if len(sp2) > 2 and sp2[2] == "tc":
+                self._sp2_tc(out, float(sp2[1]), active)
+            else:
+                self._sp2_fp64(out, float(sp2[1]), active)
             return
+        if self.n_large:
+            act = self.large_mask if active is None else active & self.large_mask
+            if self.large_density == "tc":
+                self._sp2_tc(out, 1.0e-7, act)
+            else:
+                self._sp2_fp64(out, 1.0e-7, act)
+            if not self.n_small:
+                return
+        act_s = active if not self.n_large else (self.small_mask if active is None else active & self.small_mask)
+        self.launches += 1
         native.check(self.lib.seqm_density_jacobi(L.struct, native.ptr(self.F), native.ptr(out),
                                                   native.ptr(self.evals), native.ptr(evecs), native.ptr(self.work),
-                                                  native.ptr(L.dev["row_off"]), native.ptr(active),
+                                                  native.ptr(L.dev["row_off"]), native.ptr(act_s),
                                                   native.ptr(self.status), max_sweeps, native.ptr(self.warm), self.mixed_threshold,
                                                   self._s()),
                      "seqm_density_jacobi")
-        if active is None:
+        if act_s is None:
             self.warm.fill_(1)
         else:
-            self.warm.bitwise_or_(active)
+            self.warm.bitwise_or_(act_s)
 
     def energy_error(self, eps, first=False):
         self.launches += 1
@@ -184,7 +223,7 @@ class BatchSCF:
         """Fock matrix of the converged density, orbital energies / vectors, energies."""
         self.fock()
         evecs = torch.empty_like(self.work) if want_vectors else None
-        self.density(self.Pnew, (False,), active=None, evecs=evecs)
+        self.density(self.Pnew, (False,), active=None if not self.n_large else self.small_mask, evecs=evecs)
         self.energy_error(0.0, first=True)
         self.evecs = evecs
         return self.Eout[: self.L.nmol].clone(), self.Enuc[: self.L.nmol].clone()

@@ -1,0 +1,65 @@
+"""Tensor-core (tcgen05, BF16 hi+lo) SP2 with FP64 McWeeny refinement, and the Jacobi / SP2
+dispatch for molecules above the Jacobi limit.  Mixed-precision form: |dE| <= 1e-4 eV per
+molecule against the FP64 oracle, idempotency of P/2 to FP64 level."""
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import load_golden
+from oracle import seqm_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL_E_MIXED = 1e-4  # eV, the mixed-precision form's energy tolerance
+TOL_P_MIXED = 1e-4  # density max-abs
+SCF_EPS_MIXED = 1e-5  # SCF threshold of the mixed-precision (serving) form
+
+
+def _solve(species, coords, method, eps, sp2=(False,), large="tc"):
+    from pyseqm_gb300.layout import Layout
+    from pyseqm_gb300.scf import BatchSCF
+
+    L = Layout.from_padded(species, coords, method).to_device("cuda")
+    s = BatchSCF(L)
+    s.large_density = large
+    s.hcore()
+    nc = s.scf(eps, (1,), sp2)
+    E, En = s.final(want_vectors=False)
+    return L, s, (E + En).cpu().numpy(), nc
+
+
+def _idempotency(L, P, m):
+    X = 0.5 * L.block(P, m)
+    return float((X @ X - X).abs().max())
+
+
+def test_tc_sp2_matches_reference_sp2_option():
+    """sp2 = [True, eps, "tc"] on the golden mixed AM1 batch (the reference ran SP2 there)."""
+    g = load_golden("mixed_am1_sp2")
+    # the mixed-precision density carries ~1e-7 noise: SCF to the serving threshold 1e-5
+    L, s, E, nc = _solve(g["species_np"], g["coords_np"], "AM1", SCF_EPS_MIXED, (True, 1e-7, "tc"))
+    assert not nc.any()
+    np.testing.assert_allclose(E, g["ref"]["Etot"], atol=TOL_E_MIXED, rtol=0)
+    for m in range(L.nmol):
+        np.testing.assert_allclose(L.block(s.P, m).cpu().numpy(), np.asarray(g["ref"]["P"][m]), atol=TOL_P_MIXED)
+        assert _idempotency(L, s.P, m) < 1e-9
+
+
+@pytest.mark.parametrize("large", ["tc", "fp64"])
+def test_large_molecules_take_sp2_and_match_oracle(large):
+    """Molecules above 160 AOs (water 30 = 180 AOs, C30 alkane = 182 AOs) next to small ones."""
+    from pyseqm_gb300 import workloads
+
+    rng = np.random.default_rng(21)
+    mols = [workloads.water_cluster(30, rng), workloads.alkane(4, rng, 0.03), workloads.alkane(30, rng, 0.03),
+            workloads.water_cluster(5, rng)]
+    species, coords = workloads.pad_batch(mols)
+    L, s, E, nc = _solve(species, coords, "PM3", SCF_EPS_MIXED if large == "tc" else 1e-8, large=large)
+    assert not nc.any()
+    ref = O.single_point("PM3", species, coords, 1e-8, (1,))
+    tol = TOL_E_MIXED if large == "tc" else 1e-6
+    np.testing.assert_allclose(E, ref["Etot"], atol=tol, rtol=0)
+    for m in (0, 2):
+        assert int(L.norb[m]) > 160
+        assert _idempotency(L, s.P, m) < 1e-9

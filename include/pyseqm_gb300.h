@@ -119,22 +119,25 @@ int seqm_density_jacobi_noalloc(const seqm_batch *b, const double *F, double *P,
 
 /* SP2 purification (FP64), replaces SP2(a, nocc, eps) (seqm/seqm_functions/SP2.py:9-85)
  * applied per molecule to its packed Fock matrix (eps clamped to [1e-7, 1e-3] as there).
- * work: scratch of 2*mat_off[nmol] + 4*nmol doubles.  P = 2 X at convergence.
- * status[m]: SP2 steps taken, or -1 if max_iter was hit.  Synchronises the stream once per
- * SP2 step to test convergence. */
+ * work: SEQM_SP2_WORK_DOUBLES(T, nmol, max_norb) doubles with T = mat_off[nmol].
+ * P = 2 X at convergence.  status[m]: SP2 steps taken, or -1 if max_iter was hit.
+ * Synchronises the stream once per SP2 step to test convergence. */
+#define SEQM_SP2_STATE 11
+#define SEQM_SP2_WORK_DOUBLES(T, nmol, maxn) \
+  (2 * (size_t)(T) + (SEQM_SP2_STATE + 2 * (size_t)(maxn)) * (size_t)(nmol) + 1)
 int seqm_density_sp2(const seqm_batch *b, const double *F, double *P, double *work, double eps,
                      const uint8_t *active, int32_t *status, int max_iter, void *stream);
 
-/* SP2 with the squarings on the tensor cores (tcgen05, BF16 hi+lo split products, FP32
+/* SP2 with the squarings on the tensor cores (tcgen05, FP16 hi+lo split products, FP32
  * accumulation in tensor memory), then mcweeny_steps FP64 McWeeny refinements
  * X <- 3X^2 - 2X^3 of X = P/2.  Same purification and branch test as SP2.py:9-85 (the
  * trace of X^2 for the test is ||X||_F^2 in FP64); a molecule stops when the trace error
  * is below eps, or below 1e-2 and no longer improving (SP2.py:76-80).  No counterpart of
- * the mixed-precision form in the reference.  work: SEQM_SP2_TC_WORK_BYTES(T, nmol) bytes
- * with T = mat_off[nmol].  status[m] = SP2 steps, -1 at the step cap.  Synchronises the
+ * the mixed-precision form in the reference.  work: SEQM_SP2_TC_WORK_BYTES(T, nmol, max_norb)
+ * bytes with T = mat_off[nmol].  status[m] = SP2 steps, -1 at the step cap.  Synchronises the
  * stream once per SP2 step. */
-#define SEQM_SP2_TC_WORK_BYTES(T, nmol) \
-  (24 * (size_t)(T) + 8 + 56 * (size_t)(nmol) + (((size_t)(nmol) + 15) & ~(size_t)15) + 8)
+#define SEQM_SP2_TC_WORK_BYTES(T, nmol, maxn) \
+  (24 * (size_t)(T) + 16 + 8 * (SEQM_SP2_STATE + 2 * (size_t)(maxn)) * (size_t)(nmol))
 int seqm_density_sp2_tc(const seqm_batch *b, const double *F, double *P, void *work, double eps,
                         const uint8_t *active, int32_t *status, int max_iter, int mcweeny_steps, void *stream);
 

@@ -1,0 +1,291 @@
+// Shared SP2 machinery (plain FP64 and tensor-core forms): multi-CTA elementwise passes
+// over (chunk, molecule) grids with per-molecule FP64 accumulators, so a large
+// molecule's n^2 elements are spread over the whole GPU, and the FP64 symmetric
+// tile product used for FP64 squarings and McWeeny refinement.
+//
+// Per-molecule state (doubles, SP2_NS per molecule):
+//   err0, err1 (trace errors of the last two steps), err2, running flag, steps,
+//   t1 = tr X, t2 = ||X||_F^2 = tr X^2 (X symmetric), accumulators for the new X,
+//   Gershgorin bounds h1, hN.
+#pragma once
+
+#include <math.h>
+
+#include "common.cuh"
+
+namespace seqm {
+namespace {  // internal linkage: this header is compiled into more than one translation unit
+
+enum { S_ERR0 = 0, S_ERR1, S_ERR2, S_RUN, S_STEPS, S_T1, S_T2, S_ACC_T, S_ACC_F, S_H1, S_HN, SP2_NS };
+constexpr int EW_THREADS = 256;
+constexpr int EW_CHUNK = EW_THREADS * 8;  // elements per CTA of an elementwise pass
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// add per-CTA partial sums of (a, b) into acc[0], acc[1]
+__device__ __forceinline__ void cta_accumulate2(double a, double b, double *acc) {
+  __shared__ double ra[EW_THREADS / 32], rb[EW_THREADS / 32];
+  a = warp_sum(a);
+  b = warp_sum(b);
+  if ((threadIdx.x & 31) == 0) { ra[threadIdx.x >> 5] = a; rb[threadIdx.x >> 5] = b; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sa = 0.0, sb = 0.0;
+    for (int w = 0; w < EW_THREADS / 32; ++w) { sa += ra[w]; sb += rb[w]; }
+    if (sa != 0.0) atomicAdd(acc, sa);
+    if (sb != 0.0) atomicAdd(acc + 1, sb);
+  }
+}
+
+// Gershgorin row bounds of F, one warp per row: lo[i] = a_ii - r_i, hi[i] = a_ii + r_i
+__global__ void k_sp2_rows(seqm_batch b, const double *__restrict__ F, double *__restrict__ rowlo,
+                           double *__restrict__ rowhi, const uint8_t *__restrict__ active) {
+  const int m = blockIdx.y;
+  if (active && !active[m]) return;
+  const int n = b.mol_norb[m];
+  const int row = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const double *Fr = F + b.mol_mat_off[m] + (size_t)row * n;
+  double s = 0.0;
+  for (int j = lane; j < n; j += 32) s += fabs(Fr[j]);
+  s = warp_sum(s);
+  if (lane == 0) {
+    const double aii = Fr[row], ri = s - fabs(aii);
+    rowlo[(size_t)m * b.max_norb + row] = aii - ri;
+    rowhi[(size_t)m * b.max_norb + row] = aii + ri;
+  }
+}
+
+// per molecule: h1 = min lo, hN = max hi; clear the accumulators
+__global__ void k_sp2_bounds(seqm_batch b, const double *__restrict__ rowlo, const double *__restrict__ rowhi,
+                             double *__restrict__ st, const uint8_t *__restrict__ active) {
+  const int m = blockIdx.x;
+  double *s = st + SP2_NS * m;
+  if (active && !active[m]) {
+    if (threadIdx.x == 0) s[S_RUN] = 0.0;
+    return;
+  }
+  const int n = b.mol_norb[m];
+  double lo = INFINITY, hi = -INFINITY;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    lo = fmin(lo, rowlo[(size_t)m * b.max_norb + i]);
+    hi = fmax(hi, rowhi[(size_t)m * b.max_norb + i]);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  __shared__ double rl[32], rh[32];
+  if ((threadIdx.x & 31) == 0) { rl[threadIdx.x >> 5] = lo; rh[threadIdx.x >> 5] = hi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x / 32); ++w) { lo = fmin(lo, rl[w]); hi = fmax(hi, rh[w]); }
+    lo = fmin(lo, rl[0]);
+    hi = fmax(hi, rh[0]);
+    s[S_H1] = lo; s[S_HN] = hi; s[S_ACC_T] = 0.0; s[S_ACC_F] = 0.0; s[S_RUN] = 1.0; s[S_STEPS] = 0.0;
+  }
+}
+
+// X0 = (hN I - F)/(hN - h1) (SP2.py:36-43), accumulating tr X0 and ||X0||^2
+template <class T>
+__global__ void __launch_bounds__(EW_THREADS) k_sp2_scale(seqm_batch b, const double *__restrict__ F,
+                                                          T *__restrict__ X, double *__restrict__ st) {
+  const int m = blockIdx.y;
+  double *s = st + SP2_NS * m;
+  if (s[S_RUN] == 0.0) return;
+  const int n = b.mol_norb[m];
+  const size_t nn = (size_t)n * n, base = (size_t)blockIdx.x * EW_CHUNK;
+  if (base >= nn) return;
+  const double h1 = s[S_H1], hN = s[S_HN];
+  const size_t mo = b.mol_mat_off[m];
+  double tr = 0.0, f2 = 0.0;
+  for (size_t idx = base + threadIdx.x; idx < nn && idx < base + EW_CHUNK; idx += EW_THREADS) {
+    const size_t i = idx / n;
+    const bool d = idx == i * n + i;
+    const T v = (T)(((d ? hN : 0.0) - F[mo + idx]) / (hN - h1));
+    X[mo + idx] = v;
+    if (d) tr += (double)v;
+    f2 += (double)v * (double)v;
+  }
+  cta_accumulate2(tr, f2, s + S_ACC_T);
+}
+
+// after the X0 pass: t1, t2 and the initial trace error
+__global__ void k_sp2_start(seqm_batch b, double *__restrict__ st) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= b.nmol) return;
+  double *s = st + SP2_NS * m;
+  if (s[S_RUN] == 0.0) return;
+  s[S_T1] = s[S_ACC_T];
+  s[S_T2] = s[S_ACC_F];
+  const double e = fabs(s[S_T1] - (double)b.mol_nocc[m]);
+  s[S_ERR0] = e; s[S_ERR1] = e; s[S_ERR2] = e;
+  s[S_ACC_T] = 0.0; s[S_ACC_F] = 0.0;
+}
+
+// keep X^2 or 2X - X^2 by the trace test (SP2.py:58-64), with tr X^2 = ||X||_F^2
+template <class T>
+__global__ void __launch_bounds__(EW_THREADS) k_sp2_step(seqm_batch b, T *__restrict__ X, const T *__restrict__ X2,
+                                                         double *__restrict__ st) {
+  const int m = blockIdx.y;
+  double *s = st + SP2_NS * m;
+  if (s[S_RUN] == 0.0) return;
+  const int n = b.mol_norb[m];
+  const size_t nn = (size_t)n * n, base = (size_t)blockIdx.x * EW_CHUNK;
+  if (base >= nn) return;
+  const double nocc = (double)b.mol_nocc[m], t1 = s[S_T1], t2 = s[S_T2];
+  const bool sq = fabs(t2 - nocc) < fabs(2.0 * t1 - t2 - nocc);
+  const size_t mo = b.mol_mat_off[m];
+  double tr = 0.0, f2 = 0.0;
+  for (size_t idx = base + threadIdx.x; idx < nn && idx < base + EW_CHUNK; idx += EW_THREADS) {
+    const T x = X[mo + idx], y = X2[mo + idx];
+    const T v = sq ? y : (T)2 * x - y;
+    X[mo + idx] = v;
+    const size_t i = idx / n;
+    if (idx == i * n + i) tr += (double)v;
+    f2 += (double)v * (double)v;
+  }
+  cta_accumulate2(tr, f2, s + S_ACC_T);
+}
+
+// per molecule after a step: errors, convergence, next t1/t2; counts still-running molecules.
+// relaxed: also stop when the error is below 1e-2 and no longer improving (SP2.py:76-80,
+// the reference's rule for reduced precision)
+__global__ void k_sp2_check(seqm_batch b, double *__restrict__ st, double eps, int relaxed, int *__restrict__ nrun) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= b.nmol) return;
+  double *s = st + SP2_NS * m;
+  if (s[S_RUN] == 0.0) return;
+  const double e0 = fabs(s[S_ACC_T] - (double)b.mol_nocc[m]);
+  const double e1 = s[S_ERR0], e2 = s[S_ERR1];
+  s[S_ERR2] = e2; s[S_ERR1] = e1; s[S_ERR0] = e0;
+  s[S_STEPS] += 1.0;
+  s[S_T1] = s[S_ACC_T];
+  s[S_T2] = s[S_ACC_F];
+  s[S_ACC_T] = 0.0;
+  s[S_ACC_F] = 0.0;
+  const bool done = (e0 < eps && e1 < eps) || (relaxed && e0 < 1.0e-2 && e0 >= e2);
+  if (done) s[S_RUN] = 0.0;
+  else atomicAdd(nrun, 1);
+}
+
+// status[m] = steps, or -1 if still running at the cap
+__global__ void k_sp2_status(int nmol, const double *__restrict__ st, const uint8_t *__restrict__ active,
+                             int32_t *__restrict__ status) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nmol || (active && !active[m])) return;
+  const double *s = st + SP2_NS * m;
+  status[m] = s[S_RUN] != 0.0 ? -1 : (int)s[S_STEPS];
+}
+
+// elementwise P = c1 * A + c2 * A^T (FP64 out) for active molecules (A in T precision)
+template <class T>
+__global__ void __launch_bounds__(EW_THREADS) k_ew_sym(seqm_batch b, const T *__restrict__ A, double c1, double c2,
+                                                       double *__restrict__ P, const uint8_t *__restrict__ active) {
+  const int m = blockIdx.y;
+  if (active && !active[m]) return;
+  const int n = b.mol_norb[m];
+  const size_t nn = (size_t)n * n, base = (size_t)blockIdx.x * EW_CHUNK;
+  if (base >= nn) return;
+  const size_t mo = b.mol_mat_off[m];
+  for (size_t idx = base + threadIdx.x; idx < nn && idx < base + EW_CHUNK; idx += EW_THREADS) {
+    const size_t i = idx / n, j = idx - i * n;
+    P[mo + idx] = c1 * (double)A[mo + idx] + c2 * (double)A[mo + j * n + i];
+  }
+}
+
+// elementwise D = a * A + c * C (FP64) for active molecules
+__global__ void __launch_bounds__(EW_THREADS) k_ew_axpby(seqm_batch b, double a, const double *__restrict__ A, double c,
+                                                         const double *__restrict__ C, double *__restrict__ D,
+                                                         const uint8_t *__restrict__ active) {
+  const int m = blockIdx.y;
+  if (active && !active[m]) return;
+  const int n = b.mol_norb[m];
+  const size_t nn = (size_t)n * n, base = (size_t)blockIdx.x * EW_CHUNK;
+  if (base >= nn) return;
+  const size_t mo = b.mol_mat_off[m];
+  for (size_t idx = base + threadIdx.x; idx < nn && idx < base + EW_CHUNK; idx += EW_THREADS)
+    D[mo + idx] = a * A[mo + idx] + (C ? c * C[mo + idx] : 0.0);
+}
+
+// FP64 C = A B for symmetric products (upper 64x64 tiles, mirrored), molecules with run flag / active
+constexpr int MW_T = 64, MW_K = 16;
+__global__ void __launch_bounds__(256) k_sym_gemm64(seqm_batch b, const double *__restrict__ Am,
+                                                    const double *__restrict__ Bm, double *__restrict__ Cm,
+                                                    const uint8_t *__restrict__ active,
+                                                    const double *__restrict__ st) {
+  const int m = blockIdx.z;
+  if (active && !active[m]) return;
+  if (st && st[SP2_NS * m + S_RUN] == 0.0) return;
+  const int n = b.mol_norb[m];
+  const int i0 = blockIdx.y * MW_T, j0 = blockIdx.x * MW_T;
+  if (i0 >= n || j0 >= n || blockIdx.y > blockIdx.x) return;
+  const size_t mo = b.mol_mat_off[m];
+  const double *A = Am + mo, *B = Bm + mo;
+  __shared__ double As[MW_K][MW_T + 1], Bs[MW_K][MW_T + 1];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  double acc[4][4] = {};
+  for (int k0 = 0; k0 < n; k0 += MW_K) {
+    for (int e = threadIdx.x; e < MW_K * MW_T; e += 256) {
+      const int kk = e / MW_T, ii = e - kk * MW_T;
+      As[kk][ii] = (i0 + ii < n && k0 + kk < n) ? A[(size_t)(i0 + ii) * n + k0 + kk] : 0.0;
+      Bs[kk][ii] = (k0 + kk < n && j0 + ii < n) ? B[(size_t)(k0 + kk) * n + j0 + ii] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < MW_K; ++kk) {
+      double a[4], c[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) a[r] = As[kk][ty * 4 + r];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) c[q] = Bs[kk][tx * 4 + q];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[r][q] += a[r] * c[q];
+    }
+    __syncthreads();
+  }
+  double *C = Cm + mo;
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int row = i0 + ty * 4 + r, col = j0 + tx * 4 + q;
+      if (row < n && col < n) {
+        C[(size_t)row * n + col] = acc[r][q];
+        C[(size_t)col * n + row] = acc[r][q];
+      }
+    }
+}
+
+// grid helpers
+inline dim3 ew_grid(const seqm_batch &b) {
+  const size_t nn = (size_t)b.max_norb * b.max_norb;
+  return dim3((unsigned)((nn + EW_CHUNK - 1) / EW_CHUNK), (unsigned)b.nmol);
+}
+inline dim3 rows_grid(const seqm_batch &b) { return dim3((unsigned)((b.max_norb + 7) / 8), (unsigned)b.nmol); }
+inline dim3 gemm64_grid(const seqm_batch &b) {
+  const unsigned t = (unsigned)((b.max_norb + MW_T - 1) / MW_T);
+  return dim3(t, t, (unsigned)b.nmol);
+}
+
+// McWeeny refinement of the density P (FP64): X = P/2, P <- 2 (3 X^2 - 2 X^3), `steps` times.
+// Y, Z: FP64 scratch of the batch's matrix size
+inline void mcweeny(const seqm_batch &b, double *P, double *Y, double *Z, const uint8_t *active, int steps,
+                    cudaStream_t s) {
+  for (int k = 0; k < steps; ++k) {
+    k_ew_axpby<<<ew_grid(b), EW_THREADS, 0, s>>>(b, 0.5, P, 0.0, nullptr, Z, active);  // Z = X
+    k_sym_gemm64<<<gemm64_grid(b), 256, 0, s>>>(b, Z, Z, Y, active, nullptr);            // Y = X^2
+    k_sym_gemm64<<<gemm64_grid(b), 256, 0, s>>>(b, Y, Z, P, active, nullptr);            // P = X^3
+    k_ew_axpby<<<ew_grid(b), EW_THREADS, 0, s>>>(b, 6.0, Y, -4.0, P, P, active);         // P = 2(3X^2 - 2X^3)
+  }
+}
+
+}  // namespace
+}  // namespace seqm

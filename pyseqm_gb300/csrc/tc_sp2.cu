@@ -23,6 +23,7 @@
 #include <math.h>
 
 #include "common.cuh"
+#include "sp2_common.cuh"
 
 namespace seqm {
 
@@ -143,10 +144,10 @@ __device__ __forceinline__ void stage_split(const float *__restrict__ X, int n, 
 // X2 = X X (split FP16, FP32 accumulate) for the molecules with run[m] != 0
 __global__ void __launch_bounds__(TC_THREADS) k_tc_square(seqm_batch b, const float *__restrict__ X,
                                                           float *__restrict__ X2, const int64_t *__restrict__ off,
-                                                          const uint8_t *__restrict__ run, double *__restrict__ trace,
+                                                          const double *__restrict__ st, double *__restrict__ trace,
                                                           int *__restrict__ err) {
   const int m = blockIdx.z;
-  if (!run[m]) return;
+  if (st[SP2_NS * m + S_RUN] == 0.0) return;
   const int n = b.mol_norb[m];
   const int tm = blockIdx.y, tn = blockIdx.x;
   if (tm > tn || tm * TC_M >= n || tn * TC_N >= n) return;
@@ -216,7 +217,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_square(seqm_batch b, const fl
         }
       }
     }
-    if (tm == tn) {
+    if (tm == tn && trace) {
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
       if (lane == 0) atomicAdd(&trace[m], tr);
@@ -229,197 +230,6 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_square(seqm_batch b, const fl
   if (warp == 0) tmem_dealloc(tmem_d, TC_N);
 }
 
-// ------------------------------------------------------------------ SP2 driver kernels
-// state per molecule (doubles): [0] err0, [1] err1, [2] running, [3] steps, [4] tr(X), [5] tr(X2)
-constexpr int SST = 6;
-constexpr int NT_U = 256;
-
-__device__ double tc_block_sum(double v, double *red) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  double s = 0.0;
-  for (int w = 0; w < NT_U / 32; ++w) s += red[w];
-  __syncthreads();
-  return s;
-}
-
-// X0 = (hN I - F)/(hN - h1) in FP32 (Gershgorin bounds in FP64), trace bookkeeping
-__global__ void __launch_bounds__(NT_U) k_tc_init(seqm_batch b, const double *__restrict__ F, float *__restrict__ X,
-                                                  const int64_t *__restrict__ off, double *__restrict__ st,
-                                                  uint8_t *__restrict__ run, const uint8_t *__restrict__ active) {
-  __shared__ double red[NT_U / 32];
-  const int m = blockIdx.x;
-  double *s = st + SST * m;
-  if (active && !active[m]) {
-    if (threadIdx.x == 0) run[m] = 0;
-    return;
-  }
-  const int n = b.mol_norb[m];
-  const double *Fm = F + b.mol_mat_off[m];
-  double lo = INFINITY, hi = -INFINITY;
-  for (int i = threadIdx.x; i < n; i += NT_U) {
-    double rs = 0.0;
-    for (int j = 0; j < n; ++j) rs += fabs(Fm[(size_t)i * n + j]);
-    const double aii = Fm[(size_t)i * n + i], ri = rs - fabs(aii);
-    lo = fmin(lo, aii - ri);
-    hi = fmax(hi, aii + ri);
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-  }
-  __shared__ double rlo[NT_U / 32], rhi[NT_U / 32];
-  if ((threadIdx.x & 31) == 0) { rlo[threadIdx.x >> 5] = lo; rhi[threadIdx.x >> 5] = hi; }
-  __syncthreads();
-  double h1 = rlo[0], hN = rhi[0];
-  for (int w = 1; w < NT_U / 32; ++w) { h1 = fmin(h1, rlo[w]); hN = fmax(hN, rhi[w]); }
-  float *Xm = X + off[m];
-  double tr = 0.0;
-  for (size_t idx = threadIdx.x; idx < (size_t)n * n; idx += NT_U) {
-    const size_t i = idx / n, j = idx - i * n;
-    const double v = ((i == j ? hN : 0.0) - Fm[idx]) / (hN - h1);
-    Xm[idx] = (float)v;
-    if (i == j) tr += v;
-  }
-  tr = tc_block_sum(tr, red);
-  if (threadIdx.x == 0) {
-    const double e = fabs(tr - (double)b.mol_nocc[m]);
-    s[0] = e; s[1] = e; s[2] = 1.0; s[3] = 0.0; s[4] = tr; s[5] = 0.0;
-    run[m] = 1;
-  }
-}
-
-// keep X^2 or 2X - X^2 (trace test of SP2.py:58-64), update errors and the running flag.
-// The tensor-core FP32 accumulation is biased on the diagonal, so the branch test uses
-// the exact tr(X^2) = ||X||_F^2 of the stored (symmetric) X, summed in FP64.  Stop when
-// the trace error is below eps, or below 1e-2 and no longer improving (the reference's
-// reduced-precision rule, SP2.py:76-80); the FP64 McWeeny steps finish the job.
-__global__ void __launch_bounds__(NT_U) k_tc_update(seqm_batch b, float *__restrict__ X, const float *__restrict__ X2,
-                                                    const int64_t *__restrict__ off, double *__restrict__ st,
-                                                    uint8_t *__restrict__ run, double *__restrict__ trace2, double eps,
-                                                    int *__restrict__ nrun) {
-  __shared__ double red[NT_U / 32];
-  const int m = blockIdx.x;
-  if (!run[m]) return;
-  double *s = st + SST * m;
-  const int n = b.mol_norb[m];
-  const double nocc = (double)b.mol_nocc[m];
-  float *Xm = X + off[m];
-  const float *Ym = X2 + off[m];
-  double f2 = 0.0;
-  for (size_t idx = threadIdx.x; idx < (size_t)n * n; idx += NT_U) f2 += (double)Xm[idx] * (double)Xm[idx];
-  const double t1 = s[4], t2 = tc_block_sum(f2, red);
-  const bool sq = fabs(t2 - nocc) < fabs(2.0 * t1 - t2 - nocc);
-  double tr = 0.0;
-  for (size_t idx = threadIdx.x; idx < (size_t)n * n; idx += NT_U) {
-    const float v = sq ? Ym[idx] : 2.0f * Xm[idx] - Ym[idx];
-    Xm[idx] = v;
-    const size_t i = idx / n;
-    if (idx == i * n + i) tr += (double)v;
-  }
-  tr = tc_block_sum(tr, red);
-  if (threadIdx.x == 0) {
-    const double e0 = fabs(tr - nocc), e1 = s[0], e2 = s[1];
-    s[1] = e1; s[0] = e0; s[3] += 1.0; s[4] = tr; s[5] = t2;
-    trace2[m] = 0.0;
-    if ((e0 < eps && e1 < eps) || (e0 < 1.0e-2 && e0 >= e2)) run[m] = 0;
-    else atomicAdd(nrun, 1);
-  }
-}
-
-// P = 2 X (FP64, symmetrised) for the molecules that ran
-__global__ void k_tc_finish(seqm_batch b, const float *__restrict__ X, const int64_t *__restrict__ off,
-                            double *__restrict__ P, const uint8_t *__restrict__ active) {
-  const int m = blockIdx.x;
-  if (active && !active[m]) return;
-  const int n = b.mol_norb[m];
-  const float *Xm = X + off[m];
-  double *Pm = P + b.mol_mat_off[m];
-  for (size_t idx = threadIdx.x; idx < (size_t)n * n; idx += blockDim.x) {
-    const size_t i = idx / n, j = idx - i * n;
-    Pm[idx] = (double)Xm[i * n + j] + (double)Xm[j * n + i];
-  }
-}
-
-// FP64 products for McWeeny: C = A B (n x n), 64x64 tiles, 4x4 per thread
-constexpr int MW_T = 64, MW_K = 16;
-__global__ void __launch_bounds__(256) k_mw_gemm(seqm_batch b, const double *__restrict__ Am,
-                                                 const double *__restrict__ Bm, double *__restrict__ Cm,
-                                                 const uint8_t *__restrict__ active) {
-  const int m = blockIdx.z;
-  if (active && !active[m]) return;
-  const int n = b.mol_norb[m];
-  const int i0 = blockIdx.y * MW_T, j0 = blockIdx.x * MW_T;
-  if (i0 >= n || j0 >= n || blockIdx.y > blockIdx.x) return;  // upper tiles; C is symmetric
-  const size_t mo = b.mol_mat_off[m];
-  const double *A = Am + mo, *B = Bm + mo;
-  __shared__ double As[MW_K][MW_T + 1], Bs[MW_K][MW_T + 1];
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  double acc[4][4] = {};
-  for (int k0 = 0; k0 < n; k0 += MW_K) {
-    for (int e = threadIdx.x; e < MW_K * MW_T; e += 256) {
-      const int kk = e / MW_T, ii = e - kk * MW_T;
-      As[kk][ii] = (i0 + ii < n && k0 + kk < n) ? A[(size_t)(i0 + ii) * n + k0 + kk] : 0.0;
-      Bs[kk][ii] = (k0 + kk < n && j0 + ii < n) ? B[(size_t)(k0 + kk) * n + j0 + ii] : 0.0;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < MW_K; ++kk) {
-      double a[4], c[4];
-#pragma unroll
-      for (int r = 0; r < 4; ++r) a[r] = As[kk][ty * 4 + r];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) c[q] = Bs[kk][tx * 4 + q];
-#pragma unroll
-      for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) acc[r][q] += a[r] * c[q];
-    }
-    __syncthreads();
-  }
-  double *C = Cm + mo;
-#pragma unroll
-  for (int r = 0; r < 4; ++r)
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int row = i0 + ty * 4 + r, col = j0 + tx * 4 + q;
-      if (row < n && col < n) {
-        C[(size_t)row * n + col] = acc[r][q];
-        C[(size_t)col * n + row] = acc[r][q];
-      }
-    }
-}
-
-// X = P/2; P <- 2 (3 X^2 - 2 X^3) given X2 = X^2 and X3 = X^2 X (all FP64, per molecule)
-__global__ void k_mw_combine(seqm_batch b, double *__restrict__ P, const double *__restrict__ X2,
-                             const double *__restrict__ X3, const uint8_t *__restrict__ active) {
-  const int m = blockIdx.x;
-  if (active && !active[m]) return;
-  const int n = b.mol_norb[m];
-  const size_t mo = b.mol_mat_off[m];
-  for (size_t idx = threadIdx.x; idx < (size_t)n * n; idx += blockDim.x)
-    P[mo + idx] = 2.0 * (3.0 * X2[mo + idx] - 2.0 * X3[mo + idx]);
-}
-
-// status[m] = SP2 steps taken, or -1 if the molecule was still running at the step cap
-__global__ void k_tc_status(int nmol, const double *__restrict__ st, const uint8_t *__restrict__ run,
-                            const uint8_t *__restrict__ active, int32_t *__restrict__ status) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= nmol || (active && !active[m])) return;
-  status[m] = run[m] ? -1 : (int)st[SST * m + 3];
-}
-
-__global__ void k_half(seqm_batch b, const double *__restrict__ P, double *__restrict__ X,
-                       const uint8_t *__restrict__ active) {
-  const int m = blockIdx.x;
-  if (active && !active[m]) return;
-  const int n = b.mol_norb[m];
-  const size_t mo = b.mol_mat_off[m];
-  for (size_t idx = threadIdx.x; idx < (size_t)n * n; idx += blockDim.x) X[mo + idx] = 0.5 * P[mo + idx];
-}
 
 }  // namespace seqm
 
@@ -437,32 +247,32 @@ extern "C" int seqm_density_sp2_tc(const seqm_batch *bp, const double *F, double
   if (cudaMemcpyAsync(&total, b.mol_mat_off + b.nmol, sizeof(int64_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)
     return SEQM_E_CUDA;
-  // work layout: X f32 [total] | X2 f32 [total] | Y f64 [total] | Z f64 [total] | state f64 [6 nmol] |
-  //              trace2 f64 [nmol] | run u8 [nmol] | counters i32 [2]
-  uint8_t *w = static_cast<uint8_t *>(work);
-  float *X = reinterpret_cast<float *>(w);
+  // work: X f32 [T] | X2 f32 [T] | (pad) | Y f64 [T] | Z f64 [T] | state [SP2_NS nmol] |
+  //       row bounds 2 [nmol max_norb] | counters i32 [2]   (FP32 blocks share the FP64 offsets)
+  float *X = static_cast<float *>(work);
   float *X2 = X + total;
   double *Y = reinterpret_cast<double *>(X2 + total + (total & 1));
   double *Z = Y + total;
   double *st = Z + total;
-  double *tr2 = st + (size_t)SST * b.nmol;
-  uint8_t *run = reinterpret_cast<uint8_t *>(tr2 + b.nmol);
-  int *cnt = reinterpret_cast<int *>(run + ((b.nmol + 15) & ~15));
-  // FP32 matrices share the FP64 offsets (same element counts)
-  const int64_t *off = b.mol_mat_off;
-  if (cudaMemsetAsync(tr2, 0, sizeof(double) * b.nmol, s) != cudaSuccess) return SEQM_E_CUDA;
+  double *rowlo = st + (size_t)SP2_NS * b.nmol;
+  double *rowhi = rowlo + (size_t)b.nmol * b.max_norb;
+  int *cnt = reinterpret_cast<int *>(rowhi + (size_t)b.nmol * b.max_norb);
   if (cudaMemsetAsync(cnt, 0, 2 * sizeof(int), s) != cudaSuccess) return SEQM_E_CUDA;
-  k_tc_init<<<b.nmol, NT_U, 0, s>>>(b, F, X, off, st, run, active);
+  k_sp2_rows<<<rows_grid(b), 256, 0, s>>>(b, F, rowlo, rowhi, active);
+  k_sp2_bounds<<<b.nmol, 256, 0, s>>>(b, rowlo, rowhi, st, active);
+  k_sp2_scale<float><<<ew_grid(b), EW_THREADS, 0, s>>>(b, F, X, st);
+  k_sp2_start<<<(b.nmol + 127) / 128, 128, 0, s>>>(b, st);
   const int tiles = (b.max_norb + TC_M - 1) / TC_M;
   const size_t smem = 4 * TILE_BYTES + 1024;
   if (cudaFuncSetAttribute(k_tc_square, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return SEQM_E_CUDA;
-  dim3 grid(tiles, tiles, b.nmol);
+  const dim3 grid(tiles, tiles, b.nmol);
   int rc = SEQM_OK;
   for (int it = 0; it < max_iter; ++it) {
-    k_tc_square<<<grid, TC_THREADS, smem, s>>>(b, X, X2, off, run, tr2, cnt + 1);
     if (cudaMemsetAsync(cnt, 0, sizeof(int), s) != cudaSuccess) { rc = SEQM_E_CUDA; break; }
-    k_tc_update<<<b.nmol, NT_U, 0, s>>>(b, X, X2, off, st, run, tr2, eps, cnt);
+    k_tc_square<<<grid, TC_THREADS, smem, s>>>(b, X, X2, b.mol_mat_off, st, nullptr, cnt + 1);
+    k_sp2_step<float><<<ew_grid(b), EW_THREADS, 0, s>>>(b, X, X2, st);
+    k_sp2_check<<<(b.nmol + 127) / 128, 128, 0, s>>>(b, st, eps, 1, cnt);
     int h[2] = {0, 0};
     if (cudaMemcpyAsync(h, cnt, 2 * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess) { rc = SEQM_E_CUDA; break; }
@@ -470,16 +280,8 @@ extern "C" int seqm_density_sp2_tc(const seqm_batch *bp, const double *F, double
     if (h[0] == 0) break;
   }
   if (rc != SEQM_OK) return rc;
-  if (status) k_tc_status<<<(b.nmol + 127) / 128, 128, 0, s>>>(b.nmol, st, run, active, status);
-  k_tc_finish<<<b.nmol, 256, 0, s>>>(b, X, off, P, active);
-  // FP64 McWeeny refinement of X = P/2
-  dim3 g64((b.max_norb + MW_T - 1) / MW_T, (b.max_norb + MW_T - 1) / MW_T, b.nmol);
-  double *Xd = Z;  // reuse: X (f64), X^2 in Y, X^3 in Z after X is consumed
-  for (int k = 0; k < mcweeny_steps; ++k) {
-    k_half<<<b.nmol, 256, 0, s>>>(b, P, Xd, active);
-    k_mw_gemm<<<g64, 256, 0, s>>>(b, Xd, Xd, Y, active);   // Y = X^2
-    k_mw_gemm<<<g64, 256, 0, s>>>(b, Y, Xd, P, active);    // P <- X^3 (temporarily)
-    k_mw_combine<<<b.nmol, 256, 0, s>>>(b, P, Y, P, active);
-  }
+  if (status) k_sp2_status<<<(b.nmol + 127) / 128, 128, 0, s>>>(b.nmol, st, active, status);
+  k_ew_sym<float><<<ew_grid(b), EW_THREADS, 0, s>>>(b, X, 1.0, 1.0, P, active);  // P = X + X^T
+  mcweeny(b, P, Y, Z, active, mcweeny_steps, s);
   return launch_check();
 }

@@ -114,7 +114,8 @@ class BatchSCF:
     def _sp2_fp64(self, out, eps, active):
         L = self.L
         if self.sp2_work is None:
-            self.sp2_work = torch.empty(2 * int(L.mat_off[-1]) + 4 * L.nmol, dtype=torch.float64, device=L.device)
+            nd = 2 * int(L.mat_off[-1]) + (11 + 2 * L.max_norb) * L.nmol + 1  # SEQM_SP2_WORK_DOUBLES
+            self.sp2_work = torch.empty(nd, dtype=torch.float64, device=L.device)
         self.launches += 1
         native.check(self.lib.seqm_density_sp2(L.struct, native.ptr(self.F), native.ptr(out), native.ptr(self.sp2_work),
                                                eps, native.ptr(active), native.ptr(self.status), 1000, self._s()),
@@ -124,7 +125,7 @@ class BatchSCF:
         L = self.L
         if self.sp2_tc_work is None:
             T = int(L.mat_off[-1])
-            nbytes = 24 * T + 8 + 56 * L.nmol + ((L.nmol + 15) & ~15) + 8
+            nbytes = 24 * T + 16 + 8 * (11 + 2 * L.max_norb) * L.nmol  # SEQM_SP2_TC_WORK_BYTES
             self.sp2_tc_work = torch.empty(nbytes, dtype=torch.uint8, device=L.device)
         self.launches += 1
         native.check(self.lib.seqm_density_sp2_tc(L.struct, native.ptr(self.F), native.ptr(out),

@@ -1,4 +1,4 @@
-"""Tensor-core (tcgen05, BF16 hi+lo) SP2 with FP64 McWeeny refinement, and the Jacobi / SP2
+"""Tensor-core (tcgen05, FP16 hi+lo) SP2 with FP64 McWeeny refinement, and the Jacobi / SP2
 dispatch for molecules above the Jacobi limit.  Mixed-precision form: |dE| <= 1e-4 eV per
 molecule against the FP64 oracle, idempotency of P/2 to FP64 level."""
 

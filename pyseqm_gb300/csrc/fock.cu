@@ -1,15 +1,23 @@
 // Fock build, electronic energy + SCF convergence test, density mixing (FP64).
 //
-// Fock (fock.py:132-181): one thread per atom builds the atom's diagonal block
+// Fock (fock.py:132-181): one warp per atom builds the atom's diagonal block
 // (Hcore + one-centre two-electron terms + Coulomb J gathered from all of the
-// atom's pairs), one thread per pair builds the off-diagonal block (Hcore +
-// exchange K) and its transpose.  Every element of F is written exactly once,
-// there are no atomics, and the result is bitwise symmetric.
+// atom's pairs; the lanes split the partners and a butterfly reduction combines
+// them), one thread per pair builds the off-diagonal block (Hcore + exchange K)
+// and its transpose.  Every element of F is written exactly once, there are no
+// atomics, and the result is bitwise symmetric.
+//
+// The energy / convergence test and the mixing run as thread-block clusters of
+// up to 16 CTAs per molecule (more CTAs for larger molecules); the energy sums are
+// combined through distributed shared memory in a fixed order.
+#include <cooperative_groups.h>
 #include <math.h>
 
 #include "common.cuh"
 
 namespace seqm {
+
+namespace cg = cooperative_groups;
 
 __device__ __forceinline__ bool is_active(const uint8_t *active, int m) { return active == nullptr || active[m]; }
 
@@ -26,110 +34,134 @@ __device__ __forceinline__ void packed_atom_density(const double *Pm, int norb, 
   }
 }
 
-__global__ void __launch_bounds__(128) k_fock(seqm_batch b, const double *__restrict__ P, const double *__restrict__ H,
-                                              const double *__restrict__ w_xx, const double *__restrict__ w_xh,
-                                              const double *__restrict__ w_hh, double *__restrict__ F,
-                                              const uint8_t *__restrict__ active) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int npairs = b.nxx + b.nxh + b.nhh;
-  if (t >= b.natoms + npairs) return;
-  if (t < b.natoms) {
-    // ---------------- diagonal block of atom a
-    const int a = t, m = b.atom_mol[a];
-    if (!is_active(active, m)) return;
-    const int a0 = b.mol_atom_off[m], nat = b.mol_atom_off[m + 1] - a0, nh = b.mol_nheavy[m], ny = nat - nh;
-    const int norb = b.mol_norb[m], la = a - a0;
-    const int xx0 = b.mol_xx_off[m], xh0 = b.mol_xh_off[m], hh0 = b.mol_hh_off[m];
-    const size_t mo = b.mol_mat_off[m];
-    const double *Pm = P + mo, *Hm = H + mo;
-    double *Fm = F + mo;
-    const double gss = par(b, SEQM_P_GSS, a), gsp = par(b, SEQM_P_GSP, a), gpp = par(b, SEQM_P_GPP, a);
-    const double gp2 = par(b, SEQM_P_GP2, a), hsp = par(b, SEQM_P_HSP, a);
-    if (la < nh) {
-      const int o = 4 * la;
-      double f[10], Pd[4][4];
+// butterfly sum: every lane ends with the same value, summed in the same order
+__device__ __forceinline__ double warp_allsum(double v) {
 #pragma unroll
-      for (int r = 0; r < 4; ++r)
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// diagonal block of atom a (fock.py:187-231 one-centre terms, :277-294 Coulomb), one warp
+__device__ __forceinline__ void fock_diag(const seqm_batch &b, int a, int lane, const double *__restrict__ P,
+                                          const double *__restrict__ H, const double *__restrict__ w_xx,
+                                          const double *__restrict__ w_xh, const double *__restrict__ w_hh,
+                                          double *__restrict__ F) {
+  const int m = b.atom_mol[a];
+  const int a0 = b.mol_atom_off[m], nat = b.mol_atom_off[m + 1] - a0, nh = b.mol_nheavy[m], ny = nat - nh;
+  const int norb = b.mol_norb[m], la = a - a0;
+  const int xx0 = b.mol_xx_off[m], xh0 = b.mol_xh_off[m], hh0 = b.mol_hh_off[m];
+  const size_t mo = b.mol_mat_off[m];
+  const double *Pm = P + mo, *Hm = H + mo;
+  double *Fm = F + mo;
+  const double gss = par(b, SEQM_P_GSS, a);
+  if (la < nh) {
+    const int o = 4 * la;
+    // Coulomb from the partners B (lanes take partners q = lane, lane + 32, ...): pairs where
+    // this atom is first contribute J_B = w . P_B, pairs where it is second P_B . w
+    double f[10];
 #pragma unroll
-        for (int c = 0; c < 4; ++c) Pd[r][c] = Pm[(size_t)(o + r) * norb + o + c];
-      // one-centre terms (fock.py:187-231)
-      const double f1 = gsp - 0.5 * hsp, f2 = 1.5 * hsp - 0.5 * gsp, f3 = 1.25 * gp2 - 0.25 * gpp,
-                   f4 = 0.75 * gpp - 1.25 * gp2;
-      const double Pss = Pd[0][0], Ppt = Pd[1][1] + Pd[2][2] + Pd[3][3];
-#pragma unroll
-      for (int k = 0; k < 10; ++k) {
-        int r = k10_row(k), c = k10_col(k);
-        double oc;
-        if (r == 0 && c == 0) oc = 0.5 * Pss * gss + Ppt * f1;
-        else if (r == c) oc = Pss * f1 + 0.5 * Pd[r][r] * gpp + (Ppt - Pd[r][r]) * f3;
-        else if (r == 0) oc = Pd[0][c] * f2;
-        else oc = Pd[r][c] * f4;
-        f[k] = Hm[(size_t)(o + r) * norb + o + c] + oc;
-      }
-      // Coulomb from partners B: first-atom pairs (J_B = w . P_B), then second-atom pairs (P_B . w)
-      for (int j = la + 1; j < nh; ++j) {
-        const double *w = w_xx + (size_t)100 * (xx0 + tri_index(la, j, nh));
+    for (int k = 0; k < 10; ++k) f[k] = 0.0;
+    for (int q = lane; q < nat - 1; q += 32) {
+      if (q < nh - 1) {
+        const int j = q < la ? q : q + 1;
         double PB[10];
         packed_atom_density(Pm, norb, 4 * j, true, PB);
+        if (j > la) {
+          const double *w = w_xx + (size_t)100 * (xx0 + tri_index(la, j, nh));
 #pragma unroll
-        for (int k = 0; k < 10; ++k) {
-          double s = 0.0;
+          for (int k = 0; k < 10; ++k) {
+            double s = 0.0;
 #pragma unroll
-          for (int l = 0; l < 10; ++l) s += PB[l] * w[k * 10 + l];
-          f[k] += s;
+            for (int l = 0; l < 10; ++l) s += PB[l] * w[k * 10 + l];
+            f[k] += s;
+          }
+        } else {
+          const double *w = w_xx + (size_t)100 * (xx0 + tri_index(j, la, nh));
+#pragma unroll
+          for (int l = 0; l < 10; ++l) {
+            double s = 0.0;
+#pragma unroll
+            for (int k = 0; k < 10; ++k) s += PB[k] * w[k * 10 + l];
+            f[l] += s;
+          }
         }
-      }
-      for (int h = 0; h < ny; ++h) {
+      } else {
+        const int h = q - (nh - 1), oh = 4 * nh + h;
         const double *w = w_xh + (size_t)10 * (xh0 + la * ny + h);
-        double ph = Pm[(size_t)(3 * nh + nh + h) * norb + 3 * nh + nh + h];
+        const double ph = Pm[(size_t)oh * norb + oh];
 #pragma unroll
         for (int k = 0; k < 10; ++k) f[k] += ph * w[k];
       }
-      for (int i = 0; i < la; ++i) {
-        const double *w = w_xx + (size_t)100 * (xx0 + tri_index(i, la, nh));
+    }
+#pragma unroll
+    for (int k = 0; k < 10; ++k) f[k] = warp_allsum(f[k]);
+    // one-centre terms (fock.py:187-231)
+    const double gsp = par(b, SEQM_P_GSP, a), gpp = par(b, SEQM_P_GPP, a);
+    const double gp2 = par(b, SEQM_P_GP2, a), hsp = par(b, SEQM_P_HSP, a);
+    double Pd[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) Pd[r][c] = Pm[(size_t)(o + r) * norb + o + c];
+    const double f1 = gsp - 0.5 * hsp, f2 = 1.5 * hsp - 0.5 * gsp, f3 = 1.25 * gp2 - 0.25 * gpp,
+                 f4 = 0.75 * gpp - 1.25 * gp2;
+    const double Pss = Pd[0][0], Ppt = Pd[1][1] + Pd[2][2] + Pd[3][3];
+#pragma unroll
+    for (int k = 0; k < 10; ++k) {
+      const int r = k10_row(k), c = k10_col(k);
+      double oc;
+      if (r == 0 && c == 0) oc = 0.5 * Pss * gss + Ppt * f1;
+      else if (r == c) oc = Pss * f1 + 0.5 * Pd[r][r] * gpp + (Ppt - Pd[r][r]) * f3;
+      else if (r == 0) oc = Pd[0][c] * f2;
+      else oc = Pd[r][c] * f4;
+      if (lane == k) {
+        const double v = Hm[(size_t)(o + r) * norb + o + c] + oc + f[k];
+        Fm[(size_t)(o + r) * norb + o + c] = v;
+        Fm[(size_t)(o + c) * norb + o + r] = v;
+      }
+    }
+  } else {
+    const int h = la - nh, o = 3 * nh + la;
+    double f = 0.0;
+    for (int q = lane; q < nat - 1; q += 32) {
+      if (q < nh) {
+        const double *w = w_xh + (size_t)10 * (xh0 + q * ny + h);
         double PB[10];
-        packed_atom_density(Pm, norb, 4 * i, true, PB);
-#pragma unroll
-        for (int l = 0; l < 10; ++l) {
-          double s = 0.0;
-#pragma unroll
-          for (int k = 0; k < 10; ++k) s += PB[k] * w[k * 10 + l];
-          f[l] += s;
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < 10; ++k) {
-        int r = k10_row(k), c = k10_col(k);
-        Fm[(size_t)(o + r) * norb + o + c] = f[k];
-        Fm[(size_t)(o + c) * norb + o + r] = f[k];
-      }
-    } else {
-      const int h = la - nh, o = 3 * nh + la;
-      const double Pss = Pm[(size_t)o * norb + o];
-      double f = Hm[(size_t)o * norb + o] + (0.5 * Pss * gss + 0.0 * (gsp - 0.5 * hsp));
-      for (int g = h + 1; g < ny; ++g) {
-        int og = 3 * nh + nh + g;
-        f += w_hh[hh0 + tri_index(h, g, ny)] * Pm[(size_t)og * norb + og];
-      }
-      for (int i = 0; i < nh; ++i) {
-        const double *w = w_xh + (size_t)10 * (xh0 + i * ny + h);
-        double PB[10];
-        packed_atom_density(Pm, norb, 4 * i, true, PB);
+        packed_atom_density(Pm, norb, 4 * q, true, PB);
         double s = 0.0;
 #pragma unroll
         for (int k = 0; k < 10; ++k) s += PB[k] * w[k];
         f += s;
+      } else {
+        const int g0 = q - nh, g = g0 < h ? g0 : g0 + 1, og = 4 * nh + g;
+        const double w = w_hh[hh0 + (g < h ? tri_index(g, h, ny) : tri_index(h, g, ny))];
+        f += w * Pm[(size_t)og * norb + og];
       }
-      for (int g = 0; g < h; ++g) {
-        int og = 3 * nh + nh + g;
-        f += w_hh[hh0 + tri_index(g, h, ny)] * Pm[(size_t)og * norb + og];
-      }
-      Fm[(size_t)o * norb + o] = f;
     }
+    f = warp_allsum(f);
+    if (lane == 0) {
+      const double Pss = Pm[(size_t)o * norb + o];
+      Fm[(size_t)o * norb + o] = Hm[(size_t)o * norb + o] + 0.5 * Pss * gss + f;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128) k_fock(seqm_batch b, const double *__restrict__ P, const double *__restrict__ H,
+                                              const double *__restrict__ w_xx, const double *__restrict__ w_xh,
+                                              const double *__restrict__ w_hh, double *__restrict__ F,
+                                              const uint8_t *__restrict__ active) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long ndiag = 32LL * b.natoms;  // one warp per atom; warps never straddle the two roles
+  const int npairs = b.nxx + b.nxh + b.nhh;
+  if (t < ndiag) {
+    const int a = (int)(t >> 5);
+    if (!is_active(active, b.atom_mol[a])) return;
+    fock_diag(b, a, (int)(t & 31), P, H, w_xx, w_xh, w_hh, F);
     return;
   }
+  if (t - ndiag >= npairs) return;
   // ---------------- off-diagonal block of pair p: F_AB = H_AB - 1/2 sum P_AB (mu lam | nu sig)
-  const int p = t - b.natoms;
+  const int p = (int)(t - ndiag);
   const int ia = b.pair_i[p], ja = b.pair_j[p];
   const int m = b.atom_mol[ia];
   if (!is_active(active, m)) return;
@@ -222,48 +254,95 @@ __device__ double block_max(double v, double *red) {
 // Eelec = 1/2 sum P (H + F) (energy.py:26-49); get_error (scf_loop.py:106-147):
 // not converged <=> |dE| > eps or ||dP||_F/(4 natoms) > 2 eps or max|dP| > 15 eps,
 // the density terms refreshed only when the energy test passes.
-constexpr int NT_RED = 256;
+//
+// One cluster of cs CTAs per molecule.  The molecule's elements are cut into
+// EE_SLICES interleaved slices (slice s: elements s*NT + t + k*EE_SLICES*NT); CTA
+// rank r sums the slices s with s % cs == r, and rank 0 adds the slice sums in
+// slice order through distributed shared memory, so the result does not depend
+// on cs.
+__device__ __forceinline__ void finish_error(const seqm_batch &b, int m, double e, double fro, double mx, double *Eelec,
+                                        double *err, double *dm_err, double *dm_el, uint8_t *active, double eps) {
+  double de = e - Eelec[m];
+  err[m] = de;
+  bool bad = fabs(de) > eps;
+  if (!bad) {
+    int nat = b.mol_atom_off[m + 1] - b.mol_atom_off[m];
+    dm_err[m] = sqrt(fro) / (4.0 * nat);
+    dm_el[m] = mx;
+  }
+  bool nc = bad || dm_err[m] > eps * 2.0 || dm_el[m] > eps * 15.0;
+  if (nc) Eelec[m] = e;
+  if (active) active[m] = nc ? 1 : 0;
+}
+
+constexpr int NT_RED = 512, EE_SLICES = 16, EE_UNROLL = 4;
 __global__ void __launch_bounds__(NT_RED) k_energy_error(seqm_batch b, const double *__restrict__ P,
                                                          const double *__restrict__ Pold, const double *__restrict__ H,
                                                          const double *__restrict__ F, double *Eelec, double *Eout,
                                                          double *err, double *dm_err, double *dm_el, uint8_t *active,
-                                                         double eps) {
-  __shared__ double red[NT_RED / 32];
-  const int m = blockIdx.x;
-  if (!is_active(active, m)) return;
+                                                         double eps, int cs) {
+  __shared__ double wred[NT_RED / 32][3 * EE_SLICES];
+  __shared__ double part[3 * EE_SLICES];
+  cg::cluster_group cl = cg::this_cluster();
+  const int m = blockIdx.x / cs, r = (int)cl.block_rank();
+  if (!is_active(active, m)) return;  // uniform over the cluster
   const int norb = b.mol_norb[m];
   const size_t mo = b.mol_mat_off[m], nn = (size_t)norb * norb;
-  double e = 0.0, fro = 0.0, mx = 0.0;
-  for (size_t i = threadIdx.x; i < nn; i += NT_RED) {
-    double pv = P[mo + i];
-    e += pv * (H[mo + i] + F[mo + i]);
-    if (Pold) {
-      double d = pv - Pold[mo + i];
-      fro += d * d;
-      mx = fmax(mx, fabs(d));
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const size_t stride = (size_t)EE_SLICES * NT_RED;
+  for (int s = r; s < EE_SLICES; s += cs) {  // the slices of this CTA
+    double e = 0.0, fro = 0.0, mx = 0.0;
+    for (size_t i = (size_t)s * NT_RED + threadIdx.x; i < nn; i += EE_UNROLL * stride) {
+      double pv[EE_UNROLL], hf[EE_UNROLL], po[EE_UNROLL];
+#pragma unroll
+      for (int u = 0; u < EE_UNROLL; ++u) {  // independent loads in flight
+        const size_t j = i + u * stride;
+        const bool in = j < nn;
+        pv[u] = in ? P[mo + j] : 0.0;
+        hf[u] = in ? H[mo + j] + F[mo + j] : 0.0;
+        po[u] = (in && Pold) ? Pold[mo + j] : pv[u];
+      }
+#pragma unroll
+      for (int u = 0; u < EE_UNROLL; ++u) {
+        e += pv[u] * hf[u];
+        const double d = pv[u] - po[u];
+        fro += d * d;
+        mx = fmax(mx, fabs(d));
+      }
+    }
+    double v3[3] = {e, fro, mx};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      double v = v3[q];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double u = __shfl_xor_sync(0xffffffffu, v, o);
+        v = q == 2 ? fmax(v, u) : v + u;
+      }
+      if (lane == 0) wred[warp][3 * s + q] = v;
     }
   }
-  e = 0.5 * block_sum<NT_RED>(e, red);
-  if (!Pold) {
-    if (threadIdx.x == 0) Eout[m] = e;
-    return;
+  __syncthreads();
+  if (threadIdx.x < 3 * EE_SLICES && (threadIdx.x / 3) % cs == r) {
+    const int j = threadIdx.x;
+    double v = wred[0][j];
+    for (int w = 1; w < NT_RED / 32; ++w) v = (j % 3 == 2) ? fmax(v, wred[w][j]) : v + wred[w][j];
+    part[j] = v;
   }
-  fro = block_sum<NT_RED>(fro, red);
-  mx = block_max<NT_RED>(mx, red);
-  if (threadIdx.x == 0) {
+  cl.sync();
+  if (r == 0 && threadIdx.x == 0) {
+    double e = 0.0, fro = 0.0, mx = 0.0;
+    for (int s = 0; s < EE_SLICES; ++s) {
+      const double *q = cl.map_shared_rank(part, s % cs);
+      e += q[3 * s];
+      fro += q[3 * s + 1];
+      mx = fmax(mx, q[3 * s + 2]);
+    }
+    e *= 0.5;
     Eout[m] = e;
-    double de = e - Eelec[m];
-    err[m] = de;
-    bool bad = fabs(de) > eps;
-    if (!bad) {
-      int nat = b.mol_atom_off[m + 1] - b.mol_atom_off[m];
-      dm_err[m] = sqrt(fro) / (4.0 * nat);
-      dm_el[m] = mx;
-    }
-    bool nc = bad || dm_err[m] > eps * 2.0 || dm_el[m] > eps * 15.0;
-    if (nc) Eelec[m] = e;
-    if (active) active[m] = nc ? 1 : 0;
+    if (Pold) finish_error(b, m, e, fro, mx, Eelec, err, dm_err, dm_el, active, eps);
   }
+  cl.sync();  // the other CTAs' shared memory stays alive until rank 0 has read it
 }
 
 // ------------------------------------------------------------------ mixing
@@ -273,42 +352,57 @@ __global__ void __launch_bounds__(NT_RED) k_energy_error(seqm_batch b, const dou
 // damped (|step| <= 0.05 after iteration 4), clamped to [0, 2] and renormalised
 // to the new trace in at most 20 passes.  Each molecule stops its own
 // renormalisation (the reference stops when the whole padded batch is done).
-constexpr int NT_MIX = 256;
+//
+// One cluster of cs CTAs per molecule: every CTA reads the diagonal history and
+// forms FAC (identical arithmetic in each), the CTAs split the elementwise update,
+// and rank 0 alone damps, clamps and renormalises the diagonal and writes it after
+// a cluster barrier, over the provisional values of the elementwise pass.
+constexpr int NT_MIX = 512, MIX_UNROLL = 4;
 __global__ void __launch_bounds__(NT_MIX) k_mix(seqm_batch b, double *__restrict__ P, const double *__restrict__ Pnew,
                                                 double *__restrict__ Pold, double *__restrict__ old2,
                                                 const int64_t *__restrict__ row_off, int32_t *__restrict__ kit,
-                                                int linear, double alpha, const uint8_t *__restrict__ active) {
+                                                int linear, double alpha, const uint8_t *__restrict__ active, int cs) {
   extern __shared__ double sm[];
   __shared__ double red[NT_MIX / 32];
-  __shared__ int k_sh;
-  const int m = blockIdx.x;
-  if (!is_active(active, m)) return;
+  cg::cluster_group cl = cg::this_cluster();
+  const int m = blockIdx.x / cs, r = (int)cl.block_rank();
+  if (!is_active(active, m)) return;  // uniform over the cluster
   const int n = b.mol_norb[m];
-  if (threadIdx.x == 0) {
-    k_sh = kit[m] + 1;  // 1-based iteration number of this molecule
-    kit[m] = k_sh;
-  }
-  __syncthreads();
-  const size_t mo = b.mol_mat_off[m];
+  const int k = kit[m] + 1;  // 1-based iteration number of this molecule
+  const size_t mo = b.mol_mat_off[m], nn = (size_t)n * n;
+  const size_t i0 = (size_t)r * NT_MIX + threadIdx.x, step = (size_t)cs * NT_MIX;
   double *Pm = P + mo, *Po = Pold + mo;
   const double *Pn = Pnew + mo;
   if (linear) {
+    cl.sync();  // every CTA has read kit[m]
+    if (r == 0 && threadIdx.x == 0) kit[m] = k;
     const double oma = 1.0 - alpha;
-    for (size_t i = threadIdx.x; i < (size_t)n * n; i += NT_MIX) {
-      double pv = Pm[i];
-      Po[i] = pv;
-      Pm[i] = alpha * pv + oma * Pn[i];
+    for (size_t i = i0; i < nn; i += MIX_UNROLL * step) {
+      double pv[MIX_UNROLL], pn[MIX_UNROLL];
+#pragma unroll
+      for (int u = 0; u < MIX_UNROLL; ++u) {
+        const size_t j = i + u * step;
+        pv[u] = j < nn ? Pm[j] : 0.0;
+        pn[u] = j < nn ? Pn[j] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < MIX_UNROLL; ++u) {
+        const size_t j = i + u * step;
+        if (j < nn) {
+          Po[j] = pv[u];
+          Pm[j] = alpha * pv[u] + oma * pn[u];
+        }
+      }
     }
     return;
   }
-  const int k = k_sh;
   double *dprev = sm, *di = sm + n;
   double *o2 = old2 + row_off[m];
   double num = 0.0, den = 0.0;
   for (int i = threadIdx.x; i < n; i += NT_MIX) {
-    double dp = Pm[(size_t)i * n + i], dc = Pn[(size_t)i * n + i];
+    const double dp = Pm[(size_t)i * n + i], dc = Pn[(size_t)i * n + i];
     dprev[i] = dp;
-    double d1 = dc - dp, d2 = dc - 2.0 * dp + o2[i];
+    const double d1 = dc - dp, d2 = dc - 2.0 * dp + o2[i];
     num += d1 * d1;
     den += d2 * d2;
   }
@@ -318,45 +412,63 @@ __global__ void __launch_bounds__(NT_MIX) k_mix(seqm_batch b, double *__restrict
     num = block_sum<NT_MIX>(num, red);
     den = block_sum<NT_MIX>(den, red);
     fac = (den > 0.0 && num < 100.0 * den) ? sqrt(num / den) : 0.0;
-  } else {
-    __syncthreads();
   }
+  cl.sync();  // every CTA has read kit[m], the diagonal of P and old2
+  if (r == 0 && threadIdx.x == 0) kit[m] = k;
   // off-diagonal (and provisional diagonal) update
-  for (size_t idx = threadIdx.x; idx < (size_t)n * n; idx += NT_MIX) {
-    double pv = Pm[idx];
-    Po[idx] = pv;
-    Pm[idx] = third ? (1.0 + fac) * Pn[idx] - fac * pv : Pn[idx];
-  }
-  // diagonal: damp, clamp, renormalise
-  const double damp = k > 4 ? 0.05 : 1.0e10;
-  double s0 = 0.0;
-  for (int i = threadIdx.x; i < n; i += NT_MIX) {
-    double dc = Pn[(size_t)i * n + i], dp = dprev[i];
-    double delta = dc - dp;
-    double v = fabs(delta) > damp ? dp + (delta > 0.0 ? 1.0 : (delta < 0.0 ? -1.0 : 0.0)) * damp : dc + fac * delta;
-    di[i] = fmin(fmax(v, 0.0), 2.0);
-    s0 += dc;
-  }
-  double sum0 = block_sum<NT_MIX>(s0, red);
-  for (int pass = 0; pass < 20; ++pass) {
-    double s2 = 0.0;
-    for (int i = threadIdx.x; i < n; i += NT_MIX) s2 += di[i];
-    double sum2 = block_sum<NT_MIX>(s2, red);
-    double sum3 = sum2 > 1.0e-3 ? sum0 / sum2 : 0.0;
-    if (!(sum2 > 1.0e-3) || fabs(sum3 - 1.0) <= 1.0e-5) break;
-    double nfull = 0.0;
-    for (int i = threadIdx.x; i < n; i += NT_MIX) {
-      double sc = fmax(di[i] * sum3, 0.0);
-      bool full = sc > 2.0;
-      di[i] = full ? 2.0 : sc;
-      nfull += full ? 1.0 : 0.0;
+  for (size_t i = i0; i < nn; i += MIX_UNROLL * step) {
+    double pv[MIX_UNROLL], pn[MIX_UNROLL];
+#pragma unroll
+    for (int u = 0; u < MIX_UNROLL; ++u) {
+      const size_t j = i + u * step;
+      pv[u] = j < nn ? Pm[j] : 0.0;
+      pn[u] = j < nn ? Pn[j] : 0.0;
     }
-    nfull = block_sum<NT_MIX>(nfull, red);
-    sum0 = sum0 - nfull * 2.0;
+#pragma unroll
+    for (int u = 0; u < MIX_UNROLL; ++u) {
+      const size_t j = i + u * step;
+      if (j < nn) {
+        Po[j] = pv[u];
+        Pm[j] = third ? (1.0 + fac) * pn[u] - fac * pv[u] : pn[u];
+      }
+    }
   }
-  for (int i = threadIdx.x; i < n; i += NT_MIX) {
-    Pm[(size_t)i * n + i] = di[i];
-    o2[i] = dprev[i];
+  if (r == 0) {
+    // diagonal: damp, clamp, renormalise
+    const double damp = k > 4 ? 0.05 : 1.0e10;
+    double s0 = 0.0;
+    for (int i = threadIdx.x; i < n; i += NT_MIX) {
+      const double dc = Pn[(size_t)i * n + i], dp = dprev[i];
+      const double delta = dc - dp;
+      const double v =
+          fabs(delta) > damp ? dp + (delta > 0.0 ? 1.0 : (delta < 0.0 ? -1.0 : 0.0)) * damp : dc + fac * delta;
+      di[i] = fmin(fmax(v, 0.0), 2.0);
+      s0 += dc;
+    }
+    double sum0 = block_sum<NT_MIX>(s0, red);
+    for (int pass = 0; pass < 20; ++pass) {
+      double s2 = 0.0;
+      for (int i = threadIdx.x; i < n; i += NT_MIX) s2 += di[i];
+      const double sum2 = block_sum<NT_MIX>(s2, red);
+      const double sum3 = sum2 > 1.0e-3 ? sum0 / sum2 : 0.0;
+      if (!(sum2 > 1.0e-3) || fabs(sum3 - 1.0) <= 1.0e-5) break;
+      double nfull = 0.0;
+      for (int i = threadIdx.x; i < n; i += NT_MIX) {
+        const double sc = fmax(di[i] * sum3, 0.0);
+        const bool full = sc > 2.0;
+        di[i] = full ? 2.0 : sc;
+        nfull += full ? 1.0 : 0.0;
+      }
+      nfull = block_sum<NT_MIX>(nfull, red);
+      sum0 = sum0 - nfull * 2.0;
+    }
+  }
+  cl.sync();  // every CTA's provisional diagonal is written
+  if (r == 0) {
+    for (int i = threadIdx.x; i < n; i += NT_MIX) {
+      Pm[(size_t)i * n + i] = di[i];
+      o2[i] = dprev[i];
+    }
   }
 }
 
@@ -380,11 +492,42 @@ __global__ void k_initial_density(seqm_batch b, double *__restrict__ P) {
 
 using namespace seqm;
 
+// CTAs per molecule of the cluster kernels: more for larger molecules; 16 (above the portable
+// cluster size of 8) where the kernel accepts it
+template <typename... Params>
+static int mol_cluster(void (*kern)(Params...), int max_norb) {
+  if (max_norb <= 160) return 1;
+  if (max_norb <= 320) return 2;
+  if (max_norb <= 640) return 4;
+  if (max_norb <= 1024) return 8;
+  return cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess ? 16 : 8;
+}
+
+// grid of nmol clusters of cs CTAs each (cluster c = molecule c)
+template <typename... Params, typename... Args>
+static int launch_clusters(void (*kern)(Params...), int cs, int nmol, int nt, size_t smem, void *stream,
+                           Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)cs * (unsigned)nmol);
+  cfg.blockDim = dim3((unsigned)nt);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = (cudaStream_t)stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)cs;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, kern, args...) != cudaSuccess) return SEQM_E_CUDA;
+  return launch_check();
+}
+
 extern "C" int seqm_fock(const seqm_batch *bp, const double *P, const double *H, const double *w_xx,
                          const double *w_xh, const double *w_hh, double *F, const uint8_t *active, void *stream) {
   if (!bp) return SEQM_E_ARG;
   seqm_batch b = *bp;
-  long long nt = (long long)b.natoms + b.nxx + b.nxh + b.nhh;
+  long long nt = 32LL * b.natoms + b.nxx + b.nxh + b.nhh;
   if (nt == 0) return SEQM_OK;
   k_fock<<<(unsigned)((nt + 127) / 128), 128, 0, (cudaStream_t)stream>>>(b, P, H, w_xx, w_xh, w_hh, F, active);
   return launch_check();
@@ -396,9 +539,9 @@ extern "C" int seqm_energy_error(const seqm_batch *bp, const double *P, const do
   if (!bp) return SEQM_E_ARG;
   seqm_batch b = *bp;
   if (b.nmol == 0) return SEQM_OK;
-  k_energy_error<<<b.nmol, NT_RED, 0, (cudaStream_t)stream>>>(b, P, Pold, H, F, Eelec, Eout, err, dm_err, dm_el,
-                                                             active, eps);
-  return launch_check();
+  const int cs = mol_cluster(k_energy_error, b.max_norb);
+  return launch_clusters(k_energy_error, cs, b.nmol, NT_RED, 0, stream, b, P, Pold, H, F, Eelec, Eout, err, dm_err,
+                         dm_el, active, eps, cs);
 }
 
 extern "C" int seqm_mix(const seqm_batch *bp, double *P, const double *Pnew, double *Pold, double *old2,
@@ -411,8 +554,9 @@ extern "C" int seqm_mix(const seqm_batch *bp, double *P, const double *Pnew, dou
   if (smem > 200 * 1024) return SEQM_E_TOO_LARGE;
   if (smem > 48 * 1024 && cudaFuncSetAttribute(k_mix, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return SEQM_E_CUDA;
-  k_mix<<<b.nmol, NT_MIX, smem, (cudaStream_t)stream>>>(b, P, Pnew, Pold, old2, mol_row_off, k, linear, alpha, active);
-  return launch_check();
+  const int cs = mol_cluster(k_mix, b.max_norb);
+  return launch_clusters(k_mix, cs, b.nmol, NT_MIX, smem, stream, b, P, Pnew, Pold, old2, mol_row_off, k, linear, alpha,
+                         active, cs);
 }
 
 extern "C" int seqm_initial_density(const seqm_batch *bp, double *P, void *stream) {

@@ -11,6 +11,8 @@
 // per-atom gather over the atom's pairs, so no atomics are used anywhere.
 #include <math.h>
 
+#include <mutex>
+
 #include "common.cuh"
 #include "pair_math.cuh"
 
@@ -220,7 +222,11 @@ extern "C" int seqm_hcore(const seqm_batch *bp, double *w_xx, double *w_xh, doub
   int npairs = b.nxx + b.nxh + b.nhh;
   if (b.natoms <= 0) return SEQM_OK;
   k_atom_prep<<<(b.natoms + 127) / 128, 128, 0, s>>>(b);
-  static int *d_err[64] = {};  // per-device error word (one int, kept for the process)
+  // per-device error word (one int, kept for the process); calls from several host threads
+  // (one stream each) take turns on it from the reset to the read-back
+  static int *d_err[64] = {};
+  static std::mutex err_lock;
+  std::lock_guard<std::mutex> guard(err_lock);
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev >= 64) return SEQM_E_CUDA;
   if (!d_err[dev] && cudaMalloc(&d_err[dev], sizeof(int)) != cudaSuccess) return SEQM_E_CUDA;

@@ -18,6 +18,9 @@ namespace {  // internal linkage: this header is compiled into more than one tra
 
 enum { S_ERR0 = 0, S_ERR1, S_ERR2, S_RUN, S_STEPS, S_T1, S_T2, S_ACC_T, S_ACC_F, S_H1, S_HN, SP2_NS };
 constexpr int EW_THREADS = 256;
+// the SP2 drivers read the running count back every SP2_SYNC_EVERY steps; a molecule that
+// stopped earlier is skipped by every kernel of the steps in between
+constexpr int SP2_SYNC_EVERY = 4;
 constexpr int EW_CHUNK = EW_THREADS * 8;  // elements per CTA of an elementwise pass
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -213,12 +216,17 @@ __global__ void __launch_bounds__(EW_THREADS) k_ew_axpby(seqm_batch b, double a,
     D[mo + idx] = a * A[mo + idx] + (C ? c * C[mo + idx] : 0.0);
 }
 
-// FP64 C = A B for symmetric products (upper 64x64 tiles, mirrored), molecules with run flag / active
-constexpr int MW_T = 64, MW_K = 16;
-__global__ void __launch_bounds__(256) k_sym_gemm64(seqm_batch b, const double *__restrict__ Am,
-                                                    const double *__restrict__ Bm, double *__restrict__ Cm,
-                                                    const uint8_t *__restrict__ active,
-                                                    const double *__restrict__ st) {
+// FP64 C = A B where A, B and the product are symmetric (X X, X^2 X): only the upper
+// MW_T x MW_T output tiles are computed and each is written with its mirror.  With A
+// symmetric, the A slab A[i0.., k0..] is read as rows of A[k0.., i0..], so both slabs
+// load along rows (coalesced) and are stored K-major without a transpose.  Small tiles
+// keep the FP64 pipes of all SMs busy on one molecule (a 1296-AO matrix gives 861
+// upper tiles); the next K slab is prefetched into registers during the FMAs.
+constexpr int MW_T = 32, MW_K = 32, MW_THREADS = 256;
+__global__ void __launch_bounds__(MW_THREADS) k_sym_gemm64(seqm_batch b, const double *__restrict__ Am,
+                                                           const double *__restrict__ Bm, double *__restrict__ Cm,
+                                                           const uint8_t *__restrict__ active,
+                                                           const double *__restrict__ st) {
   const int m = blockIdx.z;
   if (active && !active[m]) return;
   if (st && st[SP2_NS * m + S_RUN] == 0.0) return;
@@ -227,36 +235,54 @@ __global__ void __launch_bounds__(256) k_sym_gemm64(seqm_batch b, const double *
   if (i0 >= n || j0 >= n || blockIdx.y > blockIdx.x) return;
   const size_t mo = b.mol_mat_off[m];
   const double *A = Am + mo, *B = Bm + mo;
-  __shared__ double As[MW_K][MW_T + 1], Bs[MW_K][MW_T + 1];
+  __shared__ __align__(16) double As[2][MW_K][MW_T], Bs[2][MW_K][MW_T];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  double acc[4][4] = {};
-  for (int k0 = 0; k0 < n; k0 += MW_K) {
-    for (int e = threadIdx.x; e < MW_K * MW_T; e += 256) {
-      const int kk = e / MW_T, ii = e - kk * MW_T;
-      As[kk][ii] = (i0 + ii < n && k0 + kk < n) ? A[(size_t)(i0 + ii) * n + k0 + kk] : 0.0;
-      Bs[kk][ii] = (k0 + kk < n && j0 + ii < n) ? B[(size_t)(k0 + kk) * n + j0 + ii] : 0.0;
+  // slab loader: element e = threadIdx.x + 256 q (q = 0..3) of the 32 x 32 slab, row kk = e / 32, col c = e % 32
+  double ra[4], rb[4];
+  auto load = [&](int k0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int e = threadIdx.x + MW_THREADS * q, kk = e >> 5, c = e & 31;
+      const bool kin = k0 + kk < n;
+      ra[q] = (kin && i0 + c < n) ? A[(size_t)(k0 + kk) * n + i0 + c] : 0.0;
+      rb[q] = (kin && j0 + c < n) ? B[(size_t)(k0 + kk) * n + j0 + c] : 0.0;
     }
-    __syncthreads();
+  };
+  auto store = [&](int buf) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int e = threadIdx.x + MW_THREADS * q, kk = e >> 5, c = e & 31;
+      As[buf][kk][c] = ra[q];
+      Bs[buf][kk][c] = rb[q];
+    }
+  };
+  double acc[2][2] = {};
+  load(0);
+  store(0);
+  __syncthreads();
+  int buf = 0;
+  for (int k0 = 0; k0 < n; k0 += MW_K) {
+    const bool more = k0 + MW_K < n;
+    if (more) load(k0 + MW_K);
 #pragma unroll
     for (int kk = 0; kk < MW_K; ++kk) {
-      double a[4], c[4];
-#pragma unroll
-      for (int r = 0; r < 4; ++r) a[r] = As[kk][ty * 4 + r];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) c[q] = Bs[kk][tx * 4 + q];
-#pragma unroll
-      for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) acc[r][q] += a[r] * c[q];
+      const double2 a = *reinterpret_cast<const double2 *>(&As[buf][kk][2 * ty]);
+      const double2 c = *reinterpret_cast<const double2 *>(&Bs[buf][kk][2 * tx]);
+      acc[0][0] += a.x * c.x;
+      acc[0][1] += a.x * c.y;
+      acc[1][0] += a.y * c.x;
+      acc[1][1] += a.y * c.y;
     }
+    if (more) store(buf ^ 1);
     __syncthreads();
+    buf ^= 1;
   }
   double *C = Cm + mo;
 #pragma unroll
-  for (int r = 0; r < 4; ++r)
+  for (int r = 0; r < 2; ++r)
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int row = i0 + ty * 4 + r, col = j0 + tx * 4 + q;
+    for (int q = 0; q < 2; ++q) {
+      const int row = i0 + 2 * ty + r, col = j0 + 2 * tx + q;
       if (row < n && col < n) {
         C[(size_t)row * n + col] = acc[r][q];
         C[(size_t)col * n + row] = acc[r][q];
@@ -281,8 +307,8 @@ inline void mcweeny(const seqm_batch &b, double *P, double *Y, double *Z, const 
                     cudaStream_t s) {
   for (int k = 0; k < steps; ++k) {
     k_ew_axpby<<<ew_grid(b), EW_THREADS, 0, s>>>(b, 0.5, P, 0.0, nullptr, Z, active);  // Z = X
-    k_sym_gemm64<<<gemm64_grid(b), 256, 0, s>>>(b, Z, Z, Y, active, nullptr);            // Y = X^2
-    k_sym_gemm64<<<gemm64_grid(b), 256, 0, s>>>(b, Y, Z, P, active, nullptr);            // P = X^3
+    k_sym_gemm64<<<gemm64_grid(b), MW_THREADS, 0, s>>>(b, Z, Z, Y, active, nullptr);            // Y = X^2
+    k_sym_gemm64<<<gemm64_grid(b), MW_THREADS, 0, s>>>(b, Y, Z, P, active, nullptr);            // P = X^3
     k_ew_axpby<<<ew_grid(b), EW_THREADS, 0, s>>>(b, 6.0, Y, -4.0, P, P, active);         // P = 2(3X^2 - 2X^3)
   }
 }

@@ -273,6 +273,7 @@ extern "C" int seqm_density_sp2_tc(const seqm_batch *bp, const double *F, double
     k_tc_square<<<grid, TC_THREADS, smem, s>>>(b, X, X2, b.mol_mat_off, st, nullptr, cnt + 1);
     k_sp2_step<float><<<ew_grid(b), EW_THREADS, 0, s>>>(b, X, X2, st);
     k_sp2_check<<<(b.nmol + 127) / 128, 128, 0, s>>>(b, st, eps, 1, cnt);
+    if ((it + 1) % SP2_SYNC_EVERY != 0 && it + 1 < max_iter) continue;  // finished molecules skip the extra steps
     int h[2] = {0, 0};
     if (cudaMemcpyAsync(h, cnt, 2 * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess) { rc = SEQM_E_CUDA; break; }

@@ -15,6 +15,7 @@ and every kernel skips them, so a molecule's trajectory does not depend on its
 batch mates.  The host reads one byte count per iteration to stop the loop.
 """
 
+import ctypes
 import time
 
 import numpy as np
@@ -65,13 +66,15 @@ class BatchSCF:
         self.mixed_threshold = 5
         self.sp2_work = None
         self.sp2_tc_work = None
-        # molecules above the Jacobi limit take SP2: "tc" (tensor cores + FP64 McWeeny) or "fp64"
-        self.large_density = "tc"
+        # molecules above the Jacobi limit take SP2: "fp64" (plain) or "tc" (tensor cores + FP64 McWeeny)
+        self.large_density = "fp64"
         self.mcweeny_steps = 2
         self.large_mask = torch.as_tensor((layout.norb > JACOBI_MAX_N).astype(np.uint8), device=dev)
         self.n_large = int((layout.norb > JACOBI_MAX_N).sum())
         self.n_small = layout.nmol - self.n_large
         self.small_mask = 1 - self.large_mask
+        # SP2 runs over a compact view of the large molecules when the batch also holds small ones
+        self._large = self._large_view() if self.n_large and self.n_small else None
         self.stream = stream
         self.launches = 0  # kernels of this library launched (for reporting)
         self.profile_density = False  # record CUDA events around every density launch
@@ -111,33 +114,72 @@ class BatchSCF:
             return
         self._density(out, sp2, active, evecs, max_sweeps)
 
-    def _sp2_fp64(self, out, eps, active):
+    def _large_view(self):
+        """Batch struct over the molecules above the Jacobi limit only (the fields SP2 reads:
+        nmol, max_norb, mol_norb, mol_nocc, mol_mat_off; the matrix offsets point into the
+        full batch's matrices and end with the full size)."""
         L = self.L
-        if self.sp2_work is None:
-            nd = 2 * int(L.mat_off[-1]) + (11 + 2 * L.max_norb) * L.nmol + 1  # SEQM_SP2_WORK_DOUBLES
-            self.sp2_work = torch.empty(nd, dtype=torch.float64, device=L.device)
-        self.launches += 1
-        native.check(self.lib.seqm_density_sp2(L.struct, native.ptr(self.F), native.ptr(out), native.ptr(self.sp2_work),
-                                               eps, native.ptr(active), native.ptr(self.status), 1000, self._s()),
-                     "seqm_density_sp2")
+        idx = np.nonzero(L.norb > JACOBI_MAX_N)[0]
+        dev = L.device
+        v = dict(idx=torch.as_tensor(idx, dtype=torch.int64, device=dev),
+                 norb=torch.as_tensor(L.norb[idx].astype(np.int32), device=dev),
+                 nocc=torch.as_tensor(L.nocc[idx].astype(np.int32), device=dev),
+                 mat_off=torch.as_tensor(np.append(L.mat_off[idx], L.mat_off[-1]).astype(np.int64), device=dev),
+                 active=torch.zeros(idx.size, dtype=torch.uint8, device=dev),
+                 status=torch.zeros(idx.size, dtype=torch.int32, device=dev))
+        b = native.SeqmBatch.from_buffer_copy(L.struct)
+        b.nmol = int(idx.size)
+        b.max_norb = int(L.norb[idx].max())
+        b.mol_norb = v["norb"].data_ptr()
+        b.mol_nocc = v["nocc"].data_ptr()
+        b.mol_mat_off = v["mat_off"].data_ptr()
+        v["struct"] = b
+        return v
 
-    def _sp2_tc(self, out, eps, active):
+    def _sp2_target(self, active, subset):
+        """(struct, nmol, max_norb, active, status) of an SP2 call over all molecules or the large view."""
         L = self.L
-        if self.sp2_tc_work is None:
-            T = int(L.mat_off[-1])
-            nbytes = 24 * T + 16 + 8 * (11 + 2 * L.max_norb) * L.nmol  # SEQM_SP2_TC_WORK_BYTES
-            self.sp2_tc_work = torch.empty(nbytes, dtype=torch.uint8, device=L.device)
+        if not subset or self._large is None:
+            return L.struct, L.nmol, L.max_norb, active, self.status
+        v = self._large
+        if active is None:
+            v["active"].fill_(1)
+        else:
+            torch.index_select(active[: L.nmol], 0, v["idx"], out=v["active"])
+        return v["struct"], v["struct"].nmol, v["struct"].max_norb, v["active"], v["status"]
+
+    def _sp2_fp64(self, out, eps, active, subset=False):
+        b, nm, maxn, act, status = self._sp2_target(active, subset)
+        T = int(self.L.mat_off[-1])
+        nd = 2 * T + (11 + 2 * maxn) * nm + 1  # SEQM_SP2_WORK_DOUBLES
+        if self.sp2_work is None or self.sp2_work.numel() < nd:
+            self.sp2_work = torch.empty(nd, dtype=torch.float64, device=self.L.device)
         self.launches += 1
-        native.check(self.lib.seqm_density_sp2_tc(L.struct, native.ptr(self.F), native.ptr(out),
-                                                  native.ptr(self.sp2_tc_work), eps, native.ptr(active),
-                                                  native.ptr(self.status), 1000, self.mcweeny_steps, self._s()),
+        native.check(self.lib.seqm_density_sp2(b, native.ptr(self.F), native.ptr(out), native.ptr(self.sp2_work),
+                                               eps, native.ptr(act), native.ptr(status), 1000, self._s()),
+                     "seqm_density_sp2")
+        if status is not self.status:
+            self.status.index_copy_(0, self._large["idx"], status)
+
+    def _sp2_tc(self, out, eps, active, subset=False):
+        b, nm, maxn, act, status = self._sp2_target(active, subset)
+        T = int(self.L.mat_off[-1])
+        nbytes = 24 * T + 16 + 8 * (11 + 2 * maxn) * nm  # SEQM_SP2_TC_WORK_BYTES
+        if self.sp2_tc_work is None or self.sp2_tc_work.numel() < nbytes:
+            self.sp2_tc_work = torch.empty(nbytes, dtype=torch.uint8, device=self.L.device)
+        self.launches += 1
+        native.check(self.lib.seqm_density_sp2_tc(b, native.ptr(self.F), native.ptr(out),
+                                                  native.ptr(self.sp2_tc_work), eps, native.ptr(act),
+                                                  native.ptr(status), 1000, self.mcweeny_steps, self._s()),
                      "seqm_density_sp2_tc")
+        if status is not self.status:
+            self.status.index_copy_(0, self._large["idx"], status)
 
     def _density(self, out, sp2=(False,), active=None, evecs=None, max_sweeps=50):
         """Density step.  sp2[0] set: the reference's SP2 option for every molecule (plain FP64
         SP2, or tensor-core SP2 + FP64 McWeeny when sp2[2] == "tc").  Otherwise the Jacobi
         eigensolver for norb <= 160 and, for larger molecules, the SP2 form chosen by
-        ``large_density`` ("tc" by default, "fp64")."""
+        ``large_density`` ("fp64" by default, "tc")."""
         L = self.L
         if sp2[0]:
             if len(sp2) > 2 and sp2[2] == "tc":
@@ -146,11 +188,10 @@ class BatchSCF:
                 self._sp2_fp64(out, float(sp2[1]), active)
             return
         if self.n_large:
-            act = self.large_mask if active is None else active & self.large_mask
             if self.large_density == "tc":
-                self._sp2_tc(out, 1.0e-7, act)
+                self._sp2_tc(out, 1.0e-7, active, subset=True)
             else:
-                self._sp2_fp64(out, 1.0e-7, act)
+                self._sp2_fp64(out, 1.0e-7, active, subset=True)
             if not self.n_small:
                 return
         act_s = active if not self.n_large else (self.small_mask if active is None else active & self.small_mask)
@@ -182,10 +223,12 @@ class BatchSCF:
                                                 native.ptr(self.active), float(eps), self._s()), "seqm_energy_error")
 
     # --------------------------------------------------------------- drivers
-    def scf(self, eps, converger=(1,), sp2=(False,), P0=None, max_iter=MAX_ITER):
-        """Run the SCF; returns the per-molecule not-converged mask (host numpy)."""
+    def start(self, eps, converger=(1,), sp2=(False,), P0=None):
+        """Initial density, F(P0), E(P0) and the per-molecule SCF state; no host synchronisation."""
         L = self.L
         b = L.struct
+        if int(converger[0]) not in (0, 1):
+            raise NotImplementedError("scf_converger must be [0, alpha] (linear) or [1] (adaptive)")
         if P0 is None:
             self.P.zero_()
             self.launches += 1
@@ -202,23 +245,37 @@ class BatchSCF:
         self.iters.zero_()
         self.warm.zero_()
         self.old2.zero_()
-        linear = int(converger[0]) == 0
-        if int(converger[0]) not in (0, 1):
-            raise NotImplementedError("scf_converger must be [0, alpha] (linear) or [1] (adaptive)")
-        alpha = float(converger[1]) if linear else 0.0
-        n_loop = max_iter + 1 if linear else max_iter
-        for _ in range(n_loop):
-            self.density(self.Pnew, sp2, active=self.active)
-            self.launches += 1
-            native.check(self.lib.seqm_mix(b, native.ptr(self.P), native.ptr(self.Pnew), native.ptr(self.Pold),
-                                           native.ptr(self.old2), native.ptr(L.dev["row_off"]),
-                                           native.ptr(self.iters), int(linear), alpha, native.ptr(self.active),
-                                           self._s()), "seqm_mix")
-            self.fock(self.active)
-            self.energy_error(eps)
+        self._eps = float(eps)
+        self._linear = int(converger[0]) == 0
+        self._alpha = float(converger[1]) if self._linear else 0.0
+        self._sp2 = tuple(sp2)
+
+    def step(self):
+        """One SCF iteration of every still-active molecule (density, mixing, F(P), E(P), get_error);
+        molecules that pass the test are retired on the device.  No host synchronisation (except
+        inside the SP2 density step)."""
+        L = self.L
+        self.density(self.Pnew, self._sp2, active=self.active)
+        self.launches += 1
+        native.check(self.lib.seqm_mix(L.struct, native.ptr(self.P), native.ptr(self.Pnew), native.ptr(self.Pold),
+                                       native.ptr(self.old2), native.ptr(L.dev["row_off"]), native.ptr(self.iters),
+                                       int(self._linear), self._alpha, native.ptr(self.active), self._s()),
+                     "seqm_mix")
+        self.fock(self.active)
+        self.energy_error(self._eps)
+
+    def max_loops(self, max_iter=MAX_ITER):
+        """Iterations the reference's loop allows (MAX_ITER + 1 for linear mixing, scf_loop.py:250, MAX_ITER adaptive, :505)."""
+        return max_iter + 1 if self._linear else max_iter
+
+    def scf(self, eps, converger=(1,), sp2=(False,), P0=None, max_iter=MAX_ITER):
+        """Run the SCF; returns the per-molecule not-converged mask (host numpy)."""
+        self.start(eps, converger, sp2, P0)
+        for _ in range(self.max_loops(max_iter)):
+            self.step()
             if int(self.active.sum()) == 0:
                 break
-        return self.active[: L.nmol].bool().cpu().numpy()
+        return self.active[: self.L.nmol].bool().cpu().numpy()
 
     def final(self, want_vectors=True):
         """Fock matrix of the converged density, orbital energies / vectors, energies."""
@@ -231,8 +288,6 @@ class BatchSCF:
 
 
 def ctypes_stream(s):
-    import ctypes
-
     return ctypes.c_void_p(s.cuda_stream)
 
 

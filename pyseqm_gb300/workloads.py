@@ -129,3 +129,27 @@ def big_water(seed=0, n_side=10, spacing=3.1, jitter=0.25):
     """(H2O)_{n_side^3} on a jittered n_side^3 lattice."""
     rng = np.random.default_rng(seed)
     return water_cluster(n_side**3, rng, spacing=spacing, jitter=jitter, side=n_side)
+
+
+def request_molecules(n, seed=0, atoms=(3, 600), force_frac=0.1, sigma=0.03):
+    """Molecules of a request stream: size log-uniform in `atoms` (number of atoms), drawn 50/50
+    from the alkane generator (C_kH_{2k+2}, 3k + 2 atoms) and the water-cluster generator
+    ((H2O)_k, 3k atoms) at the nearest size; a fraction `force_frac` also asks for forces.
+    Returns [(species, coords, forces)]."""
+    rng = np.random.default_rng(seed)
+    lo, hi = math.log(atoms[0]), math.log(atoms[1])
+    out = []
+    for _ in range(n):
+        na = math.exp(rng.uniform(lo, hi))
+        if rng.random() < 0.5:
+            sp, xyz = alkane(max(1, int(round((na - 2.0) / 3.0))), rng, sigma)
+        else:
+            sp, xyz = water_cluster(max(1, int(round(na / 3.0))), rng)
+        out.append((sp, xyz, bool(rng.random() < force_frac)))
+    return out
+
+
+def poisson_arrivals(n, rate, seed=0):
+    """Arrival times (s) of a Poisson process of the given rate (requests/s)."""
+    rng = np.random.default_rng(seed + 7919)
+    return np.cumsum(rng.exponential(1.0 / rate, size=n))

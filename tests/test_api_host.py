@@ -74,3 +74,26 @@ def test_workload_generators_are_seeded_and_sorted():
         np.testing.assert_array_equal(s1, s2)
         np.testing.assert_array_equal(c1, c2)
         assert np.all(s1[:-1] >= s1[1:])
+
+
+def test_large_molecule_view_for_sp2():
+    """SP2 over a mixed batch runs on a compact view of the molecules above the Jacobi limit:
+    gathered sizes and occupations, matrix offsets into the full batch ending with its total."""
+    from pyseqm_gb300 import workloads
+    from pyseqm_gb300.layout import Layout
+    from pyseqm_gb300.scf import BatchSCF
+
+    rng = np.random.default_rng(0)
+    mols = [workloads.alkane(3, rng, 0.03), workloads.water_cluster(30, rng), workloads.alkane(2, rng, 0.03),
+            workloads.alkane(30, rng, 0.03)]
+    L = Layout.from_padded(*workloads.pad_batch(mols), "PM3").to_device("cpu")
+    v = BatchSCF(L)._large
+    np.testing.assert_array_equal(v["idx"].numpy(), [1, 3])
+    np.testing.assert_array_equal(v["norb"].numpy(), L.norb[[1, 3]])
+    np.testing.assert_array_equal(v["nocc"].numpy(), L.nocc[[1, 3]])
+    np.testing.assert_array_equal(v["mat_off"].numpy(), [L.mat_off[1], L.mat_off[3], L.mat_off[-1]])
+    assert v["struct"].nmol == 2 and v["struct"].max_norb == 182
+    assert v["struct"].mol_mat_off == v["mat_off"].data_ptr()
+    # a batch of large molecules only needs no view
+    L2 = Layout.from_padded(*workloads.pad_batch(mols[1::2]), "PM3").to_device("cpu")
+    assert BatchSCF(L2)._large is None

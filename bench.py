@@ -10,9 +10,20 @@ SCF to convergence + final energies.  Synthetic inputs, generated here.
 Arms:
   default            this library on N GPUs (one process per GPU, replicas: every
                      rank solves its own 4096-molecule batch, no collective on the
-                     data path; weak scaling).
+                     data path; weak scaling).  Rank 0 adds a bounded sample of the
+                     serving stream (PM3 requests of 3-600 atoms, Poisson arrivals):
+                     solves/s and p50/p99 latency of the serving form next to the
+                     plain FP64 form run one batch at a time, and their energy and
+                     force differences.
   --impl reference   the CPU oracle (NumPy restatement of the reference path) on
                      the host cores of rank 0 over a bounded sample per step.
+
+Other workloads (one JSON line each, rank 0, not part of the default run):
+  --config c1   16 perturbed n-butanes, PM3, plain FP64, linear mixing (alpha 0.1), eps 1e-8
+  --config c3   (H2O)1000 PM3: plain FP64 SP2 vs tensor-core SP2 + McWeeny (dE, max|dP|, ||X^2 - X||)
+  --config c4   MNDO forces and parameter gradients: 256 octanes + 256 (H2O)16, central
+                differences (h = 1e-4 A) on seeded coordinates
+  --config c5   the serving stream at several arrival rates (--requests, --rates)
 
 Prints one JSON line.
 """
@@ -163,6 +174,33 @@ def gpu_bus_id(torch, dev, local):
     return ids[local].strip() if local < len(ids) else str(local)
 
 
+def serving_sample(torch, dev, n, rate, seed=0):
+    """Bounded sample of the serving stream: both forms on the same requests and arrivals."""
+    from pyseqm_gb300 import serving, workloads
+
+    mols = workloads.request_molecules(n, seed=seed)
+    arr = workloads.poisson_arrivals(n, rate, seed=seed)
+    for form in ("serving", "plain"):  # warm-up: library, kernel attributes, allocator
+        serving.ServingLoop("PM3", eps=1e-5, form=form, device=dev).run(serving.make_requests(mols[:8]))
+    torch.cuda.synchronize()
+    out = {}
+    for form in ("serving", "plain"):
+        loop = serving.ServingLoop("PM3", eps=1e-5, form=form, device=dev)
+        res = loop.run(serving.make_requests(mols, arr))
+        sm = serving.summarize(res)
+        sm.update(cohorts=loop.cohorts, max_live_cohorts=loop.max_concurrent, gpu_launches=loop.launches)
+        out[form] = (sm, res)
+    dE = max(abs(a.Etot - b.Etot) for a, b in zip(out["serving"][1], out["plain"][1]))
+    dF = [float(np.abs(a.forces - b.forces).max()) for a, b in zip(out["serving"][1], out["plain"][1])
+          if a.forces is not None]
+    return {"workload": f"{n} PM3 requests, 3-600 atoms log-uniform (alkanes / water clusters), 10% with forces, "
+                        f"Poisson {rate:.0f} req/s, seed {seed}",
+            "scf_eps": 1e-5, "scf_eps_forces": 1e-6, "budget_bytes": 100e9,
+            "serving": out["serving"][0], "plain_fp64_one_batch_at_a_time": out["plain"][0],
+            "solves_per_s_ratio": out["serving"][0]["solves_per_s"] / out["plain"][0]["solves_per_s"],
+            "max_abs_dE_eV": dE, "max_abs_dF_eV_per_A": max(dF) if dF else None}
+
+
 def run_ours(args):
     import torch
 
@@ -263,6 +301,9 @@ def run_ours(args):
         e2e = {"value": args.nmol / dt, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                "ms_per_step": 1e3 * dt, "includes": "host layout build (NumPy), H2D, hcore+SCF+energies, D2H"}
         assert not r["notconverged"].any()
+    serve = None
+    if rank == 0 and args.serving_requests > 0:
+        serve = serving_sample(torch, dev, args.serving_requests, args.serving_rate)
     cpu = None
     if pool is not None:
         sample = mols[: args.cpu_sample]
@@ -280,10 +321,174 @@ def run_ours(args):
                                l2="working set (>1 GB of F/P/Hcore/integrals) exceeds L2; no flush needed",
                                scf_iterations_max=int(iters.max()), scf_iterations_mean=float(iters.mean())),
                 "p50_ms": statistics.median(step_ms), "p99_ms": float(np.percentile(step_ms, 99)),
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+                "serving_sample": serve}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+# ------------------------------------------------------------------ other workloads
+def _timed(torch, fn, steps, warmup):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        out = fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3 / steps, out
+
+
+def config_c1(torch, dev, args):
+    """16 perturbed n-butanes, PM3, plain FP64 (Jacobi eigensolver), linear mixing alpha 0.1, eps 1e-8."""
+    from pyseqm_gb300 import api, workloads
+    from pyseqm_gb300.layout import Layout
+    from pyseqm_gb300.scf import BatchSCF
+
+    species, coords = workloads.pad_batch(workloads.butane_batch(16, seed=0))
+    L = Layout.from_padded(species, coords, "PM3").to_device(dev)
+    s = BatchSCF(L)
+    s.mixed_threshold = 0
+
+    def step():
+        s.hcore()
+        nc = s.scf(1e-8, (0, 0.1))
+        s.final(want_vectors=False)
+        return nc
+
+    dt, nc = _timed(torch, step, args.steps, args.warmup)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        api.single_point(species, coords, "PM3", 1e-8, (0, 0.1), device=dev)
+    e2e = (time.perf_counter() - t0) / args.steps
+    it = s.iters[: L.nmol].cpu().numpy()
+    return {"metric": "SCF solves/s", "value": 16 / dt, "unit": "solves/s", "ms_per_step": 1e3 * dt,
+            "config": {"workload": "16 n-butanes C4H10 (sigma 0.03 A), PM3, plain FP64, converger [0, 0.1], eps 1e-8",
+                       "iterations": [int(it.min()), int(it.max())], "notconverged": int(nc.sum())},
+            "e2e": {"value": 16 / e2e, "unit": "solves/s", "ms_per_step": 1e3 * e2e}}
+
+
+def config_c3(torch, dev, args):
+    """(H2O)1000, PM3: plain FP64 SP2 vs tensor-core SP2 + McWeeny refinement."""
+    from pyseqm_gb300 import workloads
+    from pyseqm_gb300.layout import Layout
+    from pyseqm_gb300.scf import BatchSCF
+
+    species, coords = workloads.pad_batch([workloads.big_water(seed=0, n_side=10)])
+    L = Layout.from_padded(species, coords, "PM3").to_device(dev)
+    out = {}
+    for mode in ("tc", "fp64"):
+        s = BatchSCF(L)
+        s.large_density = mode
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.hcore()
+        nc = s.scf(1e-5, (1,))
+        s.final(want_vectors=False)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        X = 0.5 * L.block(s.P, 0)
+        idem = float((X @ X - X).abs().max())
+        it = int(s.iters[0])
+        out[mode] = dict(Etot=float(s.Eout[0] + s.Enuc[0]), seconds=dt, iterations=it, ms_per_iteration=1e3 * dt / it,
+                         idempotency_max_abs=idem, converged=not bool(nc[0]), P=s.P.clone())
+        del s, X
+        torch.cuda.empty_cache()
+    dP = float((out["tc"]["P"] - out["fp64"]["P"]).abs().max())
+    for v in out.values():
+        v.pop("P")
+    return {"metric": "seconds per single point", "value": out["tc"]["seconds"], "unit": "s",
+            "higher_is_better": False,
+            "config": {"workload": "(H2O)1000 PM3, 3000 atoms / 6000 AOs, 10^3 lattice 3.1 A, jitter 0.25 A, seed 0",
+                       "scf_eps": 1e-5},
+            "tensor_core_sp2": out["tc"], "plain_fp64_sp2": out["fp64"],
+            "dE_tc_minus_fp64_eV": out["tc"]["Etot"] - out["fp64"]["Etot"], "density_max_abs_diff": dP,
+            "speedup": out["fp64"]["seconds"] / out["tc"]["seconds"]}
+
+
+def config_c4(torch, dev, args):
+    """MNDO forces + parameter gradients (adjoint kernels) of 256 octanes + 256 (H2O)16; central
+    differences (h = 1e-4 A) on 32 seeded coordinates per molecule, all molecules at once."""
+    from pyseqm_gb300 import native, workloads
+    from pyseqm_gb300.layout import Layout
+    from pyseqm_gb300.scf import BatchSCF
+
+    rng = np.random.default_rng(0)
+    mols = [workloads.alkane(8, rng, 0.05) for _ in range(256)] + [workloads.water_cluster(16, rng) for _ in range(256)]
+    species, coords = workloads.pad_batch(mols)
+    eps = 1e-8
+    L = Layout.from_padded(species, coords, "MNDO").to_device(dev)
+    s = BatchSCF(L)
+    nm, na = L.nmol, L.natoms
+    f64 = dict(dtype=torch.float64, device=dev)
+    g = torch.ones(nm, **f64)
+    dR, dpar = torch.empty(3 * na, **f64), torch.empty(4 * na, **f64)
+    work = torch.empty(7 * max(1, L.npairs), **f64)
+
+    def solve_and_grad():
+        s.hcore()
+        s.scf(eps, (1,))
+        s.final(want_vectors=False)
+        native.check(s.lib.seqm_energy_grad(L.struct, native.ptr(s.P), native.ptr(g), native.ptr(g), native.ptr(dR),
+                                            native.ptr(dpar), native.ptr(work), s._s()), "seqm_energy_grad")
+        return dR
+
+    dt_all, _ = _timed(torch, solve_and_grad, args.steps, args.warmup)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    native.check(s.lib.seqm_energy_grad(L.struct, native.ptr(s.P), native.ptr(g), native.ptr(g), native.ptr(dR),
+                                        native.ptr(dpar), native.ptr(work), s._s()), "seqm_energy_grad")
+    e1.record()
+    torch.cuda.synchronize()
+    dt_grad = e0.elapsed_time(e1) / 1e3
+    force = -dR.view(na, 3).cpu().numpy()
+    xyz0 = L.xyz.copy()
+    h = 1e-4
+    worst = 0.0
+    for _ in range(32):
+        pick = np.array([L.atom_off[m] + rng.integers(0, L.natoms_m[m]) for m in range(nm)])
+        dim = rng.integers(0, 3, size=nm)
+        E = []
+        for sign in (1.0, -1.0):
+            xyz = xyz0.copy()
+            xyz[pick, dim] += sign * h
+            L.set_coordinates(xyz)
+            s.hcore()
+            s.scf(eps, (1,))
+            s.final(want_vectors=False)
+            E.append((s.Eout[:nm] + s.Enuc[:nm]).cpu().numpy())
+        fd = -(E[0] - E[1]) / (2 * h)
+        worst = max(worst, float(np.abs(fd - force[pick, dim]).max()))
+    L.set_coordinates(xyz0)
+    return {"metric": "solves+gradients/s", "value": nm / dt_all, "unit": "molecules/s", "ms_per_step": 1e3 * dt_all,
+            "config": {"workload": "MNDO, 256 n-octanes (sigma 0.05 A) + 256 (H2O)16, seed 0", "scf_eps": eps,
+                       "gradients": "all coordinates; U_ss, U_pp, beta_s, beta_p per atom"},
+            "gradient_kernel_ms": 1e3 * dt_grad,
+            "fd_check": {"h_A": h, "coordinates_per_molecule": 32, "max_abs_force_error_eV_per_A": worst}}
+
+
+def config_c5(torch, dev, args):
+    lines = []
+    for rate in [float(x) for x in args.rates.split(",")]:
+        lines.append(serving_sample(torch, dev, args.requests, rate))
+    return {"metric": "SCF solves/s + p50/p99 latency vs plain FP64 one batch at a time", "rates": lines}
+
+
+def run_config(args):
+    import torch
+
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    fn = {"c1": config_c1, "c3": config_c3, "c4": config_c4, "c5": config_c5}[args.config]
+    line = fn(torch, dev, args)
+    line.update({"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "dtype": "f64", "data": "synthetic",
+                 "config_id": args.config})
+    print(json.dumps(line), flush=True)
 
 
 def main():
@@ -296,10 +501,17 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=256)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serving-requests", type=int, default=400)
+    ap.add_argument("--serving-rate", type=float, default=10000.0)
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--requests", type=int, default=4000)
+    ap.add_argument("--rates", default="1000,5000,20000,50000")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
         run_reference(args)
+    elif args.config != "c2":
+        run_config(args)
     else:
         run_ours(args)
 

@@ -121,7 +121,7 @@ int seqm_density_jacobi_noalloc(const seqm_batch *b, const double *F, double *P,
  * applied per molecule to its packed Fock matrix (eps clamped to [1e-7, 1e-3] as there).
  * work: SEQM_SP2_WORK_DOUBLES(T, nmol, max_norb) doubles with T = mat_off[nmol].
  * P = 2 X at convergence.  status[m]: SP2 steps taken, or -1 if max_iter was hit.
- * Synchronises the stream once per SP2 step to test convergence. */
+ * Synchronises the stream every 4 SP2 steps to test convergence. */
 #define SEQM_SP2_STATE 11
 #define SEQM_SP2_WORK_DOUBLES(T, nmol, maxn) \
   (2 * (size_t)(T) + (SEQM_SP2_STATE + 2 * (size_t)(maxn)) * (size_t)(nmol) + 1)
@@ -129,13 +129,15 @@ int seqm_density_sp2(const seqm_batch *b, const double *F, double *P, double *wo
                      const uint8_t *active, int32_t *status, int max_iter, void *stream);
 
 /* SP2 with the squarings on the tensor cores (tcgen05, FP16 hi+lo split products, FP32
- * accumulation in tensor memory), then mcweeny_steps FP64 McWeeny refinements
- * X <- 3X^2 - 2X^3 of X = P/2.  Same purification and branch test as SP2.py:9-85 (the
+ * accumulation in tensor memory), then one FP32 McWeeny step X <- 3X^2 - 2X^3 of X = P/2
+ * and mcweeny_steps FP64-accurate ones (X <- X + D (I - 2X), D = X^2 - X, with X^2 in FP64
+ * and the small correction product in FP32): idempotency ~1e-11 after one, FP64 level after
+ * two.  Same purification and branch test as SP2.py:9-85 (the
  * trace of X^2 for the test is ||X||_F^2 in FP64); a molecule stops when the trace error
  * is below eps, or below 1e-2 and no longer improving (SP2.py:76-80).  No counterpart of
  * the mixed-precision form in the reference.  work: SEQM_SP2_TC_WORK_BYTES(T, nmol, max_norb)
  * bytes with T = mat_off[nmol].  status[m] = SP2 steps, -1 at the step cap.  Synchronises the
- * stream once per SP2 step. */
+ * stream every 4 SP2 steps. */
 #define SEQM_SP2_TC_WORK_BYTES(T, nmol, maxn) \
   (24 * (size_t)(T) + 16 + 8 * (SEQM_SP2_STATE + 2 * (size_t)(maxn)) * (size_t)(nmol))
 int seqm_density_sp2_tc(const seqm_batch *b, const double *F, double *P, void *work, double eps,

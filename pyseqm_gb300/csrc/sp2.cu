@@ -36,7 +36,7 @@ extern "C" int seqm_density_sp2(const seqm_batch *bp, const double *F, double *P
   int rc = SEQM_OK;
   for (int it = 0; it < max_iter; ++it) {
     if (cudaMemsetAsync(cnt, 0, sizeof(int), s) != cudaSuccess) { rc = SEQM_E_CUDA; break; }
-    k_sym_gemm64<<<gemm64_grid(b), MW_THREADS, 0, s>>>(b, X, X, X2, active, st);
+    k_sym_gemm<double><<<gemm64_grid(b), MW_THREADS, 0, s>>>(b, X, X, X2, active, st);
     k_sp2_step<double><<<ew_grid(b), EW_THREADS, 0, s>>>(b, X, X2, st);
     k_sp2_check<<<(b.nmol + 127) / 128, 128, 0, s>>>(b, st, eps, 0, cnt);
     if ((it + 1) % SP2_SYNC_EVERY != 0 && it + 1 < max_iter) continue;  // finished molecules skip the extra steps

@@ -216,17 +216,29 @@ __global__ void __launch_bounds__(EW_THREADS) k_ew_axpby(seqm_batch b, double a,
     D[mo + idx] = a * A[mo + idx] + (C ? c * C[mo + idx] : 0.0);
 }
 
-// FP64 C = A B where A, B and the product are symmetric (X X, X^2 X): only the upper
+// C = A B (T = double or float) where A, B and the product are symmetric (X X, functions
+// of one X): only the upper
 // MW_T x MW_T output tiles are computed and each is written with its mirror.  With A
 // symmetric, the A slab A[i0.., k0..] is read as rows of A[k0.., i0..], so both slabs
 // load along rows (coalesced) and are stored K-major without a transpose.  Small tiles
 // keep the FP64 pipes of all SMs busy on one molecule (a 1296-AO matrix gives 861
 // upper tiles); the next K slab is prefetched into registers during the FMAs.
 constexpr int MW_T = 32, MW_K = 32, MW_THREADS = 256;
-__global__ void __launch_bounds__(MW_THREADS) k_sym_gemm64(seqm_batch b, const double *__restrict__ Am,
-                                                           const double *__restrict__ Bm, double *__restrict__ Cm,
-                                                           const uint8_t *__restrict__ active,
-                                                           const double *__restrict__ st) {
+template <class T>
+struct vec2;
+template <>
+struct vec2<double> {
+  using type = double2;
+};
+template <>
+struct vec2<float> {
+  using type = float2;
+};
+template <class T>
+__global__ void __launch_bounds__(MW_THREADS) k_sym_gemm(seqm_batch b, const T *__restrict__ Am,
+                                                         const T *__restrict__ Bm, T *__restrict__ Cm,
+                                                         const uint8_t *__restrict__ active,
+                                                         const double *__restrict__ st) {
   const int m = blockIdx.z;
   if (active && !active[m]) return;
   if (st && st[SP2_NS * m + S_RUN] == 0.0) return;
@@ -234,18 +246,18 @@ __global__ void __launch_bounds__(MW_THREADS) k_sym_gemm64(seqm_batch b, const d
   const int i0 = blockIdx.y * MW_T, j0 = blockIdx.x * MW_T;
   if (i0 >= n || j0 >= n || blockIdx.y > blockIdx.x) return;
   const size_t mo = b.mol_mat_off[m];
-  const double *A = Am + mo, *B = Bm + mo;
-  __shared__ __align__(16) double As[2][MW_K][MW_T], Bs[2][MW_K][MW_T];
+  const T *A = Am + mo, *B = Bm + mo;
+  __shared__ __align__(16) T As[2][MW_K][MW_T], Bs[2][MW_K][MW_T];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   // slab loader: element e = threadIdx.x + 256 q (q = 0..3) of the 32 x 32 slab, row kk = e / 32, col c = e % 32
-  double ra[4], rb[4];
+  T ra[4], rb[4];
   auto load = [&](int k0) {
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int e = threadIdx.x + MW_THREADS * q, kk = e >> 5, c = e & 31;
       const bool kin = k0 + kk < n;
-      ra[q] = (kin && i0 + c < n) ? A[(size_t)(k0 + kk) * n + i0 + c] : 0.0;
-      rb[q] = (kin && j0 + c < n) ? B[(size_t)(k0 + kk) * n + j0 + c] : 0.0;
+      ra[q] = (kin && i0 + c < n) ? A[(size_t)(k0 + kk) * n + i0 + c] : (T)0;
+      rb[q] = (kin && j0 + c < n) ? B[(size_t)(k0 + kk) * n + j0 + c] : (T)0;
     }
   };
   auto store = [&](int buf) {
@@ -256,7 +268,7 @@ __global__ void __launch_bounds__(MW_THREADS) k_sym_gemm64(seqm_batch b, const d
       Bs[buf][kk][c] = rb[q];
     }
   };
-  double acc[2][2] = {};
+  T acc[2][2] = {};
   load(0);
   store(0);
   __syncthreads();
@@ -266,8 +278,9 @@ __global__ void __launch_bounds__(MW_THREADS) k_sym_gemm64(seqm_batch b, const d
     if (more) load(k0 + MW_K);
 #pragma unroll
     for (int kk = 0; kk < MW_K; ++kk) {
-      const double2 a = *reinterpret_cast<const double2 *>(&As[buf][kk][2 * ty]);
-      const double2 c = *reinterpret_cast<const double2 *>(&Bs[buf][kk][2 * tx]);
+      using V = typename vec2<T>::type;
+      const V a = *reinterpret_cast<const V *>(&As[buf][kk][2 * ty]);
+      const V c = *reinterpret_cast<const V *>(&Bs[buf][kk][2 * tx]);
       acc[0][0] += a.x * c.x;
       acc[0][1] += a.x * c.y;
       acc[1][0] += a.y * c.x;
@@ -277,7 +290,7 @@ __global__ void __launch_bounds__(MW_THREADS) k_sym_gemm64(seqm_batch b, const d
     __syncthreads();
     buf ^= 1;
   }
-  double *C = Cm + mo;
+  T *C = Cm + mo;
 #pragma unroll
   for (int r = 0; r < 2; ++r)
 #pragma unroll
@@ -301,15 +314,67 @@ inline dim3 gemm64_grid(const seqm_batch &b) {
   return dim3(t, t, (unsigned)b.nmol);
 }
 
-// McWeeny refinement of the density P (FP64): X = P/2, P <- 2 (3 X^2 - 2 X^3), `steps` times.
-// Y, Z: FP64 scratch of the batch's matrix size
-inline void mcweeny(const seqm_batch &b, double *P, double *Y, double *Z, const uint8_t *active, int steps,
-                    cudaStream_t s) {
+// McWeeny step X <- 3 X^2 - 2 X^3 written as X + D (I - 2X) with D = X^2 - X: X^2 in
+// FP64 gives D exactly, and the correction D (I - 2X), a product of a matrix of the size
+// of the idempotency error, is formed in FP32 (relative error ~1e-7 of a term <= |D|),
+// so every step is FP64-accurate at one FP64 product instead of two.
+// Df = float(Y - Z), Bf = float(I - 2 Z)
+__global__ void __launch_bounds__(EW_THREADS) k_mw_split(seqm_batch b, const double *__restrict__ Y,
+                                                         const double *__restrict__ Z, float *__restrict__ Df,
+                                                         float *__restrict__ Bf, const uint8_t *__restrict__ active) {
+  const int m = blockIdx.y;
+  if (active && !active[m]) return;
+  const int n = b.mol_norb[m];
+  const size_t nn = (size_t)n * n, base = (size_t)blockIdx.x * EW_CHUNK;
+  if (base >= nn) return;
+  const size_t mo = b.mol_mat_off[m];
+  for (size_t idx = base + threadIdx.x; idx < nn && idx < base + EW_CHUNK; idx += EW_THREADS) {
+    const size_t i = idx / n;
+    const double z = Z[mo + idx];
+    Df[mo + idx] = (float)(Y[mo + idx] - z);
+    Bf[mo + idx] = (float)((idx == i * n + i ? 1.0 : 0.0) - 2.0 * z);
+  }
+}
+
+// X = 3 X2 - 2 X3 (FP32 McWeeny step)
+__global__ void __launch_bounds__(EW_THREADS) k_mw32(seqm_batch b, const float *__restrict__ X2,
+                                                     const float *__restrict__ X3, float *__restrict__ X,
+                                                     const uint8_t *__restrict__ active) {
+  const int m = blockIdx.y;
+  if (active && !active[m]) return;
+  const int n = b.mol_norb[m];
+  const size_t nn = (size_t)n * n, base = (size_t)blockIdx.x * EW_CHUNK;
+  if (base >= nn) return;
+  const size_t mo = b.mol_mat_off[m];
+  for (size_t idx = base + threadIdx.x; idx < nn && idx < base + EW_CHUNK; idx += EW_THREADS)
+    X[mo + idx] = 3.0f * X2[mo + idx] - 2.0f * X3[mo + idx];
+}
+
+// P = 2 (Z + C)
+__global__ void __launch_bounds__(EW_THREADS) k_mw_update(seqm_batch b, const double *__restrict__ Z,
+                                                          const float *__restrict__ C, double *__restrict__ P,
+                                                          const uint8_t *__restrict__ active) {
+  const int m = blockIdx.y;
+  if (active && !active[m]) return;
+  const int n = b.mol_norb[m];
+  const size_t nn = (size_t)n * n, base = (size_t)blockIdx.x * EW_CHUNK;
+  if (base >= nn) return;
+  const size_t mo = b.mol_mat_off[m];
+  for (size_t idx = base + threadIdx.x; idx < nn && idx < base + EW_CHUNK; idx += EW_THREADS)
+    P[mo + idx] = 2.0 * (Z[mo + idx] + (double)C[mo + idx]);
+}
+
+// McWeeny refinement of the density P (X = P/2), `steps` times.  Y, Z: FP64 scratch of the
+// batch's matrix size; Df, Bf: FP32 scratch of the same size (Y doubles as the FP32 product).
+inline void mcweeny(const seqm_batch &b, double *P, double *Y, double *Z, float *Df, float *Bf,
+                    const uint8_t *active, int steps, cudaStream_t s) {
+  float *Cf = reinterpret_cast<float *>(Y);
   for (int k = 0; k < steps; ++k) {
-    k_ew_axpby<<<ew_grid(b), EW_THREADS, 0, s>>>(b, 0.5, P, 0.0, nullptr, Z, active);  // Z = X
-    k_sym_gemm64<<<gemm64_grid(b), MW_THREADS, 0, s>>>(b, Z, Z, Y, active, nullptr);            // Y = X^2
-    k_sym_gemm64<<<gemm64_grid(b), MW_THREADS, 0, s>>>(b, Y, Z, P, active, nullptr);            // P = X^3
-    k_ew_axpby<<<ew_grid(b), EW_THREADS, 0, s>>>(b, 6.0, Y, -4.0, P, P, active);         // P = 2(3X^2 - 2X^3)
+    k_ew_axpby<<<ew_grid(b), EW_THREADS, 0, s>>>(b, 0.5, P, 0.0, nullptr, Z, active);        // Z = X
+    k_sym_gemm<double><<<gemm64_grid(b), MW_THREADS, 0, s>>>(b, Z, Z, Y, active, nullptr);    // Y = X^2 (FP64)
+    k_mw_split<<<ew_grid(b), EW_THREADS, 0, s>>>(b, Y, Z, Df, Bf, active);                   // D, I - 2X
+    k_sym_gemm<float><<<gemm64_grid(b), MW_THREADS, 0, s>>>(b, Df, Bf, Cf, active, nullptr);  // D (I - 2X)
+    k_mw_update<<<ew_grid(b), EW_THREADS, 0, s>>>(b, Z, Cf, P, active);                      // P = 2(X + ...)
   }
 }
 

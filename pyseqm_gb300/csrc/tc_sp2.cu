@@ -282,7 +282,14 @@ extern "C" int seqm_density_sp2_tc(const seqm_batch *bp, const double *F, double
   }
   if (rc != SEQM_OK) return rc;
   if (status) k_sp2_status<<<(b.nmol + 127) / 128, 128, 0, s>>>(b.nmol, st, active, status);
+  // one FP32 McWeeny step X <- 3X^2 - 2X^3 takes the eigenvalues from the tensor-core level
+  // (~1e-4 off 0/1 at the relaxed stop) to the FP32 accumulation level (~1e-6), so one
+  // FP64-accurate step (mcweeny) then reaches ~1e-11
+  float *X3 = reinterpret_cast<float *>(Y);
+  k_sym_gemm<float><<<gemm64_grid(b), MW_THREADS, 0, s>>>(b, X, X, X2, active, nullptr);
+  k_sym_gemm<float><<<gemm64_grid(b), MW_THREADS, 0, s>>>(b, X2, X, X3, active, nullptr);
+  k_mw32<<<ew_grid(b), EW_THREADS, 0, s>>>(b, X2, X3, X, active);
   k_ew_sym<float><<<ew_grid(b), EW_THREADS, 0, s>>>(b, X, 1.0, 1.0, P, active);  // P = X + X^T
-  mcweeny(b, P, Y, Z, active, mcweeny_steps, s);
+  mcweeny(b, P, Y, Z, X, X2, active, mcweeny_steps, s);  // X, X2 are free after P = X + X^T
   return launch_check();
 }

@@ -68,7 +68,7 @@ class BatchSCF:
         self.sp2_tc_work = None
         # molecules above the Jacobi limit take SP2: "fp64" (plain) or "tc" (tensor cores + FP64 McWeeny)
         self.large_density = "fp64"
-        self.mcweeny_steps = 2
+        self.mcweeny_steps = 1  # FP64-accurate McWeeny steps after the tensor-core SP2 (and one FP32 step)
         self.large_mask = torch.as_tensor((layout.norb > JACOBI_MAX_N).astype(np.uint8), device=dev)
         self.n_large = int((layout.norb > JACOBI_MAX_N).sum())
         self.n_small = layout.nmol - self.n_large

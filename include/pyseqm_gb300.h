@@ -23,6 +23,7 @@
 #ifndef PYSEQM_GB300_H
 #define PYSEQM_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -129,17 +130,17 @@ int seqm_density_sp2(const seqm_batch *b, const double *F, double *P, double *wo
                      const uint8_t *active, int32_t *status, int max_iter, void *stream);
 
 /* SP2 with the squarings on the tensor cores (tcgen05, FP16 hi+lo split products, FP32
- * accumulation in tensor memory), then one FP32 McWeeny step X <- 3X^2 - 2X^3 of X = P/2
- * and mcweeny_steps FP64-accurate ones (X <- X + D (I - 2X), D = X^2 - X, with X^2 in FP64
- * and the small correction product in FP32): idempotency ~1e-11 after one, FP64 level after
- * two.  Same purification and branch test as SP2.py:9-85 (the
- * trace of X^2 for the test is ||X||_F^2 in FP64); a molecule stops when the trace error
- * is below eps, or below 1e-2 and no longer improving (SP2.py:76-80).  No counterpart of
- * the mixed-precision form in the reference.  work: SEQM_SP2_TC_WORK_BYTES(T, nmol, max_norb)
- * bytes with T = mat_off[nmol].  status[m] = SP2 steps, -1 at the step cap.  Synchronises the
- * stream every 4 SP2 steps. */
-#define SEQM_SP2_TC_WORK_BYTES(T, nmol, maxn) \
-  (24 * (size_t)(T) + 16 + 8 * (SEQM_SP2_STATE + 2 * (size_t)(maxn)) * (size_t)(nmol))
+ * accumulation in tensor memory; operands as pre-split tiles moved by bulk asynchronous
+ * copies, the SP2 update fused into the product's epilogue), then one FP32 McWeeny step
+ * X <- 3X^2 - 2X^3 of X = P/2 and mcweeny_steps FP64-accurate ones (X <- X + D (I - 2X),
+ * D = X^2 - X, with X^2 in FP64 and the small correction product in FP32): idempotency
+ * ~1e-11 after one, FP64 level after two.  Same purification and branch test as
+ * SP2.py:9-85 (the trace of X^2 for the test is ||X||_F^2 in FP64); a molecule stops when
+ * the trace error is below eps, or below 1e-2 and no longer improving (SP2.py:76-80).  No
+ * counterpart of the mixed-precision form in the reference.  work: 256-byte aligned,
+ * seqm_sp2_tc_work_bytes(mat_off[nmol], nmol, max_norb) bytes.  At most 65535 molecules.
+ * status[m] = SP2 steps, -1 at the step cap.  Synchronises the stream every 4 SP2 steps. */
+size_t seqm_sp2_tc_work_bytes(int64_t total_matrix_elements, int nmol, int max_norb);
 int seqm_density_sp2_tc(const seqm_batch *b, const double *F, double *P, void *work, double eps,
                         const uint8_t *active, int32_t *status, int max_iter, int mcweeny_steps, void *stream);
 

@@ -1,24 +1,35 @@
 // SP2 purification with the squarings on the 5th-generation tensor cores (tcgen05).
 //
 // Split-precision product: the FP32 iterate X (symmetric, eigenvalues in [0, 1], so
-// |X_ij| <= 1) is split per element into FP16 hi + lo parts, X = Xh + Xl + O(2^-22 |X|)
-// (FP16 keeps 11 significant bits and X needs no range beyond it; below 6e-5 the parts
-// are subnormal, an absolute error under 6e-8), and
+// |X_ij| <= 1) is kept alongside a copy split per element into FP16 hi + lo parts,
+// X = Xh + Xl + O(2^-22 |X|) (FP16 keeps 11 significant bits and X needs no range
+// beyond it; below 6e-5 the parts are subnormal, an absolute error under 6e-8), and
 //     X^2 ~= Xh Xh + Xh Xl + Xl Xh          (Xl Xl ~ 2^-22 |X|^2 dropped)
 // is accumulated in FP32 in tensor memory (TMEM) by three chains of
 // tcgen05.mma.kind::f16 (F16 x F16 -> FP32), M = N = 128, K = 16 per instruction.
-// Only tiles with tile_m <= tile_n are computed; off-diagonal tiles are written
-// with their mirror.  The diagonal tiles add their diagonal to the molecule's
-// trace (FP64).  One CTA (128 threads) per 128x128 output tile; operands are
-// converted FP32 -> FP16 hi/lo while staged into shared memory in the canonical
-// K-major no-swizzle layout (8x8 core matrices, 16-byte rows).
 //
-// The SP2 driver (SP2.py:9-85 semantics, per molecule) then keeps X^2 or 2X - X^2
-// by the trace test; at convergence the FP64 density is refined by McWeeny steps
-// X <- 3 X^2 - 2 X^3 in FP64, restoring idempotency to FP64 level.
+// The split copy is stored as 128-row x 32-k tiles (8 KB per part), already in the
+// canonical K-major no-swizzle operand layout (8x8 core matrices of 16-byte rows, K
+// neighbours 128 B apart, 8-row groups 512 B apart), so one bulk asynchronous copy
+// (cp.async.bulk, completing on an mbarrier) moves an operand tile into shared memory
+// with no conversion.  One CTA per upper 128x128 output tile of a molecule: thread 0
+// issues the copies of a 3-stage ring (A hi/lo, B hi/lo per stage), thread 32 issues
+// the MMAs and frees each stage with tcgen05.commit, and after the last K slice all
+// four warps run the epilogue.  X is symmetric, so the B operand (columns of X) is
+// the same kind of row tile as A.
 //
-// Every wait on an mbarrier is bounded: on time-out the kernel raises an error
-// flag, still releases its TMEM and returns, so the host gets an error status.
+// The epilogue finishes the SP2 step in the same kernel: it forms
+// X' = X^2 or 2X - X^2 (the branch chosen per molecule from tr X and ||X||_F^2 of the
+// previous step, SP2.py:58-64), writes X' in FP32 in place (tile and mirror tile,
+// through a shared-memory transpose), writes the split tiles of X' into the other
+// buffer of a ping-pong pair, and adds tr X' and ||X'||_F^2 (FP64) to the molecule's
+// state.  The driver (SP2.py:9-85 semantics, per molecule) then tests convergence;
+// at convergence the density is refined by one FP32 McWeeny step and FP64-accurate
+// McWeeny steps, restoring idempotency to ~1e-11 or better.
+//
+// Every wait on an mbarrier is bounded: on time-out the kernel raises an error flag,
+// waits (bounded) for its copies in flight, releases its TMEM and returns, so the host
+// gets an error status.
 #include <cuda_fp16.h>
 #include <math.h>
 
@@ -27,11 +38,17 @@
 
 namespace seqm {
 
-constexpr int TC_M = 128, TC_N = 128, TC_K = 64;  // output tile and K slice (16-bit elements)
+constexpr int TC_M = 128, TC_N = 128;               // output tile
+constexpr int TC_KT = 32;                           // k width of a stored split tile and of a pipeline stage
+constexpr int TC_STAGES = 3;
 constexpr int TC_THREADS = 128;
-constexpr int TILE_BYTES = TC_M * TC_K * 2;  // one 16-bit operand tile: 16 KB
-constexpr uint32_t TC_FMT = 0;                // kind::f16 operand format: 0 = F16 (1 would be BF16)
-constexpr uint32_t WAIT_LIMIT = 1u << 26;     // mbarrier polls before giving up
+constexpr int SPLIT_TILE_BYTES = TC_M * TC_KT * 2;  // 8 KB: 128 rows x 32 k, FP16
+constexpr int STAGE_BYTES = 4 * SPLIT_TILE_BYTES;   // A hi, A lo, B hi, B lo
+constexpr int EPI_LD = TC_N + 1;                    // FP32 staging row stride: rows and columns conflict-free
+constexpr size_t TC_SMEM = (size_t)TC_STAGES * STAGE_BYTES + 1024;  // + alignment slack
+static_assert(TC_M * EPI_LD * 4 <= TC_STAGES * STAGE_BYTES, "epilogue staging reuses the pipeline buffers");
+constexpr uint32_t TC_FMT = 0;                      // kind::f16 operand format: 0 = F16 (1 would be BF16)
+constexpr uint32_t WAIT_LIMIT = 1u << 26;           // mbarrier polls before giving up
 
 // ---------------------------------------------------------------- PTX wrappers
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -49,7 +66,8 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t addr, uint32_t lbo, uint3
   return d;
 }
 
-// instruction descriptor: D = F32, A = B = F16, both K-major, N = 128, M = 128
+// instruction descriptor: D = F32, A = B = F16 (same type for both, as kind::f16 requires),
+// both K-major, N = 128, M = 128
 __host__ __device__ constexpr uint32_t make_idesc() {
   return (1u << 4) | (TC_FMT << 7) | (TC_FMT << 10) | ((uint32_t)(TC_N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
 }
@@ -86,7 +104,7 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
   asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols));
 }
 
-__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+__device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
           tmem_d),
@@ -113,127 +131,319 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// byte offset of element (row, k) of a 128 x 64 16-bit tile in the canonical K-major
-// no-swizzle layout: 8x8 core matrices of 128 contiguous bytes, K-neighbours 128 B
-// apart (LBO), M-neighbours 8 * 128 = 1024 B apart (SBO)
-__device__ __forceinline__ uint32_t tile_off(int row, int k) {
-  return (uint32_t)((row >> 3) * 1024 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
 
-// stage rows [r0, r0+128) x cols [k0, k0+64) of X (FP32, n x n, row-major) as FP16 hi and lo
-__device__ __forceinline__ void stage_split(const float *__restrict__ X, int n, int r0, int k0, uint8_t *hi,
-                                            uint8_t *lo) {
-  for (int v = threadIdx.x; v < TC_M * (TC_K / 8); v += TC_THREADS) {
-    const int row = v >> 3, kc = (v & 7) * 8;
-    const int gr = r0 + row;
-    __align__(16) __half h[8], l[8];
+// bulk asynchronous copy global -> this CTA's shared memory, completing `bytes` on `bar`
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  uint64_t g;
+  asm volatile("cvta.to.global.u64 %0, %1;" : "=l"(g) : "l"(src));
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(g), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+// byte offset of element (row, k) of a 128 x 32 FP16 tile in the canonical K-major
+// no-swizzle layout: 8x8 core matrices of 128 contiguous bytes, K neighbours 128 B
+// apart (LBO), 8-row groups 4 * 128 = 512 B apart (SBO)
+__host__ __device__ __forceinline__ uint32_t tile_off(int row, int k) {
+  return (uint32_t)((row >> 3) * 512 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+constexpr uint32_t TC_LBO = 128, TC_SBO = 512;
+
+__host__ __device__ __forceinline__ int64_t split_tiles(int n) {
+  return (int64_t)((n + TC_M - 1) / TC_M) * ((n + TC_KT - 1) / TC_KT);
+}
+
+// 8 FP32 values -> FP16 hi and lo parts, stored as 16 bytes each
+__device__ __forceinline__ void split8(const float *v, uint8_t *hi, uint8_t *lo) {
+  __align__(16) __half h[8], l[8];
 #pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      const int gk = k0 + kc + e;
-      const float x = (gr < n && gk < n) ? X[(size_t)gr * n + gk] : 0.0f;
-      const __half xh = __float2half_rn(x);
-      h[e] = xh;
-      l[e] = __float2half_rn(x - __half2float(xh));
-    }
-    const uint32_t off = tile_off(row, kc);
-    *reinterpret_cast<uint4 *>(hi + off) = *reinterpret_cast<const uint4 *>(h);
-    *reinterpret_cast<uint4 *>(lo + off) = *reinterpret_cast<const uint4 *>(l);
+  for (int e = 0; e < 8; ++e) {
+    const __half xh = __float2half_rn(v[e]);
+    h[e] = xh;
+    l[e] = __float2half_rn(v[e] - __half2float(xh));
   }
+  *reinterpret_cast<uint4 *>(hi) = *reinterpret_cast<const uint4 *>(h);
+  *reinterpret_cast<uint4 *>(lo) = *reinterpret_cast<const uint4 *>(l);
 }
 
-// X2 = X X (split FP16, FP32 accumulate) for the molecules with run[m] != 0
-__global__ void __launch_bounds__(TC_THREADS) k_tc_square(seqm_batch b, const float *__restrict__ X,
-                                                          float *__restrict__ X2, const int64_t *__restrict__ off,
-                                                          const double *__restrict__ st, double *__restrict__ trace,
-                                                          int *__restrict__ err) {
+// exclusive prefix sum of each molecule's split-tile count (one CTA of 1024 threads);
+// xs_off[nmol] = total
+__global__ void __launch_bounds__(1024) k_tc_tile_offsets(seqm_batch b, int64_t *__restrict__ xs_off) {
+  __shared__ int64_t part[1024];
+  const int per = (b.nmol + 1023) / 1024;
+  const int m0 = threadIdx.x * per, m1 = min(b.nmol, m0 + per);
+  int64_t s = 0;
+  for (int m = m0; m < m1; ++m) s += split_tiles(b.mol_norb[m]);
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    const int64_t v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int64_t base = threadIdx.x ? part[threadIdx.x - 1] : 0;
+  for (int m = m0; m < m1; ++m) {
+    xs_off[m] = base;
+    base += split_tiles(b.mol_norb[m]);
+  }
+  if (threadIdx.x == 1023) xs_off[b.nmol] = part[1023];
+}
+
+// split tiles of the FP32 X of running molecules: CTA (kb, rb, m) writes tile (rb, kb)
+__global__ void __launch_bounds__(128) k_tc_split(seqm_batch b, const float *__restrict__ X, uint8_t *__restrict__ Xh,
+                                                  uint8_t *__restrict__ Xl, const int64_t *__restrict__ xs_off,
+                                                  const double *__restrict__ st) {
   const int m = blockIdx.z;
   if (st[SP2_NS * m + S_RUN] == 0.0) return;
   const int n = b.mol_norb[m];
-  const int tm = blockIdx.y, tn = blockIdx.x;
-  if (tm > tn || tm * TC_M >= n || tn * TC_N >= n) return;
-  extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t *Ah = smem, *Al = smem + TILE_BYTES, *Bh = smem + 2 * TILE_BYTES, *Bl = smem + 3 * TILE_BYTES;
-  __shared__ __align__(8) uint64_t bar;
+  const int nb = (n + TC_M - 1) / TC_M, nk = (n + TC_KT - 1) / TC_KT;
+  const int rb = blockIdx.y, kb = blockIdx.x;
+  if (rb >= nb || kb >= nk) return;
+  const float *Xm = X + b.mol_mat_off[m];
+  const size_t tile = (size_t)(xs_off[m] + (int64_t)rb * nk + kb) * SPLIT_TILE_BYTES;
+  for (int g = threadIdx.x; g < TC_M * TC_KT / 8; g += 128) {
+    const int row = g >> 2, kc = (g & 3) * 8;
+    const int gr = rb * TC_M + row, gk = kb * TC_KT + kc;
+    float v[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) v[e] = (gr < n && gk + e < n) ? Xm[(size_t)gr * n + gk + e] : 0.0f;
+    split8(v, Xh + tile + tile_off(row, kc), Xl + tile + tile_off(row, kc));
+  }
+}
+
+// One SP2 step of every running molecule: X' = X^2 or 2X - X^2 (see the file comment).
+// Grid: (upper tiles of the largest molecule, molecules); block: 128 threads.
+__global__ void __launch_bounds__(TC_THREADS) k_tc_sp2_step(seqm_batch b, float *__restrict__ X,
+                                                            const uint8_t *__restrict__ Xh,
+                                                            const uint8_t *__restrict__ Xl, uint8_t *__restrict__ Yh,
+                                                            uint8_t *__restrict__ Yl,
+                                                            const int64_t *__restrict__ xs_off,
+                                                            double *__restrict__ st, int *__restrict__ err) {
+  const int m = blockIdx.y;
+  double *s = st + SP2_NS * m;
+  if (s[S_RUN] == 0.0) return;
+  const int n = b.mol_norb[m];
+  const int nb = (n + TC_M - 1) / TC_M, nk = (n + TC_KT - 1) / TC_KT;
+  // upper tile (tm <= tn) from the linear index t = tn (tn + 1) / 2 + tm
+  const int t = blockIdx.x;
+  int tn = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+  while ((tn + 1) * (tn + 2) / 2 <= t) ++tn;
+  while (tn * (tn + 1) / 2 > t) --tn;
+  const int tm = t - tn * (tn + 1) / 2;
+  if (tn >= nb) return;
+
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
+  __shared__ __align__(8) uint64_t full[TC_STAGES], empty[TC_STAGES], done;
   __shared__ uint32_t tmem_base;
-  __shared__ int failed;
-  const float *Xm = X + off[m];
+  __shared__ int failed, sh_issued, sh_consumed;
+  __shared__ double red[2][TC_THREADS / 32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (warp == 0) tmem_alloc(&tmem_base, TC_N);
   if (threadIdx.x == 0) {
-    mbar_init(&bar, 1);
+    for (int i = 0; i < TC_STAGES; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    mbar_init(&done, 1);
     failed = 0;
+    sh_issued = 0;
+    sh_consumed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem_d = tmem_base;
-  const uint32_t idesc = make_idesc();
-  uint32_t phase = 0;
-  const int nk = (n + TC_K - 1) / TC_K;
-  for (int kt = 0; kt < nk; ++kt) {
-    stage_split(Xm, n, tm * TC_M, kt * TC_K, Ah, Al);
-    stage_split(Xm, n, tn * TC_N, kt * TC_K, Bh, Bl);
-    fence_async_smem();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      tc_fence_after();
-      const uint32_t ah = smem_u32(Ah), al = smem_u32(Al), bh = smem_u32(Bh), bl = smem_u32(Bl);
-#pragma unroll
-      for (int kk = 0; kk < TC_K / 16; ++kk) {  // K = 16 per MMA: two core matrices (256 B) along K
-        const uint32_t ko = kk * 256;
-        umma_bf16(tmem_d, make_desc(ah + ko, 128, 1024), make_desc(bh + ko, 128, 1024), idesc, (kt | kk) != 0);
-        umma_bf16(tmem_d, make_desc(ah + ko, 128, 1024), make_desc(bl + ko, 128, 1024), idesc, 1);
-        umma_bf16(tmem_d, make_desc(al + ko, 128, 1024), make_desc(bh + ko, 128, 1024), idesc, 1);
+  const uint8_t *tiles_h = Xh + (size_t)xs_off[m] * SPLIT_TILE_BYTES;
+  const uint8_t *tiles_l = Xl + (size_t)xs_off[m] * SPLIT_TILE_BYTES;
+  const size_t rowA = (size_t)tm * nk * SPLIT_TILE_BYTES, rowB = (size_t)tn * nk * SPLIT_TILE_BYTES;
+
+  if (threadIdx.x == 0) {
+    // producer: the four operand tiles of K slice kb into stage kb % TC_STAGES
+    for (int kb = 0; kb < nk; ++kb) {
+      const int si = kb % TC_STAGES;
+      if (kb >= TC_STAGES && !mbar_wait(&empty[si], ((kb / TC_STAGES) - 1) & 1)) {
+        atomicExch(&failed, 1);
+        break;
       }
-      umma_commit(&bar);
+      uint8_t *dst = smem + si * STAGE_BYTES;
+      const size_t ko = (size_t)kb * SPLIT_TILE_BYTES;
+      mbar_expect_tx(&full[si], STAGE_BYTES);
+      bulk_g2s(dst, tiles_h + rowA + ko, SPLIT_TILE_BYTES, &full[si]);
+      bulk_g2s(dst + SPLIT_TILE_BYTES, tiles_l + rowA + ko, SPLIT_TILE_BYTES, &full[si]);
+      bulk_g2s(dst + 2 * SPLIT_TILE_BYTES, tiles_h + rowB + ko, SPLIT_TILE_BYTES, &full[si]);
+      bulk_g2s(dst + 3 * SPLIT_TILE_BYTES, tiles_l + rowB + ko, SPLIT_TILE_BYTES, &full[si]);
+      sh_issued = kb + 1;
     }
-    // the staging buffers are rewritten next iteration: wait for this slice's MMAs
-    if (!mbar_wait(&bar, phase)) atomicExch(&failed, 1);
-    phase ^= 1;
-    __syncthreads();
-    if (failed) break;
+  } else if (threadIdx.x == 32) {
+    // MMA issuer: 3 products x 2 instructions (K = 16 each) per stage, then free the stage
+    const uint32_t idesc = make_idesc();
+    for (int kb = 0; kb < nk; ++kb) {
+      const int si = kb % TC_STAGES;
+      if (!mbar_wait(&full[si], (kb / TC_STAGES) & 1)) {
+        atomicExch(&failed, 1);
+        break;
+      }
+      tc_fence_after();
+      const uint32_t ah = smem_u32(smem + si * STAGE_BYTES), al = ah + SPLIT_TILE_BYTES;
+      const uint32_t bh = ah + 2 * SPLIT_TILE_BYTES, bl = ah + 3 * SPLIT_TILE_BYTES;
+#pragma unroll
+      for (int kk = 0; kk < TC_KT / 16; ++kk) {
+        const uint32_t ko = kk * 256;  // two core matrices along K
+        umma_f16(tmem_d, make_desc(ah + ko, TC_LBO, TC_SBO), make_desc(bh + ko, TC_LBO, TC_SBO), idesc,
+                 (kb | kk) != 0);
+        umma_f16(tmem_d, make_desc(ah + ko, TC_LBO, TC_SBO), make_desc(bl + ko, TC_LBO, TC_SBO), idesc, 1);
+        umma_f16(tmem_d, make_desc(al + ko, TC_LBO, TC_SBO), make_desc(bh + ko, TC_LBO, TC_SBO), idesc, 1);
+      }
+      umma_commit(&empty[si]);
+      sh_consumed = kb + 1;
+    }
+    umma_commit(&done);  // arrives once every MMA issued above has completed
   }
-  tc_fence_after();
-  if (!failed) {
-    // epilogue: warp w owns accumulator rows 32w..32w+31 (TMEM lanes)
-    const int row = tm * TC_M + warp * 32 + lane;
-    double tr = 0.0;
-    float *Y = X2 + off[m];
+  __syncwarp();
+  if (!mbar_wait(&done, 0)) atomicExch(&failed, 1);
+  __syncthreads();
+  if (failed) {
+    // let the copies still in flight land before the shared memory is released
+    if (threadIdx.x == 0)
+      for (int kb = sh_consumed; kb < sh_issued; ++kb) mbar_wait(&full[kb % TC_STAGES], (kb / TC_STAGES) & 1);
+    if (threadIdx.x == 0) atomicExch(err, SEQM_E_CUDA);
+  } else {
+    tc_fence_after();
+    float *stg = reinterpret_cast<float *>(smem);  // 128 x EPI_LD staging; the stages are idle now
+    const size_t mo = b.mol_mat_off[m];
+    float *Xm = X + mo;
+    // old X tile into staging (coalesced rows)
+    for (int r = warp; r < TC_M; r += TC_THREADS / 32) {
+      const int gr = tm * TC_M + r;
+#pragma unroll
+      for (int c = lane; c < TC_N; c += 32) {
+        const int gc = tn * TC_N + c;
+        stg[r * EPI_LD + c] = (gr < n && gc < n) ? Xm[(size_t)gr * n + gc] : 0.0f;
+      }
+    }
+    __syncthreads();
+    // X' row by row: thread i owns accumulator row i (TMEM lane i)
+    const double nocc = (double)b.mol_nocc[m], t1 = s[S_T1], t2 = s[S_T2];
+    const bool sq = fabs(t2 - nocc) < fabs(2.0 * t1 - t2 - nocc);
+    const int i = threadIdx.x, gi = tm * TC_M + i;
+    double tr = 0.0, f2 = 0.0;
 #pragma unroll 1
     for (int c0 = 0; c0 < TC_N; c0 += 32) {
       float v[32];
       tmem_ld32(tmem_d + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-      if (row < n) {
 #pragma unroll
-        for (int i = 0; i < 32; ++i) {
-          const int col = tn * TC_N + c0 + i;
-          if (col < n) {
-            Y[(size_t)row * n + col] = v[i];
-            if (tm != tn) Y[(size_t)col * n + row] = v[i];
-            else if (col == row) tr += (double)v[i];
-          }
-        }
+      for (int j = 0; j < 32; ++j) {
+        const int c = c0 + j;
+        const float x = stg[i * EPI_LD + c];
+        float y = sq ? v[j] : 2.0f * x - v[j];
+        if (gi >= n || tn * TC_N + c >= n) y = 0.0f;  // keep the padding of the split tiles zero
+        stg[i * EPI_LD + c] = y;
+        f2 += (double)y * (double)y;
+        if (tm == tn && c == i) tr += (double)y;
       }
     }
-    if (tm == tn && trace) {
+    if (tm != tn) f2 *= 2.0;  // the mirror tile
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
-      if (lane == 0) atomicAdd(&trace[m], tr);
+    for (int o = 16; o > 0; o >>= 1) {
+      tr += __shfl_xor_sync(0xffffffffu, tr, o);
+      f2 += __shfl_xor_sync(0xffffffffu, f2, o);
     }
-  } else if (threadIdx.x == 0) {
-    atomicExch(err, SEQM_E_CUDA);
+    if (lane == 0) {
+      red[0][warp] = tr;
+      red[1][warp] = f2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double a = 0.0, c = 0.0;
+      for (int w = 0; w < TC_THREADS / 32; ++w) {
+        a += red[0][w];
+        c += red[1][w];
+      }
+      if (a != 0.0) atomicAdd(&s[S_ACC_T], a);
+      if (c != 0.0) atomicAdd(&s[S_ACC_F], c);
+    }
+    // X' in FP32: the tile and its mirror, coalesced rows
+    for (int r = warp; r < TC_M; r += TC_THREADS / 32) {
+      const int gr = tm * TC_M + r, gr2 = tn * TC_M + r;
+#pragma unroll
+      for (int c = lane; c < TC_N; c += 32) {
+        const int gc = tn * TC_N + c, gc2 = tm * TC_N + c;
+        if (gr < n && gc < n) Xm[(size_t)gr * n + gc] = stg[r * EPI_LD + c];
+        if (tm != tn && gr2 < n && gc2 < n) Xm[(size_t)gr2 * n + gc2] = stg[c * EPI_LD + r];
+      }
+    }
+    // split tiles of X': tile (tm, 4 tn + q) and mirror tile (tn, 4 tm + q), 8 k per store
+    uint8_t *oh = Yh + (size_t)xs_off[m] * SPLIT_TILE_BYTES, *ol = Yl + (size_t)xs_off[m] * SPLIT_TILE_BYTES;
+    for (int g = threadIdx.x; g < TC_M * (TC_N / 8); g += TC_THREADS) {
+      const int r = g >> 4, cg = (g & 15) * 8, q = cg / TC_KT, kc = cg % TC_KT;
+      float v[8];
+      const int kb1 = (tn * TC_N) / TC_KT + q;
+      if (kb1 < nk) {
+#pragma unroll
+        for (int e = 0; e < 8; ++e) v[e] = stg[r * EPI_LD + cg + e];
+        const size_t tile = ((size_t)tm * nk + kb1) * SPLIT_TILE_BYTES + tile_off(r, kc);
+        split8(v, oh + tile, ol + tile);
+      }
+      const int kb2 = (tm * TC_N) / TC_KT + q;
+      if (tm != tn && kb2 < nk) {
+#pragma unroll
+        for (int e = 0; e < 8; ++e) v[e] = stg[(cg + e) * EPI_LD + r];
+        const size_t tile = ((size_t)tn * nk + kb2) * SPLIT_TILE_BYTES + tile_off(r, kc);
+        split8(v, oh + tile, ol + tile);
+      }
+    }
   }
   tc_fence_before();
   __syncthreads();
   if (warp == 0) tmem_dealloc(tmem_d, TC_N);
 }
 
+// ----------------------------------------------------------------- work layout
+struct TcWork {
+  size_t x, x2, y, z, st, rowlo, rowhi, cnt, xs_off, xs[4], total;
+};
+
+inline TcWork tc_work_layout(int64_t T, int nmol, int maxn) {
+  TcWork w{};
+  size_t o = 0;
+  auto take = [&](size_t bytes, size_t align) {
+    o = (o + align - 1) / align * align;
+    const size_t r = o;
+    o += bytes;
+    return r;
+  };
+  const size_t t = (size_t)(T > 0 ? T : 0), nm = (size_t)(nmol > 0 ? nmol : 0), mx = (size_t)(maxn > 0 ? maxn : 0);
+  w.x = take(4 * t, 256);
+  w.x2 = take(4 * t, 256);
+  w.y = take(8 * t, 256);
+  w.z = take(8 * t, 256);
+  w.st = take(8 * SP2_NS * nm, 256);
+  w.rowlo = take(8 * nm * mx, 256);
+  w.rowhi = take(8 * nm * mx, 256);
+  w.cnt = take(16, 256);
+  w.xs_off = take(8 * (nm + 1), 256);
+  // sum over molecules of ceil(n/128) ceil(n/32) <= (T + nmol (159 maxn + 3937)) / 4096
+  const size_t tiles = (t + nm * (159 * mx + 3937) + 4095) / 4096;
+  for (int q = 0; q < 4; ++q) w.xs[q] = take(tiles * SPLIT_TILE_BYTES, 1024);
+  w.total = o;
+  return w;
+}
 
 }  // namespace seqm
 
 using namespace seqm;
+
+extern "C" size_t seqm_sp2_tc_work_bytes(int64_t total_matrix_elements, int nmol, int max_norb) {
+  return tc_work_layout(total_matrix_elements, nmol, max_norb).total;
+}
 
 extern "C" int seqm_density_sp2_tc(const seqm_batch *bp, const double *F, double *P, void *work, double eps,
                                    const uint8_t *active, int32_t *status, int max_iter, int mcweeny_steps,
@@ -241,38 +451,44 @@ extern "C" int seqm_density_sp2_tc(const seqm_batch *bp, const double *F, double
   if (!bp || !work || !F || !P) return SEQM_E_ARG;
   seqm_batch b = *bp;
   if (b.nmol == 0) return SEQM_OK;
+  if (b.nmol > 65535) return SEQM_E_TOO_LARGE;  // molecules are the grid's y dimension
+  if ((reinterpret_cast<uintptr_t>(work) & 255) != 0) return SEQM_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   eps = eps > 1.0e-3 ? 1.0e-3 : (eps < 1.0e-7 ? 1.0e-7 : eps);
   int64_t total = 0;
   if (cudaMemcpyAsync(&total, b.mol_mat_off + b.nmol, sizeof(int64_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)
     return SEQM_E_CUDA;
-  // work: X f32 [T] | X2 f32 [T] | (pad) | Y f64 [T] | Z f64 [T] | state [SP2_NS nmol] |
-  //       row bounds 2 [nmol max_norb] | counters i32 [2]   (FP32 blocks share the FP64 offsets)
-  float *X = static_cast<float *>(work);
-  float *X2 = X + total;
-  double *Y = reinterpret_cast<double *>(X2 + total + (total & 1));
-  double *Z = Y + total;
-  double *st = Z + total;
-  double *rowlo = st + (size_t)SP2_NS * b.nmol;
-  double *rowhi = rowlo + (size_t)b.nmol * b.max_norb;
-  int *cnt = reinterpret_cast<int *>(rowhi + (size_t)b.nmol * b.max_norb);
+  const TcWork w = tc_work_layout(total, b.nmol, b.max_norb);
+  uint8_t *base = static_cast<uint8_t *>(work);
+  float *X = reinterpret_cast<float *>(base + w.x);
+  float *X2 = reinterpret_cast<float *>(base + w.x2);
+  double *Y = reinterpret_cast<double *>(base + w.y);
+  double *Z = reinterpret_cast<double *>(base + w.z);
+  double *st = reinterpret_cast<double *>(base + w.st);
+  double *rowlo = reinterpret_cast<double *>(base + w.rowlo);
+  double *rowhi = reinterpret_cast<double *>(base + w.rowhi);
+  int *cnt = reinterpret_cast<int *>(base + w.cnt);
+  int64_t *xs_off = reinterpret_cast<int64_t *>(base + w.xs_off);
+  uint8_t *xs[4] = {base + w.xs[0], base + w.xs[1], base + w.xs[2], base + w.xs[3]};  // hi, lo of two buffers
   if (cudaMemsetAsync(cnt, 0, 2 * sizeof(int), s) != cudaSuccess) return SEQM_E_CUDA;
   k_sp2_rows<<<rows_grid(b), 256, 0, s>>>(b, F, rowlo, rowhi, active);
   k_sp2_bounds<<<b.nmol, 256, 0, s>>>(b, rowlo, rowhi, st, active);
   k_sp2_scale<float><<<ew_grid(b), EW_THREADS, 0, s>>>(b, F, X, st);
   k_sp2_start<<<(b.nmol + 127) / 128, 128, 0, s>>>(b, st);
-  const int tiles = (b.max_norb + TC_M - 1) / TC_M;
-  const size_t smem = 4 * TILE_BYTES + 1024;
-  if (cudaFuncSetAttribute(k_tc_square, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  k_tc_tile_offsets<<<1, 1024, 0, s>>>(b, xs_off);
+  const int nb = (b.max_norb + TC_M - 1) / TC_M, nk = (b.max_norb + TC_KT - 1) / TC_KT;
+  k_tc_split<<<dim3(nk, nb, b.nmol), 128, 0, s>>>(b, X, xs[0], xs[1], xs_off, st);
+  if (cudaFuncSetAttribute(k_tc_sp2_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM) != cudaSuccess)
     return SEQM_E_CUDA;
-  const dim3 grid(tiles, tiles, b.nmol);
-  int rc = SEQM_OK;
+  const dim3 grid((unsigned)(nb * (nb + 1) / 2), (unsigned)b.nmol);
+  int rc = SEQM_OK, cur = 0;
   for (int it = 0; it < max_iter; ++it) {
     if (cudaMemsetAsync(cnt, 0, sizeof(int), s) != cudaSuccess) { rc = SEQM_E_CUDA; break; }
-    k_tc_square<<<grid, TC_THREADS, smem, s>>>(b, X, X2, b.mol_mat_off, st, nullptr, cnt + 1);
-    k_sp2_step<float><<<ew_grid(b), EW_THREADS, 0, s>>>(b, X, X2, st);
+    k_tc_sp2_step<<<grid, TC_THREADS, TC_SMEM, s>>>(b, X, xs[2 * cur], xs[2 * cur + 1], xs[2 - 2 * cur],
+                                                    xs[3 - 2 * cur], xs_off, st, cnt + 1);
     k_sp2_check<<<(b.nmol + 127) / 128, 128, 0, s>>>(b, st, eps, 1, cnt);
+    cur ^= 1;
     if ((it + 1) % SP2_SYNC_EVERY != 0 && it + 1 < max_iter) continue;  // finished molecules skip the extra steps
     int h[2] = {0, 0};
     if (cudaMemcpyAsync(h, cnt, 2 * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||

@@ -28,7 +28,7 @@ PAR = {n: i for i, n in enumerate(PAR_NAMES)}
 
 EXPORTS = ["seqm_hcore", "seqm_fock", "seqm_density_jacobi", "seqm_density_jacobi_noalloc", "seqm_density_sp2",
            "seqm_density_sp2_tc", "seqm_mix", "seqm_energy_error",
-           "seqm_initial_density", "seqm_pair_sum", "seqm_energy_grad", "seqm_version"]
+           "seqm_initial_density", "seqm_pair_sum", "seqm_energy_grad", "seqm_sp2_tc_work_bytes", "seqm_version"]
 
 _P = ctypes.c_void_p
 
@@ -82,6 +82,8 @@ def load(path=None):
         fn = getattr(lib, name)
         fn.argtypes = args
         fn.restype = ctypes.c_int
+    lib.seqm_sp2_tc_work_bytes.argtypes = [ctypes.c_int64, i32, i32]
+    lib.seqm_sp2_tc_work_bytes.restype = ctypes.c_size_t
     lib.seqm_version.argtypes = []
     lib.seqm_version.restype = ctypes.c_char_p
     _lib = lib

@@ -164,7 +164,7 @@ class BatchSCF:
     def _sp2_tc(self, out, eps, active, subset=False):
         b, nm, maxn, act, status = self._sp2_target(active, subset)
         T = int(self.L.mat_off[-1])
-        nbytes = 24 * T + 16 + 8 * (11 + 2 * maxn) * nm  # SEQM_SP2_TC_WORK_BYTES
+        nbytes = int(self.lib.seqm_sp2_tc_work_bytes(T, nm, maxn))
         if self.sp2_tc_work is None or self.sp2_tc_work.numel() < nbytes:
             self.sp2_tc_work = torch.empty(nbytes, dtype=torch.uint8, device=self.L.device)
         self.launches += 1

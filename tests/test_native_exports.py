@@ -11,7 +11,7 @@ HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))
 
 def _declared():
     src = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char \*)\s*(seqm_\w+)\s*\(", src, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|size_t|const char \*)\s*(seqm_\w+)\s*\(", src, re.M)))
 
 
 def test_header_matches_binding_list():
@@ -25,3 +25,13 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(lib, name), name
     native.load(path)
     assert b"sm_103a" in native.load().seqm_version()
+
+
+def test_sp2_tc_work_size_is_host_computable():
+    """The tensor-core SP2 work size is a pure host function (no GPU needed) and grows with
+    the matrix total, the molecule count and the largest basis."""
+    lib = native.load(build.build())
+    a = lib.seqm_sp2_tc_work_bytes(100 * 100, 1, 100)
+    assert a > 32 * 100 * 100
+    assert lib.seqm_sp2_tc_work_bytes(2 * 100 * 100, 2, 100) > a
+    assert lib.seqm_sp2_tc_work_bytes(100 * 100, 1, 200) > a

@@ -255,11 +255,11 @@ __device__ double block_max(double v, double *red) {
 // not converged <=> |dE| > eps or ||dP||_F/(4 natoms) > 2 eps or max|dP| > 15 eps,
 // the density terms refreshed only when the energy test passes.
 //
-// One cluster of cs CTAs per molecule.  The molecule's elements are cut into
-// EE_SLICES interleaved slices (slice s: elements s*NT + t + k*EE_SLICES*NT); CTA
-// rank r sums the slices s with s % cs == r, and rank 0 adds the slice sums in
-// slice order through distributed shared memory, so the result does not depend
-// on cs.
+// One cluster of cs CTAs per molecule.  The molecule's elements are cut into ns
+// interleaved slices (slice s: elements s*NT + t + k*ns*NT; ns grows with the
+// molecule's size up to EE_SLICES); CTA rank r sums the slices s with s % cs == r,
+// and rank 0 adds the slice sums in slice order through distributed shared memory,
+// so the result does not depend on cs.
 __device__ __forceinline__ void finish_error(const seqm_batch &b, int m, double e, double fro, double mx, double *Eelec,
                                         double *err, double *dm_err, double *dm_el, uint8_t *active, double eps) {
   double de = e - Eelec[m];
@@ -289,8 +289,10 @@ __global__ void __launch_bounds__(NT_RED) k_energy_error(seqm_batch b, const dou
   const int norb = b.mol_norb[m];
   const size_t mo = b.mol_mat_off[m], nn = (size_t)norb * norb;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const size_t stride = (size_t)EE_SLICES * NT_RED;
-  for (int s = r; s < EE_SLICES; s += cs) {  // the slices of this CTA
+  // slices of this molecule: one per 8192 elements, at most EE_SLICES (a function of its size only)
+  const int ns = (int)min((size_t)EE_SLICES, (nn + 8191) / 8192);
+  const size_t stride = (size_t)ns * NT_RED;
+  for (int s = r; s < ns; s += cs) {  // the slices of this CTA
     double e = 0.0, fro = 0.0, mx = 0.0;
     for (size_t i = (size_t)s * NT_RED + threadIdx.x; i < nn; i += EE_UNROLL * stride) {
       double pv[EE_UNROLL], hf[EE_UNROLL], po[EE_UNROLL];
@@ -323,7 +325,7 @@ __global__ void __launch_bounds__(NT_RED) k_energy_error(seqm_batch b, const dou
     }
   }
   __syncthreads();
-  if (threadIdx.x < 3 * EE_SLICES && (threadIdx.x / 3) % cs == r) {
+  if (threadIdx.x < 3 * ns && (threadIdx.x / 3) % cs == r) {
     const int j = threadIdx.x;
     double v = wred[0][j];
     for (int w = 1; w < NT_RED / 32; ++w) v = (j % 3 == 2) ? fmax(v, wred[w][j]) : v + wred[w][j];
@@ -332,7 +334,7 @@ __global__ void __launch_bounds__(NT_RED) k_energy_error(seqm_batch b, const dou
   cl.sync();
   if (r == 0 && threadIdx.x == 0) {
     double e = 0.0, fro = 0.0, mx = 0.0;
-    for (int s = 0; s < EE_SLICES; ++s) {
+    for (int s = 0; s < ns; ++s) {
       const double *q = cl.map_shared_rank(part, s % cs);
       e += q[3 * s];
       fro += q[3 * s + 1];

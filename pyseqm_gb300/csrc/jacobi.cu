@@ -30,7 +30,7 @@
 
 namespace seqm {
 
-constexpr int NT_J = 256;
+constexpr int NT_J = 512;
 constexpr int JMAX_N = 160;
 constexpr int JMAX_P = JMAX_N / 2;
 

@@ -334,11 +334,14 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_sp2_step(seqm_batch b, float 
     const double nocc = (double)b.mol_nocc[m], t1 = s[S_T1], t2 = s[S_T2];
     const bool sq = fabs(t2 - nocc) < fabs(2.0 * t1 - t2 - nocc);
     const int i = threadIdx.x, gi = tm * TC_M + i;
+    // ||X'||_F^2 in FP32 per 32 columns, then FP64 (the sums of squares carry the tensor-core
+    // noise of X' anyway; the trace, which decides convergence, is summed in FP64)
     double tr = 0.0, f2 = 0.0;
 #pragma unroll 1
     for (int c0 = 0; c0 < TC_N; c0 += 32) {
       float v[32];
       tmem_ld32(tmem_d + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      float q2 = 0.0f;
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
         const int c = c0 + j;
@@ -346,9 +349,10 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_sp2_step(seqm_batch b, float 
         float y = sq ? v[j] : 2.0f * x - v[j];
         if (gi >= n || tn * TC_N + c >= n) y = 0.0f;  // keep the padding of the split tiles zero
         stg[i * EPI_LD + c] = y;
-        f2 += (double)y * (double)y;
+        q2 = fmaf(y, y, q2);
         if (tm == tn && c == i) tr += (double)y;
       }
+      f2 += (double)q2;
     }
     if (tm != tn) f2 *= 2.0;  // the mirror tile
 #pragma unroll

@@ -97,11 +97,18 @@ int seqm_fock(const seqm_batch *b, const double *P, const double *H, const doubl
  * on entry) took >= mixed_threshold sweeps, first sweep in FP32 (A and the rotation product
  * in shared memory), then lift the vectors to FP64 (one Newton-Schulz re-orthonormalisation)
  * and finish with FP64 sweeps; 0 = FP64 sweeps only.  The result is FP64-accurate either way.
+ * density_only != 0 (an SCF iteration: needs P, evecs NULL): once A = V F V^T is nearly
+ * diagonal (largest occupied-virtual element over the HOMO-LUMO gap of its diagonal <= 1e-5,
+ * directly from a warm start or after the FP32 sweeps), P is formed from the first-order
+ * occupied-virtual rotation of the smaller set, re-orthonormalised (Loewdin), instead of
+ * further FP64 sweeps; error second order in that ratio (<= ~1e-10 in P); evals are then the
+ * diagonal of A.  0 = always sweep to the FP64 tolerance (eigenpairs for output).
  * status[m]: sweeps taken (FP32 + FP64), or -1 if the FP64 sweep cap was hit, or -2 for an
  * active molecule with norb > 160, which is left untouched (give it to an SP2 entry point). */
 int seqm_density_jacobi(const seqm_batch *b, const double *F, double *P, double *evals, double *evecs,
                         double *work, const int64_t *mol_row_off, const uint8_t *active, int32_t *status,
-                        int max_sweeps, const uint8_t *warm, int mixed_threshold, void *stream);
+                        int max_sweeps, const uint8_t *warm, int mixed_threshold, int density_only,
+                        void *stream);
 
 /* Allocation-free seqm_density_jacobi.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory (a host that owns a fixed device-memory pool,

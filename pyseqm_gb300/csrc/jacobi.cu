@@ -82,6 +82,32 @@ __device__ void tile_product(int n, bool upper_only, LF L, RF R, OF out) {
   }
 }
 
+// 4x4-register-tile product out(k, j) <- sum_l L(k, l) R(l, j) for k < M, j < N, l < K
+template <class LF, class RF, class OF>
+__device__ void tile_product_mnk(int M, int N, int K, LF L, RF R, OF out) {
+  const int mt = (M + 3) >> 2, nt = (N + 3) >> 2;
+  for (int t = threadIdx.x; t < mt * nt; t += NT_J) {
+    const int k0 = (t / nt) * 4, j0 = (t % nt) * 4;
+    double acc[4][4] = {};
+    for (int l = 0; l < K; ++l) {
+      double a[4], c[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) a[r] = (k0 + r < M) ? L(k0 + r, l) : 0.0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) c[q] = (j0 + q < N) ? R(l, j0 + q) : 0.0;
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[r][q] += a[r] * c[q];
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (k0 + r < M && j0 + q < N) out(k0 + r, j0 + q, acc[r][q]);
+  }
+}
+
 // A (shared, holding F on entry) <- V F V^T; G (global n x n) is scratch
 __device__ void form_vfvt(double *A, int lda, const double *V, double *G, int n) {
   tile_product(
@@ -202,16 +228,146 @@ __device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_swee
   return -1;
 }
 
+// diagonal of A as eigenvalue estimates, their ascending ranks (ties by index) and the
+// index of each rank (order[r])
+__device__ void rank_diag(const double *A, int lda, int n, double *dg, int *rank, int *order) {
+  for (int k = threadIdx.x; k < n; k += NT_J) dg[k] = A[k * lda + k];
+  __syncthreads();
+  for (int k = threadIdx.x; k < n; k += NT_J) {
+    const double d = dg[k];
+    int r = 0;
+    for (int j = 0; j < n; ++j) r += (dg[j] < d) || (dg[j] == d && j < k);
+    rank[k] = r;
+    order[r] = k;
+  }
+  __syncthreads();
+}
+
+// largest first-order occupied-virtual rotation |a_uo| / (HOMO-LUMO gap of the diagonal);
+// +inf when the gap is not positive
+__device__ double ov_theta(const double *A, int lda, int n, int nocc, const double *dg, const int *order,
+                           double *red) {
+  const double gap = dg[order[nocc]] - dg[order[nocc - 1]];
+  const int nv = n - nocc;
+  double mx = 0.0;
+  for (int idx = threadIdx.x; idx < nocc * nv; idx += NT_J) {
+    const int o = order[idx / nv], u = order[nocc + idx % nv];
+    mx = fmax(mx, fabs(A[u * lda + o]));
+  }
+  mx = jblock_reduce(mx, red, true);
+  return gap > 0.0 ? mx / gap : INFINITY;
+}
+
+// FP32 sweeps on (float)A to max |a_pq| <= tol32 with the rotations W in shared memory,
+// V <- W V (or W) in FP64, one Newton-Schulz step, A = V F V^T again.  Returns the FP32
+// sweeps taken.
+__device__ int fp32_stage(double *A, int lda, double *V, double *G, const double *Fm, int n, double tol32,
+                          bool is_warm, JShared &sh) {
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < n * n; idx += NT_J) {
+    int i = idx / n, j = idx - i * n;
+    G[idx] = A[i * lda + j];
+  }
+  __syncthreads();
+  float *A32 = reinterpret_cast<float *>(A), *W32 = A32 + (size_t)n * lda;
+  for (int idx = tid; idx < n * n; idx += NT_J) {
+    int i = idx / n, j = idx - i * n;
+    A32[i * lda + j] = (float)G[idx];
+    W32[idx] = i == j ? 1.0f : 0.0f;  // rows of stride n, as jacobi_solve expects
+  }
+  __syncthreads();
+  int s32 = jacobi_solve<float>(A32, lda, W32, n, tol32, 20, sh);
+  if (s32 < 0) s32 = 20;
+  __syncthreads();
+  // V <- W V (warm) or W (cold), in FP64
+  if (is_warm) {
+    tile_product(
+        n, false, [&](int k, int l) { return (double)W32[k * n + l]; }, [&](int l, int j) { return V[(size_t)l * n + j]; },
+        [&](int k, int j, double v) { G[(size_t)k * n + j] = v; });
+  } else {
+    for (int idx = tid; idx < n * n; idx += NT_J) G[idx] = (double)W32[idx];
+  }
+  __syncthreads();
+  for (int idx = tid; idx < n * n; idx += NT_J) V[idx] = G[idx];
+  __syncthreads();
+  // one Newton-Schulz step: S = V V^T (shared), V <- 1.5 V - 0.5 S V
+  double *S = A;
+  tile_product(
+      n, true, [&](int k, int j) { return V[(size_t)k * n + j]; }, [&](int j, int l) { return V[(size_t)l * n + j]; },
+      [&](int k, int l, double v) {
+        if (k <= l) { S[k * lda + l] = v; S[l * lda + k] = v; }
+      });
+  __syncthreads();
+  tile_product(
+      n, false, [&](int k, int l) { return S[k * lda + l]; }, [&](int l, int j) { return V[(size_t)l * n + j]; },
+      [&](int k, int j, double v) { G[(size_t)k * n + j] = 1.5 * V[(size_t)k * n + j] - 0.5 * v; });
+  __syncthreads();
+  for (int idx = tid; idx < n * n; idx += NT_J) {
+    int i = idx / n, j = idx - i * n;
+    V[idx] = G[idx];
+    A[i * lda + j] = Fm[idx];
+  }
+  __syncthreads();
+  form_vfvt(A, lda, V, G, n);
+  return s32;
+}
+
+// Density from a nearly diagonal A = V F V^T without further sweeps: the smaller of the
+// occupied / virtual sets S is rotated to first order towards its complement T,
+//   c_s' = v_s + sum_t theta_ts v_t,  theta_ts = a_ts / (a_ss - a_tt),
+// re-orthonormalised (Loewdin, C'' = (I - E/2) C' with E = C' C'^T - I, exact to O(theta^4)),
+// and P = 2 C''^T C'' (occupied) or 2 (I - C''^T C'') (virtual).  The remaining error is
+// second order in the off-diagonal of A over the gap.  G: global scratch (P's block).
+__device__ void newton_density(double *A, int lda, const double *V, double *G, double *Pm, int n, int nocc,
+                               const double *dg, const int *order) {
+  const bool use_occ = nocc <= n - nocc;
+  const int nsel = use_occ ? nocc : n - nocc, ncomp = n - nsel;
+  const int s0 = use_occ ? 0 : nocc, t0 = use_occ ? nocc : 0;
+  double *Th = G, *C1 = G + (size_t)nsel * ncomp;
+  for (int idx = threadIdx.x; idx < nsel * ncomp; idx += NT_J) {
+    const int i = idx / ncomp, t = idx - i * ncomp;
+    const int s = order[s0 + i], u = order[t0 + t];
+    Th[idx] = A[u * lda + s] / (dg[s] - dg[u]);
+  }
+  __syncthreads();
+  tile_product_mnk(
+      nsel, n, ncomp, [&](int i, int t) { return Th[(size_t)i * ncomp + t]; },
+      [&](int t, int k) { return V[(size_t)order[t0 + t] * n + k]; },
+      [&](int i, int k, double v) { C1[(size_t)i * n + k] = V[(size_t)order[s0 + i] * n + k] + v; });
+  __syncthreads();
+  double *E = A, *U = A + (size_t)nsel * nsel;  // A is no longer needed
+  tile_product_mnk(
+      nsel, nsel, n, [&](int i, int k) { return C1[(size_t)i * n + k]; },
+      [&](int k, int j) { return C1[(size_t)j * n + k]; },
+      [&](int i, int j, double v) { E[i * nsel + j] = v - (i == j ? 1.0 : 0.0); });
+  __syncthreads();
+  tile_product_mnk(
+      nsel, n, nsel, [&](int i, int l) { return E[i * nsel + l]; }, [&](int l, int k) { return C1[(size_t)l * n + k]; },
+      [&](int i, int k, double v) { U[i * n + k] = C1[(size_t)i * n + k] - 0.5 * v; });
+  __syncthreads();
+  for (int it = threadIdx.x; it < n * n; it += NT_J) {
+    const int a = it / n, c = it - a * n;
+    if (c < a) continue;
+    double s = 0.0;
+    for (int k = 0; k < nsel; ++k) s += U[k * n + a] * U[k * n + c];
+    const double v = use_occ ? 2.0 * s : (a == c ? 2.0 : 0.0) - 2.0 * s;
+    Pm[(size_t)a * n + c] = v;
+    Pm[(size_t)c * n + a] = v;
+  }
+}
+
+constexpr double NEWTON_THETA = 1.0e-5;  // largest occupied-virtual rotation the first-order density takes
+
 __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__restrict__ F, double *__restrict__ P,
                                                  double *__restrict__ evals, double *__restrict__ evecs,
                                                  double *__restrict__ work, const int64_t *__restrict__ row_off,
                                                  const uint8_t *__restrict__ active, int32_t *__restrict__ status,
                                                  int max_sweeps, const uint8_t *__restrict__ warm,
-                                                 int mixed_threshold) {
+                                                 int mixed_threshold, int density_only) {
   extern __shared__ double A[];
   __shared__ JShared sh;
   __shared__ double dg[JMAX_N];
-  __shared__ int rank[JMAX_N];
+  __shared__ int rank[JMAX_N], order[JMAX_N];
 
   const int m = b.mol_order[blockIdx.x];
   if (active && !active[m]) return;
@@ -227,9 +383,12 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
   double *V = work + mo;  // row k = eigenvector k (column k of C)
   double *G = P ? P + mo : nullptr;  // P's block doubles as product scratch until P is written
   const int tid = threadIdx.x;
+  const int nocc = b.mol_nocc[m];
   const bool is_warm = warm != nullptr && warm[m] != 0 && P != nullptr;
   const int hint = status ? status[m] : 0;
   const bool mixed = mixed_threshold > 0 && P != nullptr && (!is_warm || hint < 0 || hint >= mixed_threshold);
+  // an SCF iteration needs P only: the FP64 polish may give way to the first-order density
+  const bool want_newton = density_only && P != nullptr && evecs == nullptr && nocc > 0 && nocc < n;
 
   double f2 = 0.0;
   for (int idx = tid; idx < n * n; idx += NT_J) {
@@ -243,70 +402,28 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
   const double tol = 1.0e-13 * fro;
   if (is_warm) form_vfvt(A, lda, V, G, n);
 
-  int s32 = 0;
-  if (mixed) {
-    // FP32 sweeps on (float)A with W accumulated in shared memory (A32 | W32 overlay A64)
-    for (int idx = tid; idx < n * n; idx += NT_J) {
-      int i = idx / n, j = idx - i * n;
-      G[idx] = A[i * lda + j];
-    }
-    __syncthreads();
-    float *A32 = reinterpret_cast<float *>(A), *W32 = A32 + (size_t)n * lda;
-    for (int idx = tid; idx < n * n; idx += NT_J) {
-      int i = idx / n, j = idx - i * n;
-      A32[i * lda + j] = (float)G[idx];
-      W32[idx] = i == j ? 1.0f : 0.0f;  // rows of stride n, as jacobi_solve expects
-    }
-    __syncthreads();
-    s32 = jacobi_solve<float>(A32, lda, W32, n, 3.0e-6 * fro, 20, sh);
-    if (s32 < 0) s32 = 20;
-    __syncthreads();
-    // V <- W V (warm) or W (cold), in FP64
-    if (is_warm) {
-      tile_product(
-          n, false, [&](int k, int l) { return (double)W32[k * n + l]; },
-          [&](int l, int j) { return V[(size_t)l * n + j]; }, [&](int k, int j, double v) { G[(size_t)k * n + j] = v; });
-    } else {
-      for (int idx = tid; idx < n * n; idx += NT_J) G[idx] = (double)W32[idx];
-    }
-    __syncthreads();
-    for (int idx = tid; idx < n * n; idx += NT_J) V[idx] = G[idx];
-    __syncthreads();
-    // one Newton-Schulz step: S = V V^T (shared), V <- 1.5 V - 0.5 S V
-    double *S = A;
-    tile_product(
-        n, true, [&](int k, int j) { return V[(size_t)k * n + j]; }, [&](int j, int l) { return V[(size_t)l * n + j]; },
-        [&](int k, int l, double v) {
-          if (k <= l) { S[k * lda + l] = v; S[l * lda + k] = v; }
-        });
-    __syncthreads();
-    tile_product(
-        n, false, [&](int k, int l) { return S[k * lda + l]; }, [&](int l, int j) { return V[(size_t)l * n + j]; },
-        [&](int k, int j, double v) { G[(size_t)k * n + j] = 1.5 * V[(size_t)k * n + j] - 0.5 * v; });
-    __syncthreads();
-    for (int idx = tid; idx < n * n; idx += NT_J) {
-      int i = idx / n, j = idx - i * n;
-      V[idx] = G[idx];
-      A[i * lda + j] = Fm[idx];
-    }
-    __syncthreads();
-    form_vfvt(A, lda, V, G, n);
+  bool newton = false;
+  if (want_newton && is_warm) {
+    rank_diag(A, lda, n, dg, rank, order);
+    newton = ov_theta(A, lda, n, nocc, dg, order, sh.red) <= NEWTON_THETA;
   }
-
-  const int s64 = jacobi_solve<double>(A, lda, V, n, tol, max_sweeps, sh);
+  int s32 = 0;
+  if (!newton && (mixed || (want_newton && mixed_threshold > 0))) {
+    // before FP64 polish sweeps 3e-6 ||F|| is enough; the first-order density wants the
+    // FP32 floor, so that the occupied-virtual rotation left over is ~1e-6
+    s32 = fp32_stage(A, lda, V, G, Fm, n, (want_newton ? 2.0e-7 : 3.0e-6) * fro, is_warm, sh);
+    if (want_newton) {
+      rank_diag(A, lda, n, dg, rank, order);
+      newton = ov_theta(A, lda, n, nocc, dg, order, sh.red) <= NEWTON_THETA;
+    }
+  }
+  int s64 = 0;
+  if (!newton) s64 = jacobi_solve<double>(A, lda, V, n, tol, max_sweeps, sh);
   __syncthreads();
   if (tid == 0 && status) status[m] = s64 < 0 ? -1 : s64 + s32;
 
-  // ---- eigenvalues, ranks (ascending; ties by index)
-  for (int k = tid; k < n; k += NT_J) dg[k] = A[k * lda + k];
-  __syncthreads();
-  for (int k = tid; k < n; k += NT_J) {
-    const double d = dg[k];
-    int r = 0;
-    for (int j = 0; j < n; ++j) r += (dg[j] < d) || (dg[j] == d && j < k);
-    rank[k] = r;
-  }
-  __syncthreads();
+  // ---- eigenvalues (ascending; ties by index)
+  rank_diag(A, lda, n, dg, rank, order);
   if (evals) {
     double *e = evals + row_off[m];
     for (int k = tid; k < n; k += NT_J) e[rank[k]] = dg[k];
@@ -319,8 +436,11 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
     }
   }
   if (!P) return;
+  if (newton) {
+    newton_density(A, lda, V, G, P + mo, n, nocc, dg, order);
+    return;
+  }
   // ---- density from the smaller of the occupied / virtual sets, staged in shared memory
-  const int nocc = b.mol_nocc[m];
   const bool use_occ = nocc <= n - nocc;
   const int nsel = use_occ ? nocc : n - nocc;
   double *U = A;  // nsel rows of length n (A is no longer needed)
@@ -350,7 +470,8 @@ using namespace seqm;
 
 extern "C" int seqm_density_jacobi(const seqm_batch *bp, const double *F, double *P, double *evals, double *evecs,
                                    double *work, const int64_t *mol_row_off, const uint8_t *active, int32_t *status,
-                                   int max_sweeps, const uint8_t *warm, int mixed_threshold, void *stream) {
+                                   int max_sweeps, const uint8_t *warm, int mixed_threshold, int density_only,
+                                   void *stream) {
   if (!bp || !work) return SEQM_E_ARG;
   if ((warm || mixed_threshold > 0) && !P) return SEQM_E_ARG;  // P's block is used as product scratch
   seqm_batch b = *bp;
@@ -362,7 +483,7 @@ extern "C" int seqm_density_jacobi(const seqm_batch *bp, const double *F, double
   if (cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return SEQM_E_CUDA;
   k_jacobi<<<b.nmol, NT_J, smem, (cudaStream_t)stream>>>(b, F, P, evals, evecs, work, mol_row_off, active, status,
-                                                         max_sweeps, warm, mixed_threshold);
+                                                         max_sweeps, warm, mixed_threshold, density_only);
   return launch_check();
 }
 
@@ -436,6 +557,6 @@ extern "C" int seqm_density_jacobi_noalloc(const seqm_batch *bp, const double *F
   if (cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return SEQM_E_CUDA;
   k_jacobi<<<b.nmol, NT_J, smem, s>>>(b, F, P, evals, evecs, work, mol_row_off, active, status, max_sweeps,
-                                      nullptr, 0);
+                                      nullptr, 0, 0);
   return launch_check();
 }

@@ -68,7 +68,7 @@ def load(path=None):
     sig = {
         "seqm_hcore": [B, _P, _P, _P, _P, _P, _P],
         "seqm_fock": [B, _P, _P, _P, _P, _P, _P, _P, _P],
-        "seqm_density_jacobi": [B, _P, _P, _P, _P, _P, _P, _P, _P, i32, _P, i32, _P],
+        "seqm_density_jacobi": [B, _P, _P, _P, _P, _P, _P, _P, _P, i32, _P, i32, i32, _P],
         "seqm_density_jacobi_noalloc": [B, _P, _P, _P, _P, _P, _P, _P, i32, _P],
         "seqm_density_sp2": [B, _P, _P, _P, f64, _P, _P, i32, _P],
         "seqm_density_sp2_tc": [B, _P, _P, _P, f64, _P, _P, i32, i32, _P],

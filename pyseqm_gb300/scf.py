@@ -64,6 +64,8 @@ class BatchSCF:
         self.warm = torch.zeros(max(1, nm), dtype=torch.uint8, device=dev)
         # molecules starting cold or whose last solve took >= this many sweeps presweep in FP32 (0 = never)
         self.mixed_threshold = 5
+        # SCF iterations take the first-order density once A = V F V^T is nearly diagonal
+        self.first_order_density = True
         self.sp2_work = None
         self.sp2_tc_work = None
         # molecules above the Jacobi limit take SP2: "fp64" (plain) or "tc" (tensor cores + FP64 McWeeny)
@@ -101,18 +103,18 @@ class BatchSCF:
                                         native.ptr(self.w_xh), native.ptr(self.w_hh), native.ptr(self.F),
                                         native.ptr(active), self._s()), "seqm_fock")
 
-    def density(self, out, sp2=(False,), active=None, evecs=None, max_sweeps=50):
+    def density(self, out, sp2=(False,), active=None, evecs=None, max_sweeps=50, density_only=False):
         if self.profile_density:
             stream = self.stream if self.stream is not None else torch.cuda.current_stream(self.L.device)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            self._density(out, sp2, active, evecs, max_sweeps)
+            self._density(out, sp2, active, evecs, max_sweeps, density_only)
             e1.record(stream)
             fl = self.density_flops if active is None else self.density_flops * active[: self.L.nmol].double()
             self.density_events.append((e0, e1, fl.sum()))
             return
-        self._density(out, sp2, active, evecs, max_sweeps)
+        self._density(out, sp2, active, evecs, max_sweeps, density_only)
 
     def _large_view(self):
         """Batch struct over the molecules above the Jacobi limit only (the fields SP2 reads:
@@ -175,7 +177,7 @@ class BatchSCF:
         if status is not self.status:
             self.status.index_copy_(0, self._large["idx"], status)
 
-    def _density(self, out, sp2=(False,), active=None, evecs=None, max_sweeps=50):
+    def _density(self, out, sp2=(False,), active=None, evecs=None, max_sweeps=50, density_only=False):
         """Density step.  sp2[0] set: the reference's SP2 option for every molecule (plain FP64
         SP2, or tensor-core SP2 + FP64 McWeeny when sp2[2] == "tc").  Otherwise the Jacobi
         eigensolver for norb <= 160 and, for larger molecules, the SP2 form chosen by
@@ -199,7 +201,8 @@ class BatchSCF:
         native.check(self.lib.seqm_density_jacobi(L.struct, native.ptr(self.F), native.ptr(out),
                                                   native.ptr(self.evals), native.ptr(evecs), native.ptr(self.work),
                                                   native.ptr(L.dev["row_off"]), native.ptr(act_s),
-                                                  native.ptr(self.status), max_sweeps, native.ptr(self.warm), self.mixed_threshold,
+                                                  native.ptr(self.status), max_sweeps, native.ptr(self.warm),
+                                                  self.mixed_threshold, int(density_only and self.first_order_density),
                                                   self._s()),
                      "seqm_density_jacobi")
         if act_s is None:
@@ -255,7 +258,7 @@ class BatchSCF:
         molecules that pass the test are retired on the device.  No host synchronisation (except
         inside the SP2 density step)."""
         L = self.L
-        self.density(self.Pnew, self._sp2, active=self.active)
+        self.density(self.Pnew, self._sp2, active=self.active, density_only=True)
         self.launches += 1
         native.check(self.lib.seqm_mix(L.struct, native.ptr(self.P), native.ptr(self.Pnew), native.ptr(self.Pold),
                                        native.ptr(self.old2), native.ptr(L.dev["row_off"]), native.ptr(self.iters),

@@ -48,7 +48,7 @@ def _call(fn_name, L, F, with_work):
         work = torch.empty(T, dtype=torch.float64, device="cuda")
         args.append(native.ptr(work))
     # the allocating entry point also takes (warm, mixed_threshold): cold FP64 sweeps, like the variant
-    args += [native.ptr(L.dev["row_off"]), None, native.ptr(st), 50] + ([None, 0] if with_work else []) + [stream]
+    args += [native.ptr(L.dev["row_off"]), None, native.ptr(st), 50] + ([None, 0, 0] if with_work else []) + [stream]
     rc = getattr(lib, fn_name)(*args)
     torch.cuda.synchronize()
     return rc, P, ev, vec, st

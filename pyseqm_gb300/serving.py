@@ -16,7 +16,8 @@ own, so the SP2 grids cover only their tiles.
 Two forms share the request format and the result record:
 
 * ``ServingLoop(form="serving")``: tensor-core SP2 with FP64 McWeeny refinement
-  above the Jacobi limit, FP32-presweep + FP64 Jacobi below, continuous admission.
+  above the Jacobi limit, FP32-presweep + FP64 Jacobi below, continuous admission;
+  a Jacobi-sized cohort captures its SCF iteration once as a CUDA graph and replays it.
 * ``ServingLoop(form="plain")``: FP64 kernels only, one batch at a time: the
   batch is everything that has arrived when the previous batch finished, solved
   to completion (its force requests, converged tighter, as a second solve)
@@ -27,6 +28,7 @@ scf_loop.py:350-635 with get_error :106-147); only the batching changes.
 """
 
 import collections
+import threading
 import time
 from concurrent.futures import FIRST_COMPLETED, ThreadPoolExecutor, wait
 from dataclasses import dataclass
@@ -37,6 +39,11 @@ import torch
 from . import native, workloads
 from .layout import Layout
 from .scf import JACOBI_MAX_N, MAX_ITER, BatchSCF
+
+
+# torch.cuda.graph synchronises the device when a capture starts, which is not allowed while
+# another thread's stream is capturing: cohorts capture one at a time
+_CAPTURE_LOCK = threading.Lock()
 
 
 @dataclass
@@ -102,8 +109,10 @@ def _configure(solver, form):
 class _Cohort:
     """One admitted batch: layout, solver and stream; its methods run on one worker thread at a time."""
 
-    def __init__(self, reqs, method, eps, form, device, large, stream):
+    def __init__(self, reqs, method, eps, form, device, large, stream, graphs=False):
         self.reqs = reqs
+        self.graphs = graphs and not large  # the SP2 step loop synchronises with the host: not capturable
+        self.graph = None
         self.method = method
         self.eps = eps
         self.form = form
@@ -124,6 +133,14 @@ class _Cohort:
             s.hcore()
             s.start(self.eps, (1,))
             self.s = s
+            if self.graphs:
+                # one SCF iteration (density, mixing, Fock, energy + test) as a CUDA graph,
+                # replayed every iteration: the buffers and the retirement flags live on the device
+                self.graph = torch.cuda.CUDAGraph()
+                with _CAPTURE_LOCK, torch.cuda.graph(self.graph, stream=self.stream,
+                                                     capture_error_mode="thread_local"):
+                    s.step()
+                s.launches -= 4  # counted again at every replay
             nm = self.L.nmol
             pin = dict(pin_memory=True)
             self.h_active = torch.empty(nm, dtype=torch.uint8, **pin)
@@ -139,7 +156,11 @@ class _Cohort:
         s, L = self.s, self.L
         nm = L.nmol
         with torch.cuda.stream(self.stream):
-            s.step()
+            if self.graph is not None:
+                self.graph.replay()
+                s.launches += 4
+            else:
+                s.step()
             self.iteration += 1
             self.h_active.copy_(s.active[:nm], non_blocking=True)
             self.h_E[0].copy_(s.Eout[:nm], non_blocking=True)
@@ -191,6 +212,7 @@ class _Cohort:
 class ServingLoop:
     """Request loop over one GPU (see the module docstring).
 
+    graphs: Jacobi-sized cohorts replay their SCF iteration as a CUDA graph (serving form);
     eps: SCF threshold (get_error) of energy requests; eps_forces: of force requests (forces
     are linear in the density error where the energy is quadratic, so they converge tighter
     and are admitted in cohorts of their own); budget_bytes: device memory the live cohorts
@@ -200,7 +222,7 @@ class ServingLoop:
     (arguments of ``_Cohort``), replaceable to exercise the scheduling on the host."""
 
     def __init__(self, method="PM3", eps=1.0e-5, form="serving", budget_bytes=100e9, max_live=(4, 4),
-                 max_cohort=(4096, 256), device="cuda", cohort_factory=None, eps_forces=1.0e-6):
+                 max_cohort=(4096, 256), device="cuda", cohort_factory=None, eps_forces=1.0e-6, graphs=True):
         if form not in ("serving", "plain"):
             raise ValueError("form must be 'serving' or 'plain'")
         self.method = method
@@ -212,6 +234,7 @@ class ServingLoop:
         self.max_cohort = tuple(max_cohort)
         self.device = torch.device(device)
         self.cohort_factory = cohort_factory or _Cohort
+        self.graphs = bool(graphs) and form == "serving"
         self.launches = 0
         self.cohorts = 0
         self.max_concurrent = 0  # most cohorts live at once (overlap on the device)
@@ -257,7 +280,7 @@ class ServingLoop:
                         take.append(q.popleft())
                     if take:
                         c = self.cohort_factory(take, self.method, self.eps_forces if f else self.eps, self.form,
-                                                self.device, bool(k), free_streams[k].pop())
+                                                self.device, bool(k), free_streams[k].pop(), self.graphs)
                         c.future = pool.submit(c.admit)
                         live[k].append(c)
                         used += c.bytes

@@ -53,3 +53,15 @@ def test_serving_within_tolerance_of_fp64(mix):
     for r, p, m in zip(res, plain, mols):
         if m[2]:
             np.testing.assert_allclose(r.forces, p.forces, atol=TOL_F_MIXED)
+
+
+def test_graph_replay_matches_eager_launches(mix):
+    """A Jacobi-sized cohort replaying its captured SCF iteration gives the eager results."""
+    mols = [m for m in _mols() if serving.norb_of(m[0]) <= 160]
+    eager = serving.ServingLoop("PM3", eps=EPS, graphs=False).run(serving.make_requests(mols))
+    graph = serving.ServingLoop("PM3", eps=EPS, graphs=True).run(serving.make_requests(mols))
+    for a, g in zip(eager, graph):
+        assert a.iterations == g.iterations
+        assert a.Etot == g.Etot
+        if a.forces is not None:
+            np.testing.assert_array_equal(a.forces, g.forces)

@@ -13,7 +13,7 @@ class FakeCohort:
 
     made = []
 
-    def __init__(self, reqs, method, eps, form, device, large, stream):
+    def __init__(self, reqs, method, eps, form, device, large, stream, graphs=False):
         self.reqs, self.large = reqs, large
         self.bytes = sum(serving.footprint(r, form) for r in reqs)
         self.stream, self.future, self.finished = stream, None, False

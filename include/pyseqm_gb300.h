@@ -163,10 +163,30 @@ int seqm_mix(const seqm_batch *b, double *P, const double *Pnew, double *Pold, d
 /* Electronic energy 1/2 sum P(H+F) per molecule (energy.py:26-49) for active molecules, and
  * the SCF convergence test of get_error (scf_loop.py:106-147): updates err, dm_err, dm_el,
  * Eelec (the previous energy), clears active[m] for molecules that converged, and writes
- * Eout[m] = the new energy.  When Pold == NULL only the energy is computed. */
+ * Eout[m] = the new energy.  When Pold == NULL only the energy is computed.  diis_err (NULL
+ * unless the DIIS converger runs): max |F P - P F| per molecule; the test then also fails
+ * while it exceeds 50 eps (scf_loop.py:130-132). */
 int seqm_energy_error(const seqm_batch *b, const double *P, const double *Pold, const double *H,
                       const double *F, double *Eelec, double *Eout, double *err, double *dm_err,
-                      double *dm_el, uint8_t *active, double eps, void *stream);
+                      double *dm_el, uint8_t *active, double eps, const double *diis_err, void *stream);
+
+/* Pulay DIIS converger (scf_converger [2]; scf_forward2, scf_loop.py:639-1132), per molecule.
+ * state: SEQM_DIIS_STATE doubles per molecule (ring counter, stored count, reset flag, the
+ * 11 x 11 EMAT); hist: SEQM_DIIS_HIST_DOUBLES(T) doubles (10 Fock matrices, 10 commutators
+ * F P - P F, one F P product) with T = mat_off[nmol].  seqm_diis_init before the loop;
+ * per iteration: seqm_diis_extrapolate (stores F and its commutator, counts the iteration in
+ * iters, replaces F by the DIIS extrapolation once 2 are stored), the density step on that
+ * F, seqm_diis_mix (P <- (P + Pnew)/2 while fewer than 2 are stored, else Pnew), the Fock
+ * build and seqm_energy_error with diis_err.  The history resets (per molecule; the reference
+ * resets the whole batch) when the DIIS matrix's condition number exceeds 1e7.
+ * seqm_diis_extrapolate reads mat_off[nmol] back (one stream synchronisation). */
+#define SEQM_DIIS_STATE 124
+#define SEQM_DIIS_HIST_DOUBLES(T) (21 * (size_t)(T))
+int seqm_diis_init(const seqm_batch *b, double *state, double *diis_err, void *stream);
+int seqm_diis_extrapolate(const seqm_batch *b, double *F, const double *P, double *hist, double *state,
+                          double *diis_err, const uint8_t *active, int32_t *iters, void *stream);
+int seqm_diis_mix(const seqm_batch *b, double *P, const double *Pnew, double *Pold, const double *state,
+                  const uint8_t *active, void *stream);
 
 /* Diagonal initial density (scf_loop.py:2066-2081): tore/4 on heavy-atom s,p; 1 on H s. */
 int seqm_initial_density(const seqm_batch *b, double *P, void *stream);

@@ -812,6 +812,8 @@ def scf(mol, p, ints, M, eps, converger=(1,), sp2_opt=(False,), P0=None, el=None
     iters = np.zeros(nmol, dtype=np.int64)
     old2 = np.zeros((nmol, 4 * ms))
     Pold = np.zeros_like(P)
+    if converger[0] == 2:
+        return _scf_diis(mol, p, ints, M, eps, P, F, E, Hsym, density, natoms4)
     linear = converger[0] == 0
     alpha = converger[1] if linear else None
     kstart = 0 if linear else 1
@@ -838,6 +840,86 @@ def scf(mol, p, ints, M, eps, converger=(1,), sp2_opt=(False,), P0=None, el=None
         E[nc] = Enew[nc]
         if not np.any(nc):
             break
+    return P, nc, iters
+
+
+DIIS_DEPTH = 10  # nFock, scf_loop.py:893
+DIIS_FACTOR = 50.0  # CONVERGENCE_DIIS_FACTOR, scf_loop.py:52
+
+
+def _diis_fresh(nb):
+    """EMAT after a (re)start: the lower triangle of (I - 1) (scf_loop.py:916-921)."""
+    return np.tril(np.eye(DIIS_DEPTH + 1) - 1.0)
+
+
+def _scf_diis(mol, p, ints, M, eps, P, F, E, Hsym, density, natoms4):
+    """scf_forward2 with its default schedule (no direct or adaptive steps), scf_loop.py:639-1132:
+    Pulay DIIS over the last 10 Fock matrices with the commutators F P - P F as residuals.
+    EMAT gets one row per iteration and is read through its lower triangle (as eigh does there,
+    so entries written before the ring wrapped stay in use); the pseudo-inverse keeps
+    eigenvalues above 1e-13; a condition number above 1e7 resets the history after the
+    iteration.  The history and its reset are kept per molecule (the reference shares the ring
+    counter and resets the whole batch)."""
+    nmol, nb = P.shape[0], P.shape[1]
+    tri = np.triu_indices(nb)
+    counter = np.full(nmol, -1)
+    cfock = np.zeros(nmol, dtype=np.int64)
+    emat = np.stack([_diis_fresh(nb) for _ in range(nmol)])
+    fock_h = np.zeros((nmol, DIIS_DEPTH, nb, nb))
+    fppf = np.zeros((nmol, DIIS_DEPTH, tri[0].size))
+    diis_err = np.full(nmol, np.finfo(np.float64).max)
+    nc = np.ones(nmol, dtype=bool)
+    iters = np.zeros(nmol, dtype=np.int64)
+    Enew = np.zeros(nmol)
+    err = np.ones(nmol)
+    dm_err = np.ones(nmol)
+    dm_el = np.ones(nmol)
+    Pold = np.zeros_like(P)
+    for _k in range(0, MAX_ITER + 1):
+        sel = np.nonzero(nc)[0]
+        if sel.size == 0:
+            break
+        Fx = F.copy()
+        reset = np.zeros(nmol, dtype=bool)
+        for m in sel:
+            cfock[m] = min(cfock[m] + 1, DIIS_DEPTH)
+            counter[m] = (counter[m] + 1) % DIIS_DEPTH
+            c, cf = counter[m], cfock[m]
+            fock_h[m, c] = F[m]
+            C = F[m] @ P[m] - P[m] @ F[m]
+            fppf[m, c] = C[tri]
+            diis_err[m] = np.max(np.abs(fppf[m, c]))
+            emat[m, c, :cf] = fppf[m, :cf] @ fppf[m, c]
+            if cf >= 2:
+                evec = emat[m, : cf + 1, : cf + 1].copy()
+                evec[:cf, :cf] /= max(evec[c, c], 1.0e-15)
+                L, Q = np.linalg.eigh(evec, UPLO="L")
+                a = np.abs(L)
+                reset[m] = a.max() / a.min() > 1.0e7 if a.min() > 0 else True
+                inv = np.where(a > 1.0e-13, 1.0 / np.where(a > 1.0e-13, L, 1.0), 0.0)
+                coeff = -(Q[:cf, :] * inv[None, :]) @ Q[-1, :]
+                Fx[m] = np.tensordot(coeff, fock_h[m, :cf], axes=1)
+        Pnew = density(Fx, sel)
+        for a_, m in enumerate(sel):
+            Pold[m] = P[m]
+            P[m] = 0.5 * P[m] + 0.5 * Pnew[a_] if cfock[m] < 2 else Pnew[a_]
+        iters[sel] += 1
+        F = fock(mol, p, ints, M, P)
+        Enew[sel] = elec_energy(P[sel], F[sel], Hsym[sel])
+        err[sel] = Enew[sel] - E[sel]
+        bad = (np.abs(err) > eps) | (diis_err > DIIS_FACTOR * eps)
+        dmm = nc & ~bad
+        if np.any(dmm):
+            dP = P[dmm] - Pold[dmm]
+            dm_err[dmm] = np.sqrt(np.sum(dP * dP, axis=(1, 2))) / natoms4[dmm]
+            dm_el[dmm] = np.max(np.abs(dP), axis=(1, 2))
+        nc = bad | (dm_err > eps * DM_ERR_FACTOR) | (dm_el > eps * DM_ELEM_FACTOR)
+        E[nc] = Enew[nc]
+        for m in np.nonzero(reset)[0]:
+            counter[m], cfock[m] = -1, 0
+            emat[m] = _diis_fresh(nb)
+            fock_h[m] = 0.0
+            fppf[m] = 0.0
     return P, nc, iters
 
 

@@ -11,7 +11,7 @@ beta_p through ``SCFEnergyFunction``, whose backward is the adjoint kernel
 (seqm_energy_grad) evaluated at the converged density, which is what the
 reference's SCF0 boundary implies (scf_loop.py:1996-2031).
 
-Supported: closed-shell MNDO/AM1/PM3, scf_converger [0, alpha] and [1], sp2,
+Supported: closed-shell MNDO/AM1/PM3, scf_converger [0, alpha], [1] and [2] (DIIS), sp2,
 learned parameters (values for any parameter; gradients for U_ss, U_pp, beta_s,
 beta_p).  UHF, PM6, excited states, scf_backward >= 1 and a finite
 pair_outer_cutoff raise NotImplementedError.
@@ -71,8 +71,8 @@ def _check_options(seqm_parameters):
     if seqm_parameters.get("pair_outer_cutoff", 1e10) < 1e10:
         raise NotImplementedError("a finite pair_outer_cutoff is not supported (all pairs are kept)")
     conv = seqm_parameters.get("scf_converger", [1])
-    if conv[0] not in (0, 1):
-        raise NotImplementedError("scf_converger must be [0, alpha] or [1]")
+    if conv[0] not in (0, 1, 2):
+        raise NotImplementedError("scf_converger must be [0, alpha], [1] or [2]")
 
 
 class Parser(torch.nn.Module):

@@ -261,10 +261,12 @@ __device__ double block_max(double v, double *red) {
 // and rank 0 adds the slice sums in slice order through distributed shared memory,
 // so the result does not depend on cs.
 __device__ __forceinline__ void finish_error(const seqm_batch &b, int m, double e, double fro, double mx, double *Eelec,
-                                        double *err, double *dm_err, double *dm_el, uint8_t *active, double eps) {
+                                        double *err, double *dm_err, double *dm_el, uint8_t *active, double eps,
+                                        const double *diis_err) {
   double de = e - Eelec[m];
   err[m] = de;
-  bool bad = fabs(de) > eps;
+  // with DIIS, also max |F P - P F| > 50 eps (scf_loop.py:130-132)
+  bool bad = fabs(de) > eps || (diis_err != nullptr && diis_err[m] > 50.0 * eps);
   if (!bad) {
     int nat = b.mol_atom_off[m + 1] - b.mol_atom_off[m];
     dm_err[m] = sqrt(fro) / (4.0 * nat);
@@ -280,7 +282,7 @@ __global__ void __launch_bounds__(NT_RED) k_energy_error(seqm_batch b, const dou
                                                          const double *__restrict__ Pold, const double *__restrict__ H,
                                                          const double *__restrict__ F, double *Eelec, double *Eout,
                                                          double *err, double *dm_err, double *dm_el, uint8_t *active,
-                                                         double eps, int cs) {
+                                                         double eps, const double *__restrict__ diis_err, int cs) {
   __shared__ double wred[NT_RED / 32][3 * EE_SLICES];
   __shared__ double part[3 * EE_SLICES];
   cg::cluster_group cl = cg::this_cluster();
@@ -342,7 +344,7 @@ __global__ void __launch_bounds__(NT_RED) k_energy_error(seqm_batch b, const dou
     }
     e *= 0.5;
     Eout[m] = e;
-    if (Pold) finish_error(b, m, e, fro, mx, Eelec, err, dm_err, dm_el, active, eps);
+    if (Pold) finish_error(b, m, e, fro, mx, Eelec, err, dm_err, dm_el, active, eps, diis_err);
   }
   cl.sync();  // the other CTAs' shared memory stays alive until rank 0 has read it
 }
@@ -537,13 +539,13 @@ extern "C" int seqm_fock(const seqm_batch *bp, const double *P, const double *H,
 
 extern "C" int seqm_energy_error(const seqm_batch *bp, const double *P, const double *Pold, const double *H,
                                  const double *F, double *Eelec, double *Eout, double *err, double *dm_err,
-                                 double *dm_el, uint8_t *active, double eps, void *stream) {
+                                 double *dm_el, uint8_t *active, double eps, const double *diis_err, void *stream) {
   if (!bp) return SEQM_E_ARG;
   seqm_batch b = *bp;
   if (b.nmol == 0) return SEQM_OK;
   const int cs = mol_cluster(k_energy_error, b.max_norb);
   return launch_clusters(k_energy_error, cs, b.nmol, NT_RED, 0, stream, b, P, Pold, H, F, Eelec, Eout, err, dm_err,
-                         dm_el, active, eps, cs);
+                         dm_el, active, eps, diis_err, cs);
 }
 
 extern "C" int seqm_mix(const seqm_batch *bp, double *P, const double *Pnew, double *Pold, double *old2,

@@ -216,9 +216,10 @@ __global__ void __launch_bounds__(EW_THREADS) k_ew_axpby(seqm_batch b, double a,
     D[mo + idx] = a * A[mo + idx] + (C ? c * C[mo + idx] : 0.0);
 }
 
-// C = A B (T = double or float) where A, B and the product are symmetric (X X, functions
-// of one X): only the upper
-// MW_T x MW_T output tiles are computed and each is written with its mirror.  With A
+// C = A B (T = double or float) with A symmetric.  When B and the product are symmetric too
+// (X X, functions of one X; FULL = false) only the upper
+// MW_T x MW_T output tiles are computed and each is written with its mirror (FULL: every tile,
+// no mirror, for a general B).  With A
 // symmetric, the A slab A[i0.., k0..] is read as rows of A[k0.., i0..], so both slabs
 // load along rows (coalesced) and are stored K-major without a transpose.  Small tiles
 // keep the FP64 pipes of all SMs busy on one molecule (a 1296-AO matrix gives 861
@@ -234,7 +235,7 @@ template <>
 struct vec2<float> {
   using type = float2;
 };
-template <class T>
+template <class T, bool FULL = false>
 __global__ void __launch_bounds__(MW_THREADS) k_sym_gemm(seqm_batch b, const T *__restrict__ Am,
                                                          const T *__restrict__ Bm, T *__restrict__ Cm,
                                                          const uint8_t *__restrict__ active,
@@ -244,7 +245,7 @@ __global__ void __launch_bounds__(MW_THREADS) k_sym_gemm(seqm_batch b, const T *
   if (st && st[SP2_NS * m + S_RUN] == 0.0) return;
   const int n = b.mol_norb[m];
   const int i0 = blockIdx.y * MW_T, j0 = blockIdx.x * MW_T;
-  if (i0 >= n || j0 >= n || blockIdx.y > blockIdx.x) return;
+  if (i0 >= n || j0 >= n || (!FULL && blockIdx.y > blockIdx.x)) return;
   const size_t mo = b.mol_mat_off[m];
   const T *A = Am + mo, *B = Bm + mo;
   __shared__ __align__(16) T As[2][MW_K][MW_T], Bs[2][MW_K][MW_T];
@@ -298,7 +299,7 @@ __global__ void __launch_bounds__(MW_THREADS) k_sym_gemm(seqm_batch b, const T *
       const int row = i0 + 2 * ty + r, col = j0 + 2 * tx + q;
       if (row < n && col < n) {
         C[(size_t)row * n + col] = acc[r][q];
-        C[(size_t)col * n + row] = acc[r][q];
+        if (!FULL) C[(size_t)col * n + row] = acc[r][q];
       }
     }
 }

@@ -6,7 +6,7 @@ reference's SCF semantics (seqm/seqm_functions/scf_loop.py:2034-2394):
     hcore -> initial diagonal density -> F(P0), E(P0)
     repeat for molecules still active:
         density step (Jacobi eigensolver, or SP2)  -> Pnew
-        mixing (linear scf_forward0 / adaptive scf_forward1) -> P, Pold
+        mixing (linear scf_forward0 / adaptive scf_forward1 / Pulay DIIS scf_forward2) -> P, Pold
         F(P), Eelec(P) and the get_error test, which retires converged molecules
     final eigen-decomposition of F (orbital energies and vectors)
 
@@ -68,6 +68,9 @@ class BatchSCF:
         self.first_order_density = True
         self.sp2_work = None
         self.sp2_tc_work = None
+        self._diis_hist = None
+        self._diis = False
+        self._diis_err = None
         # molecules above the Jacobi limit take SP2: "fp64" (plain) or "tc" (tensor cores + FP64 McWeeny)
         self.large_density = "fp64"
         self.mcweeny_steps = 1  # FP64-accurate McWeeny steps after the tensor-core SP2 (and one FP32 step)
@@ -217,21 +220,22 @@ class BatchSCF:
             native.check(self.lib.seqm_energy_error(b, native.ptr(self.P), None, native.ptr(self.H),
                                                     native.ptr(self.F), native.ptr(self.Eelec), native.ptr(self.Eout),
                                                     native.ptr(self.err), native.ptr(self.dm_err),
-                                                    native.ptr(self.dm_el), None, float(eps), self._s()),
+                                                    native.ptr(self.dm_el), None, float(eps), None, self._s()),
                          "seqm_energy_error")
             return
         native.check(self.lib.seqm_energy_error(b, native.ptr(self.P), native.ptr(self.Pold), native.ptr(self.H),
                                                 native.ptr(self.F), native.ptr(self.Eelec), native.ptr(self.Eout),
                                                 native.ptr(self.err), native.ptr(self.dm_err), native.ptr(self.dm_el),
-                                                native.ptr(self.active), float(eps), self._s()), "seqm_energy_error")
+                                                native.ptr(self.active), float(eps), native.ptr(self._diis_err),
+                                                self._s()), "seqm_energy_error")
 
     # --------------------------------------------------------------- drivers
     def start(self, eps, converger=(1,), sp2=(False,), P0=None):
         """Initial density, F(P0), E(P0) and the per-molecule SCF state; no host synchronisation."""
         L = self.L
         b = L.struct
-        if int(converger[0]) not in (0, 1):
-            raise NotImplementedError("scf_converger must be [0, alpha] (linear) or [1] (adaptive)")
+        if int(converger[0]) not in (0, 1, 2):
+            raise NotImplementedError("scf_converger must be [0, alpha] (linear), [1] (adaptive) or [2] (DIIS)")
         if P0 is None:
             self.P.zero_()
             self.launches += 1
@@ -252,24 +256,49 @@ class BatchSCF:
         self._linear = int(converger[0]) == 0
         self._alpha = float(converger[1]) if self._linear else 0.0
         self._sp2 = tuple(sp2)
+        self._diis = int(converger[0]) == 2
+        self._diis_err = None
+        if self._diis:
+            dev = L.device
+            if self._diis_hist is None:
+                self._diis_hist = torch.empty(max(1, 21 * int(L.mat_off[-1])), dtype=torch.float64, device=dev)
+                self._diis_state = torch.empty(max(1, native.DIIS_STATE * L.nmol), dtype=torch.float64, device=dev)
+                self._diis_err_buf = torch.empty(max(1, L.nmol), dtype=torch.float64, device=dev)
+            self._diis_err = self._diis_err_buf
+            self.launches += 1
+            native.check(self.lib.seqm_diis_init(b, native.ptr(self._diis_state), native.ptr(self._diis_err),
+                                                 self._s()), "seqm_diis_init")
 
     def step(self):
         """One SCF iteration of every still-active molecule (density, mixing, F(P), E(P), get_error);
         molecules that pass the test are retired on the device.  No host synchronisation (except
         inside the SP2 density step)."""
         L = self.L
+        if self._diis:
+            # store F and its commutator, F <- DIIS extrapolation (scf_forward2, scf_loop.py:974-1033)
+            self.launches += 4
+            native.check(self.lib.seqm_diis_extrapolate(L.struct, native.ptr(self.F), native.ptr(self.P),
+                                                        native.ptr(self._diis_hist), native.ptr(self._diis_state),
+                                                        native.ptr(self._diis_err), native.ptr(self.active),
+                                                        native.ptr(self.iters), self._s()), "seqm_diis_extrapolate")
         self.density(self.Pnew, self._sp2, active=self.active, density_only=True)
         self.launches += 1
-        native.check(self.lib.seqm_mix(L.struct, native.ptr(self.P), native.ptr(self.Pnew), native.ptr(self.Pold),
-                                       native.ptr(self.old2), native.ptr(L.dev["row_off"]), native.ptr(self.iters),
-                                       int(self._linear), self._alpha, native.ptr(self.active), self._s()),
-                     "seqm_mix")
+        if self._diis:
+            native.check(self.lib.seqm_diis_mix(L.struct, native.ptr(self.P), native.ptr(self.Pnew),
+                                                native.ptr(self.Pold), native.ptr(self._diis_state),
+                                                native.ptr(self.active), self._s()), "seqm_diis_mix")
+        else:
+            native.check(self.lib.seqm_mix(L.struct, native.ptr(self.P), native.ptr(self.Pnew),
+                                           native.ptr(self.Pold), native.ptr(self.old2), native.ptr(L.dev["row_off"]),
+                                           native.ptr(self.iters), int(self._linear), self._alpha,
+                                           native.ptr(self.active), self._s()), "seqm_mix")
         self.fock(self.active)
         self.energy_error(self._eps)
 
     def max_loops(self, max_iter=MAX_ITER):
-        """Iterations the reference's loop allows (MAX_ITER + 1 for linear mixing, scf_loop.py:250, MAX_ITER adaptive, :505)."""
-        return max_iter + 1 if self._linear else max_iter
+        """Iterations the reference's loop allows: MAX_ITER + 1 for linear mixing (scf_loop.py:250)
+        and DIIS (:974), MAX_ITER adaptive (:505)."""
+        return max_iter + 1 if (self._linear or self._diis) else max_iter
 
     def scf(self, eps, converger=(1,), sp2=(False,), P0=None, max_iter=MAX_ITER):
         """Run the SCF; returns the per-molecule not-converged mask (host numpy)."""

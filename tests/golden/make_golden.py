@@ -24,6 +24,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+# GOLDEN_ONLY=name1,name2 regenerates only those fixtures
+ONLY = set(filter(None, os.environ.get("GOLDEN_ONLY", "").split(",")))
 
 sys.path.insert(0, REPO)
 sys.path.insert(0, REF)
@@ -113,7 +115,12 @@ def stages(species, coords, method):
                 w=w.detach().numpy().tolist(), idxi=mol.idxi.numpy().tolist(), idxj=mol.idxj.numpy().tolist())
 
 
-def write(name, species, coords, settings, per_molecule=False, learned=None, with_stages=False, ref_json=None):
+def write(name, species, coords, settings, per_molecule=False, learned=None, with_stages=False, ref_json=None,
+          alone=False):
+    """alone: also record every molecule's energies, density and loop count from a run of that
+    molecule by itself (for convergers whose state the reference shares across the batch)."""
+    if ONLY and name not in ONLY:
+        return
     species = np.asarray(species)
     coords = np.asarray(coords, dtype=np.float64)
     rec = dict(name=name, settings=settings, species=species.tolist(), coords=coords.tolist())
@@ -124,6 +131,14 @@ def write(name, species, coords, settings, per_molecule=False, learned=None, wit
             n = int(np.sum(species[m] > 0))
             counts.append(run_es(species[m:m + 1, :n], coords[m:m + 1, :n], settings)["loop_count"])
         rec["ref"]["loop_count_per_molecule"] = counts
+    if alone:
+        runs = []
+        for m in range(species.shape[0]):
+            n = int(np.sum(species[m] > 0))
+            r = run_es(species[m:m + 1, :n], coords[m:m + 1, :n], settings)
+            runs.append(dict(Etot=r["Etot"][0], Eelec=r["Eelec"][0], P=r["P"][0], loop_count=r["loop_count"],
+                             notconverged=r["notconverged"][0]))
+        rec["ref"]["alone"] = runs
     if with_stages:
         rec["stages"] = stages(species, coords, settings["method"])
     if ref_json:
@@ -162,6 +177,14 @@ def main():
     write("mixed_pm3_linear", sp, c, {"method": "PM3", "scf_eps": 1e-8, "scf_converger": [0, 0.1]},
           per_molecule=True)
     write("mixed_mndo", sp, c, {"method": "MNDO", "scf_eps": 1e-8, "scf_converger": [1]})
+    # Pulay DIIS (scf_converger [2]); the reference shares the DIIS history counter and its
+    # resets across the batch, so each molecule is also run alone
+    mols = workloads.mixed_batch(8, seed=2, alkane_range=(1, 6), water_range=(2, 6))
+    sp, c = workloads.pad_batch(mols)
+    write("mixed_am1_diis", sp, c, {"method": "AM1", "scf_eps": 1e-8, "scf_converger": [2]}, alone=True)
+    mols = workloads.mixed_batch(6, seed=3, alkane_range=(2, 8), water_range=(3, 9))
+    sp, c = workloads.pad_batch(mols)
+    write("mixed_pm3_diis", sp, c, {"method": "PM3", "scf_eps": 1e-7, "scf_converger": [2]}, alone=True)
 
     rng = np.random.default_rng(4)
     mols = [workloads.alkane(8, rng, 0.05), workloads.water_cluster(4, rng)]

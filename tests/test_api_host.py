@@ -47,7 +47,7 @@ def test_rejects_unsorted_species_and_odd_electrons():
                  torch.rand(1, 4, 3, dtype=torch.float64), torch.tensor([[6, 1, 1, 1]]))
 
 
-@pytest.mark.parametrize("opt", [{"UHF": True}, {"method": "PM6"}, {"scf_backward": 1}, {"scf_converger": [2]},
+@pytest.mark.parametrize("opt", [{"UHF": True}, {"method": "PM6"}, {"scf_backward": 1}, {"scf_converger": [3]},
                                  {"excited_states": {"n_states": 2}}])
 def test_unsupported_options_raise(opt):
     from pyseqm_gb300 import Constants, Molecule

@@ -19,8 +19,12 @@ def test_oracle_matches_reference(name):
     out = O.single_point(s["method"], g["species_np"], g["coords_np"], s["scf_eps"], tuple(s["scf_converger"]),
                          tuple(s.get("sp2", [False])))
     sp2 = s.get("sp2", [False])[0]
-    # energies 1e-6 eV, density 1e-7 (the eigensolver path agrees to ~1e-12)
-    tolE, tolP = (1e-6, 1e-7)
+    # energies 1e-6 eV, density 1e-7 (the eigensolver path agrees to ~1e-12); where the reference
+    # shares converger state across the batch ("alone" fixtures), its batch result differs from
+    # per-molecule runs by up to the convergence threshold, and the tight check is against "alone"
+    shared = "alone" in ref
+    tolE, tolP, tolO = (1e-6, max(1e-7, 15.0 * s["scf_eps"]), max(1e-8, 100.0 * s["scf_eps"])) if shared else \
+        (1e-6, 1e-7, 1e-8)
     for key in ("Etot", "Eelec", "Enuc", "Hf", "Eiso"):
         np.testing.assert_allclose(out[key], ref[key], atol=tolE, rtol=0)
     for m in range(g["species_np"].shape[0]):
@@ -28,10 +32,17 @@ def test_oracle_matches_reference(name):
     assert int(np.max(out["iters"])) in (ref["loop_count"], ref["loop_count"] - 1, ref["loop_count"] + 1)
     if "loop_count_per_molecule" in ref:
         assert np.all(np.abs(out["iters"] - np.asarray(ref["loop_count_per_molecule"])) <= (1 if sp2 else 0))
+    if "alone" in ref:
+        # convergers whose state the reference shares across the batch: each molecule as run alone
+        alone = ref["alone"]
+        np.testing.assert_array_equal(out["iters"], [a["loop_count"] for a in alone])
+        np.testing.assert_allclose(out["Etot"], [a["Etot"] for a in alone], atol=1e-9, rtol=0)
+        for m in range(len(alone)):
+            np.testing.assert_allclose(_packed(out, m), np.asarray(alone[m]["P"]), atol=1e-9, rtol=0)
     if not sp2:
         for m in range(g["species_np"].shape[0]):
             n = out["mol"]["nheavy"][m] * 4 + out["mol"]["nhyd"][m]
-            np.testing.assert_allclose(out["e"][m][:n], np.asarray(ref["e"][m])[:n], atol=1e-8, rtol=0)
+            np.testing.assert_allclose(out["e"][m][:n], np.asarray(ref["e"][m])[:n], atol=tolO, rtol=0)
     if "stages" in g:
         st = g["stages"]
         mol = out["mol"]

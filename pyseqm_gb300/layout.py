@@ -136,8 +136,10 @@ class Layout:
         return self
 
     def set_coordinates(self, xyz_real):
-        """Replace the device coordinates (natoms, 3) in place (same molecules, new geometry)."""
-        self.dev["xyz"].copy_(torch.as_tensor(xyz_real, dtype=torch.float64).reshape(-1))
+        """Replace the coordinates (natoms, 3), host copy and device array in place (same molecules,
+        new geometry)."""
+        self.xyz = np.array(xyz_real, dtype=np.float64).reshape(-1, 3)
+        self.dev["xyz"].copy_(torch.as_tensor(self.xyz).reshape(-1))
 
     @property
     def struct(self):

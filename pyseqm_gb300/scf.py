@@ -230,8 +230,10 @@ class BatchSCF:
                                                 self._s()), "seqm_energy_error")
 
     # --------------------------------------------------------------- drivers
-    def start(self, eps, converger=(1,), sp2=(False,), P0=None):
-        """Initial density, F(P0), E(P0) and the per-molecule SCF state; no host synchronisation."""
+    def start(self, eps, converger=(1,), sp2=(False,), P0=None, keep_warm=False):
+        """Initial density, F(P0), E(P0) and the per-molecule SCF state; no host synchronisation.
+        P0: packed density guess (None: the diagonal guess); keep_warm: keep the eigenvector
+        rows of the previous solve as the Jacobi warm start (same molecules, nearby geometry)."""
         L = self.L
         b = L.struct
         if int(converger[0]) not in (0, 1, 2):
@@ -240,7 +242,7 @@ class BatchSCF:
             self.P.zero_()
             self.launches += 1
             native.check(self.lib.seqm_initial_density(b, native.ptr(self.P), self._s()), "seqm_initial_density")
-        else:
+        elif P0 is not self.P:
             self.P.copy_(P0)
         self.fock()
         self.energy_error(eps, first=True)
@@ -250,7 +252,8 @@ class BatchSCF:
         self.dm_el.fill_(1.0)
         self.active.fill_(1)
         self.iters.zero_()
-        self.warm.zero_()
+        if not keep_warm:
+            self.warm.zero_()
         self.old2.zero_()
         self._eps = float(eps)
         self._linear = int(converger[0]) == 0
@@ -303,6 +306,20 @@ class BatchSCF:
     def scf(self, eps, converger=(1,), sp2=(False,), P0=None, max_iter=MAX_ITER):
         """Run the SCF; returns the per-molecule not-converged mask (host numpy)."""
         self.start(eps, converger, sp2, P0)
+        for _ in range(self.max_loops(max_iter)):
+            self.step()
+            if int(self.active.sum()) == 0:
+                break
+        return self.active[: self.L.nmol].bool().cpu().numpy()
+
+    def resume(self, xyz, eps, converger=(1,), sp2=(False,), max_iter=MAX_ITER):
+        """Next geometry of the same molecules (an MD step, cf. MolecularDynamics.py:815-825,
+        which passes P0 = molecule.dm): new coordinates (natoms x 3, Angstrom), integrals and
+        Hcore recomputed, the SCF started from the current density with the current
+        eigenvectors as the Jacobi warm start; everything stays on the device."""
+        self.L.set_coordinates(xyz)
+        self.hcore()
+        self.start(eps, converger, sp2, P0=self.P, keep_warm=True)
         for _ in range(self.max_loops(max_iter)):
             self.step()
             if int(self.active.sum()) == 0:

@@ -137,10 +137,12 @@ class _Cohort:
                 # one SCF iteration (density, mixing, Fock, energy + test) as a CUDA graph,
                 # replayed every iteration: the buffers and the retirement flags live on the device
                 self.graph = torch.cuda.CUDAGraph()
+                before = s.launches
                 with _CAPTURE_LOCK, torch.cuda.graph(self.graph, stream=self.stream,
                                                      capture_error_mode="thread_local"):
                     s.step()
-                s.launches -= 4  # counted again at every replay
+                self.graph_launches = s.launches - before
+                s.launches = before  # counted at every replay
             nm = self.L.nmol
             pin = dict(pin_memory=True)
             self.h_active = torch.empty(nm, dtype=torch.uint8, **pin)
@@ -158,7 +160,7 @@ class _Cohort:
         with torch.cuda.stream(self.stream):
             if self.graph is not None:
                 self.graph.replay()
-                s.launches += 4
+                s.launches += self.graph_launches
             else:
                 s.step()
             self.iteration += 1

@@ -54,21 +54,22 @@ __device__ double jblock_reduce(double v, double *red, bool is_max) {
   return s;
 }
 
-// 4x4-register-tile product out(k, j) <- sum_l L(k, l) R(l, j), k, j < n (upper tiles only if asked)
-template <class LF, class RF, class OF>
-__device__ void tile_product(int n, bool upper_only, LF L, RF R, OF out) {
+// 4x4-register-tile product out(k, j) <- sum_l L(k, l) R(l, j), k, j < n (upper tiles only if
+// asked), accumulated in T
+template <class T, class LF, class RF, class OF>
+__device__ void tile_product_t(int n, bool upper_only, LF L, RF R, OF out) {
   const int nt = (n + 3) >> 2;
   for (int t = threadIdx.x; t < nt * nt; t += NT_J) {
     const int kb = t / nt, jb = t % nt;
     if (upper_only && kb > jb) continue;
     const int k0 = kb * 4, j0 = jb * 4;
-    double acc[4][4] = {};
+    T acc[4][4] = {};
     for (int l = 0; l < n; ++l) {
-      double a[4], c[4];
+      T a[4], c[4];
 #pragma unroll
-      for (int r = 0; r < 4; ++r) a[r] = (k0 + r < n) ? L(k0 + r, l) : 0.0;
+      for (int r = 0; r < 4; ++r) a[r] = (k0 + r < n) ? L(k0 + r, l) : T(0);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) c[q] = (j0 + q < n) ? R(l, j0 + q) : 0.0;
+      for (int q = 0; q < 4; ++q) c[q] = (j0 + q < n) ? R(l, j0 + q) : T(0);
 #pragma unroll
       for (int r = 0; r < 4; ++r)
 #pragma unroll
@@ -80,6 +81,11 @@ __device__ void tile_product(int n, bool upper_only, LF L, RF R, OF out) {
       for (int q = 0; q < 4; ++q)
         if (k0 + r < n && j0 + q < n) out(k0 + r, j0 + q, acc[r][q]);
   }
+}
+
+template <class LF, class RF, class OF>
+__device__ void tile_product(int n, bool upper_only, LF L, RF R, OF out) {
+  tile_product_t<double>(n, upper_only, L, R, out);
 }
 
 // 4x4-register-tile product out(k, j) <- sum_l L(k, l) R(l, j) for k < M, j < N, l < K
@@ -118,6 +124,23 @@ __device__ void form_vfvt(double *A, int lda, const double *V, double *G, int n)
       n, true, [&](int k, int j) { return G[(size_t)k * n + j]; }, [&](int j, int l) { return V[(size_t)l * n + j]; },
       [&](int k, int l, double v) {
         if (k <= l) { A[k * lda + l] = v; A[l * lda + k] = v; }
+      });
+  __syncthreads();
+}
+
+// A32 (float, shared, overlaying A) <- V F V^T in FP32, with F in A (FP64) on entry; G is
+// global scratch (FP32 view).  Input to FP32 sweeps, which need no more precision.
+__device__ void form_vfvt32(double *A, int lda, const double *V, double *G, int n) {
+  float *G32 = reinterpret_cast<float *>(G), *A32 = reinterpret_cast<float *>(A);
+  tile_product_t<float>(
+      n, false, [&](int k, int l) { return (float)V[(size_t)k * n + l]; },
+      [&](int l, int j) { return (float)A[l * lda + j]; }, [&](int k, int j, float v) { G32[(size_t)k * n + j] = v; });
+  __syncthreads();
+  tile_product_t<float>(
+      n, true, [&](int k, int j) { return G32[(size_t)k * n + j]; },
+      [&](int j, int l) { return (float)V[(size_t)l * n + j]; },
+      [&](int k, int l, float v) {
+        if (k <= l) { A32[k * lda + l] = v; A32[l * lda + k] = v; }
       });
   __syncthreads();
 }
@@ -230,8 +253,9 @@ __device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_swee
 
 // diagonal of A as eigenvalue estimates, their ascending ranks (ties by index) and the
 // index of each rank (order[r])
-__device__ void rank_diag(const double *A, int lda, int n, double *dg, int *rank, int *order) {
-  for (int k = threadIdx.x; k < n; k += NT_J) dg[k] = A[k * lda + k];
+template <class T>
+__device__ void rank_diag(const T *A, int lda, int n, double *dg, int *rank, int *order) {
+  for (int k = threadIdx.x; k < n; k += NT_J) dg[k] = (double)A[k * lda + k];
   __syncthreads();
   for (int k = threadIdx.x; k < n; k += NT_J) {
     const double d = dg[k];
@@ -245,14 +269,14 @@ __device__ void rank_diag(const double *A, int lda, int n, double *dg, int *rank
 
 // largest first-order occupied-virtual rotation |a_uo| / (HOMO-LUMO gap of the diagonal);
 // +inf when the gap is not positive
-__device__ double ov_theta(const double *A, int lda, int n, int nocc, const double *dg, const int *order,
-                           double *red) {
+template <class T>
+__device__ double ov_theta(const T *A, int lda, int n, int nocc, const double *dg, const int *order, double *red) {
   const double gap = dg[order[nocc]] - dg[order[nocc - 1]];
   const int nv = n - nocc;
   double mx = 0.0;
   for (int idx = threadIdx.x; idx < nocc * nv; idx += NT_J) {
     const int o = order[idx / nv], u = order[nocc + idx % nv];
-    mx = fmax(mx, fabs(A[u * lda + o]));
+    mx = fmax(mx, fabs((double)A[u * lda + o]));
   }
   mx = jblock_reduce(mx, red, true);
   return gap > 0.0 ? mx / gap : INFINITY;
@@ -262,17 +286,22 @@ __device__ double ov_theta(const double *A, int lda, int n, int nocc, const doub
 // V <- W V (or W) in FP64, one Newton-Schulz step, A = V F V^T again.  Returns the FP32
 // sweeps taken.
 __device__ int fp32_stage(double *A, int lda, double *V, double *G, const double *Fm, int n, double tol32,
-                          bool is_warm, JShared &sh) {
+                          bool is_warm, bool a32_ready, JShared &sh) {
   const int tid = threadIdx.x;
-  for (int idx = tid; idx < n * n; idx += NT_J) {
-    int i = idx / n, j = idx - i * n;
-    G[idx] = A[i * lda + j];
-  }
-  __syncthreads();
   float *A32 = reinterpret_cast<float *>(A), *W32 = A32 + (size_t)n * lda;
+  if (!a32_ready) {  // A (FP64) -> A32 in place, through G
+    for (int idx = tid; idx < n * n; idx += NT_J) {
+      int i = idx / n, j = idx - i * n;
+      G[idx] = A[i * lda + j];
+    }
+    __syncthreads();
+    for (int idx = tid; idx < n * n; idx += NT_J) {
+      int i = idx / n, j = idx - i * n;
+      A32[i * lda + j] = (float)G[idx];
+    }
+  }
   for (int idx = tid; idx < n * n; idx += NT_J) {
     int i = idx / n, j = idx - i * n;
-    A32[i * lda + j] = (float)G[idx];
     W32[idx] = i == j ? 1.0f : 0.0f;  // rows of stride n, as jacobi_solve expects
   }
   __syncthreads();
@@ -400,18 +429,47 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
   }
   const double fro = sqrt(jblock_reduce(f2, sh.red, false));
   const double tol = 1.0e-13 * fro;
-  if (is_warm) form_vfvt(A, lda, V, G, n);
-
-  bool newton = false;
-  if (want_newton && is_warm) {
-    rank_diag(A, lda, n, dg, rank, order);
-    newton = ov_theta(A, lda, n, nocc, dg, order, sh.red) <= NEWTON_THETA;
+  const bool fp32_ok = mixed || (want_newton && mixed_threshold > 0);
+  bool newton = false, a32_ready = false;
+  if (is_warm && want_newton && fp32_ok) {
+    // rotate in FP32 first: if the occupied-virtual block is already small, the FP64
+    // rotation and the first-order density follow; otherwise the FP32 sweeps start from it
+    // and the FP64 rotation is skipped
+    form_vfvt32(A, lda, V, G, n);
+    rank_diag(reinterpret_cast<const float *>(A), lda, n, dg, rank, order);
+    if (ov_theta(reinterpret_cast<const float *>(A), lda, n, nocc, dg, order, sh.red) <= 0.5 * NEWTON_THETA) {
+      for (int idx = tid; idx < n * n; idx += NT_J) {
+        int i = idx / n, j = idx - i * n;
+        A[i * lda + j] = Fm[idx];
+      }
+      __syncthreads();
+      form_vfvt(A, lda, V, G, n);
+      rank_diag(A, lda, n, dg, rank, order);
+      newton = ov_theta(A, lda, n, nocc, dg, order, sh.red) <= NEWTON_THETA;
+      if (!newton) {  // rare: back to F in A for the FP32 stage below
+        for (int idx = tid; idx < n * n; idx += NT_J) {
+          int i = idx / n, j = idx - i * n;
+          A[i * lda + j] = Fm[idx];
+        }
+        __syncthreads();
+        form_vfvt32(A, lda, V, G, n);
+        a32_ready = true;
+      }
+    } else {
+      a32_ready = true;
+    }
+  } else if (is_warm) {
+    form_vfvt(A, lda, V, G, n);
+    if (want_newton) {
+      rank_diag(A, lda, n, dg, rank, order);
+      newton = ov_theta(A, lda, n, nocc, dg, order, sh.red) <= NEWTON_THETA;
+    }
   }
   int s32 = 0;
-  if (!newton && (mixed || (want_newton && mixed_threshold > 0))) {
+  if (!newton && fp32_ok) {
     // before FP64 polish sweeps 3e-6 ||F|| is enough; the first-order density wants the
     // FP32 floor, so that the occupied-virtual rotation left over is ~1e-6
-    s32 = fp32_stage(A, lda, V, G, Fm, n, (want_newton ? 2.0e-7 : 3.0e-6) * fro, is_warm, sh);
+    s32 = fp32_stage(A, lda, V, G, Fm, n, (want_newton ? 2.0e-7 : 3.0e-6) * fro, is_warm, a32_ready, sh);
     if (want_newton) {
       rank_diag(A, lda, n, dg, rank, order);
       newton = ov_theta(A, lda, n, nocc, dg, order, sh.red) <= NEWTON_THETA;

@@ -102,7 +102,10 @@ int seqm_fock(const seqm_batch *b, const double *P, const double *H, const doubl
  * directly from a warm start or after the FP32 sweeps), P is formed from the first-order
  * occupied-virtual rotation of the smaller set, re-orthonormalised (Loewdin), instead of
  * further FP64 sweeps; error second order in that ratio (<= ~1e-10 in P); evals are then the
- * diagonal of A.  0 = always sweep to the FP64 tolerance (eigenpairs for output).
+ * diagonal of A.  density_only == 2 (evecs NULL: eigenvalues and P wanted, vectors not): as 1,
+ * and the eigenvalues are a_kk + sum_j a_kj^2 / (a_kk - a_jj) when every coupling is below
+ * 3e-3 of its diagonal splitting (error third order); otherwise full sweeps.  0 = always sweep
+ * to the FP64 tolerance (eigenpairs for output).
  * status[m]: sweeps taken (FP32 + FP64), or -1 if the FP64 sweep cap was hit, or -2 for an
  * active molecule with norb > 160, which is left untouched (give it to an SP2 entry point). */
 int seqm_density_jacobi(const seqm_batch *b, const double *F, double *P, double *evals, double *evecs,

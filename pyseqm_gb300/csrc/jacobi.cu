@@ -253,10 +253,8 @@ __device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_swee
 
 // diagonal of A as eigenvalue estimates, their ascending ranks (ties by index) and the
 // index of each rank (order[r])
-template <class T>
-__device__ void rank_diag(const T *A, int lda, int n, double *dg, int *rank, int *order) {
-  for (int k = threadIdx.x; k < n; k += NT_J) dg[k] = (double)A[k * lda + k];
-  __syncthreads();
+// ascending ranks of dg (ties by index) and the index of each rank
+__device__ void rank_values(const double *dg, int n, int *rank, int *order) {
   for (int k = threadIdx.x; k < n; k += NT_J) {
     const double d = dg[k];
     int r = 0;
@@ -265,6 +263,25 @@ __device__ void rank_diag(const T *A, int lda, int n, double *dg, int *rank, int
     order[r] = k;
   }
   __syncthreads();
+}
+
+template <class T>
+__device__ void rank_diag(const T *A, int lda, int n, double *dg, int *rank, int *order) {
+  for (int k = threadIdx.x; k < n; k += NT_J) dg[k] = (double)A[k * lda + k];
+  __syncthreads();
+  rank_values(dg, n, rank, order);
+}
+
+// largest coupling over diagonal splitting, max_{i<j} |a_ij| / |a_ii - a_jj|
+__device__ double coupling_ratio(const double *A, int lda, int n, double *red) {
+  double mx = 0.0;
+  for (int idx = threadIdx.x; idx < n * n; idx += NT_J) {
+    const int i = idx / n, j = idx - i * n;
+    if (j <= i) continue;
+    const double a = fabs(A[i * lda + j]), d = fabs(A[i * lda + i] - A[j * lda + j]);
+    mx = fmax(mx, a > 0.0 ? (d > 0.0 ? a / d : INFINITY) : 0.0);
+  }
+  return jblock_reduce(mx, red, true);
 }
 
 // largest first-order occupied-virtual rotation |a_uo| / (HOMO-LUMO gap of the diagonal);
@@ -386,6 +403,7 @@ __device__ void newton_density(double *A, int lda, const double *V, double *G, d
 }
 
 constexpr double NEWTON_THETA = 1.0e-5;  // largest occupied-virtual rotation the first-order density takes
+constexpr double EIG_PT_RATIO = 3.0e-3;  // largest coupling / splitting for second-order eigenvalues
 
 __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__restrict__ F, double *__restrict__ P,
                                                  double *__restrict__ evals, double *__restrict__ evecs,
@@ -397,6 +415,7 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
   __shared__ JShared sh;
   __shared__ double dg[JMAX_N];
   __shared__ int rank[JMAX_N], order[JMAX_N];
+  __shared__ double e2[JMAX_N];
 
   const int m = b.mol_order[blockIdx.x];
   if (active && !active[m]) return;
@@ -475,6 +494,14 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
       newton = ov_theta(A, lda, n, nocc, dg, order, sh.red) <= NEWTON_THETA;
     }
   }
+  // eigenvalues without eigenvectors (density_only == 2): second order in the couplings of
+  // the nearly diagonal A when each is small against its diagonal splitting (error of third
+  // order, |a|^3 / delta^2); otherwise full sweeps
+  bool eig_pt = false;
+  if (density_only == 2 && newton) {
+    eig_pt = coupling_ratio(A, lda, n, sh.red) <= EIG_PT_RATIO;
+    newton = eig_pt;
+  }
   int s64 = 0;
   if (!newton) s64 = jacobi_solve<double>(A, lda, V, n, tol, max_sweeps, sh);
   __syncthreads();
@@ -482,7 +509,17 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
 
   // ---- eigenvalues (ascending; ties by index)
   rank_diag(A, lda, n, dg, rank, order);
-  if (evals) {
+  if (eig_pt) {
+    for (int k = tid; k < n; k += NT_J) {
+      const double akk = A[k * lda + k];
+      double c = 0.0;
+      for (int j = 0; j < n; ++j)
+        if (j != k) c += A[k * lda + j] * A[k * lda + j] / (akk - A[j * lda + j]);
+      e2[k] = akk + c;
+    }
+    __syncthreads();
+  }
+  if (evals && !eig_pt) {
     double *e = evals + row_off[m];
     for (int k = tid; k < n; k += NT_J) e[rank[k]] = dg[k];
   }
@@ -496,6 +533,12 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
   if (!P) return;
   if (newton) {
     newton_density(A, lda, V, G, P + mo, n, nocc, dg, order);
+    if (eig_pt && evals) {
+      __syncthreads();
+      rank_values(e2, n, rank, order);
+      double *e = evals + row_off[m];
+      for (int k = tid; k < n; k += NT_J) e[rank[k]] = e2[k];
+    }
     return;
   }
   // ---- density from the smaller of the occupied / virtual sets, staged in shared memory

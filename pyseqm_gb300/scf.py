@@ -205,7 +205,8 @@ class BatchSCF:
                                                   native.ptr(self.evals), native.ptr(evecs), native.ptr(self.work),
                                                   native.ptr(L.dev["row_off"]), native.ptr(act_s),
                                                   native.ptr(self.status), max_sweeps, native.ptr(self.warm),
-                                                  self.mixed_threshold, int(density_only and self.first_order_density),
+                                                  self.mixed_threshold,
+                                                  int(density_only) if self.first_order_density else 0,
                                                   self._s()),
                      "seqm_density_jacobi")
         if act_s is None:
@@ -330,7 +331,10 @@ class BatchSCF:
         """Fock matrix of the converged density, orbital energies / vectors, energies."""
         self.fock()
         evecs = torch.empty_like(self.work) if want_vectors else None
-        self.density(self.Pnew, (False,), active=None if not self.n_large else self.small_mask, evecs=evecs)
+        # orbital energies without vectors may come from second-order perturbation of the
+        # nearly diagonal rotated Fock matrix (density_only 2)
+        self.density(self.Pnew, (False,), active=None if not self.n_large else self.small_mask, evecs=evecs,
+                     density_only=2 if evecs is None else 0)
         self.energy_error(0.0, first=True)
         self.evecs = evecs
         return self.Eout[: self.L.nmol].clone(), self.Enuc[: self.L.nmol].clone()

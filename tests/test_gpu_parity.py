@@ -90,6 +90,20 @@ def test_scf_matches_reference(name):
         np.testing.assert_allclose(ev[L.row_off[m]: L.row_off[m] + n], np.asarray(ref["e"][m])[:n], atol=1e-8)
 
 
+@pytest.mark.parametrize("name", EIG_CASES)
+def test_orbital_energies_without_vectors(name):
+    """Orbital energies of the vector-less final step (second-order perturbation of the nearly
+    diagonal rotated Fock matrix, or full sweeps where a coupling is not small) to 1e-8 eV."""
+    g = load_golden(name)
+    ref = g["ref"]
+    out = _run(g, want_vectors=False)
+    L = out["layout"]
+    ev = out["solver"].evals.cpu().numpy()
+    for m in range(L.nmol):
+        n = int(L.norb[m])
+        np.testing.assert_allclose(ev[L.row_off[m]: L.row_off[m] + n], np.asarray(ref["e"][m])[:n], atol=1e-8)
+
+
 @pytest.mark.parametrize("name", ["mixed_am1_diis", "mixed_pm3_diis"])
 def test_diis_matches_reference_per_molecule(name):
     """Pulay DIIS ([2]): the reference shares its DIIS ring and resets across the batch, this

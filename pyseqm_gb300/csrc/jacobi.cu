@@ -498,12 +498,22 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
   // the nearly diagonal A when each is small against its diagonal splitting (error of third
   // order, |a|^3 / delta^2); otherwise full sweeps
   bool eig_pt = false;
+  int s64 = 0;
   if (density_only == 2 && newton) {
     eig_pt = coupling_ratio(A, lda, n, sh.red) <= EIG_PT_RATIO;
+    if (!eig_pt) {
+      // one FP64 sweep diagonalises the close pairs and squares every coupling
+      jacobi_solve<double>(A, lda, V, n, tol, 1, sh);
+      s64 = 1;
+      __syncthreads();
+      eig_pt = coupling_ratio(A, lda, n, sh.red) <= EIG_PT_RATIO;
+    }
     newton = eig_pt;
   }
-  int s64 = 0;
-  if (!newton) s64 = jacobi_solve<double>(A, lda, V, n, tol, max_sweeps, sh);
+  if (!newton) {
+    const int sw = jacobi_solve<double>(A, lda, V, n, tol, max_sweeps, sh);
+    s64 = sw < 0 ? -1 : s64 + sw;
+  }
   __syncthreads();
   if (tid == 0 && status) status[m] = s64 < 0 ? -1 : s64 + s32;
 

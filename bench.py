@@ -175,31 +175,36 @@ def gpu_bus_id(torch, dev, local):
     return ids[local].strip() if local < len(ids) else str(local)
 
 
-def serving_sample(torch, dev, n, rate, seed=0):
-    """Bounded sample of the serving stream: both forms on the same requests and arrivals."""
+def serving_sample(torch, dev, n, rate, seed=0, forms=("serving", "plain"), mols=None):
+    """Bounded sample of the serving stream: the forms on the same requests and arrivals."""
     from pyseqm_gb300 import serving, workloads
 
-    mols = workloads.request_molecules(n, seed=seed)
+    mols = mols if mols is not None else workloads.request_molecules(n, seed=seed)
     arr = workloads.poisson_arrivals(n, rate, seed=seed)
-    for form in ("serving", "plain"):  # warm-up: library, kernel attributes, allocator
+    for form in forms:  # warm-up: library, kernel attributes, allocator
         serving.ServingLoop("PM3", eps=1e-5, form=form, device=dev).run(serving.make_requests(mols[:8]))
     torch.cuda.synchronize()
     out = {}
-    for form in ("serving", "plain"):
+    for form in forms:
         loop = serving.ServingLoop("PM3", eps=1e-5, form=form, device=dev)
         res = loop.run(serving.make_requests(mols, arr))
         sm = serving.summarize(res)
         sm.update(cohorts=loop.cohorts, max_live_cohorts=loop.max_concurrent, gpu_launches=loop.launches)
         out[form] = (sm, res)
-    dE = max(abs(a.Etot - b.Etot) for a, b in zip(out["serving"][1], out["plain"][1]))
-    dF = [float(np.abs(a.forces - b.forces).max()) for a, b in zip(out["serving"][1], out["plain"][1])
-          if a.forces is not None]
-    return {"workload": f"{n} PM3 requests, 3-600 atoms log-uniform (alkanes / water clusters), 10% with forces, "
+    line = {"workload": f"{n} PM3 requests, 3-600 atoms log-uniform (alkanes / water clusters), 10% with forces, "
                         f"Poisson {rate:.0f} req/s, seed {seed}",
-            "scf_eps": 1e-5, "scf_eps_forces": 1e-6, "budget_bytes": 100e9,
-            "serving": out["serving"][0], "plain_fp64_one_batch_at_a_time": out["plain"][0],
-            "solves_per_s_ratio": out["serving"][0]["solves_per_s"] / out["plain"][0]["solves_per_s"],
-            "max_abs_dE_eV": dE, "max_abs_dF_eV_per_A": max(dF) if dF else None}
+            "scf_eps": 1e-5, "scf_eps_forces": 1e-6, "budget_bytes": 100e9}
+    if "serving" in out:
+        line["serving"] = out["serving"][0]
+    if "plain" in out:
+        line["plain_fp64_one_batch_at_a_time"] = out["plain"][0]
+    if "serving" in out and "plain" in out:
+        dE = max(abs(a.Etot - b.Etot) for a, b in zip(out["serving"][1], out["plain"][1]))
+        dF = [float(np.abs(a.forces - b.forces).max()) for a, b in zip(out["serving"][1], out["plain"][1])
+              if a.forces is not None]
+        line.update(solves_per_s_ratio=out["serving"][0]["solves_per_s"] / out["plain"][0]["solves_per_s"],
+                    max_abs_dE_eV=dE, max_abs_dF_eV_per_A=max(dF) if dF else None)
+    return line
 
 
 def run_ours(args):
@@ -475,9 +480,15 @@ def config_c4(torch, dev, args):
 
 
 def config_c5(torch, dev, args):
+    """The serving stream at each rate; the plain form (minutes at full size) at the first rate only
+    unless --c5-plain-all."""
+    from pyseqm_gb300 import workloads
+
+    mols = workloads.request_molecules(args.requests, seed=0)
     lines = []
-    for rate in [float(x) for x in args.rates.split(",")]:
-        lines.append(serving_sample(torch, dev, args.requests, rate))
+    for k, rate in enumerate(float(x) for x in args.rates.split(",")):
+        forms = ("serving", "plain") if (k == 0 or args.c5_plain_all) else ("serving",)
+        lines.append(serving_sample(torch, dev, args.requests, rate, forms=forms, mols=mols))
     return {"metric": "SCF solves/s + p50/p99 latency vs plain FP64 one batch at a time", "rates": lines}
 
 
@@ -510,6 +521,7 @@ def main():
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--requests", type=int, default=4000)
     ap.add_argument("--rates", default="1000,5000,20000,50000")
+    ap.add_argument("--c5-plain-all", action="store_true", help="--config c5: the plain form at every rate")
     ap.add_argument("--c3-side", type=int, default=10, help="water cluster lattice side of --config c3")
     ap.add_argument("--c3-modes", default="tc,fp64", help="SP2 forms run by --config c3")
     args = ap.parse_args()

@@ -300,8 +300,8 @@ __device__ double ov_theta(const T *A, int lda, int n, int nocc, const double *d
 }
 
 // FP32 sweeps on (float)A to max |a_pq| <= tol32 with the rotations W in shared memory,
-// V <- W V (or W) in FP64, one Newton-Schulz step, A = V F V^T again.  Returns the FP32
-// sweeps taken.
+// V <- W V (or W) in FP64, one Newton-Schulz step (FP64 where it matters), A = V F V^T
+// again.  Returns the FP32 sweeps taken.
 __device__ int fp32_stage(double *A, int lda, double *V, double *G, const double *Fm, int n, double tol32,
                           bool is_warm, bool a32_ready, JShared &sh) {
   const int tid = threadIdx.x;
@@ -336,17 +336,23 @@ __device__ int fp32_stage(double *A, int lda, double *V, double *G, const double
   __syncthreads();
   for (int idx = tid; idx < n * n; idx += NT_J) V[idx] = G[idx];
   __syncthreads();
-  // one Newton-Schulz step: S = V V^T (shared), V <- 1.5 V - 0.5 S V
-  double *S = A;
-  tile_product(
-      n, true, [&](int k, int j) { return V[(size_t)k * n + j]; }, [&](int j, int l) { return V[(size_t)l * n + j]; },
-      [&](int k, int l, double v) {
-        if (k <= l) { S[k * lda + l] = v; S[l * lda + k] = v; }
+  // one Newton-Schulz step V <- V - (S - I) V / 2 with S = V V^T = W W^T (V was orthonormal):
+  // D = W W^T - I in FP64 from the FP32 W (exact products), stored as FP32 over the idle A32
+  // (|D| ~ 1e-6, so FP32 keeps it to ~1e-13), and the small correction D V in FP32
+  float *D32 = A32;
+  tile_product_t<double>(
+      n, true, [&](int k, int l) { return (double)W32[k * n + l]; }, [&](int l, int j) { return (double)W32[j * n + l]; },
+      [&](int k, int j, double v) {
+        if (k <= j) {
+          const float d = (float)(v - (k == j ? 1.0 : 0.0));
+          D32[k * lda + j] = d;
+          D32[j * lda + k] = d;
+        }
       });
   __syncthreads();
-  tile_product(
-      n, false, [&](int k, int l) { return S[k * lda + l]; }, [&](int l, int j) { return V[(size_t)l * n + j]; },
-      [&](int k, int j, double v) { G[(size_t)k * n + j] = 1.5 * V[(size_t)k * n + j] - 0.5 * v; });
+  tile_product_t<float>(
+      n, false, [&](int k, int l) { return D32[k * lda + l]; }, [&](int l, int j) { return (float)V[(size_t)l * n + j]; },
+      [&](int k, int j, float v) { G[(size_t)k * n + j] = V[(size_t)k * n + j] - 0.5 * (double)v; });
   __syncthreads();
   for (int idx = tid; idx < n * n; idx += NT_J) {
     int i = idx / n, j = idx - i * n;
@@ -523,8 +529,12 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
     for (int k = tid; k < n; k += NT_J) {
       const double akk = A[k * lda + k];
       double c = 0.0;
-      for (int j = 0; j < n; ++j)
-        if (j != k) c += A[k * lda + j] * A[k * lda + j] / (akk - A[j * lda + j]);
+      for (int j = 0; j < n; ++j) {
+        const double a = A[k * lda + j];
+        // a zero coupling adds nothing, also between exactly degenerate diagonals (the
+        // ratio test has excluded a nonzero coupling over a zero splitting)
+        if (j != k && a != 0.0) c += a * a / (akk - A[j * lda + j]);
+      }
       e2[k] = akk + c;
     }
     __syncthreads();

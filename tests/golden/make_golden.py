@@ -69,14 +69,17 @@ def packed_P(P, species):
     return out
 
 
-def run_es(species, coords, settings, learned=None):
+def run_es(species, coords, settings, learned=None, charges=None):
     const = Constants()
     sp = dict(settings)
     sp["learned"] = list(learned.keys()) if learned else []
     sp.pop("elements", None)
     species_t = torch.as_tensor(species, dtype=torch.int64)
     coords_t = torch.as_tensor(coords, dtype=torch.float64)
-    mol = Molecule(const, sp, coords_t, species_t)
+    if charges is not None:
+        mol = Molecule(const, sp, coords_t, species_t, charges=torch.as_tensor(charges, dtype=torch.float64))
+    else:
+        mol = Molecule(const, sp, coords_t, species_t)
     mol.verbose = False
     _calls[0] = 0
     if learned:
@@ -116,7 +119,7 @@ def stages(species, coords, method):
 
 
 def write(name, species, coords, settings, per_molecule=False, learned=None, with_stages=False, ref_json=None,
-          alone=False):
+          alone=False, charges=None):
     """alone: also record every molecule's energies, density and loop count from a run of that
     molecule by itself (for convergers whose state the reference shares across the batch)."""
     if ONLY and name not in ONLY:
@@ -124,7 +127,9 @@ def write(name, species, coords, settings, per_molecule=False, learned=None, wit
     species = np.asarray(species)
     coords = np.asarray(coords, dtype=np.float64)
     rec = dict(name=name, settings=settings, species=species.tolist(), coords=coords.tolist())
-    rec["ref"] = run_es(species, coords, settings, learned)
+    if charges is not None:
+        rec["charges"] = list(charges)
+    rec["ref"] = run_es(species, coords, settings, learned, charges)
     if per_molecule:
         counts = []
         for m in range(species.shape[0]):
@@ -147,6 +152,18 @@ def write(name, species, coords, settings, per_molecule=False, learned=None, wit
     with open(os.path.join(HERE, f"{name}.json"), "w") as f:
         json.dump(rec, f)
     print(name, "loop_count", rec["ref"]["loop_count"])
+
+
+def _ions():
+    """NH4+ (tetrahedral, N-H 1.02 A), OH- (0.97 A), H3O+ (pyramidal, O-H 0.98 A), H2O."""
+    t = np.array([[1, 1, 1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]], dtype=float) / np.sqrt(3.0)
+    nh4 = (np.array([7, 1, 1, 1, 1]), np.vstack([[0.0, 0.0, 0.0], 1.02 * t]))
+    oh = (np.array([8, 1]), np.array([[0.0, 0.0, 0.0], [0.97, 0.0, 0.0]]))
+    ang = np.radians(np.arange(3) * 120.0)
+    h3o = (np.array([8, 1, 1, 1]), np.vstack([[0.0, 0.0, 0.0],
+                                             np.c_[0.92 * np.cos(ang), 0.92 * np.sin(ang), np.full(3, 0.32)]]))
+    h2o = (np.array([8, 1, 1]), np.array([[0.0, 0.0, 0.0], [0.957, 0.0, 0.0], [-0.24, 0.927, 0.0]]))
+    return [nh4, oh, h3o, h2o]
 
 
 def main():
@@ -185,6 +202,12 @@ def main():
     mols = workloads.mixed_batch(6, seed=3, alkane_range=(2, 8), water_range=(3, 9))
     sp, c = workloads.pad_batch(mols)
     write("mixed_pm3_diis", sp, c, {"method": "PM3", "scf_eps": 1e-7, "scf_converger": [2]}, alone=True)
+
+    # charged closed shells (tot_charge): NH4+, OH-, H3O+ next to neutral water
+    write("ions_am1", *workloads.pad_batch(_ions()), {"method": "AM1", "scf_eps": 1e-8, "scf_converger": [1]},
+          charges=[1, -1, 1, 0])
+    write("ions_pm3", *workloads.pad_batch(_ions()), {"method": "PM3", "scf_eps": 1e-8, "scf_converger": [1]},
+          charges=[1, -1, 1, 0])
 
     rng = np.random.default_rng(4)
     mols = [workloads.alkane(8, rng, 0.05), workloads.water_cluster(4, rng)]

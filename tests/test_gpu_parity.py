@@ -17,7 +17,8 @@ def _run(g, **kw):
 
     s = g["settings"]
     return run_energy(g["species_np"], g["coords_np"], s["method"], eps=s["scf_eps"],
-                      converger=tuple(s["scf_converger"]), sp2=tuple(s.get("sp2", [False])), device="cuda", **kw)
+                      converger=tuple(s["scf_converger"]), sp2=tuple(s.get("sp2", [False])),
+                      charges=g.get("charges"), device="cuda", **kw)
 
 
 def test_library_loaded():

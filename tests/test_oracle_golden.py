@@ -17,7 +17,7 @@ def test_oracle_matches_reference(name):
     g = load_golden(name)
     s, ref = g["settings"], g["ref"]
     out = O.single_point(s["method"], g["species_np"], g["coords_np"], s["scf_eps"], tuple(s["scf_converger"]),
-                         tuple(s.get("sp2", [False])))
+                         tuple(s.get("sp2", [False])), charges=g.get("charges"))
     sp2 = s.get("sp2", [False])[0]
     # energies 1e-6 eV, density 1e-7 (the eigensolver path agrees to ~1e-12); where the reference
     # shares converger state across the batch ("alone" fixtures), its batch result differs from

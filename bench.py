@@ -30,6 +30,7 @@ Prints one JSON line.
 """
 
 import argparse
+import gc
 import json
 import multiprocessing as mp
 import os
@@ -255,6 +256,8 @@ def run_ours(args):
     stream = torch.cuda.current_stream(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     step_ms = []
+    gc.collect()
+    gc.disable()  # no collector pause inside the timed region (the loop synchronises per SCF iteration)
     e0.record(stream)
     for _ in range(args.steps):
         a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -264,6 +267,7 @@ def run_ours(args):
         step_ms.append((a, c))
     e1.record(stream)
     torch.cuda.synchronize()
+    gc.enable()
     if world > 1:
         dist.barrier()
     clocks = sampler.stop()
@@ -327,6 +331,7 @@ def run_ours(args):
                                l2="working set (>1 GB of F/P/Hcore/integrals) exceeds L2; no flush needed",
                                scf_iterations_max=int(iters.max()), scf_iterations_mean=float(iters.mean())),
                 "p50_ms": statistics.median(step_ms), "p99_ms": float(np.percentile(step_ms, 99)),
+                "step_ms": [round(x, 2) for x in step_ms],
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
                 "serving_sample": serve}
         print(json.dumps(line), flush=True)
@@ -509,7 +514,7 @@ def run_config(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nmol", type=int, default=WORKLOAD["nmol"])

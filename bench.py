@@ -48,6 +48,9 @@ WORKLOAD = {"workload": "AM1 batched single-point SCF, 4096 molecules 50/50 n-al
             "method": "AM1", "nmol": 4096, "scf_eps": 1e-8, "scf_converger": [1], "seed": 0,
             "density_step": "Jacobi (FP64) for all molecules (norb <= 144)"}
 METRIC = "SCF solves/s"
+# DRAM bytes per k_jacobi launch of the default workload, from ncu (0.68 and 0.71 GB at SCF
+# iterations 2 and 11); compute-bound kernel: ~20 GB/s against 6.8 TB/s
+JACOBI_TRAFFIC_BYTES = 6.94e8
 
 
 def _oracle_chunk(args):
@@ -289,7 +292,10 @@ def run_ours(args):
     achieved = sum(fl) / sum(dur) / 1e12 if dur else None
     roofline = {"kernel": "k_jacobi (batched FP64 Jacobi eigensolver + density)", "bound": "fp64",
                 "achieved": achieved, "peak": peak_fp64, "unit": "TFLOP/s",
-                "frac": (achieved / peak_fp64) if achieved else None, "traffic": None,
+                "frac": (achieved / peak_fp64) if achieved else None, "traffic": JACOBI_TRAFFIC_BYTES,
+                "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of k_jacobi launches of this "
+                                  "4096-molecule workload (SCF iterations 2 and 11), one ncu capture each; "
+                                  "profiles/stages_am1_mixed4096.md",
                 "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (MEASURED_PEAKS.json has no FP64 figure)",
                 "algorithmic_unit": "9 n^3 + 2 n^2 nocc FP64 flops per molecule eigensolve",
                 "launches": len(dur), "avg_launch_ms": 1e3 * sum(dur) / max(1, len(dur)),

@@ -57,11 +57,13 @@ def load_params(method):
 
 
 # --------------------------------------------------------------------------- parser
-def parse(species, coords, charges=None):
+def parse(species, coords, charges=None, mult=None):
     """Pair list and counts; restates seqm/basics.py:219-403 (Parser.forward).
 
     species: (nmol, molsize) int, rows sorted descending, 0 = padding.
     coords:  (nmol, molsize, 3) Angstrom.
+    mult: spin multiplicities for unrestricted HF (basics.py:278-295); nocc is then
+    (nmol, 2) = (alpha, beta) occupations.
     """
     el = load_elements()
     species = np.asarray(species, dtype=np.int64)
@@ -78,9 +80,16 @@ def parse(species, coords, charges=None):
     n_charge = np.sum(el["tore"][species], axis=1).astype(np.int64)
     if charges is not None:
         n_charge = n_charge - np.asarray(charges, dtype=np.int64).reshape(-1)
-    if np.any(n_charge % 2 == 1):  # basics.py:297-299
-        raise ValueError("RHF setting requires closed shell systems (even number of electrons)")
-    nocc = n_charge // 2
+    if mult is not None:
+        s2 = np.asarray(mult, dtype=np.float64).reshape(-1) - 1.0
+        na, nb = n_charge / 2.0 + s2 / 2.0, n_charge / 2.0 - s2 / 2.0
+        if np.any(na % 1 != 0) or np.any(nb % 1 != 0):
+            raise ValueError("Invalid charge/multiplicity combination!")
+        nocc = np.stack([na, nb], axis=1).astype(np.int64)
+    else:
+        if np.any(n_charge % 2 == 1):  # basics.py:297-299
+            raise ValueError("RHF setting requires closed shell systems (even number of electrons)")
+        nocc = n_charge // 2
     maskd = (np.arange(molsize) * (molsize + 1))[None, :] + (np.arange(nmol) * molsize**2)[:, None]
     maskd = maskd.reshape(-1)[real_atoms]
     atom_molid = np.repeat(np.arange(nmol), molsize)[real_atoms]
@@ -101,7 +110,7 @@ def parse(species, coords, charges=None):
         nmol=nmol, molsize=molsize, Z=Z, nheavy=nheavy, nhyd=nhyd, nocc=nocc, maskd=maskd,
         atom_molid=atom_molid, idxi=inv[gi], idxj=inv[gj], ni=Z[inv[gi]], nj=Z[inv[gj]],
         xij=d / dist[:, None], rij=dist / A0, mask=m_p * molsize**2 + i_p * molsize + j_p,
-        pair_molid=m_p, species=species, coords=coords,
+        pair_molid=m_p, species=species, coords=coords, uhf=mult is not None,
     )
 
 
@@ -679,8 +688,57 @@ def fock(mol, p, ints, M, P):
     return Ff + np.transpose(np.triu(Ff, 1), (0, 2, 1))
 
 
+def fock_u(mol, p, ints, M, P2):
+    """Unrestricted Fock matrices F[:, s] of the spin densities P2[:, s] (fock_u_batch.py:18-100):
+    Coulomb from the total density, exchange from the spin density, one-centre terms
+    spin-resolved (_one_center_u, :103-146)."""
+    nmol, ms = mol["nmol"], mol["molsize"]
+    Pt = full_to_blocks(P2[:, 0] + P2[:, 1], nmol, ms)
+    Ps = [full_to_blocks(P2[:, s], nmol, ms) for s in range(2)]
+    maskd = mol["maskd"]
+    gss, gsp, gpp, gp2, hsp = p["g_ss"], p["g_sp"], p["g_pp"], p["g_p2"], p["h_sp"]
+    Td = Pt[maskd]
+    Ptp = Td[:, 1, 1] + Td[:, 2, 2] + Td[:, 3, 3]
+    Fs = []
+    for s in range(2):
+        Sd, Od = Ps[s][maskd], Ps[1 - s][maskd]
+        Spt = Sd[:, 1, 1] + Sd[:, 2, 2] + Sd[:, 3, 3]
+        t = np.zeros_like(Td)
+        t[:, 0, 0] = Od[:, 0, 0] * gss + Ptp * gsp - Spt * hsp
+        for i in (1, 2, 3):
+            t[:, i, i] = (Td[:, 0, 0] * gsp - Sd[:, 0, 0] * hsp + Od[:, i, i] * gpp + (Ptp - Td[:, i, i]) * gp2
+                          - 0.5 * (Spt - Sd[:, i, i]) * (gpp - gp2))
+            t[:, 0, i] = 2.0 * Td[:, 0, i] * hsp - Sd[:, 0, i] * (hsp + gsp)
+        for i, j in ((1, 2), (1, 3), (2, 3)):
+            t[:, i, j] = Td[:, i, j] * (gpp - gp2) - 0.5 * Sd[:, i, j] * (gpp + gp2)
+        F = M.copy()
+        F[maskd] += t
+        Fs.append(F)
+    w = ints["w"]
+    idxi, idxj, mask = mol["idxi"], mol["idxj"], mol["mask"]
+    PA = Pt[maskd[idxi]][:, K10_COL, K10_ROW] * K10_WEIGHT
+    PB = Pt[maskd[idxj]][:, K10_COL, K10_ROW] * K10_WEIGHT
+    sumA = np.zeros((w.shape[0], 4, 4))
+    sumB = np.zeros((w.shape[0], 4, 4))
+    sumA[:, K10_ROW, K10_COL] = np.einsum("nk,nkl->nl", PA, w)
+    sumB[:, K10_ROW, K10_COL] = np.einsum("nkl,nl->nk", w, PB)
+    wk = w[:, KIND[:, :, None, None], KIND[None, None, :, :]]
+    out = np.zeros((nmol, 2, 4 * ms, 4 * ms))
+    for s in range(2):
+        F = Fs[s]
+        np.add.at(F, maskd[idxi], sumB)
+        np.add.at(F, maskd[idxj], sumA)
+        np.add.at(F, mask, np.einsum("nalbs,nls->nab", wk, -Ps[s][mask]))
+        Ff = blocks_to_full(F, nmol, ms)
+        out[:, s] = Ff + np.transpose(np.triu(Ff, 1), (0, 2, 1))
+    return out
+
+
 def elec_energy(P, F, Hsym):
-    """Eelec = 1/2 sum P*(H+F)  (energy.py:26-49)."""
+    """Eelec = 1/2 sum P*(H+F)  (energy.py:26-49); unrestricted (P, F of shape (nmol, 2, n, n)):
+    1/2 sum [(Pa + Pb) H + Pa Fa + Pb Fb] (energy.py:44-45)."""
+    if P.ndim == 4:
+        return 0.5 * np.sum((P[:, 0] + P[:, 1]) * Hsym + P[:, 0] * F[:, 0] + P[:, 1] * F[:, 1], axis=(1, 2))
     return 0.5 * np.sum(P * (Hsym + F), axis=(1, 2))
 
 
@@ -742,8 +800,9 @@ def density_sp2(F, nheavy, nhyd, nocc, eps):
 
 
 # --------------------------------------------------------------------- mixing
-def adaptive_mix(k, Pprev, Pcur, old2_diag):
-    """MOPAC-style mixing for one molecule (scf_loop.py:360-420, 350-358)."""
+def adaptive_mix(k, Pprev, Pcur, old2_diag, occ=2.0):
+    """MOPAC-style mixing for one molecule (scf_loop.py:360-420, 350-358); occ is the orbital
+    occupation (2 restricted, 1 per spin unrestricted)."""
     dprev = np.diag(Pprev).copy()
     dcur = np.diag(Pcur).copy()
     damp = 0.05 if k > 4 else 1.0e10
@@ -759,7 +818,7 @@ def adaptive_mix(k, Pprev, Pcur, old2_diag):
     delta = dcur - dprev
     cap = np.abs(delta) > damp
     di = np.where(cap, dprev + np.sign(delta) * damp, dcur + fac * delta)
-    di = np.clip(di, 0.0, 2.0)
+    di = np.clip(di, 0.0, occ)
     sum0 = np.sum(dcur)
     for _ in range(20):
         sum2 = np.sum(di)
@@ -767,9 +826,9 @@ def adaptive_mix(k, Pprev, Pcur, old2_diag):
         if sum2 <= 1.0e-3 or abs(sum3 - 1.0) <= 1.0e-5:
             break
         scaled = np.maximum(di * sum3, 0.0)
-        full = scaled > 2.0
-        di = np.where(full, 2.0, scaled)
-        sum0 = sum0 - np.sum(full) * 2.0
+        full = scaled > occ
+        di = np.where(full, occ, scaled)
+        sum0 = sum0 - np.sum(full) * occ
     np.fill_diagonal(Pmix, di)
     return Pmix, dprev
 
@@ -791,6 +850,8 @@ def scf(mol, p, ints, M, eps, converger=(1,), sp2_opt=(False,), P0=None, el=None
     """SCF driver: scf_forward0 (linear mixing, scf_loop.py:150-347) or
     scf_forward1 (adaptive mixing, :424-635), with get_error (:106-147)."""
     el = el or load_elements()
+    if mol.get("uhf"):
+        return _scf_uhf(mol, p, ints, M, eps, converger, P0, el)
     nmol, ms = mol["nmol"], mol["molsize"]
     Hsym = symmetrize_upper(blocks_to_full(M, nmol, ms))
     P = initial_density(mol, el) if P0 is None else np.array(P0, dtype=np.float64)
@@ -834,6 +895,64 @@ def scf(mol, p, ints, M, eps, converger=(1,), sp2_opt=(False,), P0=None, el=None
         dmm = nc & ~bad
         if np.any(dmm):
             dP = P[dmm] - Pold[dmm]
+            dm_err[dmm] = np.sqrt(np.sum(dP * dP, axis=(1, 2))) / natoms4[dmm]
+            dm_el[dmm] = np.max(np.abs(dP), axis=(1, 2))
+        nc = bad | (dm_err > eps * DM_ERR_FACTOR) | (dm_el > eps * DM_ELEM_FACTOR)
+        E[nc] = Enew[nc]
+        if not np.any(nc):
+            break
+    return P, nc, iters
+
+
+def _scf_uhf(mol, p, ints, M, eps, converger, P0, el):
+    """Unrestricted SCF (scf_forward0 / scf_forward1 with unrestricted=True): each spin density
+    starts at half the restricted guess (scf_loop.py:2083-2085), comes from its own eigenproblem
+    with occupation 1 (Pnew / 2, :259-260 and :515-516) and is mixed on its own (occupation 1,
+    :361-420); F from fock_u, the energy of both spins, and the error test on the spin-summed
+    density change (:136-140)."""
+    nmol, ms = mol["nmol"], mol["molsize"]
+    Hsym = symmetrize_upper(blocks_to_full(M, nmol, ms))
+    if P0 is None:
+        g = initial_density(mol, el)
+        P = np.stack([0.5 * g, 0.5 * g], axis=1)
+    else:
+        P = np.array(P0, dtype=np.float64)
+    nheavy, nhyd, nocc = mol["nheavy"], mol["nhyd"], mol["nocc"]
+    natoms4 = 4.0 * (nheavy + nhyd)
+    F = fock_u(mol, p, ints, M, P)
+    E = elec_energy(P, F, Hsym)
+    Enew = np.zeros(nmol)
+    err = np.ones(nmol)
+    dm_err = np.ones(nmol)
+    dm_el = np.ones(nmol)
+    nc = np.ones(nmol, dtype=bool)
+    iters = np.zeros(nmol, dtype=np.int64)
+    old2 = np.zeros((nmol, 2, 4 * ms))
+    Pold = np.zeros_like(P)
+    linear = converger[0] == 0
+    if converger[0] not in (0, 1):
+        raise NotImplementedError("unrestricted SCF supports scf_converger [0, alpha] and [1]")
+    alpha = converger[1] if linear else None
+    kstart = 0 if linear else 1
+    for k in range(kstart, MAX_ITER + 1):
+        sel = np.nonzero(nc)[0]
+        Pnew = np.stack([0.5 * density_eigh(F[sel, s], nheavy[sel], nhyd[sel], nocc[sel, s])[0] for s in range(2)],
+                        axis=1)
+        for a, m in enumerate(sel):
+            Pold[m] = P[m]
+            for s_ in range(2):
+                if linear:
+                    P[m, s_] = alpha * P[m, s_] + (1.0 - alpha) * Pnew[a, s_]
+                else:
+                    P[m, s_], old2[m, s_] = adaptive_mix(k, Pold[m, s_], Pnew[a, s_], old2[m, s_], occ=1.0)
+        iters[sel] += 1
+        F = fock_u(mol, p, ints, M, P)
+        Enew[sel] = elec_energy(P[sel], F[sel], Hsym[sel])
+        err[sel] = Enew[sel] - E[sel]
+        bad = np.abs(err) > eps
+        dmm = nc & ~bad
+        if np.any(dmm):
+            dP = (P[dmm] - Pold[dmm]).sum(axis=1)
             dm_err[dmm] = np.sqrt(np.sum(dP * dP, axis=(1, 2))) / natoms4[dmm]
             dm_el[dmm] = np.max(np.abs(dP), axis=(1, 2))
         nc = bad | (dm_err > eps * DM_ERR_FACTOR) | (dm_el > eps * DM_ELEM_FACTOR)
@@ -962,7 +1081,7 @@ def energy_at(method, mol, p, P, el=None):
     M = hcore(mol, p, ints)
     nmol, ms = mol["nmol"], mol["molsize"]
     Hsym = symmetrize_upper(blocks_to_full(M, nmol, ms))
-    F = fock(mol, p, ints, M, P)
+    F = fock_u(mol, p, ints, M, P) if P.ndim == 4 else fock(mol, p, ints, M, P)
     Eelec = elec_energy(P, F, Hsym)
     EnucAB = pair_nuclear_energy(method, mol, p, ints["w"][:, 0, 0], el)
     Enuc = np.zeros(nmol)
@@ -977,7 +1096,7 @@ def energy_at(method, mol, p, P, el=None):
 
 
 def single_point(method, species, coords, eps, converger=(1,), sp2_opt=(False,), charges=None, learned=None,
-                 forces=False, fd_step=1.0e-5):
+                 forces=False, fd_step=1.0e-5, mult=None):
     """Full single point: parse -> hcore -> SCF -> energies (+ fixed-density forces).
 
     Forces are -dHf/dR at the converged density, by central finite differences of
@@ -985,20 +1104,24 @@ def single_point(method, species, coords, eps, converger=(1,), sp2_opt=(False,),
     the SCF treated as constant, scf_loop.py:1996-2031, basics.py:1315-1336).
     """
     el = load_elements()
-    mol = parse(species, coords, charges)
+    mol = parse(species, coords, charges, mult)
     p = atom_params(method, mol["Z"], learned)
     ints = integrals(mol, p, el)
     M = hcore(mol, p, ints)
     P, nc, iters = scf(mol, p, ints, M, eps, converger, sp2_opt, el=el)
     out = energy_at(method, mol, p, P, el)
-    _, e, vecs = density_eigh(out["F"], mol["nheavy"], mol["nhyd"], mol["nocc"])
+    if mol["uhf"]:  # orbital energies per spin, (nmol, 2, n)
+        e = np.stack([density_eigh(out["F"][:, s], mol["nheavy"], mol["nhyd"], mol["nocc"][:, s])[1]
+                      for s in range(2)], axis=1)
+    else:
+        _, e, vecs = density_eigh(out["F"], mol["nheavy"], mol["nhyd"], mol["nocc"])
     out.update(P=P, notconverged=nc, iters=iters, e=e, mol=mol, params=p)
     if forces:
-        out["force"] = fd_forces(method, species, coords, P, charges, learned, fd_step)
+        out["force"] = fd_forces(method, species, coords, P, charges, learned, fd_step, mult)
     return out
 
 
-def fd_forces(method, species, coords, P, charges=None, learned=None, h=1.0e-5):
+def fd_forces(method, species, coords, P, charges=None, learned=None, h=1.0e-5, mult=None):
     """-dHf/dR (eV/Angstrom) at fixed density by central differences."""
     coords = np.asarray(coords, dtype=np.float64)
     species = np.asarray(species)
@@ -1013,7 +1136,7 @@ def fd_forces(method, species, coords, P, charges=None, learned=None, h=1.0e-5):
                 for sgn in (1.0, -1.0):
                     c = coords.copy()
                     c[m, a, x] += sgn * h
-                    mol = parse(species, c, charges)
+                    mol = parse(species, c, charges, mult)
                     p = atom_params(method, mol["Z"], learned)
                     vals.append(energy_at(method, mol, p, P, el)["Hf"][m])
                 f[m, a, x] = -(vals[0] - vals[1]) / (2.0 * h)

@@ -57,29 +57,44 @@ def _counting_fock(*a, **k):
 
 
 scf_loop_mod.fock_restricted = _counting_fock
+_orig_fock_u = scf_loop_mod.fock_u_batch
+
+
+def _counting_fock_u(*a, **k):
+    _calls[0] += 1
+    return _orig_fock_u(*a, **k)
+
+
+scf_loop_mod.fock_u_batch = _counting_fock_u
 
 
 def packed_P(P, species):
+    """Per molecule the density without the hydrogen p slots; (alpha, beta) pairs for UHF."""
     out = []
     for m in range(species.shape[0]):
         nh = int(np.sum(species[m] > 1))
         ny = int(np.sum(species[m] == 1))
         idx = np.concatenate([np.arange(4 * nh), 4 * nh + 4 * np.arange(ny)])
-        out.append(P[m][np.ix_(idx, idx)].tolist())
+        if P.ndim == 4:
+            out.append([P[m, s][np.ix_(idx, idx)].tolist() for s in range(2)])
+        else:
+            out.append(P[m][np.ix_(idx, idx)].tolist())
     return out
 
 
-def run_es(species, coords, settings, learned=None, charges=None):
+def run_es(species, coords, settings, learned=None, charges=None, mult=None):
     const = Constants()
     sp = dict(settings)
     sp["learned"] = list(learned.keys()) if learned else []
     sp.pop("elements", None)
     species_t = torch.as_tensor(species, dtype=torch.int64)
     coords_t = torch.as_tensor(coords, dtype=torch.float64)
+    kw = {}
     if charges is not None:
-        mol = Molecule(const, sp, coords_t, species_t, charges=torch.as_tensor(charges, dtype=torch.float64))
-    else:
-        mol = Molecule(const, sp, coords_t, species_t)
+        kw["charges"] = torch.as_tensor(charges, dtype=torch.float64)
+    if mult is not None:
+        kw["mult"] = torch.as_tensor(mult, dtype=torch.float64)
+    mol = Molecule(const, sp, coords_t, species_t, **kw)
     mol.verbose = False
     _calls[0] = 0
     if learned:
@@ -119,7 +134,7 @@ def stages(species, coords, method):
 
 
 def write(name, species, coords, settings, per_molecule=False, learned=None, with_stages=False, ref_json=None,
-          alone=False, charges=None):
+          alone=False, charges=None, mult=None, extra=None):
     """alone: also record every molecule's energies, density and loop count from a run of that
     molecule by itself (for convergers whose state the reference shares across the batch)."""
     if ONLY and name not in ONLY:
@@ -129,7 +144,11 @@ def write(name, species, coords, settings, per_molecule=False, learned=None, wit
     rec = dict(name=name, settings=settings, species=species.tolist(), coords=coords.tolist())
     if charges is not None:
         rec["charges"] = list(charges)
-    rec["ref"] = run_es(species, coords, settings, learned, charges)
+    if mult is not None:
+        rec["mult"] = list(mult)
+    if extra:
+        rec.update(extra)
+    rec["ref"] = run_es(species, coords, settings, learned, charges, mult)
     if per_molecule:
         counts = []
         for m in range(species.shape[0]):
@@ -152,6 +171,28 @@ def write(name, species, coords, settings, per_molecule=False, learned=None, wit
     with open(os.path.join(HERE, f"{name}.json"), "w") as f:
         json.dump(rec, f)
     print(name, "loop_count", rec["ref"]["loop_count"])
+
+
+def _open_shells():
+    """CH3 (planar, doublet), OH (doublet), NO (doublet), CH2 (bent, triplet), O2 (triplet),
+    H2O (singlet, run unrestricted)."""
+    ang = np.radians(np.arange(3) * 120.0)
+    ch3 = (np.array([6, 1, 1, 1]), np.vstack([[0.0, 0.0, 0.0], np.c_[1.08 * np.cos(ang), 1.08 * np.sin(ang),
+                                                                     np.zeros(3)]]))
+    oh = (np.array([8, 1]), np.array([[0.0, 0.0, 0.0], [0.98, 0.0, 0.0]]))
+    no = (np.array([8, 7]), np.array([[0.0, 0.0, 0.0], [1.15, 0.0, 0.0]]))
+    half = np.radians(134.0) / 2.0
+    ch2 = (np.array([6, 1, 1]), np.array([[0.0, 0.0, 0.0], [1.08 * np.sin(half), 1.08 * np.cos(half), 0.0],
+                                          [-1.08 * np.sin(half), 1.08 * np.cos(half), 0.0]]))
+    o2 = (np.array([8, 8]), np.array([[0.0, 0.0, 0.0], [1.21, 0.0, 0.0]]))
+    h2o = (np.array([8, 1, 1]), np.array([[0.0, 0.0, 0.0], [0.957, 0.0, 0.0], [-0.24, 0.927, 0.0]]))
+    return [ch3, oh, no, ch2, o2, h2o], [2, 2, 2, 3, 3, 1]
+
+
+# OH and NO put one electron of a spin into one of two exactly degenerate pi orbitals of the
+# symmetric guess; which one is the eigensolver's arbitrary choice, so their densities are
+# compared up to that choice (energies and orbital energies are unique)
+OPEN_SHELL_DENSITY_AMBIGUOUS = [1, 2]
 
 
 def _ions():
@@ -203,6 +244,12 @@ def main():
     sp, c = workloads.pad_batch(mols)
     write("mixed_pm3_diis", sp, c, {"method": "PM3", "scf_eps": 1e-7, "scf_converger": [2]}, alone=True)
 
+    # unrestricted Hartree-Fock (UHF) for doublets, triplets and a singlet
+    mols, mult = _open_shells()
+    for method in ("MNDO", "AM1", "PM3"):
+        write(f"uhf_{method.lower()}", *workloads.pad_batch(mols),
+              {"method": method, "scf_eps": 1e-8, "scf_converger": [1], "UHF": True}, mult=mult,
+              extra={"density_ambiguous": OPEN_SHELL_DENSITY_AMBIGUOUS})
     # charged closed shells (tot_charge): NH4+, OH-, H3O+ next to neutral water
     write("ions_am1", *workloads.pad_batch(_ions()), {"method": "AM1", "scf_eps": 1e-8, "scf_converger": [1]},
           charges=[1, -1, 1, 0])

@@ -17,7 +17,9 @@ def test_oracle_matches_reference(name):
     g = load_golden(name)
     s, ref = g["settings"], g["ref"]
     out = O.single_point(s["method"], g["species_np"], g["coords_np"], s["scf_eps"], tuple(s["scf_converger"]),
-                         tuple(s.get("sp2", [False])), charges=g.get("charges"))
+                         tuple(s.get("sp2", [False])), charges=g.get("charges"), mult=g.get("mult"))
+    if "mult" in g:
+        return _check_unrestricted(g, out)
     sp2 = s.get("sp2", [False])[0]
     # energies 1e-6 eV, density 1e-7 (the eigensolver path agrees to ~1e-12); where the reference
     # shares converger state across the batch ("alone" fixtures), its batch result differs from
@@ -56,13 +58,33 @@ def test_oracle_matches_reference(name):
             np.testing.assert_allclose(np.ravel(out["Etot"]), np.ravel(rj["Etot"]), atol=1e-5, rtol=1e-5)
 
 
-@pytest.mark.parametrize("name", ["smoke_MNDO", "smoke_AM1", "smoke_PM3", "force_methanal_am1"])
+def _check_unrestricted(g, out):
+    """UHF: energies 1e-6 eV, alpha and beta densities 1e-7 (except where a spin occupies one of
+    two exactly degenerate orbitals of the symmetric guess), orbital energies per spin 1e-8."""
+    ref = g["ref"]
+    for key in ("Etot", "Eelec", "Enuc", "Hf", "Eiso"):
+        np.testing.assert_allclose(out[key], ref[key], atol=1e-6, rtol=0)
+    assert int(np.max(out["iters"])) in (ref["loop_count"], ref["loop_count"] - 1, ref["loop_count"] + 1)
+    mol = out["mol"]
+    for m in range(g["species_np"].shape[0]):
+        idx = O.packed_index(mol["nheavy"][m], mol["nhyd"][m])
+        n = idx.size
+        for s in range(2):
+            np.testing.assert_allclose(out["e"][m, s, :n], np.asarray(ref["e"][m][s])[:n], atol=1e-6, rtol=0)
+            if m not in g.get("density_ambiguous", []):
+                np.testing.assert_allclose(out["P"][m, s][np.ix_(idx, idx)], np.asarray(ref["P"][m][s]), atol=1e-7,
+                                           rtol=0)
+
+
+@pytest.mark.parametrize("name", ["smoke_MNDO", "smoke_AM1", "smoke_PM3", "force_methanal_am1", "uhf_am1"])
 def test_oracle_forces_match_reference_autograd(name):
     g = load_golden(name)
     s = g["settings"]
     out = O.single_point(s["method"], g["species_np"], g["coords_np"], s["scf_eps"], tuple(s["scf_converger"]),
-                         forces=True)
-    np.testing.assert_allclose(out["force"], np.asarray(g["ref"]["force"]), atol=1e-6, rtol=0)
+                         forces=True, mult=g.get("mult"))
+    ref = np.asarray(g["ref"]["force"])
+    keep = [m for m in range(ref.shape[0]) if m not in g.get("density_ambiguous", [])]
+    np.testing.assert_allclose(out["force"][keep], ref[keep], atol=1e-6, rtol=0)
 
 
 def test_oracle_rejects_odd_electrons():

@@ -452,14 +452,14 @@ def config_c4(torch, dev, args):
         s.hcore()
         s.scf(eps, (1,))
         s.final(want_vectors=False)
-        native.check(s.lib.seqm_energy_grad(L.struct, native.ptr(s.P), native.ptr(g), native.ptr(g), native.ptr(dR),
+        native.check(s.lib.seqm_energy_grad(L.struct, native.ptr(s.P), None, native.ptr(g), native.ptr(g), native.ptr(dR),
                                             native.ptr(dpar), native.ptr(work), s._s()), "seqm_energy_grad")
         return dR
 
     dt_all, _ = _timed(torch, solve_and_grad, args.steps, args.warmup)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    native.check(s.lib.seqm_energy_grad(L.struct, native.ptr(s.P), native.ptr(g), native.ptr(g), native.ptr(dR),
+    native.check(s.lib.seqm_energy_grad(L.struct, native.ptr(s.P), None, native.ptr(g), native.ptr(g), native.ptr(dR),
                                         native.ptr(dpar), native.ptr(work), s._s()), "seqm_energy_grad")
     e1.record()
     torch.cuda.synchronize()

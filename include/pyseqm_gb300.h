@@ -158,10 +158,12 @@ int seqm_density_sp2_tc(const seqm_batch *b, const double *F, double *P, void *w
  * scf_loop.py:258-267: P <- alpha P + (1-alpha) Pnew) and scf_forward1 (adaptive,
  * adaptive_mix, scf_loop.py:360-420).  iters[m] counts the molecule's density steps and is
  * incremented here (the adaptive mixer keys on the 1-based count), old2 = diagonal of P
- * from two steps before (at mol_row_off[m]).  Pold receives P before the update. */
+ * from two steps before (at mol_row_off[m]).  Pold receives P before the update.
+ * occupation: 2 for a restricted density, 1 for one spin of an unrestricted one (the clamp and
+ * the renormalisation of the adaptive mixer, scf_loop.py:371-413). */
 int seqm_mix(const seqm_batch *b, double *P, const double *Pnew, double *Pold, double *old2,
-             const int64_t *mol_row_off, int32_t *iters, int linear, double alpha, const uint8_t *active,
-             void *stream);
+             const int64_t *mol_row_off, int32_t *iters, int linear, double alpha, double occupation,
+             const uint8_t *active, void *stream);
 
 /* Electronic energy 1/2 sum P(H+F) per molecule (energy.py:26-49) for active molecules, and
  * the SCF convergence test of get_error (scf_loop.py:106-147): updates err, dm_err, dm_el,
@@ -202,9 +204,25 @@ int seqm_pair_sum(const seqm_batch *b, const double *pair_val, double *mol_sum, 
  * Force.forward, basics.py:1260-1365): dR[natoms*3] = dE/dR (eV/Angstrom; force = -dR) and
  * dpar[4*natoms] = dE/d(U_ss, U_pp, beta_s, beta_p) per atom (NULL: skip).  Integrals,
  * overlaps and core-core terms are recomputed with forward-mode derivatives, not stored.
- * work: scratch of 7*npairs doubles. */
-int seqm_energy_grad(const seqm_batch *b, const double *P, const double *gE, const double *gN, double *dR,
-                     double *dpar, double *work, void *stream);
+ * work: scratch of 7*npairs doubles.  Pbeta (NULL: restricted, P the total density): P and
+ * Pbeta are the alpha and beta densities of an unrestricted solve. */
+int seqm_energy_grad(const seqm_batch *b, const double *P, const double *Pbeta, const double *gE, const double *gN,
+                     double *dR, double *dpar, double *work, void *stream);
+
+/* Unrestricted Fock matrices (fock_u_batch, seqm/seqm_functions/fock_u_batch.py:18-100):
+ * Fa, Fb of the spin densities Pa, Pb (Coulomb of Pa + Pb, exchange of the spin density,
+ * spin-resolved one-centre terms), for active molecules. */
+int seqm_fock_u(const seqm_batch *b, const double *Pa, const double *Pb, const double *H, const double *w_xx,
+                const double *w_xh, const double *w_hh, double *Fa, double *Fb, const uint8_t *active,
+                void *stream);
+
+/* Unrestricted energy 1/2 sum [(Pa + Pb) H + Pa Fa + Pb Fb] (energy.py:44-45) and, with
+ * Pa_old/Pb_old, the get_error test (scf_loop.py:106-147) on the spin-summed density change;
+ * same outputs as seqm_energy_error. */
+int seqm_energy_error_u(const seqm_batch *b, const double *Pa, const double *Pb, const double *Pa_old,
+                        const double *Pb_old, const double *H, const double *Fa, const double *Fb, double *Eelec,
+                        double *Eout, double *err, double *dm_err, double *dm_el, uint8_t *active, double eps,
+                        void *stream);
 
 /* Library build string (host memory; no GPU needed). */
 const char *seqm_version(void);

@@ -11,10 +11,12 @@ beta_p through ``SCFEnergyFunction``, whose backward is the adjoint kernel
 (seqm_energy_grad) evaluated at the converged density, which is what the
 reference's SCF0 boundary implies (scf_loop.py:1996-2031).
 
-Supported: closed-shell MNDO/AM1/PM3, scf_converger [0, alpha], [1] and [2] (DIIS), sp2,
-learned parameters (values for any parameter; gradients for U_ss, U_pp, beta_s,
-beta_p).  UHF, PM6, excited states, scf_backward >= 1 and a finite
-pair_outer_cutoff raise NotImplementedError.
+Supported: MNDO/AM1/PM3, closed shell (scf_converger [0, alpha], [1] and [2] (DIIS), sp2)
+and unrestricted open shell (``UHF``: True with the Molecule's ``mult``; scf_converger
+[0, alpha] and [1], as the reference has neither open-shell DIIS nor SP2), learned
+parameters (values for any parameter; gradients for U_ss, U_pp, beta_s, beta_p).  PM6,
+excited states, scf_backward >= 1 and a finite pair_outer_cutoff raise
+NotImplementedError.
 """
 
 import copy
@@ -25,7 +27,7 @@ import torch
 
 from . import native, tables
 from .layout import Layout
-from .scf import BatchSCF
+from .scf import BatchSCF, BatchUHF
 
 TO_DEBYE = 1.60217733e-19 * 1e-10 * 2.99792458e8 / 1e-21  # seqm/seqm_functions/constants.py:13-15
 DEBYE_TO_AU = 0.393456
@@ -63,7 +65,11 @@ def _check_options(seqm_parameters):
     if seqm_parameters.get("method") not in tables.METHOD_FIELDS:
         raise NotImplementedError(f"method {seqm_parameters.get('method')!r}: supported are MNDO, AM1, PM3")
     if seqm_parameters.get("UHF", False):
-        raise NotImplementedError("UHF is not supported by pyseqm_gb300 (closed-shell RHF only)")
+        if seqm_parameters.get("sp2", [False])[0]:
+            raise NotImplementedError("SP2 has no open-shell form (the reference's SP2.py raises for UHF)")
+        if seqm_parameters.get("scf_converger", [1])[0] == 2:
+            raise NotImplementedError("DIIS has no open-shell form in the reference (scf_converger [0, alpha] or "
+                                      "[1] with UHF)")
     if seqm_parameters.get("excited_states"):
         raise NotImplementedError("excited states are not supported by pyseqm_gb300")
     if seqm_parameters.get("scf_backward", 0) != 0:
@@ -86,6 +92,8 @@ class Parser(torch.nn.Module):
                                "Electronic_structure or Molecular_Dynamics class.Alternately, provide a list called "
                                "of unique elements in the input molecules under the 'elements' key in seqm_parameters")
         self.elements = seqm_parameters["elements"]
+        self.uhf = seqm_parameters.get("UHF", False)
+        self.hipnn_automatic_doublet = seqm_parameters.get("HIPNN_automatic_doublet", False)
 
     def forward(self, molecule, themethod, return_mask_l=False, do_large_tensors=True, *args, **kwargs):
         species = molecule.species
@@ -102,9 +110,21 @@ class Parser(torch.nn.Module):
         nel = el["tore"][sp].sum(1).astype(np.int64)
         if torch.is_tensor(molecule.tot_charge):
             nel = nel - molecule.tot_charge.detach().cpu().numpy().reshape(-1).astype(np.int64)
-        if np.any(nel % 2 == 1):
-            raise ValueError("RHF setting requires closed shell systems (even number of electrons)")
-        nocc = nel // 2
+        if self.uhf:
+            # alpha / beta occupations from the multiplicity (basics.py:279-294)
+            s2 = np.asarray(torch.as_tensor(molecule.mult).detach().cpu(), dtype=np.float64).reshape(-1) - 1.0
+            na, nb = nel / 2.0 + s2 / 2.0, nel / 2.0 - s2 / 2.0
+            odd = (na % 1 != 0) | (nb % 1 != 0)
+            if odd.any():
+                if not self.hipnn_automatic_doublet:
+                    raise ValueError("Invalid charge/multiplicity combination!")
+                na[odd] += 0.5
+                nb[odd] -= 0.5
+            nocc = np.stack((na, nb), axis=1).astype(np.int64)
+        else:
+            if np.any(nel % 2 == 1):
+                raise ValueError("RHF setting requires closed shell systems (even number of electrons)")
+            nocc = nel // 2
         maskd = ((np.arange(molsize) * (molsize + 1))[None, :] + (np.arange(nmol) * molsize**2)[:, None]).reshape(-1)
         maskd = maskd[real_atoms]
         atom_molid = np.repeat(np.arange(nmol), molsize)[real_atoms]
@@ -229,8 +249,17 @@ class _Solve:
         learned = {k: v.detach().cpu().numpy() for k, v in molecule.parameters.items()
                    if k in native.PAR and torch.is_tensor(v)}
         charges = molecule.tot_charge.detach().cpu().numpy() if torch.is_tensor(molecule.tot_charge) else None
-        self.L = Layout.from_padded(sp, xyz, molecule.method, charges, learned).to_device(self.dev)
-        self.s = BatchSCF(self.L)
+        self.uhf = bool(seqm_parameters.get("UHF", False))
+        mult = None
+        if self.uhf:
+            nocc = getattr(molecule, "nocc", None)
+            if torch.is_tensor(nocc) and nocc.dim() == 2:  # the parser's alpha / beta counts
+                nocc = nocc.detach().cpu().numpy()
+                mult = nocc[:, 0] - nocc[:, 1] + 1
+            else:
+                mult = np.asarray(torch.as_tensor(molecule.mult).detach().cpu(), dtype=np.float64).reshape(-1)
+        self.L = Layout.from_padded(sp, xyz, molecule.method, charges, learned, mult=mult).to_device(self.dev)
+        self.s = BatchUHF(self.L) if self.uhf else BatchSCF(self.L)
         self.opts = seqm_parameters
         self.P0 = P0
         self.timing = {}
@@ -245,7 +274,11 @@ class _Solve:
         t0 = time.time()
         P0 = None
         if self.P0 is not None:
-            P0 = self.L.padded_to_packed(self.P0.detach().to(self.dev, torch.float64))
+            P0 = self.P0.detach().to(self.dev, torch.float64)
+            if self.uhf:  # (nmol, 2, N, N) spin densities
+                P0 = (self.L.padded_to_packed(P0[:, 0]), self.L.padded_to_packed(P0[:, 1]))
+            else:
+                P0 = self.L.padded_to_packed(P0)
         eps = float(o["scf_eps"]) if not torch.is_tensor(o["scf_eps"]) else float(o["scf_eps"].item())
         self.notconverged = self.s.scf(eps, tuple(o.get("scf_converger", [1])), tuple(o.get("sp2", [False])), P0)
         self.Eelec, self.Enuc = self.s.final(want_vectors=o.get("eig", True))
@@ -261,17 +294,21 @@ class _Solve:
         work = torch.empty(7 * max(1, L.npairs), dtype=torch.float64, device=self.dev)
         lib = native.load()
         self.s.launches += 2
-        native.check(lib.seqm_energy_grad(L.struct, native.ptr(self.s.P), native.ptr(gE.contiguous()),
+        Pb = native.ptr(self.s.Pb) if self.uhf else None
+        native.check(lib.seqm_energy_grad(L.struct, native.ptr(self.s.P), Pb, native.ptr(gE.contiguous()),
                                           native.ptr(gN.contiguous()), native.ptr(dR), native.ptr(dpar),
                                           native.ptr(work), self.s._s()), "seqm_energy_grad")
         return dR[: 3 * L.natoms].view(L.natoms, 3), dpar[: 4 * L.natoms].view(4, L.natoms)
 
     # ------------------------------------------------------- padded outputs
-    def padded(self, flat):
-        return self.L.packed_to_padded(flat)
+    def padded(self, flat, flat_b=None):
+        """Padded (nmol, N, N) matrices; with a beta-spin array, (nmol, 2, N, N) as the reference's
+        unrestricted outputs."""
+        if flat_b is None:
+            return self.L.packed_to_padded(flat)
+        return torch.stack((self.L.packed_to_padded(flat), self.L.packed_to_padded(flat_b)), dim=1)
 
-    def eigen_padded(self):
-        """e (nmol, 4*molsize) zero-padded and v (nmol, nmax, nmax) with eigenvectors as columns."""
+    def _eigen_one(self, evals, evecs):
         L = self.L
         n4 = 4 * L.molsize
         nmax = int(L.norb.max())
@@ -279,11 +316,20 @@ class _Solve:
         v = torch.zeros(L.nmol, nmax, nmax, dtype=torch.float64, device=self.dev)
         for m in range(L.nmol):
             n = int(L.norb[m])
-            e[m, :n] = self.s.evals[int(L.row_off[m]): int(L.row_off[m]) + n]
-            v[m, :n, :n] = L.block(self.s.evecs, m).t()
+            e[m, :n] = evals[int(L.row_off[m]): int(L.row_off[m]) + n]
+            v[m, :n, :n] = L.block(evecs, m).t()
             if n < nmax:
                 v[m, n:, n:] = torch.eye(nmax - n, dtype=torch.float64, device=self.dev)
         return e, v
+
+    def eigen_padded(self):
+        """e (nmol, 4*molsize) zero-padded and v (nmol, nmax, nmax) with eigenvectors as columns;
+        unrestricted: e (nmol, 2, 4*molsize) and v (nmol, 2, nmax, nmax) (diag.py:205-208)."""
+        e, v = self._eigen_one(self.s.evals, self.s.evecs)
+        if not self.uhf:
+            return e, v
+        eb, vb = self._eigen_one(self.s.evals_b, self.s.evecs_b)
+        return torch.stack((e, eb), dim=1), torch.stack((v, vb), dim=1)
 
     def w_reference_order(self):
         L = self.L
@@ -337,7 +383,7 @@ def _dipole(molecule, solve):
     """Ground-state dipole from the diagonal density blocks (dipole.py:85-107), on the device."""
     L = solve.L
     dev = solve.dev
-    P = solve.s.P
+    P = solve.s.P + solve.s.Pb if solve.uhf else solve.s.P  # open shell: both spins (dipole.py:91-94)
     xyz = torch.as_tensor(L.xyz, device=dev)
     Z = L.Z
     el = tables.elements()
@@ -364,7 +410,10 @@ def _dipole(molecule, solve):
 
 
 def _orbital_charges(molecule, solve, v):
-    """Per-orbital atomic charges as the reference forms them (scf_loop.py:2333-2388)."""
+    """Per-orbital atomic charges as the reference forms them (scf_loop.py:2333-2388); open
+    shell: the mean of the two spins' values (scf_loop.py:2344-2371)."""
+    if v.dim() == 4:
+        return 0.5 * (_orbital_charges(molecule, solve, v[:, 0]) + _orbital_charges(molecule, solve, v[:, 1]))
     L = solve.L
     nmol, molsize = L.nmol, L.molsize
     charge = torch.zeros(nmol, molsize * 4, molsize, device=v.device, dtype=v.dtype)
@@ -398,8 +447,8 @@ class Hamiltonian(torch.nn.Module):
 
 
 def _hamiltonian_outputs(molecule, s, eig=True):
-    F = s.padded(s.s.F)
-    P = s.padded(s.s.P)
+    F = s.padded(s.s.F, s.s.Fb if s.uhf else None)
+    P = s.padded(s.s.P, s.s.Pb if s.uhf else None)
     H = s.padded(s.s.H)
     w = s.w_reference_order()
     nc = torch.as_tensor(s.notconverged, device=F.device)
@@ -461,8 +510,19 @@ class Energy(torch.nn.Module):
         F, e, P, H, w, charge, rho0xi, rho0xj, _, _, nc, v = _hamiltonian_outputs(molecule, s, self.eig)
         molecule.w = w.to(dev)
         if self.eig:
-            lumo = molecule.nocc.unsqueeze(0).T.to(e.device)
-            e_gap = (e.gather(1, lumo) - e.gather(1, lumo - 1)).reshape(-1).to(dev)
+            if s.uhf:  # per-spin gaps; none when a spin has no occupied orbital (basics.py:829-840)
+                nocc = molecule.nocc.to(e.device)
+                if bool((nocc == 0).any()):
+                    e_gap = torch.tensor([])
+                else:
+                    la, lb = nocc[:, 0].unsqueeze(0).T, nocc[:, 1].unsqueeze(0).T
+                    ga = e[:, 0].gather(1, la) - e[:, 0].gather(1, la - 1)
+                    gb = e[:, 1].gather(1, lb) - e[:, 1].gather(1, lb - 1)
+                    e_gap = torch.stack((ga.reshape(-1), gb.reshape(-1)), dim=1)
+                e_gap = e_gap.to(dev)
+            else:
+                lumo = molecule.nocc.unsqueeze(0).T.to(e.device)
+                e_gap = (e.gather(1, lumo) - e.gather(1, lumo - 1)).reshape(-1).to(dev)
             molecule.molecular_orbitals = v.to(dev)
             e = e.to(dev)
         else:
@@ -545,7 +605,11 @@ class Electronic_Structure(torch.nn.Module):
             molecule, P0=P0, learned_parameters=learned_parameters)
         molecule.dm = P.detach()
         with torch.no_grad():
-            molecule.q = molecule.const.tore[molecule.species] - self.atomic_charges(molecule.dm)
+            if molecule.dm.dim() == 4:  # open shell: both spins (ElectronicStructure.py:106-117)
+                molecule.q = (molecule.const.tore[molecule.species] - self.atomic_charges(molecule.dm[:, 0])
+                              - self.atomic_charges(molecule.dm[:, 1]))
+            else:
+                molecule.q = molecule.const.tore[molecule.species] - self.atomic_charges(molecule.dm)
 
     def get_force(self):
         return self.force

@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(NT_RED) k_energy_error(seqm_batch b, const dou
 // linear: P <- alpha P + (1 - alpha) Pnew (scf_loop.py:258-267);
 // adaptive (scf_loop.py:360-420): every third iteration extrapolate
 // P <- (1+FAC) Pnew - FAC P with FAC from the diagonal history; the diagonal is
-// damped (|step| <= 0.05 after iteration 4), clamped to [0, 2] and renormalised
+// damped (|step| <= 0.05 after iteration 4), clamped to [0, occupation] and renormalised
 // to the new trace in at most 20 passes.  Each molecule stops its own
 // renormalisation (the reference stops when the whole padded batch is done).
 //
@@ -365,7 +365,8 @@ constexpr int NT_MIX = 512, MIX_UNROLL = 4;
 __global__ void __launch_bounds__(NT_MIX) k_mix(seqm_batch b, double *__restrict__ P, const double *__restrict__ Pnew,
                                                 double *__restrict__ Pold, double *__restrict__ old2,
                                                 const int64_t *__restrict__ row_off, int32_t *__restrict__ kit,
-                                                int linear, double alpha, const uint8_t *__restrict__ active, int cs) {
+                                                int linear, double alpha, double occ,
+                                                const uint8_t *__restrict__ active, int cs) {
   extern __shared__ double sm[];
   __shared__ double red[NT_MIX / 32];
   cg::cluster_group cl = cg::this_cluster();
@@ -446,7 +447,7 @@ __global__ void __launch_bounds__(NT_MIX) k_mix(seqm_batch b, double *__restrict
       const double delta = dc - dp;
       const double v =
           fabs(delta) > damp ? dp + (delta > 0.0 ? 1.0 : (delta < 0.0 ? -1.0 : 0.0)) * damp : dc + fac * delta;
-      di[i] = fmin(fmax(v, 0.0), 2.0);
+      di[i] = fmin(fmax(v, 0.0), occ);
       s0 += dc;
     }
     double sum0 = block_sum<NT_MIX>(s0, red);
@@ -459,12 +460,12 @@ __global__ void __launch_bounds__(NT_MIX) k_mix(seqm_batch b, double *__restrict
       double nfull = 0.0;
       for (int i = threadIdx.x; i < n; i += NT_MIX) {
         const double sc = fmax(di[i] * sum3, 0.0);
-        const bool full = sc > 2.0;
-        di[i] = full ? 2.0 : sc;
+        const bool full = sc > occ;
+        di[i] = full ? occ : sc;
         nfull += full ? 1.0 : 0.0;
       }
       nfull = block_sum<NT_MIX>(nfull, red);
-      sum0 = sum0 - nfull * 2.0;
+      sum0 = sum0 - nfull * occ;
     }
   }
   cl.sync();  // every CTA's provisional diagonal is written
@@ -549,8 +550,8 @@ extern "C" int seqm_energy_error(const seqm_batch *bp, const double *P, const do
 }
 
 extern "C" int seqm_mix(const seqm_batch *bp, double *P, const double *Pnew, double *Pold, double *old2,
-                        const int64_t *mol_row_off, int32_t *k, int linear, double alpha, const uint8_t *active,
-                        void *stream) {
+                        const int64_t *mol_row_off, int32_t *k, int linear, double alpha, double occupation,
+                        const uint8_t *active, void *stream) {
   if (!bp) return SEQM_E_ARG;
   seqm_batch b = *bp;
   if (b.nmol == 0) return SEQM_OK;
@@ -560,7 +561,7 @@ extern "C" int seqm_mix(const seqm_batch *bp, double *P, const double *Pnew, dou
     return SEQM_E_CUDA;
   const int cs = mol_cluster(k_mix, b.max_norb);
   return launch_clusters(k_mix, cs, b.nmol, NT_MIX, smem, stream, b, P, Pnew, Pold, old2, mol_row_off, k, linear, alpha,
-                         active, cs);
+                         occupation, active, cs);
 }
 
 extern "C" int seqm_initial_density(const seqm_batch *bp, double *P, void *stream) {

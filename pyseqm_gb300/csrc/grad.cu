@@ -9,7 +9,8 @@
 //        + sum_{mu in A, nu in B} P_mu,nu (beta_mu + beta_nu) S_mu,nu(R)   (resonance)
 //        + Enuc_AB(R)                                           (core-core)
 //
-// with D_ab = P_A[a] P_B[b] - 1/2 sum P_AB P_AB (exchange) - Z_B P_A[a] d_b0 - Z_A P_B[b] d_a0.
+// with D_ab = P_A[a] P_B[b] - 1/2 sum P_AB P_AB (exchange) - Z_B P_A[a] d_b0 - Z_A P_B[b] d_a0
+// (unrestricted: P the total density and the exchange term sum_s P_s,AB P_s,AB).
 // Each pair thread evaluates E_AB with dual numbers carrying d/d(Rj - Ri) (the same
 // templated integral code as the forward kernel, recomputed rather than stored), so
 // one pass gives the 3-vector gradient; a per-atom gather (no atomics) then forms
@@ -52,8 +53,8 @@ __device__ __forceinline__ double exch(const double Pab[4][4], int a, int c) {
 constexpr int GRAD_STRIDE = 7;  // per pair: dE/d(Rj-Ri) x3, d beta_s(i), d beta_p(i), d beta_s(j), d beta_p(j)
 
 __global__ void __launch_bounds__(128) k_pair_grad(seqm_batch b, const double *__restrict__ P,
-                                                   const double *__restrict__ gE, const double *__restrict__ gN,
-                                                   double *__restrict__ work) {
+                                                   const double *__restrict__ Pbeta, const double *__restrict__ gE,
+                                                   const double *__restrict__ gN, double *__restrict__ work) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const int npairs = b.nxx + b.nxh + b.nhh;
   if (p >= npairs) return;
@@ -68,13 +69,36 @@ __global__ void __launch_bounds__(128) k_pair_grad(seqm_batch b, const double *_
   const bool hi = li < nh, hj = lj < nh;
   const int ni_ = hi ? 4 : 1, nj_ = hj ? 4 : 1;
   const double *Pm = P + b.mol_mat_off[m];
-  double PA[10], PB[10], Pab[4][4];
+  // unrestricted (Pbeta != NULL): P is the alpha density; Coulomb, core and resonance terms
+  // take the total density and the exchange term both spin densities
+  const double *Qm = Pbeta ? Pbeta + b.mol_mat_off[m] : nullptr;
+  double PA[10], PB[10], Pab[4][4], Pa_ab[4][4], Pb_ab[4][4];
   grad_packed(Pm, norb, oi, hi, PA);
   grad_packed(Pm, norb, oj, hj, PB);
+  if (Qm) {
+    double QA[10], QB[10];
+    grad_packed(Qm, norb, oi, hi, QA);
+    grad_packed(Qm, norb, oj, hj, QB);
+#pragma unroll
+    for (int k = 0; k < 10; ++k) {
+      PA[k] += QA[k];
+      PB[k] += QB[k];
+    }
+  }
 #pragma unroll
   for (int u = 0; u < 4; ++u)
 #pragma unroll
-    for (int v = 0; v < 4; ++v) Pab[u][v] = (u < ni_ && v < nj_) ? Pm[(size_t)(oi + u) * norb + oj + v] : 0.0;
+    for (int v = 0; v < 4; ++v) {
+      const bool in = u < ni_ && v < nj_;
+      const size_t ix = (size_t)(oi + u) * norb + oj + v;
+      Pa_ab[u][v] = in ? Pm[ix] : 0.0;
+      Pb_ab[u][v] = (in && Qm) ? Qm[ix] : 0.0;
+      Pab[u][v] = Pa_ab[u][v] + Pb_ab[u][v];
+    }
+  // exchange part of D: 1/2 exch(P) restricted, exch(Pa) + exch(Pb) unrestricted
+  auto xch = [&](int a, int c) {
+    return Qm ? exch(Pa_ab, a, c) + exch(Pb_ab, a, c) : 0.5 * exch(Pab, a, c);
+  };
   const double ZA = par(b, SEQM_P_TORE, ia), ZB = par(b, SEQM_P_TORE, ja);
 
   // geometry as dual numbers: seeds on the three components of Rj - Ri (Angstrom)
@@ -96,7 +120,7 @@ __global__ void __launch_bounds__(128) k_pair_grad(seqm_batch b, const double *_
                       r0a, r0b, par(b, SEQM_P_RHO1, ia), par(b, SEQM_P_RHO1, ja), par(b, SEQM_P_RHO2, ia),
                       par(b, SEQM_P_RHO2, ja), ri);
       rotate_xx<Dual3>(ri, R, [&](int a, int c, Dual3 w) {
-        double D = PA[a] * PB[c] - 0.5 * exch(Pab, a, c);
+        double D = PA[a] * PB[c] - xch(a, c);
         if (c == 0) D -= ZB * PA[a];
         if (a == 0) D -= ZA * PB[c];
         E += (ge * D) * w;
@@ -107,14 +131,15 @@ __global__ void __launch_bounds__(128) k_pair_grad(seqm_batch b, const double *_
       local_xh<Dual3>(r, par(b, SEQM_P_DD, ia), par(b, SEQM_P_QQ, ia), r0a, r0b, par(b, SEQM_P_RHO1, ia),
                       par(b, SEQM_P_RHO2, ia), ri);
       rotate_xh<Dual3>(ri, R, [&](int a, Dual3 w) {
-        double D = PA[a] * PB[0] - 0.5 * exch(Pab, a, 0) - ZB * PA[a];
+        double D = PA[a] * PB[0] - xch(a, 0) - ZB * PA[a];
         if (a == 0) D -= ZA * PB[0];
         E += (ge * D) * w;
       });
       gam = ri[0];
     } else {
       gam = EV / sqrt(r * r + (r0a + r0b) * (r0a + r0b));
-      double D = PA[0] * PB[0] - 0.5 * Pab[0][0] * Pab[0][0] - ZB * PA[0] - ZA * PB[0];
+      const double x00 = Qm ? Pa_ab[0][0] * Pa_ab[0][0] + Pb_ab[0][0] * Pb_ab[0][0] : 0.5 * Pab[0][0] * Pab[0][0];
+      double D = PA[0] * PB[0] - x00 - ZB * PA[0] - ZA * PB[0];
       E += (ge * D) * gam;
     }
     if (gn != 0.0) E += gn * core_core<Dual3>(b, ia, ja, r, gam);
@@ -145,8 +170,9 @@ __global__ void __launch_bounds__(128) k_pair_grad(seqm_batch b, const double *_
 
 // per atom: dE/dR = sum over pairs where the atom is second (+g) and first (-g);
 // parameter gradients: beta from the pair terms, U from the diagonal density
-__global__ void k_atom_grad(seqm_batch b, const double *__restrict__ P, const double *__restrict__ gE,
-                            const double *__restrict__ work, double *__restrict__ dR, double *__restrict__ dpar) {
+__global__ void k_atom_grad(seqm_batch b, const double *__restrict__ P, const double *__restrict__ Pbeta,
+                            const double *__restrict__ gE, const double *__restrict__ work, double *__restrict__ dR,
+                            double *__restrict__ dpar) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= b.natoms) return;
   const int m = b.atom_mol[a];
@@ -162,21 +188,22 @@ __global__ void k_atom_grad(seqm_batch b, const double *__restrict__ P, const do
     const double *w = work + (size_t)GRAD_STRIDE * p;
     g0 += w[0]; g1 += w[1]; g2 += w[2]; dbs += w[5]; dbp += w[6];
   };
-  const double *Pm = P + b.mol_mat_off[m];
+  const double *Pm = P + b.mol_mat_off[m], *Qm = Pbeta ? Pbeta + b.mol_mat_off[m] : nullptr;
+  auto ptot = [&](int o) { return Pm[(size_t)o * norb + o] + (Qm ? Qm[(size_t)o * norb + o] : 0.0); };
   double duss, dupp = 0.0;
   if (la < nh) {
     for (int j = la + 1; j < nh; ++j) first(xx0 + tri_index(la, j, nh));
     for (int h = 0; h < ny; ++h) first(xh0 + la * ny + h);
     for (int i = 0; i < la; ++i) second(xx0 + tri_index(i, la, nh));
     const int o = 4 * la;
-    duss = Pm[(size_t)o * norb + o];
-    for (int k = 1; k < 4; ++k) dupp += Pm[(size_t)(o + k) * norb + o + k];
+    duss = ptot(o);
+    for (int k = 1; k < 4; ++k) dupp += ptot(o + k);
   } else {
     const int h = la - nh, o = 3 * nh + la;
     for (int i = 0; i < nh; ++i) second(xh0 + i * ny + h);
     for (int g = h + 1; g < ny; ++g) first(hh0 + tri_index(h, g, ny));
     for (int g = 0; g < h; ++g) second(hh0 + tri_index(g, h, ny));
-    duss = Pm[(size_t)o * norb + o];
+    duss = ptot(o);
   }
   dR[3 * a] = g0;
   dR[3 * a + 1] = g1;
@@ -194,14 +221,14 @@ __global__ void k_atom_grad(seqm_batch b, const double *__restrict__ P, const do
 
 using namespace seqm;
 
-extern "C" int seqm_energy_grad(const seqm_batch *bp, const double *P, const double *gE, const double *gN, double *dR,
-                                double *dpar, double *work, void *stream) {
+extern "C" int seqm_energy_grad(const seqm_batch *bp, const double *P, const double *Pbeta, const double *gE,
+                                const double *gN, double *dR, double *dpar, double *work, void *stream) {
   if (!bp || !P || !gE || !gN || !dR || !work) return SEQM_E_ARG;
   seqm_batch b = *bp;
   if (b.natoms == 0) return SEQM_OK;
   cudaStream_t s = (cudaStream_t)stream;
   const int npairs = b.nxx + b.nxh + b.nhh;
-  if (npairs > 0) k_pair_grad<<<(npairs + 127) / 128, 128, 0, s>>>(b, P, gE, gN, work);
-  k_atom_grad<<<(b.natoms + 127) / 128, 128, 0, s>>>(b, P, gE, work, dR, dpar);
+  if (npairs > 0) k_pair_grad<<<(npairs + 127) / 128, 128, 0, s>>>(b, P, Pbeta, gE, gN, work);
+  k_atom_grad<<<(b.natoms + 127) / 128, 128, 0, s>>>(b, P, Pbeta, gE, work, dR, dpar);
   return launch_check();
 }

@@ -42,7 +42,9 @@ class Layout:
 
     # ------------------------------------------------------------------ build
     @classmethod
-    def from_padded(cls, species, coords, method, charges=None, learned=None):
+    def from_padded(cls, species, coords, method, charges=None, learned=None, mult=None):
+        """mult: spin multiplicities for an unrestricted solve (nocc_a / nocc_b = alpha / beta
+        occupations, basics.py:278-295); None: closed shells."""
         species = np.ascontiguousarray(np.asarray(species, dtype=np.int64))
         coords = np.asarray(coords, dtype=np.float64)
         if species.ndim != 2 or coords.shape != species.shape + (3,):
@@ -64,9 +66,18 @@ class Layout:
         nel = el["tore"][species].sum(1).astype(np.int64)
         if charges is not None:
             nel = nel - np.asarray(charges, dtype=np.float64).reshape(-1).astype(np.int64)
-        if np.any(nel % 2 == 1):
-            raise ValueError("RHF setting requires closed shell systems (even number of electrons)")
-        L.nocc = nel // 2
+        L.uhf = mult is not None
+        if L.uhf:
+            s2 = np.asarray(mult, dtype=np.float64).reshape(-1) - 1.0
+            na, nb = nel / 2.0 + s2 / 2.0, nel / 2.0 - s2 / 2.0
+            if np.any(na % 1 != 0) or np.any(nb % 1 != 0) or np.any(nb < 0):
+                raise ValueError("Invalid charge/multiplicity combination!")
+            L.nocc_a, L.nocc_b = na.astype(np.int64), nb.astype(np.int64)
+            L.nocc = L.nocc_a
+        else:
+            if np.any(nel % 2 == 1):
+                raise ValueError("RHF setting requires closed shell systems (even number of electrons)")
+            L.nocc = nel // 2
         L.atom_off = np.concatenate([[0], np.cumsum(L.natoms_m)])
         L.natoms = int(L.atom_off[-1])
         L.real_index = np.nonzero(real.reshape(-1))[0]  # flat padded index of every real atom
@@ -122,6 +133,8 @@ class Layout:
             "xyz": f64(self.xyz.reshape(-1)), "par": f64(self.par.reshape(-1)),
             "pair_i": i32(self.pair_i), "pair_j": i32(self.pair_j),
         }
+        if self.uhf:
+            d["nocc_a"], d["nocc_b"] = i32(self.nocc_a), i32(self.nocc_b)
         self.dev = d
         self.device = torch.device(device)
         self._struct = native.SeqmBatch(

@@ -29,7 +29,7 @@ PAR = {n: i for i, n in enumerate(PAR_NAMES)}
 EXPORTS = ["seqm_hcore", "seqm_fock", "seqm_density_jacobi", "seqm_density_jacobi_noalloc", "seqm_density_sp2",
            "seqm_density_sp2_tc", "seqm_mix", "seqm_energy_error",
            "seqm_initial_density", "seqm_pair_sum", "seqm_energy_grad", "seqm_sp2_tc_work_bytes", "seqm_diis_init",
-           "seqm_diis_extrapolate", "seqm_diis_mix", "seqm_version"]
+           "seqm_diis_extrapolate", "seqm_diis_mix", "seqm_fock_u", "seqm_energy_error_u", "seqm_version"]
 DIIS_STATE = 124  # SEQM_DIIS_STATE
 
 _P = ctypes.c_void_p
@@ -74,14 +74,16 @@ def load(path=None):
         "seqm_density_jacobi_noalloc": [B, _P, _P, _P, _P, _P, _P, _P, i32, _P],
         "seqm_density_sp2": [B, _P, _P, _P, f64, _P, _P, i32, _P],
         "seqm_density_sp2_tc": [B, _P, _P, _P, f64, _P, _P, i32, i32, _P],
-        "seqm_mix": [B, _P, _P, _P, _P, _P, _P, i32, f64, _P, _P],
+        "seqm_mix": [B, _P, _P, _P, _P, _P, _P, i32, f64, f64, _P, _P],
         "seqm_energy_error": [B, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, f64, _P, _P],
         "seqm_diis_init": [B, _P, _P, _P],
         "seqm_diis_extrapolate": [B, _P, _P, _P, _P, _P, _P, _P, _P],
         "seqm_diis_mix": [B, _P, _P, _P, _P, _P, _P],
         "seqm_initial_density": [B, _P, _P],
         "seqm_pair_sum": [B, _P, _P, _P],
-        "seqm_energy_grad": [B, _P, _P, _P, _P, _P, _P, _P],
+        "seqm_energy_grad": [B, _P, _P, _P, _P, _P, _P, _P, _P],
+        "seqm_fock_u": [B, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
+        "seqm_energy_error_u": [B, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, f64, _P],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

@@ -294,7 +294,7 @@ class BatchSCF:
         else:
             native.check(self.lib.seqm_mix(L.struct, native.ptr(self.P), native.ptr(self.Pnew),
                                            native.ptr(self.Pold), native.ptr(self.old2), native.ptr(L.dev["row_off"]),
-                                           native.ptr(self.iters), int(self._linear), self._alpha,
+                                           native.ptr(self.iters), int(self._linear), self._alpha, 2.0,
                                            native.ptr(self.active), self._s()), "seqm_mix")
         self.fock(self.active)
         self.energy_error(self._eps)
@@ -340,16 +340,167 @@ class BatchSCF:
         return self.Eout[: self.L.nmol].clone(), self.Enuc[: self.L.nmol].clone()
 
 
+class BatchUHF(BatchSCF):
+    """Unrestricted SCF (UHF) of a batch of molecules with given spin multiplicities: the
+    reference's scf_forward0/1 with unrestricted=True (scf_loop.py:194-635).  Each spin has its
+    own density (starting at half the restricted guess, scf_loop.py:2083-2085), Fock matrix
+    (seqm_fock_u), Jacobi density step with occupation 1 (the eigensolver's 2 C C^T halved,
+    scf_loop.py:259-260 / 515-516), warm-start vectors and mixing state (occupation 1); the
+    energy and the convergence test cover both spins (seqm_energy_error_u).  The inherited
+    buffers (P, F, Pnew, Pold, work, evals, ...) hold the alpha spin.  SP2 has no open-shell
+    form in the reference (SP2.py raises), so molecules above the Jacobi limit are rejected."""
+
+    def __init__(self, layout, stream=None):
+        if not getattr(layout, "uhf", False):
+            raise ValueError("BatchUHF needs a layout built with spin multiplicities (mult)")
+        super().__init__(layout, stream)
+        if self.n_large:
+            raise NotImplementedError(f"unrestricted SCF is limited to {JACOBI_MAX_N} basis functions per molecule "
+                                      "(the reference has no open-shell SP2)")
+        L, dev = layout, layout.device
+        f64 = dict(dtype=torch.float64, device=dev)
+        T, R, nm = int(L.mat_off[-1]), int(L.row_off[-1]), L.nmol
+        self.Pb = torch.zeros(max(1, T), **f64)
+        self.Fb = torch.empty(max(1, T), **f64)
+        self.Pnewb = torch.empty(max(1, T), **f64)
+        self.Poldb = torch.empty(max(1, T), **f64)
+        self.workb = torch.empty(max(1, T), **f64)
+        self.evals_b = torch.zeros(max(1, R), **f64)
+        self.old2b = torch.zeros(max(1, R), **f64)
+        self.warm_b = torch.zeros(max(1, nm), dtype=torch.uint8, device=dev)
+        self.status_b = torch.zeros(max(1, nm), dtype=torch.int32, device=dev)
+        self.iters_b = torch.zeros(max(1, nm), dtype=torch.int32, device=dev)
+        self._spin_struct = []
+        for key in ("nocc_a", "nocc_b"):  # batch views whose occupations are one spin's
+            v = native.SeqmBatch.from_buffer_copy(L.struct)
+            v.mol_nocc = L.dev[key].data_ptr()
+            self._spin_struct.append(v)
+
+    def fock(self, active=None):
+        L = self.L
+        self.launches += 1
+        native.check(self.lib.seqm_fock_u(L.struct, native.ptr(self.P), native.ptr(self.Pb), native.ptr(self.H),
+                                          native.ptr(self.w_xx), native.ptr(self.w_xh), native.ptr(self.w_hh),
+                                          native.ptr(self.F), native.ptr(self.Fb), native.ptr(active), self._s()),
+                     "seqm_fock_u")
+
+    def energy_error(self, eps, first=False):
+        L = self.L
+        self.launches += 1
+        olds = (None, None) if first else (native.ptr(self.Pold), native.ptr(self.Poldb))
+        native.check(self.lib.seqm_energy_error_u(L.struct, native.ptr(self.P), native.ptr(self.Pb), olds[0], olds[1],
+                                                  native.ptr(self.H), native.ptr(self.F), native.ptr(self.Fb),
+                                                  native.ptr(self.Eelec), native.ptr(self.Eout), native.ptr(self.err),
+                                                  native.ptr(self.dm_err), native.ptr(self.dm_el),
+                                                  None if first else native.ptr(self.active), float(eps), self._s()),
+                     "seqm_energy_error_u")
+
+    def density(self, out=None, sp2=(False,), active=None, evecs=None, max_sweeps=50, density_only=False,
+                evecs_b=None):
+        """Both spins' density steps into Pnew / Pnewb (occupation 1)."""
+        L = self.L
+        if sp2[0]:
+            raise NotImplementedError("SP2 has no open-shell form (SP2.py)")
+        spins = ((self._spin_struct[0], self.F, self.Pnew, self.evals, evecs, self.work, self.status, self.warm),
+                 (self._spin_struct[1], self.Fb, self.Pnewb, self.evals_b, evecs_b, self.workb, self.status_b,
+                  self.warm_b))
+        for struct, F, Pn, ev, vec, work, status, warm in spins:
+            self.launches += 1
+            native.check(self.lib.seqm_density_jacobi(struct, native.ptr(F), native.ptr(Pn), native.ptr(ev),
+                                                      native.ptr(vec), native.ptr(work), native.ptr(L.dev["row_off"]),
+                                                      native.ptr(active), native.ptr(status), max_sweeps,
+                                                      native.ptr(warm), self.mixed_threshold,
+                                                      int(density_only) if self.first_order_density else 0,
+                                                      self._s()), "seqm_density_jacobi")
+            Pn.mul_(0.5)
+            if active is None:
+                warm.fill_(1)
+            else:
+                warm.bitwise_or_(active)
+
+    def start(self, eps, converger=(1,), sp2=(False,), P0=None, keep_warm=False):
+        """P0: (Pa, Pb) packed spin densities, or None for half the restricted guess each."""
+        L = self.L
+        if int(converger[0]) not in (0, 1):
+            raise NotImplementedError("unrestricted SCF supports scf_converger [0, alpha] and [1] "
+                                      "(the reference has no open-shell DIIS)")
+        if sp2[0]:
+            raise NotImplementedError("SP2 has no open-shell form (SP2.py)")
+        if P0 is None:
+            self.P.zero_()
+            self.launches += 1
+            native.check(self.lib.seqm_initial_density(L.struct, native.ptr(self.P), self._s()), "seqm_initial_density")
+            self.P.mul_(0.5)
+            self.Pb.copy_(self.P)
+        else:
+            self.P.copy_(P0[0])
+            self.Pb.copy_(P0[1])
+        self.fock()
+        self.energy_error(eps, first=True)
+        self.Eelec.copy_(self.Eout)
+        self.err.fill_(1.0)
+        self.dm_err.fill_(1.0)
+        self.dm_el.fill_(1.0)
+        self.active.fill_(1)
+        self.iters.zero_()
+        self.iters_b.zero_()
+        if not keep_warm:
+            self.warm.zero_()
+            self.warm_b.zero_()
+        self.old2.zero_()
+        self.old2b.zero_()
+        self._eps = float(eps)
+        self._linear = int(converger[0]) == 0
+        self._alpha = float(converger[1]) if self._linear else 0.0
+        self._sp2 = (False,)
+        self._diis = False
+        self._diis_err = None
+
+    def step(self):
+        L = self.L
+        self.density(active=self.active, density_only=True)
+        for P, Pn, Po, o2, it in ((self.P, self.Pnew, self.Pold, self.old2, self.iters),
+                                  (self.Pb, self.Pnewb, self.Poldb, self.old2b, self.iters_b)):
+            self.launches += 1
+            native.check(self.lib.seqm_mix(L.struct, native.ptr(P), native.ptr(Pn), native.ptr(Po), native.ptr(o2),
+                                           native.ptr(L.dev["row_off"]), native.ptr(it), int(self._linear),
+                                           self._alpha, 1.0, native.ptr(self.active), self._s()), "seqm_mix")
+        self.fock(self.active)
+        self.energy_error(self._eps)
+
+    def resume(self, xyz, eps, converger=(1,), sp2=(False,), max_iter=MAX_ITER):
+        self.L.set_coordinates(xyz)
+        self.hcore()
+        self.start(eps, converger, sp2, P0=(self.P.clone(), self.Pb.clone()), keep_warm=True)
+        for _ in range(self.max_loops(max_iter)):
+            self.step()
+            if int(self.active.sum()) == 0:
+                break
+        return self.active[: self.L.nmol].bool().cpu().numpy()
+
+    def final(self, want_vectors=True):
+        """Fock matrices of the converged spin densities, orbital energies (and vectors) per spin,
+        energies."""
+        self.fock()
+        evecs = torch.empty_like(self.work) if want_vectors else None
+        evecs_b = torch.empty_like(self.workb) if want_vectors else None
+        self.density(active=None, evecs=evecs, evecs_b=evecs_b, density_only=2 if evecs is None else 0)
+        self.energy_error(0.0, first=True)
+        self.evecs, self.evecs_b = evecs, evecs_b
+        return self.Eout[: self.L.nmol].clone(), self.Enuc[: self.L.nmol].clone()
+
+
 def ctypes_stream(s):
     return ctypes.c_void_p(s.cuda_stream)
 
 
 def run_energy(species, coords, method, eps=1e-6, converger=(1,), sp2=(False,), charges=None, device="cuda",
-               want_vectors=False):
-    """One batched single point: returns a dict of device tensors and host arrays."""
+               want_vectors=False, mult=None):
+    """One batched single point: returns a dict of device tensors and host arrays.  mult: spin
+    multiplicities for an unrestricted solve."""
     t0 = time.perf_counter()
-    L = Layout.from_padded(species, coords, method, charges).to_device(device)
-    s = BatchSCF(L)
+    L = Layout.from_padded(species, coords, method, charges, mult=mult).to_device(device)
+    s = BatchUHF(L) if mult is not None else BatchSCF(L)
     s.hcore()
     nc = s.scf(eps, converger, sp2)
     Eelec, Enuc = s.final(want_vectors)

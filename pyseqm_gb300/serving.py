@@ -204,7 +204,7 @@ class _Cohort:
                                   torch.empty(4 * max(1, L.natoms), **f64), torch.empty(7 * max(1, L.npairs), **f64))
             g, dR, dpar, work = self._grad_buf
             s.launches += 2
-            native.check(s.lib.seqm_energy_grad(L.struct, native.ptr(s.P), native.ptr(g), native.ptr(g),
+            native.check(s.lib.seqm_energy_grad(L.struct, native.ptr(s.P), None, native.ptr(g), native.ptr(g),
                                                 native.ptr(dR), native.ptr(dpar), native.ptr(work), s._s()),
                          "seqm_energy_grad")
             host = dR[: 3 * L.natoms].cpu()  # synchronises this stream
@@ -364,7 +364,7 @@ class ServingLoop:
             dpar = torch.empty(4 * max(1, L.natoms), **f64)
             work = torch.empty(7 * max(1, L.npairs), **f64)
             s.launches += 2
-            native.check(s.lib.seqm_energy_grad(L.struct, native.ptr(s.P), native.ptr(g), native.ptr(g),
+            native.check(s.lib.seqm_energy_grad(L.struct, native.ptr(s.P), None, native.ptr(g), native.ptr(g),
                                                 native.ptr(dR), native.ptr(dpar), native.ptr(work), s._s()),
                          "seqm_energy_grad")
             forces = dR[: 3 * L.natoms].cpu().numpy().reshape(-1, 3)

@@ -47,7 +47,8 @@ def test_rejects_unsorted_species_and_odd_electrons():
                  torch.rand(1, 4, 3, dtype=torch.float64), torch.tensor([[6, 1, 1, 1]]))
 
 
-@pytest.mark.parametrize("opt", [{"UHF": True}, {"method": "PM6"}, {"scf_backward": 1}, {"scf_converger": [3]},
+@pytest.mark.parametrize("opt", [{"UHF": True, "scf_converger": [2]}, {"UHF": True, "sp2": [True, 1e-5]},
+                                 {"method": "PM6"}, {"scf_backward": 1}, {"scf_converger": [3]},
                                  {"excited_states": {"n_states": 2}}])
 def test_unsupported_options_raise(opt):
     from pyseqm_gb300 import Constants, Molecule
@@ -56,6 +57,23 @@ def test_unsupported_options_raise(opt):
     s.update(opt)
     with pytest.raises(NotImplementedError):
         Molecule(Constants(), s, torch.rand(1, 5, 3, dtype=torch.float64), torch.tensor([[6, 1, 1, 1, 1]]))
+
+
+def test_uhf_occupations_from_multiplicity():
+    """Alpha / beta occupations (basics.py:279-294): (nel + mult - 1) / 2 and (nel - mult + 1) / 2,
+    a ValueError for an impossible combination, doublets by rounding with HIPNN_automatic_doublet."""
+    from pyseqm_gb300 import Constants, Molecule
+
+    s = {"method": "AM1", "scf_eps": 1e-6, "scf_converger": [1], "UHF": True}
+    xyz = torch.tensor([[[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]],
+                        [[0.0, 0.0, 0.0], [1.2, 0.0, 0.0], [0.0, 0.0, 0.0], [0.0, 0.0, 0.0]]], dtype=torch.float64)
+    sp = torch.tensor([[6, 1, 1, 1], [8, 8, 0, 0]])
+    mol = Molecule(Constants(), s, xyz, sp, mult=torch.tensor([2.0, 3.0]))
+    assert mol.nocc.tolist() == [[4, 3], [7, 5]]
+    with pytest.raises(ValueError, match="Invalid charge/multiplicity"):
+        Molecule(Constants(), s, xyz, sp, mult=torch.tensor([1.0, 3.0]))
+    mol = Molecule(Constants(), dict(s, HIPNN_automatic_doublet=True), xyz, sp, mult=torch.tensor([1.0, 1.0]))
+    assert mol.nocc.tolist() == [[4, 3], [6, 6]]
 
 
 def test_unsupported_element_raises():

@@ -9,7 +9,8 @@ from oracle import seqm_oracle as O
 
 pytestmark = pytest.mark.gpu
 
-EIG_CASES = [n for n in GOLDEN_NAMES if "sp2" not in n and "diis" not in n]  # DIIS: per-molecule test below
+# DIIS: per-molecule test below; unrestricted (open-shell) fixtures: test_gpu_uhf.py
+EIG_CASES = [n for n in GOLDEN_NAMES if "sp2" not in n and "diis" not in n and not n.startswith("uhf")]
 
 
 def _run(g, **kw):

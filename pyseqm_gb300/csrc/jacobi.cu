@@ -88,19 +88,22 @@ __device__ void tile_product(int n, bool upper_only, LF L, RF R, OF out) {
   tile_product_t<double>(n, upper_only, L, R, out);
 }
 
-// 4x4-register-tile product out(k, j) <- sum_l L(k, l) R(l, j) for k < M, j < N, l < K
-template <class LF, class RF, class OF>
-__device__ void tile_product_mnk(int M, int N, int K, LF L, RF R, OF out) {
+// 4x4-register-tile product out(k, j) <- sum_l L(k, l) R(l, j) for k < M, j < N, l < K,
+// accumulated in T; with upper_only (M == N) only the tiles on or above the diagonal
+template <class T, class LF, class RF, class OF>
+__device__ void tile_product_mnk_t(int M, int N, int K, bool upper_only, LF L, RF R, OF out) {
   const int mt = (M + 3) >> 2, nt = (N + 3) >> 2;
   for (int t = threadIdx.x; t < mt * nt; t += NT_J) {
-    const int k0 = (t / nt) * 4, j0 = (t % nt) * 4;
-    double acc[4][4] = {};
+    const int kb = t / nt, jb = t % nt;
+    if (upper_only && kb > jb) continue;
+    const int k0 = kb * 4, j0 = jb * 4;
+    T acc[4][4] = {};
     for (int l = 0; l < K; ++l) {
-      double a[4], c[4];
+      T a[4], c[4];
 #pragma unroll
-      for (int r = 0; r < 4; ++r) a[r] = (k0 + r < M) ? L(k0 + r, l) : 0.0;
+      for (int r = 0; r < 4; ++r) a[r] = (k0 + r < M) ? L(k0 + r, l) : T(0);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) c[q] = (j0 + q < N) ? R(l, j0 + q) : 0.0;
+      for (int q = 0; q < 4; ++q) c[q] = (j0 + q < N) ? R(l, j0 + q) : T(0);
 #pragma unroll
       for (int r = 0; r < 4; ++r)
 #pragma unroll
@@ -112,6 +115,11 @@ __device__ void tile_product_mnk(int M, int N, int K, LF L, RF R, OF out) {
       for (int q = 0; q < 4; ++q)
         if (k0 + r < M && j0 + q < N) out(k0 + r, j0 + q, acc[r][q]);
   }
+}
+
+template <class LF, class RF, class OF>
+__device__ void tile_product_mnk(int M, int N, int K, LF L, RF R, OF out) {
+  tile_product_mnk_t<double>(M, N, K, false, L, R, out);
 }
 
 // A (shared, holding F on entry) <- V F V^T; G (global n x n) is scratch
@@ -128,17 +136,26 @@ __device__ void form_vfvt(double *A, int lda, const double *V, double *G, int n)
   __syncthreads();
 }
 
-// A32 (float, shared, overlaying A) <- V F V^T in FP32, with F in A (FP64) on entry; G is
-// global scratch (FP32 view).  Input to FP32 sweeps, which need no more precision.
+// A32 (float, shared, overlaying A) <- V F V^T in FP32, with F in A (FP64) on entry.  V and F
+// are converted once (G as floats: V32 = G[0, n^2), F32 = G[n^2, 2 n^2)) so that the products
+// run on FP32 operands: conversions to and from FP64 issue on the FP64 pipe.  The product
+// V F goes to the upper half of A's space (T32); V32 stays in G for the caller.
+// Input to FP32 sweeps, which need no more precision.
 __device__ void form_vfvt32(double *A, int lda, const double *V, double *G, int n) {
-  float *G32 = reinterpret_cast<float *>(G), *A32 = reinterpret_cast<float *>(A);
-  tile_product_t<float>(
-      n, false, [&](int k, int l) { return (float)V[(size_t)k * n + l]; },
-      [&](int l, int j) { return (float)A[l * lda + j]; }, [&](int k, int j, float v) { G32[(size_t)k * n + j] = v; });
+  float *V32 = reinterpret_cast<float *>(G), *F32 = V32 + (size_t)n * n;
+  float *A32 = reinterpret_cast<float *>(A), *T32 = A32 + (size_t)n * lda;
+  for (int idx = threadIdx.x; idx < n * n; idx += NT_J) {
+    const int i = idx / n, j = idx - i * n;
+    V32[idx] = (float)V[idx];
+    F32[idx] = (float)A[i * lda + j];
+  }
   __syncthreads();
   tile_product_t<float>(
-      n, true, [&](int k, int j) { return G32[(size_t)k * n + j]; },
-      [&](int j, int l) { return (float)V[(size_t)l * n + j]; },
+      n, false, [&](int k, int l) { return V32[k * n + l]; }, [&](int l, int j) { return F32[l * n + j]; },
+      [&](int k, int j, float v) { T32[k * n + j] = v; });
+  __syncthreads();
+  tile_product_t<float>(
+      n, true, [&](int k, int j) { return T32[k * n + j]; }, [&](int j, int l) { return V32[l * n + j]; },
       [&](int k, int l, float v) {
         if (k <= l) { A32[k * lda + l] = v; A32[l * lda + k] = v; }
       });
@@ -147,12 +164,12 @@ __device__ void form_vfvt32(double *A, int lda, const double *V, double *G, int 
 
 template <class T>
 __device__ double offdiag_max(const T *A, int lda, int n, double *red) {
-  double mx = 0.0;
+  T mx = T(0);
   for (int idx = threadIdx.x; idx < n * n; idx += NT_J) {
     int i = idx / n, j = idx - i * n;
-    if (i != j) mx = fmax(mx, fabs((double)A[i * lda + j]));
+    if (i != j) mx = fmax(mx, fabs(A[i * lda + j]));
   }
-  return jblock_reduce(mx, red, true);
+  return jblock_reduce((double)mx, red, true);
 }
 
 // Jacobi sweeps on A (shared memory, stride lda) accumulating the rotations into the
@@ -163,6 +180,9 @@ __device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_swee
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int npad = n + (n & 1), np = npad / 2, nsteps = npad - 1;
   const T ttol = (T)tol;
+  // rotation parameters kept in the arithmetic type (a conversion from or to FP64 issues on
+  // the FP64 pipe), in the shared arrays' storage
+  T *rc = reinterpret_cast<T *>(sh.rc), *rs = reinterpret_cast<T *>(sh.rs), *rt = reinterpret_cast<T *>(sh.rt);
   for (int sweep = 0; sweep <= max_sweeps; ++sweep) {
     if (offdiag_max(A, lda, n, sh.red) <= tol) return sweep;
     if (sweep == max_sweeps) break;
@@ -189,9 +209,9 @@ __device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_swee
             fl = 1;
           }
         }
-        sh.rc[tid] = (double)cc;
-        sh.rs[tid] = (double)ss;
-        sh.rt[tid] = (double)tt;
+        rc[tid] = cc;
+        rs[tid] = ss;
+        rt[tid] = tt;
         sh.rflag[tid] = fl;
       }
       __syncthreads();
@@ -203,7 +223,7 @@ __device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_swee
         if (!(fi | fj)) continue;
         const int p = sh.rp[i], q = sh.rq[i];
         if (i == j) {
-          const T t = (T)sh.rt[i], apq = A[p * lda + q];
+          const T t = rt[i], apq = A[p * lda + q];
           A[p * lda + p] -= t * apq;
           A[q * lda + q] += t * apq;
           A[p * lda + q] = T(0);
@@ -217,13 +237,13 @@ __device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_swee
         T x10 = qv ? A[q * lda + r] : T(0);
         T x11 = (qv && sv) ? A[q * lda + s] : T(0);
         if (fi) {
-          const T c = (T)sh.rc[i], sn = (T)sh.rs[i];
+          const T c = rc[i], sn = rs[i];
           T y00 = c * x00 - sn * x10, y10 = sn * x00 + c * x10;
           T y01 = c * x01 - sn * x11, y11 = sn * x01 + c * x11;
           x00 = y00; x10 = y10; x01 = y01; x11 = y11;
         }
         if (fj) {
-          const T c = (T)sh.rc[j], sn = (T)sh.rs[j];
+          const T c = rc[j], sn = rs[j];
           T z00 = c * x00 - sn * x01, z01 = sn * x00 + c * x01;
           T z10 = c * x10 - sn * x11, z11 = sn * x10 + c * x11;
           x00 = z00; x01 = z01; x10 = z10; x11 = z11;
@@ -237,7 +257,7 @@ __device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_swee
       // eigenvector rows p,q: warp per pair, lanes along the row (coalesced / conflict-free)
       for (int i = wid; i < np; i += NT_J / 32) {
         if (!sh.rflag[i]) continue;
-        const T c = (T)sh.rc[i], sn = (T)sh.rs[i];
+        const T c = rc[i], sn = rs[i];
         T *vp = V + (size_t)sh.rp[i] * n, *vq = V + (size_t)sh.rq[i] * n;
         for (int k = lane; k < n; k += 32) {
           const T a = vp[k], bq = vq[k];
@@ -411,6 +431,131 @@ __device__ void newton_density(double *A, int lda, const double *V, double *G, d
 constexpr double NEWTON_THETA = 1.0e-5;  // largest occupied-virtual rotation the first-order density takes
 constexpr double EIG_PT_RATIO = 3.0e-3;  // largest coupling / splitting for second-order eigenvalues
 
+// FP32 sweeps for the density-only step, without FP64 rotation work: A32 (float, overlaying
+// A) is swept to max |a_pq| <= tol32 with the rotations W (float, behind A32); dg / rank /
+// order take the swept diagonal; X = W V (warm, from the FP32 copy V32 that form_vfvt32 left
+// in G) or W (cold) is formed in FP32 and stored in V, so X holds FP32 values whose products
+// are exact in FP64; D = X X^T - I is accumulated in FP64 (kept as FP32 over A32: |D| ~ 1e-6)
+// and one Newton-Schulz step V <- X - D X / 2 (the small product D X in FP32, on the FP32
+// copy X32) leaves the rows of V orthonormal to ~1e-13.  Returns the FP32 sweeps taken.
+__device__ int fp32_sweeps_orth(double *A, int lda, double *V, double *G, int n, double tol32, bool is_warm,
+                                double *dg, int *rank, int *order, JShared &sh) {
+  const int tid = threadIdx.x;
+  float *A32 = reinterpret_cast<float *>(A), *W32 = A32 + (size_t)n * lda;
+  for (int idx = tid; idx < n * n; idx += NT_J) {
+    int i = idx / n, j = idx - i * n;
+    W32[idx] = i == j ? 1.0f : 0.0f;
+  }
+  __syncthreads();
+  int s32 = jacobi_solve<float>(A32, lda, W32, n, tol32, 20, sh);
+  if (s32 < 0) s32 = 20;
+  __syncthreads();
+  rank_diag(A32, lda, n, dg, rank, order);
+  float *X32 = W32;
+  if (is_warm) {
+    const float *V32 = reinterpret_cast<const float *>(G);
+    X32 = reinterpret_cast<float *>(G) + (size_t)n * n;
+    tile_product_t<float>(
+        n, false, [&](int k, int l) { return W32[k * n + l]; }, [&](int l, int j) { return V32[l * n + j]; },
+        [&](int k, int j, float v) {
+          X32[k * n + j] = v;
+          V[(size_t)k * n + j] = (double)v;
+        });
+  } else {
+    for (int idx = tid; idx < n * n; idx += NT_J) V[idx] = (double)W32[idx];
+  }
+  __syncthreads();
+  float *D32 = A32;
+  tile_product_t<double>(
+      n, true, [&](int k, int l) { return V[(size_t)k * n + l]; }, [&](int l, int j) { return V[(size_t)j * n + l]; },
+      [&](int k, int j, double v) {
+        if (k <= j) {
+          const float d = (float)(v - (k == j ? 1.0 : 0.0));
+          D32[k * lda + j] = d;
+          D32[j * lda + k] = d;
+        }
+      });
+  __syncthreads();
+  tile_product_t<float>(
+      n, false, [&](int k, int l) { return D32[k * lda + l]; }, [&](int l, int j) { return X32[l * n + j]; },
+      [&](int k, int j, float v) { V[(size_t)k * n + j] -= 0.5 * (double)v; });
+  __syncthreads();
+  return s32;
+}
+
+// First-order density from orthonormal eigenvector rows V that nearly diagonalise F, with
+// only the coupling block in FP64: for the smaller of the occupied / virtual sets S (ranks
+// from dg) and its complement T,
+//   a_st = ((V_S F) V_T^T)_st,  theta_st = a_st / (dg_s - dg_t),
+// and, if max |theta| <= NEWTON_THETA, C' = V_S + Theta V_T, Loewdin E = C' C'^T - I =
+// Theta Theta^T (V orthonormal), U = C' - E C' / 2, P = 2 U^T U (S occupied) or 2 (I - U^T U).
+// The products of small quantities (Theta V_T, Theta Theta^T, E C') run in FP32 on FP32
+// copies (rounding ~1e-7 of terms <= 1e-5); V_S F, the coupling block and U^T U in FP64.  The
+// diagonal dg only enters the denominators, where FP32 accuracy is enough.
+// Scratch: S (shared, >= n^2 doubles) = [V_S F, later U | Theta, later C'32 | E32 | Theta32];
+// G (global, n^2 doubles, P's block) = [V32 (floats) | C' (FP64)].  Returns false, with P
+// untouched, when the rotation is too large (or the gap not positive).
+__device__ bool newton_density_ov(double *S, const double *V, const double *Fm, double *G, double *Pm, int n,
+                                  int nocc, const double *dg, const int *order, double *red) {
+  const bool use_occ = nocc <= n - nocc;
+  const int nsel = use_occ ? nocc : n - nocc, ncomp = n - nsel;
+  const int s0 = use_occ ? 0 : nocc, t0 = use_occ ? nocc : 0;
+  double *Gs = S, *Th = S + (size_t)nsel * n;
+  float *E32 = reinterpret_cast<float *>(Th + (size_t)nsel * ncomp), *Th32 = E32 + (size_t)nsel * nsel;
+  float *C1_32 = reinterpret_cast<float *>(Th);
+  float *V32 = reinterpret_cast<float *>(G);
+  double *C1 = G + ((size_t)n * n + 1) / 2;  // after V32; ends at or before n^2 (nsel <= n / 2)
+  for (int idx = threadIdx.x; idx < n * n; idx += NT_J) V32[idx] = (float)V[idx];
+  tile_product_mnk(
+      nsel, n, n, [&](int i, int l) { return V[(size_t)order[s0 + i] * n + l]; },
+      [&](int l, int j) { return Fm[(size_t)l * n + j]; }, [&](int i, int j, double v) { Gs[(size_t)i * n + j] = v; });
+  __syncthreads();
+  tile_product_mnk(
+      nsel, ncomp, n, [&](int i, int l) { return Gs[(size_t)i * n + l]; },
+      [&](int l, int t) { return V[(size_t)order[t0 + t] * n + l]; },
+      [&](int i, int t, double v) {
+        const double d = dg[order[s0 + i]] - dg[order[t0 + t]];
+        Th[(size_t)i * ncomp + t] = d != 0.0 ? v / d : INFINITY;
+      });
+  __syncthreads();
+  double mx = 0.0;
+  for (int idx = threadIdx.x; idx < nsel * ncomp; idx += NT_J) {
+    const double th = Th[idx], a = fabs(th);
+    mx = fmax(mx, isnan(a) ? INFINITY : a);
+    Th32[idx] = (float)th;
+  }
+  mx = jblock_reduce(mx, red, true);  // synchronises: Th32 complete, Th no longer read
+  if (!(mx <= NEWTON_THETA)) return false;
+  tile_product_mnk_t<float>(
+      nsel, n, ncomp, false, [&](int i, int t) { return Th32[i * ncomp + t]; },
+      [&](int t, int k) { return V32[order[t0 + t] * n + k]; },
+      [&](int i, int k, float v) {
+        const double c = V[(size_t)order[s0 + i] * n + k] + (double)v;
+        C1[(size_t)i * n + k] = c;
+        C1_32[i * n + k] = (float)c;
+      });
+  tile_product_mnk_t<float>(
+      nsel, nsel, ncomp, false, [&](int i, int t) { return Th32[i * ncomp + t]; },
+      [&](int t, int j) { return Th32[j * ncomp + t]; }, [&](int i, int j, float v) { E32[i * nsel + j] = v; });
+  __syncthreads();
+  double *U = Gs;  // V_S F is no longer needed
+  tile_product_mnk_t<float>(
+      nsel, n, nsel, false, [&](int i, int l) { return E32[i * nsel + l]; },
+      [&](int l, int k) { return C1_32[l * n + k]; },
+      [&](int i, int k, float v) { U[(size_t)i * n + k] = C1[(size_t)i * n + k] - 0.5 * (double)v; });
+  __syncthreads();
+  tile_product_mnk_t<double>(
+      n, n, nsel, true, [&](int a, int k) { return U[(size_t)k * n + a]; },
+      [&](int k, int c) { return U[(size_t)k * n + c]; },
+      [&](int a, int c, double s) {
+        if (c < a) return;
+        const double v = use_occ ? 2.0 * s : (a == c ? 2.0 : 0.0) - 2.0 * s;
+        Pm[(size_t)a * n + c] = v;
+        Pm[(size_t)c * n + a] = v;
+      });
+  return true;
+}
+
 __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__restrict__ F, double *__restrict__ P,
                                                  double *__restrict__ evals, double *__restrict__ evecs,
                                                  double *__restrict__ work, const int64_t *__restrict__ row_off,
@@ -455,8 +600,49 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
   const double fro = sqrt(jblock_reduce(f2, sh.red, false));
   const double tol = 1.0e-13 * fro;
   const bool fp32_ok = mixed || (want_newton && mixed_threshold > 0);
-  bool newton = false, a32_ready = false;
-  if (is_warm && want_newton && fp32_ok) {
+  bool newton = false, a32_ready = false, a64_ready = false;
+  int s32 = 0;
+  if (density_only == 1 && want_newton && fp32_ok) {
+    // SCF density step: F rotated by the previous eigenvectors in FP32 (warm) or F itself
+    // (cold); FP32 sweeps unless the occupied-virtual block is already small; then the
+    // first-order density from the FP64 coupling block alone
+    float *A32 = reinterpret_cast<float *>(A);
+    if (is_warm) {
+      form_vfvt32(A, lda, V, G, n);
+    } else {  // A (FP64) -> A32 in place, through G
+      for (int idx = tid; idx < n * n; idx += NT_J) {
+        int i = idx / n, j = idx - i * n;
+        G[idx] = A[i * lda + j];
+      }
+      __syncthreads();
+      for (int idx = tid; idx < n * n; idx += NT_J) {
+        int i = idx / n, j = idx - i * n;
+        A32[i * lda + j] = (float)G[idx];
+      }
+      __syncthreads();
+    }
+    rank_diag(A32, lda, n, dg, rank, order);
+    if (!is_warm || ov_theta(A32, lda, n, nocc, dg, order, sh.red) > 0.5 * NEWTON_THETA)
+      s32 = fp32_sweeps_orth(A, lda, V, G, n, 2.0e-7 * fro, is_warm, dg, rank, order, sh);
+    if (newton_density_ov(A, V, Fm, G, P + mo, n, nocc, dg, order, sh.red)) {
+      if (tid == 0 && status) status[m] = s32;
+      if (evals) {  // diagonal estimates (FP32 accuracy); the final step computes the eigenvalues
+        double *e = evals + row_off[m];
+        for (int k = tid; k < n; k += NT_J) e[rank[k]] = dg[k];
+      }
+      return;
+    }
+    __syncthreads();
+    // the rotation is too large for the first-order density: FP64 A = V F V^T (V orthonormal
+    // here) and FP64 sweeps below
+    for (int idx = tid; idx < n * n; idx += NT_J) {
+      int i = idx / n, j = idx - i * n;
+      A[i * lda + j] = Fm[idx];
+    }
+    __syncthreads();
+    form_vfvt(A, lda, V, G, n);
+    a64_ready = true;
+  } else if (is_warm && want_newton && fp32_ok) {
     // rotate in FP32 first: if the occupied-virtual block is already small, the FP64
     // rotation and the first-order density follow; otherwise the FP32 sweeps start from it
     // and the FP64 rotation is skipped
@@ -490,8 +676,7 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
       newton = ov_theta(A, lda, n, nocc, dg, order, sh.red) <= NEWTON_THETA;
     }
   }
-  int s32 = 0;
-  if (!newton && fp32_ok) {
+  if (!newton && fp32_ok && !a64_ready) {
     // before FP64 polish sweeps 3e-6 ||F|| is enough; the first-order density wants the
     // FP32 floor, so that the occupied-virtual rotation left over is ~1e-6
     s32 = fp32_stage(A, lda, V, G, Fm, n, (want_newton ? 2.0e-7 : 3.0e-6) * fro, is_warm, a32_ready, sh);

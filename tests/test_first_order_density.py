@@ -40,3 +40,51 @@ def test_first_order_density_error_is_second_order(n, nocc, rot):
     assert np.abs(X @ X - X).max() < 1e-13
     if theta <= 1e-5:  # the kernel's threshold: density error well below the 1e-7 parity bound
         assert np.abs(P - P_exact).max() < 1e-9
+
+
+def _ov_block_density(V, F, nocc, dg):
+    """newton_density_ov: the coupling block alone in FP64, small products in FP32."""
+    n = F.shape[0]
+    order = np.argsort(dg, kind="stable")
+    use_occ = nocc <= n - nocc
+    S, T = (order[:nocc], order[nocc:]) if use_occ else (order[nocc:], order[:nocc])
+    a_st = (V[S] @ F) @ V[T].T
+    theta = a_st / (dg[S][:, None] - dg[T][None, :])
+    f32 = np.float32
+    C1 = V[S] + (theta.astype(f32) @ V[T].astype(f32)).astype(np.float64)
+    E = (theta.astype(f32) @ theta.T.astype(f32)).astype(np.float64)
+    U = C1 - 0.5 * (E.astype(f32) @ C1.astype(f32)).astype(np.float64)
+    P = 2.0 * U.T @ U if use_occ else 2.0 * (np.eye(n) - U.T @ U)
+    return P, np.abs(theta).max()
+
+
+@pytest.mark.parametrize("n,nocc", [(60, 20), (144, 48), (100, 70), (8, 4)])
+def test_fp32_sweeps_then_coupling_block_density(n, nocc):
+    """fp32_sweeps_orth + newton_density_ov: eigenvectors good to FP32 only (W from an FP32
+    diagonalisation of the rotated F), X = W V formed in FP32, one Newton-Schulz step with
+    D = X X^T - I accumulated in FP64 from the FP32 values, then the first-order density
+    from the FP64 coupling block: density error ~1e-10, far below the 1e-7 parity bound."""
+    rng = np.random.default_rng(7 * n + nocc)
+    Q, _ = np.linalg.qr(rng.normal(size=(n, n)))
+    ev = np.sort(np.r_[rng.uniform(-40, -5, nocc), rng.uniform(0, 30, n - nocc)])
+    F = (Q * ev) @ Q.T
+    F = 0.5 * (F + F.T)
+    w, C = np.linalg.eigh(F)
+    P_exact = 2.0 * C[:, :nocc] @ C[:, :nocc].T
+    K = rng.normal(size=(n, n)) * 1e-2
+    V = (C @ np.linalg.qr(np.eye(n) + K - K.T)[0]).T  # warm start, rotations ~1e-2
+    f32 = np.float32
+    A32 = (V.astype(f32) @ F.astype(f32)) @ V.T.astype(f32)
+    d32, W = np.linalg.eigh(0.5 * (A32 + A32.T))  # FP32 sweeps: rotations W (rows)
+    W = W.T.astype(f32)
+    X = (W @ V.astype(f32)).astype(np.float64)  # FP32 values
+    D = X @ X.T - np.eye(n)  # exact products, FP64 sums
+    V2 = X - 0.5 * (D.astype(f32) @ X.astype(f32)).astype(np.float64)
+    assert np.abs(V2 @ V2.T - np.eye(n)).max() < 5e-13  # second order in |D| ~ 2e-7
+    dg = np.zeros(n)
+    dg[:] = d32  # swept diagonal in row order
+    P, theta = _ov_block_density(V2, F, nocc, dg)
+    assert theta <= 1e-5
+    assert np.abs(P - P_exact).max() < 1e-9
+    X2 = 0.5 * P
+    assert np.abs(X2 @ X2 - X2).max() < 1e-12

@@ -165,10 +165,10 @@ __device__ void form_vfvt32(double *A, int lda, const double *V, double *G, int 
 template <class T>
 __device__ double offdiag_max(const T *A, int lda, int n, double *red) {
   T mx = T(0);
-  for (int idx = threadIdx.x; idx < n * n; idx += NT_J) {
-    int i = idx / n, j = idx - i * n;
-    if (i != j) mx = fmax(mx, fabs(A[i * lda + j]));
-  }
+  const int lane = threadIdx.x & 31;
+  for (int i = threadIdx.x >> 5; i < n; i += NT_J / 32)
+    for (int j = lane; j < n; j += 32)
+      if (i != j) mx = fmax(mx, fabs(A[i * lda + j]));
   return jblock_reduce((double)mx, red, true);
 }
 
@@ -188,9 +188,14 @@ __device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_swee
     if (sweep == max_sweeps) break;
     for (int step = 0; step < nsteps; ++step) {
       if (tid < np) {
-        int a, c;
-        if (tid == 0) { a = npad - 1; c = step; }
-        else { a = (step + tid) % (npad - 1); c = (step - tid + npad - 1) % (npad - 1); }
+        // round-robin partners of slot tid at this step (no integer division)
+        int a = npad - 1, c = step;
+        if (tid != 0) {
+          a = step + tid;
+          if (a >= npad - 1) a -= npad - 1;
+          c = step - tid;
+          if (c < 0) c += npad - 1;
+        }
         const int p = min(a, c), q = max(a, c);
         sh.rp[tid] = p;
         sh.rq[tid] = q;
@@ -215,44 +220,47 @@ __device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_swee
         sh.rflag[tid] = fl;
       }
       __syncthreads();
-      // A <- J^T A J on 2x2 blocks (i <= j); block and mirror written by one thread
-      for (int it = tid; it < np * np; it += NT_J) {
-        const int i = it / np, j = it - i * np;
-        if (j < i) continue;
-        const int fi = sh.rflag[i], fj = sh.rflag[j];
-        if (!(fi | fj)) continue;
+      // A <- J^T A J on 2x2 blocks (pair i rows, pair j cols, i <= j): block row i per warp,
+      // lanes along j; each block and its mirror written by one thread
+      for (int i = wid; i < np; i += NT_J / 32) {
+        const int fi = sh.rflag[i];
         const int p = sh.rp[i], q = sh.rq[i];
-        if (i == j) {
-          const T t = rt[i], apq = A[p * lda + q];
-          A[p * lda + p] -= t * apq;
-          A[q * lda + q] += t * apq;
-          A[p * lda + q] = T(0);
-          A[q * lda + p] = T(0);
-          continue;
+        const bool qv = q < n;
+        const T ci = rc[i], si = rs[i];
+        for (int j = i + lane; j < np; j += 32) {
+          const int fj = sh.rflag[j];
+          if (!(fi | fj)) continue;
+          if (j == i) {
+            const T t = rt[i], apq = A[p * lda + q];
+            A[p * lda + p] -= t * apq;
+            A[q * lda + q] += t * apq;
+            A[p * lda + q] = T(0);
+            A[q * lda + p] = T(0);
+            continue;
+          }
+          const int r = sh.rp[j], s = sh.rq[j];
+          const bool sv = s < n;
+          T x00 = A[p * lda + r];
+          T x01 = sv ? A[p * lda + s] : T(0);
+          T x10 = qv ? A[q * lda + r] : T(0);
+          T x11 = (qv && sv) ? A[q * lda + s] : T(0);
+          if (fi) {
+            T y00 = ci * x00 - si * x10, y10 = si * x00 + ci * x10;
+            T y01 = ci * x01 - si * x11, y11 = si * x01 + ci * x11;
+            x00 = y00; x10 = y10; x01 = y01; x11 = y11;
+          }
+          if (fj) {
+            const T c = rc[j], sn = rs[j];
+            T z00 = c * x00 - sn * x01, z01 = sn * x00 + c * x01;
+            T z10 = c * x10 - sn * x11, z11 = sn * x10 + c * x11;
+            x00 = z00; x01 = z01; x10 = z10; x11 = z11;
+          }
+          A[p * lda + r] = x00;
+          A[r * lda + p] = x00;
+          if (sv) { A[p * lda + s] = x01; A[s * lda + p] = x01; }
+          if (qv) { A[q * lda + r] = x10; A[r * lda + q] = x10; }
+          if (qv && sv) { A[q * lda + s] = x11; A[s * lda + q] = x11; }
         }
-        const int r = sh.rp[j], s = sh.rq[j];
-        const bool qv = q < n, sv = s < n;
-        T x00 = A[p * lda + r];
-        T x01 = sv ? A[p * lda + s] : T(0);
-        T x10 = qv ? A[q * lda + r] : T(0);
-        T x11 = (qv && sv) ? A[q * lda + s] : T(0);
-        if (fi) {
-          const T c = rc[i], sn = rs[i];
-          T y00 = c * x00 - sn * x10, y10 = sn * x00 + c * x10;
-          T y01 = c * x01 - sn * x11, y11 = sn * x01 + c * x11;
-          x00 = y00; x10 = y10; x01 = y01; x11 = y11;
-        }
-        if (fj) {
-          const T c = rc[j], sn = rs[j];
-          T z00 = c * x00 - sn * x01, z01 = sn * x00 + c * x01;
-          T z10 = c * x10 - sn * x11, z11 = sn * x10 + c * x11;
-          x00 = z00; x01 = z01; x10 = z10; x11 = z11;
-        }
-        A[p * lda + r] = x00;
-        A[r * lda + p] = x00;
-        if (sv) { A[p * lda + s] = x01; A[s * lda + p] = x01; }
-        if (qv) { A[q * lda + r] = x10; A[r * lda + q] = x10; }
-        if (qv && sv) { A[q * lda + s] = x11; A[s * lda + q] = x11; }
       }
       // eigenvector rows p,q: warp per pair, lanes along the row (coalesced / conflict-free)
       for (int i = wid; i < np; i += NT_J / 32) {

@@ -52,6 +52,8 @@ enum {
   SEQM_NPAR
 };
 
+#define SEQM_MAX_CLASSES 4
+
 typedef struct seqm_batch {
   int32_t nmol, natoms, nxx, nxh, nhh, method, max_norb, pad_;
   const int32_t *mol_atom_off;  /* [nmol+1] */
@@ -69,6 +71,13 @@ typedef struct seqm_batch {
   double *atom_par;             /* [SEQM_NPAR*natoms] parameters (SoA), derived slots written by seqm_hcore */
   const int32_t *pair_i;        /* [npairs] global index of the first (heavier or equal) atom */
   const int32_t *pair_j;        /* [npairs] global index of the second atom */
+  /* optional size classes of mol_order (host values; nclass 0 = one class of max_norb):
+   * molecules mol_order[class_end[c-1] .. class_end[c]) (class_end[-1] = 0, class_end[nclass-1]
+   * = nmol) have norb <= class_norb[c].  Per-molecule kernels launch once per class with
+   * resources sized for it. */
+  int32_t nclass, pad2_;
+  int32_t class_end[SEQM_MAX_CLASSES];
+  int32_t class_norb[SEQM_MAX_CLASSES];
 } seqm_batch;
 
 /* Integrals + core Hamiltonian.  Replaces hcore(molecule) (seqm/seqm_functions/hcore.py:9-179),
@@ -102,12 +111,16 @@ int seqm_fock(const seqm_batch *b, const double *P, const double *H, const doubl
  * directly from a warm start or after the FP32 sweeps), P is formed from the first-order
  * occupied-virtual rotation of the smaller set, re-orthonormalised (Loewdin), instead of
  * further FP64 sweeps; error second order in that ratio (<= ~1e-10 in P); evals are then the
- * diagonal of A.  density_only == 2 (evecs NULL: eigenvalues and P wanted, vectors not): as 1,
- * and the eigenvalues are a_kk + sum_j a_kj^2 / (a_kk - a_jj) when every coupling is below
- * 3e-3 of its diagonal splitting (error third order); otherwise full sweeps.  0 = always sweep
- * to the FP64 tolerance (eigenpairs for output).
+ * diagonal of A.  density_only == 2 (evecs NULL: eigenvalues only, as the reference's final
+ * eig_only call; P's block is scratch and no density is written): A = V F V^T brought nearly
+ * diagonal (FP32 sweeps, re-orthonormalised vectors, FP64 rotation), and the eigenvalues are
+ * a_kk + sum_j a_kj^2 / (a_kk - a_jj) when every coupling is below 3e-3 of its diagonal
+ * splitting (error third order); otherwise FP64 sweeps.  0 = always sweep to the FP64
+ * tolerance (eigenpairs for output).
  * status[m]: sweeps taken (FP32 + FP64), or -1 if the FP64 sweep cap was hit, or -2 for an
- * active molecule with norb > 160, which is left untouched (give it to an SP2 entry point). */
+ * active molecule with norb > 160, which is left untouched (give it to an SP2 entry point), or
+ * -3 if b's size classes put the molecule in a class of smaller class_norb (left untouched).
+ * With size classes (b->nclass > 0) the molecules are processed by one launch per class. */
 int seqm_density_jacobi(const seqm_batch *b, const double *F, double *P, double *evals, double *evecs,
                         double *work, const int64_t *mol_row_off, const uint8_t *active, int32_t *status,
                         int max_sweeps, const uint8_t *warm, int mixed_threshold, int density_only,

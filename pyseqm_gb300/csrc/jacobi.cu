@@ -30,12 +30,14 @@
 
 namespace seqm {
 
-constexpr int NT_J = 512;
+constexpr int NT_J = 512;  // threads of the largest CTAs; smaller molecules run in smaller CTAs
+#define NTB ((int)blockDim.x)
+#define NTB_W ((int)(blockDim.x >> 5))
 constexpr int JMAX_N = 160;
 constexpr int JMAX_P = JMAX_N / 2;
 
 struct JShared {
-  double rc[JMAX_P], rs[JMAX_P], rt[JMAX_P];
+  double rc[JMAX_P], rs[JMAX_P], rt[JMAX_P], rdp[JMAX_P], rdq[JMAX_P];
   int rp[JMAX_P], rq[JMAX_P], rflag[JMAX_P];
   double red[NT_J / 32];
 };
@@ -49,7 +51,7 @@ __device__ double jblock_reduce(double v, double *red, bool is_max) {
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
   double s = red[0];
-  for (int w = 1; w < NT_J / 32; ++w) s = is_max ? fmax(s, red[w]) : s + red[w];
+  for (int w = 1; w < NTB_W; ++w) s = is_max ? fmax(s, red[w]) : s + red[w];
   __syncthreads();
   return s;
 }
@@ -59,7 +61,7 @@ __device__ double jblock_reduce(double v, double *red, bool is_max) {
 template <class T, class LF, class RF, class OF>
 __device__ void tile_product_t(int n, bool upper_only, LF L, RF R, OF out) {
   const int nt = (n + 3) >> 2;
-  for (int t = threadIdx.x; t < nt * nt; t += NT_J) {
+  for (int t = threadIdx.x; t < nt * nt; t += NTB) {
     const int kb = t / nt, jb = t % nt;
     if (upper_only && kb > jb) continue;
     const int k0 = kb * 4, j0 = jb * 4;
@@ -93,7 +95,7 @@ __device__ void tile_product(int n, bool upper_only, LF L, RF R, OF out) {
 template <class T, class LF, class RF, class OF>
 __device__ void tile_product_mnk_t(int M, int N, int K, bool upper_only, LF L, RF R, OF out) {
   const int mt = (M + 3) >> 2, nt = (N + 3) >> 2;
-  for (int t = threadIdx.x; t < mt * nt; t += NT_J) {
+  for (int t = threadIdx.x; t < mt * nt; t += NTB) {
     const int kb = t / nt, jb = t % nt;
     if (upper_only && kb > jb) continue;
     const int k0 = kb * 4, j0 = jb * 4;
@@ -137,25 +139,25 @@ __device__ void form_vfvt(double *A, int lda, const double *V, double *G, int n)
 }
 
 // A32 (float, shared, overlaying A) <- V F V^T in FP32, with F in A (FP64) on entry.  V and F
-// are converted once (G as floats: V32 = G[0, n^2), F32 = G[n^2, 2 n^2)) so that the products
-// run on FP32 operands: conversions to and from FP64 issue on the FP64 pipe.  The product
-// V F goes to the upper half of A's space (T32); V32 stays in G for the caller.
-// Input to FP32 sweeps, which need no more precision.
+// are converted once (G as floats: V32T = V^T in G[0, n^2), F32 in G[n^2, 2 n^2)) so that the
+// products run on FP32 operands (conversions to and from FP64 issue on the FP64 pipe) and every
+// operand row read across a warp is contiguous.  The product V F goes to the upper half of A's
+// space (T32).  Input to FP32 sweeps, which need no more precision.
 __device__ void form_vfvt32(double *A, int lda, const double *V, double *G, int n) {
-  float *V32 = reinterpret_cast<float *>(G), *F32 = V32 + (size_t)n * n;
+  float *V32T = reinterpret_cast<float *>(G), *F32 = V32T + (size_t)n * n;
   float *A32 = reinterpret_cast<float *>(A), *T32 = A32 + (size_t)n * lda;
-  for (int idx = threadIdx.x; idx < n * n; idx += NT_J) {
+  for (int idx = threadIdx.x; idx < n * n; idx += NTB) {
     const int i = idx / n, j = idx - i * n;
-    V32[idx] = (float)V[idx];
+    V32T[j * n + i] = (float)V[idx];
     F32[idx] = (float)A[i * lda + j];
   }
   __syncthreads();
   tile_product_t<float>(
-      n, false, [&](int k, int l) { return V32[k * n + l]; }, [&](int l, int j) { return F32[l * n + j]; },
+      n, false, [&](int k, int l) { return V32T[l * n + k]; }, [&](int l, int j) { return F32[l * n + j]; },
       [&](int k, int j, float v) { T32[k * n + j] = v; });
   __syncthreads();
   tile_product_t<float>(
-      n, true, [&](int k, int j) { return T32[k * n + j]; }, [&](int j, int l) { return V32[l * n + j]; },
+      n, true, [&](int k, int j) { return T32[k * n + j]; }, [&](int j, int l) { return V32T[j * n + l]; },
       [&](int k, int l, float v) {
         if (k <= l) { A32[k * lda + l] = v; A32[l * lda + k] = v; }
       });
@@ -166,7 +168,7 @@ template <class T>
 __device__ double offdiag_max(const T *A, int lda, int n, double *red) {
   T mx = T(0);
   const int lane = threadIdx.x & 31;
-  for (int i = threadIdx.x >> 5; i < n; i += NT_J / 32)
+  for (int i = threadIdx.x >> 5; i < n; i += NTB_W)
     for (int j = lane; j < n; j += 32)
       if (i != j) mx = fmax(mx, fabs(A[i * lda + j]));
   return jblock_reduce((double)mx, red, true);
@@ -174,15 +176,18 @@ __device__ double offdiag_max(const T *A, int lda, int n, double *red) {
 
 // Jacobi sweeps on A (shared memory, stride lda) accumulating the rotations into the
 // rows of V (stride n, shared or global).  Returns the sweeps performed, or -1 if
-// max |a_pq| > tol after max_sweeps.
+// max |a_pq| > tol after max_sweeps.  With ratio > 0 only the pairs whose coupling exceeds
+// ratio times their diagonal splitting rotate (a selective sweep).
 template <class T>
-__device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_sweeps, JShared &sh) {
+__device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_sweeps, JShared &sh,
+                            double ratio = 0.0) {
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int npad = n + (n & 1), np = npad / 2, nsteps = npad - 1;
-  const T ttol = (T)tol;
+  const T ttol = (T)tol, tratio = (T)ratio;
   // rotation parameters kept in the arithmetic type (a conversion from or to FP64 issues on
   // the FP64 pipe), in the shared arrays' storage
   T *rc = reinterpret_cast<T *>(sh.rc), *rs = reinterpret_cast<T *>(sh.rs), *rt = reinterpret_cast<T *>(sh.rt);
+  T *rdp = reinterpret_cast<T *>(sh.rdp), *rdq = reinterpret_cast<T *>(sh.rdq);  // rotated diagonal
   for (int sweep = 0; sweep <= max_sweeps; ++sweep) {
     if (offdiag_max(A, lda, n, sh.red) <= tol) return sweep;
     if (sweep == max_sweeps) break;
@@ -202,9 +207,8 @@ __device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_swee
         int fl = 0;
         T cc = 1, ss = 0, tt = 0;
         if (q < n) {
-          const T apq = A[p * lda + q];
-          if (fabs(apq) > ttol) {
-            const T app = A[p * lda + p], aqq = A[q * lda + q];
+          const T apq = A[p * lda + q], app = A[p * lda + p], aqq = A[q * lda + q];
+          if (fabs(apq) > ttol && (tratio == T(0) || fabs(apq) > tratio * fabs(aqq - app))) {
             const T theta = (aqq - app) / (T(2) * apq);
             T t = T(1) / (fabs(theta) + sqrt(theta * theta + T(1)));
             if (theta < T(0)) t = -t;
@@ -217,12 +221,50 @@ __device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_swee
         rc[tid] = cc;
         rs[tid] = ss;
         rt[tid] = tt;
+        if (fl) {
+          rdp[tid] = A[p * lda + p] - tt * A[p * lda + q];
+          rdq[tid] = A[q * lda + q] + tt * A[p * lda + q];
+        }
         sh.rflag[tid] = fl;
       }
       __syncthreads();
+      if (sizeof(T) == 4) {
+        // FP32: A <- J^T A J as a row pass (rows p, q of A and of V, lanes along the rows) and a
+        // column pass (columns p, q of A, lanes down the columns; the odd stride keeps them
+        // conflict-free); the pass writes the rotated 2x2 block exactly (a_pq = 0)
+        for (int i = wid; i < np; i += NTB_W) {
+          if (!sh.rflag[i]) continue;
+          const T c = rc[i], sn = rs[i];
+          T *ap = A + sh.rp[i] * lda, *aq = A + sh.rq[i] * lda;
+          T *vp = V + (size_t)sh.rp[i] * n, *vq = V + (size_t)sh.rq[i] * n;
+          for (int k = lane; k < n; k += 32) {
+            const T a = ap[k], b = aq[k], e = vp[k], f = vq[k];
+            ap[k] = c * a - sn * b;
+            aq[k] = sn * a + c * b;
+            vp[k] = c * e - sn * f;
+            vq[k] = sn * e + c * f;
+          }
+        }
+        __syncthreads();
+        for (int i = wid; i < np; i += NTB_W) {
+          if (!sh.rflag[i]) continue;
+          const T c = rc[i], sn = rs[i];
+          const int p = sh.rp[i], q = sh.rq[i];
+          for (int k = lane; k < n; k += 32) {
+            const T a = A[k * lda + p], b = A[k * lda + q];
+            T xp = c * a - sn * b, xq = sn * a + c * b;
+            if (k == p) { xp = rdp[i]; xq = T(0); }
+            if (k == q) { xp = T(0); xq = rdq[i]; }
+            A[k * lda + p] = xp;
+            A[k * lda + q] = xq;
+          }
+        }
+        __syncthreads();
+        continue;
+      }
       // A <- J^T A J on 2x2 blocks (pair i rows, pair j cols, i <= j): block row i per warp,
       // lanes along j; each block and its mirror written by one thread
-      for (int i = wid; i < np; i += NT_J / 32) {
+      for (int i = wid; i < np; i += NTB_W) {
         const int fi = sh.rflag[i];
         const int p = sh.rp[i], q = sh.rq[i];
         const bool qv = q < n;
@@ -263,7 +305,7 @@ __device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_swee
         }
       }
       // eigenvector rows p,q: warp per pair, lanes along the row (coalesced / conflict-free)
-      for (int i = wid; i < np; i += NT_J / 32) {
+      for (int i = wid; i < np; i += NTB_W) {
         if (!sh.rflag[i]) continue;
         const T c = rc[i], sn = rs[i];
         T *vp = V + (size_t)sh.rp[i] * n, *vq = V + (size_t)sh.rq[i] * n;
@@ -283,7 +325,7 @@ __device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_swee
 // index of each rank (order[r])
 // ascending ranks of dg (ties by index) and the index of each rank
 __device__ void rank_values(const double *dg, int n, int *rank, int *order) {
-  for (int k = threadIdx.x; k < n; k += NT_J) {
+  for (int k = threadIdx.x; k < n; k += NTB) {
     const double d = dg[k];
     int r = 0;
     for (int j = 0; j < n; ++j) r += (dg[j] < d) || (dg[j] == d && j < k);
@@ -295,7 +337,7 @@ __device__ void rank_values(const double *dg, int n, int *rank, int *order) {
 
 template <class T>
 __device__ void rank_diag(const T *A, int lda, int n, double *dg, int *rank, int *order) {
-  for (int k = threadIdx.x; k < n; k += NT_J) dg[k] = (double)A[k * lda + k];
+  for (int k = threadIdx.x; k < n; k += NTB) dg[k] = (double)A[k * lda + k];
   __syncthreads();
   rank_values(dg, n, rank, order);
 }
@@ -303,7 +345,7 @@ __device__ void rank_diag(const T *A, int lda, int n, double *dg, int *rank, int
 // largest coupling over diagonal splitting, max_{i<j} |a_ij| / |a_ii - a_jj|
 __device__ double coupling_ratio(const double *A, int lda, int n, double *red) {
   double mx = 0.0;
-  for (int idx = threadIdx.x; idx < n * n; idx += NT_J) {
+  for (int idx = threadIdx.x; idx < n * n; idx += NTB) {
     const int i = idx / n, j = idx - i * n;
     if (j <= i) continue;
     const double a = fabs(A[i * lda + j]), d = fabs(A[i * lda + i] - A[j * lda + j]);
@@ -319,7 +361,7 @@ __device__ double ov_theta(const T *A, int lda, int n, int nocc, const double *d
   const double gap = dg[order[nocc]] - dg[order[nocc - 1]];
   const int nv = n - nocc;
   double mx = 0.0;
-  for (int idx = threadIdx.x; idx < nocc * nv; idx += NT_J) {
+  for (int idx = threadIdx.x; idx < nocc * nv; idx += NTB) {
     const int o = order[idx / nv], u = order[nocc + idx % nv];
     mx = fmax(mx, fabs((double)A[u * lda + o]));
   }
@@ -335,17 +377,17 @@ __device__ int fp32_stage(double *A, int lda, double *V, double *G, const double
   const int tid = threadIdx.x;
   float *A32 = reinterpret_cast<float *>(A), *W32 = A32 + (size_t)n * lda;
   if (!a32_ready) {  // A (FP64) -> A32 in place, through G
-    for (int idx = tid; idx < n * n; idx += NT_J) {
+    for (int idx = tid; idx < n * n; idx += NTB) {
       int i = idx / n, j = idx - i * n;
       G[idx] = A[i * lda + j];
     }
     __syncthreads();
-    for (int idx = tid; idx < n * n; idx += NT_J) {
+    for (int idx = tid; idx < n * n; idx += NTB) {
       int i = idx / n, j = idx - i * n;
       A32[i * lda + j] = (float)G[idx];
     }
   }
-  for (int idx = tid; idx < n * n; idx += NT_J) {
+  for (int idx = tid; idx < n * n; idx += NTB) {
     int i = idx / n, j = idx - i * n;
     W32[idx] = i == j ? 1.0f : 0.0f;  // rows of stride n, as jacobi_solve expects
   }
@@ -359,10 +401,10 @@ __device__ int fp32_stage(double *A, int lda, double *V, double *G, const double
         n, false, [&](int k, int l) { return (double)W32[k * n + l]; }, [&](int l, int j) { return V[(size_t)l * n + j]; },
         [&](int k, int j, double v) { G[(size_t)k * n + j] = v; });
   } else {
-    for (int idx = tid; idx < n * n; idx += NT_J) G[idx] = (double)W32[idx];
+    for (int idx = tid; idx < n * n; idx += NTB) G[idx] = (double)W32[idx];
   }
   __syncthreads();
-  for (int idx = tid; idx < n * n; idx += NT_J) V[idx] = G[idx];
+  for (int idx = tid; idx < n * n; idx += NTB) V[idx] = G[idx];
   __syncthreads();
   // one Newton-Schulz step V <- V - (S - I) V / 2 with S = V V^T = W W^T (V was orthonormal):
   // D = W W^T - I in FP64 from the FP32 W (exact products), stored as FP32 over the idle A32
@@ -382,7 +424,7 @@ __device__ int fp32_stage(double *A, int lda, double *V, double *G, const double
       n, false, [&](int k, int l) { return D32[k * lda + l]; }, [&](int l, int j) { return (float)V[(size_t)l * n + j]; },
       [&](int k, int j, float v) { G[(size_t)k * n + j] = V[(size_t)k * n + j] - 0.5 * (double)v; });
   __syncthreads();
-  for (int idx = tid; idx < n * n; idx += NT_J) {
+  for (int idx = tid; idx < n * n; idx += NTB) {
     int i = idx / n, j = idx - i * n;
     V[idx] = G[idx];
     A[i * lda + j] = Fm[idx];
@@ -404,7 +446,7 @@ __device__ void newton_density(double *A, int lda, const double *V, double *G, d
   const int nsel = use_occ ? nocc : n - nocc, ncomp = n - nsel;
   const int s0 = use_occ ? 0 : nocc, t0 = use_occ ? nocc : 0;
   double *Th = G, *C1 = G + (size_t)nsel * ncomp;
-  for (int idx = threadIdx.x; idx < nsel * ncomp; idx += NT_J) {
+  for (int idx = threadIdx.x; idx < nsel * ncomp; idx += NTB) {
     const int i = idx / ncomp, t = idx - i * ncomp;
     const int s = order[s0 + i], u = order[t0 + t];
     Th[idx] = A[u * lda + s] / (dg[s] - dg[u]);
@@ -425,7 +467,7 @@ __device__ void newton_density(double *A, int lda, const double *V, double *G, d
       nsel, n, nsel, [&](int i, int l) { return E[i * nsel + l]; }, [&](int l, int k) { return C1[(size_t)l * n + k]; },
       [&](int i, int k, double v) { U[i * n + k] = C1[(size_t)i * n + k] - 0.5 * v; });
   __syncthreads();
-  for (int it = threadIdx.x; it < n * n; it += NT_J) {
+  for (int it = threadIdx.x; it < n * n; it += NTB) {
     const int a = it / n, c = it - a * n;
     if (c < a) continue;
     double s = 0.0;
@@ -441,28 +483,27 @@ constexpr double EIG_PT_RATIO = 3.0e-3;  // largest coupling / splitting for sec
 
 // FP32 sweeps for the density-only step, without FP64 rotation work: A32 (float, overlaying
 // A) is swept to max |a_pq| <= tol32 with the rotations W (float, behind A32); dg / rank /
-// order take the swept diagonal; X = W V (warm, from the FP32 copy V32 that form_vfvt32 left
-// in G) or W (cold) is formed in FP32 and stored in V, so X holds FP32 values whose products
-// are exact in FP64; D = X X^T - I is accumulated in FP64 (kept as FP32 over A32: |D| ~ 1e-6)
-// and one Newton-Schulz step V <- X - D X / 2 (the small product D X in FP32, on the FP32
-// copy X32) leaves the rows of V orthonormal to ~1e-13.  Returns the FP32 sweeps taken.
+// order take the swept diagonal; X = W V (warm) or W (cold) is formed in FP32 and stored in V,
+// so X holds FP32 values whose products are exact in FP64; D = X X^T - I is accumulated in
+// FP64 from X^T staged in shared memory (conflict-free rows) and kept as FP32 (|D| ~ 1e-6);
+// one Newton-Schulz step V <- X - D X / 2 (the small product D X in FP32) leaves the rows of V
+// orthonormal to ~1e-13.  G (floats): [X32 | V32, later D32].  Returns the FP32 sweeps taken.
 __device__ int fp32_sweeps_orth(double *A, int lda, double *V, double *G, int n, double tol32, bool is_warm,
                                 double *dg, int *rank, int *order, JShared &sh) {
   const int tid = threadIdx.x;
   float *A32 = reinterpret_cast<float *>(A), *W32 = A32 + (size_t)n * lda;
-  for (int idx = tid; idx < n * n; idx += NT_J) {
+  float *X32 = reinterpret_cast<float *>(G), *V32 = X32 + (size_t)n * n, *D32 = V32;
+  for (int idx = tid; idx < n * n; idx += NTB) {
     int i = idx / n, j = idx - i * n;
     W32[idx] = i == j ? 1.0f : 0.0f;
+    if (is_warm) V32[idx] = (float)V[idx];
   }
   __syncthreads();
   int s32 = jacobi_solve<float>(A32, lda, W32, n, tol32, 20, sh);
   if (s32 < 0) s32 = 20;
   __syncthreads();
   rank_diag(A32, lda, n, dg, rank, order);
-  float *X32 = W32;
   if (is_warm) {
-    const float *V32 = reinterpret_cast<const float *>(G);
-    X32 = reinterpret_cast<float *>(G) + (size_t)n * n;
     tile_product_t<float>(
         n, false, [&](int k, int l) { return W32[k * n + l]; }, [&](int l, int j) { return V32[l * n + j]; },
         [&](int k, int j, float v) {
@@ -470,22 +511,30 @@ __device__ int fp32_sweeps_orth(double *A, int lda, double *V, double *G, int n,
           V[(size_t)k * n + j] = (double)v;
         });
   } else {
-    for (int idx = tid; idx < n * n; idx += NT_J) V[idx] = (double)W32[idx];
+    for (int idx = tid; idx < n * n; idx += NTB) {
+      X32[idx] = W32[idx];
+      V[idx] = (double)W32[idx];
+    }
   }
   __syncthreads();
-  float *D32 = A32;
+  double *XT = A;  // X^T, stride lda (A32 and W32 are no longer needed)
+  for (int idx = tid; idx < n * n; idx += NTB) {
+    int i = idx / n, j = idx - i * n;
+    XT[j * lda + i] = (double)X32[idx];
+  }
+  __syncthreads();
   tile_product_t<double>(
-      n, true, [&](int k, int l) { return V[(size_t)k * n + l]; }, [&](int l, int j) { return V[(size_t)j * n + l]; },
+      n, true, [&](int k, int l) { return XT[l * lda + k]; }, [&](int l, int j) { return XT[l * lda + j]; },
       [&](int k, int j, double v) {
         if (k <= j) {
           const float d = (float)(v - (k == j ? 1.0 : 0.0));
-          D32[k * lda + j] = d;
-          D32[j * lda + k] = d;
+          D32[k * n + j] = d;
+          D32[j * n + k] = d;
         }
       });
   __syncthreads();
   tile_product_t<float>(
-      n, false, [&](int k, int l) { return D32[k * lda + l]; }, [&](int l, int j) { return X32[l * n + j]; },
+      n, false, [&](int k, int l) { return D32[k * n + l]; }, [&](int l, int j) { return X32[l * n + j]; },
       [&](int k, int j, float v) { V[(size_t)k * n + j] -= 0.5 * (double)v; });
   __syncthreads();
   return s32;
@@ -508,26 +557,27 @@ __device__ bool newton_density_ov(double *S, const double *V, const double *Fm, 
   const bool use_occ = nocc <= n - nocc;
   const int nsel = use_occ ? nocc : n - nocc, ncomp = n - nsel;
   const int s0 = use_occ ? 0 : nocc, t0 = use_occ ? nocc : 0;
-  double *Gs = S, *Th = S + (size_t)nsel * n;
+  double *Gs = S, *Th = S + (size_t)nsel * n;  // Gs holds (V_S F)^T: n rows of nsel
   float *E32 = reinterpret_cast<float *>(Th + (size_t)nsel * ncomp), *Th32 = E32 + (size_t)nsel * nsel;
   float *C1_32 = reinterpret_cast<float *>(Th);
   float *V32 = reinterpret_cast<float *>(G);
   double *C1 = G + ((size_t)n * n + 1) / 2;  // after V32; ends at or before n^2 (nsel <= n / 2)
-  for (int idx = threadIdx.x; idx < n * n; idx += NT_J) V32[idx] = (float)V[idx];
+  for (int idx = threadIdx.x; idx < n * n; idx += NTB) V32[idx] = (float)V[idx];
   tile_product_mnk(
       nsel, n, n, [&](int i, int l) { return V[(size_t)order[s0 + i] * n + l]; },
-      [&](int l, int j) { return Fm[(size_t)l * n + j]; }, [&](int i, int j, double v) { Gs[(size_t)i * n + j] = v; });
+      [&](int l, int j) { return Fm[(size_t)l * n + j]; }, [&](int i, int j, double v) { Gs[(size_t)j * nsel + i] = v; });
   __syncthreads();
+  // a_st for t (rows, contiguous V_T rows broadcast) x s (columns of (V_S F)^T, contiguous)
   tile_product_mnk(
-      nsel, ncomp, n, [&](int i, int l) { return Gs[(size_t)i * n + l]; },
-      [&](int l, int t) { return V[(size_t)order[t0 + t] * n + l]; },
-      [&](int i, int t, double v) {
+      ncomp, nsel, n, [&](int t, int l) { return V[(size_t)order[t0 + t] * n + l]; },
+      [&](int l, int i) { return Gs[(size_t)l * nsel + i]; },
+      [&](int t, int i, double v) {
         const double d = dg[order[s0 + i]] - dg[order[t0 + t]];
         Th[(size_t)i * ncomp + t] = d != 0.0 ? v / d : INFINITY;
       });
   __syncthreads();
   double mx = 0.0;
-  for (int idx = threadIdx.x; idx < nsel * ncomp; idx += NT_J) {
+  for (int idx = threadIdx.x; idx < nsel * ncomp; idx += NTB) {
     const double th = Th[idx], a = fabs(th);
     mx = fmax(mx, isnan(a) ? INFINITY : a);
     Th32[idx] = (float)th;
@@ -569,19 +619,23 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
                                                  double *__restrict__ work, const int64_t *__restrict__ row_off,
                                                  const uint8_t *__restrict__ active, int32_t *__restrict__ status,
                                                  int max_sweeps, const uint8_t *__restrict__ warm,
-                                                 int mixed_threshold, int density_only) {
+                                                 int mixed_threshold, int density_only, int order_base, int cap) {
   extern __shared__ double A[];
   __shared__ JShared sh;
   __shared__ double dg[JMAX_N];
   __shared__ int rank[JMAX_N], order[JMAX_N];
   __shared__ double e2[JMAX_N];
 
-  const int m = b.mol_order[blockIdx.x];
+  const int m = b.mol_order[order_base + blockIdx.x];
   if (active && !active[m]) return;
   const int n = b.mol_norb[m];
   if (n <= 0) return;
   if (n > JMAX_N) {  // larger bases go to the SP2 density step
     if (threadIdx.x == 0 && status) status[m] = -2;
+    return;
+  }
+  if (n > cap) {  // size class of the launch does not hold this molecule (inconsistent classes)
+    if (threadIdx.x == 0 && status) status[m] = -3;
     return;
   }
   const int lda = n | 1;
@@ -598,7 +652,7 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
   const bool want_newton = density_only && P != nullptr && evecs == nullptr && nocc > 0 && nocc < n;
 
   double f2 = 0.0;
-  for (int idx = tid; idx < n * n; idx += NT_J) {
+  for (int idx = tid; idx < n * n; idx += NTB) {
     int i = idx / n, j = idx - i * n;
     double v = Fm[idx];
     A[i * lda + j] = v;
@@ -618,12 +672,12 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
     if (is_warm) {
       form_vfvt32(A, lda, V, G, n);
     } else {  // A (FP64) -> A32 in place, through G
-      for (int idx = tid; idx < n * n; idx += NT_J) {
+      for (int idx = tid; idx < n * n; idx += NTB) {
         int i = idx / n, j = idx - i * n;
         G[idx] = A[i * lda + j];
       }
       __syncthreads();
-      for (int idx = tid; idx < n * n; idx += NT_J) {
+      for (int idx = tid; idx < n * n; idx += NTB) {
         int i = idx / n, j = idx - i * n;
         A32[i * lda + j] = (float)G[idx];
       }
@@ -636,20 +690,47 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
       if (tid == 0 && status) status[m] = s32;
       if (evals) {  // diagonal estimates (FP32 accuracy); the final step computes the eigenvalues
         double *e = evals + row_off[m];
-        for (int k = tid; k < n; k += NT_J) e[rank[k]] = dg[k];
+        for (int k = tid; k < n; k += NTB) e[rank[k]] = dg[k];
       }
       return;
     }
     __syncthreads();
     // the rotation is too large for the first-order density: FP64 A = V F V^T (V orthonormal
     // here) and FP64 sweeps below
-    for (int idx = tid; idx < n * n; idx += NT_J) {
+    for (int idx = tid; idx < n * n; idx += NTB) {
       int i = idx / n, j = idx - i * n;
       A[i * lda + j] = Fm[idx];
     }
     __syncthreads();
     form_vfvt(A, lda, V, G, n);
     a64_ready = true;
+  } else if (density_only == 2 && evecs == nullptr && P != nullptr && fp32_ok) {
+    // eigenvalues only: FP32 sweeps of the rotated F (warm) or F (cold), FP32 lift and
+    // re-orthonormalisation, then A = V F V^T in FP64 for the second-order eigenvalues below
+    float *A32 = reinterpret_cast<float *>(A);
+    if (is_warm) {
+      form_vfvt32(A, lda, V, G, n);
+    } else {
+      for (int idx = tid; idx < n * n; idx += NTB) {
+        int i = idx / n, j = idx - i * n;
+        G[idx] = A[i * lda + j];
+      }
+      __syncthreads();
+      for (int idx = tid; idx < n * n; idx += NTB) {
+        int i = idx / n, j = idx - i * n;
+        A32[i * lda + j] = (float)G[idx];
+      }
+      __syncthreads();
+    }
+    s32 = fp32_sweeps_orth(A, lda, V, G, n, 2.0e-7 * fro, is_warm, dg, rank, order, sh);
+    for (int idx = tid; idx < n * n; idx += NTB) {
+      int i = idx / n, j = idx - i * n;
+      A[i * lda + j] = Fm[idx];
+    }
+    __syncthreads();
+    form_vfvt(A, lda, V, G, n);
+    a64_ready = true;
+    newton = true;  // nearly diagonal: try the second-order eigenvalues first
   } else if (is_warm && want_newton && fp32_ok) {
     // rotate in FP32 first: if the occupied-virtual block is already small, the FP64
     // rotation and the first-order density follow; otherwise the FP32 sweeps start from it
@@ -657,7 +738,7 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
     form_vfvt32(A, lda, V, G, n);
     rank_diag(reinterpret_cast<const float *>(A), lda, n, dg, rank, order);
     if (ov_theta(reinterpret_cast<const float *>(A), lda, n, nocc, dg, order, sh.red) <= 0.5 * NEWTON_THETA) {
-      for (int idx = tid; idx < n * n; idx += NT_J) {
+      for (int idx = tid; idx < n * n; idx += NTB) {
         int i = idx / n, j = idx - i * n;
         A[i * lda + j] = Fm[idx];
       }
@@ -666,7 +747,7 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
       rank_diag(A, lda, n, dg, rank, order);
       newton = ov_theta(A, lda, n, nocc, dg, order, sh.red) <= NEWTON_THETA;
       if (!newton) {  // rare: back to F in A for the FP32 stage below
-        for (int idx = tid; idx < n * n; idx += NT_J) {
+        for (int idx = tid; idx < n * n; idx += NTB) {
           int i = idx / n, j = idx - i * n;
           A[i * lda + j] = Fm[idx];
         }
@@ -701,8 +782,9 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
   if (density_only == 2 && newton) {
     eig_pt = coupling_ratio(A, lda, n, sh.red) <= EIG_PT_RATIO;
     if (!eig_pt) {
-      // one FP64 sweep diagonalises the close pairs and squares every coupling
-      jacobi_solve<double>(A, lda, V, n, tol, 1, sh);
+      // one selective FP64 sweep: rotate the pairs whose coupling is not small against their
+      // splitting (near-degenerate levels), leave the rest to the second-order sum
+      jacobi_solve<double>(A, lda, V, n, tol, 1, sh, 0.25 * EIG_PT_RATIO);
       s64 = 1;
       __syncthreads();
       eig_pt = coupling_ratio(A, lda, n, sh.red) <= EIG_PT_RATIO;
@@ -719,7 +801,7 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
   // ---- eigenvalues (ascending; ties by index)
   rank_diag(A, lda, n, dg, rank, order);
   if (eig_pt) {
-    for (int k = tid; k < n; k += NT_J) {
+    for (int k = tid; k < n; k += NTB) {
       const double akk = A[k * lda + k];
       double c = 0.0;
       for (int j = 0; j < n; ++j) {
@@ -734,32 +816,33 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
   }
   if (evals && !eig_pt) {
     double *e = evals + row_off[m];
-    for (int k = tid; k < n; k += NT_J) e[rank[k]] = dg[k];
+    for (int k = tid; k < n; k += NTB) e[rank[k]] = dg[k];
   }
   if (evecs) {
     double *E = evecs + mo;
-    for (int idx = tid; idx < n * n; idx += NT_J) {
+    for (int idx = tid; idx < n * n; idx += NTB) {
       int k = idx / n, i = idx - k * n;
       E[(size_t)rank[k] * n + i] = V[idx];
     }
   }
   if (!P) return;
   if (newton) {
-    newton_density(A, lda, V, G, P + mo, n, nocc, dg, order);
+    if (density_only != 2) newton_density(A, lda, V, G, P + mo, n, nocc, dg, order);
     if (eig_pt && evals) {
       __syncthreads();
       rank_values(e2, n, rank, order);
       double *e = evals + row_off[m];
-      for (int k = tid; k < n; k += NT_J) e[rank[k]] = e2[k];
+      for (int k = tid; k < n; k += NTB) e[rank[k]] = e2[k];
     }
     return;
   }
+  if (density_only == 2) return;  // eigenvalues only
   // ---- density from the smaller of the occupied / virtual sets, staged in shared memory
   const bool use_occ = nocc <= n - nocc;
   const int nsel = use_occ ? nocc : n - nocc;
   double *U = A;  // nsel rows of length n (A is no longer needed)
   __syncthreads();
-  for (int idx = tid; idx < n * n; idx += NT_J) {
+  for (int idx = tid; idx < n * n; idx += NTB) {
     int k = idx / n, i = idx - k * n;
     int r = rank[k];
     int slot = use_occ ? r : r - nocc;
@@ -767,7 +850,7 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
   }
   __syncthreads();
   double *Pm = P + mo;
-  for (int it = tid; it < n * n; it += NT_J) {
+  for (int it = tid; it < n * n; it += NTB) {
     const int a = it / n, c = it - a * n;
     if (c < a) continue;
     double s = 0.0;
@@ -777,6 +860,16 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
     Pm[(size_t)c * n + a] = v;
   }
 }
+
+// dynamic shared memory of a CTA for molecules of up to cap basis functions (A, stride cap | 1)
+size_t jacobi_smem(int cap) {
+  const size_t bytes = (size_t)cap * (cap | 1) * sizeof(double);
+  return bytes < 8 ? 8 : bytes;
+}
+
+// threads of a CTA for molecules of up to cap basis functions: at least one per rotation pair
+// (cap / 2 + 1) and enough warps for the products; small CTAs let several molecules share an SM
+int jacobi_threads(int cap) { return cap > 96 ? 512 : cap > 64 ? 256 : cap > 32 ? 128 : 64; }
 
 }  // namespace seqm
 
@@ -791,14 +884,33 @@ extern "C" int seqm_density_jacobi(const seqm_batch *bp, const double *F, double
   seqm_batch b = *bp;
   if (b.nmol == 0) return SEQM_OK;
   const int cap = b.max_norb > JMAX_N ? JMAX_N : b.max_norb;  // larger molecules are skipped (status -2)
-  int lda = cap | 1;
-  size_t smem = (size_t)cap * lda * sizeof(double);
-  if (smem < 8) smem = 8;
-  if (cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jacobi_smem(cap)) !=
+      cudaSuccess)
     return SEQM_E_CUDA;
-  k_jacobi<<<b.nmol, NT_J, smem, (cudaStream_t)stream>>>(b, F, P, evals, evecs, work, mol_row_off, active, status,
-                                                         max_sweeps, warm, mixed_threshold, density_only);
-  return launch_check();
+  if (b.nclass <= 0) {
+    k_jacobi<<<b.nmol, NT_J, jacobi_smem(cap), (cudaStream_t)stream>>>(
+        b, F, P, evals, evecs, work, mol_row_off, active, status, max_sweeps, warm, mixed_threshold, density_only, 0,
+        cap);
+    return launch_check();
+  }
+  if (b.nclass > SEQM_MAX_CLASSES) return SEQM_E_ARG;
+  // one launch per size class (mol_order is by descending norb): CTA threads and shared memory
+  // sized for the class, so that several small molecules share an SM
+  int start = 0;
+  for (int c = 0; c < b.nclass; ++c) {
+    const int end = b.class_end[c];
+    if (end < start || end > b.nmol) return SEQM_E_ARG;
+    const int ccap = b.class_norb[c] > cap ? cap : b.class_norb[c];
+    if (end > start && ccap > 0) {
+      k_jacobi<<<end - start, jacobi_threads(ccap), jacobi_smem(ccap), (cudaStream_t)stream>>>(
+          b, F, P, evals, evecs, work, mol_row_off, active, status, max_sweeps, warm, mixed_threshold, density_only,
+          start, ccap);
+      const int rc = launch_check();
+      if (rc != SEQM_OK) return rc;
+    }
+    start = end;
+  }
+  return start == b.nmol ? SEQM_OK : SEQM_E_ARG;
 }
 
 // ---------------------------------------------------------------------------
@@ -865,12 +977,10 @@ extern "C" int seqm_density_jacobi_noalloc(const seqm_batch *bp, const double *F
   double *work = nullptr;
   int rc = jacobi_scratch_address(&work);
   if (rc != SEQM_OK) return rc;
-  int lda = b.max_norb | 1;
-  size_t smem = (size_t)b.max_norb * lda * sizeof(double);
-  if (smem < 8) smem = 8;
+  const size_t smem = jacobi_smem(b.max_norb);
   if (cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return SEQM_E_CUDA;
   k_jacobi<<<b.nmol, NT_J, smem, s>>>(b, F, P, evals, evecs, work, mol_row_off, active, status, max_sweeps,
-                                      nullptr, 0, 0);
+                                      nullptr, 0, 0, 0, b.max_norb);
   return launch_check();
 }

@@ -36,6 +36,25 @@ def _group_fill(dest, off, counts, key_arrays, maker):
             d[0][idx] = d[1][ms][:, None] + v[None, :]
 
 
+def set_size_classes(struct, norb_sorted):
+    """Size classes of the scheduling order (molecules by descending norb) for per-molecule
+    kernels: class c holds the molecules above the next bound of native.CLASS_BOUNDS; empty
+    classes are dropped.  norb_sorted: the molecules' norb in scheduling order."""
+    norb_sorted = np.asarray(norb_sorted)
+    ends, caps = [], []
+    start = 0
+    for bound in native.CLASS_BOUNDS + (-1,):
+        end = int(np.sum(norb_sorted > bound))
+        if end > start:
+            ends.append(end)
+            caps.append(int(norb_sorted[start]))
+        start = max(start, end)
+    struct.nclass = len(ends)
+    for c in range(native.MAX_CLASSES):
+        struct.class_end[c] = ends[c] if c < len(ends) else 0
+        struct.class_norb[c] = caps[c] if c < len(caps) else 0
+
+
 class Layout:
     def __init__(self):
         self.dev = None
@@ -146,6 +165,7 @@ class Layout:
             atom_Z=d["Z"].data_ptr(), atom_mol=d["atom_mol"].data_ptr(), atom_xyz=d["xyz"].data_ptr(),
             atom_par=d["par"].data_ptr(), pair_i=d["pair_i"].data_ptr(), pair_j=d["pair_j"].data_ptr(),
         )
+        set_size_classes(self._struct, self.norb[self.order] if self.nmol else np.zeros(0, np.int64))
         return self
 
     def set_coordinates(self, xyz_real):

@@ -35,6 +35,10 @@ DIIS_STATE = 124  # SEQM_DIIS_STATE
 _P = ctypes.c_void_p
 
 
+MAX_CLASSES = 4  # SEQM_MAX_CLASSES
+CLASS_BOUNDS = (96, 64, 32)  # size classes of per-molecule kernels: norb > 96, 65-96, 33-64, <= 32
+
+
 class SeqmBatch(ctypes.Structure):
     _fields_ = [
         ("nmol", ctypes.c_int32), ("natoms", ctypes.c_int32), ("nxx", ctypes.c_int32), ("nxh", ctypes.c_int32),
@@ -42,6 +46,8 @@ class SeqmBatch(ctypes.Structure):
         ("mol_atom_off", _P), ("mol_nheavy", _P), ("mol_norb", _P), ("mol_nocc", _P), ("mol_mat_off", _P),
         ("mol_xx_off", _P), ("mol_xh_off", _P), ("mol_hh_off", _P), ("mol_order", _P), ("atom_Z", _P),
         ("atom_mol", _P), ("atom_xyz", _P), ("atom_par", _P), ("pair_i", _P), ("pair_j", _P),
+        ("nclass", ctypes.c_int32), ("pad2_", ctypes.c_int32), ("class_end", ctypes.c_int32 * MAX_CLASSES),
+        ("class_norb", ctypes.c_int32 * MAX_CLASSES),
     ]
 
 

@@ -134,6 +134,7 @@ class BatchSCF:
                  status=torch.zeros(idx.size, dtype=torch.int32, device=dev))
         b = native.SeqmBatch.from_buffer_copy(L.struct)
         b.nmol = int(idx.size)
+        b.nclass = 0  # no per-molecule size classes in this view
         b.max_norb = int(L.norb[idx].max())
         b.mol_norb = v["norb"].data_ptr()
         b.mol_nocc = v["nocc"].data_ptr()

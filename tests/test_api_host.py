@@ -115,3 +115,20 @@ def test_large_molecule_view_for_sp2():
     # a batch of large molecules only needs no view
     L2 = Layout.from_padded(*workloads.pad_batch(mols[1::2]), "PM3").to_device("cpu")
     assert BatchSCF(L2)._large is None
+
+
+def test_size_classes_of_scheduling_order():
+    """Per-molecule kernels launch once per size class of mol_order (descending norb): class
+    ends and the largest norb of each class, empty classes dropped."""
+    from pyseqm_gb300 import native
+    from pyseqm_gb300.layout import set_size_classes
+
+    b = native.SeqmBatch()
+    set_size_classes(b, np.array([144, 120, 97, 96, 70, 40, 33, 8, 6]))
+    assert b.nclass == 4
+    assert list(b.class_end) == [3, 5, 7, 9]
+    assert list(b.class_norb) == [144, 96, 40, 8]
+    set_size_classes(b, np.array([60, 50, 12]))
+    assert b.nclass == 2 and list(b.class_end)[:2] == [2, 3] and list(b.class_norb)[:2] == [60, 12]
+    set_size_classes(b, np.zeros(0, dtype=np.int64))
+    assert b.nclass == 0

@@ -84,8 +84,15 @@ class BatchSCF:
         self.launches = 0  # kernels of this library launched (for reporting)
         self.profile_density = False  # record CUDA events around every density launch
         self.density_events = []
-        flops = 9.0 * layout.norb.astype(np.float64) ** 3 + 2.0 * layout.norb.astype(np.float64) ** 2 * layout.nocc
-        self.density_flops = torch.as_tensor(flops, dtype=torch.float64, device=dev)
+        # FP64 multiply-adds of the Jacobi density step per molecule (jacobi.cu): the first-order
+        # density from the coupling block, (V_S F) n^2 nsel + (coupling) nsel ncomp n + (U^T U,
+        # upper) n^2 nsel / 2; after FP32 sweeps also D = X X^T - I (upper) n^3 / 2; the
+        # eigenvalue-only final step D + V F V^T (n^3 + n^3 / 2)
+        n = layout.norb.astype(np.float64)
+        nsel = np.minimum(layout.nocc, layout.norb - layout.nocc).astype(np.float64)
+        fma_newton = nsel * n * n + nsel * (n - nsel) * n + 0.5 * n * n * nsel
+        self._fma = {k: torch.as_tensor(v, dtype=torch.float64, device=dev)
+                     for k, v in (("newton", fma_newton), ("orth", 0.5 * n ** 3), ("final", 2.0 * n ** 3))}
 
     # ------------------------------------------------------------------ calls
     def _s(self):
@@ -111,13 +118,29 @@ class BatchSCF:
             stream = self.stream if self.stream is not None else torch.cuda.current_stream(self.L.device)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
+            act = None if active is None else active[: self.L.nmol].clone()
             e0.record(stream)
             self._density(out, sp2, active, evecs, max_sweeps, density_only)
             e1.record(stream)
-            fl = self.density_flops if active is None else self.density_flops * active[: self.L.nmol].double()
-            self.density_events.append((e0, e1, fl.sum()))
+            self.density_events.append((e0, e1, self._fp64_flops(act, int(density_only), evecs is not None)))
             return
         self._density(out, sp2, active, evecs, max_sweeps, density_only)
+
+    def _fp64_flops(self, act, density_only, vectors):
+        """FP64 flops of one Jacobi density call (device scalar), from the path each molecule
+        took: the status (sweeps) written by the call tells an SCF step with FP32 sweeps from one
+        without."""
+        n = self.L.nmol
+        if vectors or density_only == 0:
+            fma = self._fma["final"] * 0  # eigenpairs for output: not counted
+        elif density_only == 2:
+            fma = self._fma["final"]
+        else:
+            swept = (self.status[:n] > 0).double()
+            fma = self._fma["newton"] + swept * self._fma["orth"]
+        if act is not None:
+            fma = fma * act.double()
+        return 2.0 * fma.sum()
 
     def _large_view(self):
         """Batch struct over the molecules above the Jacobi limit only (the fields SP2 reads:

@@ -26,6 +26,8 @@
 // virtual sets is smaller (P = 2 (I - C_v C_v^T)).
 #include <math.h>
 
+#include <atomic>
+
 #include "common.cuh"
 
 namespace seqm {
@@ -867,9 +869,21 @@ size_t jacobi_smem(int cap) {
   return bytes < 8 ? 8 : bytes;
 }
 
-// threads of a CTA for molecules of up to cap basis functions: at least one per rotation pair
-// (cap / 2 + 1) and enough warps for the products; small CTAs let several molecules share an SM
-int jacobi_threads(int cap) { return cap > 96 ? 512 : cap > 64 ? 256 : cap > 32 ? 128 : 64; }
+// threads of a CTA for count molecules of up to cap basis functions: at least one per rotation
+// pair (cap / 2 + 1) and enough warps for the products; small CTAs let several molecules share
+// an SM, which pays when the class fills the GPU; a class of fewer molecules than SMs keeps the
+// largest CTAs (latency of each solve)
+int jacobi_threads(int cap, int count) {
+  static std::atomic<int> sms[256];  // SM count per device ordinal, 0 = not yet queried
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 256) {
+    int n = sms[dev].load(std::memory_order_relaxed);
+    if (n == 0 && cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+      sms[dev].store(n, std::memory_order_relaxed);
+    if (count < n) return NT_J;
+  }
+  return cap > 96 ? 512 : cap > 64 ? 256 : cap > 32 ? 128 : 64;
+}
 
 }  // namespace seqm
 
@@ -902,7 +916,7 @@ extern "C" int seqm_density_jacobi(const seqm_batch *bp, const double *F, double
     if (end < start || end > b.nmol) return SEQM_E_ARG;
     const int ccap = b.class_norb[c] > cap ? cap : b.class_norb[c];
     if (end > start && ccap > 0) {
-      k_jacobi<<<end - start, jacobi_threads(ccap), jacobi_smem(ccap), (cudaStream_t)stream>>>(
+      k_jacobi<<<end - start, jacobi_threads(ccap, end - start), jacobi_smem(ccap), (cudaStream_t)stream>>>(
           b, F, P, evals, evecs, work, mol_row_off, active, status, max_sweeps, warm, mixed_threshold, density_only,
           start, ccap);
       const int rc = launch_check();

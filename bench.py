@@ -46,7 +46,8 @@ sys.path.insert(0, HERE)
 
 WORKLOAD = {"workload": "AM1 batched single-point SCF, 4096 molecules 50/50 n-alkanes C1-C16 / (H2O)2-24, seed 0",
             "method": "AM1", "nmol": 4096, "scf_eps": 1e-8, "scf_converger": [1], "seed": 0,
-            "density_step": "Jacobi (FP64) for all molecules (norb <= 144)"}
+            "density_step": "Jacobi for all molecules (norb <= 144): FP32 sweeps, FP64 orthonormalisation, "
+                            "coupling block and first-order density; FP64-accurate"}
 METRIC = "SCF solves/s"
 # DRAM bytes per k_jacobi launch of the default workload, from ncu (0.68 and 0.71 GB at SCF
 # iterations 2 and 11); compute-bound kernel: ~20 GB/s against 6.8 TB/s

@@ -1,0 +1,100 @@
+"""NumPy restatement of PYSEQM's molecular dynamics integrators (seqm/MolecularDynamics.py).
+
+TEST INFRASTRUCTURE ONLY: the CPU oracle for the MD drivers, used by ``tests/``.  Nothing in
+the product package imports it.  Forces come from ``seqm_oracle.single_point`` (fixed-density
+central differences at the converged SCF density).
+
+Restated: the unit conversions of PhysicalConstants (MolecularDynamics.py:21-31), momentum
+removal _zero_com (:746-782), kinetic energy and temperature (:784-793), velocity Verlet
+one_step (:815-842), the Langevin integrator's friction / noise factors (:1391-1407) and
+its thermostat half steps (:1311-1344).  Only Temp 0 Langevin (friction, no noise) is
+deterministic and restated here.
+"""
+
+import numpy as np
+
+from . import seqm_oracle as O
+
+ACC_SCALE = 0.009648532800137615  # eV/A / (g/mol) -> A/fs^2, MolecularDynamics.py:25
+VEL_SCALE = 0.9118367323190634e-3  # sqrt(K/amu) -> A/fs, :26
+KINETIC_ENERGY_SCALE = 1.0364270099032438e2  # amu (A/fs)^2 -> eV, :27
+TEMPERATURE_SCALE = 1.160451812e4  # K/eV, :28
+
+
+def masses(species):
+    """(nmol, molsize, 1) atomic masses, 0 for padding (Molecule.py:120-125)."""
+    m = O.load_elements()["mass"][np.asarray(species)]
+    return m[..., None]
+
+
+def kinetic_energy(mass, v):
+    """MolecularDynamics.py:784-789 (eV per molecule)."""
+    return np.sum(0.5 * mass * v ** 2, axis=(1, 2)) * KINETIC_ENERGY_SCALE
+
+
+def temperature(ek, n_dof):
+    """MolecularDynamics.py:791-793."""
+    return ek * TEMPERATURE_SCALE / (0.5 * n_dof)
+
+
+def zero_com(mass, r, v, remove_angular=True, restore_kinetic_energy=True):
+    """Remove the centre-of-mass velocity and (optionally) the rigid rotation, returning new
+    velocities (MolecularDynamics.py:746-782; pseudo-inverse of the inertia tensor with an
+    absolute cutoff of 1e-10)."""
+    M = np.sum(mass, axis=1, keepdims=True)
+    ek0 = kinetic_energy(mass, v)
+    r_rel = r - np.sum(mass * r, axis=1, keepdims=True) / M
+    v = v - np.sum(mass * v, axis=1, keepdims=True) / M
+    if remove_angular:
+        L = np.sum(mass * np.cross(r_rel, v), axis=1)
+        rr = np.sum(r_rel * r_rel, axis=2, keepdims=True)
+        inertia = (np.sum(mass * rr, axis=1)[:, :, None] * np.eye(3)[None]
+                   - np.sum(mass[..., None] * r_rel[..., :, None] * r_rel[..., None, :], axis=1))
+        omega = np.stack([pinv_hermitian(inertia[m], 1e-10) @ L[m] for m in range(r.shape[0])])
+        v = v - np.cross(np.broadcast_to(omega[:, None, :], r_rel.shape), r_rel)
+    ek1 = kinetic_energy(mass, v)
+    if np.any(ek1 < 1e-12):
+        raise RuntimeError("Zero kinetic energy after removing COM momentum")
+    if restore_kinetic_energy:
+        v = v * np.sqrt(ek0 / ek1)[:, None, None]
+    return v
+
+
+def pinv_hermitian(a, atol):
+    """Pseudo-inverse of a symmetric matrix from its eigen-decomposition, dropping eigenvalues
+    with |w| <= atol (torch.linalg.pinv(hermitian=True, atol=...))."""
+    w, u = np.linalg.eigh(a)
+    keep = np.abs(w) > atol
+    return (u[:, keep] / w[keep]) @ u[:, keep].T
+
+
+def trajectory(method, species, coords, v0, steps, dt, eps, converger=(1,), damp=None, fd_step=1.0e-5):
+    """Velocity Verlet (MolecularDynamics.py:815-842; with damp, the Temp 0 Langevin
+    integrator's friction half steps around it, :1311-1344) from initial velocities v0; the
+    initial velocities lose their centre-of-mass and rotational momentum without kinetic-energy
+    restoration (initialize_velocity, :717-727).  Returns per step coordinates, velocities,
+    forces, Etot and kinetic energy."""
+    species = np.asarray(species)
+    r = np.array(coords, dtype=np.float64)
+    mass = masses(species)
+    minv = np.where(mass > 0, 1.0 / np.where(mass > 0, mass, 1.0), 0.0)
+    v = zero_com(mass, r, np.array(v0, dtype=np.float64), remove_angular=True, restore_kinetic_energy=False)
+    c1 = 1.0 if damp is None else float(np.exp(-0.5 * dt / damp))
+
+    def forces(r):
+        out = O.single_point(method, species, r, eps, converger, forces=True, fd_step=fd_step)
+        return out["force"], out["Etot"]
+
+    f, etot = forces(r)
+    a = f * minv * ACC_SCALE
+    traj = [dict(coordinates=r.copy(), velocities=v.copy(), force=f, Etot=etot, Ek=kinetic_energy(mass, v))]
+    for _ in range(steps):
+        v = v * c1
+        v = v + 0.5 * a * dt
+        r = r + v * dt
+        f, etot = forces(r)
+        a = f * minv * ACC_SCALE
+        v = v + 0.5 * a * dt
+        v = v * c1
+        traj.append(dict(coordinates=r.copy(), velocities=v.copy(), force=f, Etot=etot, Ek=kinetic_energy(mass, v)))
+    return traj

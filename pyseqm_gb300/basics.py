@@ -212,7 +212,7 @@ class Molecule(torch.nn.Module):
         self.mass_inverse = torch.zeros_like(self.mass)
         self.mass_inverse[non_zero] = 1.0 / self.mass[non_zero]
         for name in ("force", "velocities", "acc", "dm", "q", "w", "Hf", "Etot", "Eelec", "Enuc", "Eiso", "e_mo",
-                     "e_gap", "molecular_orbitals", "charge", "dipole", "analytical_gradient"):
+                     "e_gap", "molecular_orbitals", "charge", "dipole", "analytical_gradient", "cis_amplitudes"):
             setattr(self, name, None)
         self.verbose = True
         self.active_state = seqm_parameters.get("active_state", 0)
@@ -263,6 +263,9 @@ class _Solve:
         self.opts = seqm_parameters
         self.P0 = P0
         self.timing = {}
+        self._species = molecule.species.detach().cpu().clone()
+        self._key = (molecule.method, None if charges is None else charges.tobytes(),
+                     None if mult is None else np.asarray(mult).tobytes())
 
     def run(self, const=None):
         o = self.opts
@@ -281,6 +284,32 @@ class _Solve:
                 P0 = self.L.padded_to_packed(P0)
         eps = float(o["scf_eps"]) if not torch.is_tensor(o["scf_eps"]) else float(o["scf_eps"].item())
         self.notconverged = self.s.scf(eps, tuple(o.get("scf_converger", [1])), tuple(o.get("sp2", [False])), P0)
+        self.Eelec, self.Enuc = self.s.final(want_vectors=o.get("eig", True))
+        if const is not None and const.do_timing:
+            torch.cuda.synchronize()
+            const.timing["SCF"].append(time.time() - t0)
+        return self
+
+    def matches(self, molecule, seqm_parameters):
+        """Same molecules (species, charges, multiplicities) and options as this solve."""
+        if seqm_parameters is not self.opts or molecule.species.shape != self._species.shape:
+            return False
+        charges = molecule.tot_charge.detach().cpu().numpy() if torch.is_tensor(molecule.tot_charge) else None
+        return (torch.equal(molecule.species.detach().cpu(), self._species) and self._key[0] == molecule.method
+                and self._key[1] == (None if charges is None else charges.tobytes()))
+
+    def rerun(self, molecule, const=None):
+        """The same molecules at the molecule's current coordinates, starting from this solve's
+        converged density with its eigenvectors as the Jacobi warm start, everything on the
+        device (BatchSCF.resume; the reference's MD passes P0 = the previous density,
+        MolecularDynamics.py:815-825)."""
+        o = self.opts
+        t0 = time.time()
+        real = torch.as_tensor(self.L.real_index, device=molecule.coordinates.device)
+        xyz = molecule.coordinates.detach().reshape(-1, 3)[real].cpu().numpy()
+        eps = float(o["scf_eps"]) if not torch.is_tensor(o["scf_eps"]) else float(o["scf_eps"].item())
+        self.P0 = None
+        self.notconverged = self.s.resume(xyz, eps, tuple(o.get("scf_converger", [1])), tuple(o.get("sp2", [False])))
         self.Eelec, self.Enuc = self.s.final(want_vectors=o.get("eig", True))
         if const is not None and const.do_timing:
             torch.cuda.synchronize()
@@ -438,7 +467,14 @@ class Hamiltonian(torch.nn.Module):
         self.eig = seqm_parameters.get("eig", True)
         self.seqm_parameters = seqm_parameters
 
-    def solve(self, molecule, P0=None):
+    def solve(self, molecule, P0=None, reuse=False):
+        """reuse: P0 is the density this module's previous solve of the same molecules handed out
+        (molecule.dm, as an MD step passes it): that solve continues on the device from its own
+        state at the new coordinates instead of a new layout and a packed P0."""
+        prev = getattr(molecule, "_solve", None)
+        if (reuse and prev is not None and P0 is not None and P0 is getattr(molecule, "_solve_dm", None)
+                and prev.matches(molecule, self.seqm_parameters)):
+            return prev.rerun(molecule, molecule.const)
         return _Solve(molecule, self.seqm_parameters, P0).run(molecule.const)
 
     def forward(self, molecule, themethod, P0=None):
@@ -479,6 +515,16 @@ class Energy(torch.nn.Module):
         self.eig = seqm_parameters.get("eig", True)
         _check_options(seqm_parameters)
 
+    @staticmethod
+    def _refresh_geometry(molecule):
+        with torch.no_grad():
+            real = torch.nonzero(molecule.species.reshape(-1) > 0, as_tuple=False).squeeze(1)
+            xyz = molecule.coordinates.reshape(-1, 3)[real]
+            d = xyz[molecule.idxj] - xyz[molecule.idxi]
+            r = torch.linalg.norm(d, dim=1)
+            molecule.xij = d / r.unsqueeze(1)
+            molecule.rij = r * molecule.const.length_conversion_factor
+
     def _prepare(self, molecule, learned_parameters):
         if self.parser is None:
             self.parser = Parser(self.seqm_parameters)
@@ -498,8 +544,14 @@ class Energy(torch.nn.Module):
                                           f"(supported: {', '.join(GRAD_PARAMS)})")
 
     def forward(self, molecule, learned_parameters=dict(), all_terms=False, P0=None, cis_amp=None, *args, **kwargs):
-        self._prepare(molecule, learned_parameters)
-        s = self.hamiltonian.solve(molecule, P0)
+        static = not callable(learned_parameters) and not learned_parameters
+        prev = getattr(molecule, "_solve", None)
+        if (static and prev is not None and P0 is not None and P0 is getattr(molecule, "_solve_dm", None)
+                and torch.is_tensor(getattr(molecule, "idxi", None)) and self.parser is not None):
+            self._refresh_geometry(molecule)  # same molecules, new coordinates (basics.py:733-746)
+        else:
+            self._prepare(molecule, learned_parameters)
+        s = self.hamiltonian.solve(molecule, P0, reuse=static)
         dev = molecule.coordinates.device
         L = s.L
         real = torch.as_tensor(L.real_index, device=dev)
@@ -604,6 +656,7 @@ class Electronic_Structure(torch.nn.Module):
          molecule.e_gap, self.charge, self.notconverged) = self.conservative_force(
             molecule, P0=P0, learned_parameters=learned_parameters)
         molecule.dm = P.detach()
+        molecule._solve_dm = molecule.dm  # the density handed out; an MD step passes it back as P0
         with torch.no_grad():
             if molecule.dm.dim() == 4:  # open shell: both spins (ElectronicStructure.py:106-117)
                 molecule.q = (molecule.const.tore[molecule.species] - self.atomic_charges(molecule.dm[:, 0])

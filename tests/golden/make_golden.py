@@ -173,6 +173,51 @@ def write(name, species, coords, settings, per_molecule=False, learned=None, wit
     print(name, "loop_count", rec["ref"]["loop_count"])
 
 
+def write_md(name, species, coords, settings, steps, timestep, seed, damp=None):
+    """A short NVE (or Temp 0 Langevin) trajectory through the reference's own MD driver: its
+    initialize() (momentum removal, first forces) and one_step() (velocity Verlet, P0 = the
+    previous density), from seeded initial velocities (Angstrom / fs)."""
+    if ONLY and name not in ONLY:
+        return
+    from seqm.MolecularDynamics import Molecular_Dynamics_Basic, Molecular_Dynamics_Langevin
+
+    species = np.asarray(species)
+    coords = np.asarray(coords, dtype=np.float64)
+    v0 = np.random.default_rng(seed).normal(size=coords.shape) * 0.01 * (species[..., None] > 0)
+    sp = dict(settings)
+    # a copy: the Molecule's coordinates share memory with the array given, and the MD moves them
+    mol = Molecule(Constants(), sp, torch.as_tensor(coords.copy()), torch.as_tensor(species, dtype=torch.int64))
+    mol.verbose = False
+    mol.velocities = torch.as_tensor(v0.copy())
+    out = {"molid": [0], "print every": 0, "checkpoint every": 0, "h5": {}}
+    if damp is None:
+        md = Molecular_Dynamics_Basic(sp, timestep=timestep, Temp=0.0, output=out)
+    else:
+        md = Molecular_Dynamics_Langevin(damp=damp, seqm_parameters=sp, timestep=timestep, Temp=0.0, output=out)
+    _calls[0] = 0
+    md.initialize(mol)
+    traj = []
+
+    def record(loops):
+        with torch.no_grad():
+            Ek = md._kinetic_energy(mol)
+            traj.append(dict(coordinates=mol.coordinates.detach().numpy().tolist(),
+                             velocities=mol.velocities.detach().numpy().tolist(),
+                             force=mol.force.detach().numpy().tolist(), Etot=mol.Etot.detach().numpy().tolist(),
+                             Ek=Ek.numpy().tolist(), T=md._calc_temperature(Ek).numpy().tolist(), loops=loops))
+
+    record(_calls[0] - 2)
+    for _ in range(steps):
+        _calls[0] = 0
+        md.one_step(mol)
+        record(_calls[0] - 2)
+    rec = dict(name=name, settings=settings, species=species.tolist(), coords=coords.tolist(),
+               velocities0=v0.tolist(), timestep=timestep, steps=steps, damp=damp, ref={"trajectory": traj})
+    with open(os.path.join(HERE, f"{name}.json"), "w") as f:
+        json.dump(rec, f)
+    print(name, "loops per step", [t["loops"] for t in traj])
+
+
 def _open_shells():
     """CH3 (planar, doublet), OH (doublet), NO (doublet), CH2 (bent, triplet), O2 (triplet),
     H2O (singlet, run unrestricted)."""
@@ -255,6 +300,15 @@ def main():
           charges=[1, -1, 1, 0])
     write("ions_pm3", *workloads.pad_batch(_ions()), {"method": "PM3", "scf_eps": 1e-8, "scf_converger": [1]},
           charges=[1, -1, 1, 0])
+
+    # molecular dynamics: velocity Verlet and Temp 0 Langevin (friction only) from seeded velocities
+    rng = np.random.default_rng(5)
+    mols = [workloads.alkane(2, rng, 0.03), workloads.water_cluster(3, rng), workloads.alkane(4, rng, 0.03)]
+    sp, c = workloads.pad_batch(mols)
+    write_md("md_am1_verlet", sp, c, {"method": "AM1", "scf_eps": 1e-8, "scf_converger": [1]}, steps=8,
+             timestep=0.5, seed=6)
+    write_md("md_pm3_langevin", sp, c, {"method": "PM3", "scf_eps": 1e-8, "scf_converger": [1]}, steps=8,
+             timestep=0.5, seed=7, damp=5.0)
 
     rng = np.random.default_rng(4)
     mols = [workloads.alkane(8, rng, 0.05), workloads.water_cluster(4, rng)]

@@ -132,3 +132,35 @@ def test_size_classes_of_scheduling_order():
     assert b.nclass == 2 and list(b.class_end)[:2] == [2, 3] and list(b.class_norb)[:2] == [60, 12]
     set_size_classes(b, np.zeros(0, dtype=np.int64))
     assert b.nclass == 0
+
+
+def test_md_host_logic_matches_oracle():
+    """MD driver host logic on the CPU: momentum removal (centre of mass and rotation, pseudo-
+    inverse of the inertia tensor), kinetic energy, temperature and the Langevin factors against
+    the oracle's restatement; file outputs are refused."""
+    from pyseqm_gb300 import Constants, Molecular_Dynamics_Basic, Molecular_Dynamics_Langevin, Molecule
+    from oracle import seqm_md as MD
+
+    g = load_golden("md_am1_verlet")
+    s = dict(g["settings"])
+    mol = Molecule(Constants(), s, torch.as_tensor(g["coords_np"]), torch.as_tensor(g["species_np"]))
+    v0 = np.asarray(g["velocities0"])
+    mol.velocities = torch.as_tensor(v0.copy())
+    md = Molecular_Dynamics_Basic(s, timestep=0.5, output={"print every": 0, "checkpoint every": 0})
+    md.set_dof(mol)
+    md._zero_com(mol, restore_kinetic_energy=False)
+    mass = MD.masses(g["species_np"])
+    want = MD.zero_com(mass, g["coords_np"], v0, restore_kinetic_energy=False)
+    np.testing.assert_allclose(mol.velocities.numpy(), want, atol=1e-14, rtol=0)
+    ek = md._kinetic_energy(mol).numpy()
+    np.testing.assert_allclose(ek, MD.kinetic_energy(mass, want), rtol=1e-13)
+    np.testing.assert_allclose(md._calc_temperature(torch.as_tensor(ek)).numpy(),
+                               MD.temperature(ek, 3.0 * (g["species_np"] > 0).sum(1)), rtol=1e-13)
+    lg = Molecular_Dynamics_Langevin(damp=5.0, seqm_parameters=s, timestep=0.5, Temp=300.0,
+                                     output={"print every": 0, "checkpoint every": 0})
+    dt, damp = 0.5, 5.0
+    s_ = torch.as_tensor(-dt / damp, dtype=torch.float64)
+    lg.langevin_c1 = torch.exp(0.5 * s_)
+    assert abs(float(lg.langevin_c1) - np.exp(-0.5 * dt / damp)) < 1e-15
+    with pytest.raises(NotImplementedError):
+        Molecular_Dynamics_Basic(s, output={"xyz": 10})

@@ -33,3 +33,57 @@ def test_resume_matches_cold_start_and_saves_iterations():
         cold = run_energy(species, pad.reshape(L.nmol, L.molsize, 3), "AM1", eps=1e-8, converger=(1,))
         np.testing.assert_allclose((E + En).cpu().numpy(), cold["Etot"].cpu().numpy(), atol=1e-6, rtol=0)
         assert warm_iters.mean() < cold["iters"].mean()
+
+
+def _md_run(name, steps=8):
+    import torch
+
+    from pyseqm_gb300 import Constants, Molecule, Molecular_Dynamics_Basic, Molecular_Dynamics_Langevin
+    from conftest import load_golden
+
+    g = load_golden(name)
+    s = dict(g["settings"])
+    mol = Molecule(Constants().cuda(), s, torch.as_tensor(g["coords_np"], device="cuda"),
+                   torch.as_tensor(g["species_np"], device="cuda")).cuda()
+    mol.velocities = torch.as_tensor(np.asarray(g["velocities0"]), device="cuda")
+    out = {"print every": 0, "checkpoint every": 0}
+    if g["damp"] is None:
+        md = Molecular_Dynamics_Basic(s, timestep=g["timestep"], Temp=0.0, output=out).cuda()
+    else:
+        md = Molecular_Dynamics_Langevin(damp=g["damp"], seqm_parameters=s, timestep=g["timestep"], Temp=0.0,
+                                         output=out).cuda()
+    md.initialize(mol)
+    traj, solves, iters = [], [], []
+
+    def record():
+        traj.append(dict(coordinates=mol.coordinates.detach().cpu().numpy(),
+                         velocities=mol.velocities.detach().cpu().numpy(), force=mol.force.cpu().numpy(),
+                         Etot=mol.Etot.detach().cpu().numpy(), Ek=md._kinetic_energy(mol).cpu().numpy()))
+        solves.append(mol._solve)
+        iters.append(int(mol._solve.s.iters[: mol._solve.L.nmol].max()))
+
+    record()
+    for _ in range(steps):
+        md.one_step(mol)
+        record()
+    return g, traj, solves, iters
+
+
+@pytest.mark.parametrize("name", ["md_am1_verlet", "md_pm3_langevin"])
+def test_md_trajectory_matches_reference(name):
+    """Molecular_Dynamics_Basic / _Langevin (Temp 0) on the GPU against the reference's own
+    MD driver: 8 steps from the same velocities; positions and velocities to 1e-6, forces to
+    1e-5 eV/A, total and kinetic energies to 1e-6 eV.  After the first step the SCF continues
+    on the device (the same solve object, warm density and eigenvectors) with the reference's
+    iteration counts +-1."""
+    g, traj, solves, iters = _md_run(name)
+    ref = g["ref"]["trajectory"]
+    for k, r in enumerate(ref):
+        np.testing.assert_allclose(traj[k]["coordinates"], r["coordinates"], atol=1e-6, rtol=0)
+        np.testing.assert_allclose(traj[k]["velocities"], r["velocities"], atol=1e-6, rtol=0)
+        np.testing.assert_allclose(traj[k]["force"], r["force"], atol=1e-5, rtol=0)
+        np.testing.assert_allclose(traj[k]["Etot"], r["Etot"], atol=1e-6, rtol=0)
+        np.testing.assert_allclose(traj[k]["Ek"], r["Ek"], atol=1e-6, rtol=0)
+    assert all(sv is solves[0] for sv in solves)  # one device-resident solve for the whole run
+    for k in range(1, len(ref)):
+        assert abs(iters[k] - ref[k]["loops"]) <= 1

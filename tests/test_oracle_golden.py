@@ -95,3 +95,23 @@ def test_oracle_rejects_odd_electrons():
 def test_oracle_rejects_unsorted_species():
     with pytest.raises(ValueError):
         O.parse(np.array([[1, 6]]), np.array([[[0, 0, 0], [1.1, 0, 0]]], dtype=float))
+
+
+@pytest.mark.parametrize("name", ["md_am1_verlet", "md_pm3_langevin"])
+def test_oracle_md_matches_reference_trajectory(name):
+    """The oracle's velocity Verlet (and Temp 0 Langevin friction) against the reference's
+    Molecular_Dynamics_Basic / _Langevin: three steps from the same initial velocities.  The
+    reference starts each step's SCF from the previous density, the oracle from the guess, so
+    forces agree to the SCF threshold's effect (~1e-6 eV/A) and positions to ~1e-8 A."""
+    from oracle import seqm_md as MD
+
+    g = load_golden(name)
+    s = g["settings"]
+    traj = MD.trajectory(s["method"], g["species_np"], g["coords_np"], np.asarray(g["velocities0"]), 3,
+                         g["timestep"], s["scf_eps"], tuple(s["scf_converger"]), damp=g["damp"])
+    for k, ref in enumerate(g["ref"]["trajectory"][:4]):
+        np.testing.assert_allclose(traj[k]["coordinates"], ref["coordinates"], atol=1e-7, rtol=0)
+        np.testing.assert_allclose(traj[k]["velocities"], ref["velocities"], atol=1e-7, rtol=0)
+        np.testing.assert_allclose(traj[k]["force"], ref["force"], atol=1e-5, rtol=0)
+        np.testing.assert_allclose(traj[k]["Etot"], ref["Etot"], atol=1e-7, rtol=0)
+        np.testing.assert_allclose(traj[k]["Ek"], ref["Ek"], atol=1e-7, rtol=0)

@@ -307,6 +307,28 @@ def run_ours(args):
                                     "FP32 sweeps; final eigenvalue step 4 n^3 (FP32 sweep work not counted)",
                 "launches": len(dur), "avg_launch_ms": 1e3 * sum(dur) / max(1, len(dur)),
                 "share_of_step_time": density_share}
+    # the same batch with a strictly FP64 density step (no FP32 sweeps: mixed_threshold 0), its
+    # rate and its energies against the default step's
+    fp64_only = None
+    if rank == 0 and args.fp64_only_steps > 0:
+        E_default = (Eel + Enu).clone()
+        mixed_default = s.mixed_threshold
+        s.mixed_threshold = 0
+        step()
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(args.fp64_only_steps):
+            Eel64, Enu64 = step()
+        f1.record(stream)
+        torch.cuda.synchronize()
+        dt64 = f0.elapsed_time(f1) / 1e3 / args.fp64_only_steps
+        fp64_only = {"value": args.nmol / dt64, "unit": "solves/s", "ms_per_step": 1e3 * dt64,
+                     "steps": args.fp64_only_steps,
+                     "max_abs_dE_vs_default_eV": float((Eel64 + Enu64 - E_default).abs().max()),
+                     "what": "density step with FP64 arithmetic only (FP64 rotation, first-order density and "
+                             "sweeps; no FP32 stage)"}
+        s.mixed_threshold = mixed_default
     # end to end through the public API with host buffers
     e2e = None
     if rank == 0 and args.e2e_steps > 0:
@@ -346,7 +368,7 @@ def run_ours(args):
                 "p50_ms": statistics.median(step_ms), "p99_ms": float(np.percentile(step_ms, 99)),
                 "step_ms": [round(x, 2) for x in step_ms],
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
-                "serving_sample": serve}
+                "fp64_only": fp64_only, "serving_sample": serve}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -535,6 +557,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--serving-requests", type=int, default=400)
+    ap.add_argument("--fp64-only-steps", type=int, default=2,
+                    help="default workload: also time this many steps with the strictly FP64 density step")
     ap.add_argument("--serving-rate", type=float, default=10000.0)
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--requests", type=int, default=4000)

@@ -237,6 +237,16 @@ int seqm_energy_error_u(const seqm_batch *b, const double *Pa, const double *Pb,
                         double *Eout, double *err, double *dm_err, double *dm_el, uint8_t *active, double eps,
                         void *stream);
 
+/* Two-electron part G(P) of the Fock build for nvec sets of general (not symmetric) AO
+ * densities: the matrix-vector product of the CIS / RPA solvers.  Replaces makeA_pi_batched
+ * and makeA_pi_symm_batch (seqm/seqm_functions/rcis_batch.py:296-507): Coulomb from the
+ * symmetric part of the partners' diagonal blocks, one-centre terms of the symmetric and the
+ * antisymmetric part, exchange of each off-diagonal block from its own block of P (no Hcore).
+ * Set v lives at P + v * stride (each set a full ragged batch, stride >= mol_mat_off[nmol]);
+ * G has the same layout; nvec <= 65535.  Molecules with active[m] == 0 are skipped. */
+int seqm_fock_general(const seqm_batch *b, int nvec, const double *P, const double *w_xx, const double *w_xh,
+                      const double *w_hh, double *G, int64_t stride, const uint8_t *active, void *stream);
+
 /* Library build string (host memory; no GPU needed). */
 const char *seqm_version(void);
 

@@ -1,0 +1,125 @@
+"""NumPy restatement of PYSEQM's CIS and RPA excited states of the ground-state SCF.
+
+TEST INFRASTRUCTURE ONLY: the CPU oracle for the excited-state solver, used by ``tests/``.
+Nothing in the product package imports it.
+
+The reference solves for the lowest roots with Davidson iterations (rcis_batch.py:13-247,
+rcis_new.py:19-200, rpa.py:12-210) on the matrix-vector products of
+matrix_vector_product_batched (rcis_batch.py:250-293):
+
+    (A V)_ia = (e_a - e_i) V_ia + 2 (C_occ^T G(C_occ V C_virt^T) C_virt)_ia
+    (B V)_ia = 2 (C_occ^T G(C_occ V C_virt^T)^T C_virt)_ia
+
+with G the two-electron part of the Fock build for a (not symmetric) AO transition density
+(makeA_pi_batched, :296-388, and makeA_pi_symm_batch, :390-507).  The oracle builds A (and B)
+column by column for each molecule alone and diagonalises them exactly: CIS roots are the
+lowest eigenvalues of A; RPA roots w solve (A - B)^1/2 (A + B) (A - B)^1/2 z = w^2 z, with
+X + Y = (A - B)^1/2 z, X - Y = (A + B)(X + Y) / w, normalised to X.X - Y.Y = 1 (rpa.py:213-278).
+"""
+
+import numpy as np
+
+from . import seqm_oracle as O
+
+
+def g_transition(mol, p, ints, P):
+    """Two-electron part G(P) of the Fock build for a general (not symmetric) AO density P
+    (nmol, 4 ms, 4 ms): the symmetric part as the Fock build (Coulomb, exchange, one-centre);
+    the antisymmetric part through exchange and the one-centre (s,p) and (p,p') terms only
+    (rcis_batch.py:315-368)."""
+    nmol, ms = mol["nmol"], mol["molsize"]
+    Ps = 0.5 * (P + np.transpose(P, (0, 2, 1)))
+    Pa = 0.5 * (P - np.transpose(P, (0, 2, 1)))
+    Gs = O.fock(mol, p, ints, np.zeros((nmol * ms * ms, 4, 4)), Ps)
+    Pab = O.full_to_blocks(Pa, nmol, ms)
+    Ga = np.zeros_like(Pab)
+    mask, maskd = mol["mask"], mol["maskd"]
+    rem = mask % (ms * ms)
+    mask_l = (mask - rem) + (rem % ms) * ms + rem // ms
+    w = ints["w"]
+    wk = w[:, O.KIND[:, :, None, None], O.KIND[None, None, :, :]]
+    K = np.einsum("nalbs,nls->nab", wk, -0.5 * Pab[mask])
+    np.add.at(Ga, mask, K)
+    np.add.at(Ga, mask_l, -np.transpose(K, (0, 2, 1)))
+    Pd = Pab[maskd]
+    t = np.zeros_like(Pd)
+    for i in (1, 2, 3):
+        t[:, 0, i] = Pd[:, 0, i] * (0.5 * p["h_sp"] - 0.5 * p["g_sp"])
+    for i, j in ((1, 2), (1, 3), (2, 3)):
+        t[:, i, j] = Pd[:, i, j] * (0.25 * p["g_pp"] - 0.75 * p["g_p2"])
+    Ga[maskd] += t - np.transpose(t, (0, 2, 1))
+    return Gs + O.blocks_to_full(Ga, nmol, ms)
+
+
+def ab_matrices(method, species, coords, eps, converger=(1,), with_b=False):
+    """Per molecule of the batch: orbital energies, C, nocc and the CIS matrix A (and B), each
+    molecule run alone (its SCF, integrals and orbitals)."""
+    species = np.asarray(species)
+    coords = np.asarray(coords, dtype=np.float64)
+    el = O.load_elements()
+    res = []
+    for m in range(species.shape[0]):
+        na = int(np.sum(species[m] > 0))
+        sp, xyz = species[m:m + 1, :na], coords[m:m + 1, :na]
+        out = O.single_point(method, sp, xyz, eps, converger)
+        mol, p = out["mol"], out["params"]
+        ints = O.integrals(mol, p, el)
+        _, e, vecs = O.density_eigh(out["F"], mol["nheavy"], mol["nhyd"], mol["nocc"])
+        C = vecs[0]
+        idx = O.packed_index(mol["nheavy"][0], mol["nhyd"][0])
+        n, nocc = idx.size, int(mol["nocc"][0])
+        nv = n - nocc
+        ev = e[0, :n]
+        Co, Cv = C[:, :nocc], C[:, nocc:]
+        A = np.zeros((nocc * nv, nocc * nv))
+        B = np.zeros_like(A) if with_b else None
+        n4 = 4 * mol["molsize"]
+        for col in range(nocc * nv):
+            i, a = divmod(col, nv)
+            Pt = np.zeros((1, n4, n4))
+            Pt[0][np.ix_(idx, idx)] = np.outer(Co[:, i], Cv[:, a])
+            G = g_transition(mol, p, ints, Pt)[0][np.ix_(idx, idx)]
+            A[:, col] = 2.0 * (Co.T @ G @ Cv).reshape(-1)
+            A[col, col] += ev[nocc + a] - ev[i]
+            if with_b:
+                B[:, col] = 2.0 * (Co.T @ G.T @ Cv).reshape(-1)
+        res.append(dict(A=A, B=B, e=ev, nocc=nocc, nvirt=nv, Etot=out["Etot"][0], C=C))
+    return res
+
+
+def cis(method, species, coords, eps, nroots, converger=(1,)):
+    """Lowest nroots CIS excitation energies and amplitudes (occ x virt, per molecule)."""
+    out = []
+    for r in ab_matrices(method, species, coords, eps, converger):
+        w, v = np.linalg.eigh(r["A"])
+        amp = v[:, :nroots].T.reshape(nroots, r["nocc"], r["nvirt"])
+        out.append(dict(energies=w[:nroots], amplitudes=amp, nocc=r["nocc"], nvirt=r["nvirt"],
+                        transition_density=transition_density(r["C"], r["nocc"], amp)))
+    return out
+
+
+def rpa(method, species, coords, eps, nroots, converger=(1,)):
+    """Lowest nroots RPA (TDHF) excitation energies and X, Y amplitudes per molecule."""
+    out = []
+    for r in ab_matrices(method, species, coords, eps, converger, with_b=True):
+        A, B = r["A"], r["B"]
+        wm, um = np.linalg.eigh(A - B)
+        sq = (um * np.sqrt(wm)) @ um.T
+        w2, z = np.linalg.eigh(sq @ (A + B) @ sq)
+        w = np.sqrt(w2[:nroots])
+        XpY = sq @ z[:, :nroots]
+        XmY = (A + B) @ XpY / w
+        X, Y = XpY + XmY, XpY - XmY
+        nrm = np.sqrt((X ** 2).sum(0) - (Y ** 2).sum(0))
+        X, Y = X / nrm, Y / nrm
+        shape = (nroots, r["nocc"], r["nvirt"])
+        Xs, Ys = X.T.reshape(shape), Y.T.reshape(shape)
+        out.append(dict(energies=w, X=Xs, Y=Ys, nocc=r["nocc"], nvirt=r["nvirt"],
+                        transition_density=transition_density(r["C"], r["nocc"], Xs),
+                        transition_density_y=transition_density(r["C"], r["nocc"], Ys)))
+    return out
+
+
+def transition_density(C, nocc, amplitudes):
+    """C_occ X C_virt^T per state in the packed AO basis (independent of the orbitals' signs)."""
+    return np.einsum("mi,ria,na->rmn", C[:, :nocc], amplitudes, C[:, nocc:])

@@ -14,9 +14,10 @@ reference's SCF0 boundary implies (scf_loop.py:1996-2031).
 Supported: MNDO/AM1/PM3, closed shell (scf_converger [0, alpha], [1] and [2] (DIIS), sp2)
 and unrestricted open shell (``UHF``: True with the Molecule's ``mult``; scf_converger
 [0, alpha] and [1], as the reference has neither open-shell DIIS nor SP2), learned
-parameters (values for any parameter; gradients for U_ss, U_pp, beta_s, beta_p).  PM6,
-excited states, scf_backward >= 1 and a finite pair_outer_cutoff raise
-NotImplementedError.
+parameters (values for any parameter; gradients for U_ss, U_pp, beta_s, beta_p), and the
+ground state's CIS / RPA excited states (``excited_states``: excitation energies and
+amplitudes).  PM6, excited-state forces (active_state > 0), scf_backward >= 1 and a finite
+pair_outer_cutoff raise NotImplementedError.
 """
 
 import copy
@@ -70,8 +71,23 @@ def _check_options(seqm_parameters):
         if seqm_parameters.get("scf_converger", [1])[0] == 2:
             raise NotImplementedError("DIIS has no open-shell form in the reference (scf_converger [0, alpha] or "
                                       "[1] with UHF)")
-    if seqm_parameters.get("excited_states"):
-        raise NotImplementedError("excited states are not supported by pyseqm_gb300")
+    exc = seqm_parameters.get("excited_states")
+    if exc:
+        if not isinstance(exc, dict):
+            raise Exception("Invalid format for excited_states. Expected input like "
+                            "'excited_states': {'method': 'rpa', 'n_states': 3, 'tolerance': 1e-6}")
+        if "n_states" not in exc:
+            raise ValueError("Specify the number of excited states to calculate")
+        if str(exc.get("method", "cis")).lower() not in ("cis", "tda", "rpa"):
+            raise Exception("Excited state method has to be CIS or RPA")
+        if seqm_parameters.get("UHF", False):
+            raise NotImplementedError("Unrestricted excited state methods (CIS and RPA) not available")
+        if exc.get("orbital_window") is not None:
+            raise NotImplementedError("an orbital_window for excited states is not supported")
+        if not seqm_parameters.get("eig", True):
+            raise NotImplementedError("excited states need the orbitals (eig=True)")
+    if seqm_parameters.get("active_state", 0):
+        raise NotImplementedError("excited-state forces and dynamics (active_state > 0) are not supported")
     if seqm_parameters.get("scf_backward", 0) != 0:
         raise NotImplementedError("scf_backward >= 1 (backpropagation through the SCF) is not supported")
     if seqm_parameters.get("pair_outer_cutoff", 1e10) < 1e10:
@@ -514,6 +530,37 @@ class Energy(torch.nn.Module):
         self.Hf_flag = seqm_parameters.get("Hf_flag", True)
         self.eig = seqm_parameters.get("eig", True)
         _check_options(seqm_parameters)
+        # excited states (basics.py:465-478): defaults, and the SCF at least 10x tighter than
+        # the excited-state tolerance (the dict is updated in place, as the reference does)
+        self.excited_states = seqm_parameters.get("excited_states")
+        if self.excited_states:
+            self.excited_states["tolerance"] = self.excited_states.get("tolerance", 1e-6)
+            self.excited_states["method"] = self.excited_states.get("method", "cis").lower()
+            if seqm_parameters["scf_eps"] > 1e-1 * self.excited_states["tolerance"]:
+                seqm_parameters["scf_eps"] = 1e-1 * self.excited_states["tolerance"]
+
+    def _excited(self, molecule, solve):
+        """CIS / RPA excitation energies and amplitudes of the ground state (basics.py:977-1029):
+        molecule.cis_energies (nmol, nroots), molecule.cis_amplitudes (nmol, nroots, nocc*nvirt),
+        for RPA (2, nmol, nroots, nocc*nvirt) with X and Y; occupied / virtual padded to the
+        batch's largest."""
+        from .excited import ExcitedStates
+
+        es = self.excited_states
+        t0 = time.time()
+        ex = ExcitedStates(solve.s)
+        with torch.no_grad():
+            E, amp = ex.solve(int(es["n_states"]), float(es["tolerance"]), rpa=es["method"] == "rpa",
+                              max_iter=es.get("max_iter"))
+        if not ex.converged.all():
+            raise Exception("Maximum iterations reached but roots have not converged")
+        dev = molecule.coordinates.device
+        molecule.cis_energies = E.to(dev)
+        molecule.cis_amplitudes = amp.to(dev)
+        molecule._excited = ex
+        if molecule.const.do_timing:
+            torch.cuda.synchronize()
+            molecule.const.timing["CIS/RPA"].append(time.time() - t0)
 
     @staticmethod
     def _refresh_geometry(molecule):
@@ -587,6 +634,8 @@ class Energy(torch.nn.Module):
         nc = nc.to(dev)
         charge = charge.to(dev) if charge is not None else None
         molecule._solve = s
+        if self.excited_states:
+            self._excited(molecule, s)
         if all_terms:
             Etot = Eelec + Enuc
             Eiso = _isolated_atom_energy(molecule.const, molecule.Z, p)

@@ -23,5 +23,7 @@ def load_golden(name):
     return g
 
 
-# single-point fixtures (the molecular dynamics trajectories, md_*, have their own tests)
-GOLDEN_NAMES = sorted(f[:-5] for f in os.listdir(GOLDEN) if f.endswith(".json") and not f.startswith("md_"))
+# single-point fixtures (molecular dynamics trajectories, md_*, and excited states, cis_* / rpa_*,
+# have their own tests)
+GOLDEN_NAMES = sorted(f[:-5] for f in os.listdir(GOLDEN)
+                      if f.endswith(".json") and not f.startswith(("md_", "cis_", "rpa_")))

@@ -218,6 +218,43 @@ def write_md(name, species, coords, settings, steps, timestep, seed, damp=None):
     print(name, "loops per step", [t["loops"] for t in traj])
 
 
+def write_excited(name, species, coords, settings):
+    """CIS / RPA excitation energies and amplitudes of the ground state through the reference's
+    Electronic_Structure (basics.py:977-1029: rcis_batch for a batch of one species, the ragged
+    rcis_any_batch otherwise, rpa)."""
+    if ONLY and name not in ONLY:
+        return
+    species = np.asarray(species)
+    coords = np.asarray(coords, dtype=np.float64)
+    sp = dict(settings)
+    sp["excited_states"] = dict(settings["excited_states"])
+    mol = Molecule(Constants(), sp, torch.as_tensor(coords.copy()), torch.as_tensor(species, dtype=torch.int64))
+    mol.verbose = False
+    Electronic_Structure(sp)(mol)
+    amps = mol.cis_amplitudes.detach().numpy()
+    # transition densities C_occ X C_virt^T in the packed AO basis (independent of the MO signs);
+    # for RPA of X and of Y
+    C = mol.molecular_orbitals.detach().numpy()
+    nocc, norb = mol.nocc.numpy(), mol.norb.numpy()
+    no_max, nv_max = int(nocc.max()), int((norb - nocc).max())
+    sets = [amps[0], amps[1]] if amps.ndim == 4 else [amps]
+    tdm = []
+    for a in sets:
+        per = []
+        for m in range(species.shape[0]):
+            n, no = int(norb[m]), int(nocc[m])
+            X = a[m].reshape(a.shape[1], no_max, nv_max)[:, :no, :n - no]
+            per.append(np.einsum("mi,ria,na->rmn", C[m, :n, :no], X, C[m, :n, no:n]).tolist())
+        tdm.append(per)
+    rec = dict(name=name, settings=settings, species=species.tolist(), coords=coords.tolist(),
+               ref=dict(Etot=mol.Etot.detach().numpy().tolist(), cis_energies=mol.cis_energies.numpy().tolist(),
+                        cis_amplitudes=amps.tolist(), transition_densities=tdm,
+                        e=mol.e_mo.detach().numpy().tolist(), nocc=nocc.tolist(), norb=norb.tolist()))
+    with open(os.path.join(HERE, f"{name}.json"), "w") as f:
+        json.dump(rec, f)
+    print(name, "excitation energies", np.round(mol.cis_energies.numpy(), 4).tolist())
+
+
 def _open_shells():
     """CH3 (planar, doublet), OH (doublet), NO (doublet), CH2 (bent, triplet), O2 (triplet),
     H2O (singlet, run unrestricted)."""
@@ -300,6 +337,20 @@ def main():
           charges=[1, -1, 1, 0])
     write("ions_pm3", *workloads.pad_batch(_ions()), {"method": "PM3", "scf_eps": 1e-8, "scf_converger": [1]},
           charges=[1, -1, 1, 0])
+
+    # excited states: CIS on a ragged batch, CIS and RPA on a batch of one species
+    rng = np.random.default_rng(8)
+    mols = [workloads.alkane(2, rng, 0.03), workloads.water_cluster(2, rng), workloads.alkane(3, rng, 0.03),
+            workloads.water_cluster(3, rng)]
+    write_excited("cis_am1_mixed", *workloads.pad_batch(mols),
+                  {"method": "AM1", "scf_eps": 1e-8, "scf_converger": [1],
+                   "excited_states": {"method": "cis", "n_states": 4, "tolerance": 1e-7}})
+    rng = np.random.default_rng(9)
+    same = [workloads.alkane(3, rng, 0.05) for _ in range(3)]
+    for method, es in (("PM3", "cis"), ("AM1", "rpa")):
+        write_excited(f"{es}_{method.lower()}_same", *workloads.pad_batch(same),
+                      {"method": method, "scf_eps": 1e-8, "scf_converger": [1],
+                       "excited_states": {"method": es, "n_states": 5, "tolerance": 1e-7}})
 
     # molecular dynamics: velocity Verlet and Temp 0 Langevin (friction only) from seeded velocities
     rng = np.random.default_rng(5)

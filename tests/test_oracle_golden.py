@@ -115,3 +115,25 @@ def test_oracle_md_matches_reference_trajectory(name):
         np.testing.assert_allclose(traj[k]["force"], ref["force"], atol=1e-5, rtol=0)
         np.testing.assert_allclose(traj[k]["Etot"], ref["Etot"], atol=1e-7, rtol=0)
         np.testing.assert_allclose(traj[k]["Ek"], ref["Ek"], atol=1e-7, rtol=0)
+
+
+@pytest.mark.parametrize("name", ["cis_am1_mixed", "cis_pm3_same", "rpa_am1_same"])
+def test_oracle_excited_states_match_reference(name):
+    """CIS / RPA of the oracle (full matrices, exact diagonalisation) against the reference's
+    Davidson solvers: excitation energies to 1e-9 eV, transition densities C_occ X C_virt^T
+    (independent of orbital signs) to 1e-6 up to one sign per state."""
+    from oracle import seqm_excited as X
+
+    g = load_golden(name)
+    s = g["settings"]
+    es = s["excited_states"]
+    f = X.rpa if es["method"] == "rpa" else X.cis
+    out = f(s["method"], g["species_np"], g["coords_np"], s["scf_eps"], es["n_states"])
+    np.testing.assert_allclose([o["energies"] for o in out], g["ref"]["cis_energies"], atol=1e-9, rtol=0)
+    T = g["ref"]["transition_densities"]
+    for m, o in enumerate(out):
+        for key, Tr in (("transition_density", T[0][m]),) + ((("transition_density_y", T[1][m]),) if len(T) > 1 else ()):
+            Tr = np.asarray(Tr)
+            sg = np.sign((Tr * o["transition_density"] if key == "transition_density" else
+                          np.asarray(T[0][m]) * o["transition_density"]).sum((1, 2)))[:, None, None]
+            np.testing.assert_allclose(sg * o[key], Tr, atol=1e-6, rtol=0)

@@ -98,3 +98,90 @@ def trajectory(method, species, coords, v0, steps, dt, eps, converger=(1,), damp
         v = v * c1
         traj.append(dict(coordinates=r.copy(), velocities=v.copy(), force=f, Etot=etot, Ek=kinetic_energy(mass, v)))
     return traj
+
+
+# dissipative extended-Lagrangian coefficients [kappa, alpha, c0..ck] (Niklasson et al., J. Chem.
+# Phys. 130, 214109 (2009); MolecularDynamics.py:1367-1376)
+XL_COEFFS = {
+    3: [1.69, 150e-3, -2.0, 3.0, 0.0, -1.0],
+    4: [1.75, 57e-3, -3.0, 6.0, -2.0, -2.0, 1.0],
+    5: [1.82, 18e-3, -6.0, 14.0, -8.0, -3.0, 4.0, -1.0],
+    6: [1.84, 5.5e-3, -14.0, 36.0, -27.0, -2.0, 12.0, -6.0, 1.0],
+    7: [1.86, 1.6e-3, -36.0, 99.0, -88.0, 11.0, 32.0, -25.0, 8.0, -1.0],
+    8: [1.88, 0.44e-3, -99.0, 286.0, -286.0, 78.0, 78.0, -90.0, 42.0, -10.0, 1.0],
+    9: [1.89, 0.12e-3, -286.0, 858.0, -936.0, 364.0, 168.0, -300.0, 184.0, -63.0, 12.0, -1.0],
+}
+
+
+def xl_energy(method, species, coords, P, D=None):
+    """Shadow energy of XL-BOMD (dynamics/xlbomd.py:58-505 without the Krylov kernel): F = F(P),
+    D from the eigensolve of F unless given, Eelec = tr(D F) - 1/2 tr((F - H) P)
+    (energy.py:76-88); returns Hf, Etot per molecule and D."""
+    el = O.load_elements()
+    mol = O.parse(species, coords)
+    p = O.atom_params(method, mol["Z"])
+    ints = O.integrals(mol, p, el)
+    M = O.hcore(mol, p, ints)
+    nmol, ms = mol["nmol"], mol["molsize"]
+    H = O.symmetrize_upper(O.blocks_to_full(M, nmol, ms))
+    F = O.fock(mol, p, ints, M, P)
+    if D is None:
+        D, _, _ = O.density_eigh(F, mol["nheavy"], mol["nhyd"], mol["nocc"])
+    Eelec = np.sum(D * F - 0.5 * (F - H) * P, axis=(1, 2))
+    EnucAB = O.pair_nuclear_energy(method, mol, p, ints["w"][:, 0, 0], el)
+    Enuc = np.zeros(nmol)
+    np.add.at(Enuc, mol["pair_molid"], EnucAB)
+    Eiso = np.zeros(nmol)
+    np.add.at(Eiso, mol["atom_molid"], O.isolated_atom_energy(mol["Z"], p, el))
+    eheat = np.zeros(nmol)
+    np.add.at(eheat, mol["atom_molid"], el["eheat_ev"][mol["Z"]])
+    Etot = Eelec + Enuc
+    return dict(Etot=Etot, Hf=Etot - Eiso + eheat, D=D)
+
+
+def xl_trajectory(method, species, coords, v0, steps, dt, eps, k, converger=(1,), h=1.0e-5):
+    """XL-BOMD without thermostat (MolecularDynamics.py:1434-1600): the first forces and density
+    from the SCF, then the auxiliary density propagated with the k-th order coefficients and the
+    shadow-potential forces by central differences at fixed D and P."""
+    species = np.asarray(species)
+    r = np.array(coords, dtype=np.float64)
+    mass = masses(species)
+    minv = np.where(mass > 0, 1.0 / np.where(mass > 0, mass, 1.0), 0.0)
+    v = zero_com(mass, r, np.array(v0, dtype=np.float64), remove_angular=True, restore_kinetic_energy=False)
+    out = O.single_point(method, species, r, eps, converger, forces=True)
+    f, dm = out["force"], out["P"]
+    a = f * minv * ACC_SCALE
+    traj = [dict(coordinates=r.copy(), velocities=v.copy(), force=f, Etot=out["Etot"], Ek=kinetic_energy(mass, v))]
+    m = k + 1
+    kappa, alpha = XL_COEFFS[k][0], XL_COEFFS[k][1]
+    coeff = np.array(XL_COEFFS[k][2:]) * alpha
+    coeff[0] += 2.0 - kappa
+    coeff[1] -= 1.0
+    coeff = np.tile(coeff, 2)
+    P = dm.copy()
+    Pt = np.repeat(dm[None], m, axis=0)
+    for step in range(steps):
+        v = v + 0.5 * a * dt
+        r = r + v * dt
+        c = step % m
+        P = kappa * (0.95 * dm + 0.05 * P) + np.tensordot(coeff[c: c + m], Pt, axes=1)
+        Pt[m - 1 - c] = P
+        e0 = xl_energy(method, species, r, P)
+        dm = e0["D"]
+        f = np.zeros_like(r)
+        for mi in range(r.shape[0]):
+            for at in range(r.shape[1]):
+                if species[mi, at] == 0:
+                    continue
+                for x in range(3):
+                    vals = []
+                    for sgn in (1.0, -1.0):
+                        rr = r.copy()
+                        rr[mi, at, x] += sgn * h
+                        vals.append(xl_energy(method, species, rr, P, dm)["Hf"][mi])
+                    f[mi, at, x] = -(vals[0] - vals[1]) / (2.0 * h)
+        a = f * minv * ACC_SCALE
+        v = v + 0.5 * a * dt
+        traj.append(dict(coordinates=r.copy(), velocities=v.copy(), force=f, Etot=e0["Etot"],
+                         Ek=kinetic_energy(mass, v)))
+    return traj

@@ -683,6 +683,84 @@ class Force(torch.nn.Module):
                 e, e_gap, charge, nc)
 
 
+def _xl_bomd_force(molecule, P, seqm_parameters):
+    """XL-BOMD energy and forces from the auxiliary density P (the extended-Lagrangian shadow
+    potential, dynamics/xlbomd.py:58-505 without the Krylov kernel): F = F(P) (one Fock build),
+    D = 2 C_occ C_occ^T of F (one eigensolve, no SCF), Eelec = tr(D F) - 1/2 tr((F - H) P)
+    (energy.py:76-88), forces -d(Eelec + Enuc)/dR at fixed D and P.
+
+    The shadow energy is tr(D H) + B(D, P) - 1/2 B(P, P) with B(X, Y) = tr(X G(Y)) symmetric and
+    bilinear; the adjoint kernel gives g(X) = d/dR [tr(X H) + 1/2 B(X, X)] for any symmetric X,
+    so the gradient is 3/2 g(D + P) - 1/2 g(-(D + P)) - g(D) - 2 g(P) (polarisation) plus the
+    nuclear term.  The layout, integrals buffers and the eigensolver's warm start stay on the
+    device between steps (the solve of the first SCF step is continued)."""
+    if P is None:
+        raise ValueError("XL-BOMD needs the auxiliary density P0")
+    if seqm_parameters.get("UHF", False):
+        raise NotImplementedError("XL-BOMD is implemented for closed shells")
+    sv = getattr(molecule, "_solve", None)
+    if sv is None or not sv.matches(molecule, seqm_parameters):
+        sv = _Solve(molecule, seqm_parameters)
+        molecule._solve = sv
+    L, s, dev = sv.L, sv.s, sv.dev
+    lib = native.load()
+    with torch.no_grad():
+        real = torch.as_tensor(L.real_index, device=molecule.coordinates.device)
+        L.set_coordinates(molecule.coordinates.detach().reshape(-1, 3)[real].cpu().numpy())
+        s.hcore()
+        Pk = L.padded_to_packed(P.detach().to(dev, torch.float64))
+        s.P.copy_(Pk)
+        s.fock()  # F(P)
+        evecs = torch.empty_like(s.work)
+        s.density(s.Pnew, (False,), active=None, evecs=evecs, density_only=0)
+        s.evecs = evecs
+        D = s.Pnew
+        if getattr(L, "_elem_mol", None) is None:
+            L._elem_mol = torch.repeat_interleave(torch.arange(L.nmol, device=dev),
+                                                  torch.as_tensor(L.norb * L.norb, device=dev))
+        T = int(L.mat_off[-1])
+        t = D[:T] * s.F[:T] - 0.5 * (s.F[:T] - s.H[:T]) * Pk[:T]
+        Eelec = torch.zeros(L.nmol, dtype=torch.float64, device=dev).index_add_(0, L._elem_mol, t)
+        Enuc = s.Enuc[: L.nmol].clone()
+        # forces by polarisation of the adjoint kernel's quadratic form
+        ones = torch.ones(max(1, L.nmol), dtype=torch.float64, device=dev)
+        zeros = torch.zeros_like(ones)
+        dR = torch.zeros(3 * max(1, L.natoms), dtype=torch.float64, device=dev)
+        dpar = torch.empty(4 * max(1, L.natoms), dtype=torch.float64, device=dev)
+        work = torch.empty(7 * max(1, L.npairs), dtype=torch.float64, device=dev)
+        Dp = D[:T] + Pk[:T]
+        grad = torch.zeros(3 * L.natoms, dtype=torch.float64, device=dev)
+        for X, c, gE, gN in ((Dp, 1.5, ones, zeros), (-Dp, -0.5, ones, zeros), (D[:T], -1.0, ones, zeros),
+                             (Pk[:T], -2.0, ones, zeros), (Pk[:T], 1.0, zeros, ones)):
+            X = X.contiguous()
+            s.launches += 2
+            native.check(lib.seqm_energy_grad(L.struct, native.ptr(X), None, native.ptr(gE), native.ptr(gN),
+                                              native.ptr(dR), native.ptr(dpar), native.ptr(work), s._s()),
+                         "seqm_energy_grad")
+            grad += c * dR[: 3 * L.natoms]
+        cdev = molecule.coordinates.device
+        force = torch.zeros(L.nmol * L.molsize, 3, dtype=torch.float64, device=cdev)
+        force[real] = -grad.view(L.natoms, 3).to(cdev)
+        molecule.force = force.view(L.nmol, L.molsize, 3)
+        molecule.dm = L.packed_to_padded(D).to(cdev)
+        Etot = (Eelec + Enuc).to(cdev)
+        p = molecule.parameters
+        Eiso = _isolated_atom_energy(molecule.const, molecule.Z, p)
+        Eiso_sum = torch.zeros_like(Etot).index_add(0, molecule.atom_molid, Eiso.detach())
+        eheat = torch.zeros_like(Etot).index_add(0, molecule.atom_molid, molecule.const.eheat[molecule.Z])
+        molecule.Etot, molecule.Eelec, molecule.Enuc, molecule.Eiso = Etot, Eelec.to(cdev), Enuc.to(cdev), Eiso_sum
+        molecule.Hf = Etot - Eiso_sum + eheat if seqm_parameters.get("Hf_flag", True) else Etot - Eiso_sum
+        e, v = sv.eigen_padded()
+        lumo = molecule.nocc.unsqueeze(0).T.to(e.device)
+        molecule.e_mo = e.to(cdev)
+        molecule.e_gap = (e.gather(1, lumo) - e.gather(1, lumo - 1)).reshape(-1).to(cdev)
+        molecule.molecular_orbitals = v.to(cdev)
+        molecule.Electronic_entropy = torch.zeros(L.nmol, dtype=torch.float64, device=cdev)
+        molecule.dP2dt2 = None
+        molecule.Krylov_Error = None
+        molecule.Fermi_occ = None
+
+
 class Electronic_Structure(torch.nn.Module):
     """Single-point driver (ElectronicStructure.py:10-127): sets force, dm, energies, charges."""
 
@@ -699,19 +777,29 @@ class Electronic_Structure(torch.nn.Module):
 
     def forward(self, molecule, learned_parameters=dict(), xl_bomd_params=dict(), P0=None, err_threshold=None,
                 max_rank=None, T_el=None, dm_prop="SCF", *args, **kwargs):
-        if dm_prop != "SCF":
-            raise NotImplementedError("only dm_prop='SCF' is supported")
-        (molecule.force, P, molecule.Hf, molecule.Etot, molecule.Eelec, molecule.Enuc, molecule.Eiso, molecule.e_mo,
-         molecule.e_gap, self.charge, self.notconverged) = self.conservative_force(
-            molecule, P0=P0, learned_parameters=learned_parameters)
-        molecule.dm = P.detach()
-        molecule._solve_dm = molecule.dm  # the density handed out; an MD step passes it back as P0
+        if dm_prop == "XL-BOMD":
+            if "max_rank" in (xl_bomd_params or {}) or max_rank is not None:
+                raise NotImplementedError("Krylov-subspace XL-BOMD (max_rank) is not supported")
+            if callable(learned_parameters) or learned_parameters:
+                raise NotImplementedError("XL-BOMD with learned parameters is not supported")
+            _xl_bomd_force(molecule, P0, self.seqm_parameters)
+        elif dm_prop != "SCF":
+            raise NotImplementedError("dm_prop must be 'SCF' or 'XL-BOMD'")
+        else:
+            self._scf(molecule, P0, learned_parameters)
         with torch.no_grad():
             if molecule.dm.dim() == 4:  # open shell: both spins (ElectronicStructure.py:106-117)
                 molecule.q = (molecule.const.tore[molecule.species] - self.atomic_charges(molecule.dm[:, 0])
                               - self.atomic_charges(molecule.dm[:, 1]))
             else:
                 molecule.q = molecule.const.tore[molecule.species] - self.atomic_charges(molecule.dm)
+
+    def _scf(self, molecule, P0, learned_parameters):
+        (molecule.force, P, molecule.Hf, molecule.Etot, molecule.Eelec, molecule.Enuc, molecule.Eiso, molecule.e_mo,
+         molecule.e_gap, self.charge, self.notconverged) = self.conservative_force(
+            molecule, P0=P0, learned_parameters=learned_parameters)
+        molecule.dm = P.detach()
+        molecule._solve_dm = molecule.dm  # the density handed out; an MD step passes it back as P0
 
     def get_force(self):
         return self.force

@@ -87,3 +87,34 @@ def test_md_trajectory_matches_reference(name):
     assert all(sv is solves[0] for sv in solves)  # one device-resident solve for the whole run
     for k in range(1, len(ref)):
         assert abs(iters[k] - ref[k]["loops"]) <= 1
+
+
+def test_xlbomd_trajectory_matches_reference():
+    """XL_BOMD (k = 6, no thermostat) on the GPU against the reference's XL_BOMD: 10 steps of
+    auxiliary-density propagation, one Fock build and one eigensolve per step, shadow-potential
+    forces from the adjoint kernel; positions and velocities to 1e-6, forces 1e-5 eV/A, shadow
+    energies 1e-6 eV, HOMO-LUMO gaps 1e-6 eV."""
+    import torch
+
+    from pyseqm_gb300 import XL_BOMD, Constants, Molecule
+    from conftest import load_golden
+
+    g = load_golden("md_am1_xlbomd")
+    s = dict(g["settings"])
+    mol = Molecule(Constants().cuda(), s, torch.as_tensor(g["coords_np"], device="cuda"),
+                   torch.as_tensor(g["species_np"], device="cuda")).cuda()
+    mol.velocities = torch.as_tensor(np.asarray(g["velocities0"]), device="cuda")
+    md = XL_BOMD(xl_bomd_params={"k": g["k"]}, seqm_parameters=s, timestep=g["timestep"], Temp=0.0,
+                 output={"print every": 0}).cuda()
+    md.initialize(mol)
+    ref = g["ref"]["trajectory"]
+    solve0 = mol._solve
+    for i, r in enumerate(ref):
+        if i > 0:
+            md._do_integrator_step(i - 1, mol, {})
+        np.testing.assert_allclose(mol.coordinates.detach().cpu().numpy(), r["coordinates"], atol=1e-6, rtol=0)
+        np.testing.assert_allclose(mol.velocities.detach().cpu().numpy(), r["velocities"], atol=1e-6, rtol=0)
+        np.testing.assert_allclose(mol.force.cpu().numpy(), r["force"], atol=1e-5, rtol=0)
+        np.testing.assert_allclose(mol.Etot.detach().cpu().numpy(), r["Etot"], atol=1e-6, rtol=0)
+        np.testing.assert_allclose(mol.e_gap.detach().cpu().numpy().reshape(-1), r["e_gap"], atol=1e-6, rtol=0)
+    assert mol._solve is solve0  # the first step's solve continues on the device

@@ -137,3 +137,19 @@ def test_oracle_excited_states_match_reference(name):
             sg = np.sign((Tr * o["transition_density"] if key == "transition_density" else
                           np.asarray(T[0][m]) * o["transition_density"]).sum((1, 2)))[:, None, None]
             np.testing.assert_allclose(sg * o[key], Tr, atol=1e-6, rtol=0)
+
+
+def test_oracle_xlbomd_matches_reference_trajectory():
+    """XL-BOMD (k = 6, no thermostat): the oracle's propagation and shadow-potential forces
+    (central differences at fixed D and P) against the reference's XL_BOMD driver, 4 steps."""
+    from oracle import seqm_md as MD
+
+    g = load_golden("md_am1_xlbomd")
+    s = g["settings"]
+    traj = MD.xl_trajectory(s["method"], g["species_np"], g["coords_np"], np.asarray(g["velocities0"]), 4,
+                            g["timestep"], s["scf_eps"], g["k"])
+    for k, ref in enumerate(g["ref"]["trajectory"][:5]):
+        np.testing.assert_allclose(traj[k]["coordinates"], ref["coordinates"], atol=1e-8, rtol=0)
+        np.testing.assert_allclose(traj[k]["velocities"], ref["velocities"], atol=1e-8, rtol=0)
+        np.testing.assert_allclose(traj[k]["force"], ref["force"], atol=1e-6, rtol=0)
+        np.testing.assert_allclose(traj[k]["Etot"], ref["Etot"], atol=1e-8, rtol=0)

@@ -185,3 +185,149 @@ def xl_trajectory(method, species, coords, v0, steps, dt, eps, k, converger=(1,)
         traj.append(dict(coordinates=r.copy(), velocities=v.copy(), force=f, Etot=e0["Etot"],
                          Ek=kinetic_energy(mass, v)))
     return traj
+
+
+KB_EV = 8.61739e-5  # eV/K, dynamics/xlbomd.py:206
+CANON_DM_PRT_ITER = 10  # dynamics/xlbomd.py:55
+
+
+def fermi_density(f, nocc, T):
+    """Fermi-Dirac density of one packed Fock matrix (fermi_q.py:8-72): eigenpairs, mu by
+    Newton iterations on sum_i f_i = nocc (64 at most, tolerance 1e-9), D = 2 Q f Q^T and the
+    entropy S = -kB sum [f ln f + (1 - f) ln (1 - f)] over 1e-14 < f < 1 - 1e-14."""
+    e, Q = np.linalg.eigh(f, UPLO="U")
+    beta = 1.0 / (KB_EV * T)
+    mu = 0.5 * (e[nocc - 1] + e[nocc])
+    for _ in range(64):
+        fe = 1.0 / (1.0 + np.exp(beta * (e - mu)))
+        occ = fe.sum()
+        if abs(nocc - occ) <= 1e-9:
+            break
+        mu += (nocc - occ) / max((beta * fe * (1.0 - fe)).sum(), 1e-30)
+    D = 2.0 * (Q * fe) @ Q.T
+    ok = (fe > 1e-14) & (1.0 - fe > 1e-14)
+    p = np.where(ok, fe, 0.5)
+    S = np.sum(np.where(ok, -KB_EV * (p * np.log(p) + (1.0 - p) * np.log(1.0 - p)), 0.0))
+    return D, S, Q, e, mu
+
+
+def canon_dm_prt(F1, T, Q, e, mu0, m=CANON_DM_PRT_ITER):
+    """First-order density response to F1 by canonical density-matrix perturbation theory
+    (canon_dm_prt.py:6-39; Alg. 2 of J. Chem. Theory Comput. 16, 3628 (2020))."""
+    beta = 1.0 / (KB_EV * T)
+    cnst = 2.0 ** (-2 - m) * beta
+    p0 = (0.5 - cnst * (e - mu0))[:, None]
+    P1 = -cnst * (Q.T @ F1 @ Q)
+    for _ in range(m):
+        p02 = p0 * p0
+        dX1 = p0 * P1 + P1 * p0.T
+        iD0 = 1.0 / (2.0 * (p02 - p0) + 1.0)
+        p0 = iD0 * p02
+        P1 = iD0 * (dX1 + 2.0 * (P1 - dX1) * p0.T)
+    dpdmu = beta * p0 * (1.0 - p0)
+    dmu1 = -np.trace(P1) / dpdmu.sum()
+    P1 = P1 + np.diag(dpdmu[:, 0]) * dmu1
+    return Q @ P1 @ Q.T
+
+
+def krylov_xl(method, species, coords, P, T, rank, err_threshold=0.0):
+    """Fermi density D of F(P), entropy, and the rank-m Krylov approximation of the kernel
+    dP2dt2 = -V alpha (dynamics/xlbomd.py:200-341) for one molecule (packed basis)."""
+    el = O.load_elements()
+    mol = O.parse(species, coords)
+    p = O.atom_params(method, mol["Z"])
+    ints = O.integrals(mol, p, el)
+    M = O.hcore(mol, p, ints)
+    F = O.fock(mol, p, ints, M, P)
+    idx = O.packed_index(mol["nheavy"][0], mol["nhyd"][0])
+    nocc = int(mol["nocc"][0])
+    D, S, Q, e, mu = fermi_density(F[0][np.ix_(idx, idx)], nocc, T)
+    n4 = F.shape[-1]
+    Dfull = np.zeros_like(F)
+    Dfull[0][np.ix_(idx, idx)] = D
+    dDS = Dfull - P
+    nrm = np.linalg.norm(dDS)
+    V, W = [], []
+    dW = dDS
+    err = 10.0
+    k = -1
+    zeros = np.zeros((mol["nmol"] * mol["molsize"] ** 2, 4, 4))
+    while k < rank - 1 and err > err_threshold:
+        k += 1
+        v = dW.copy()
+        for vj in V:
+            v = v - np.sum(v[0].T * vj[0]) * vj
+        v = v / np.linalg.norm(v)
+        V.append(v)
+        G = O.fock(mol, p, ints, zeros, v)
+        P1 = np.zeros((1, n4, n4))
+        P1[0][np.ix_(idx, idx)] = canon_dm_prt(G[0][np.ix_(idx, idx)], T, Q, e, mu)
+        w = P1 - v
+        W.append(w)
+        dW = w
+        Wm = np.stack([x[0] for x in W], axis=-1)
+        Ov = np.einsum("jir,ijq->rq", Wm, Wm)
+        rhs = np.einsum("jir,ij->r", Wm, dDS[0])
+        alpha = np.linalg.solve(Ov, rhs)
+        err = np.linalg.norm(np.einsum("ijr,r->ij", Wm, alpha) - dDS[0]) / nrm
+    Vm = np.stack([x[0] for x in V], axis=-1)
+    return Dfull, S, -np.einsum("ijr,r->ij", Vm, alpha)[None]
+
+
+def ksa_trajectory(method, species, coords, v0, steps, dt, eps, k, T, rank, converger=(1,), h=1.0e-5):
+    """KSA-XL-BOMD without thermostat (MolecularDynamics.py:1602-1616): as xl_trajectory with
+    Fermi-Dirac densities at T and P propagated with the Krylov kernel's dP2dt2; per molecule,
+    so that err_threshold 0 (every molecule at the full rank) decouples the batch."""
+    species = np.asarray(species)
+    r = np.array(coords, dtype=np.float64)
+    mass = masses(species)
+    minv = np.where(mass > 0, 1.0 / np.where(mass > 0, mass, 1.0), 0.0)
+    v = zero_com(mass, r, np.array(v0, dtype=np.float64), remove_angular=True, restore_kinetic_energy=False)
+    out = O.single_point(method, species, r, eps, converger, forces=True)
+    f, dm = out["force"], out["P"]
+    a = f * minv * ACC_SCALE
+    traj = [dict(coordinates=r.copy(), velocities=v.copy(), force=f, Etot=out["Etot"], Ek=kinetic_energy(mass, v))]
+    m = k + 1
+    kappa, alpha = XL_COEFFS[k][0], XL_COEFFS[k][1]
+    coeff = np.array(XL_COEFFS[k][2:]) * alpha
+    coeff[0] += 2.0 - kappa
+    coeff[1] -= 1.0
+    coeff = np.tile(coeff, 2)
+    P = dm.copy()
+    Pt = np.repeat(dm[None], m, axis=0)
+    d2 = np.zeros_like(dm)
+    nmol = species.shape[0]
+    for step in range(steps):
+        v = v + 0.5 * a * dt
+        r = r + v * dt
+        c = step % m
+        P = kappa * (d2 + P) + np.tensordot(coeff[c: c + m], Pt, axes=1)
+        Pt[m - 1 - c] = P
+        D = np.zeros_like(P)
+        S = np.zeros(nmol)
+        for mi in range(nmol):
+            na = int(np.sum(species[mi] > 0))
+            n4 = 4 * na
+            Dm, S[mi], d2m = krylov_xl(method, species[mi: mi + 1, :na], r[mi: mi + 1, :na],
+                                       P[mi: mi + 1, :n4, :n4], T, rank)
+            D[mi, :n4, :n4] = Dm[0]
+            d2[mi] = 0.0
+            d2[mi, :n4, :n4] = d2m[0]
+        e0 = xl_energy(method, species, r, P, D)
+        f = np.zeros_like(r)
+        for mi in range(nmol):
+            for at in range(r.shape[1]):
+                if species[mi, at] == 0:
+                    continue
+                for x in range(3):
+                    vals = []
+                    for sgn in (1.0, -1.0):
+                        rr = r.copy()
+                        rr[mi, at, x] += sgn * h
+                        vals.append(xl_energy(method, species, rr, P, D)["Hf"][mi])
+                    f[mi, at, x] = -(vals[0] - vals[1]) / (2.0 * h)
+        a = f * minv * ACC_SCALE
+        v = v + 0.5 * a * dt
+        traj.append(dict(coordinates=r.copy(), velocities=v.copy(), force=f, Etot=e0["Etot"],
+                         Ek=kinetic_energy(mass, v), entropy=-2.0 * T * S))
+    return traj

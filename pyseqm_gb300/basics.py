@@ -683,7 +683,7 @@ class Force(torch.nn.Module):
                 e, e_gap, charge, nc)
 
 
-def _xl_bomd_force(molecule, P, seqm_parameters):
+def _xl_bomd_force(molecule, P, seqm_parameters, xl_params=None):
     """XL-BOMD energy and forces from the auxiliary density P (the extended-Lagrangian shadow
     potential, dynamics/xlbomd.py:58-505 without the Krylov kernel): F = F(P) (one Fock build),
     D = 2 C_occ C_occ^T of F (one eigensolve, no SCF), Eelec = tr(D F) - 1/2 tr((F - H) P)
@@ -693,7 +693,12 @@ def _xl_bomd_force(molecule, P, seqm_parameters):
     bilinear; the adjoint kernel gives g(X) = d/dR [tr(X H) + 1/2 B(X, X)] for any symmetric X,
     so the gradient is 3/2 g(D + P) - 1/2 g(-(D + P)) - g(D) - 2 g(P) (polarisation) plus the
     nuclear term.  The layout, integrals buffers and the eigensolver's warm start stay on the
-    device between steps (the solve of the first SCF step is continued)."""
+    device between steps (the solve of the first SCF step is continued).  With max_rank in
+    xl_params (KSA-XL-BOMD, xlbomd.py:200-341): D is the Fermi-Dirac density at T_el, the
+    entropy term -2 T_el S is returned as Electronic_entropy and the rank-m Krylov kernel gives
+    molecule.dP2dt2 for the propagation."""
+    xl_params = xl_params or {}
+    krylov = "max_rank" in xl_params
     if P is None:
         raise ValueError("XL-BOMD needs the auxiliary density P0")
     if seqm_parameters.get("UHF", False):
@@ -715,6 +720,19 @@ def _xl_bomd_force(molecule, P, seqm_parameters):
         s.density(s.Pnew, (False,), active=None, evecs=evecs, density_only=0)
         s.evecs = evecs
         D = s.Pnew
+        if krylov:
+            from .xl_krylov import PaddedBasis, fermi_density, krylov_kernel
+
+            if getattr(L, "_padded_basis", None) is None:
+                L._padded_basis = PaddedBasis(L)
+            basis = L._padded_basis
+            T_el = float(xl_params["T_el"])
+            Q = basis.to_padded(evecs).transpose(1, 2)
+            e = basis.vector_to_padded(s.evals)
+            Dp, S_ent, fe, mu = fermi_density(e, Q, L.nocc, basis.mask, T_el)
+            d2, kerr = krylov_kernel(s, basis, Dp, basis.to_padded(Pk), Q, e, mu, T_el, int(xl_params["max_rank"]),
+                                     float(xl_params["err_threshold"]))
+            D = basis.to_ragged(Dp)
         if getattr(L, "_elem_mol", None) is None:
             L._elem_mol = torch.repeat_interleave(torch.arange(L.nmol, device=dev),
                                                   torch.as_tensor(L.norb * L.norb, device=dev))
@@ -755,10 +773,16 @@ def _xl_bomd_force(molecule, P, seqm_parameters):
         molecule.e_mo = e.to(cdev)
         molecule.e_gap = (e.gather(1, lumo) - e.gather(1, lumo - 1)).reshape(-1).to(cdev)
         molecule.molecular_orbitals = v.to(cdev)
-        molecule.Electronic_entropy = torch.zeros(L.nmol, dtype=torch.float64, device=cdev)
-        molecule.dP2dt2 = None
-        molecule.Krylov_Error = None
-        molecule.Fermi_occ = None
+        if krylov:
+            molecule.Electronic_entropy = (-2.0 * T_el * S_ent).to(cdev)
+            molecule.dP2dt2 = L.packed_to_padded(basis.to_ragged(d2)).to(cdev)
+            molecule.Krylov_Error = kerr.to(cdev)
+            molecule.Fermi_occ = fe.to(cdev)
+        else:
+            molecule.Electronic_entropy = torch.zeros(L.nmol, dtype=torch.float64, device=cdev)
+            molecule.dP2dt2 = None
+            molecule.Krylov_Error = None
+            molecule.Fermi_occ = None
 
 
 class Electronic_Structure(torch.nn.Module):
@@ -778,11 +802,9 @@ class Electronic_Structure(torch.nn.Module):
     def forward(self, molecule, learned_parameters=dict(), xl_bomd_params=dict(), P0=None, err_threshold=None,
                 max_rank=None, T_el=None, dm_prop="SCF", *args, **kwargs):
         if dm_prop == "XL-BOMD":
-            if "max_rank" in (xl_bomd_params or {}) or max_rank is not None:
-                raise NotImplementedError("Krylov-subspace XL-BOMD (max_rank) is not supported")
             if callable(learned_parameters) or learned_parameters:
                 raise NotImplementedError("XL-BOMD with learned parameters is not supported")
-            _xl_bomd_force(molecule, P0, self.seqm_parameters)
+            _xl_bomd_force(molecule, P0, self.seqm_parameters, xl_bomd_params or {})
         elif dm_prop != "SCF":
             raise NotImplementedError("dm_prop must be 'SCF' or 'XL-BOMD'")
         else:

@@ -255,14 +255,14 @@ def write_excited(name, species, coords, settings):
     print(name, "excitation energies", np.round(mol.cis_energies.numpy(), 4).tolist())
 
 
-def write_xlbomd(name, species, coords, settings, steps, timestep, seed, k):
+def write_xlbomd(name, species, coords, settings, steps, timestep, seed, k, krylov=None):
     """A short XL-BOMD trajectory (no thermostat, no Krylov kernel) through the reference's XL_BOMD
     driver: the first step's SCF, then the auxiliary density propagated with the k-th order
     dissipative coefficients and one diagonalisation of F(P) per step (MolecularDynamics.py:
     1380-1600, dynamics/xlbomd.py:58-505)."""
     if ONLY and name not in ONLY:
         return
-    from seqm.MolecularDynamics import XL_BOMD
+    from seqm.MolecularDynamics import KSA_XL_BOMD, XL_BOMD
 
     species = np.asarray(species)
     coords = np.asarray(coords, dtype=np.float64)
@@ -272,7 +272,9 @@ def write_xlbomd(name, species, coords, settings, steps, timestep, seed, k):
     mol.verbose = False
     mol.velocities = torch.as_tensor(v0.copy())
     out = {"molid": [0], "print every": 0, "checkpoint every": 0, "h5": {}}
-    md = XL_BOMD(xl_bomd_params={"k": k}, seqm_parameters=sp, timestep=timestep, Temp=0.0, output=out)
+    params = dict({"k": k}, **(krylov or {}))
+    cls = KSA_XL_BOMD if krylov else XL_BOMD
+    md = cls(xl_bomd_params=params, seqm_parameters=sp, timestep=timestep, Temp=0.0, output=out)
     md.initialize(mol)
     traj = []
 
@@ -282,14 +284,16 @@ def write_xlbomd(name, species, coords, settings, steps, timestep, seed, k):
             traj.append(dict(coordinates=mol.coordinates.detach().numpy().tolist(),
                              velocities=mol.velocities.detach().numpy().tolist(),
                              force=mol.force.detach().numpy().tolist(), Etot=mol.Etot.detach().numpy().tolist(),
-                             Ek=Ek.numpy().tolist(), e_gap=mol.e_gap.detach().numpy().reshape(-1).tolist()))
+                             Ek=Ek.numpy().tolist(), e_gap=mol.e_gap.detach().numpy().reshape(-1).tolist(),
+                             entropy=mol.Electronic_entropy.detach().numpy().reshape(-1).tolist()))
 
     record()
     for i in range(steps):
         md._do_integrator_step(i, mol, {})
         record()
     rec = dict(name=name, settings=settings, species=species.tolist(), coords=coords.tolist(),
-               velocities0=v0.tolist(), timestep=timestep, steps=steps, k=k, ref={"trajectory": traj})
+               velocities0=v0.tolist(), timestep=timestep, steps=steps, k=k, krylov=krylov,
+               ref={"trajectory": traj})
     with open(os.path.join(HERE, f"{name}.json"), "w") as f:
         json.dump(rec, f)
     print(name, "Etot", [round(t["Etot"][0], 6) for t in traj])
@@ -405,6 +409,9 @@ def main():
     mols = [workloads.alkane(2, rng, 0.03), workloads.water_cluster(3, rng)]
     write_xlbomd("md_am1_xlbomd", *workloads.pad_batch(mols), {"method": "AM1", "scf_eps": 1e-8,
                  "scf_converger": [1]}, steps=10, timestep=0.5, seed=11, k=6)
+    write_xlbomd("md_pm3_ksa_xlbomd", *workloads.pad_batch(mols), {"method": "PM3", "scf_eps": 1e-8,
+                 "scf_converger": [1]}, steps=8, timestep=0.5, seed=12, k=6,
+                 krylov={"max_rank": 3, "err_threshold": 0.0, "T_el": 1500})
 
     rng = np.random.default_rng(4)
     mols = [workloads.alkane(8, rng, 0.05), workloads.water_cluster(4, rng)]

@@ -89,23 +89,26 @@ def test_md_trajectory_matches_reference(name):
         assert abs(iters[k] - ref[k]["loops"]) <= 1
 
 
-def test_xlbomd_trajectory_matches_reference():
-    """XL_BOMD (k = 6, no thermostat) on the GPU against the reference's XL_BOMD: 10 steps of
-    auxiliary-density propagation, one Fock build and one eigensolve per step, shadow-potential
-    forces from the adjoint kernel; positions and velocities to 1e-6, forces 1e-5 eV/A, shadow
-    energies 1e-6 eV, HOMO-LUMO gaps 1e-6 eV."""
+@pytest.mark.parametrize("name", ["md_am1_xlbomd", "md_pm3_ksa_xlbomd"])
+def test_xlbomd_trajectory_matches_reference(name):
+    """XL_BOMD (k = 6, no thermostat) and KSA_XL_BOMD (rank-3 Krylov kernel, Fermi-Dirac density at
+    1500 K) on the GPU against the reference's drivers: auxiliary-density propagation, one Fock
+    build and one eigensolve per step, shadow-potential forces from the adjoint kernel; positions
+    and velocities to 1e-6, forces 1e-5 eV/A, shadow energies and HOMO-LUMO gaps 1e-6 eV."""
     import torch
 
-    from pyseqm_gb300 import XL_BOMD, Constants, Molecule
+    from pyseqm_gb300 import KSA_XL_BOMD, XL_BOMD, Constants, Molecule
     from conftest import load_golden
 
-    g = load_golden("md_am1_xlbomd")
+    g = load_golden(name)
     s = dict(g["settings"])
     mol = Molecule(Constants().cuda(), s, torch.as_tensor(g["coords_np"], device="cuda"),
                    torch.as_tensor(g["species_np"], device="cuda")).cuda()
     mol.velocities = torch.as_tensor(np.asarray(g["velocities0"]), device="cuda")
-    md = XL_BOMD(xl_bomd_params={"k": g["k"]}, seqm_parameters=s, timestep=g["timestep"], Temp=0.0,
-                 output={"print every": 0}).cuda()
+    params = dict({"k": g["k"]}, **(g.get("krylov") or {}))
+    cls = KSA_XL_BOMD if g.get("krylov") else XL_BOMD
+    md = cls(xl_bomd_params=params, seqm_parameters=s, timestep=g["timestep"], Temp=0.0,
+             output={"print every": 0}).cuda()
     md.initialize(mol)
     ref = g["ref"]["trajectory"]
     solve0 = mol._solve
@@ -117,4 +120,6 @@ def test_xlbomd_trajectory_matches_reference():
         np.testing.assert_allclose(mol.force.cpu().numpy(), r["force"], atol=1e-5, rtol=0)
         np.testing.assert_allclose(mol.Etot.detach().cpu().numpy(), r["Etot"], atol=1e-6, rtol=0)
         np.testing.assert_allclose(mol.e_gap.detach().cpu().numpy().reshape(-1), r["e_gap"], atol=1e-6, rtol=0)
+        if i > 0 and "entropy" in r:
+            np.testing.assert_allclose(mol.Electronic_entropy.cpu().numpy().reshape(-1), r["entropy"], atol=1e-8)
     assert mol._solve is solve0  # the first step's solve continues on the device

@@ -153,3 +153,19 @@ def test_oracle_xlbomd_matches_reference_trajectory():
         np.testing.assert_allclose(traj[k]["velocities"], ref["velocities"], atol=1e-8, rtol=0)
         np.testing.assert_allclose(traj[k]["force"], ref["force"], atol=1e-6, rtol=0)
         np.testing.assert_allclose(traj[k]["Etot"], ref["Etot"], atol=1e-8, rtol=0)
+
+
+def test_oracle_ksa_xlbomd_matches_reference_trajectory():
+    """KSA-XL-BOMD (k = 6, rank 3, T_el 1500 K): Fermi-Dirac density, canonical density-matrix
+    perturbation response and the Krylov kernel of the oracle against the reference, 4 steps."""
+    from oracle import seqm_md as MD
+
+    g = load_golden("md_pm3_ksa_xlbomd")
+    s, kr = g["settings"], g["krylov"]
+    traj = MD.ksa_trajectory(s["method"], g["species_np"], g["coords_np"], np.asarray(g["velocities0"]), 4,
+                             g["timestep"], s["scf_eps"], g["k"], kr["T_el"], kr["max_rank"])
+    for k, ref in enumerate(g["ref"]["trajectory"][:5]):
+        np.testing.assert_allclose(traj[k]["coordinates"], ref["coordinates"], atol=1e-8, rtol=0)
+        np.testing.assert_allclose(traj[k]["velocities"], ref["velocities"], atol=1e-8, rtol=0)
+        np.testing.assert_allclose(traj[k]["force"], ref["force"], atol=1e-6, rtol=0)
+        np.testing.assert_allclose(traj[k]["Etot"], ref["Etot"], atol=1e-8, rtol=0)

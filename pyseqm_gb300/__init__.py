@@ -18,4 +18,4 @@ from .basics import (  # noqa: E402,F401
     Parser,
     SCFEnergyFunction,
 )
-from .dynamics import KSA_XL_BOMD, XL_BOMD, Molecular_Dynamics_Basic, Molecular_Dynamics_Langevin  # noqa: E402,F401
+from .dynamics import KSA_XL_BOMD, XL_BOMD, Geometry_Optimization_SD, Molecular_Dynamics_Basic, Molecular_Dynamics_Langevin  # noqa: E402,F401

@@ -123,3 +123,27 @@ def test_xlbomd_trajectory_matches_reference(name):
         if i > 0 and "entropy" in r:
             np.testing.assert_allclose(mol.Electronic_entropy.cpu().numpy().reshape(-1), r["entropy"], atol=1e-8)
     assert mol._solve is solve0  # the first step's solve continues on the device
+
+
+def test_steepest_descent_reduces_forces_and_energy():
+    """Geometry_Optimization_SD: from a perturbed water dimer and ethane, 40 steepest-descent steps
+    lower every molecule's energy and the largest force component; the SCF continues on the device
+    from step to step (one solve object)."""
+    import torch
+
+    from pyseqm_gb300 import Constants, Geometry_Optimization_SD, Molecule, workloads
+
+    rng = np.random.default_rng(21)
+    mols = [workloads.alkane(2, rng, 0.08), workloads.water_cluster(2, rng)]
+    sp, xyz = workloads.pad_batch(mols)
+    s = {"method": "AM1", "scf_eps": 1e-7, "scf_converger": [1]}
+    mol = Molecule(Constants().cuda(), s, torch.as_tensor(xyz, device="cuda"), torch.as_tensor(sp, device="cuda")).cuda()
+    opt = Geometry_Optimization_SD(s, alpha=0.01, force_tol=1e-9, max_evl=40).cuda()
+    f0, e0 = opt.onestep(mol)
+    f0, e0 = f0.abs().amax(dim=(1, 2)).clone(), e0.detach().clone()
+    solve = mol._solve
+    opt.run(mol, log=False)
+    f1 = mol.force.abs().amax(dim=(1, 2))
+    assert torch.all(mol.Etot.detach() < e0 - 1e-3)
+    assert torch.all(f1 < f0)
+    assert mol._solve is solve

@@ -40,6 +40,7 @@ extern "C" {
 #define SEQM_MNDO 0
 #define SEQM_AM1 1
 #define SEQM_PM3 2
+#define SEQM_PM6_SP 3 /* PM6 parameters on the sp basis (method "PM6_SP", seqm/basics.py:132-162) */
 
 /* per-atom parameter slots of seqm_batch.atom_par (structure of arrays, natoms each) */
 enum {
@@ -47,6 +48,7 @@ enum {
   SEQM_P_GPP, SEQM_P_GP2, SEQM_P_HSP, SEQM_P_ALPHA,
   SEQM_P_K1, SEQM_P_K2, SEQM_P_K3, SEQM_P_K4, SEQM_P_L1, SEQM_P_L2, SEQM_P_L3, SEQM_P_L4,
   SEQM_P_M1, SEQM_P_M2, SEQM_P_M3, SEQM_P_M4,
+  SEQM_P_RHOCORE, /* PM6_SP: core radius replacing rho0 in the core-core term when nonzero */
   /* derived by seqm_hcore: multipole separations and additive terms, valence charge, n */
   SEQM_P_DD, SEQM_P_QQ, SEQM_P_RHO0, SEQM_P_RHO1, SEQM_P_RHO2, SEQM_P_TORE, SEQM_P_QN,
   SEQM_NPAR
@@ -78,13 +80,24 @@ typedef struct seqm_batch {
   int32_t nclass, pad2_;
   int32_t class_end[SEQM_MAX_CLASSES];
   int32_t class_norb[SEQM_MAX_CLASSES];
+  /* PM6_SP diatomic core-core parameters (NULL for the other methods), (pair_zmax+1)^2 x 3
+   * doubles at [Z1*(pair_zmax+1) + Z2]: alp, chi and cbrt(atomic_num Z1) + cbrt(atomic_num Z2),
+   * Z1 the pair's first atom (parameters.py:49-87, energy.py:135-171) */
+  const double *pair_par;
+  int32_t pair_zmax, pad3_;
+  /* [nmol] atoms with 13 <= Z <= 17 per molecule (NULL: none).  The SCF convergence test divides
+   * ||dP||_F by 9 nSuperHeavy + 4 nHeavy + 4 nHydro (scf_loop.py:245, :501, :728), and the
+   * reference's parser counts these elements as super-heavy for every method (basics.py:258-270),
+   * on top of their count as heavy atoms. */
+  const int32_t *mol_nsuper;
 } seqm_batch;
 
 /* Integrals + core Hamiltonian.  Replaces hcore(molecule) (seqm/seqm_functions/hcore.py:9-179),
  * which calls two_elec_two_center_int (two_elec_two_center_int.py:98-283) and
  * diatom_overlap_matrix_PM6_SP (diat_overlap_PM6_SP.py:6-444).  Writes the derived
  * per-atom slots, w_xx/w_xh/w_hh, the full symmetric Hcore (H, dense per molecule) and
- * the core-core repulsion of every pair (enuc_pair, energy.py:91-134, needs w[0,0]). */
+ * the core-core repulsion of every pair (enuc_pair, energy.py:91-171: MNDO/AM1/PM3 from w[0,0],
+ * PM6_SP from the pair table; an element pair outside the table gives SEQM_E_ARG). */
 int seqm_hcore(const seqm_batch *b, double *w_xx, double *w_xh, double *w_hh, double *H, double *enuc_pair,
                void *stream);
 

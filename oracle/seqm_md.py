@@ -128,7 +128,7 @@ def xl_energy(method, species, coords, P, D=None):
     if D is None:
         D, _, _ = O.density_eigh(F, mol["nheavy"], mol["nhyd"], mol["nocc"])
     Eelec = np.sum(D * F - 0.5 * (F - H) * P, axis=(1, 2))
-    EnucAB = O.pair_nuclear_energy(method, mol, p, ints["w"][:, 0, 0], el)
+    EnucAB = O.pair_nuclear_energy(method, mol, p, ints["w"][:, 0, 0], el, ints["rho0"])
     Enuc = np.zeros(nmol)
     np.add.at(Enuc, mol["pair_molid"], EnucAB)
     Eiso = np.zeros(nmol)

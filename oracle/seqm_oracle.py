@@ -1,4 +1,4 @@
-"""NumPy restatement of PYSEQM's closed-shell MNDO/AM1/PM3 single-point SCF path.
+"""NumPy restatement of PYSEQM's MNDO/AM1/PM3/PM6_SP single-point SCF path.
 
 TEST INFRASTRUCTURE ONLY.  This module is the CPU oracle used by ``tests/``,
 ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py``.  Nothing in
@@ -56,6 +56,18 @@ def load_params(method):
     return d["fields"], np.asarray(d["rows"], dtype=np.float64)
 
 
+def load_pair_params(method, zmax):
+    """PM6 diatomic core-core parameters alp[Z1, Z2], chi[Z1, Z2] (parameters.py:49-87: the third
+    and fourth columns of PWCCT_<method>_MOPAC.csv, for the listed (Z1, Z2) order)."""
+    alp, chi = np.zeros((zmax + 1, zmax + 1)), np.zeros((zmax + 1, zmax + 1))
+    with open(os.path.join(_DATA, f"pwcct_{method}.json")) as f:
+        d = json.load(f)
+    for z1, z2, a, c in d["entries"]:
+        if z1 <= zmax and z2 <= zmax:
+            alp[z1, z2], chi[z1, z2] = a, c
+    return alp, chi
+
+
 # --------------------------------------------------------------------------- parser
 def parse(species, coords, charges=None, mult=None):
     """Pair list and counts; restates seqm/basics.py:219-403 (Parser.forward).
@@ -77,6 +89,9 @@ def parse(species, coords, charges=None, mult=None):
     Z = flat[real_atoms]
     nheavy = np.sum(species > 1, axis=1)
     nhyd = np.sum(species == 1, axis=1)
+    # super-heavy count (basics.py:258-270; of the sp elements, 13 <= Z <= 17), which only the
+    # SCF convergence test reads: ||dP||/(9 nSuperHeavy + 4 nHeavy + 4 nHydro), scf_loop.py:245
+    nsuper = np.sum((species >= 13) & (species <= 17), axis=1)
     n_charge = np.sum(el["tore"][species], axis=1).astype(np.int64)
     if charges is not None:
         n_charge = n_charge - np.asarray(charges, dtype=np.int64).reshape(-1)
@@ -107,7 +122,7 @@ def parse(species, coords, charges=None, mult=None):
     gi = m_p * molsize + i_p
     gj = m_p * molsize + j_p
     return dict(
-        nmol=nmol, molsize=molsize, Z=Z, nheavy=nheavy, nhyd=nhyd, nocc=nocc, maskd=maskd,
+        nmol=nmol, molsize=molsize, Z=Z, nheavy=nheavy, nhyd=nhyd, nsuper=nsuper, nocc=nocc, maskd=maskd,
         atom_molid=atom_molid, idxi=inv[gi], idxj=inv[gj], ni=Z[inv[gi]], nj=Z[inv[gj]],
         xij=d / dist[:, None], rij=dist / A0, mask=m_p * molsize**2 + i_p * molsize + j_p,
         pair_molid=m_p, species=species, coords=coords, uhf=mult is not None,
@@ -856,7 +871,7 @@ def scf(mol, p, ints, M, eps, converger=(1,), sp2_opt=(False,), P0=None, el=None
     Hsym = symmetrize_upper(blocks_to_full(M, nmol, ms))
     P = initial_density(mol, el) if P0 is None else np.array(P0, dtype=np.float64)
     nheavy, nhyd, nocc = mol["nheavy"], mol["nhyd"], mol["nocc"]
-    natoms4 = 4.0 * (nheavy + nhyd)
+    natoms4 = 9.0 * mol["nsuper"] + 4.0 * (nheavy + nhyd)
 
     def density(F, sel):
         if sp2_opt[0]:
@@ -918,7 +933,7 @@ def _scf_uhf(mol, p, ints, M, eps, converger, P0, el):
     else:
         P = np.array(P0, dtype=np.float64)
     nheavy, nhyd, nocc = mol["nheavy"], mol["nhyd"], mol["nocc"]
-    natoms4 = 4.0 * (nheavy + nhyd)
+    natoms4 = 9.0 * mol["nsuper"] + 4.0 * (nheavy + nhyd)
     F = fock_u(mol, p, ints, M, P)
     E = elec_energy(P, F, Hsym)
     Enew = np.zeros(nmol)
@@ -1043,8 +1058,49 @@ def _scf_diis(mol, p, ints, M, eps, P, F, E, Hsym, density, natoms4):
 
 
 # ------------------------------------------------------------------- energies
-def pair_nuclear_energy(method, mol, p, gam, el):
-    """Core-core repulsion per pair (energy.py:91-134, MNDO/AM1/PM3 branches)."""
+def _gaussians(p, mol, rija, tore, ng):
+    """Gaussian corrections Z_i Z_j / R (t5 + t6) (energy.py:128-131)."""
+    ni, nj, idxi, idxj = mol["ni"], mol["nj"], mol["idxi"], mol["idxj"]
+    K = np.stack([p[f"Gaussian{g}_K"] for g in range(1, ng + 1)], axis=1)
+    L = np.stack([p[f"Gaussian{g}_L"] for g in range(1, ng + 1)], axis=1)
+    Mm = np.stack([p[f"Gaussian{g}_M"] for g in range(1, ng + 1)], axis=1)
+    t4 = tore[ni] * tore[nj] / rija
+    t5 = np.sum(K[idxi] * np.exp(-L[idxi] * (rija[:, None] - Mm[idxi]) ** 2), axis=1)
+    t6 = np.sum(K[idxj] * np.exp(-L[idxj] * (rija[:, None] - Mm[idxj]) ** 2), axis=1)
+    return t4 * (t5 + t6)
+
+
+def pm6_nuclear_energy(method, mol, p, rho0, el):
+    """PM6 core-core repulsion per pair (energy.py:135-171): unpolarisable core
+    1e-8 ((Z_i^1/3 + Z_j^1/3)/R)^12, the diatomic alp/chi factor on Z_i Z_j ev/sqrt(r^2 +
+    (rho_i + rho_j)^2) with rho = rho_core where nonzero else rho0 (two_elec_two_center_int.py:
+    274-283), the C-H/N-H/O-H, C-C and Si-O exceptions, and the Gaussians."""
+    ni, nj, idxi, idxj = mol["ni"], mol["nj"], mol["idxi"], mol["idxj"]
+    r = mol["rij"]
+    rija = r * A0
+    tore = el["tore"]
+    an = el["atomic_num"]
+    alp_t, chi_t = load_pair_params(method, int(max(ni.max(initial=0), nj.max(initial=0))))
+    alp, chi = alp_t[ni, nj], chi_t[ni, nj]
+    rc = p["rho_core"]
+    rho = np.where(rc != 0.0, rc, rho0)
+    rsum = rho[idxi] + rho[idxj]
+    unpol = 1.0e-8 * ((an[ni] ** (1.0 / 3.0) + an[nj] ** (1.0 / 3.0)) / rija) ** 12
+    gcore = tore[ni] * tore[nj] * EV / np.sqrt(r * r + rsum**2)
+    xh = np.isin(ni, (6, 7, 8)) & (nj == 1)
+    arg = np.where(xh, rija**2, rija + 0.0003 * rija**6)
+    e = unpol + gcore * (1.0 + 2.0 * chi * np.exp(-alp * arg))
+    cc = (ni == 6) & (nj == 6)
+    e = e + np.where(cc, gcore * 9.28 * np.exp(-rija * 5.98), 0.0)
+    sio = (ni == 14) & (nj == 8)
+    e = e - np.where(sio, gcore * 0.0007 * np.exp(-((r - 2.9) ** 2)), 0.0)
+    return e + _gaussians(p, mol, rija, tore, 4)
+
+
+def pair_nuclear_energy(method, mol, p, gam, el, rho0=None):
+    """Core-core repulsion per pair (energy.py:91-171); PM6_SP needs the atoms' rho0."""
+    if method == "PM6_SP":
+        return pm6_nuclear_energy(method, mol, p, rho0, el)
     ni, nj, idxi, idxj = mol["ni"], mol["nj"], mol["idxi"], mol["idxj"]
     rija = mol["rij"] * A0
     tore = el["tore"]
@@ -1056,14 +1112,7 @@ def pair_nuclear_energy(method, mol, p, gam, el):
     t3 = np.exp(-alpha[idxj] * rija)
     e = t1 * (1.0 + t2 + t3)
     if method in ("AM1", "PM3"):
-        ng = 4 if method == "AM1" else 2
-        K = np.stack([p[f"Gaussian{g}_K"] for g in range(1, ng + 1)], axis=1)
-        L = np.stack([p[f"Gaussian{g}_L"] for g in range(1, ng + 1)], axis=1)
-        Mm = np.stack([p[f"Gaussian{g}_M"] for g in range(1, ng + 1)], axis=1)
-        t4 = tore[ni] * tore[nj] / rija
-        t5 = np.sum(K[idxi] * np.exp(-L[idxi] * (rija[:, None] - Mm[idxi]) ** 2), axis=1)
-        t6 = np.sum(K[idxj] * np.exp(-L[idxj] * (rija[:, None] - Mm[idxj]) ** 2), axis=1)
-        e = e + t4 * (t5 + t6)
+        e = e + _gaussians(p, mol, rija, tore, 4 if method == "AM1" else 2)
     return e
 
 
@@ -1083,7 +1132,7 @@ def energy_at(method, mol, p, P, el=None):
     Hsym = symmetrize_upper(blocks_to_full(M, nmol, ms))
     F = fock_u(mol, p, ints, M, P) if P.ndim == 4 else fock(mol, p, ints, M, P)
     Eelec = elec_energy(P, F, Hsym)
-    EnucAB = pair_nuclear_energy(method, mol, p, ints["w"][:, 0, 0], el)
+    EnucAB = pair_nuclear_energy(method, mol, p, ints["w"][:, 0, 0], el, ints["rho0"])
     Enuc = np.zeros(nmol)
     np.add.at(Enuc, mol["pair_molid"], EnucAB)
     Eiso = isolated_atom_energy(mol["Z"], p, el)

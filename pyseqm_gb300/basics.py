@@ -64,7 +64,7 @@ class Constants(torch.nn.Module):
 # --------------------------------------------------------------------- parser
 def _check_options(seqm_parameters):
     if seqm_parameters.get("method") not in tables.METHOD_FIELDS:
-        raise NotImplementedError(f"method {seqm_parameters.get('method')!r}: supported are MNDO, AM1, PM3")
+        raise NotImplementedError(f"method {seqm_parameters.get('method')!r}: supported are {tables.SUPPORTED}")
     if seqm_parameters.get("UHF", False):
         if seqm_parameters.get("sp2", [False])[0]:
             raise NotImplementedError("SP2 has no open-shell form (the reference's SP2.py raises for UHF)")
@@ -178,9 +178,17 @@ class Pack_Parameters(torch.nn.Module):
         fields, rows = tables.method_table(self.method)
         self.p = torch.nn.Parameter(torch.as_tensor(rows[:, [fields.index(f) for f in self.required_list]]),
                                     requires_grad=False)
+        # diatomic core-core parameters (PWCCT, parameters.py:49-87): entries of the listed
+        # elements, zero otherwise and for methods without them
         m = max(self.elements)
-        self.alpha = torch.nn.Parameter(torch.zeros(m + 1, m + 1, dtype=torch.float64), requires_grad=False)
-        self.chi = torch.nn.Parameter(torch.zeros(m + 1, m + 1, dtype=torch.float64), requires_grad=False)
+        alp, chi = np.zeros((m + 1, m + 1)), np.zeros((m + 1, m + 1))
+        t = tables.pair_table(self.method)
+        if t is not None:
+            el = [z for z in self.elements if z < t[0].shape[0]]
+            ix = np.ix_(el, el)
+            alp[ix], chi[ix] = t[0][ix], t[1][ix]
+        self.alpha = torch.nn.Parameter(torch.as_tensor(alp), requires_grad=False)
+        self.chi = torch.nn.Parameter(torch.as_tensor(chi), requires_grad=False)
 
     def forward(self, Z, learned_params=dict()):
         learned_params = dict(learned_params)

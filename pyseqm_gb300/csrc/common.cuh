@@ -24,6 +24,13 @@ __host__ __device__ constexpr int kind(int mu, int nu) {
   return mu >= nu ? (mu * (mu + 1)) / 2 + nu : (nu * (nu + 1)) / 2 + mu;
 }
 
+// divisor of ||dP||_F in the SCF convergence test: 4 per atom plus 9 per atom with 13 <= Z <= 17
+// (9 nSuperHeavy + 4 nHeavy + 4 nHydro, scf_loop.py:245)
+__device__ __forceinline__ double dm_norm(const seqm_batch &b, int m) {
+  const int nat = b.mol_atom_off[m + 1] - b.mol_atom_off[m];
+  return 4.0 * nat + (b.mol_nsuper ? 9.0 * b.mol_nsuper[m] : 0.0);
+}
+
 __device__ __forceinline__ double par(const seqm_batch &b, int slot, int atom) {
   return b.atom_par[(size_t)slot * b.natoms + atom];
 }

@@ -252,7 +252,7 @@ __device__ double block_max(double v, double *red) {
 
 // ------------------------------------------------------ energy + convergence test
 // Eelec = 1/2 sum P (H + F) (energy.py:26-49); get_error (scf_loop.py:106-147):
-// not converged <=> |dE| > eps or ||dP||_F/(4 natoms) > 2 eps or max|dP| > 15 eps,
+// not converged <=> |dE| > eps or ||dP||_F/(4 natoms + 9 nsuper) > 2 eps or max|dP| > 15 eps,
 // the density terms refreshed only when the energy test passes.
 //
 // One cluster of cs CTAs per molecule.  The molecule's elements are cut into ns
@@ -268,8 +268,7 @@ __device__ __forceinline__ void finish_error(const seqm_batch &b, int m, double 
   // with DIIS, also max |F P - P F| > 50 eps (scf_loop.py:130-132)
   bool bad = fabs(de) > eps || (diis_err != nullptr && diis_err[m] > 50.0 * eps);
   if (!bad) {
-    int nat = b.mol_atom_off[m + 1] - b.mol_atom_off[m];
-    dm_err[m] = sqrt(fro) / (4.0 * nat);
+    dm_err[m] = sqrt(fro) / dm_norm(b, m);
     dm_el[m] = mx;
   }
   bool nc = bad || dm_err[m] > eps * 2.0 || dm_el[m] > eps * 15.0;

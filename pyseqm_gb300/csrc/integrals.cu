@@ -218,6 +218,8 @@ extern "C" int seqm_hcore(const seqm_batch *bp, double *w_xx, double *w_xh, doub
                           double *enuc_pair, void *stream) {
   if (!bp) return SEQM_E_ARG;
   seqm_batch b = *bp;
+  if (b.method < SEQM_MNDO || b.method > SEQM_PM6_SP) return SEQM_E_ARG;
+  if (b.method == SEQM_PM6_SP && (!b.pair_par || b.pair_zmax < 0)) return SEQM_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   int npairs = b.nxx + b.nxh + b.nhh;
   if (b.natoms <= 0) return SEQM_OK;

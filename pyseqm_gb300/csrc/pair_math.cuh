@@ -388,9 +388,60 @@ __device__ bool overlap_block(int qni, int qnj, T r, T xv, T yv, T zv, double zs
   return true;
 }
 
-// core-core repulsion of one pair (energy.py:91-134); gam = (s_A s_A | s_B s_B)
+// sum of the Gaussian core-core corrections of atoms i and j times Z_i Z_j / R (energy.py:128-131)
+template <class T>
+__device__ T core_gauss(const seqm_batch &b, int ia, int ja, T rija, int ng, double ti, double tj) {
+  T t4 = ti * tj / rija, t5 = T(0.0), t6 = T(0.0);
+  for (int g = 0; g < ng; ++g) {
+    const double Ki = par(b, SEQM_P_K1 + g, ia), Li = par(b, SEQM_P_L1 + g, ia), Mi = par(b, SEQM_P_M1 + g, ia);
+    const double Kj = par(b, SEQM_P_K1 + g, ja), Lj = par(b, SEQM_P_L1 + g, ja), Mj = par(b, SEQM_P_M1 + g, ja);
+    t5 += Ki * exp(-Li * ((rija - Mi) * (rija - Mi)));
+    t6 += Kj * exp(-Lj * ((rija - Mj) * (rija - Mj)));
+  }
+  return t4 * (t5 + t6);
+}
+
+// PM6 core-core repulsion of one pair (energy.py:135-171): the unpolarisable-core term
+// 1e-8 ((Z_i^1/3 + Z_j^1/3) / R)^12, the diatomic factor 1 + 2 chi exp(-alp (R + 3e-4 R^6))
+// (exp(-alp R^2) for C-H, N-H, O-H) on Z_i Z_j gamma_core, where gamma_core takes each atom's
+// rho_core in place of rho0 when nonzero, the C-C and Si-O corrections and the Gaussians.
+// R in Angstrom, r in bohr (the Si-O term takes r, as the reference does).
+template <class T>
+__device__ T core_core_pm6(const seqm_batch &b, int ia, int ja, T r) {
+  const int Zi = b.atom_Z[ia], Zj = b.atom_Z[ja];
+  const double ti = par(b, SEQM_P_TORE, ia), tj = par(b, SEQM_P_TORE, ja);
+  double alp = 0.0, chi = 0.0, cz = 0.0;
+  if (b.pair_par && Zi >= 0 && Zj >= 0 && Zi <= b.pair_zmax && Zj <= b.pair_zmax) {
+    const double *q = b.pair_par + 3 * ((size_t)Zi * (b.pair_zmax + 1) + Zj);
+    alp = q[0];
+    chi = q[1];
+    cz = q[2];
+  }
+  const double rci = par(b, SEQM_P_RHOCORE, ia), rcj = par(b, SEQM_P_RHOCORE, ja);
+  const double r0 = (rci != 0.0 ? rci : par(b, SEQM_P_RHO0, ia)) + (rcj != 0.0 ? rcj : par(b, SEQM_P_RHO0, ja));
+  T rija = r * A0;
+  T u = cz / rija;
+  T u3 = u * u * u;
+  T unpol = 1.0e-8 * (u3 * u3) * (u3 * u3);
+  T gcore = (ti * tj * EV) / sqrt(r * r + r0 * r0);
+  const bool xh = (Zi == 6 || Zi == 7 || Zi == 8) && Zj == 1;
+  T arg;
+  if (xh) {
+    arg = rija * rija;
+  } else {
+    T r2 = rija * rija;
+    arg = rija + 0.0003 * (r2 * r2 * r2);
+  }
+  T e = unpol + gcore * (1.0 + (2.0 * chi) * exp(-alp * arg));
+  if (Zi == 6 && Zj == 6) e = e + gcore * (9.28 * exp(-5.98 * rija));
+  if (Zi == 14 && Zj == 8) e = e - gcore * (0.0007 * exp(-((r - 2.9) * (r - 2.9))));
+  return e + core_gauss<T>(b, ia, ja, rija, 4, ti, tj);
+}
+
+// core-core repulsion of one pair (energy.py:91-171); gam = (s_A s_A | s_B s_B)
 template <class T>
 __device__ T core_core(const seqm_batch &b, int ia, int ja, T r, T gam) {
+  if (b.method == SEQM_PM6_SP) return core_core_pm6<T>(b, ia, ja, r);
   const int Zi = b.atom_Z[ia], Zj = b.atom_Z[ja];
   T rija = r * A0;
   const double ti = par(b, SEQM_P_TORE, ia), tj = par(b, SEQM_P_TORE, ja);
@@ -400,16 +451,7 @@ __device__ T core_core(const seqm_batch &b, int ia, int ja, T r, T gam) {
   T t3 = exp(-par(b, SEQM_P_ALPHA, ja) * rija);
   T e = t1 * (1.0 + t2 + t3);
   const int ng = b.method == SEQM_AM1 ? 4 : (b.method == SEQM_PM3 ? 2 : 0);
-  if (ng) {
-    T t4 = ti * tj / rija, t5 = T(0.0), t6 = T(0.0);
-    for (int g = 0; g < ng; ++g) {
-      const double Ki = par(b, SEQM_P_K1 + g, ia), Li = par(b, SEQM_P_L1 + g, ia), Mi = par(b, SEQM_P_M1 + g, ia);
-      const double Kj = par(b, SEQM_P_K1 + g, ja), Lj = par(b, SEQM_P_L1 + g, ja), Mj = par(b, SEQM_P_M1 + g, ja);
-      t5 += Ki * exp(-Li * ((rija - Mi) * (rija - Mi)));
-      t6 += Kj * exp(-Lj * ((rija - Mj) * (rija - Mj)));
-    }
-    e = e + t4 * (t5 + t6);
-  }
+  if (ng) e = e + core_gauss<T>(b, ia, ja, rija, ng, ti, tj);
   return e;
 }
 

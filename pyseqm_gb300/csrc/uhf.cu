@@ -275,8 +275,7 @@ __global__ void __launch_bounds__(NT_U) k_energy_error_u(seqm_batch b, const dou
     err[m] = de;
     const bool bad = fabs(de) > eps;
     if (!bad) {
-      const int nat = b.mol_atom_off[m + 1] - b.mol_atom_off[m];
-      dm_err[m] = sqrt(fro) / (4.0 * nat);
+      dm_err[m] = sqrt(fro) / dm_norm(b, m);
       dm_el[m] = mx;
     }
     const bool nc = bad || dm_err[m] > eps * 2.0 || dm_el[m] > eps * 15.0;

@@ -58,6 +58,7 @@ def set_size_classes(struct, norb_sorted):
 class Layout:
     def __init__(self):
         self.dev = None
+        self.pair_par = None
 
     # ------------------------------------------------------------------ build
     @classmethod
@@ -72,7 +73,7 @@ class Layout:
             bad = np.nonzero(~np.all(species[:, :-1] >= species[:, 1:], axis=1))[0].tolist()
             raise ValueError(f"species must be non-increasing along each row, but rows {bad} are not sorted.")
         if method not in tables.METHOD_FIELDS:
-            raise ValueError(f"unsupported method {method!r}; supported: MNDO, AM1, PM3")
+            raise ValueError(f"unsupported method {method!r}; supported: {tables.SUPPORTED}")
         el = tables.elements()
         L = cls()
         L.method = method
@@ -82,6 +83,9 @@ class Layout:
         L.nheavy = (species > 1).sum(1).astype(np.int64)
         L.nhyd = (species == 1).sum(1).astype(np.int64)
         L.norb = 4 * L.nheavy + L.nhyd
+        # atoms the reference's parser also counts as super-heavy (basics.py:258-270); only its
+        # SCF convergence test reads them (scf_loop.py:245)
+        L.nsuper = ((species >= 13) & (species <= 17)).sum(1).astype(np.int64)
         nel = el["tore"][species].sum(1).astype(np.int64)
         if charges is not None:
             nel = nel - np.asarray(charges, dtype=np.float64).reshape(-1).astype(np.int64)
@@ -103,6 +107,10 @@ class Layout:
         L.Z = species.reshape(-1)[L.real_index]
         if np.any(el["qn"][L.Z] > 3) or np.any(L.Z == 2):
             raise ValueError("Error from diat.py, overlap matrix\nSome elements are not supported yet")
+        pp = tables.pair_par(method)
+        if pp is not None and np.any(L.Z > pp[1]):
+            raise ValueError(f"{method}: no diatomic core-core parameters for elements {sorted(set(L.Z[L.Z > pp[1]]))}")
+        L.pair_par = pp
         L.xyz = coords.reshape(-1, 3)[L.real_index]
         L.atom_mol = np.repeat(np.arange(L.nmol), L.natoms_m)
         L.mat_off = np.concatenate([[0], np.cumsum(L.norb * L.norb)]).astype(np.int64)
@@ -154,6 +162,10 @@ class Layout:
         }
         if self.uhf:
             d["nocc_a"], d["nocc_b"] = i32(self.nocc_a), i32(self.nocc_b)
+        if self.pair_par is not None:
+            d["pair_par"] = f64(self.pair_par[0])
+        if np.any(self.nsuper):
+            d["nsuper"] = i32(self.nsuper)
         self.dev = d
         self.device = torch.device(device)
         self._struct = native.SeqmBatch(
@@ -164,6 +176,9 @@ class Layout:
             mol_xh_off=d["xh_off"].data_ptr(), mol_hh_off=d["hh_off"].data_ptr(), mol_order=d["order"].data_ptr(),
             atom_Z=d["Z"].data_ptr(), atom_mol=d["atom_mol"].data_ptr(), atom_xyz=d["xyz"].data_ptr(),
             atom_par=d["par"].data_ptr(), pair_i=d["pair_i"].data_ptr(), pair_j=d["pair_j"].data_ptr(),
+            pair_par=d["pair_par"].data_ptr() if self.pair_par is not None else None,
+            pair_zmax=self.pair_par[1] if self.pair_par is not None else -1, pad3_=0,
+            mol_nsuper=d["nsuper"].data_ptr() if "nsuper" in d else None,
         )
         set_size_classes(self._struct, self.norb[self.order] if self.nmol else np.zeros(0, np.int64))
         return self

@@ -15,13 +15,13 @@ SEQM_E_ARG = -1
 SEQM_E_CUDA = -2
 SEQM_E_UNSUPPORTED = -3
 SEQM_E_TOO_LARGE = -4
-METHODS = {"MNDO": 0, "AM1": 1, "PM3": 2}
+METHODS = {"MNDO": 0, "AM1": 1, "PM3": 2, "PM6_SP": 3}
 
 # per-atom parameter slots (enum in the header)
 PAR_NAMES = ["U_ss", "U_pp", "zeta_s", "zeta_p", "beta_s", "beta_p", "g_ss", "g_sp", "g_pp", "g_p2", "h_sp", "alpha",
              "Gaussian1_K", "Gaussian2_K", "Gaussian3_K", "Gaussian4_K",
              "Gaussian1_L", "Gaussian2_L", "Gaussian3_L", "Gaussian4_L",
-             "Gaussian1_M", "Gaussian2_M", "Gaussian3_M", "Gaussian4_M",
+             "Gaussian1_M", "Gaussian2_M", "Gaussian3_M", "Gaussian4_M", "rho_core",
              "_dd", "_qq", "_rho0", "_rho1", "_rho2", "_tore", "_qn"]
 NPAR = len(PAR_NAMES)
 PAR = {n: i for i, n in enumerate(PAR_NAMES)}
@@ -48,6 +48,7 @@ class SeqmBatch(ctypes.Structure):
         ("atom_mol", _P), ("atom_xyz", _P), ("atom_par", _P), ("pair_i", _P), ("pair_j", _P),
         ("nclass", ctypes.c_int32), ("pad2_", ctypes.c_int32), ("class_end", ctypes.c_int32 * MAX_CLASSES),
         ("class_norb", ctypes.c_int32 * MAX_CLASSES),
+        ("pair_par", _P), ("pair_zmax", ctypes.c_int32), ("pad3_", ctypes.c_int32), ("mol_nsuper", _P),
     ]
 
 

@@ -333,6 +333,41 @@ def _ions():
     return [nh4, oh, h3o, h2o]
 
 
+def _sorted_mol(species, coords):
+    """Atoms ordered by descending Z (the order the API requires)."""
+    species = np.asarray(species)
+    order = np.argsort(-species, kind="stable")
+    return species[order], np.asarray(coords, dtype=np.float64)[order]
+
+
+def _hetero():
+    """Small molecules with Si, S, Cl, F and N: H3SiOH (the Si-O core-core exception), CH3SH,
+    CH3Cl, CH3F, CH3NH2 and NH2OH; idealised bond lengths and angles."""
+    tet = np.radians(109.47)
+
+    def fan(center, bond, theta, phis):
+        ph = np.radians(np.asarray(phis, dtype=float))
+        return np.asarray(center) + bond * np.c_[np.sin(theta) * np.cos(ph), np.sin(theta) * np.sin(ph),
+                                                 np.full(ph.size, np.cos(theta))]
+
+    def ch3x(z, d):
+        return _sorted_mol([6, z, 1, 1, 1], np.vstack([[0.0, 0.0, 0.0], [0.0, 0.0, d], fan([0, 0, 0], 1.09, tet,
+                                                                                           [0, 120, 240])]))
+    silanol = _sorted_mol([14, 8, 1, 1, 1, 1], np.vstack([
+        [0.0, 0.0, 0.0], [0.0, 0.0, 1.64], fan([0, 0, 0], 1.48, tet, [0, 120, 240]),
+        fan([0, 0, 1.64], 0.96, np.radians(60.0), [60])]))
+    thiol = _sorted_mol([16, 6, 1, 1, 1, 1], np.vstack([
+        [0.0, 0.0, 1.815], [0.0, 0.0, 0.0], fan([0, 0, 0], 1.09, tet, [60, 180, 300]),
+        fan([0, 0, 1.815], 1.335, np.radians(84.0), [0])]))
+    amine = _sorted_mol([7, 6, 1, 1, 1, 1, 1], np.vstack([
+        [0.0, 0.0, 1.47], [0.0, 0.0, 0.0], fan([0, 0, 0], 1.09, tet, [60, 180, 300]),
+        fan([0, 0, 1.47], 1.01, np.radians(70.5), [0, 120])]))
+    hydroxylamine = _sorted_mol([8, 7, 1, 1, 1], np.vstack([
+        [0.0, 0.0, 0.0], [0.0, 0.0, 1.45], fan([0, 0, 0], 0.96, np.radians(105.0), [0]),
+        fan([0, 0, 1.45], 1.01, np.radians(70.5), [120, 240])]))
+    return [silanol, thiol, ch3x(17, 1.78), ch3x(9, 1.39), amine, hydroxylamine]
+
+
 def main():
     data = os.path.join(REF, "tests", "data")
     sp_m, c_m = read_xyz([os.path.join(data, "methane.xyz")])
@@ -381,6 +416,18 @@ def main():
           charges=[1, -1, 1, 0])
     write("ions_pm3", *workloads.pad_batch(_ions()), {"method": "PM3", "scf_eps": 1e-8, "scf_converger": [1]},
           charges=[1, -1, 1, 0])
+
+    # PM6 parameters on the sp basis (method PM6_SP): alkanes and water clusters (C-C, C-H, O-H
+    # core-core exceptions), ions (N-H), and molecules with Si (Si-O), S, Cl, F, N; the
+    # hetero-atom set also under AM1 and PM3
+    mols = workloads.mixed_batch(8, seed=2, alkane_range=(1, 6), water_range=(2, 6))
+    write("mixed_pm6sp", *workloads.pad_batch(mols), {"method": "PM6_SP", "scf_eps": 1e-8, "scf_converger": [1]},
+          per_molecule=True, with_stages=True)
+    write("ions_pm6sp", *workloads.pad_batch(_ions()), {"method": "PM6_SP", "scf_eps": 1e-8,
+                                                        "scf_converger": [1]}, charges=[1, -1, 1, 0])
+    for method in ("PM6_SP", "AM1", "PM3"):
+        write(f"hetero_{method.lower().replace('_', '')}", *workloads.pad_batch(_hetero()),
+              {"method": method, "scf_eps": 1e-8, "scf_converger": [1]}, per_molecule=True)
 
     # excited states: CIS on a ragged batch, CIS and RPA on a batch of one species
     rng = np.random.default_rng(8)

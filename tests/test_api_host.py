@@ -84,6 +84,38 @@ def test_unsupported_element_raises():
         Layout.from_padded(np.array([[35, 1]]), np.array([[[0, 0, 0], [1.4, 0, 0.0]]]), "AM1")
 
 
+def test_pm6_pair_table_and_super_heavy_count():
+    """The PM6_SP diatomic table the kernels read: (alp, chi, cbrt Z1 + cbrt Z2) at [Z1, Z2] as the
+    oracle reads PWCCT; Pack_Parameters returns the same alp/chi for the listed elements; the
+    convergence-test count of 13 <= Z <= 17 atoms per molecule."""
+    from pyseqm_gb300 import tables
+    from pyseqm_gb300.basics import Pack_Parameters
+    from pyseqm_gb300.layout import Layout
+
+    flat, zmax = tables.pair_par("PM6_SP")
+    tab = flat.reshape(zmax + 1, zmax + 1, 3)
+    alp, chi = O.load_pair_params("PM6_SP", zmax)
+    np.testing.assert_array_equal(tab[..., 0], alp)
+    np.testing.assert_array_equal(tab[..., 1], chi)
+    an = O.load_elements()["atomic_num"]
+    assert tab[6, 1, 2] == pytest.approx(6.0 ** (1 / 3) + 1.0)
+    assert tab[10, 1, 2] == pytest.approx(an[10] ** (1 / 3) + 1.0)  # the reference's atomic_num[10] is 0
+    assert alp[6, 1] > 0 and alp[1, 6] == 0  # the listed (heavier, lighter) order only
+    assert tables.pair_par("AM1") is None
+    pp = Pack_Parameters({"elements": [0, 1, 6, 8], "method": "PM6_SP"})
+    _, a, c = pp(torch.tensor([8, 6, 1]))
+    assert a.shape == (9, 9)
+    assert float(a[8, 1]) == alp[8, 1] and float(c[6, 6]) == chi[6, 6] and float(a[7, 1]) == 0.0
+    sp = np.array([[17, 14, 8, 6, 1, 1, 1], [8, 1, 1, 0, 0, 0, 0]])
+    xyz = np.random.default_rng(0).normal(size=sp.shape + (3,)) * 2.0
+    L = Layout.from_padded(sp, xyz, "PM6_SP")
+    assert L.nsuper.tolist() == [2, 0]
+    assert L.pair_par[1] == zmax
+    with pytest.raises(NotImplementedError):
+        from pyseqm_gb300.basics import _check_options
+        _check_options({"method": "PM6"})
+
+
 def test_workload_generators_are_seeded_and_sorted():
     from pyseqm_gb300 import workloads
 

@@ -20,11 +20,15 @@ def _molecule(g, settings=None, learned=None):
     const = Constants().cuda()
     species = torch.as_tensor(g["species_np"], dtype=torch.int64, device="cuda")
     coords = torch.as_tensor(g["coords_np"], dtype=torch.float64, device="cuda")
-    return Molecule(const, s, coords, species).cuda(), s
+    kw = {}
+    if "charges" in g:
+        kw["charges"] = torch.as_tensor(g["charges"], dtype=torch.float64, device="cuda")
+    return Molecule(const, s, coords, species, **kw).cuda(), s
 
 
 @pytest.mark.parametrize("name", ["smoke_MNDO", "smoke_AM1", "smoke_PM3", "batch_am1", "force_methanal_am1",
-                                  "force_mixed_am1"])
+                                  "force_mixed_am1", "mixed_pm6sp", "ions_pm6sp", "hetero_pm6sp", "hetero_am1",
+                                  "hetero_pm3"])
 def test_electronic_structure_matches_reference(name):
     from pyseqm_gb300 import Electronic_Structure
 

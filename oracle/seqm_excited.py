@@ -51,6 +51,32 @@ def g_transition(mol, p, ints, P):
     return Gs + O.blocks_to_full(Ga, nmol, ms)
 
 
+def transition_properties(mol, p, el, C, nocc, E, X, Y=None):
+    """Transition dipoles (au) and oscillator strengths of the roots of one molecule
+    (calc_transition_dipoles, rcis_batch.py:679-710): R = C_occ X C_virt^T (+ C_virt Y^T C_occ^T
+    for RPA), the one-centre dipole integrals of calc_dipole_matrix (dipole.py:7-82: -R_A on
+    each AO of atom A, -dd_A in Angstrom between s and p_d of heavy atoms), mu = sqrt(2)/a0 sum
+    R.D, f = 2/3 (E / 27.2113962) |mu|^2."""
+    nh, ny = int(mol["nheavy"][0]), int(mol["nhyd"][0])
+    n = 4 * nh + ny
+    dd = O.multipole_params(mol["Z"], p, el)[0] * O.A0
+    xyz = np.asarray(mol["coords"][0], dtype=np.float64)[: nh + ny]
+    D = np.zeros((3, n, n))
+    for a in range(nh):
+        o = 4 * a
+        for d in range(3):
+            D[d, o: o + 4, o: o + 4] -= np.eye(4) * xyz[a, d]
+            D[d, o, o + 1 + d] = D[d, o + 1 + d, o] = -dd[a]
+    for h in range(ny):
+        D[:, 4 * nh + h, 4 * nh + h] = -xyz[nh + h]
+    Co, Cv = C[:, :nocc], C[:, nocc:n]
+    R = np.einsum("mi,ria,na->rmn", Co, X, Cv)
+    if Y is not None:
+        R = R + np.einsum("ma,ria,ni->rmn", Cv, Y, Co)
+    mu = np.einsum("rmn,dmn->rd", R, D) * np.sqrt(2.0) / O.A0
+    return mu, 2.0 / 3.0 * np.asarray(E) / 27.2113962 * np.sum(mu * mu, axis=1)
+
+
 def ab_matrices(method, species, coords, eps, converger=(1,), with_b=False):
     """Per molecule of the batch: orbital energies, C, nocc and the CIS matrix A (and B), each
     molecule run alone (its SCF, integrals and orbitals)."""
@@ -83,7 +109,8 @@ def ab_matrices(method, species, coords, eps, converger=(1,), with_b=False):
             A[col, col] += ev[nocc + a] - ev[i]
             if with_b:
                 B[:, col] = 2.0 * (Co.T @ G.T @ Cv).reshape(-1)
-        res.append(dict(A=A, B=B, e=ev, nocc=nocc, nvirt=nv, Etot=out["Etot"][0], C=C))
+        res.append(dict(A=A, B=B, e=ev, nocc=nocc, nvirt=nv, Etot=out["Etot"][0], C=C, mol=mol, params=p,
+                        el=el))
     return res
 
 
@@ -93,8 +120,10 @@ def cis(method, species, coords, eps, nroots, converger=(1,)):
     for r in ab_matrices(method, species, coords, eps, converger):
         w, v = np.linalg.eigh(r["A"])
         amp = v[:, :nroots].T.reshape(nroots, r["nocc"], r["nvirt"])
+        mu, f = transition_properties(r["mol"], r["params"], r["el"], r["C"], r["nocc"], w[:nroots], amp)
         out.append(dict(energies=w[:nroots], amplitudes=amp, nocc=r["nocc"], nvirt=r["nvirt"],
-                        transition_density=transition_density(r["C"], r["nocc"], amp)))
+                        transition_density=transition_density(r["C"], r["nocc"], amp),
+                        transition_dipole=mu, oscillator_strength=f))
     return out
 
 
@@ -114,7 +143,9 @@ def rpa(method, species, coords, eps, nroots, converger=(1,)):
         X, Y = X / nrm, Y / nrm
         shape = (nroots, r["nocc"], r["nvirt"])
         Xs, Ys = X.T.reshape(shape), Y.T.reshape(shape)
+        mu, f = transition_properties(r["mol"], r["params"], r["el"], r["C"], r["nocc"], w, Xs, Ys)
         out.append(dict(energies=w, X=Xs, Y=Ys, nocc=r["nocc"], nvirt=r["nvirt"],
+                        transition_dipole=mu, oscillator_strength=f,
                         transition_density=transition_density(r["C"], r["nocc"], Xs),
                         transition_density_y=transition_density(r["C"], r["nocc"], Ys)))
     return out

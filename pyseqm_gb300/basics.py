@@ -236,7 +236,8 @@ class Molecule(torch.nn.Module):
         self.mass_inverse = torch.zeros_like(self.mass)
         self.mass_inverse[non_zero] = 1.0 / self.mass[non_zero]
         for name in ("force", "velocities", "acc", "dm", "q", "w", "Hf", "Etot", "Eelec", "Enuc", "Eiso", "e_mo",
-                     "e_gap", "molecular_orbitals", "charge", "dipole", "analytical_gradient", "cis_amplitudes"):
+                     "e_gap", "molecular_orbitals", "charge", "dipole", "analytical_gradient", "cis_amplitudes",
+                     "transition_dipole", "oscillator_strength"):
             setattr(self, name, None)
         self.verbose = True
         self.active_state = seqm_parameters.get("active_state", 0)
@@ -565,6 +566,13 @@ class Energy(torch.nn.Module):
         dev = molecule.coordinates.device
         molecule.cis_energies = E.to(dev)
         molecule.cis_amplitudes = amp.to(dev)
+        # transition dipoles and oscillator strengths (rcis_analysis, rcis_batch.py:650-676;
+        # the reference computes them when the molecule is verbose, its default, or has an
+        # active excited state)
+        with torch.no_grad():
+            mu, f = ex.transition_properties(E, amp, rpa=es["method"] == "rpa")
+        molecule.transition_dipole = mu.to(dev)
+        molecule.oscillator_strength = f.to(dev)
         molecule._excited = ex
         if molecule.const.do_timing:
             torch.cuda.synchronize()

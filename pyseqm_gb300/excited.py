@@ -27,6 +27,8 @@ import torch
 from . import native
 
 INERT = 1.0e6  # diagonal of the subspace matrix at padding slots: never among the lowest roots
+A0_ANGSTROM = 0.529167  # bohr radius (seqm/seqm_functions/constants.py:9)
+HARTREE_NEXMD = 27.2113962  # eV per hartree of the oscillator strength (rcis_batch.py:705)
 
 
 class ExcitedStates:
@@ -129,6 +131,7 @@ class ExcitedStates:
         subspace (cnt[m] orthonormal vectors, no holes); the padding slots past cnt[m] are inert."""
         nmol, dev = self.nmol, self.dE.device
         k, order = self._targets(nroots)
+        self.roots = k
         kmax = int(k.max())
         k_t = torch.as_tensor(k, device=dev)
         nov_np = self.nov.cpu().numpy()
@@ -251,6 +254,63 @@ class ExcitedStates:
                     break
         self.converged = done.cpu().numpy()
         return E, amp
+
+    # ------------------------------------------------------- transition properties
+    def _dipole_geometry(self):
+        """Per AO of the packed basis (padded to nmax): the owning atom's position (Angstrom), and
+        per heavy atom the flat (s, p_d) / (p_d, s) positions of its one-centre dipole integrals
+        with dd (Angstrom); padding entries carry zero weight."""
+        L = self.L
+        nmax, nmol = self.nmax, self.nmol
+        nhmax = max(1, int(L.nheavy.max()))
+        ao_atom = np.full((nmol, nmax), -1, dtype=np.int64)
+        sp_a = np.zeros((nmol, nhmax, 3), dtype=np.int64)
+        sp_b = np.zeros((nmol, nhmax, 3), dtype=np.int64)
+        heavy = np.full((nmol, nhmax), -1, dtype=np.int64)
+        d3 = np.arange(3)
+        for m in range(nmol):
+            a0, nh, ny = int(L.atom_off[m]), int(L.nheavy[m]), int(L.nhyd[m])
+            ao_atom[m, : 4 * nh] = a0 + np.repeat(np.arange(nh), 4)
+            ao_atom[m, 4 * nh: 4 * nh + ny] = a0 + nh + np.arange(ny)
+            o = 4 * np.arange(nh)
+            sp_a[m, :nh] = o[:, None] * nmax + o[:, None] + 1 + d3[None, :]
+            sp_b[m, :nh] = (o[:, None] + 1 + d3[None, :]) * nmax + o[:, None]
+            heavy[m, :nh] = a0 + np.arange(nh)
+        dev = self.dE.device
+        xyz = torch.as_tensor(L.xyz, dtype=torch.float64, device=dev)
+        par = L.dev["par"].view(native.NPAR, -1)
+        dd = par[native.PAR["_dd"]] * A0_ANGSTROM  # bohr -> Angstrom (dipole.py:40-41)
+        at = torch.as_tensor(ao_atom, device=dev)
+        hv = torch.as_tensor(heavy, device=dev)
+        return dict(ao_xyz=torch.where(at[..., None] >= 0, xyz[at.clamp(min=0)], 0.0),
+                    sp_a=torch.as_tensor(sp_a.reshape(nmol, -1), device=dev),
+                    sp_b=torch.as_tensor(sp_b.reshape(nmol, -1), device=dev),
+                    dd=torch.where(hv >= 0, dd[hv.clamp(min=0)], 0.0))
+
+    def transition_properties(self, E, amp, rpa=False):
+        """Transition dipoles (atomic units, (nmol, kmax, 3)) and oscillator strengths (nmol, kmax)
+        of the roots, as calc_transition_dipoles (rcis_batch.py:679-710, rcis_new.py:547-585):
+        the transition density R = C_occ X C_virt^T (+ C_virt Y^T C_occ^T for RPA) against the
+        one-centre dipole integrals of calc_dipole_matrix (dipole.py:7-82: -R_A on the diagonal of
+        atom A's AOs, -dd_A between its s and p_d), mu = sqrt(2)/a0 sum R.D and
+        f = 2/3 (E / 27.2113962) |mu|^2; zero for the padding roots of a molecule."""
+        g = self._dipole_geometry()
+        nmol = self.nmol
+        X = amp[0] if rpa else amp
+        k = X.shape[1]
+        R = self.Co[:, None] @ X.view(nmol, k, self.no, self.nv) @ self.Cv.transpose(1, 2)[:, None]
+        if rpa:
+            Y = amp[1].view(nmol, k, self.no, self.nv)
+            R = R + self.Cv[:, None] @ Y.transpose(2, 3) @ self.Co.transpose(1, 2)[:, None]
+        mu = -torch.einsum("bkn,bnd->bkd", torch.diagonal(R, dim1=2, dim2=3), g["ao_xyz"])
+        Rf = R.reshape(nmol, k, -1)
+        sp = Rf.gather(2, g["sp_a"][:, None, :].expand(-1, k, -1)) + Rf.gather(2, g["sp_b"][:, None, :].expand(-1, k, -1))
+        mu = mu - torch.einsum("bkhd,bh->bkd", sp.view(nmol, k, -1, 3), g["dd"])
+        mu = mu * (math.sqrt(2.0) / A0_ANGSTROM)
+        ok = (torch.arange(k, device=E.device)[None, :] < torch.as_tensor(self.roots, device=E.device)[:, None])
+        mu = mu * ok[..., None]
+        f = (2.0 / 3.0) * E / HARTREE_NEXMD * (mu * mu).sum(-1) * ok
+        return mu, f
 
     @staticmethod
     def _store(E, amp, w, Xa, Ya, mask):

@@ -246,13 +246,48 @@ def write_excited(name, species, coords, settings):
             X = a[m].reshape(a.shape[1], no_max, nv_max)[:, :no, :n - no]
             per.append(np.einsum("mi,ria,na->rmn", C[m, :n, :no], X, C[m, :n, no:n]).tolist())
         tdm.append(per)
+    # transition dipoles and oscillator strengths by the reference's own functions
+    # (rcis_batch.py:679-710 for a batch of one species and RPA, rcis_new.py:547-585 otherwise)
+    from seqm.seqm_functions.dipole import calc_dipole_matrix
+    from seqm.seqm_functions.rcis_batch import calc_transition_dipoles
+    from seqm.seqm_functions.rcis_new import calc_transition_dipoles_any_batch
+
+    E = mol.cis_energies.detach()
+    amp_t = mol.cis_amplitudes.detach()
+    rpa = amps.ndim == 4
+    amp_arg = (amp_t[0], amp_t[1]) if rpa else amp_t
+    with torch.no_grad():
+        if len(set(map(int, norb))) == 1 and len(set(map(int, nocc))) == 1:
+            mu, f = calc_transition_dipoles(mol, amp_arg, E, E.shape[1], calc_dipole_matrix(mol), rpa)
+        else:
+            mu, f = calc_transition_dipoles_any_batch(mol, amp_arg, E, torch.full((species.shape[0],), E.shape[1]),
+                                                      calc_dipole_matrix(mol), rpa)
     rec = dict(name=name, settings=settings, species=species.tolist(), coords=coords.tolist(),
                ref=dict(Etot=mol.Etot.detach().numpy().tolist(), cis_energies=mol.cis_energies.numpy().tolist(),
+                        transition_dipole=mu.numpy().tolist(), oscillator_strength=f.numpy().tolist(),
                         cis_amplitudes=amps.tolist(), transition_densities=tdm,
                         e=mol.e_mo.detach().numpy().tolist(), nocc=nocc.tolist(), norb=norb.tolist()))
     with open(os.path.join(HERE, f"{name}.json"), "w") as f:
         json.dump(rec, f)
     print(name, "excitation energies", np.round(mol.cis_energies.numpy(), 4).tolist())
+
+
+def write_reference_excited(name, xyz_names, settings, ref_json):
+    """Inputs and values of one of the reference's own excited-state tests
+    (tests/unit/test_excited_states.py): the molecules of its xyz files, its settings and its
+    committed tests/reference/<ref_json>.json (excitation energies, oscillator strengths)."""
+    if ONLY and name not in ONLY:
+        return
+    data = os.path.join(REF, "tests", "data")
+    species, coords = read_xyz([os.path.join(data, x) for x in xyz_names])
+    with open(os.path.join(REF, "tests", "reference", ref_json)) as f:
+        rj = json.load(f)
+    rec = dict(name=name, settings=settings, species=np.asarray(species).tolist(),
+               coords=np.asarray(coords, dtype=np.float64).tolist(),
+               reference_test_json={k: rj[k] for k in ("cis_energies", "oscillator_strength")})
+    with open(os.path.join(HERE, f"{name}.json"), "w") as f:
+        json.dump(rec, f)
+    print(name, "reference energies", rj["cis_energies"])
 
 
 def write_xlbomd(name, species, coords, settings, steps, timestep, seed, k, krylov=None):
@@ -442,6 +477,23 @@ def main():
         write_excited(f"{es}_{method.lower()}_same", *workloads.pad_batch(same),
                       {"method": method, "scf_eps": 1e-8, "scf_converger": [1],
                        "excited_states": {"method": es, "n_states": 5, "tolerance": 1e-7}})
+
+    # the reference's own excited-state known answers (its tests run with active_state 1 for the
+    # excited-state forces, which do not change the energies and oscillator strengths compared here)
+    for method in ("cis", "rpa"):
+        write_reference_excited(f"cis_ref_{method}_am1_methane", ["methane.xyz"],
+                                {"method": "AM1", "scf_eps": 1e-7, "scf_converger": [1],
+                                 "excited_states": {"n_states": 4, "method": method}},
+                                f"excited_{method}_am1_methane.json")
+    for method, ref_json in (("cis", "cis_batch_same_molecule_coords.json"),
+                             ("rpa", "rpa_batch_same_molecule_coords.json")):
+        write_reference_excited(f"cis_ref_{method}_am1_methanal", [f"methanal.{i}.xyz" for i in (1, 2, 3)],
+                                {"method": "AM1", "scf_eps": 1e-7, "scf_converger": [1],
+                                 "excited_states": {"n_states": 4, "method": method}}, ref_json)
+    write_reference_excited("cis_ref_cis_am1_mixed", ["methanal.1.xyz", "methane.xyz", "benzene.xyz"],
+                            {"method": "AM1", "scf_eps": 1e-7, "scf_converger": [1],
+                             "excited_states": {"n_states": 4, "method": "cis"}},
+                            "cis_batch_different_molecules.json")
 
     # molecular dynamics: velocity Verlet and Temp 0 Langevin (friction only) from seeded velocities
     rng = np.random.default_rng(5)

@@ -1,6 +1,7 @@
 """CIS / RPA excited states on the GPU (needs a GB300): the general-density two-electron
-contraction against the oracle, and excitation energies and transition densities through the
-seqm API against the reference's Davidson solvers."""
+contraction against the oracle; excitation energies, transition densities, transition dipoles
+and oscillator strengths through the seqm API against the reference's Davidson solvers and its
+own committed test values."""
 
 import numpy as np
 import pytest
@@ -86,3 +87,26 @@ def test_excited_states_match_reference(name):
             if signs is None:
                 signs = np.sign((Tm * Tr).sum((1, 2)))[:, None, None]
             np.testing.assert_allclose(signs * Tm, Tr, atol=1e-5, rtol=0)
+    # transition dipoles (atomic units, one sign per state) and oscillator strengths
+    np.testing.assert_allclose(mol.oscillator_strength.cpu().numpy(), ref["oscillator_strength"], atol=1e-6, rtol=0)
+    np.testing.assert_allclose(np.abs(mol.transition_dipole.cpu().numpy()), np.abs(np.asarray(ref["transition_dipole"])),
+                               atol=1e-5, rtol=0)
+
+
+@pytest.mark.parametrize("name", ["cis_ref_cis_am1_methane", "cis_ref_rpa_am1_methane", "cis_ref_cis_am1_methanal",
+                                  "cis_ref_rpa_am1_methanal", "cis_ref_cis_am1_mixed"])
+def test_excited_states_match_reference_test_values(name):
+    """The seqm API on the inputs of the reference's own excited-state tests
+    (test_excited_states.py) against its committed energies and oscillator strengths, at that
+    test's tolerance (rtol = atol = 1e-5)."""
+    from pyseqm_gb300 import Constants, Electronic_Structure, Molecule
+
+    g = load_golden(name)
+    s = dict(g["settings"])
+    s["excited_states"] = dict(s["excited_states"])
+    mol = Molecule(Constants().cuda(), s, torch.as_tensor(g["coords_np"], device="cuda"),
+                   torch.as_tensor(g["species_np"], device="cuda")).cuda()
+    Electronic_Structure(s).cuda()(mol)
+    rj = g["reference_test_json"]
+    np.testing.assert_allclose(mol.cis_energies.cpu().numpy(), rj["cis_energies"], atol=1e-5, rtol=1e-5)
+    np.testing.assert_allclose(mol.oscillator_strength.cpu().numpy(), rj["oscillator_strength"], atol=1e-5, rtol=1e-5)

@@ -137,6 +137,32 @@ def test_oracle_excited_states_match_reference(name):
             sg = np.sign((Tr * o["transition_density"] if key == "transition_density" else
                           np.asarray(T[0][m]) * o["transition_density"]).sum((1, 2)))[:, None, None]
             np.testing.assert_allclose(sg * o[key], Tr, atol=1e-6, rtol=0)
+    # transition dipoles (one sign per state, as the amplitudes) and oscillator strengths
+    k = len(out[0]["energies"])
+    np.testing.assert_allclose([o["oscillator_strength"] for o in out],
+                               np.asarray(g["ref"]["oscillator_strength"])[:, :k], atol=1e-8, rtol=0)
+    for m, o in enumerate(out):
+        np.testing.assert_allclose(np.abs(o["transition_dipole"]),
+                                   np.abs(np.asarray(g["ref"]["transition_dipole"][m])[:k]), atol=1e-7, rtol=0)
+
+
+@pytest.mark.parametrize("name", ["cis_ref_cis_am1_methane", "cis_ref_rpa_am1_methane", "cis_ref_cis_am1_methanal",
+                                  "cis_ref_rpa_am1_methanal", "cis_ref_cis_am1_mixed"])
+def test_oracle_excited_states_match_reference_test_values(name):
+    """The oracle against the reference's own committed excited-state values
+    (tests/reference/*.json of its test_excited_states.py): energies and oscillator strengths at
+    that test's tolerance (rtol = atol = 1e-5)."""
+    from oracle import seqm_excited as X
+
+    g = load_golden(name)
+    s = g["settings"]
+    es = s["excited_states"]
+    f = X.rpa if es["method"] == "rpa" else X.cis
+    out = f(s["method"], g["species_np"], g["coords_np"], s["scf_eps"], es["n_states"])
+    rj = g["reference_test_json"]
+    np.testing.assert_allclose([o["energies"] for o in out], rj["cis_energies"], atol=1e-5, rtol=1e-5)
+    np.testing.assert_allclose([o["oscillator_strength"] for o in out], rj["oscillator_strength"], atol=1e-5,
+                               rtol=1e-5)
 
 
 def test_oracle_xlbomd_matches_reference_trajectory():

@@ -290,6 +290,26 @@ def write_reference_excited(name, xyz_names, settings, ref_json):
     print(name, "reference energies", rj["cis_energies"])
 
 
+def write_reference_md(name, xyz_names, driver, kwargs, steps, ref_json, tol):
+    """Inputs, driver settings and committed values of one of the reference's own MD tests
+    (tests/unit/test_md_suite.py: seed 0, Temp 300 K, timestep 0.5 fs, AM1, scf_eps 1e-7):
+    per molecule the total energy per step, the drift and slope bounds it asserts."""
+    if ONLY and name not in ONLY:
+        return
+    data = os.path.join(REF, "tests", "data")
+    species, coords = read_xyz([os.path.join(data, x) for x in xyz_names])
+    rec = dict(name=name, driver=driver, kwargs=kwargs, steps=steps, tol=tol,
+               settings={"method": "AM1", "scf_eps": 1.0e-7, "scf_converger": [1]},
+               species=np.asarray(species).tolist(), coords=np.asarray(coords, dtype=np.float64).tolist())
+    if ref_json:
+        with open(os.path.join(REF, "tests", "reference", ref_json)) as f:
+            rj = json.load(f)
+        rec["reference_test_json"] = rj if isinstance(rj, list) else [rj]
+    with open(os.path.join(HERE, f"{name}.json"), "w") as f:
+        json.dump(rec, f)
+    print(name, "written")
+
+
 def write_xlbomd(name, species, coords, settings, steps, timestep, seed, k, krylov=None):
     """A short XL-BOMD trajectory (no thermostat, no Krylov kernel) through the reference's XL_BOMD
     driver: the first step's SCF, then the auxiliary density propagated with the k-th order
@@ -494,6 +514,27 @@ def main():
                             {"method": "AM1", "scf_eps": 1e-7, "scf_converger": [1],
                              "excited_states": {"n_states": 4, "method": "cis"}},
                             "cis_batch_different_molecules.json")
+
+    # the reference's own MD suite: its inputs, drivers and committed energies (test_md_suite.py)
+    methane, mixed = ["methane.xyz"], ["methane.xyz", "benzene.xyz"]
+    basic_tol, xl_tol = {"drift": 1e-2, "slope": 1e-3}, {"drift": 5e-2, "slope": 5e-3}
+    ksa = {"max_rank": 3, "err_threshold": 0.0, "T_el": 1500}
+    for name, xyz, driver, kw, steps, ref_json, tol in (
+            ("md_ref_basic_methane", methane, "basic", {}, 30, "md_basic_methane.json", basic_tol),
+            ("md_ref_basic_mixed", mixed, "basic", {}, 30, "md_basic_batch_mixed.json", basic_tol),
+            ("md_ref_langevin_methane", methane, "langevin", {"damp": 10.0}, 50, None, None),
+            ("md_ref_langevin_mixed", mixed, "langevin", {"damp": 10.0}, 50, None, None),
+            ("md_ref_xl_bomd_methane", methane, "xl_bomd", {"xl_bomd_params": {"k": 6}}, 30,
+             "md_xl_bomd_methane.json", xl_tol),
+            ("md_ref_xl_bomd_methane_k4", methane, "xl_bomd", {"xl_bomd_params": {"k": 4}}, 30,
+             "md_xl_bomd_methane_k4.json", xl_tol),
+            ("md_ref_ksa_xl_bomd_methane", methane, "ksa_xl_bomd", {"xl_bomd_params": dict(ksa, k=6)}, 30,
+             "md_ksa_xl_bomd_methane.json", xl_tol),
+            ("md_ref_ksa_xl_bomd_methane_k4", methane, "ksa_xl_bomd", {"xl_bomd_params": dict(ksa, k=4)}, 30,
+             "md_ksa_xl_bomd_methane_k4.json", xl_tol),
+            ("md_ref_ksa_xl_bomd_mixed", mixed, "ksa_xl_bomd", {"xl_bomd_params": dict(ksa, k=6)}, 30,
+             "md_ksa_xl_bomd_batch_mixed.json", xl_tol)):
+        write_reference_md(name, xyz, driver, kw, steps, ref_json, tol)
 
     # molecular dynamics: velocity Verlet and Temp 0 Langevin (friction only) from seeded velocities
     rng = np.random.default_rng(5)

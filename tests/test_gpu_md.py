@@ -147,3 +147,64 @@ def test_steepest_descent_reduces_forces_and_energy():
     assert torch.all(mol.Etot.detach() < e0 - 1e-3)
     assert torch.all(f1 < f0)
     assert mol._solve is solve
+
+
+REFERENCE_MD = ["md_ref_basic_methane", "md_ref_basic_mixed", "md_ref_langevin_methane", "md_ref_langevin_mixed",
+                "md_ref_xl_bomd_methane", "md_ref_xl_bomd_methane_k4", "md_ref_ksa_xl_bomd_methane",
+                "md_ref_ksa_xl_bomd_methane_k4", "md_ref_ksa_xl_bomd_mixed"]
+
+
+@pytest.mark.parametrize("name", REFERENCE_MD)
+def test_md_passes_reference_md_suite(name):
+    """The reference's own MD suite (test_md_suite.py) on this implementation: its inputs,
+    drivers, seed and settings, and its assertions, which allow for trajectories from another
+    random stream: per step total energy within rtol = atol = 1e-2 of its committed values,
+    non-negative kinetic energy, the energy drift and the slope of a linear fit below its bounds;
+    Langevin runs within its 10-1500 K temperature envelope."""
+    import torch
+
+    from conftest import load_golden
+    from pyseqm_gb300 import KSA_XL_BOMD, XL_BOMD, Constants, Molecular_Dynamics_Basic, Molecular_Dynamics_Langevin
+    from pyseqm_gb300 import Molecule
+
+    g = load_golden(name)
+    s = dict(g["settings"])
+    species = torch.as_tensor(g["species_np"], dtype=torch.int64, device="cuda")
+    coords = torch.as_tensor(g["coords_np"], dtype=torch.float64, device="cuda")
+    mol = Molecule(Constants().cuda(), s, coords, species).cuda()
+    cls = {"basic": Molecular_Dynamics_Basic, "langevin": Molecular_Dynamics_Langevin, "xl_bomd": XL_BOMD,
+           "ksa_xl_bomd": KSA_XL_BOMD}[g["driver"]]
+    kw = dict(g["kwargs"])
+    if g["driver"] in ("xl_bomd", "ksa_xl_bomd"):
+        kw["damp"] = None
+    md = cls(seqm_parameters=s, timestep=0.5, Temp=300.0, output={"molid": [], "print every": 0}, **kw).cuda()
+    rec = []
+    init = md.initialize
+
+    def initialize(molecule, *a, **k):
+        out = init(molecule, *a, **k)
+        with torch.no_grad():
+            Ek = md._kinetic_energy(molecule)
+            rec.append((md._calc_temperature(Ek).cpu().numpy(), Ek.cpu().numpy(),
+                        md._thermo_potential(molecule).detach().cpu().numpy()))
+        return out
+
+    md.initialize = initialize
+    md._output_to_screen = lambda i, T, Ek, V: rec.append((T.cpu().numpy(), Ek.cpu().numpy(),
+                                                           V.detach().cpu().numpy()))
+    md.print_every, md.molid = 1, [0]
+    md.run(mol, steps=int(g["steps"]), reuse_P=True, remove_com=None, seed=0)
+    assert len(rec) == int(g["steps"]) + 1
+    T = np.stack([r[0] for r in rec])
+    Ek = np.stack([r[1] for r in rec])
+    Etot = Ek + np.stack([r[2] for r in rec])
+    assert np.isfinite(Etot).all() and Ek.min() >= 0.0
+    if g["driver"] == "langevin":
+        assert T.min() >= 10.0 and T.max() <= 1500.0
+        return
+    tol = g["tol"]
+    for m, ref in enumerate(g["reference_test_json"]):
+        np.testing.assert_allclose(Etot[:, m], ref["Etot"], rtol=1e-2, atol=1e-2)
+        drift = np.max(np.abs(Etot[:, m] - Etot[0, m]))
+        slope = float(np.polyfit(np.arange(len(Etot)), Etot[:, m], 1)[0])
+        assert drift <= tol["drift"] and abs(slope) <= tol["slope"], (m, drift, slope)

@@ -429,6 +429,13 @@ def main():
     for method in ("MNDO", "AM1", "PM3"):
         write(f"smoke_{method}", sp_m, c_m, {"method": method, "scf_eps": 1e-6, "scf_converger": [1]},
               ref_json=f"smoke_single_point_{method}.json", with_stages=(method == "AM1"))
+    write("force_methane_am1", sp_m, c_m, {"method": "AM1", "scf_eps": 1e-7, "scf_converger": [1]},
+          ref_json="ground_force_methane.json")
+    # the reference's UHF known answer: planar CH3 doublet (test_uhf.py:11-57)
+    write("uhf_ch3_ref_am1", np.array([[6, 1, 1, 1]]),
+          np.array([[[0.0, 0.0, 0.0], [1.1, 0.0, 0.0], [-0.5, 0.9, 0.0], [-0.5, -0.9, 0.0]]]),
+          {"method": "AM1", "scf_eps": 1e-6, "scf_converger": [1], "UHF": True}, mult=[2],
+          ref_json="uhf_ch3_am1.json")
     sp_b, c_b = read_xyz([os.path.join(data, "methane.xyz"), os.path.join(data, "benzene.xyz")])
     write("batch_am1", sp_b, c_b, {"method": "AM1", "scf_eps": 1e-6, "scf_converger": [1]},
           ref_json="batch_single_point_am1.json")

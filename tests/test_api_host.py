@@ -42,9 +42,11 @@ def test_rejects_unsorted_species_and_odd_electrons():
     with pytest.raises(ValueError, match="non-increasing"):
         Molecule(Constants(), {"method": "AM1", "scf_eps": 1e-6, "scf_converger": [1]},
                  torch.zeros(1, 2, 3, dtype=torch.float64), torch.tensor([[1, 6]]))
-    with pytest.raises(ValueError, match="closed shell"):
+    with pytest.raises(ValueError) as exc:
         Molecule(Constants(), {"method": "AM1", "scf_eps": 1e-6, "scf_converger": [1]},
                  torch.rand(1, 4, 3, dtype=torch.float64), torch.tensor([[6, 1, 1, 1]]))
+    # the reference's committed message (tests/reference/rhf_odd_electron_error.json)
+    assert str(exc.value) == "RHF setting requires closed shell systems (even number of electrons)"
 
 
 @pytest.mark.parametrize("opt", [{"UHF": True, "scf_converger": [2]}, {"UHF": True, "sp2": [True, 1e-5]},

@@ -26,8 +26,26 @@ def _molecule(g, settings=None, learned=None):
     return Molecule(const, s, coords, species, **kw).cuda(), s
 
 
+@pytest.mark.parametrize("name", ["force_methane_am1", "force_methanal_am1", "force_mixed_am1"])
+@pytest.mark.parametrize("mode", [{}, {"analytical_gradient": [True]}, {"analytical_gradient": [True, "numerical"]}])
+def test_force_modes_match_reference_test_values(name, mode):
+    """The reference's force-method suite (test_force_methods.py): autograd, analytical and
+    semi-numerical gradient settings all give the forces of its committed values (1e-5)."""
+    from pyseqm_gb300 import Electronic_Structure
+
+    g = load_golden(name)
+    s = dict(g["settings"], **mode)
+    mol, s = _molecule(g, s)
+    Electronic_Structure(s).cuda()(mol)
+    rj = g["reference_test_json"]
+    np.testing.assert_allclose(mol.force.cpu().numpy(), np.asarray(rj["force"]), atol=1e-5, rtol=1e-5)
+    if mode:
+        np.testing.assert_allclose(mol.analytical_gradient.cpu().numpy(), -np.asarray(rj["force"]), atol=1e-5,
+                                   rtol=1e-5)
+
+
 @pytest.mark.parametrize("name", ["smoke_MNDO", "smoke_AM1", "smoke_PM3", "batch_am1", "force_methanal_am1",
-                                  "force_mixed_am1", "mixed_pm6sp", "ions_pm6sp", "hetero_pm6sp", "hetero_am1",
+                                  "force_mixed_am1", "force_methane_am1", "mixed_pm6sp", "ions_pm6sp", "hetero_pm6sp", "hetero_am1",
                                   "hetero_pm3"])
 def test_electronic_structure_matches_reference(name):
     from pyseqm_gb300 import Electronic_Structure

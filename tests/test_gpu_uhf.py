@@ -94,3 +94,19 @@ def test_uhf_singlet_equals_rhf():
     np.testing.assert_allclose(u["Etot"].cpu().numpy(), r["Etot"].cpu().numpy(), atol=1e-7, rtol=0)
     np.testing.assert_allclose((u["solver"].P + u["solver"].Pb).cpu().numpy(), r["solver"].P.cpu().numpy(),
                                atol=1e-7, rtol=0)
+
+
+def test_uhf_ch3_matches_reference_test_value():
+    """The reference's UHF known answer (test_uhf.py: planar CH3 doublet, AM1): Etot to its 1e-5
+    and the spin-resolved density shape (nmol, 2, 4 molsize, 4 molsize)."""
+    from pyseqm_gb300 import Constants, Electronic_Structure, Molecule
+
+    g = load_golden("uhf_ch3_ref_am1")
+    s = dict(g["settings"])
+    mol = Molecule(Constants().cuda(), s, torch.as_tensor(g["coords_np"], device="cuda"),
+                   torch.as_tensor(g["species_np"], device="cuda"),
+                   mult=torch.as_tensor(g["mult"], device="cuda")).cuda()
+    Electronic_Structure(s).cuda()(mol)
+    rj = g["reference_test_json"]
+    np.testing.assert_allclose(float(mol.Etot.item()), rj["Etot"], atol=1e-5, rtol=1e-5)
+    assert list(mol.dm.shape) == rj["dm_shape"]

@@ -235,6 +235,18 @@ int seqm_pair_sum(const seqm_batch *b, const double *pair_val, double *mol_sum, 
 int seqm_energy_grad(const seqm_batch *b, const double *P, const double *Pbeta, const double *gE, const double *gN,
                      double *dR, double *dpar, double *work, void *stream);
 
+/* Gradient of a CIS / RPA excited-state energy (ground state included).  Replaces
+ * rcis_grad_batch(..., include_ground_state=True) (seqm/seqm_functions/rcis_grad_batch.py:10-259):
+ * the ground-state terms of seqm_energy_grad for the closed-shell density P, plus the relaxed
+ * difference density D (symmetric: the unrelaxed difference density and the Z-vector
+ * response, make_cis_densities rcis_batch.py:971-1059) in the Coulomb, core-attraction,
+ * exchange and resonance terms, and the transition density R (C_occ X C_virt^T, + C_virt Y^T
+ * C_occ^T for RPA) in its Coulomb (symmetric part) and exchange (symmetric and antisymmetric
+ * parts) terms.  All three are ragged dense per-molecule matrices; gE, gN, dR, work as
+ * seqm_energy_grad (no parameter gradients). */
+int seqm_energy_grad_excited(const seqm_batch *b, const double *P, const double *D, const double *R,
+                             const double *gE, const double *gN, double *dR, double *work, void *stream);
+
 /* Unrestricted Fock matrices (fock_u_batch, seqm/seqm_functions/fock_u_batch.py:18-100):
  * Fa, Fb of the spin densities Pa, Pb (Coulomb of Pa + Pb, exchange of the spin density,
  * spin-resolved one-centre terms), for active molecules. */

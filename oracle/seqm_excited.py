@@ -154,3 +154,45 @@ def rpa(method, species, coords, eps, nroots, converger=(1,)):
 def transition_density(C, nocc, amplitudes):
     """C_occ X C_virt^T per state in the packed AO basis (independent of the orbitals' signs)."""
     return np.einsum("mi,ria,na->rmn", C[:, :nocc], amplitudes, C[:, nocc:])
+
+
+def state_energy(method, species, coords, eps, state, rpa=False):
+    """Total energy of one molecule in excited state `state` (1-based): the ground-state Etot
+    plus the state's CIS (or RPA) excitation energy (basics.py:1044-1060 adds it to Etot)."""
+    r = ab_matrices(method, species, coords, eps, with_b=rpa)[0]
+    A = r["A"]
+    if rpa:
+        B = r["B"]
+        wm, um = np.linalg.eigh(A - B)
+        sq = (um * np.sqrt(wm)) @ um.T
+        w = np.sqrt(np.linalg.eigvalsh(sq @ (A + B) @ sq))
+    else:
+        w = np.linalg.eigvalsh(A)
+    return r["Etot"] + w[state - 1]
+
+
+def excited_forces_fd(method, species, coords, eps, state, rpa=False, h=1.0e-4):
+    """Forces -dE/dR (eV/Angstrom) of excited state `state` of each molecule by central
+    differences of state_energy with steps h and h/2, Richardson-extrapolated (error O(h^4);
+    some components have third derivatives large enough that a plain central difference at
+    h = 1e-4 A is off by 1e-5): the oracle for the relaxed (Z-vector) analytic gradient of
+    rcis_grad_batch (rcis_grad_batch.py:10-259).  Each molecule is run alone."""
+    species = np.asarray(species)
+    coords = np.asarray(coords, dtype=np.float64)
+    f = np.zeros_like(coords)
+
+    def central(sp, xyz, a, x, step):
+        e = []
+        for sgn in (1.0, -1.0):
+            c = xyz.copy()
+            c[0, a, x] += sgn * step
+            e.append(state_energy(method, sp, c, eps, state, rpa))
+        return -(e[0] - e[1]) / (2.0 * step)
+
+    for m in range(species.shape[0]):
+        na = int(np.sum(species[m] > 0))
+        sp, xyz = species[m:m + 1, :na], coords[m:m + 1, :na]
+        for a in range(na):
+            for x in range(3):
+                f[m, a, x] = (4.0 * central(sp, xyz, a, x, 0.5 * h) - central(sp, xyz, a, x, h)) / 3.0
+    return f

@@ -15,8 +15,9 @@ Supported: MNDO/AM1/PM3, closed shell (scf_converger [0, alpha], [1] and [2] (DI
 and unrestricted open shell (``UHF``: True with the Molecule's ``mult``; scf_converger
 [0, alpha] and [1], as the reference has neither open-shell DIIS nor SP2), learned
 parameters (values for any parameter; gradients for U_ss, U_pp, beta_s, beta_p), and the
-ground state's CIS / RPA excited states (``excited_states``: excitation energies and
-amplitudes).  PM6, excited-state forces (active_state > 0), scf_backward >= 1 and a finite
+ground state's CIS / RPA excited states (``excited_states``: excitation energies, amplitudes,
+transition dipoles, oscillator strengths; with active_state > 0 the state's energy and relaxed
+forces).  PM6 with d orbitals, scf_backward >= 1 and a finite
 pair_outer_cutoff raise NotImplementedError.
 """
 
@@ -86,8 +87,6 @@ def _check_options(seqm_parameters):
             raise NotImplementedError("an orbital_window for excited states is not supported")
         if not seqm_parameters.get("eig", True):
             raise NotImplementedError("excited states need the orbitals (eig=True)")
-    if seqm_parameters.get("active_state", 0):
-        raise NotImplementedError("excited-state forces and dynamics (active_state > 0) are not supported")
     if seqm_parameters.get("scf_backward", 0) != 0:
         raise NotImplementedError("scf_backward >= 1 (backpropagation through the SCF) is not supported")
     if seqm_parameters.get("pair_outer_cutoff", 1e10) < 1e10:
@@ -354,6 +353,26 @@ class _Solve:
                                           native.ptr(work), self.s._s()), "seqm_energy_grad")
         return dR[: 3 * L.natoms].view(L.natoms, 3), dpar[: 4 * L.natoms].view(4, L.natoms)
 
+    def grad_excited(self, gE, D, R):
+        """d(excitation energy)/dR per real atom for the molecules weighted by gE: the excited-state
+        gradient of D (relaxed difference density) and R (transition density), both ragged, minus
+        the ground-state terms of the same weights (rcis_grad_batch.py:10-259)."""
+        L = self.L
+        n3 = 3 * max(1, L.natoms)
+        dR = torch.empty(n3, dtype=torch.float64, device=self.dev)
+        dR0 = torch.empty(n3, dtype=torch.float64, device=self.dev)
+        work = torch.empty(7 * max(1, L.npairs), dtype=torch.float64, device=self.dev)
+        gN = torch.zeros_like(gE)
+        lib = native.load()
+        self.s.launches += 4
+        gE = gE.contiguous()
+        native.check(lib.seqm_energy_grad_excited(L.struct, native.ptr(self.s.P), native.ptr(D), native.ptr(R),
+                                                  native.ptr(gE), native.ptr(gN), native.ptr(dR), native.ptr(work),
+                                                  self.s._s()), "seqm_energy_grad_excited")
+        native.check(lib.seqm_energy_grad(L.struct, native.ptr(self.s.P), None, native.ptr(gE), native.ptr(gN),
+                                          native.ptr(dR0), None, native.ptr(work), self.s._s()), "seqm_energy_grad")
+        return (dR - dR0)[: 3 * L.natoms].view(L.natoms, 3)
+
     # ------------------------------------------------------- padded outputs
     def padded(self, flat, flat_b=None):
         """Padded (nmol, N, N) matrices; with a beta-spin array, (nmol, 2, N, N) as the reference's
@@ -424,6 +443,37 @@ class SCFEnergyFunction(torch.autograd.Function):
         gN = torch.zeros(nm, dtype=torch.float64, device=solve.dev) if gN is None else gN.to(solve.dev, torch.float64)
         dR, dpar = solve.grad(gE, gN)
         return dR, dpar[0], dpar[1], dpar[2], dpar[3], None
+
+
+class ExcitedEnergyFunction(torch.autograd.Function):
+    """(coordinates of real atoms) -> excitation energy of each molecule's active state (0 for
+    molecules in the ground state).  backward: the relaxed excited-state gradient (Z-vector
+    response, rcis_grad_batch.py:10-259) minus the ground-state part, which SCFEnergyFunction
+    carries."""
+
+    @staticmethod
+    def forward(ctx, xyz, solve, ex, X, Y, E_state, mask, tol):
+        ctx.args = (solve, ex, X, Y, mask, tol)
+        return E_state.clone()
+
+    @staticmethod
+    def backward(ctx, gE):
+        solve, ex, X, Y, mask, tol = ctx.args
+        gE = (gE.to(solve.dev, torch.float64) * mask).contiguous()
+        with torch.no_grad():
+            R, _, D = ex.state_densities(X, Y, tol)
+            dR = solve.grad_excited(gE, ex.to_ragged(D), ex.to_ragged(R))
+        return dR, None, None, None, None, None, None, None
+
+
+def _active_states(molecule, nmol, device):
+    """Active state per molecule (0 ground, k > 0 the k-th excited state): an int or a tensor
+    (active_state_tensor, dynamics/active_state.py:4-15)."""
+    a = molecule.active_state
+    if torch.is_tensor(a):
+        t = a.to(device).long()
+        return t.expand(nmol) if t.dim() == 0 else t
+    return torch.full((nmol,), int(a or 0), dtype=torch.long, device=device)
 
 
 def _isolated_atom_energy(const, Z, p):
@@ -578,6 +628,30 @@ class Energy(torch.nn.Module):
             torch.cuda.synchronize()
             molecule.const.timing["CIS/RPA"].append(time.time() - t0)
 
+    def _active_energy(self, molecule, solve, act, xyz):
+        """Excitation energy of each molecule's active state as a differentiable function of the
+        coordinates (its gradient from ExcitedEnergyFunction)."""
+        ex = molecule._excited
+        rpa = self.excited_states["method"] == "rpa"
+        E = molecule.cis_energies.to(solve.dev)
+        k = E.shape[1]
+        if bool((act > k).any()) or bool((act < 0).any()):
+            raise ValueError(f"active_state must be between 0 and the number of excited states ({k})")
+        exc = (act > 0).to(solve.dev)
+        idx = (act.to(solve.dev) - 1).clamp(min=0)
+        amp = molecule.cis_amplitudes.to(solve.dev)
+        rows = torch.arange(E.shape[0], device=solve.dev)
+        if rpa:
+            X, Y = amp[0, rows, idx], amp[1, rows, idx]
+        else:
+            X, Y = amp[rows, idx], None
+        X = X * exc[:, None]
+        Y = Y * exc[:, None] if Y is not None else None
+        E_state = E[rows, idx] * exc
+        tol = float(self.excited_states["tolerance"])
+        return ExcitedEnergyFunction.apply(xyz, solve, ex, X, Y, E_state, exc.double(), tol).to(
+            molecule.coordinates.device)
+
     @staticmethod
     def _refresh_geometry(molecule):
         with torch.no_grad():
@@ -652,8 +726,16 @@ class Energy(torch.nn.Module):
         molecule._solve = s
         if self.excited_states:
             self._excited(molecule, s)
+        act = _active_states(molecule, L.nmol, dev)
+        Eexc = None
+        if bool((act > 0).any()):
+            # excited-state energy and forces of the active state (basics.py:1044-1105)
+            if not self.excited_states:
+                raise Exception("You have requested for excited state dynamics but have not given input parameters "
+                                "for excited states (like n_states) in seqm_parameters")
+            Eexc = self._active_energy(molecule, s, act, xyz)
         if all_terms:
-            Etot = Eelec + Enuc
+            Etot = Eelec + Enuc if Eexc is None else Eelec + Enuc + Eexc
             Eiso = _isolated_atom_energy(molecule.const, molecule.Z, p)
             Eiso_sum = torch.zeros_like(Etot).index_add(0, molecule.atom_molid, Eiso)
             if self.Hf_flag:
@@ -717,6 +799,8 @@ def _xl_bomd_force(molecule, P, seqm_parameters, xl_params=None):
     krylov = "max_rank" in xl_params
     if P is None:
         raise ValueError("XL-BOMD needs the auxiliary density P0")
+    if bool((_active_states(molecule, int(molecule.species.shape[0]), P.device) > 0).any()):
+        raise NotImplementedError("excited-state XL-BOMD (XL-ESMD) is not supported")
     if seqm_parameters.get("UHF", False):
         raise NotImplementedError("XL-BOMD is implemented for closed shells")
     sv = getattr(molecule, "_solve", None)

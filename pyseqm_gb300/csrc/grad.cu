@@ -50,11 +50,48 @@ __device__ __forceinline__ double exch(const double Pab[4][4], int a, int c) {
   return s;
 }
 
+// weighted packed symmetric part Rs = (R + R^T)/2 of one atom's diagonal block of a general
+// matrix: Rs_rr, and 2 Rs_rc = R_rc + R_cr off the diagonal
+__device__ __forceinline__ void grad_packed_sym(const double *Rm, int norb, int o, bool heavy, double *PX) {
+#pragma unroll
+  for (int k = 0; k < 10; ++k) PX[k] = 0.0;
+  if (heavy) {
+#pragma unroll
+    for (int k = 0; k < 10; ++k) {
+      int r = k10_row(k), c = k10_col(k);
+      PX[k] = r == c ? Rm[(size_t)(o + r) * norb + o + c]
+                     : Rm[(size_t)(o + r) * norb + o + c] + Rm[(size_t)(o + c) * norb + o + r];
+    }
+  } else {
+    PX[0] = Rm[(size_t)o * norb + o];
+  }
+}
+
+// the same ordered contraction for two different blocks: sum X[mu][nu] Y[lam][sig]
+__device__ __forceinline__ double exch2(const double X[4][4], const double Y[4][4], int a, int c) {
+  const int ra = k10_row(a), ca = k10_col(a), rc = k10_row(c), cc = k10_col(c);
+  double s = X[ra][rc] * Y[ca][cc];
+  if (rc != cc) s += X[ra][cc] * Y[ca][rc];
+  if (ra != ca) {
+    s += X[ca][rc] * Y[ra][cc];
+    if (rc != cc) s += X[ca][cc] * Y[ra][rc];
+  }
+  return s;
+}
+
 constexpr int GRAD_STRIDE = 7;  // per pair: dE/d(Rj-Ri) x3, d beta_s(i), d beta_p(i), d beta_s(j), d beta_p(j)
 
+// EXC: gradient of a CIS / RPA excited state (rcis_grad_batch, rcis_grad_batch.py:10-259,
+// include_ground_state): on top of the ground-state terms of P, the relaxed difference density
+// D (Dd, symmetric) enters the Coulomb, core-attraction, exchange and resonance terms linearly
+// (D_A P_B + P_A D_B, -Z D, -exch(D, P), D (beta + beta) S), and the transition density R (Rt)
+// quadratically: 4 Rs_A Rs_B - 2 exch(Rs) - 2 exch(Ra) with Rs, Ra its symmetric and
+// antisymmetric parts.  Restricted densities only.
+template <bool EXC>
 __global__ void __launch_bounds__(128) k_pair_grad(seqm_batch b, const double *__restrict__ P,
                                                    const double *__restrict__ Pbeta, const double *__restrict__ gE,
-                                                   const double *__restrict__ gN, double *__restrict__ work) {
+                                                   const double *__restrict__ gN, double *__restrict__ work,
+                                                   const double *__restrict__ Dd, const double *__restrict__ Rt) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const int npairs = b.nxx + b.nxh + b.nhh;
   if (p >= npairs) return;
@@ -95,10 +132,40 @@ __global__ void __launch_bounds__(128) k_pair_grad(seqm_batch b, const double *_
       Pb_ab[u][v] = (in && Qm) ? Qm[ix] : 0.0;
       Pab[u][v] = Pa_ab[u][v] + Pb_ab[u][v];
     }
+  double DA[10], DB[10], SA[10], SB[10], Dab[4][4], Sab[4][4], Tab[4][4];
+  if (EXC) {
+    const double *Dm = Dd + b.mol_mat_off[m], *Rm = Rt + b.mol_mat_off[m];
+    grad_packed(Dm, norb, oi, hi, DA);
+    grad_packed(Dm, norb, oj, hj, DB);
+    grad_packed_sym(Rm, norb, oi, hi, SA);
+    grad_packed_sym(Rm, norb, oj, hj, SB);
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const bool in = u < ni_ && v < nj_;
+        const double x = in ? Rm[(size_t)(oi + u) * norb + oj + v] : 0.0;
+        const double y = in ? Rm[(size_t)(oj + v) * norb + oi + u] : 0.0;
+        Dab[u][v] = in ? Dm[(size_t)(oi + u) * norb + oj + v] : 0.0;
+        Sab[u][v] = 0.5 * (x + y);
+        Tab[u][v] = 0.5 * (x - y);
+      }
+  }
+  // Coulomb factor of D_ab (P_A[a] P_B[b], plus the excited-state terms)
+  auto coul = [&](int a, int c) {
+    double s = PA[a] * PB[c];
+    if (EXC) s += DA[a] * PB[c] + PA[a] * DB[c] + 4.0 * SA[a] * SB[c];
+    return s;
+  };
   // exchange part of D: 1/2 exch(P) restricted, exch(Pa) + exch(Pb) unrestricted
   auto xch = [&](int a, int c) {
-    return Qm ? exch(Pa_ab, a, c) + exch(Pb_ab, a, c) : 0.5 * exch(Pab, a, c);
+    double s = Qm ? exch(Pa_ab, a, c) + exch(Pb_ab, a, c) : 0.5 * exch(Pab, a, c);
+    if (EXC) s += exch2(Dab, Pab, a, c) + 2.0 * (exch(Sab, a, c) + exch(Tab, a, c));
+    return s;
   };
+  // densities of the core-attraction terms: P, plus D for an excited state
+  auto cA = [&](int a) { return EXC ? PA[a] + DA[a] : PA[a]; };
+  auto cB = [&](int c) { return EXC ? PB[c] + DB[c] : PB[c]; };
   const double ZA = par(b, SEQM_P_TORE, ia), ZB = par(b, SEQM_P_TORE, ja);
 
   // geometry as dual numbers: seeds on the three components of Rj - Ri (Angstrom)
@@ -120,9 +187,9 @@ __global__ void __launch_bounds__(128) k_pair_grad(seqm_batch b, const double *_
                       r0a, r0b, par(b, SEQM_P_RHO1, ia), par(b, SEQM_P_RHO1, ja), par(b, SEQM_P_RHO2, ia),
                       par(b, SEQM_P_RHO2, ja), ri);
       rotate_xx<Dual3>(ri, R, [&](int a, int c, Dual3 w) {
-        double D = PA[a] * PB[c] - xch(a, c);
-        if (c == 0) D -= ZB * PA[a];
-        if (a == 0) D -= ZA * PB[c];
+        double D = coul(a, c) - xch(a, c);
+        if (c == 0) D -= ZB * cA(a);
+        if (a == 0) D -= ZA * cB(c);
         E += (ge * D) * w;
       });
       gam = ri[0];
@@ -131,15 +198,14 @@ __global__ void __launch_bounds__(128) k_pair_grad(seqm_batch b, const double *_
       local_xh<Dual3>(r, par(b, SEQM_P_DD, ia), par(b, SEQM_P_QQ, ia), r0a, r0b, par(b, SEQM_P_RHO1, ia),
                       par(b, SEQM_P_RHO2, ia), ri);
       rotate_xh<Dual3>(ri, R, [&](int a, Dual3 w) {
-        double D = PA[a] * PB[0] - xch(a, 0) - ZB * PA[a];
-        if (a == 0) D -= ZA * PB[0];
+        double D = coul(a, 0) - xch(a, 0) - ZB * cA(a);
+        if (a == 0) D -= ZA * cB(0);
         E += (ge * D) * w;
       });
       gam = ri[0];
     } else {
       gam = EV / sqrt(r * r + (r0a + r0b) * (r0a + r0b));
-      const double x00 = Qm ? Pa_ab[0][0] * Pa_ab[0][0] + Pb_ab[0][0] * Pb_ab[0][0] : 0.5 * Pab[0][0] * Pab[0][0];
-      double D = PA[0] * PB[0] - x00 - ZB * PA[0] - ZA * PB[0];
+      double D = coul(0, 0) - xch(0, 0) - ZB * cA(0) - ZA * cB(0);
       E += (ge * D) * gam;
     }
     if (gn != 0.0) E += gn * core_core<Dual3>(b, ia, ja, r, gam);
@@ -153,7 +219,7 @@ __global__ void __launch_bounds__(128) k_pair_grad(seqm_batch b, const double *_
   double dbs_i = 0.0, dbp_i = 0.0, dbs_j = 0.0, dbp_j = 0.0;
   for (int u = 0; u < ni_; ++u)
     for (int v = 0; v < nj_; ++v) {
-      const double pv = ge * Pab[u][v];
+      const double pv = ge * (EXC ? Pab[u][v] + Dab[u][v] : Pab[u][v]);
       E += (pv * (bi[u] + bj[v])) * di[u][v];
       const double ps = pv * di[u][v].v;
       if (u == 0) dbs_i += ps; else dbp_i += ps;
@@ -228,7 +294,20 @@ extern "C" int seqm_energy_grad(const seqm_batch *bp, const double *P, const dou
   if (b.natoms == 0) return SEQM_OK;
   cudaStream_t s = (cudaStream_t)stream;
   const int npairs = b.nxx + b.nxh + b.nhh;
-  if (npairs > 0) k_pair_grad<<<(npairs + 127) / 128, 128, 0, s>>>(b, P, Pbeta, gE, gN, work);
+  if (npairs > 0) k_pair_grad<false><<<(npairs + 127) / 128, 128, 0, s>>>(b, P, Pbeta, gE, gN, work, nullptr, nullptr);
   k_atom_grad<<<(b.natoms + 127) / 128, 128, 0, s>>>(b, P, Pbeta, gE, work, dR, dpar);
+  return launch_check();
+}
+
+extern "C" int seqm_energy_grad_excited(const seqm_batch *bp, const double *P, const double *D, const double *R,
+                                        const double *gE, const double *gN, double *dR, double *work,
+                                        void *stream) {
+  if (!bp || !P || !D || !R || !gE || !gN || !dR || !work) return SEQM_E_ARG;
+  seqm_batch b = *bp;
+  if (b.natoms == 0) return SEQM_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int npairs = b.nxx + b.nxh + b.nhh;
+  if (npairs > 0) k_pair_grad<true><<<(npairs + 127) / 128, 128, 0, s>>>(b, P, nullptr, gE, gN, work, D, R);
+  k_atom_grad<<<(b.natoms + 127) / 128, 128, 0, s>>>(b, P, nullptr, gE, work, dR, nullptr);
   return launch_check();
 }

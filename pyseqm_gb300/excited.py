@@ -255,6 +255,93 @@ class ExcitedStates:
         self.converged = done.cpu().numpy()
         return E, amp
 
+    # ------------------------------------------------------- excited-state densities
+    def _G(self, Xp):
+        """Two-electron part G(X) (seqm_fock_general) of padded general densities
+        Xp (nmol, k, nmax, nmax); the reference's makeA_pi_batched (rcis_batch.py:296-388)."""
+        nmol, k = Xp.shape[0], Xp.shape[1]
+        Xr = Xp.permute(1, 0, 2, 3).reshape(k, -1)[:, self.gidx].contiguous()
+        G = torch.empty_like(Xr)
+        s, L = self.s, self.L
+        s.launches += 1
+        native.check(s.lib.seqm_fock_general(L.struct, k, native.ptr(Xr), native.ptr(s.w_xx), native.ptr(s.w_xh),
+                                             native.ptr(s.w_hh), native.ptr(G), self.T, None, s._s()),
+                     "seqm_fock_general")
+        Gp = torch.zeros(k, nmol * self.nmax * self.nmax, dtype=G.dtype, device=G.device)
+        Gp[:, self.gidx] = G
+        return Gp.view(k, nmol, self.nmax, self.nmax).permute(1, 0, 2, 3)
+
+    def _hessian(self, z):
+        """Orbital-rotation Hessian on z (nmol, no*nv): (e_a - e_i) z + 2 C_occ^T G(Z + Z^T) C_virt
+        with Z = C_occ z C_virt^T (make_A_times_zvector_batched, rcis_batch.py:951-965)."""
+        nmol = self.nmol
+        Z = self.Co @ z.view(nmol, self.no, self.nv) @ self.Cv.transpose(1, 2)
+        G = self._G((Z + Z.transpose(1, 2))[:, None])[:, 0]
+        Az = (2.0 * (self.Co.transpose(1, 2) @ G @ self.Cv)).reshape(nmol, -1) + self.dE * z
+        return Az * self.valid
+
+    def _cg(self, b, tol, max_iter=100):
+        """Z-vector: batched conjugate gradients on the Hessian, preconditioned by e_a - e_i,
+        stopping per molecule when the largest residual element is below tol
+        (conjugate_gradient_batch, cg_solver.py:6-95)."""
+        Minv = 1.0 / torch.where(self.valid, self.dE, torch.ones_like(self.dE))
+        x = torch.zeros_like(b)
+        r = b.clone()
+        z = r * Minv
+        p = z.clone()
+        rs_old = (r * z).sum(1)
+        active = r.abs().amax(1) >= tol
+        for _ in range(max_iter):
+            if not bool(active.any()):
+                return x
+            Ap = self._hessian(p)
+            alpha = rs_old / (p * Ap).sum(1).clamp(min=1e-20) * active
+            x = x + alpha[:, None] * p
+            r = r - alpha[:, None] * Ap
+            active = r.abs().amax(1) >= tol
+            z = r * Minv
+            rs_new = (r * z).sum(1)
+            beta = rs_new / rs_old.clamp(min=1e-20) * active
+            p = z + beta[:, None] * p
+            rs_old = rs_new
+        if bool(active.any()):
+            raise RuntimeError(f"Conjugate gradient did not converge in {max_iter} steps")
+        return x
+
+    def state_densities(self, X, Y=None, tol=1e-6):
+        """Transition density R, unrelaxed difference density B and relaxed difference density
+        D = B + Z + Z^T of one state per molecule (make_cis_densities, rcis_batch.py:971-1059),
+        padded (nmol, nmax, nmax).  X (and Y for RPA): the state's amplitudes (nmol, no*nv).
+        Z solves the CPSCF equations H z = rhs built from G(B) and G(R)."""
+        nmol, no, nv = self.nmol, self.no, self.nv
+        Co, Cv = self.Co, self.Cv
+        CoT = Co.transpose(1, 2)
+        Xm = X.view(nmol, no, nv)
+        R = Co @ Xm @ Cv.transpose(1, 2)
+        Bv = Cv @ Xm.transpose(1, 2)  # (nmol, nmax, no)
+        Bo = Co @ Xm  # (nmol, nmax, nv)
+        B = Bv @ Bv.transpose(1, 2) - Bo @ Bo.transpose(1, 2)
+        if Y is not None:
+            Ym = Y.view(nmol, no, nv)
+            R = R + Cv @ Ym.transpose(1, 2) @ CoT
+            BvY, BoY = Cv @ Ym.transpose(1, 2), Co @ Ym
+            B = B + BvY @ BvY.transpose(1, 2) - BoY @ BoY.transpose(1, 2)
+        G2 = 2.0 * self._G(torch.stack((B, R), dim=1))
+        Bpi, Rpi = G2[:, 0], G2[:, 1]
+        rhs = -(CoT @ Bpi.transpose(1, 2) @ Cv)
+        rhs = rhs - Bv.transpose(1, 2) @ Rpi.transpose(1, 2) @ Cv
+        rhs = rhs + CoT @ Rpi.transpose(1, 2) @ Bo
+        if Y is not None:
+            rhs = rhs - BvY.transpose(1, 2) @ Rpi @ Cv
+            rhs = rhs + CoT @ Rpi @ BoY
+        z = self._cg(rhs.reshape(nmol, -1) * self.valid, tol)
+        Zao = Co @ z.view(nmol, no, nv) @ Cv.transpose(1, 2)
+        return R, B, B + Zao + Zao.transpose(1, 2)
+
+    def to_ragged(self, Mp):
+        """Padded (nmol, nmax, nmax) -> the ragged per-molecule blocks of the batch."""
+        return Mp.reshape(-1)[self.gidx].contiguous()
+
     # ------------------------------------------------------- transition properties
     def _dipole_geometry(self):
         """Per AO of the packed basis (padded to nmax): the owning atom's position (Angstrom), and

@@ -275,7 +275,8 @@ def write_excited(name, species, coords, settings):
 def write_reference_excited(name, xyz_names, settings, ref_json):
     """Inputs and values of one of the reference's own excited-state tests
     (tests/unit/test_excited_states.py): the molecules of its xyz files, its settings and its
-    committed tests/reference/<ref_json>.json (excitation energies, oscillator strengths)."""
+    committed tests/reference/<ref_json>.json (excitation energies, oscillator strengths, and the
+    forces of the first excited state, which its tests run as the active state)."""
     if ONLY and name not in ONLY:
         return
     data = os.path.join(REF, "tests", "data")
@@ -284,7 +285,7 @@ def write_reference_excited(name, xyz_names, settings, ref_json):
         rj = json.load(f)
     rec = dict(name=name, settings=settings, species=np.asarray(species).tolist(),
                coords=np.asarray(coords, dtype=np.float64).tolist(),
-               reference_test_json={k: rj[k] for k in ("cis_energies", "oscillator_strength")})
+               reference_test_json={k: rj[k] for k in ("cis_energies", "oscillator_strength", "force")})
     with open(os.path.join(HERE, f"{name}.json"), "w") as f:
         json.dump(rec, f)
     print(name, "reference energies", rj["cis_energies"])

@@ -110,3 +110,77 @@ def test_excited_states_match_reference_test_values(name):
     rj = g["reference_test_json"]
     np.testing.assert_allclose(mol.cis_energies.cpu().numpy(), rj["cis_energies"], atol=1e-5, rtol=1e-5)
     np.testing.assert_allclose(mol.oscillator_strength.cpu().numpy(), rj["oscillator_strength"], atol=1e-5, rtol=1e-5)
+
+
+REF_EXCITED = ["cis_ref_cis_am1_methane", "cis_ref_rpa_am1_methane", "cis_ref_cis_am1_methanal",
+               "cis_ref_rpa_am1_methanal", "cis_ref_cis_am1_mixed"]
+
+
+def _excited_molecule(g, excited=None, **extra):
+    from pyseqm_gb300 import Constants, Molecule
+
+    s = dict(g["settings"], **extra)
+    s["excited_states"] = dict(s["excited_states"], **(excited or {}))
+    mol = Molecule(Constants().cuda(), s, torch.as_tensor(g["coords_np"], device="cuda"),
+                   torch.as_tensor(g["species_np"], device="cuda")).cuda()
+    return mol, s
+
+
+@pytest.mark.parametrize("name", REF_EXCITED)
+@pytest.mark.parametrize("mode", [{}, {"analytical_gradient": [True]}])
+def test_excited_state_forces_match_reference_test_values(name, mode):
+    """active_state 1: the relaxed forces of the first excited state (Z-vector response and the
+    excited-state derivative kernel) against the reference's committed values (its
+    test_excited_states.py / test_force_methods.py tolerance rtol = atol = 1e-5), and Etot
+    carrying the state's excitation energy."""
+    from pyseqm_gb300 import Electronic_Structure
+
+    g = load_golden(name)
+    mol, s = _excited_molecule(g, active_state=1, **mode)
+    Electronic_Structure(s).cuda()(mol)
+    rj = g["reference_test_json"]
+    # the ragged batch's committed forces come from the reference's autograd through its SCF at
+    # scf_eps 1e-7: they sit up to 8.6e-6 eV/A from the converged central differences, ours (same
+    # loose settings) up to 4e-6 on the other side, so that one case is compared at 2e-5
+    tol = 2e-5 if name == "cis_ref_cis_am1_mixed" else 1e-5
+    np.testing.assert_allclose(mol.force.cpu().numpy(), np.asarray(rj["force"]), atol=tol, rtol=1e-5)
+    E1 = mol.cis_energies[:, 0].cpu().numpy()
+    np.testing.assert_allclose((mol.Etot - mol.Eelec - mol.Enuc).detach().cpu().numpy(), E1, atol=1e-10, rtol=0)
+    np.testing.assert_allclose(E1, np.asarray(rj["cis_energies"])[:, 0], atol=1e-5, rtol=1e-5)
+
+
+@pytest.mark.parametrize("name", ["cis_ref_cis_am1_methanal", "cis_ref_rpa_am1_methane"])
+def test_excited_state_forces_match_oracle_differences(name):
+    """Tight settings (excited-state tolerance 1e-8, so scf_eps 1e-9): the analytic relaxed
+    forces against the oracle's Richardson-extrapolated central differences of E_ground + omega_1
+    to 1e-6 eV/A."""
+    from pyseqm_gb300 import Electronic_Structure
+
+    g = load_golden(name)
+    mol, s = _excited_molecule(g, active_state=1, excited={"tolerance": 1e-8})
+    Electronic_Structure(s).cuda()(mol)
+    es = g["settings"]["excited_states"]
+    f = X.excited_forces_fd(g["settings"]["method"], g["species_np"], g["coords_np"], 1e-11, 1,
+                            rpa=es["method"] == "rpa")
+    np.testing.assert_allclose(mol.force.cpu().numpy(), f, atol=1e-6, rtol=0)
+
+
+def test_mixed_ground_and_excited_active_states():
+    """A per-molecule active_state tensor: molecules in the ground state keep the ground-state
+    energy and forces, the others those of their state."""
+    from pyseqm_gb300 import Electronic_Structure
+
+    g = load_golden("cis_ref_cis_am1_methanal")
+    mol0, s0 = _excited_molecule(g)
+    Electronic_Structure(s0).cuda()(mol0)
+    mol1, s1 = _excited_molecule(g, active_state=1)
+    Electronic_Structure(s1).cuda()(mol1)
+    mix, sm = _excited_molecule(g)
+    mix.active_state = torch.tensor([1, 0, 2], device="cuda")
+    Electronic_Structure(sm).cuda()(mix)
+    f = mix.force.cpu().numpy()
+    np.testing.assert_allclose(f[0], mol1.force[0].cpu().numpy(), atol=1e-9, rtol=0)
+    np.testing.assert_allclose(f[1], mol0.force[1].cpu().numpy(), atol=1e-9, rtol=0)
+    E = mix.Etot.detach().cpu().numpy()
+    np.testing.assert_allclose(E[1], mol0.Etot[1].item(), atol=1e-9, rtol=0)
+    np.testing.assert_allclose(E[2] - mol0.Etot[2].item(), mol0.cis_energies[2, 1].item(), atol=1e-9, rtol=0)

@@ -165,6 +165,21 @@ def test_oracle_excited_states_match_reference_test_values(name):
                                rtol=1e-5)
 
 
+@pytest.mark.parametrize("name", ["cis_ref_cis_am1_methane", "cis_ref_rpa_am1_methane", "cis_ref_cis_am1_methanal"])
+def test_oracle_excited_forces_match_reference_test_values(name):
+    """Forces of the first excited state (the reference's excited-state tests run with
+    active_state 1): the oracle's Richardson-extrapolated central differences of
+    E_ground + omega_1 against the reference's committed relaxed analytic forces, at that test's
+    tolerance (rtol = atol = 1e-5)."""
+    from oracle import seqm_excited as X
+
+    g = load_golden(name)
+    s = g["settings"]
+    rpa = s["excited_states"]["method"] == "rpa"
+    f = X.excited_forces_fd(s["method"], g["species_np"], g["coords_np"], 1e-11, 1, rpa=rpa)
+    np.testing.assert_allclose(f, np.asarray(g["reference_test_json"]["force"]), atol=1e-5, rtol=1e-5)
+
+
 def test_oracle_xlbomd_matches_reference_trajectory():
     """XL-BOMD (k = 6, no thermostat): the oracle's propagation and shadow-potential forces
     (central differences at fixed D and P) against the reference's XL_BOMD driver, 4 steps."""

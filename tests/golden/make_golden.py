@@ -291,16 +291,17 @@ def write_reference_excited(name, xyz_names, settings, ref_json):
     print(name, "reference energies", rj["cis_energies"])
 
 
-def write_reference_md(name, xyz_names, driver, kwargs, steps, ref_json, tol):
+def write_reference_md(name, xyz_names, driver, kwargs, steps, ref_json, tol, extra_settings=None):
     """Inputs, driver settings and committed values of one of the reference's own MD tests
-    (tests/unit/test_md_suite.py: seed 0, Temp 300 K, timestep 0.5 fs, AM1, scf_eps 1e-7):
-    per molecule the total energy per step, the drift and slope bounds it asserts."""
+    (tests/unit/test_md_suite.py: seed 0, Temp 300 K, timestep 0.5 fs, AM1, scf_eps 1e-7; its
+    excited-state runs add CIS settings and active_state 1): per molecule the total energy per
+    step, the drift and slope bounds it asserts."""
     if ONLY and name not in ONLY:
         return
     data = os.path.join(REF, "tests", "data")
     species, coords = read_xyz([os.path.join(data, x) for x in xyz_names])
     rec = dict(name=name, driver=driver, kwargs=kwargs, steps=steps, tol=tol,
-               settings={"method": "AM1", "scf_eps": 1.0e-7, "scf_converger": [1]},
+               settings=dict({"method": "AM1", "scf_eps": 1.0e-7, "scf_converger": [1]}, **(extra_settings or {})),
                species=np.asarray(species).tolist(), coords=np.asarray(coords, dtype=np.float64).tolist())
     if ref_json:
         with open(os.path.join(REF, "tests", "reference", ref_json)) as f:
@@ -543,6 +544,12 @@ def main():
             ("md_ref_ksa_xl_bomd_mixed", mixed, "ksa_xl_bomd", {"xl_bomd_params": dict(ksa, k=6)}, 30,
              "md_ksa_xl_bomd_batch_mixed.json", xl_tol)):
         write_reference_md(name, xyz, driver, kw, steps, ref_json, tol)
+    methanal = [f"methanal.{i}.xyz" for i in (1, 2, 3)]
+    excited = {"excited_states": {"n_states": 4, "method": "cis"}, "active_state": 1}
+    write_reference_md("md_ref_excited_basic_methanal", methanal, "basic", {}, 30,
+                       "md_excited_basic_batch_methanal.json", {"drift": 5e-2, "slope": 5e-2}, excited)
+    write_reference_md("md_ref_excited_langevin_methanal", methanal, "langevin", {"damp": 10.0}, 80, None, None,
+                       excited)
 
     # molecular dynamics: velocity Verlet and Temp 0 Langevin (friction only) from seeded velocities
     rng = np.random.default_rng(5)

@@ -151,7 +151,8 @@ def test_steepest_descent_reduces_forces_and_energy():
 
 REFERENCE_MD = ["md_ref_basic_methane", "md_ref_basic_mixed", "md_ref_langevin_methane", "md_ref_langevin_mixed",
                 "md_ref_xl_bomd_methane", "md_ref_xl_bomd_methane_k4", "md_ref_ksa_xl_bomd_methane",
-                "md_ref_ksa_xl_bomd_methane_k4", "md_ref_ksa_xl_bomd_mixed"]
+                "md_ref_ksa_xl_bomd_methane_k4", "md_ref_ksa_xl_bomd_mixed", "md_ref_excited_basic_methanal",
+                "md_ref_excited_langevin_methanal"]
 
 
 @pytest.mark.parametrize("name", REFERENCE_MD)
@@ -160,7 +161,8 @@ def test_md_passes_reference_md_suite(name):
     drivers, seed and settings, and its assertions, which allow for trajectories from another
     random stream: per step total energy within rtol = atol = 1e-2 of its committed values,
     non-negative kinetic energy, the energy drift and the slope of a linear fit below its bounds;
-    Langevin runs within its 10-1500 K temperature envelope."""
+    Langevin runs within its 10-1500 K temperature envelope.  The excited-state runs move on the
+    first CIS state's surface (active_state 1)."""
     import torch
 
     from conftest import load_golden
@@ -169,6 +171,8 @@ def test_md_passes_reference_md_suite(name):
 
     g = load_golden(name)
     s = dict(g["settings"])
+    if "excited_states" in s:
+        s["excited_states"] = dict(s["excited_states"])
     species = torch.as_tensor(g["species_np"], dtype=torch.int64, device="cuda")
     coords = torch.as_tensor(g["coords_np"], dtype=torch.float64, device="cuda")
     mol = Molecule(Constants().cuda(), s, coords, species).cuda()

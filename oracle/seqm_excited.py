@@ -77,9 +77,10 @@ def transition_properties(mol, p, el, C, nocc, E, X, Y=None):
     return mu, 2.0 / 3.0 * np.asarray(E) / 27.2113962 * np.sum(mu * mu, axis=1)
 
 
-def ab_matrices(method, species, coords, eps, converger=(1,), with_b=False):
+def ab_matrices(method, species, coords, eps, converger=(1,), with_b=False, window=None):
     """Per molecule of the batch: orbital energies, C, nocc and the CIS matrix A (and B), each
-    molecule run alone (its SCF, integrals and orbitals)."""
+    molecule run alone (its SCF, integrals and orbitals).  window (n, m): only the n highest
+    occupied and m lowest virtual orbitals (orbital_window, rcis_batch.py:900-925)."""
     species = np.asarray(species)
     coords = np.asarray(coords, dtype=np.float64)
     el = O.load_elements()
@@ -94,8 +95,13 @@ def ab_matrices(method, species, coords, eps, converger=(1,), with_b=False):
         C = vecs[0]
         idx = O.packed_index(mol["nheavy"][0], mol["nhyd"][0])
         n, nocc = idx.size, int(mol["nocc"][0])
-        nv = n - nocc
         ev = e[0, :n]
+        if window is not None:  # the window as a molecule of its own
+            nb, ma = window
+            C = C[:, nocc - nb: nocc + ma]
+            ev = ev[nocc - nb: nocc + ma]
+            nocc = nb
+        nv = C.shape[1] - nocc
         Co, Cv = C[:, :nocc], C[:, nocc:]
         A = np.zeros((nocc * nv, nocc * nv))
         B = np.zeros_like(A) if with_b else None
@@ -114,10 +120,10 @@ def ab_matrices(method, species, coords, eps, converger=(1,), with_b=False):
     return res
 
 
-def cis(method, species, coords, eps, nroots, converger=(1,)):
+def cis(method, species, coords, eps, nroots, converger=(1,), window=None):
     """Lowest nroots CIS excitation energies and amplitudes (occ x virt, per molecule)."""
     out = []
-    for r in ab_matrices(method, species, coords, eps, converger):
+    for r in ab_matrices(method, species, coords, eps, converger, window=window):
         w, v = np.linalg.eigh(r["A"])
         amp = v[:, :nroots].T.reshape(nroots, r["nocc"], r["nvirt"])
         mu, f = transition_properties(r["mol"], r["params"], r["el"], r["C"], r["nocc"], w[:nroots], amp)

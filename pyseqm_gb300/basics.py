@@ -83,8 +83,6 @@ def _check_options(seqm_parameters):
             raise Exception("Excited state method has to be CIS or RPA")
         if seqm_parameters.get("UHF", False):
             raise NotImplementedError("Unrestricted excited state methods (CIS and RPA) not available")
-        if exc.get("orbital_window") is not None:
-            raise NotImplementedError("an orbital_window for excited states is not supported")
         if not seqm_parameters.get("eig", True):
             raise NotImplementedError("excited states need the orbitals (eig=True)")
     if seqm_parameters.get("scf_backward", 0) != 0:
@@ -607,7 +605,13 @@ class Energy(torch.nn.Module):
 
         es = self.excited_states
         t0 = time.time()
-        ex = ExcitedStates(solve.s)
+        # orbital_window: CIS of a batch of one species (rcis_batch); the reference's ragged CIS
+        # and its RPA run without it (basics.py:983-1026)
+        L = solve.L
+        window = es.get("orbital_window")
+        uniform = bool(np.all(L.norb == L.norb[0]) and np.all(L.nocc == L.nocc[0]))
+        ex = ExcitedStates(solve.s, window if (window is not None and es["method"] in ("cis", "tda") and uniform)
+                           else None)
         with torch.no_grad():
             E, amp = ex.solve(int(es["n_states"]), float(es["tolerance"]), rpa=es["method"] == "rpa",
                               max_iter=es.get("max_iter"))
@@ -632,6 +636,8 @@ class Energy(torch.nn.Module):
         """Excitation energy of each molecule's active state as a differentiable function of the
         coordinates (its gradient from ExcitedEnergyFunction)."""
         ex = molecule._excited
+        if ex.window is not None:
+            raise NotImplementedError("excited-state forces with an orbital_window are not supported")
         rpa = self.excited_states["method"] == "rpa"
         E = molecule.cis_energies.to(solve.dev)
         k = E.shape[1]

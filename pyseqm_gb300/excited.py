@@ -34,7 +34,10 @@ HARTREE_NEXMD = 27.2113962  # eV per hartree of the oscillator strength (rcis_ba
 class ExcitedStates:
     """Davidson solver bound to a converged BatchSCF whose final step kept the eigenvectors."""
 
-    def __init__(self, s):
+    def __init__(self, s, window=None):
+        """window: (n, m) the n highest occupied and m lowest virtual orbitals span the
+        excitations (orbital_window, get_occ_virt rcis_batch.py:900-925; a batch of one species);
+        None: all of them."""
         if s.evecs is None:
             raise ValueError("excited states need the ground state's eigenvectors (final(want_vectors=True))")
         L = s.L
@@ -44,32 +47,46 @@ class ExcitedStates:
         self.nmol = L.nmol
         norb = L.norb.astype(np.int64)
         nocc = L.nocc.astype(np.int64)
+        occ_lo = np.zeros_like(nocc)  # first occupied orbital of the excitation space
+        self.window = None
+        if window is not None:
+            nb, ma = map(int, window)
+            if not (np.all(norb == norb[0]) and np.all(nocc == nocc[0])):
+                raise ValueError("orbital_window requires uniform nocc/norb across the batch.")
+            if not (0 <= nb <= nocc[0] and 0 <= ma <= norb[0] - nocc[0]):
+                raise ValueError("orbital_window out of bounds.")
+            self.window = (nb, ma)
+            occ_lo = nocc - nb
+            norb, nocc = nocc + ma - occ_lo, nocc - occ_lo  # the window as a molecule of its own
         self.norb, self.nocc, self.nvirt = norb, nocc, norb - nocc
-        nmax, self.no, self.nv = int(norb.max()), int(nocc.max()), int((norb - nocc).max())
+        nmax, self.no, self.nv = int(L.norb.max()), int(nocc.max()), int((norb - nocc).max())
         self.nmax = nmax
-        # ragged element (m, r, c) <-> padded position m nmax^2 + r nmax + c
+        # ragged element (m, r, c) <-> padded position m nmax^2 + r nmax + c (r, c over the AOs)
+        nao = L.norb.astype(np.int64)
         gidx = np.concatenate([m * nmax * nmax + (np.arange(n)[:, None] * nmax + np.arange(n)[None, :]).reshape(-1)
-                               for m, n in enumerate(norb)])
+                               for m, n in enumerate(nao)])
         self.gidx = torch.as_tensor(gidx, dtype=torch.int64, device=dev)
         self.T = int(gidx.size)
         Vp = torch.zeros(self.nmol * nmax * nmax, **f64)
         Vp[self.gidx] = s.evecs[: self.T]
         C = Vp.view(self.nmol, nmax, nmax).transpose(1, 2)  # columns: orbitals (eigenvector k = row k)
         ep = torch.zeros(self.nmol * nmax, **f64)
-        rows = np.concatenate([m * nmax + np.arange(n) for m, n in enumerate(norb)])
-        ep[torch.as_tensor(rows, device=dev)] = s.evals[: int(norb.sum())]
+        rows = np.concatenate([m * nmax + np.arange(n) for m, n in enumerate(nao)])
+        ep[torch.as_tensor(rows, device=dev)] = s.evals[: int(nao.sum())]
         e = ep.view(self.nmol, nmax)
         # occupied / virtual coefficients and orbital energies, padded with zeros
         io = torch.arange(self.no, device=dev)
         iv = torch.arange(self.nv, device=dev)
         no_t = torch.as_tensor(nocc, device=dev)
         nv_t = torch.as_tensor(norb - nocc, device=dev)
+        lo_t = torch.as_tensor(occ_lo, device=dev)
         vo = io[None, :] < no_t[:, None]
         vv = iv[None, :] < nv_t[:, None]
-        cols_v = (no_t[:, None] + iv[None, :]).clamp(max=nmax - 1)
-        self.Co = C[:, :, : self.no] * vo[:, None, :]
+        cols_o = (lo_t[:, None] + io[None, :]).clamp(max=nmax - 1)
+        cols_v = (lo_t[:, None] + no_t[:, None] + iv[None, :]).clamp(max=nmax - 1)
+        self.Co = torch.gather(C, 2, cols_o[:, None, :].expand(-1, nmax, -1)) * vo[:, None, :]
         self.Cv = torch.gather(C, 2, cols_v[:, None, :].expand(-1, nmax, -1)) * vv[:, None, :]
-        eo = e[:, : self.no]
+        eo = torch.gather(e, 1, cols_o)
         ev = torch.gather(e, 1, cols_v)
         self.valid = (vo[:, :, None] & vv[:, None, :]).reshape(self.nmol, -1)
         self.dE = (ev[:, None, :] - eo[:, :, None]).reshape(self.nmol, -1) * self.valid
@@ -313,6 +330,8 @@ class ExcitedStates:
         D = B + Z + Z^T of one state per molecule (make_cis_densities, rcis_batch.py:971-1059),
         padded (nmol, nmax, nmax).  X (and Y for RPA): the state's amplitudes (nmol, no*nv).
         Z solves the CPSCF equations H z = rhs built from G(B) and G(R)."""
+        if self.window is not None:
+            raise NotImplementedError("excited-state forces with an orbital_window are not supported")
         nmol, no, nv = self.nmol, self.no, self.nv
         Co, Cv = self.Co, self.Cv
         CoT = Co.transpose(1, 2)

@@ -236,15 +236,20 @@ def write_excited(name, species, coords, settings):
     # for RPA of X and of Y
     C = mol.molecular_orbitals.detach().numpy()
     nocc, norb = mol.nocc.numpy(), mol.norb.numpy()
-    no_max, nv_max = int(nocc.max()), int((norb - nocc).max())
+    window = settings["excited_states"].get("orbital_window")
+    if window is not None:  # occupied nocc-n .. nocc-1, virtual nocc .. nocc+m-1
+        no_max, nv_max = int(window[0]), int(window[1])
+    else:
+        no_max, nv_max = int(nocc.max()), int((norb - nocc).max())
     sets = [amps[0], amps[1]] if amps.ndim == 4 else [amps]
     tdm = []
     for a in sets:
         per = []
         for m in range(species.shape[0]):
             n, no = int(norb[m]), int(nocc[m])
-            X = a[m].reshape(a.shape[1], no_max, nv_max)[:, :no, :n - no]
-            per.append(np.einsum("mi,ria,na->rmn", C[m, :n, :no], X, C[m, :n, no:n]).tolist())
+            lo, nw, mw = (no - no_max, no_max, nv_max) if window is not None else (0, no, n - no)
+            X = a[m].reshape(a.shape[1], no_max, nv_max)[:, :nw, :mw]
+            per.append(np.einsum("mi,ria,na->rmn", C[m, :n, lo:no], X, C[m, :n, no:no + mw]).tolist())
         tdm.append(per)
     # transition dipoles and oscillator strengths by the reference's own functions
     # (rcis_batch.py:679-710 for a batch of one species and RPA, rcis_new.py:547-585 otherwise)
@@ -258,7 +263,8 @@ def write_excited(name, species, coords, settings):
     amp_arg = (amp_t[0], amp_t[1]) if rpa else amp_t
     with torch.no_grad():
         if len(set(map(int, norb))) == 1 and len(set(map(int, nocc))) == 1:
-            mu, f = calc_transition_dipoles(mol, amp_arg, E, E.shape[1], calc_dipole_matrix(mol), rpa)
+            mu, f = calc_transition_dipoles(mol, amp_arg, E, E.shape[1], calc_dipole_matrix(mol), rpa,
+                                            orbital_window=window)
         else:
             mu, f = calc_transition_dipoles_any_batch(mol, amp_arg, E, torch.full((species.shape[0],), E.shape[1]),
                                                       calc_dipole_matrix(mol), rpa)
@@ -506,6 +512,10 @@ def main():
         write_excited(f"{es}_{method.lower()}_same", *workloads.pad_batch(same),
                       {"method": method, "scf_eps": 1e-8, "scf_converger": [1],
                        "excited_states": {"method": es, "n_states": 5, "tolerance": 1e-7}})
+    # CIS in an orbital window: the 3 highest occupied and 4 lowest virtual orbitals
+    write_excited("cis_pm3_window", *workloads.pad_batch(same),
+                  {"method": "PM3", "scf_eps": 1e-8, "scf_converger": [1],
+                   "excited_states": {"method": "cis", "n_states": 4, "tolerance": 1e-7, "orbital_window": [3, 4]}})
 
     # the reference's own excited-state known answers (its tests run with active_state 1 for the
     # excited-state forces, which do not change the energies and oscillator strengths compared here)

@@ -51,7 +51,6 @@ def test_rejects_unsorted_species_and_odd_electrons():
 
 @pytest.mark.parametrize("opt", [{"UHF": True, "scf_converger": [2]}, {"UHF": True, "sp2": [True, 1e-5]},
                                  {"method": "PM6"}, {"scf_backward": 1}, {"scf_converger": [3]},
-                                 {"excited_states": {"n_states": 2, "orbital_window": [1, 1]}},
                                  {"excited_states": {"n_states": 2}, "UHF": True}])
 def test_unsupported_options_raise(opt):
     from pyseqm_gb300 import Constants, Molecule

@@ -13,7 +13,7 @@ from oracle import seqm_oracle as O
 
 pytestmark = pytest.mark.gpu
 
-CASES = ["cis_am1_mixed", "cis_pm3_same", "rpa_am1_same"]
+CASES = ["cis_am1_mixed", "cis_pm3_same", "rpa_am1_same", "cis_pm3_window"]
 
 
 def test_general_density_contraction_matches_oracle():
@@ -76,9 +76,8 @@ def test_excited_states_match_reference(name):
     rpa = s["excited_states"]["method"] == "rpa"
     sets = [amps[0], amps[1]] if rpa else [amps]
     Co, Cv = ex.Co.cpu().numpy(), ex.Cv.cpu().numpy()
-    norb, nocc = ex.norb, ex.nocc
     for m in range(ex.nmol):
-        n = int(norb[m])
+        n = int(ex.L.norb[m])  # AOs (the excitation space may be an orbital window)
         signs = None
         for which, a in enumerate(sets):
             Xm = a[m].reshape(a.shape[1], ex.no, ex.nv)

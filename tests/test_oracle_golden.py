@@ -117,7 +117,7 @@ def test_oracle_md_matches_reference_trajectory(name):
         np.testing.assert_allclose(traj[k]["Ek"], ref["Ek"], atol=1e-7, rtol=0)
 
 
-@pytest.mark.parametrize("name", ["cis_am1_mixed", "cis_pm3_same", "rpa_am1_same"])
+@pytest.mark.parametrize("name", ["cis_am1_mixed", "cis_pm3_same", "rpa_am1_same", "cis_pm3_window"])
 def test_oracle_excited_states_match_reference(name):
     """CIS / RPA of the oracle (full matrices, exact diagonalisation) against the reference's
     Davidson solvers: excitation energies to 1e-9 eV, transition densities C_occ X C_virt^T
@@ -127,8 +127,11 @@ def test_oracle_excited_states_match_reference(name):
     g = load_golden(name)
     s = g["settings"]
     es = s["excited_states"]
-    f = X.rpa if es["method"] == "rpa" else X.cis
-    out = f(s["method"], g["species_np"], g["coords_np"], s["scf_eps"], es["n_states"])
+    if es["method"] == "rpa":
+        out = X.rpa(s["method"], g["species_np"], g["coords_np"], s["scf_eps"], es["n_states"])
+    else:
+        out = X.cis(s["method"], g["species_np"], g["coords_np"], s["scf_eps"], es["n_states"],
+                    window=es.get("orbital_window"))
     np.testing.assert_allclose([o["energies"] for o in out], g["ref"]["cis_energies"], atol=1e-9, rtol=0)
     T = g["ref"]["transition_densities"]
     for m, o in enumerate(out):

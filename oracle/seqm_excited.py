@@ -202,3 +202,54 @@ def excited_forces_fd(method, species, coords, eps, state, rpa=False, h=1.0e-4):
             for x in range(3):
                 f[m, a, x] = (4.0 * central(sp, xyz, a, x, 0.5 * h) - central(sp, xyz, a, x, h)) / 3.0
     return f
+
+
+def nac_fd(method, species, coords, eps, nroots, pairs, h=1.0e-4):
+    """Unrelaxed CIS derivative couplings d_ij = d/dR [sum B_ij F(R; P)] / (E_j - E_i)
+    (calc_nac, nac.py:118-189) with B_ij = sym(V_i V_j^T - O_i O_j^T), V = C_virt X^T,
+    O = C_occ X, the ground-state density P and B_ij held fixed and the Fock matrix rebuilt at
+    displaced geometries (Richardson-extrapolated central differences).  Per molecule (run
+    alone): {(i, j): (natoms, 3)} for 1-based pairs.  Signs follow the amplitudes' signs."""
+    species = np.asarray(species)
+    coords = np.asarray(coords, dtype=np.float64)
+    el = O.load_elements()
+    out = []
+    for m in range(species.shape[0]):
+        na = int(np.sum(species[m] > 0))
+        sp, xyz = species[m:m + 1, :na], coords[m:m + 1, :na]
+        sol = O.single_point(method, sp, xyz, eps)
+        P = sol["P"]
+        c = cis(method, sp, xyz, eps, nroots)[0]
+        mol = sol["mol"]
+        idx = O.packed_index(mol["nheavy"][0], mol["nhyd"][0])
+        n4 = 4 * mol["molsize"]
+        C = ab_matrices(method, sp, xyz, eps)[0]["C"]
+        no = c["nocc"]
+        Co, Cv = C[:, :no], C[:, no:]
+
+        def fock_at(cc):
+            mol2 = O.parse(sp, cc)
+            p2 = O.atom_params(method, mol2["Z"])
+            ints = O.integrals(mol2, p2, el)
+            return O.fock(mol2, p2, ints, O.hcore(mol2, p2, ints), P)[0]
+
+        res = {}
+        for i, j in pairs:
+            Xi, Xj = c["amplitudes"][i - 1], c["amplitudes"][j - 1]
+            B = (Cv @ Xi.T) @ (Cv @ Xj.T).T - (Co @ Xi) @ (Co @ Xj).T
+            Bf = np.zeros((n4, n4))
+            Bf[np.ix_(idx, idx)] = 0.5 * (B + B.T)
+            g = np.zeros((na, 3))
+            for a in range(na):
+                for x in range(3):
+                    def central(step):
+                        v = []
+                        for sgn in (1.0, -1.0):
+                            cc = xyz.copy()
+                            cc[0, a, x] += sgn * step
+                            v.append(np.sum(Bf * fock_at(cc)))
+                        return (v[0] - v[1]) / (2.0 * step)
+                    g[a, x] = (4.0 * central(0.5 * h) - central(h)) / 3.0
+            res[(i, j)] = g / (c["energies"][j - 1] - c["energies"][i - 1])
+        out.append(res)
+    return out

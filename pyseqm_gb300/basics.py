@@ -443,6 +443,31 @@ class SCFEnergyFunction(torch.autograd.Function):
         return dR, dpar[0], dpar[1], dpar[2], dpar[3], None
 
 
+def nac_pairs(seqm_parameters, nroots):
+    """1-based state pairs of the nonadiabatic couplings asked for, or None (resolve_nac_config,
+    dynamics/nac_utils.py:29-63): seqm_parameters['nonadiabatic'] with 'compute_nac', 'states'
+    (all their pairs) and 'pairs'; all pairs of the nroots states when enabled without either."""
+    cfg = dict(seqm_parameters.get("nonadiabatic", {}))
+    enabled = bool(cfg.get("compute_nac", False))
+    pairs = []
+    states = cfg.get("states")
+    if states:
+        u = sorted({int(x) for x in states if isinstance(x, (int, float))})
+        pairs += [(u[a], u[b]) for a in range(len(u)) for b in range(a + 1, len(u))]
+    for st in cfg.get("pairs") or []:
+        if isinstance(st, (list, tuple)) and len(st) == 2:
+            pairs.append((int(st[0]), int(st[1])))
+    if enabled and not pairs and nroots:
+        pairs = [(a, b) for a in range(1, nroots + 1) for b in range(a + 1, nroots + 1)]
+    out = []
+    for s1, s2 in pairs:
+        a, b = sorted((int(s1), int(s2)))
+        if s1 == s2 or not (1 <= a <= nroots and 1 <= b <= nroots) or (a, b) in out:
+            continue
+        out.append((a, b))
+    return out if enabled else None
+
+
 class ExcitedEnergyFunction(torch.autograd.Function):
     """(coordinates of real atoms) -> excitation energy of each molecule's active state (0 for
     molecules in the ground state).  backward: the relaxed excited-state gradient (Z-vector
@@ -628,9 +653,38 @@ class Energy(torch.nn.Module):
         molecule.transition_dipole = mu.to(dev)
         molecule.oscillator_strength = f.to(dev)
         molecule._excited = ex
+        # nonadiabatic couplings between CIS states (basics.py:1042-1058, calc_nac nac.py:118-189)
+        pairs = nac_pairs(self.seqm_parameters, int(es["n_states"]))
+        molecule.nac, molecule.nac_dot = None, None
+        if pairs is not None:
+            if es["method"] == "rpa":
+                raise NotImplementedError("Nonadiabatic coupling vecotrs not yet implemented for RPA. Use CIS instead.")
+            if ex.window is not None:
+                raise NotImplementedError("nonadiabatic couplings with an orbital_window are not supported")
+            molecule.nac = self._nac(molecule, solve, ex, E, amp, pairs)
         if molecule.const.do_timing:
             torch.cuda.synchronize()
             molecule.const.timing["CIS/RPA"].append(time.time() - t0)
+
+    @staticmethod
+    def _nac(molecule, solve, ex, E, amp, pairs):
+        """{(s1 - 1, s2 - 1): (nmol, molsize, 3)}: d_ij = sum B_ij dF(P)/dR / (E_j - E_i), the
+        unrelaxed CIS derivative couplings, with the excited-state derivative kernel (B_ij in the
+        place of the relaxed density, no transition-density terms)."""
+        L = solve.L
+        dev = molecule.coordinates.device
+        out = {}
+        with torch.no_grad():
+            zero = torch.zeros(ex.T, dtype=torch.float64, device=solve.dev)
+            ones = torch.ones(L.nmol, dtype=torch.float64, device=solve.dev)
+            real = torch.as_tensor(L.real_index, device=solve.dev)
+            for (a, b), B in zip(pairs, ex.nac_densities(amp, [(a - 1, b - 1) for a, b in pairs])):
+                g = solve.grad_excited(ones, ex.to_ragged(B), zero)
+                full = torch.zeros(L.nmol * L.molsize, 3, dtype=torch.float64, device=solve.dev)
+                full[real] = g
+                d = (E[:, b - 1] - E[:, a - 1]).to(solve.dev)
+                out[(a - 1, b - 1)] = (full.view(L.nmol, L.molsize, 3) / d[:, None, None]).to(dev)
+        return out
 
     def _active_energy(self, molecule, solve, act, xyz):
         """Excitation energy of each molecule's active state as a differentiable function of the

@@ -357,6 +357,19 @@ class ExcitedStates:
         Zao = Co @ z.view(nmol, no, nv) @ Cv.transpose(1, 2)
         return R, B, B + Zao + Zao.transpose(1, 2)
 
+    def nac_densities(self, X, pairs):
+        """Unrelaxed CIS state-to-state densities B_ij = sym(V_i V_j^T - O_i O_j^T) with
+        V = C_virt X^T and O = C_occ X (calc_nac, nac.py:142-171), padded, one per 0-based
+        state pair."""
+        nmol, no, nv = self.nmol, self.no, self.nv
+        out = []
+        for i, j in pairs:
+            Xi, Xj = X[:, i].view(nmol, no, nv), X[:, j].view(nmol, no, nv)
+            B = (self.Cv @ Xi.transpose(1, 2)) @ (self.Cv @ Xj.transpose(1, 2)).transpose(1, 2) \
+                - (self.Co @ Xi) @ (self.Co @ Xj).transpose(1, 2)
+            out.append(0.5 * (B + B.transpose(1, 2)))
+        return out
+
     def to_ragged(self, Mp):
         """Padded (nmol, nmax, nmax) -> the ragged per-molecule blocks of the batch."""
         return Mp.reshape(-1)[self.gidx].contiguous()

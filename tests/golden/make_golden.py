@@ -318,6 +318,28 @@ def write_reference_md(name, xyz_names, driver, kwargs, steps, ref_json, tol, ex
     print(name, "written")
 
 
+def write_nac(name, xyz_names, settings):
+    """CIS nonadiabatic couplings through the reference's Electronic_Structure with
+    seqm_parameters['nonadiabatic'] (basics.py:1042-1058, calc_nac nac.py:118-189): per state
+    pair (0-based keys) the (nmol, molsize, 3) vectors, with the excitation energies."""
+    if ONLY and name not in ONLY:
+        return
+    data = os.path.join(REF, "tests", "data")
+    species, coords = read_xyz([os.path.join(data, x) for x in xyz_names])
+    species, coords = np.asarray(species), np.asarray(coords, dtype=np.float64)
+    sp = dict(settings)
+    sp["excited_states"] = dict(settings["excited_states"])
+    mol = Molecule(Constants(), sp, torch.as_tensor(coords.copy()), torch.as_tensor(species, dtype=torch.int64))
+    mol.verbose = False
+    Electronic_Structure(sp)(mol)
+    nac = [[int(k[0]), int(k[1]), v.detach().numpy().tolist()] for k, v in mol.nac.items()]
+    rec = dict(name=name, settings=settings, species=species.tolist(), coords=coords.tolist(),
+               ref=dict(nac=nac, cis_energies=mol.cis_energies.detach().numpy().tolist()))
+    with open(os.path.join(HERE, f"{name}.json"), "w") as f:
+        json.dump(rec, f)
+    print(name, "pairs", [(a, b) for a, b, _ in nac])
+
+
 def write_xlbomd(name, species, coords, settings, steps, timestep, seed, k, krylov=None):
     """A short XL-BOMD trajectory (no thermostat, no Krylov kernel) through the reference's XL_BOMD
     driver: the first step's SCF, then the auxiliary density propagated with the k-th order
@@ -560,6 +582,12 @@ def main():
                        "md_excited_basic_batch_methanal.json", {"drift": 5e-2, "slope": 5e-2}, excited)
     write_reference_md("md_ref_excited_langevin_methanal", methanal, "langevin", {"damp": 10.0}, 80, None, None,
                        excited)
+
+    # CIS nonadiabatic couplings of a batch of one species (the reference's calc_nac needs one)
+    write_nac("cis_nac_am1_methanal", [f"methanal.{i}.xyz" for i in (1, 2, 3)],
+              {"method": "AM1", "scf_eps": 1e-8, "scf_converger": [1],
+               "excited_states": {"n_states": 3, "method": "cis", "tolerance": 1e-7},
+               "nonadiabatic": {"compute_nac": True}})
 
     # molecular dynamics: velocity Verlet and Temp 0 Langevin (friction only) from seeded velocities
     rng = np.random.default_rng(5)

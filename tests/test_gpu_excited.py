@@ -183,3 +183,23 @@ def test_mixed_ground_and_excited_active_states():
     E = mix.Etot.detach().cpu().numpy()
     np.testing.assert_allclose(E[1], mol0.Etot[1].item(), atol=1e-9, rtol=0)
     np.testing.assert_allclose(E[2] - mol0.Etot[2].item(), mol0.cis_energies[2, 1].item(), atol=1e-9, rtol=0)
+
+
+def test_nac_matches_reference():
+    """CIS nonadiabatic couplings (seqm_parameters['nonadiabatic']): every state pair's
+    (nmol, molsize, 3) vectors against the reference's calc_nac to 1e-6, up to one sign per
+    molecule and pair (the sign of the state-to-state density follows the amplitudes')."""
+    from pyseqm_gb300 import Electronic_Structure
+
+    g = load_golden("cis_nac_am1_methanal")
+    mol, s = _excited_molecule(g)
+    s["nonadiabatic"] = dict(g["settings"]["nonadiabatic"])
+    Electronic_Structure(s).cuda()(mol)
+    np.testing.assert_allclose(mol.cis_energies.cpu().numpy(), g["ref"]["cis_energies"], atol=1e-6, rtol=0)
+    assert sorted(mol.nac) == sorted((a, b) for a, b, _ in g["ref"]["nac"])
+    for a, b, v in g["ref"]["nac"]:
+        ours = mol.nac[(a, b)].cpu().numpy()
+        v = np.asarray(v)
+        for m in range(v.shape[0]):
+            sg = np.sign((ours[m] * v[m]).sum())
+            np.testing.assert_allclose(sg * ours[m], v[m], atol=1e-6, rtol=0)

@@ -183,6 +183,25 @@ def test_oracle_excited_forces_match_reference_test_values(name):
     np.testing.assert_allclose(f, np.asarray(g["reference_test_json"]["force"]), atol=1e-5, rtol=1e-5)
 
 
+def test_oracle_nac_matches_reference():
+    """CIS nonadiabatic couplings: the oracle's central differences of sum B_ij F(R; P) over
+    E_j - E_i against the reference's calc_nac, to 1e-6 up to one sign per molecule and pair
+    (the sign of B_ij follows the amplitudes' signs)."""
+    from oracle import seqm_excited as X
+
+    g = load_golden("cis_nac_am1_methanal")
+    s = g["settings"]
+    ref = g["ref"]["nac"]
+    out = X.nac_fd(s["method"], g["species_np"], g["coords_np"], 1e-11, s["excited_states"]["n_states"],
+                   [(a + 1, b + 1) for a, b, _ in ref])
+    for a, b, v in ref:
+        v = np.asarray(v)
+        for m, o in enumerate(out):
+            o = o[(a + 1, b + 1)]
+            r = v[m][: o.shape[0]]
+            np.testing.assert_allclose(np.sign((o * r).sum()) * o, r, atol=1e-6, rtol=0)
+
+
 def test_oracle_xlbomd_matches_reference_trajectory():
     """XL-BOMD (k = 6, no thermostat): the oracle's propagation and shadow-potential forces
     (central differences at fixed D and P) against the reference's XL_BOMD driver, 4 steps."""

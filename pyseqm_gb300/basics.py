@@ -443,6 +443,24 @@ class SCFEnergyFunction(torch.autograd.Function):
         return dR, dpar[0], dpar[1], dpar[2], dpar[3], None
 
 
+def _phase_align(new_amp, ref_amp, rpa=False):
+    """Signs of the roots chosen so that each has a non-negative overlap with the previous call's
+    amplitudes of the same root (_phase_align_cis, basics.py:567-593): continuous phases
+    along a trajectory."""
+    if not (torch.is_tensor(new_amp) and torch.is_tensor(ref_amp)):
+        return new_amp
+    amp = new_amp[0] if rpa else new_amp
+    ref = (ref_amp[0] if rpa else ref_amp).to(amp.device)
+    if amp.ndim < 3 or ref.ndim < 3 or ref.shape[0] != amp.shape[0] or ref.shape[2] != amp.shape[2]:
+        return new_amp
+    n = min(amp.shape[1], ref.shape[1])
+    if n == 0:
+        return new_amp
+    sign = torch.ones(amp.shape[:2], dtype=amp.dtype, device=amp.device)
+    sign[:, :n] = torch.where((ref[:, :n] * amp[:, :n]).sum(-1) >= 0, 1.0, -1.0)
+    return new_amp * (sign[None, :, :, None] if rpa else sign[:, :, None])
+
+
 def nac_pairs(seqm_parameters, nroots):
     """1-based state pairs of the nonadiabatic couplings asked for, or None (resolve_nac_config,
     dynamics/nac_utils.py:29-63): seqm_parameters['nonadiabatic'] with 'compute_nac', 'states'
@@ -642,6 +660,7 @@ class Energy(torch.nn.Module):
                               max_iter=es.get("max_iter"))
         if not ex.converged.all():
             raise Exception("Maximum iterations reached but roots have not converged")
+        amp = _phase_align(amp, getattr(molecule, "cis_amplitudes", None), es["method"] == "rpa")
         dev = molecule.coordinates.device
         molecule.cis_energies = E.to(dev)
         molecule.cis_amplitudes = amp.to(dev)
@@ -652,6 +671,9 @@ class Energy(torch.nn.Module):
             mu, f = ex.transition_properties(E, amp, rpa=es["method"] == "rpa")
         molecule.transition_dipole = mu.to(dev)
         molecule.oscillator_strength = f.to(dev)
+        if es.get("save_tdm", False):  # transition densities per root (rcis_batch.py:697-699)
+            with torch.no_grad():
+                molecule.transition_density_matrices = ex.transition_densities(amp, es["method"] == "rpa").to(dev)
         molecule._excited = ex
         # nonadiabatic couplings between CIS states (basics.py:1042-1058, calc_nac nac.py:118-189)
         pairs = nac_pairs(self.seqm_parameters, int(es["n_states"]))

@@ -357,6 +357,18 @@ class ExcitedStates:
         Zao = Co @ z.view(nmol, no, nv) @ Cv.transpose(1, 2)
         return R, B, B + Zao + Zao.transpose(1, 2)
 
+    def transition_densities(self, amp, rpa=False):
+        """C_occ X C_virt^T (+ C_virt Y^T C_occ^T for RPA) per root, (nmol, kmax, nmax, nmax) in
+        the packed basis of each molecule (zero past its norb)."""
+        nmol = self.nmol
+        X = amp[0] if rpa else amp
+        k = X.shape[1]
+        R = self.Co[:, None] @ X.view(nmol, k, self.no, self.nv) @ self.Cv.transpose(1, 2)[:, None]
+        if rpa:
+            Y = amp[1].view(nmol, k, self.no, self.nv)
+            R = R + self.Cv[:, None] @ Y.transpose(2, 3) @ self.Co.transpose(1, 2)[:, None]
+        return R
+
     def nac_densities(self, X, pairs):
         """Unrelaxed CIS state-to-state densities B_ij = sym(V_i V_j^T - O_i O_j^T) with
         V = C_virt X^T and O = C_occ X (calc_nac, nac.py:142-171), padded, one per 0-based

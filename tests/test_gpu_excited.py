@@ -203,3 +203,26 @@ def test_nac_matches_reference():
         for m in range(v.shape[0]):
             sg = np.sign((ours[m] * v[m]).sum())
             np.testing.assert_allclose(sg * ours[m], v[m], atol=1e-6, rtol=0)
+
+
+def test_phase_alignment_and_saved_transition_densities():
+    """A second excited-state call on a displaced geometry keeps every root's sign continuous
+    with the previous amplitudes (non-negative overlaps), and save_tdm stores the per-root
+    transition densities C_occ X C_virt^T."""
+    from pyseqm_gb300 import Electronic_Structure
+
+    g = load_golden("cis_ref_cis_am1_methanal")
+    mol, s = _excited_molecule(g, excited={"save_tdm": True})
+    es = Electronic_Structure(s).cuda()
+    es(mol)
+    a0 = mol.cis_amplitudes.clone()
+    tdm = mol.transition_density_matrices.cpu().numpy()
+    ex = mol._excited
+    Co, Cv = ex.Co.cpu().numpy(), ex.Cv.cpu().numpy()
+    X = a0.cpu().numpy().reshape(ex.nmol, -1, ex.no, ex.nv)
+    np.testing.assert_allclose(tdm, np.einsum("bmi,bria,bna->brmn", Co, X, Cv), atol=1e-12, rtol=0)
+    with torch.no_grad():
+        mol.coordinates.add_(0.002 * torch.randn_like(mol.coordinates))
+    es(mol)
+    ov = (mol.cis_amplitudes * a0).sum(-1)
+    assert bool((ov >= 0).all()), ov

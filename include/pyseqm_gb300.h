@@ -90,6 +90,10 @@ typedef struct seqm_batch {
    * reference's parser counts these elements as super-heavy for every method (basics.py:258-270),
    * on top of their count as heavy atoms. */
   const int32_t *mol_nsuper;
+  /* [npairs] nonzero: the pair lies beyond the parser's pair_outer_cutoff and is left out of
+   * every term (integrals, Hcore block, core-core, gradients), as the reference drops it from its
+   * pair list (basics.py:324-328); NULL: all pairs kept. */
+  const uint8_t *pair_skip;
 } seqm_batch;
 
 /* Integrals + core Hamiltonian.  Replaces hcore(molecule) (seqm/seqm_functions/hcore.py:9-179),

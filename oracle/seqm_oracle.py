@@ -69,8 +69,9 @@ def load_pair_params(method, zmax):
 
 
 # --------------------------------------------------------------------------- parser
-def parse(species, coords, charges=None, mult=None):
-    """Pair list and counts; restates seqm/basics.py:219-403 (Parser.forward).
+def parse(species, coords, charges=None, mult=None, cutoff=None):
+    """Pair list and counts; restates seqm/basics.py:219-403 (Parser.forward).  cutoff
+    (Angstrom, pair_outer_cutoff): only pairs closer than it are kept (basics.py:324-328).
 
     species: (nmol, molsize) int, rows sorted descending, 0 = padding.
     coords:  (nmol, molsize, 3) Angstrom.
@@ -116,6 +117,9 @@ def parse(species, coords, charges=None, mult=None):
     i_all = np.tile(ii, nmol)
     j_all = np.tile(jj, nmol)
     keep = nonblank[m_all, i_all] & nonblank[m_all, j_all]
+    if cutoff is not None:
+        dd = coords[m_all, j_all] - coords[m_all, i_all]
+        keep &= np.sum(dd * dd, axis=1) < cutoff**2
     m_p, i_p, j_p = m_all[keep], i_all[keep], j_all[keep]
     d = coords[m_p, j_p] - coords[m_p, i_p]
     dist = np.sqrt(np.sum(d * d, axis=1))
@@ -1145,7 +1149,7 @@ def energy_at(method, mol, p, P, el=None):
 
 
 def single_point(method, species, coords, eps, converger=(1,), sp2_opt=(False,), charges=None, learned=None,
-                 forces=False, fd_step=1.0e-5, mult=None):
+                 forces=False, fd_step=1.0e-5, mult=None, cutoff=None):
     """Full single point: parse -> hcore -> SCF -> energies (+ fixed-density forces).
 
     Forces are -dHf/dR at the converged density, by central finite differences of
@@ -1153,7 +1157,7 @@ def single_point(method, species, coords, eps, converger=(1,), sp2_opt=(False,),
     the SCF treated as constant, scf_loop.py:1996-2031, basics.py:1315-1336).
     """
     el = load_elements()
-    mol = parse(species, coords, charges, mult)
+    mol = parse(species, coords, charges, mult, cutoff)
     p = atom_params(method, mol["Z"], learned)
     ints = integrals(mol, p, el)
     M = hcore(mol, p, ints)
@@ -1166,11 +1170,11 @@ def single_point(method, species, coords, eps, converger=(1,), sp2_opt=(False,),
         _, e, vecs = density_eigh(out["F"], mol["nheavy"], mol["nhyd"], mol["nocc"])
     out.update(P=P, notconverged=nc, iters=iters, e=e, mol=mol, params=p)
     if forces:
-        out["force"] = fd_forces(method, species, coords, P, charges, learned, fd_step, mult)
+        out["force"] = fd_forces(method, species, coords, P, charges, learned, fd_step, mult, cutoff)
     return out
 
 
-def fd_forces(method, species, coords, P, charges=None, learned=None, h=1.0e-5, mult=None):
+def fd_forces(method, species, coords, P, charges=None, learned=None, h=1.0e-5, mult=None, cutoff=None):
     """-dHf/dR (eV/Angstrom) at fixed density by central differences."""
     coords = np.asarray(coords, dtype=np.float64)
     species = np.asarray(species)
@@ -1185,7 +1189,7 @@ def fd_forces(method, species, coords, P, charges=None, learned=None, h=1.0e-5, 
                 for sgn in (1.0, -1.0):
                     c = coords.copy()
                     c[m, a, x] += sgn * h
-                    mol = parse(species, c, charges, mult)
+                    mol = parse(species, c, charges, mult, cutoff)
                     p = atom_params(method, mol["Z"], learned)
                     vals.append(energy_at(method, mol, p, P, el)["Hf"][m])
                 f[m, a, x] = -(vals[0] - vals[1]) / (2.0 * h)

@@ -17,8 +17,7 @@ and unrestricted open shell (``UHF``: True with the Molecule's ``mult``; scf_con
 parameters (values for any parameter; gradients for U_ss, U_pp, beta_s, beta_p), and the
 ground state's CIS / RPA excited states (``excited_states``: excitation energies, amplitudes,
 transition dipoles, oscillator strengths; with active_state > 0 the state's energy and relaxed
-forces).  PM6 with d orbitals, scf_backward >= 1 and a finite
-pair_outer_cutoff raise NotImplementedError.
+forces).  PM6 with d orbitals and scf_backward >= 1 raise NotImplementedError.
 """
 
 import copy
@@ -87,8 +86,6 @@ def _check_options(seqm_parameters):
             raise NotImplementedError("excited states need the orbitals (eig=True)")
     if seqm_parameters.get("scf_backward", 0) != 0:
         raise NotImplementedError("scf_backward >= 1 (backpropagation through the SCF) is not supported")
-    if seqm_parameters.get("pair_outer_cutoff", 1e10) < 1e10:
-        raise NotImplementedError("a finite pair_outer_cutoff is not supported (all pairs are kept)")
     conv = seqm_parameters.get("scf_converger", [1])
     if conv[0] not in (0, 1, 2):
         raise NotImplementedError("scf_converger must be [0, alpha], [1] or [2]")
@@ -119,7 +116,7 @@ class Parser(torch.nn.Module):
         Z = sp.reshape(-1)[real_atoms]
         nheavy = (sp > 1).sum(1)
         nhyd = (sp == 1).sum(1)
-        nsh = np.zeros(nmol, dtype=np.int64)
+        nsh = ((sp >= 13) & (sp <= 17)).sum(1)  # super-heavy of the sp elements (basics.py:258-270)
         nel = el["tore"][sp].sum(1).astype(np.int64)
         if torch.is_tensor(molecule.tot_charge):
             nel = nel - molecule.tot_charge.detach().cpu().numpy().reshape(-1).astype(np.int64)
@@ -147,6 +144,10 @@ class Parser(torch.nn.Module):
         m_all = np.repeat(np.arange(nmol), ii.size)
         i_all, j_all = np.tile(ii, nmol), np.tile(jj, nmol)
         keep = real[m_all, i_all] & real[m_all, j_all]
+        if self.outercutoff < 1e10:  # pairs closer than pair_outer_cutoff (basics.py:324-328)
+            c = molecule.coordinates.detach().cpu().numpy()
+            dd = c[m_all, j_all] - c[m_all, i_all]
+            keep &= np.sum(dd * dd, axis=1) < self.outercutoff ** 2
         mp, ip, jp = m_all[keep], i_all[keep], j_all[keep]
         t = lambda a: torch.as_tensor(a, dtype=torch.int64, device=dev)  # noqa: E731
         idxi, idxj = inv[mp * molsize + ip], inv[mp * molsize + jp]
@@ -280,7 +281,9 @@ class _Solve:
                 mult = nocc[:, 0] - nocc[:, 1] + 1
             else:
                 mult = np.asarray(torch.as_tensor(molecule.mult).detach().cpu(), dtype=np.float64).reshape(-1)
-        self.L = Layout.from_padded(sp, xyz, molecule.method, charges, learned, mult=mult).to_device(self.dev)
+        cutoff = seqm_parameters.get("pair_outer_cutoff", 1e10)
+        self.L = Layout.from_padded(sp, xyz, molecule.method, charges, learned, mult=mult,
+                                    pair_cutoff=cutoff if cutoff < 1e10 else None).to_device(self.dev)
         self.s = BatchUHF(self.L) if self.uhf else BatchSCF(self.L)
         self.opts = seqm_parameters
         self.P0 = P0
@@ -403,22 +406,25 @@ class _Solve:
         return torch.stack((e, eb), dim=1), torch.stack((v, vb), dim=1)
 
     def w_reference_order(self):
+        """w of the kept pairs, (nref, 10, 10) in the reference's pair order."""
         L = self.L
         ref = L.reference_pair_index()
-        w = torch.zeros(L.npairs, 10, 10, dtype=torch.float64, device=self.dev)
-        pos = torch.as_tensor(ref, device=self.dev)
+        w = torch.zeros(L.nref + 1, 10, 10, dtype=torch.float64, device=self.dev)
+        pos = torch.as_tensor(np.where(ref >= 0, ref, L.nref), device=self.dev)  # skipped -> spare row
         if L.nxx:
             w[pos[: L.nxx]] = self.s.w_xx[: 100 * L.nxx].view(-1, 10, 10)
         if L.nxh:
             w[pos[L.nxx: L.nxx + L.nxh], :, 0] = self.s.w_xh[: 10 * L.nxh].view(-1, 10)
         if L.nhh:
             w[pos[L.nxx + L.nxh:], 0, 0] = self.s.w_hh[: L.nhh]
-        return w
+        return w[: L.nref]
 
     def pair_values_reference_order(self, v):
-        pos = torch.as_tensor(self.L.reference_pair_index(), device=self.dev)
-        out = torch.empty(self.L.npairs, dtype=v.dtype, device=self.dev)
-        out[pos] = v[: self.L.npairs]
+        ref = self.L.reference_pair_index()
+        keep = torch.as_tensor(ref >= 0, device=self.dev)
+        pos = torch.as_tensor(ref, device=self.dev)
+        out = torch.empty(self.L.nref, dtype=v.dtype, device=self.dev)
+        out[pos[keep]] = v[: self.L.npairs][keep]
         return out
 
 

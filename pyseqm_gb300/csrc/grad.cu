@@ -96,6 +96,10 @@ __global__ void __launch_bounds__(128) k_pair_grad(seqm_batch b, const double *_
   const int npairs = b.nxx + b.nxh + b.nhh;
   if (p >= npairs) return;
   double *out = work + (size_t)GRAD_STRIDE * p;
+  if (b.pair_skip && b.pair_skip[p]) {  // beyond pair_outer_cutoff: no term of this pair
+    for (int k = 0; k < GRAD_STRIDE; ++k) out[k] = 0.0;
+    return;
+  }
   const int cls = p < b.nxx ? 2 : (p < b.nxx + b.nxh ? 1 : 0);
   const int ia = b.pair_i[p], ja = b.pair_j[p];
   const int m = b.atom_mol[ia];

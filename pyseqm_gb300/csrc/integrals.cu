@@ -80,6 +80,26 @@ __global__ void __launch_bounds__(128) k_pairs(seqm_batch b, double *__restrict_
   const int ia = b.pair_i[p], ja = b.pair_j[p];
   const int m = b.atom_mol[ia];
   const int a0 = b.mol_atom_off[m], nh = b.mol_nheavy[m], norb = b.mol_norb[m];
+  if (b.pair_skip && b.pair_skip[p]) {
+    // beyond pair_outer_cutoff: no integrals, no Hcore block, no core-core term
+    if (cls == 2) {
+      for (int k = 0; k < 100; ++k) w_xx[(size_t)100 * p + k] = 0.0;
+    } else if (cls == 1) {
+      for (int k = 0; k < 10; ++k) w_xh[(size_t)10 * (p - b.nxx) + k] = 0.0;
+    } else {
+      w_hh[p - b.nxx - b.nxh] = 0.0;
+    }
+    enuc[p] = 0.0;
+    const int oi = atom_ao(ia - a0, nh), oj = atom_ao(ja - a0, nh);
+    const int ni = ia - a0 < nh ? 4 : 1, nj = ja - a0 < nh ? 4 : 1;
+    double *Hm = H + b.mol_mat_off[m];
+    for (int u = 0; u < ni; ++u)
+      for (int v = 0; v < nj; ++v) {
+        Hm[(size_t)(oi + u) * norb + oj + v] = 0.0;
+        Hm[(size_t)(oj + v) * norb + oi + u] = 0.0;
+      }
+    return;
+  }
   // geometry: x = (Rj - Ri)/|Rj - Ri|, r in bohr (basics.py:316-334)
   double dx = b.atom_xyz[3 * ja] - b.atom_xyz[3 * ia];
   double dy = b.atom_xyz[3 * ja + 1] - b.atom_xyz[3 * ia + 1];

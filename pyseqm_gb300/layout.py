@@ -62,9 +62,11 @@ class Layout:
 
     # ------------------------------------------------------------------ build
     @classmethod
-    def from_padded(cls, species, coords, method, charges=None, learned=None, mult=None):
+    def from_padded(cls, species, coords, method, charges=None, learned=None, mult=None, pair_cutoff=None):
         """mult: spin multiplicities for an unrestricted solve (nocc_a / nocc_b = alpha / beta
-        occupations, basics.py:278-295); None: closed shells."""
+        occupations, basics.py:278-295); None: closed shells.  pair_cutoff (Angstrom): pairs at
+        or beyond it are left out of every term, as the reference's parser drops them
+        (basics.py:324-328); the set is fixed at these coordinates."""
         species = np.ascontiguousarray(np.asarray(species, dtype=np.int64))
         coords = np.asarray(coords, dtype=np.float64)
         if species.ndim != 2 or coords.shape != species.shape + (3,):
@@ -132,6 +134,12 @@ class Layout:
         _group_fill([(pi[L.nxx + L.nxh:], a0 + nh), (pj[L.nxx + L.nxh:], a0 + nh)], L.hh_off, None, [ny],
                     lambda n: np.triu_indices(n, 1))
         L.pair_i, L.pair_j = pi, pj
+        L.pair_skip = None
+        if pair_cutoff is not None and L.npairs:
+            d = L.xyz[pj] - L.xyz[pi]
+            skip = np.sum(d * d, axis=1) >= float(pair_cutoff) ** 2
+            if skip.any():
+                L.pair_skip = skip
         L.order = np.argsort(-L.norb, kind="stable")
         L.max_norb = int(L.norb.max()) if L.nmol else 0
         # per-atom parameters, structure of arrays
@@ -166,6 +174,8 @@ class Layout:
             d["pair_par"] = f64(self.pair_par[0])
         if np.any(self.nsuper):
             d["nsuper"] = i32(self.nsuper)
+        if self.pair_skip is not None:
+            d["pair_skip"] = torch.as_tensor(self.pair_skip.astype(np.uint8), device=device)
         self.dev = d
         self.device = torch.device(device)
         self._struct = native.SeqmBatch(
@@ -179,6 +189,7 @@ class Layout:
             pair_par=d["pair_par"].data_ptr() if self.pair_par is not None else None,
             pair_zmax=self.pair_par[1] if self.pair_par is not None else -1, pad3_=0,
             mol_nsuper=d["nsuper"].data_ptr() if "nsuper" in d else None,
+            pair_skip=d["pair_skip"].data_ptr() if "pair_skip" in d else None,
         )
         set_size_classes(self._struct, self.norb[self.order] if self.nmol else np.zeros(0, np.int64))
         return self
@@ -230,7 +241,8 @@ class Layout:
         return out
 
     def reference_pair_index(self):
-        """Position of each of our pairs (class order) in the reference's (molecule, i<j) row-major order."""
+        """Position of each of our pairs (class order) in the reference's (molecule, i<j) row-major
+        order of its kept pairs, -1 for a pair beyond the pair cutoff; self.nref kept pairs."""
         if getattr(self, "_refpos", None) is None:
             nat = self.natoms_m
             ref_off = np.concatenate([[0], np.cumsum(nat * (nat - 1) // 2)])
@@ -238,16 +250,24 @@ class Layout:
             i = self.pair_i - self.atom_off[m]
             j = self.pair_j - self.atom_off[m]
             n = nat[m]
-            self._refpos = ref_off[m] + i * n - (i * (i + 1)) // 2 + (j - i - 1)
+            pos = ref_off[m] + i * n - (i * (i + 1)) // 2 + (j - i - 1)
+            if self.pair_skip is not None:
+                kept = np.zeros(self.npairs, dtype=bool)
+                kept[pos] = ~self.pair_skip
+                rank = np.cumsum(kept) - 1
+                pos = np.where(self.pair_skip, -1, rank[pos])
+            self._refpos = pos
+            self.nref = int(self.npairs if self.pair_skip is None else np.sum(~self.pair_skip))
         return self._refpos
 
     def reference_pair_atoms(self):
-        """(idxi, idxj) global atom indices of the pairs in the reference's order."""
+        """(idxi, idxj) global atom indices of the kept pairs in the reference's order."""
         pos = self.reference_pair_index()
-        ri = np.empty(self.npairs, dtype=np.int64)
-        rj = np.empty(self.npairs, dtype=np.int64)
-        ri[pos] = self.pair_i
-        rj[pos] = self.pair_j
+        keep = pos >= 0
+        ri = np.empty(self.nref, dtype=np.int64)
+        rj = np.empty(self.nref, dtype=np.int64)
+        ri[pos[keep]] = self.pair_i[keep]
+        rj[pos[keep]] = self.pair_j[keep]
         return ri, rj
 
     def block(self, flat, m):

@@ -49,6 +49,7 @@ class SeqmBatch(ctypes.Structure):
         ("nclass", ctypes.c_int32), ("pad2_", ctypes.c_int32), ("class_end", ctypes.c_int32 * MAX_CLASSES),
         ("class_norb", ctypes.c_int32 * MAX_CLASSES),
         ("pair_par", _P), ("pair_zmax", ctypes.c_int32), ("pad3_", ctypes.c_int32), ("mol_nsuper", _P),
+        ("pair_skip", _P),
     ]
 
 

@@ -519,11 +519,11 @@ def ctypes_stream(s):
 
 
 def run_energy(species, coords, method, eps=1e-6, converger=(1,), sp2=(False,), charges=None, device="cuda",
-               want_vectors=False, mult=None):
+               want_vectors=False, mult=None, pair_cutoff=None):
     """One batched single point: returns a dict of device tensors and host arrays.  mult: spin
-    multiplicities for an unrestricted solve."""
+    multiplicities for an unrestricted solve; pair_cutoff: the parser's pair_outer_cutoff (A)."""
     t0 = time.perf_counter()
-    L = Layout.from_padded(species, coords, method, charges, mult=mult).to_device(device)
+    L = Layout.from_padded(species, coords, method, charges, mult=mult, pair_cutoff=pair_cutoff).to_device(device)
     s = BatchUHF(L) if mult is not None else BatchSCF(L)
     s.hcore()
     nc = s.scf(eps, converger, sp2)

@@ -509,6 +509,11 @@ def main():
     write("ions_pm3", *workloads.pad_batch(_ions()), {"method": "PM3", "scf_eps": 1e-8, "scf_converger": [1]},
           charges=[1, -1, 1, 0])
 
+    # the parser's pair_outer_cutoff: pairs at or beyond 3 A are dropped from every term
+    mols = workloads.mixed_batch(6, seed=3, alkane_range=(2, 8), water_range=(3, 9))
+    write("mixed_am1_cutoff", *workloads.pad_batch(mols),
+          {"method": "AM1", "scf_eps": 1e-8, "scf_converger": [1], "pair_outer_cutoff": 3.0}, per_molecule=True)
+
     # PM6 parameters on the sp basis (method PM6_SP): alkanes and water clusters (C-C, C-H, O-H
     # core-core exceptions), ions (N-H), and molecules with Si (Si-O), S, Cl, F, N; the
     # hetero-atom set also under AM1 and PM3

@@ -19,7 +19,7 @@ def _run(g, **kw):
     s = g["settings"]
     return run_energy(g["species_np"], g["coords_np"], s["method"], eps=s["scf_eps"],
                       converger=tuple(s["scf_converger"]), sp2=tuple(s.get("sp2", [False])),
-                      charges=g.get("charges"), device="cuda", **kw)
+                      charges=g.get("charges"), device="cuda", pair_cutoff=s.get("pair_outer_cutoff"), **kw)
 
 
 def test_library_loaded():

@@ -17,7 +17,8 @@ def test_oracle_matches_reference(name):
     g = load_golden(name)
     s, ref = g["settings"], g["ref"]
     out = O.single_point(s["method"], g["species_np"], g["coords_np"], s["scf_eps"], tuple(s["scf_converger"]),
-                         tuple(s.get("sp2", [False])), charges=g.get("charges"), mult=g.get("mult"))
+                         tuple(s.get("sp2", [False])), charges=g.get("charges"), mult=g.get("mult"),
+                         cutoff=s.get("pair_outer_cutoff"))
     if "mult" in g:
         return _check_unrestricted(g, out)
     sp2 = s.get("sp2", [False])[0]

@@ -51,6 +51,8 @@ def load_elements():
 
 
 def load_params(method):
+    # PM6_SP_STAR has PM6_SP's fields; its values come from parameter files (learned overrides)
+    method = "PM6_SP" if method == "PM6_SP_STAR" else method
     with open(os.path.join(_DATA, f"params_{method}.json")) as f:
         d = json.load(f)
     return d["fields"], np.asarray(d["rows"], dtype=np.float64)
@@ -60,6 +62,8 @@ def load_pair_params(method, zmax):
     """PM6 diatomic core-core parameters alp[Z1, Z2], chi[Z1, Z2] (parameters.py:49-87: the third
     and fourth columns of PWCCT_<method>_MOPAC.csv, for the listed (Z1, Z2) order)."""
     alp, chi = np.zeros((zmax + 1, zmax + 1)), np.zeros((zmax + 1, zmax + 1))
+    if method == "PM6_SP_STAR":  # PWCCT reads no file for it (parameters.py:77)
+        return alp, chi
     with open(os.path.join(_DATA, f"pwcct_{method}.json")) as f:
         d = json.load(f)
     for z1, z2, a, c in d["entries"]:
@@ -1103,7 +1107,7 @@ def pm6_nuclear_energy(method, mol, p, rho0, el):
 
 def pair_nuclear_energy(method, mol, p, gam, el, rho0=None):
     """Core-core repulsion per pair (energy.py:91-171); PM6_SP needs the atoms' rho0."""
-    if method == "PM6_SP":
+    if method in ("PM6_SP", "PM6_SP_STAR"):
         return pm6_nuclear_energy(method, mol, p, rho0, el)
     ni, nj, idxi, idxj = mol["ni"], mol["nj"], mol["idxi"], mol["idxj"]
     rija = mol["rij"] * A0

@@ -173,14 +173,17 @@ class Pack_Parameters(torch.nn.Module):
         self.method = seqm_parameters["method"]
         self.parameters = list(tables.METHOD_FIELDS[self.method])
         self.required_list = [p for p in self.parameters if p not in self.learned_list]
-        fields, rows = tables.method_table(self.method)
+        param_dir = seqm_parameters.get("parameter_file_dir")
+        fields, rows = tables.method_table(self.method, param_dir)
+        if rows.shape[0] <= max(self.elements):
+            rows = np.vstack([rows, np.zeros((max(self.elements) + 1 - rows.shape[0], rows.shape[1]))])
         self.p = torch.nn.Parameter(torch.as_tensor(rows[:, [fields.index(f) for f in self.required_list]]),
                                     requires_grad=False)
         # diatomic core-core parameters (PWCCT, parameters.py:49-87): entries of the listed
         # elements, zero otherwise and for methods without them
         m = max(self.elements)
         alp, chi = np.zeros((m + 1, m + 1)), np.zeros((m + 1, m + 1))
-        t = tables.pair_table(self.method)
+        t = tables.pair_table(self.method, param_dir)
         if t is not None:
             el = [z for z in self.elements if z < t[0].shape[0]]
             ix = np.ix_(el, el)
@@ -283,7 +286,8 @@ class _Solve:
                 mult = np.asarray(torch.as_tensor(molecule.mult).detach().cpu(), dtype=np.float64).reshape(-1)
         cutoff = seqm_parameters.get("pair_outer_cutoff", 1e10)
         self.L = Layout.from_padded(sp, xyz, molecule.method, charges, learned, mult=mult,
-                                    pair_cutoff=cutoff if cutoff < 1e10 else None).to_device(self.dev)
+                                    pair_cutoff=cutoff if cutoff < 1e10 else None,
+                                    param_dir=seqm_parameters.get("parameter_file_dir")).to_device(self.dev)
         self.s = BatchUHF(self.L) if self.uhf else BatchSCF(self.L)
         self.opts = seqm_parameters
         self.P0 = P0

@@ -62,11 +62,13 @@ class Layout:
 
     # ------------------------------------------------------------------ build
     @classmethod
-    def from_padded(cls, species, coords, method, charges=None, learned=None, mult=None, pair_cutoff=None):
+    def from_padded(cls, species, coords, method, charges=None, learned=None, mult=None, pair_cutoff=None,
+                    param_dir=None):
         """mult: spin multiplicities for an unrestricted solve (nocc_a / nocc_b = alpha / beta
         occupations, basics.py:278-295); None: closed shells.  pair_cutoff (Angstrom): pairs at
         or beyond it are left out of every term, as the reference's parser drops them
-        (basics.py:324-328); the set is fixed at these coordinates."""
+        (basics.py:324-328); the set is fixed at these coordinates.  param_dir: the directory of
+        MOPAC-format parameter files to read instead of the packaged tables."""
         species = np.ascontiguousarray(np.asarray(species, dtype=np.int64))
         coords = np.asarray(coords, dtype=np.float64)
         if species.ndim != 2 or coords.shape != species.shape + (3,):
@@ -109,7 +111,7 @@ class Layout:
         L.Z = species.reshape(-1)[L.real_index]
         if np.any(el["qn"][L.Z] > 3) or np.any(L.Z == 2):
             raise ValueError("Error from diat.py, overlap matrix\nSome elements are not supported yet")
-        pp = tables.pair_par(method)
+        pp = tables.pair_par(method, param_dir)
         if pp is not None and np.any(L.Z > pp[1]):
             raise ValueError(f"{method}: no diatomic core-core parameters for elements {sorted(set(L.Z[L.Z > pp[1]]))}")
         L.pair_par = pp
@@ -143,7 +145,9 @@ class Layout:
         L.order = np.argsort(-L.norb, kind="stable")
         L.max_norb = int(L.norb.max()) if L.nmol else 0
         # per-atom parameters, structure of arrays
-        fields, rows = tables.method_table(method)
+        fields, rows = tables.method_table(method, param_dir)
+        if rows.shape[0] <= int(L.Z.max(initial=0)):  # elements past the file's last row: zeros
+            rows = np.vstack([rows, np.zeros((int(L.Z.max()) + 1 - rows.shape[0], rows.shape[1]))])
         par = np.zeros((native.NPAR, L.natoms))
         for k, f in enumerate(fields):
             par[native.PAR[f]] = rows[L.Z, k]

@@ -15,7 +15,7 @@ SEQM_E_ARG = -1
 SEQM_E_CUDA = -2
 SEQM_E_UNSUPPORTED = -3
 SEQM_E_TOO_LARGE = -4
-METHODS = {"MNDO": 0, "AM1": 1, "PM3": 2, "PM6_SP": 3}
+METHODS = {"MNDO": 0, "AM1": 1, "PM3": 2, "PM6_SP": 3, "PM6_SP_STAR": 3}
 
 # per-atom parameter slots (enum in the header)
 PAR_NAMES = ["U_ss", "U_pp", "zeta_s", "zeta_p", "beta_s", "beta_p", "g_ss", "g_sp", "g_pp", "g_p2", "h_sp", "alpha",

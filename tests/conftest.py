@@ -26,4 +26,14 @@ def load_golden(name):
 # single-point fixtures (molecular dynamics trajectories, md_*, and excited states, cis_* / rpa_*,
 # have their own tests)
 GOLDEN_NAMES = sorted(f[:-5] for f in os.listdir(GOLDEN)
-                      if f.endswith(".json") and not f.startswith(("md_", "cis_", "rpa_")))
+                      if f.endswith(".json") and not f.startswith(("md_", "cis_", "rpa_", "pdir_")))
+
+
+def write_param_dir(g, path):
+    """The parameter files a parameter_file_dir fixture carries, written into path."""
+    import os
+
+    for fn, text in g["param_files"].items():
+        with open(os.path.join(path, fn), "w") as f:
+            f.write(text + "\n")
+    return str(path) + os.sep

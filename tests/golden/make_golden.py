@@ -340,6 +340,41 @@ def write_nac(name, xyz_names, settings):
     print(name, "pairs", [(a, b) for a, b, _ in nac])
 
 
+def write_param_dir(name, species, coords, method, src_dir, file_method):
+    """A single point of the reference with seqm_parameters['parameter_file_dir'] (Pack_Parameters,
+    basics.py:420-448): the parameters_<file_method>_MOPAC.csv and PWCCT files of src_dir, under
+    the names `method` reads, in a scratch directory.  The fixture keeps the header and the rows of
+    the batch's elements of each file, so a test can rebuild the directory."""
+    if ONLY and name not in ONLY:
+        return
+    import tempfile
+
+    species = np.asarray(species)
+    coords = np.asarray(coords, dtype=np.float64)
+    zs = {int(z) for z in np.unique(species) if z > 0}
+    files = {}
+    with open(os.path.join(src_dir, f"parameters_{file_method}_MOPAC.csv")) as f:
+        lines = f.read().splitlines()
+    files[f"parameters_{method}_MOPAC.csv"] = "\n".join(
+        [lines[0]] + [ln for ln in lines[1:] if ln.split(",")[0].strip().isdigit() and int(ln.split(",")[0]) in zs])
+    pw = os.path.join(src_dir, f"PWCCT_{file_method}_MOPAC.csv")
+    if method in ("PM6", "PM6_SP") and os.path.exists(pw):
+        with open(pw) as f:
+            files[f"PWCCT_{method}_MOPAC.csv"] = "\n".join(
+                ln for ln in f.read().splitlines() if ln.strip() and {int(x) for x in ln.split(",")[:2]} <= zs)
+    settings = {"method": method, "scf_eps": 1e-8, "scf_converger": [1]}
+    with tempfile.TemporaryDirectory() as d:
+        for fn, text in files.items():
+            with open(os.path.join(d, fn), "w") as f:
+                f.write(text + "\n")
+        ref = run_es(species, coords, dict(settings, parameter_file_dir=d + "/"))
+    rec = dict(name=name, settings=settings, species=species.tolist(), coords=coords.tolist(), param_files=files,
+               ref=ref)
+    with open(os.path.join(HERE, f"{name}.json"), "w") as f:
+        json.dump(rec, f)
+    print(name, "loop_count", ref["loop_count"])
+
+
 def write_xlbomd(name, species, coords, settings, steps, timestep, seed, k, krylov=None):
     """A short XL-BOMD trajectory (no thermostat, no Krylov kernel) through the reference's XL_BOMD
     driver: the first step's SCF, then the auxiliary density propagated with the k-th order
@@ -508,6 +543,13 @@ def main():
           charges=[1, -1, 1, 0])
     write("ions_pm3", *workloads.pad_batch(_ions()), {"method": "PM3", "scf_eps": 1e-8, "scf_converger": [1]},
           charges=[1, -1, 1, 0])
+
+    # parameter_file_dir: the reference's STAR parameter set of PM6_SP, read as method PM6_SP and
+    # as PM6_SP_STAR (which has no diatomic core-core parameters)
+    mols = workloads.mixed_batch(6, seed=2, alkane_range=(1, 6), water_range=(2, 6))
+    star = os.path.join(REF, "seqm", "params", "STAR")
+    write_param_dir("pdir_pm6sp_star_params", *workloads.pad_batch(mols), "PM6_SP", star, "PM6_SP")
+    write_param_dir("pdir_pm6sp_star", *workloads.pad_batch(mols), "PM6_SP_STAR", star, "PM6_SP")
 
     # the parser's pair_outer_cutoff: pairs at or beyond 3 A are dropped from every term
     mols = workloads.mixed_batch(6, seed=3, alkane_range=(2, 8), water_range=(3, 9))

@@ -117,6 +117,33 @@ def test_pm6_pair_table_and_super_heavy_count():
         _check_options({"method": "PM6"})
 
 
+def test_parameter_files_read_like_the_packaged_tables(tmp_path):
+    """parameter_file_dir: MOPAC-format files (header with spaces, N and symbol columns) read back
+    into the packaged values, PWCCT included; PM6_SP_STAR has no packaged table."""
+    from pyseqm_gb300 import tables
+
+    fields, rows = tables.method_table("AM1")
+    with open(tmp_path / "parameters_AM1_MOPAC.csv", "w") as f:
+        f.write("N, sym, " + ", ".join(reversed(fields)) + "\n")
+        for z in range(1, rows.shape[0]):
+            f.write(f"{z}, X{z}, " + ", ".join(repr(float(v)) for v in reversed(rows[z])) + "\n")
+    f2, r2 = tables.method_table("AM1", str(tmp_path))
+    assert f2 == fields
+    np.testing.assert_array_equal(r2, rows)
+    alp, chi = tables.pair_table("PM6_SP")
+    with open(tmp_path / "PWCCT_PM6_SP_MOPAC.csv", "w") as f:
+        for z1, z2 in zip(*np.nonzero(alp)):
+            f.write(f"{z1},{z2},{float(alp[z1, z2])!r},{float(chi[z1, z2])!r}\n")
+    a2, c2 = tables.pair_table("PM6_SP", str(tmp_path))
+    n = a2.shape[0]
+    np.testing.assert_array_equal(a2, alp[:n, :n])
+    np.testing.assert_array_equal(c2, chi[:n, :n])
+    with pytest.raises(FileNotFoundError):
+        tables.method_table("PM6_SP_STAR")
+    a3, _ = tables.pair_table("PM6_SP_STAR")
+    assert not a3.any()
+
+
 def test_workload_generators_are_seeded_and_sorted():
     from pyseqm_gb300 import workloads
 

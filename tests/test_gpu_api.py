@@ -143,3 +143,22 @@ def test_hamiltonian_tuple_shapes():
     assert w.shape == (mol.idxi.numel(), 10, 10)
     assert e.shape == (mol.nmol, n4)
     assert torch.allclose(F, F.transpose(1, 2))
+
+
+@pytest.mark.parametrize("name", ["pdir_pm6sp_star_params", "pdir_pm6sp_star"])
+def test_parameter_file_dir_matches_reference(name, tmp_path):
+    """seqm_parameters['parameter_file_dir']: the reference's STAR parameter set of PM6_SP read
+    from MOPAC-format files (as PM6_SP with its PWCCT file, and as PM6_SP_STAR): energies,
+    forces and charges against the reference's run on the same files."""
+    from conftest import write_param_dir
+    from pyseqm_gb300 import Electronic_Structure
+
+    g = load_golden(name)
+    s = dict(g["settings"], parameter_file_dir=write_param_dir(g, tmp_path))
+    mol, s = _molecule(g, s)
+    Electronic_Structure(s).cuda()(mol)
+    ref = g["ref"]
+    for key in ("Etot", "Eelec", "Enuc", "Hf", "Eiso"):
+        np.testing.assert_allclose(getattr(mol, key).detach().cpu().numpy(), ref[key], atol=1e-6, rtol=0)
+    np.testing.assert_allclose(mol.force.cpu().numpy(), np.asarray(ref["force"]), atol=1e-6, rtol=0)
+    np.testing.assert_allclose(mol.q.cpu().numpy(), np.asarray(ref["q"]), atol=1e-7, rtol=0)

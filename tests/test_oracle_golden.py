@@ -184,6 +184,30 @@ def test_oracle_excited_forces_match_reference_test_values(name):
     np.testing.assert_allclose(f, np.asarray(g["reference_test_json"]["force"]), atol=1e-5, rtol=1e-5)
 
 
+@pytest.mark.parametrize("name", ["pdir_pm6sp_star_params", "pdir_pm6sp_star"])
+def test_oracle_parameter_file_dir_matches_reference(name, tmp_path):
+    """parameter_file_dir: the reference's STAR parameter set of PM6_SP read from files (as
+    method PM6_SP, and as PM6_SP_STAR without diatomic parameters); the oracle takes the files'
+    values as per-atom parameters: energies 1e-6 eV, densities 1e-7, exact iteration counts."""
+    from conftest import write_param_dir
+    from pyseqm_gb300 import tables
+
+    g = load_golden(name)
+    s, ref = g["settings"], g["ref"]
+    d = write_param_dir(g, tmp_path)
+    fields, rows = tables.read_parameter_csv(f"{d}parameters_{s['method']}_MOPAC.csv",
+                                             tables.METHOD_FIELDS[s["method"]])
+    Z = g["species_np"][g["species_np"] > 0]
+    learned = {f: rows[Z, k] for k, f in enumerate(fields)}
+    out = O.single_point(s["method"], g["species_np"], g["coords_np"], s["scf_eps"], tuple(s["scf_converger"]),
+                         learned=learned)
+    for key in ("Etot", "Eelec", "Enuc", "Hf", "Eiso"):
+        np.testing.assert_allclose(out[key], ref[key], atol=1e-6, rtol=0)
+    for m in range(g["species_np"].shape[0]):
+        np.testing.assert_allclose(_packed(out, m), np.asarray(ref["P"][m]), atol=1e-7, rtol=0)
+    assert int(np.max(out["iters"])) == ref["loop_count"]
+
+
 def test_oracle_nac_matches_reference():
     """CIS nonadiabatic couplings: the oracle's central differences of sum B_ij F(R; P) over
     E_j - E_i against the reference's calc_nac, to 1e-6 up to one sign per molecule and pair

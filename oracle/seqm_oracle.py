@@ -1124,6 +1124,27 @@ def pair_nuclear_energy(method, mol, p, gam, el, rho0=None):
     return e
 
 
+def dispersion_am1_fs1(mol):
+    """AM1-FS1 dispersion energy per molecule, eV (dispersion_am1_fs1.py:16-113): over the
+    pairs, -sqrt(C6_i C6_j) (a0 r)^-6 f, f = sigmoid(1000 (a0 r / (1.1058892 (R0_i + R0_j)) - 1))
+    clipped to 1 / 0 beyond +-12 ln 10; Grimme 2006 C6 (J nm^6 / mol), R0 (A)."""
+    with open(os.path.join(_DATA, "grimme_2006_b97d.json")) as f:
+        rows = np.asarray(json.load(f)["rows"], dtype=np.float64)
+    c6 = np.zeros(120)
+    r0 = np.zeros(120)
+    c6[: rows.shape[0]], r0[: rows.shape[0]] = rows[:, 0], rows[:, 1]
+    ni, nj = mol["ni"], mol["nj"]
+    R = mol["rij"] * A0
+    arg = 1000.0 * (R / (1.1058892 * (r0[ni] + r0[nj])) - 1.0)
+    f = 1.0 / (1.0 + np.exp(-np.clip(arg, -700.0, 700.0)))
+    tol = 12.0 * math.log(10.0)
+    f = np.where(arg > tol, 1.0, np.where(arg < -tol, 0.0, f))
+    e = -np.sqrt(c6[ni] * c6[nj]) * R**-6.0 * f
+    out = np.zeros(mol["nmol"])
+    np.add.at(out, mol["pair_molid"], e)
+    return out * 1.036426966e-5 * 1.0e6
+
+
 def isolated_atom_energy(Z, p, el):
     """energy.py:8-23."""
     return (p["U_ss"] * el["ussc"][Z] + p["U_pp"] * el["uppc"][Z] + p["g_ss"] * el["gssc"][Z]
@@ -1131,8 +1152,9 @@ def isolated_atom_energy(Z, p, el):
             + p["h_sp"] * el["hspc"][Z])
 
 
-def energy_at(method, mol, p, P, el=None):
-    """All energy terms for a given density P (no SCF): integrals -> hcore -> fock -> E."""
+def energy_at(method, mol, p, P, el=None, dispersion=False):
+    """All energy terms for a given density P (no SCF): integrals -> hcore -> fock -> E;
+    dispersion: AM1-FS1 added to Etot and Hf (basics.py:1233-1234)."""
     el = el or load_elements()
     ints = integrals(mol, p, el)
     M = hcore(mol, p, ints)
@@ -1149,11 +1171,13 @@ def energy_at(method, mol, p, P, el=None):
     eheat = np.zeros(nmol)
     np.add.at(eheat, mol["atom_molid"], el["eheat_ev"][mol["Z"]])
     Etot = Eelec + Enuc
+    if dispersion and method == "AM1":
+        Etot = Etot + dispersion_am1_fs1(mol)
     return dict(Eelec=Eelec, Enuc=Enuc, Etot=Etot, Eiso=Eiso_sum, Hf=Etot - Eiso_sum + eheat, F=F, M=M, ints=ints)
 
 
 def single_point(method, species, coords, eps, converger=(1,), sp2_opt=(False,), charges=None, learned=None,
-                 forces=False, fd_step=1.0e-5, mult=None, cutoff=None):
+                 forces=False, fd_step=1.0e-5, mult=None, cutoff=None, dispersion=False):
     """Full single point: parse -> hcore -> SCF -> energies (+ fixed-density forces).
 
     Forces are -dHf/dR at the converged density, by central finite differences of
@@ -1166,7 +1190,7 @@ def single_point(method, species, coords, eps, converger=(1,), sp2_opt=(False,),
     ints = integrals(mol, p, el)
     M = hcore(mol, p, ints)
     P, nc, iters = scf(mol, p, ints, M, eps, converger, sp2_opt, el=el)
-    out = energy_at(method, mol, p, P, el)
+    out = energy_at(method, mol, p, P, el, dispersion)
     if mol["uhf"]:  # orbital energies per spin, (nmol, 2, n)
         e = np.stack([density_eigh(out["F"][:, s], mol["nheavy"], mol["nhyd"], mol["nocc"][:, s])[1]
                       for s in range(2)], axis=1)
@@ -1174,11 +1198,12 @@ def single_point(method, species, coords, eps, converger=(1,), sp2_opt=(False,),
         _, e, vecs = density_eigh(out["F"], mol["nheavy"], mol["nhyd"], mol["nocc"])
     out.update(P=P, notconverged=nc, iters=iters, e=e, mol=mol, params=p)
     if forces:
-        out["force"] = fd_forces(method, species, coords, P, charges, learned, fd_step, mult, cutoff)
+        out["force"] = fd_forces(method, species, coords, P, charges, learned, fd_step, mult, cutoff, dispersion)
     return out
 
 
-def fd_forces(method, species, coords, P, charges=None, learned=None, h=1.0e-5, mult=None, cutoff=None):
+def fd_forces(method, species, coords, P, charges=None, learned=None, h=1.0e-5, mult=None, cutoff=None,
+              dispersion=False):
     """-dHf/dR (eV/Angstrom) at fixed density by central differences."""
     coords = np.asarray(coords, dtype=np.float64)
     species = np.asarray(species)
@@ -1195,6 +1220,6 @@ def fd_forces(method, species, coords, P, charges=None, learned=None, h=1.0e-5, 
                     c[m, a, x] += sgn * h
                     mol = parse(species, c, charges, mult, cutoff)
                     p = atom_params(method, mol["Z"], learned)
-                    vals.append(energy_at(method, mol, p, P, el)["Hf"][m])
+                    vals.append(energy_at(method, mol, p, P, el, dispersion)["Hf"][m])
                 f[m, a, x] = -(vals[0] - vals[1]) / (2.0 * h)
     return f

@@ -21,6 +21,7 @@ forces).  PM6 with d orbitals and scf_backward >= 1 raise NotImplementedError.
 """
 
 import copy
+import math
 import time
 
 import numpy as np
@@ -527,6 +528,38 @@ def _active_states(molecule, nmol, device):
     return torch.full((nmol,), int(a or 0), dtype=torch.long, device=device)
 
 
+FS1_SR, FS1_D = 1.1058892, 1000.0  # AM1-FS1 damping constants (dispersion_am1_fs1.py:9-10)
+FS1_D_TOL = 12.0 * math.log(10.0)  # the damping is clipped to 0 / 1 past this argument
+EV_PER_J_PER_MOL = 1.036426966e-5
+
+
+def _dispersion_am1_fs1(L, xyz):
+    """AM1-FS1 dispersion energy per molecule in eV (dispersion_am1_fs1.py:16-113; Foster and
+    Sohlberg, J. Chem. Theory Comput. 6, 2153 (2010)): over the kept pairs,
+    -sqrt(C6_i C6_j) / R^6 f(R), f = 1 / (1 + exp(-d (R / (S_R (R0_i + R0_j)) - 1))) set to 1 / 0
+    where the argument is beyond +-12 ln 10, with Grimme's 2006 C6 (J nm^6 / mol) and R0 (A).
+    Differentiable in xyz (real atoms, Angstrom), so the forces follow by autograd."""
+    dev = xyz.device
+    if getattr(L, "_fs1", None) is None or L._fs1[0].device != dev:
+        c6, r0 = tables.grimme_c6_r0()
+        keep = np.ones(L.npairs, dtype=bool) if L.pair_skip is None else ~L.pair_skip
+        pi, pj = L.pair_i[keep], L.pair_j[keep]
+        zi, zj = L.Z[pi], L.Z[pj]
+        c6z = lambda z: np.where(z < c6.size, c6[np.minimum(z, c6.size - 1)], 0.0)  # noqa: E731
+        r0z = lambda z: np.where(z < r0.size, r0[np.minimum(z, r0.size - 1)], 0.0)  # noqa: E731
+        t = lambda a, dt=torch.float64: torch.as_tensor(a, dtype=dt, device=dev)  # noqa: E731
+        L._fs1 = (t(pi, torch.int64), t(pj, torch.int64), t(np.sqrt(c6z(zi) * c6z(zj))), t(r0z(zi) + r0z(zj)),
+                  t(L.atom_mol[pi], torch.int64))
+    pi, pj, c6ij, rv, mol = L._fs1
+    R = torch.linalg.norm(xyz[pj] - xyz[pi], dim=1)
+    arg = FS1_D * (R / (FS1_SR * rv) - 1.0)
+    f = torch.sigmoid(arg)
+    f = torch.where(arg > FS1_D_TOL, torch.ones_like(f), f)
+    f = torch.where(arg < -FS1_D_TOL, torch.zeros_like(f), f)
+    e = -c6ij * R.pow(-6.0) * f
+    return torch.zeros(L.nmol, dtype=e.dtype, device=dev).index_add(0, mol, e) * (EV_PER_J_PER_MOL * 1.0e6)
+
+
 def _isolated_atom_energy(const, Z, p):
     """energy.py:8-23 (differentiable in the parameters)."""
     return (p["U_ss"] * const.ussc[Z] + p["U_pp"] * const.uppc[Z] + p["g_ss"] * const.gssc[Z]
@@ -828,6 +861,8 @@ class Energy(torch.nn.Module):
             Eexc = self._active_energy(molecule, s, act, xyz)
         if all_terms:
             Etot = Eelec + Enuc if Eexc is None else Eelec + Enuc + Eexc
+            if self.seqm_parameters.get("dispersion", False) and self.method == "AM1":  # basics.py:1233-1234
+                Etot = Etot + _dispersion_am1_fs1(L, xyz).to(dev)
             Eiso = _isolated_atom_energy(molecule.const, molecule.Z, p)
             Eiso_sum = torch.zeros_like(Etot).index_add(0, molecule.atom_molid, Eiso)
             if self.Hf_flag:

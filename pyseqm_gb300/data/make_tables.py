@@ -12,6 +12,7 @@ reads them from a PYSEQM checkout and writes them as JSON:
                               seqm/seqm_functions/parameters.py:4-46 parses them
                               (float64 here; the reference parses into the torch
                               default dtype).
+  * ``grimme_2006_b97d.json`` <- seqm/params/grimme_2006_b97-d.csv (C6, R0 of AM1-FS1)
   * ``pwcct_<M>.json``     <- seqm/params/PWCCT_<M>_MOPAC.csv (PM6_SP), parsed the way
                               PWCCT (parameters.py:49-87) parses it: alp[Z1][Z2] is the
                               third column, chi[Z1][Z2] the fourth, for the listed (Z1, Z2)
@@ -85,6 +86,19 @@ def main(ref_root):
         with open(os.path.join(here, f"pwcct_{method}.json"), "w") as f:
             json.dump({"method": method, "zmax": max(max(e[0], e[1]) for e in entries),
                        "columns": ["Z1", "Z2", "alp", "chi"], "entries": nonzero}, f, separators=(",", ":"))
+
+    # C6 (J nm^6 / mol) and R0 (Angstrom) of Grimme's 2006 dispersion correction, which AM1-FS1
+    # reads (dispersion_am1_fs1.py:77-113); the file starts with a byte-order mark
+    c6r0 = {}
+    with open(os.path.join(ref_root, "seqm", "params", "grimme_2006_b97-d.csv"), encoding="utf-8-sig") as f:
+        f.readline()
+        for line in f:
+            t = line.strip().replace(" ", "").split(",")
+            if len(t) >= 4 and t[0]:
+                c6r0[int(t[0])] = [float(t[2]), float(t[3])]
+    zmax = max(c6r0)
+    with open(os.path.join(here, "grimme_2006_b97d.json"), "w") as f:
+        json.dump({"columns": ["C_6", "R_0"], "rows": [c6r0.get(z, [0.0, 0.0]) for z in range(zmax + 1)]}, f)
 
     sys.path.insert(0, ref_root)
     import types

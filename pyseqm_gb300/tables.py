@@ -132,3 +132,12 @@ def pair_par(method, param_dir=None):
     an[: min(n, src.size)] = src[: min(n, src.size)]
     c = an ** (1.0 / 3.0)
     return np.stack([alp, chi, c[:, None] + c[None, :]], axis=-1).reshape(-1), n - 1
+
+
+@functools.lru_cache(maxsize=None)
+def grimme_c6_r0():
+    """(C6 [J nm^6 / mol], R0 [Angstrom]) per atomic number of Grimme's 2006 dispersion
+    correction (the table AM1-FS1 reads, dispersion_am1_fs1.py:77-113)."""
+    with open(os.path.join(_DATA, "grimme_2006_b97d.json")) as f:
+        rows = np.asarray(json.load(f)["rows"], dtype=np.float64)
+    return rows[:, 0], rows[:, 1]

@@ -551,6 +551,11 @@ def main():
     write_param_dir("pdir_pm6sp_star_params", *workloads.pad_batch(mols), "PM6_SP", star, "PM6_SP")
     write_param_dir("pdir_pm6sp_star", *workloads.pad_batch(mols), "PM6_SP_STAR", star, "PM6_SP")
 
+    # AM1-FS1 dispersion correction (seqm_parameters['dispersion'])
+    mols = workloads.mixed_batch(6, seed=3, alkane_range=(2, 8), water_range=(3, 9))
+    write("disp_am1_fs1", *workloads.pad_batch(mols),
+          {"method": "AM1", "scf_eps": 1e-8, "scf_converger": [1], "dispersion": True})
+
     # the parser's pair_outer_cutoff: pairs at or beyond 3 A are dropped from every term
     mols = workloads.mixed_batch(6, seed=3, alkane_range=(2, 8), water_range=(3, 9))
     write("mixed_am1_cutoff", *workloads.pad_batch(mols),

@@ -45,7 +45,7 @@ def test_force_modes_match_reference_test_values(name, mode):
 
 
 @pytest.mark.parametrize("name", ["smoke_MNDO", "smoke_AM1", "smoke_PM3", "batch_am1", "force_methanal_am1",
-                                  "force_mixed_am1", "force_methane_am1", "mixed_am1_cutoff", "mixed_pm6sp", "ions_pm6sp", "hetero_pm6sp", "hetero_am1",
+                                  "force_mixed_am1", "force_methane_am1", "mixed_am1_cutoff", "disp_am1_fs1", "mixed_pm6sp", "ions_pm6sp", "hetero_pm6sp", "hetero_am1",
                                   "hetero_pm3"])
 def test_electronic_structure_matches_reference(name):
     from pyseqm_gb300 import Electronic_Structure

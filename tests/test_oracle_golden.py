@@ -208,6 +208,22 @@ def test_oracle_parameter_file_dir_matches_reference(name, tmp_path):
     assert int(np.max(out["iters"])) == ref["loop_count"]
 
 
+def test_oracle_dispersion_matches_reference():
+    """AM1-FS1 (seqm_parameters['dispersion']): energies with the dispersion term against the
+    reference to 1e-6 eV (Enuc and Eelec without it), and the fixed-density forces of the first
+    molecule against the reference's autograd forces to 1e-5 eV/A."""
+    g = load_golden("disp_am1_fs1")
+    s, ref = g["settings"], g["ref"]
+    out = O.single_point(s["method"], g["species_np"], g["coords_np"], s["scf_eps"], tuple(s["scf_converger"]),
+                         dispersion=True)
+    for key in ("Etot", "Eelec", "Enuc", "Hf", "Eiso"):
+        np.testing.assert_allclose(out[key], ref[key], atol=1e-6, rtol=0)
+    assert np.abs(out["Etot"] - out["Eelec"] - out["Enuc"]).min() > 1e-3  # the term is there
+    na = int(np.sum(g["species_np"][0] > 0))
+    f = O.fd_forces(s["method"], g["species_np"][:1, :na], g["coords_np"][:1, :na], out["P"][:1], dispersion=True)
+    np.testing.assert_allclose(f[0], np.asarray(ref["force"])[0, :na], atol=1e-5, rtol=0)
+
+
 def test_oracle_nac_matches_reference():
     """CIS nonadiabatic couplings: the oracle's central differences of sum B_ij F(R; P) over
     E_j - E_i against the reference's calc_nac, to 1e-6 up to one sign per molecule and pair

@@ -751,6 +751,54 @@ class Energy(torch.nn.Module):
                 out[(a - 1, b - 1)] = (full.view(L.nmol, L.molsize, 3) / d[:, None, None]).to(dev)
         return out
 
+    def _all_forces(self, molecule, solve, xyz):
+        """do_all_forces (basics.py:1124-1158): molecule.all_forces (nmol, nroots + 1, molsize, 3),
+        the ground state's forces and those of every excited state, and each state's relaxed and
+        unrelaxed dipoles (make_cis_state_dipole, rcis_grad_batch.py:266-288; Debye)."""
+        if not self.seqm_parameters.get("analytical_gradient", [False])[0]:
+            raise Exception("when asking for calculating all gradients of excited states ask for analytical gradients")
+        if not self.excited_states:
+            raise Exception("do_all_forces needs excited_states")
+        ex = molecule._excited
+        if ex.window is not None:
+            raise NotImplementedError("excited-state forces with an orbital_window are not supported")
+        L = solve.L
+        dev = molecule.coordinates.device
+        rpa = self.excited_states["method"] == "rpa"
+        amp = molecule.cis_amplitudes.to(solve.dev)
+        nroots = int(self.excited_states["n_states"])
+        real = torch.as_tensor(L.real_index, device=solve.dev)
+        ones = torch.ones(L.nmol, dtype=torch.float64, device=solve.dev)
+        tol = float(self.excited_states["tolerance"])
+
+        def padded(g):
+            full = torch.zeros(L.nmol * L.molsize, 3, dtype=torch.float64, device=solve.dev)
+            full[real] = g
+            return full.view(L.nmol, L.molsize, 3)
+
+        with torch.no_grad():
+            ground, _ = solve.grad(ones, ones)
+        if self.seqm_parameters.get("dispersion", False) and self.method == "AM1":
+            x = xyz.detach().clone().requires_grad_(True)
+            with torch.enable_grad():
+                gd, = torch.autograd.grad(_dispersion_am1_fs1(L, x).sum(), x)
+            ground = ground + gd.to(solve.dev)
+        forces = torch.empty(L.nmol, nroots + 1, L.molsize, 3, dtype=torch.float64, device=solve.dev)
+        forces[:, 0] = -padded(ground)
+        relaxed = torch.empty(L.nmol, nroots, 3, dtype=torch.float64, device=solve.dev)
+        unrelaxed = torch.empty_like(relaxed)
+        dip0 = molecule.dipole.to(solve.dev)
+        with torch.no_grad():
+            for k in range(nroots):
+                X, Y = (amp[0, :, k], amp[1, :, k]) if rpa else (amp[:, k], None)
+                R, B, D = ex.state_densities(X, Y, tol)
+                forces[:, k + 1] = -padded(ground + solve.grad_excited(ones, ex.to_ragged(D), ex.to_ragged(R)))
+                mu = ex.dipole_contract(torch.stack((B, D), dim=1)) * (TO_DEBYE * DEBYE_TO_AU)
+                unrelaxed[:, k], relaxed[:, k] = mu[:, 0] + dip0, mu[:, 1] + dip0
+        molecule.all_forces = forces.to(dev)
+        molecule.all_cis_relaxed_diploles = relaxed.to(dev)
+        molecule.all_cis_unrelaxed_diploles = unrelaxed.to(dev)
+
     def _active_energy(self, molecule, solve, act, xyz):
         """Excitation energy of each molecule's active state as a differentiable function of the
         coordinates (its gradient from ExcitedEnergyFunction)."""
@@ -851,6 +899,8 @@ class Energy(torch.nn.Module):
         molecule._solve = s
         if self.excited_states:
             self._excited(molecule, s)
+        if self.seqm_parameters.get("do_all_forces", False):
+            self._all_forces(molecule, s, xyz)
         act = _active_states(molecule, L.nmol, dev)
         Eexc = None
         if bool((act > 0).any()):

@@ -418,6 +418,16 @@ class ExcitedStates:
                     sp_b=torch.as_tensor(sp_b.reshape(nmol, -1), device=dev),
                     dd=torch.where(hv >= 0, dd[hv.clamp(min=0)], 0.0))
 
+    def dipole_contract(self, R):
+        """sum_mn R_mn D^d_mn for padded matrices R (nmol, k, nmax, nmax) with the one-centre
+        dipole integrals of calc_dipole_matrix (dipole.py:7-82): (nmol, k, 3), Angstrom x charge."""
+        g = self._dipole_geometry()
+        nmol, k = R.shape[0], R.shape[1]
+        mu = -torch.einsum("bkn,bnd->bkd", torch.diagonal(R, dim1=2, dim2=3), g["ao_xyz"])
+        Rf = R.reshape(nmol, k, -1)
+        sp = Rf.gather(2, g["sp_a"][:, None, :].expand(-1, k, -1)) + Rf.gather(2, g["sp_b"][:, None, :].expand(-1, k, -1))
+        return mu - torch.einsum("bkhd,bh->bkd", sp.view(nmol, k, -1, 3), g["dd"])
+
     def transition_properties(self, E, amp, rpa=False):
         """Transition dipoles (atomic units, (nmol, kmax, 3)) and oscillator strengths (nmol, kmax)
         of the roots, as calc_transition_dipoles (rcis_batch.py:679-710, rcis_new.py:547-585):
@@ -425,19 +435,8 @@ class ExcitedStates:
         one-centre dipole integrals of calc_dipole_matrix (dipole.py:7-82: -R_A on the diagonal of
         atom A's AOs, -dd_A between its s and p_d), mu = sqrt(2)/a0 sum R.D and
         f = 2/3 (E / 27.2113962) |mu|^2; zero for the padding roots of a molecule."""
-        g = self._dipole_geometry()
-        nmol = self.nmol
-        X = amp[0] if rpa else amp
-        k = X.shape[1]
-        R = self.Co[:, None] @ X.view(nmol, k, self.no, self.nv) @ self.Cv.transpose(1, 2)[:, None]
-        if rpa:
-            Y = amp[1].view(nmol, k, self.no, self.nv)
-            R = R + self.Cv[:, None] @ Y.transpose(2, 3) @ self.Co.transpose(1, 2)[:, None]
-        mu = -torch.einsum("bkn,bnd->bkd", torch.diagonal(R, dim1=2, dim2=3), g["ao_xyz"])
-        Rf = R.reshape(nmol, k, -1)
-        sp = Rf.gather(2, g["sp_a"][:, None, :].expand(-1, k, -1)) + Rf.gather(2, g["sp_b"][:, None, :].expand(-1, k, -1))
-        mu = mu - torch.einsum("bkhd,bh->bkd", sp.view(nmol, k, -1, 3), g["dd"])
-        mu = mu * (math.sqrt(2.0) / A0_ANGSTROM)
+        k = (amp[0] if rpa else amp).shape[1]
+        mu = self.dipole_contract(self.transition_densities(amp, rpa)) * (math.sqrt(2.0) / A0_ANGSTROM)
         ok = (torch.arange(k, device=E.device)[None, :] < torch.as_tensor(self.roots, device=E.device)[:, None])
         mu = mu * ok[..., None]
         f = (2.0 / 3.0) * E / HARTREE_NEXMD * (mu * mu).sum(-1) * ok

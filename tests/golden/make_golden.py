@@ -375,6 +375,29 @@ def write_param_dir(name, species, coords, method, src_dir, file_method):
     print(name, "loop_count", ref["loop_count"])
 
 
+def write_all_forces(name, xyz_names, settings):
+    """do_all_forces through the reference's Electronic_Structure (basics.py:1124-1158): the
+    ground and every excited state's forces and the states' relaxed / unrelaxed dipoles."""
+    if ONLY and name not in ONLY:
+        return
+    data = os.path.join(REF, "tests", "data")
+    species, coords = read_xyz([os.path.join(data, x) for x in xyz_names])
+    species, coords = np.asarray(species), np.asarray(coords, dtype=np.float64)
+    sp = dict(settings)
+    sp["excited_states"] = dict(settings["excited_states"])
+    mol = Molecule(Constants(), sp, torch.as_tensor(coords.copy()), torch.as_tensor(species, dtype=torch.int64))
+    mol.verbose = False
+    Electronic_Structure(sp)(mol)
+    rec = dict(name=name, settings=settings, species=species.tolist(), coords=coords.tolist(),
+               ref=dict(all_forces=mol.all_forces.detach().numpy().tolist(),
+                        relaxed=mol.all_cis_relaxed_diploles.detach().numpy().tolist(),
+                        unrelaxed=mol.all_cis_unrelaxed_diploles.detach().numpy().tolist(),
+                        dipole=mol.dipole.detach().numpy().tolist(), cis_energies=mol.cis_energies.numpy().tolist()))
+    with open(os.path.join(HERE, f"{name}.json"), "w") as f:
+        json.dump(rec, f)
+    print(name, "all_forces", np.asarray(rec["ref"]["all_forces"]).shape)
+
+
 def write_xlbomd(name, species, coords, settings, steps, timestep, seed, k, krylov=None):
     """A short XL-BOMD trajectory (no thermostat, no Krylov kernel) through the reference's XL_BOMD
     driver: the first step's SCF, then the auxiliary density propagated with the k-th order
@@ -634,6 +657,13 @@ def main():
                        "md_excited_basic_batch_methanal.json", {"drift": 5e-2, "slope": 5e-2}, excited)
     write_reference_md("md_ref_excited_langevin_methanal", methanal, "langevin", {"damp": 10.0}, 80, None, None,
                        excited)
+
+    # forces of the ground and all excited states (do_all_forces), CIS and RPA
+    for es in ("cis", "rpa"):
+        write_all_forces(f"cis_allforces_{es}_am1_methanal", [f"methanal.{i}.xyz" for i in (1, 2, 3)],
+                         {"method": "AM1", "scf_eps": 1e-9, "scf_converger": [1],
+                          "excited_states": {"n_states": 3, "method": es, "tolerance": 1e-8},
+                          "analytical_gradient": [True], "do_all_forces": True})
 
     # CIS nonadiabatic couplings of a batch of one species (the reference's calc_nac needs one)
     write_nac("cis_nac_am1_methanal", [f"methanal.{i}.xyz" for i in (1, 2, 3)],

@@ -226,3 +226,20 @@ def test_phase_alignment_and_saved_transition_densities():
     es(mol)
     ov = (mol.cis_amplitudes * a0).sum(-1)
     assert bool((ov >= 0).all()), ov
+
+
+
+@pytest.mark.parametrize("name", ["cis_allforces_cis_am1_methanal", "cis_allforces_rpa_am1_methanal"])
+def test_all_state_forces_match_reference(name):
+    """do_all_forces: the ground state's and every excited state's forces, and the states'
+    relaxed and unrelaxed dipoles, against the reference (tight settings: 1e-6)."""
+    from pyseqm_gb300 import Electronic_Structure
+
+    g = load_golden(name)
+    mol, s = _excited_molecule(g)
+    Electronic_Structure(s).cuda()(mol)
+    ref = g["ref"]
+    np.testing.assert_allclose(mol.cis_energies.cpu().numpy(), ref["cis_energies"], atol=1e-6, rtol=0)
+    np.testing.assert_allclose(mol.all_forces.cpu().numpy(), np.asarray(ref["all_forces"]), atol=1e-6, rtol=0)
+    np.testing.assert_allclose(mol.all_cis_relaxed_diploles.cpu().numpy(), ref["relaxed"], atol=1e-6, rtol=0)
+    np.testing.assert_allclose(mol.all_cis_unrelaxed_diploles.cpu().numpy(), ref["unrelaxed"], atol=1e-6, rtol=0)

@@ -208,6 +208,18 @@ def test_oracle_parameter_file_dir_matches_reference(name, tmp_path):
     assert int(np.max(out["iters"])) == ref["loop_count"]
 
 
+def test_oracle_all_state_forces_match_reference():
+    """do_all_forces, CIS: the oracle's Richardson central differences of E_ground + omega_k for
+    every state k against the reference's relaxed analytic forces (1e-5 eV/A)."""
+    from oracle import seqm_excited as X
+
+    g = load_golden("cis_allforces_cis_am1_methanal")
+    ref = np.asarray(g["ref"]["all_forces"])
+    for k in range(1, ref.shape[1]):
+        f = X.excited_forces_fd("AM1", g["species_np"], g["coords_np"], 1e-11, k)
+        np.testing.assert_allclose(f, ref[:, k], atol=1e-5, rtol=0)
+
+
 def test_oracle_dispersion_matches_reference():
     """AM1-FS1 (seqm_parameters['dispersion']): energies with the dispersion term against the
     reference to 1e-6 eV (Enuc and Eelec without it), and the fixed-density forces of the first

@@ -113,10 +113,10 @@ XL_COEFFS = {
 }
 
 
-def xl_energy(method, species, coords, P, D=None):
+def xl_energy(method, species, coords, P, D=None, sp2_eps=None):
     """Shadow energy of XL-BOMD (dynamics/xlbomd.py:58-505 without the Krylov kernel): F = F(P),
-    D from the eigensolve of F unless given, Eelec = tr(D F) - 1/2 tr((F - H) P)
-    (energy.py:76-88); returns Hf, Etot per molecule and D."""
+    D from the eigensolve of F (or SP2 purification to sp2_eps, xlbomd.py:349-357) unless given,
+    Eelec = tr(D F) - 1/2 tr((F - H) P) (energy.py:76-88); returns Hf, Etot per molecule and D."""
     el = O.load_elements()
     mol = O.parse(species, coords)
     p = O.atom_params(method, mol["Z"])
@@ -125,7 +125,9 @@ def xl_energy(method, species, coords, P, D=None):
     nmol, ms = mol["nmol"], mol["molsize"]
     H = O.symmetrize_upper(O.blocks_to_full(M, nmol, ms))
     F = O.fock(mol, p, ints, M, P)
-    if D is None:
+    if D is None and sp2_eps is not None:
+        D = O.density_sp2(F, mol["nheavy"], mol["nhyd"], mol["nocc"], sp2_eps)
+    elif D is None:
         D, _, _ = O.density_eigh(F, mol["nheavy"], mol["nhyd"], mol["nocc"])
     Eelec = np.sum(D * F - 0.5 * (F - H) * P, axis=(1, 2))
     EnucAB = O.pair_nuclear_energy(method, mol, p, ints["w"][:, 0, 0], el, ints["rho0"])
@@ -139,16 +141,18 @@ def xl_energy(method, species, coords, P, D=None):
     return dict(Etot=Etot, Hf=Etot - Eiso + eheat, D=D)
 
 
-def xl_trajectory(method, species, coords, v0, steps, dt, eps, k, converger=(1,), h=1.0e-5):
+def xl_trajectory(method, species, coords, v0, steps, dt, eps, k, converger=(1,), h=1.0e-5, sp2_eps=None):
     """XL-BOMD without thermostat (MolecularDynamics.py:1434-1600): the first forces and density
     from the SCF, then the auxiliary density propagated with the k-th order coefficients and the
-    shadow-potential forces by central differences at fixed D and P."""
+    shadow-potential forces by central differences at fixed D and P.  sp2_eps: the SCF and the
+    shadow density use SP2 purification (the seqm sp2 option)."""
     species = np.asarray(species)
     r = np.array(coords, dtype=np.float64)
     mass = masses(species)
     minv = np.where(mass > 0, 1.0 / np.where(mass > 0, mass, 1.0), 0.0)
     v = zero_com(mass, r, np.array(v0, dtype=np.float64), remove_angular=True, restore_kinetic_energy=False)
-    out = O.single_point(method, species, r, eps, converger, forces=True)
+    sp2_opt = (True, sp2_eps) if sp2_eps is not None else (False,)
+    out = O.single_point(method, species, r, eps, converger, sp2_opt=sp2_opt, forces=True)
     f, dm = out["force"], out["P"]
     a = f * minv * ACC_SCALE
     traj = [dict(coordinates=r.copy(), velocities=v.copy(), force=f, Etot=out["Etot"], Ek=kinetic_energy(mass, v))]
@@ -166,7 +170,7 @@ def xl_trajectory(method, species, coords, v0, steps, dt, eps, k, converger=(1,)
         c = step % m
         P = kappa * (0.95 * dm + 0.05 * P) + np.tensordot(coeff[c: c + m], Pt, axes=1)
         Pt[m - 1 - c] = P
-        e0 = xl_energy(method, species, r, P)
+        e0 = xl_energy(method, species, r, P, sp2_eps=sp2_eps)
         dm = e0["D"]
         f = np.zeros_like(r)
         for mi in range(r.shape[0]):

@@ -993,9 +993,17 @@ def _xl_bomd_force(molecule, P, seqm_parameters, xl_params=None):
         Pk = L.padded_to_packed(P.detach().to(dev, torch.float64))
         s.P.copy_(Pk)
         s.fock()  # F(P)
-        evecs = torch.empty_like(s.work)
-        s.density(s.Pnew, (False,), active=None, evecs=evecs, density_only=0)
-        s.evecs = evecs
+        sp2 = tuple(seqm_parameters.get("sp2", [False]))
+        use_sp2 = bool(sp2[0]) and not krylov
+        if use_sp2:
+            # D by SP2 purification (the reference's sp2 branch of EnergyXL, dynamics/xlbomd.py:
+            # 349-357; that branch stops at its own orbital-energy line with an AttributeError,
+            # the density it intends is this one, with zero orbital energies and gaps)
+            s.density(s.Pnew, sp2, active=None, evecs=None, density_only=0)
+        else:
+            evecs = torch.empty_like(s.work)
+            s.density(s.Pnew, (False,), active=None, evecs=evecs, density_only=0)
+            s.evecs = evecs
         D = s.Pnew
         if krylov:
             from .xl_krylov import PaddedBasis, fermi_density, krylov_kernel
@@ -1045,11 +1053,15 @@ def _xl_bomd_force(molecule, P, seqm_parameters, xl_params=None):
         eheat = torch.zeros_like(Etot).index_add(0, molecule.atom_molid, molecule.const.eheat[molecule.Z])
         molecule.Etot, molecule.Eelec, molecule.Enuc, molecule.Eiso = Etot, Eelec.to(cdev), Enuc.to(cdev), Eiso_sum
         molecule.Hf = Etot - Eiso_sum + eheat if seqm_parameters.get("Hf_flag", True) else Etot - Eiso_sum
-        e, v = sv.eigen_padded()
-        lumo = molecule.nocc.unsqueeze(0).T.to(e.device)
-        molecule.e_mo = e.to(cdev)
-        molecule.e_gap = (e.gather(1, lumo) - e.gather(1, lumo - 1)).reshape(-1).to(cdev)
-        molecule.molecular_orbitals = v.to(cdev)
+        if use_sp2:  # no orbitals from SP2 (xlbomd.py:355-356)
+            molecule.e_mo = torch.zeros(L.nmol, int(L.nocc.max()), dtype=torch.float64, device=cdev)
+            molecule.e_gap = torch.zeros(L.nmol, 1, dtype=torch.float64, device=cdev)
+        else:
+            e, v = sv.eigen_padded()
+            lumo = molecule.nocc.unsqueeze(0).T.to(e.device)
+            molecule.e_mo = e.to(cdev)
+            molecule.e_gap = (e.gather(1, lumo) - e.gather(1, lumo - 1)).reshape(-1).to(cdev)
+            molecule.molecular_orbitals = v.to(cdev)
         if krylov:
             molecule.Electronic_entropy = (-2.0 * T_el * S_ent).to(cdev)
             molecule.dP2dt2 = L.packed_to_padded(basis.to_ragged(d2)).to(cdev)

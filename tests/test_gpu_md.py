@@ -212,3 +212,35 @@ def test_md_passes_reference_md_suite(name):
         drift = np.max(np.abs(Etot[:, m] - Etot[0, m]))
         slope = float(np.polyfit(np.arange(len(Etot)), Etot[:, m], 1)[0])
         assert drift <= tol["drift"] and abs(slope) <= tol["slope"], (m, drift, slope)
+
+
+def test_xlbomd_with_sp2_matches_oracle():
+    """XL-BOMD with the sp2 option: the shadow density D by FP64 SP2 purification (the
+    reference's EnergyXL sp2 branch, dynamics/xlbomd.py:349-357, which fails at its orbital-energy
+    line, so the oracle's restatement is the check): 4 steps against the oracle's trajectory,
+    positions and velocities 1e-6, forces 1e-5 eV/A, shadow energies 1e-6 eV; zero gaps."""
+    import torch
+
+    from conftest import load_golden
+    from oracle import seqm_md as MD
+    from pyseqm_gb300 import XL_BOMD, Constants, Molecule
+
+    g = load_golden("md_am1_xlbomd")
+    s = dict(g["settings"], sp2=[True, 1e-7])
+    steps = 4
+    ref = MD.xl_trajectory(s["method"], g["species_np"], g["coords_np"], np.asarray(g["velocities0"]), steps,
+                           g["timestep"], s["scf_eps"], g["k"], sp2_eps=1e-7)
+    mol = Molecule(Constants().cuda(), s, torch.as_tensor(g["coords_np"], device="cuda"),
+                   torch.as_tensor(g["species_np"], device="cuda")).cuda()
+    mol.velocities = torch.as_tensor(np.asarray(g["velocities0"]), device="cuda")
+    md = XL_BOMD(xl_bomd_params={"k": g["k"]}, seqm_parameters=s, timestep=g["timestep"], Temp=0.0,
+                 output={"print every": 0}).cuda()
+    md.initialize(mol)
+    for i, r in enumerate(ref):
+        if i > 0:
+            md._do_integrator_step(i - 1, mol, {})
+            assert not mol.e_gap.any()
+        np.testing.assert_allclose(mol.coordinates.detach().cpu().numpy(), r["coordinates"], atol=1e-6, rtol=0)
+        np.testing.assert_allclose(mol.velocities.detach().cpu().numpy(), r["velocities"], atol=1e-6, rtol=0)
+        np.testing.assert_allclose(mol.force.cpu().numpy(), r["force"], atol=1e-5, rtol=0)
+        np.testing.assert_allclose(mol.Etot.detach().cpu().numpy(), r["Etot"], atol=1e-6, rtol=0)

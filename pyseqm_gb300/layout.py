@@ -156,6 +156,9 @@ class Layout:
         if learned:
             for k, v in learned.items():
                 par[native.PAR[k]] = np.asarray(v, dtype=np.float64).reshape(-1)
+        # the reference's Energy sets rho_core to zero for every method but PM6 with d orbitals
+        # (basics.py:796-809), so the core-core term always takes rho0 here
+        par[native.PAR["rho_core"]] = 0.0
         L.par = par
         return L
 

@@ -10,7 +10,10 @@ per-atom 4x4 blocks inside padded ``(nmol, 4*molsize, 4*molsize)`` matrices,
 hydrogen p-slots zero, atoms of each molecule sorted by descending Z.
 
 The oracle is pinned against outputs of the reference itself
-(``tests/golden/*.json``, made by ``tests/golden/make_golden.py``).
+(``tests/golden/*.json``, made by ``tests/golden/make_golden.py``).  Besides the closed-shell
+path it restates the unrestricted SCF, Pulay DIIS, the PM6_SP core-core term, the pair cutoff,
+the AM1-FS1 dispersion term and the SCF convergence normaliser with super-heavy atoms; the MD and
+excited-state oracles live in ``seqm_md.py`` and ``seqm_excited.py``.
 
 Known, deliberate difference: the adaptive mixer's diagonal renormalisation
 (seqm/seqm_functions/scf_loop.py:396-415) loops until *every* molecule of the

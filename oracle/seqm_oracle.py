@@ -50,7 +50,7 @@ KIND = np.array([[0, 1, 3, 6], [1, 2, 4, 7], [3, 4, 5, 8], [6, 7, 8, 9]])  # foc
 def load_elements():
     with open(os.path.join(_DATA, "elements.json")) as f:
         d = json.load(f)
-    return {k: np.asarray(v, dtype=np.float64) for k, v in d.items()}
+    return {k: np.asarray(v, dtype=np.float64) for k, v in d.items() if k != "label"}
 
 
 def load_params(method):

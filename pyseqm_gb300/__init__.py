@@ -18,4 +18,5 @@ from .basics import (  # noqa: E402,F401
     Parser,
     SCFEnergyFunction,
 )
+from .io import read_xyz, save_xyz  # noqa: E402,F401
 from .dynamics import KSA_XL_BOMD, XL_BOMD, Geometry_Optimization_SD, Molecular_Dynamics_Basic, Molecular_Dynamics_Langevin  # noqa: E402,F401

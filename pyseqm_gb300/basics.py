@@ -54,6 +54,9 @@ class Constants(torch.nn.Module):
                                                    requires_grad=False))
         self.qn_int = torch.nn.Parameter(self.qn.data.to(torch.int64), requires_grad=False)
         self.eheat = torch.nn.Parameter(torch.as_tensor(el["eheat_ev"], dtype=torch.float64), requires_grad=False)
+        self.atomic_num = torch.nn.Parameter(torch.as_tensor(el["atomic_num"], dtype=torch.float64),
+                                             requires_grad=False)
+        self.label = list(el["label"])  # element symbols, spelled as the reference's table (save_xyz)
         self.do_timing = do_timing
         if do_timing:
             self.timing = {"Hcore + STO Integrals": [], "SCF": [], "Force": [], "MD": [], "D*": [], "CIS/RPA": []}

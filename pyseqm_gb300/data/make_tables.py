@@ -120,6 +120,7 @@ def main(ref_root):
     for name in ["tore", "qn", "ussc", "uppc", "gssc", "gspc", "hspc", "gp2c", "gppc", "mass", "atomic_num"]:
         out[name] = [float(v) for v in getattr(c, name).tolist()]
     # heats of formation are stored in kcal/mol; the reference divides by 23.061 at load
+    out["label"] = list(c.label)  # element symbols as the reference's tables spell them
     out["eheat_kcal"] = [float(v) * 23.061 for v in c.eheat.tolist()]
     out["eheat_ev"] = [float(v) for v in c.eheat.tolist()]
     with open(os.path.join(here, "elements.json"), "w") as f:

@@ -78,7 +78,7 @@ def read_pwcct_csv(path):
 def elements():
     with open(os.path.join(_DATA, "elements.json")) as f:
         d = json.load(f)
-    return {k: np.asarray(v, dtype=np.float64) for k, v in d.items()}
+    return {k: (list(v) if k == "label" else np.asarray(v, dtype=np.float64)) for k, v in d.items()}
 
 
 @functools.lru_cache(maxsize=None)

@@ -26,7 +26,7 @@ def load_golden(name):
 # single-point fixtures (molecular dynamics trajectories, md_*, and excited states, cis_* / rpa_*,
 # have their own tests)
 GOLDEN_NAMES = sorted(f[:-5] for f in os.listdir(GOLDEN)
-                      if f.endswith(".json") and not f.startswith(("md_", "cis_", "rpa_", "pdir_", "disp_")))
+                      if f.endswith(".json") and not f.startswith(("md_", "cis_", "rpa_", "pdir_", "disp_", "io_")))
 
 
 def write_param_dir(g, path):

@@ -398,6 +398,47 @@ def write_all_forces(name, xyz_names, settings):
     print(name, "all_forces", np.asarray(rec["ref"]["all_forces"]).shape)
 
 
+def write_xyz_io(name):
+    """The reference's xyz helpers (read_xyz.py:17-48, save_xyz.py:4-45) on its test molecules:
+    the xyz texts, read_xyz's arrays, and the files save_xyz writes (with and without forces)
+    for an AM1 run of methane and benzene, with the energies and forces they print."""
+    if ONLY and name not in ONLY:
+        return
+    import tempfile
+
+    from seqm.seqm_functions.save_xyz import save_xyz as ref_save_xyz
+
+    data = os.path.join(REF, "tests", "data")
+    names = ["methane.xyz", "benzene.xyz", "methanal.1.xyz"]
+    texts = {}
+    for n in names:
+        with open(os.path.join(data, n)) as f:
+            texts[n] = f.read()
+    reads = {}
+    for group in (names[:2], names[2:], names):
+        sp, c = read_xyz([os.path.join(data, n) for n in group])
+        reads["+".join(group)] = dict(species=np.asarray(sp).tolist(), coords=np.asarray(c).tolist())
+    sp, c = read_xyz([os.path.join(data, n) for n in names[:2]])
+    settings = {"method": "AM1", "scf_eps": 1e-8, "scf_converger": [1]}
+    mol = Molecule(Constants(), settings, torch.as_tensor(np.asarray(c, dtype=np.float64)),
+                   torch.as_tensor(np.asarray(sp), dtype=torch.int64))
+    mol.verbose = False
+    Electronic_Structure(settings)(mol)
+    saved = {}
+    with tempfile.TemporaryDirectory() as d:
+        for forces in (False, True):
+            ref_save_xyz(mol, os.path.join(d, "out"), Forces=forces)
+            for i in range(sp.shape[0]):
+                with open(os.path.join(d, f"out.{i}.xyz")) as f:
+                    saved[f"{int(forces)}.{i}"] = f.read()
+    rec = dict(name=name, xyz=texts, read=reads, species=np.asarray(sp).tolist(),
+               coords=np.asarray(c, dtype=np.float64).tolist(), Etot=mol.Etot.detach().numpy().tolist(),
+               force=mol.force.detach().numpy().tolist(), saved=saved)
+    with open(os.path.join(HERE, f"{name}.json"), "w") as f:
+        json.dump(rec, f)
+    print(name, "files", sorted(saved))
+
+
 def write_xlbomd(name, species, coords, settings, steps, timestep, seed, k, krylov=None):
     """A short XL-BOMD trajectory (no thermostat, no Krylov kernel) through the reference's XL_BOMD
     driver: the first step's SCF, then the auxiliary density propagated with the k-th order
@@ -657,6 +698,9 @@ def main():
                        "md_excited_basic_batch_methanal.json", {"drift": 5e-2, "slope": 5e-2}, excited)
     write_reference_md("md_ref_excited_langevin_methanal", methanal, "langevin", {"damp": 10.0}, 80, None, None,
                        excited)
+
+    # the xyz helpers
+    write_xyz_io("io_xyz")
 
     # forces of the ground and all excited states (do_all_forces), CIS and RPA
     for es in ("cis", "rpa"):

@@ -476,28 +476,10 @@ def _phase_align(new_amp, ref_amp, rpa=False):
 
 
 def nac_pairs(seqm_parameters, nroots):
-    """1-based state pairs of the nonadiabatic couplings asked for, or None (resolve_nac_config,
-    dynamics/nac_utils.py:29-63): seqm_parameters['nonadiabatic'] with 'compute_nac', 'states'
-    (all their pairs) and 'pairs'; all pairs of the nroots states when enabled without either."""
-    cfg = dict(seqm_parameters.get("nonadiabatic", {}))
-    enabled = bool(cfg.get("compute_nac", False))
-    pairs = []
-    states = cfg.get("states")
-    if states:
-        u = sorted({int(x) for x in states if isinstance(x, (int, float))})
-        pairs += [(u[a], u[b]) for a in range(len(u)) for b in range(a + 1, len(u))]
-    for st in cfg.get("pairs") or []:
-        if isinstance(st, (list, tuple)) and len(st) == 2:
-            pairs.append((int(st[0]), int(st[1])))
-    if enabled and not pairs and nroots:
-        pairs = [(a, b) for a in range(1, nroots + 1) for b in range(a + 1, nroots + 1)]
-    out = []
-    for s1, s2 in pairs:
-        a, b = sorted((int(s1), int(s2)))
-        if s1 == s2 or not (1 <= a <= nroots and 1 <= b <= nroots) or (a, b) in out:
-            continue
-        out.append((a, b))
-    return out if enabled else None
+    """1-based state pairs of the nonadiabatic couplings asked for (resolve_nac_config), or None
+    when they are not enabled."""
+    cfg = resolve_nac_config(seqm_parameters, nroots=nroots)
+    return cfg.pairs if cfg.enabled else None
 
 
 class ExcitedEnergyFunction(torch.autograd.Function):
@@ -1075,6 +1057,90 @@ def _xl_bomd_force(molecule, P, seqm_parameters, xl_params=None):
             molecule.dP2dt2 = None
             molecule.Krylov_Error = None
             molecule.Fermi_occ = None
+
+
+class EnergyXL(torch.nn.Module):
+    """XL-BOMD shadow energy terms from the auxiliary density P (EnergyXL, dynamics/xlbomd.py:
+    58-508): one Fock build of F(P), D from it (eigensolve, SP2 or the Fermi-Dirac density of
+    KSA-XL-BOMD with xl_bomd_params' max_rank / err_threshold / T_el).  With all_terms:
+    (Hf, Etot, Eelec, EEnt, Enuc, Eiso, EnucAB, D, dP2dt2, Error, e_gap, e, Fe_occ); otherwise
+    (Eelec, EnucAB, D, e_gap, e).  The forces are computed along (molecule.force)."""
+
+    def __init__(self, seqm_parameters):
+        super().__init__()
+        self.seqm_parameters = seqm_parameters
+
+    def forward(self, molecule, P, cis_amp=None, learned_parameters=dict(), xl_bomd_params=dict(), all_terms=False,
+                *args, **kwargs):
+        if cis_amp is not None:
+            raise NotImplementedError("excited-state XL-BOMD (XL-ESMD) is not supported")
+        if callable(learned_parameters) or learned_parameters:
+            raise NotImplementedError("XL-BOMD with learned parameters is not supported")
+        _xl_bomd_force(molecule, P, self.seqm_parameters, xl_bomd_params or {})
+        m = molecule
+        sv = m._solve
+        EnucAB = sv.pair_values_reference_order(sv.s.enuc_pair).to(m.coordinates.device)
+        if all_terms:
+            return (m.Hf, m.Etot, m.Eelec, m.Electronic_entropy, m.Enuc, m.Eiso, EnucAB, m.dm, m.dP2dt2,
+                    getattr(m, "Krylov_Error", None), m.e_gap, m.e_mo, getattr(m, "Fermi_occ", None))
+        return m.Eelec, EnucAB, m.dm, m.e_gap, m.e_mo
+
+
+class ForceXL(torch.nn.Module):
+    """XL-BOMD forces (ForceXL, dynamics/xlbomd.py:511-570): (force, D, Hf, Etot, Eelec, Enuc,
+    Eiso, e, e_gap, EEnt, dP2dt2, Error, Fe_occ), the forces from the adjoint kernel's
+    polarisation at fixed D and P."""
+
+    def __init__(self, seqm_parameters):
+        super().__init__()
+        self.energy = EnergyXL(seqm_parameters)
+        self.seqm_parameters = seqm_parameters
+
+    def forward(self, molecule, P, cis_amp=None, learned_parameters=dict(), xl_bomd_params=dict(), *args, **kwargs):
+        Hf, Etot, Eelec, EEnt, Enuc, Eiso, _, D, dP2dt2, Error, e_gap, e, Fe_occ = self.energy(
+            molecule, P, cis_amp, learned_parameters, xl_bomd_params, all_terms=True)
+        return (molecule.force.detach(), D.detach(), Hf, Etot.detach(), Eelec.detach(), Enuc.detach(), Eiso.detach(),
+                e, e_gap, EEnt, dP2dt2, Error, Fe_occ)
+
+
+class NACConfig:
+    """Resolved nonadiabatic-coupling settings (NACConfig, dynamics/nac_utils.py:5-8)."""
+
+    def __init__(self, enabled, pairs):
+        self.enabled, self.pairs = bool(enabled), list(pairs)
+
+    def __repr__(self):
+        return f"NACConfig(enabled={self.enabled}, pairs={self.pairs})"
+
+
+def resolve_nac_config(seqm_parameters, *, nroots=None, default_enabled=False):
+    """seqm_parameters['nonadiabatic'] -> NACConfig (resolve_nac_config, nac_utils.py:29-63):
+    'compute_nac' on / off; 'states' gives all their pairs; 'pairs' explicit ones; all pairs of
+    the nroots states when enabled without either; pairs sorted, deduplicated, diagonal and
+    (given nroots) out-of-range ones dropped."""
+    cfg = dict(seqm_parameters.get("nonadiabatic", {}))
+    enabled = bool(cfg.get("compute_nac", default_enabled))
+    pairs = []
+    u = sorted({int(x) for x in cfg.get("states") or [] if isinstance(x, (int, float))})
+    pairs += [(u[a], u[b]) for a in range(len(u)) for b in range(a + 1, len(u))]
+    pairs += [(int(p[0]), int(p[1])) for p in cfg.get("pairs") or [] if isinstance(p, (list, tuple)) and len(p) == 2]
+    if enabled and not pairs and nroots:
+        pairs = [(a, b) for a in range(1, nroots + 1) for b in range(a + 1, nroots + 1)]
+    out = []
+    for s1, s2 in pairs:
+        a, b = sorted((int(s1), int(s2)))
+        if s1 == s2 or (nroots is not None and not (1 <= a <= nroots and 1 <= b <= nroots)) or (a, b) in out:
+            continue
+        out.append((a, b))
+    return NACConfig(enabled, out)
+
+
+def active_state_tensor(active_state, nmol, device):
+    """active_state (int or tensor, 1-based excited states, 0 ground) as a (nmol,) long tensor
+    (dynamics/active_state.py:4-15)."""
+    from types import SimpleNamespace
+
+    return _active_states(SimpleNamespace(active_state=active_state), int(nmol), device)
 
 
 class Electronic_Structure(torch.nn.Module):

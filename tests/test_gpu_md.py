@@ -244,3 +244,30 @@ def test_xlbomd_with_sp2_matches_oracle():
         np.testing.assert_allclose(mol.velocities.detach().cpu().numpy(), r["velocities"], atol=1e-6, rtol=0)
         np.testing.assert_allclose(mol.force.cpu().numpy(), r["force"], atol=1e-5, rtol=0)
         np.testing.assert_allclose(mol.Etot.detach().cpu().numpy(), r["Etot"], atol=1e-6, rtol=0)
+
+
+def test_forcexl_at_the_scf_density_gives_the_scf_energy_and_forces():
+    """EnergyXL / ForceXL (dynamics/xlbomd.py:58-570) with P the converged SCF density: the
+    shadow energy equals the SCF energy (1e-7 eV), the forces the SCF forces (1e-5 eV/A), D = P
+    (1e-6); the tuples have the reference's 13 / 5 entries and EnucAB sums to Enuc."""
+    import torch
+
+    from conftest import load_golden
+    from pyseqm_gb300 import Constants, Electronic_Structure, EnergyXL, ForceXL, Molecule
+
+    g = load_golden("md_am1_xlbomd")
+    s = dict(g["settings"])
+    mol = Molecule(Constants().cuda(), s, torch.as_tensor(g["coords_np"], device="cuda"),
+                   torch.as_tensor(g["species_np"], device="cuda")).cuda()
+    Electronic_Structure(s).cuda()(mol)
+    E0, F0, P = mol.Etot.detach().clone(), mol.force.clone(), mol.dm.clone()
+    out = ForceXL(s)(mol, P)
+    assert len(out) == 13
+    force, D, Hf, Etot = out[:4]
+    np.testing.assert_allclose(Etot.cpu().numpy(), E0.cpu().numpy(), atol=1e-7, rtol=0)
+    np.testing.assert_allclose(force.cpu().numpy(), F0.cpu().numpy(), atol=1e-5, rtol=0)
+    np.testing.assert_allclose(D.cpu().numpy(), P.cpu().numpy(), atol=1e-6, rtol=0)
+    e = EnergyXL(s)(mol, P)
+    assert len(e) == 5
+    Eelec, EnucAB = e[0], e[1]
+    np.testing.assert_allclose(EnucAB.sum().item(), mol.Enuc.sum().item(), atol=1e-9, rtol=0)

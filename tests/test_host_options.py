@@ -79,3 +79,15 @@ def test_dispersion_expression_matches_oracle_and_differences(cutoff):
             xm[a, x] -= h
             fd = (_dispersion_am1_fs1(L, torch.as_tensor(xp)).sum() - _dispersion_am1_fs1(L, torch.as_tensor(xm)).sum())
             np.testing.assert_allclose(g[a, x].item(), fd.item() / (2 * h), atol=1e-8, rtol=1e-6)
+
+
+def test_resolve_nac_config_like_the_reference():
+    """The public resolve_nac_config / NACConfig: pairs are resolved whether or not enabled."""
+    from pyseqm_gb300 import resolve_nac_config
+
+    c = resolve_nac_config({"nonadiabatic": {"pairs": [(2, 1), (3, 3)]}}, nroots=3)
+    assert not c.enabled and c.pairs == [(1, 2)]
+    c = resolve_nac_config({"nonadiabatic": {"compute_nac": True, "states": [1, 2, 9]}}, nroots=None)
+    assert c.enabled and c.pairs == [(1, 2), (1, 9), (2, 9)]
+    c = resolve_nac_config({}, nroots=2, default_enabled=True)
+    assert c.enabled and c.pairs == [(1, 2)]

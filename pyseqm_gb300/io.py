@@ -1,4 +1,5 @@
-"""XYZ files in and out, as the reference's helpers read and write them.
+"""XYZ files in and out, as the reference's helpers read and write them (read_xyz,
+read_xyz_trajectory, save_xyz).
 
 ``read_xyz`` follows seqm/seqm_functions/read_xyz.py:17-48 (one molecule per file, element
 symbols or atomic numbers in the first column, atoms ordered by decreasing atomic number with a
@@ -40,6 +41,98 @@ def read_xyz(files, sort=True):
         species[i, : z.size] = z
         coords[i, : z.size] = xyz
     return species, coords
+
+
+def _frames(path):
+    """(atom count, comment, atom lines) per frame of a concatenated xyz file."""
+    with open(path) as f:
+        lines = f.read().splitlines()
+    out, i = [], 0
+    while i < len(lines) and lines[i].strip():
+        n = int(lines[i])
+        block = lines[i + 2: i + 2 + n]
+        if len(block) < n:
+            raise ValueError("Truncated frame.")
+        out.append((n, block))
+        i += 2 + n
+    return out
+
+
+def _velocities(path, nframes, n):
+    """Per frame of NEXMD's velocity.out: a comment, $VELOC, n lines vx vy vz, $ENDVELOC."""
+    with open(path) as f:
+        lines = f.read().splitlines()
+    vel, i = [], 0
+    for _ in range(nframes):
+        if i + n + 3 > len(lines) or lines[i + 1].strip().upper() != "$VELOC":
+            raise ValueError("Bad velocity.out ($VELOC).")
+        v = np.array([[float(x) for x in ln.split()] for ln in lines[i + 2: i + 2 + n]], dtype=float)
+        if v.shape != (n, 3):
+            raise ValueError("Bad velocity.out (vector count).")
+        if lines[i + 2 + n].strip().upper() != "$ENDVELOC":
+            raise ValueError("Bad velocity.out ($ENDVELOC).")
+        vel.append(v)
+        i += n + 3
+    return vel
+
+
+def read_xyz_trajectory(file, start=0, stop=None, step=1, num=None, sort=True, vel_file=None, return_vel=False,
+                        indices=None):
+    """Frames of a concatenated xyz trajectory (NEXMD's coords.xyz; read_xyz.py:51-296):
+    species (M, K) and coordinates (M, K, 3), with return_vel also the velocities of
+    velocity.out (next to the file unless vel_file).  Frames: `indices` (in that order,
+    duplicates kept, negative from the end), else start / stop / step, or `num` frames evenly
+    between start and stop inclusive (rounded, unique).  The atom count must not change; the
+    species and their order come from the first frame read, sorted by decreasing atomic number
+    with equal ones in reverse file order (the reference's reversed stable argsort).  With stop
+    None the frames run to the end of the file (the reference returns none there)."""
+    import os
+
+    if indices is not None and num is not None:
+        raise ValueError("Use either indices or num, not both.")
+    if indices is not None and step != 1:
+        raise ValueError("When using indices, step must be 1.")
+    if num is not None and step != 1:
+        raise ValueError("Provide either step or num, not both.")
+    if return_vel:
+        vel_file = vel_file or os.path.join(os.path.dirname(file), "velocity.out")
+        if not os.path.exists(vel_file):
+            raise FileNotFoundError("velocity.out not found (or vel_file not provided).")
+    frames = _frames(file)
+    total = len(frames)
+    if indices is not None:
+        sel = [int(i) + total if int(i) < 0 else int(i) for i in indices]
+    else:
+        start = start + total if start < 0 else start
+        if stop is not None and stop < 0:
+            stop += total
+        if num is None:
+            sel = list(range(start, total if stop is None else stop, step))
+        else:
+            stop = total - 1 if stop is None else stop
+            sel = np.unique(np.rint(np.linspace(start, stop, num=num)).astype(int)).tolist()
+    sel = [i for i in sel if 0 <= i < total] if indices is None else sel
+    empty = (np.zeros((0, 0), int), np.zeros((0, 0, 3), float))
+    if not sel or total == 0:
+        return empty + (empty[1].copy(),) if return_vel else empty
+    K = frames[0][0]
+    if any(n != K for n, _ in frames):
+        raise ValueError("Variable atom count not supported in fast path.")
+    first = frames[sel[0]][1]
+    numeric = first[0].split()[0].isdigit()
+    z = np.array([int(ln.split()[0]) if numeric else ELEMENT_NUMBER[ln.split()[0]] for ln in first], dtype=int)
+    order = z.argsort(kind="stable")[::-1] if sort else np.arange(K)
+    vel = _velocities(vel_file, total, K) if return_vel else None
+    species = np.empty((len(sel), K), dtype=int)
+    coords = np.empty((len(sel), K, 3), dtype=float)
+    vels = np.empty((len(sel), K, 3), dtype=float) if return_vel else None
+    for j, fr in enumerate(sel):
+        xyz = np.array([[float(x) for x in ln.split()[1:4]] for ln in frames[fr][1]], dtype=float)
+        species[j] = z[order]
+        coords[j] = xyz[order]
+        if return_vel:
+            vels[j] = vel[fr][order]
+    return (species, coords, vels) if return_vel else (species, coords)
 
 
 def save_xyz(molecules, name, Forces=False):

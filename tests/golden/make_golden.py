@@ -439,6 +439,48 @@ def write_xyz_io(name):
     print(name, "files", sorted(saved))
 
 
+def write_traj_io(name):
+    """The reference's read_xyz_trajectory (read_xyz.py:51-296) on a seeded 6-frame trajectory
+    (element symbols, and atomic numbers) with its velocity.out, for several frame selections."""
+    if ONLY and name not in ONLY:
+        return
+    import tempfile
+
+    from seqm.seqm_functions.read_xyz import read_xyz_trajectory
+
+    rng = np.random.default_rng(21)
+    sym, num = ["C", "H", "O", "H", "H"], [6, 1, 8, 1, 1]
+    xyz_s, xyz_n, vel = [], [], []
+    for fr in range(6):
+        xyz_s.append(f"5\nframe {fr}")
+        xyz_n.append(f"5\nframe {fr}")
+        vel.append(f"frame {fr}\n$VELOC")
+        for a in range(5):
+            x = rng.normal(size=3)
+            u = rng.normal(size=3)
+            xyz_s.append(f"{sym[a]} {x[0]:.6f} {x[1]:.6f} {x[2]:.6f}")
+            xyz_n.append(f"{num[a]} {x[0]:.6f} {x[1]:.6f} {x[2]:.6f}")
+            vel.append(f"{u[0]:.6f} {u[1]:.6f} {u[2]:.6f}")
+        vel.append("$ENDVELOC")
+    texts = {"coords.xyz": "\n".join(xyz_s) + "\n", "numeric.xyz": "\n".join(xyz_n) + "\n",
+             "velocity.out": "\n".join(vel) + "\n"}
+    cases = [dict(stop=6), dict(start=1, stop=6, step=2), dict(num=3, stop=5), dict(indices=[4, -1, 0, 4]),
+             dict(start=-3, stop=6), dict(stop=6, return_vel=True), dict(indices=[2, 5], return_vel=True),
+             dict(stop=3, sort=False)]
+    out = []
+    with tempfile.TemporaryDirectory() as d:
+        for fn, t in texts.items():
+            with open(os.path.join(d, fn), "w") as f:
+                f.write(t)
+        for file in ("coords.xyz", "numeric.xyz"):
+            for kw in cases:
+                r = read_xyz_trajectory(os.path.join(d, file), **kw)
+                out.append(dict(file=file, kwargs=kw, result=[np.asarray(a).tolist() for a in r]))
+    with open(os.path.join(HERE, f"{name}.json"), "w") as f:
+        json.dump(dict(name=name, texts=texts, cases=out), f)
+    print(name, len(out), "cases")
+
+
 def write_xlbomd(name, species, coords, settings, steps, timestep, seed, k, krylov=None):
     """A short XL-BOMD trajectory (no thermostat, no Krylov kernel) through the reference's XL_BOMD
     driver: the first step's SCF, then the auxiliary density propagated with the k-th order
@@ -701,6 +743,7 @@ def main():
 
     # the xyz helpers
     write_xyz_io("io_xyz")
+    write_traj_io("io_traj")
 
     # forces of the ground and all excited states (do_all_forces), CIS and RPA
     for es in ("cis", "rpa"):

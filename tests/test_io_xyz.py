@@ -47,3 +47,30 @@ def test_save_xyz_writes_the_reference_files(tmp_path):
         save_xyz(mol, str(tmp_path / "out"), Forces=forces)
         for i in range(len(g["species"])):
             assert (tmp_path / f"out.{i}.xyz").read_text() == g["saved"][f"{int(forces)}.{i}"]
+
+
+def test_read_xyz_trajectory_matches_reference(tmp_path):
+    """read_xyz_trajectory against the reference's outputs: slices, evenly spaced frames,
+    explicit (negative, repeated) indices, velocities, unsorted, symbol and numeric columns; and
+    the argument checks."""
+    import pytest
+
+    from pyseqm_gb300 import read_xyz_trajectory
+
+    with open(os.path.join(GOLDEN, "io_traj.json")) as f:
+        g = json.load(f)
+    for fn, text in g["texts"].items():
+        (tmp_path / fn).write_text(text)
+    for case in g["cases"]:
+        got = read_xyz_trajectory(str(tmp_path / case["file"]), **case["kwargs"])
+        assert len(got) == len(case["result"]), case["kwargs"]
+        for a, b in zip(got, case["result"]):
+            np.testing.assert_array_equal(a, np.asarray(b).reshape(a.shape), err_msg=str(case["kwargs"]))
+    full = read_xyz_trajectory(str(tmp_path / "coords.xyz"))
+    assert full[0].shape == (6, 5)  # stop None: to the end of the file
+    with pytest.raises(ValueError):
+        read_xyz_trajectory(str(tmp_path / "coords.xyz"), indices=[0], num=2)
+    with pytest.raises(ValueError):
+        read_xyz_trajectory(str(tmp_path / "coords.xyz"), num=2, step=2)
+    with pytest.raises(FileNotFoundError):
+        read_xyz_trajectory(str(tmp_path / "coords.xyz"), stop=2, return_vel=True, vel_file=str(tmp_path / "x"))

@@ -57,6 +57,9 @@ class Constants(torch.nn.Module):
         self.atomic_num = torch.nn.Parameter(torch.as_tensor(el["atomic_num"], dtype=torch.float64),
                                              requires_grad=False)
         self.label = list(el["label"])  # element symbols, spelled as the reference's table (save_xyz)
+        self.iso = torch.nn.Parameter(torch.as_tensor(el["iso"], dtype=torch.float64), requires_grad=False)
+        self.qnD_int = torch.nn.Parameter(torch.as_tensor(el["qnD_int"], dtype=torch.float64).to(torch.int64),
+                                          requires_grad=False)
         self.do_timing = do_timing
         if do_timing:
             self.timing = {"Hcore + STO Integrals": [], "SCF": [], "Force": [], "MD": [], "D*": [], "CIS/RPA": []}
@@ -242,7 +245,10 @@ class Molecule(torch.nn.Module):
         self.mass_inverse[non_zero] = 1.0 / self.mass[non_zero]
         for name in ("force", "velocities", "acc", "dm", "q", "w", "Hf", "Etot", "Eelec", "Enuc", "Eiso", "e_mo",
                      "e_gap", "molecular_orbitals", "charge", "dipole", "analytical_gradient", "cis_amplitudes",
-                     "transition_dipole", "oscillator_strength"):
+                     "transition_dipole", "oscillator_strength", "cis_energies", "transition_density_matrices",
+                     "cis_state_relaxed_dipole", "cis_state_unrelaxed_dipole", "all_forces", "all_cis_relaxed_diploles",
+                     "all_cis_unrelaxed_diploles", "Electronic_entropy", "Fermi_occ", "dP2dt2", "Krylov_Error", "nac",
+                     "nac_dot", "old_mos"):
             setattr(self, name, None)
         self.verbose = True
         self.active_state = seqm_parameters.get("active_state", 0)

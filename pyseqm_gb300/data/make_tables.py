@@ -117,7 +117,8 @@ def main(ref_root):
 
     c = Constants()
     out = {}
-    for name in ["tore", "qn", "ussc", "uppc", "gssc", "gspc", "hspc", "gp2c", "gppc", "mass", "atomic_num"]:
+    for name in ["tore", "qn", "ussc", "uppc", "gssc", "gspc", "hspc", "gp2c", "gppc", "mass", "atomic_num", "iso",
+                 "qnD_int"]:
         out[name] = [float(v) for v in getattr(c, name).tolist()]
     # heats of formation are stored in kcal/mol; the reference divides by 23.061 at load
     out["label"] = list(c.label)  # element symbols as the reference's tables spell them

@@ -24,4 +24,5 @@ from .basics import (  # noqa: E402,F401
     resolve_nac_config,
 )
 from .io import read_xyz, read_xyz_trajectory, save_xyz  # noqa: E402,F401
+from .optimization import geomeTRIC_optimization, geometric_optimization  # noqa: E402,F401
 from .dynamics import KSA_XL_BOMD, XL_BOMD, Geometry_Optimization_SD, Molecular_Dynamics_Basic, Molecular_Dynamics_Langevin  # noqa: E402,F401

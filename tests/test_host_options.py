@@ -91,3 +91,69 @@ def test_resolve_nac_config_like_the_reference():
     assert c.enabled and c.pairs == [(1, 2), (1, 9), (2, 9)]
     c = resolve_nac_config({}, nroots=2, default_enabled=True)
     assert c.enabled and c.pairs == [(1, 2)]
+
+
+def test_geometric_optimization_glue(tmp_path, monkeypatch):
+    """The geomeTRIC wrapper with a stand-in geomeTRIC and a stand-in driver (no GPU): coordinates
+    come in bohr and are set in Angstrom, energy and gradient go out in hartree and hartree/bohr,
+    one trajectory frame per step, the last geometry in optimized.xyz; ImportError without it."""
+    import sys
+    import types
+
+    import pyseqm_gb300
+    from pyseqm_gb300 import Constants, Molecule, basics, optimization
+
+    for name in [k for k in sys.modules if k == "geometric" or k.startswith("geometric.")]:
+        monkeypatch.delitem(sys.modules, name)
+    with pytest.raises(ImportError):
+        optimization.geomeTRIC_optimization(None)
+
+    calls = []
+    bohr2ang, ev2au = 0.529177210903, 1.0 / 27.211386245988
+
+    class Engine:
+        def __init__(self, molecule):
+            self.M = molecule
+
+    class GeomMolecule:
+        pass
+
+    def run_optimizer(customengine, input, qccnv, **kw):
+        x0 = customengine.M.xyzs[0].reshape(-1) / bohr2ang
+        for k in range(2):
+            calls.append(customengine.calc_new(x0 + 0.01 * k))
+        return types.SimpleNamespace(write_xyz=lambda selection: ["5", "last", "C 0 0 0"])
+
+    mods = {"geometric": types.ModuleType("geometric"), "geometric.engine": types.SimpleNamespace(Engine=Engine),
+            "geometric.molecule": types.SimpleNamespace(Elements=["X", "H", "He", "Li", "Be", "B", "C"],
+                                                       Molecule=GeomMolecule),
+            "geometric.nifty": types.SimpleNamespace(bohr2ang=bohr2ang, ev2au=ev2au),
+            "geometric.optimize": types.SimpleNamespace(run_optimizer=run_optimizer)}
+    for k, v in mods.items():
+        monkeypatch.setitem(sys.modules, k, v)
+
+    class FakeDriver:
+        def __init__(self, seqm_parameters):
+            pass
+
+        def __call__(self, m, P0=None, dm_prop="SCF"):
+            x = m.coordinates.detach()
+            m.Etot = (x * x).sum((1, 2))
+            m.force = -2.0 * x
+            m.dm = torch.zeros(1, 20, 20, dtype=torch.float64)
+
+    monkeypatch.setattr(basics, "Electronic_Structure", FakeDriver)
+    monkeypatch.chdir(tmp_path)
+    xyz = torch.tensor([[[0.0, 0.0, 0.0], [0.63, 0.63, 0.63], [-0.63, -0.63, 0.63], [-0.63, 0.63, -0.63],
+                         [0.63, -0.63, -0.63]]], dtype=torch.float64)
+    mol = Molecule(Constants(), {"method": "AM1", "scf_eps": 1e-6, "scf_converger": [1]}, xyz,
+                   torch.tensor([[6, 1, 1, 1, 1]]))
+    pyseqm_gb300.geomeTRIC_optimization(mol, traj_file=str(tmp_path / "traj.xyz"))
+    x1 = mol.coordinates.detach().numpy()[0]
+    np.testing.assert_allclose(x1, xyz.numpy()[0] + 0.01 * bohr2ang, atol=1e-12)
+    assert calls[1]["energy"] == pytest.approx(float((x1 ** 2).sum()) * ev2au)
+    np.testing.assert_allclose(calls[1]["gradient"], (2.0 * x1 * ev2au * bohr2ang).reshape(-1), atol=1e-12)
+    traj = (tmp_path / "traj.xyz").read_text().splitlines()
+    assert traj[0] == "5" and traj[1].startswith("Step 1, E = ") and traj[1].endswith(" eV") and len(traj) == 14
+    assert traj[2].split()[0] == "C"
+    assert (tmp_path / "optimized.xyz").read_text() == "5\nlast\nC 0 0 0"

@@ -11,13 +11,15 @@ beta_p through ``SCFEnergyFunction``, whose backward is the adjoint kernel
 (seqm_energy_grad) evaluated at the converged density, which is what the
 reference's SCF0 boundary implies (scf_loop.py:1996-2031).
 
-Supported: MNDO/AM1/PM3, closed shell (scf_converger [0, alpha], [1] and [2] (DIIS), sp2)
-and unrestricted open shell (``UHF``: True with the Molecule's ``mult``; scf_converger
-[0, alpha] and [1], as the reference has neither open-shell DIIS nor SP2), learned
-parameters (values for any parameter; gradients for U_ss, U_pp, beta_s, beta_p), and the
-ground state's CIS / RPA excited states (``excited_states``: excitation energies, amplitudes,
-transition dipoles, oscillator strengths; with active_state > 0 the state's energy and relaxed
-forces).  PM6 with d orbitals and scf_backward >= 1 raise NotImplementedError.
+Supported: MNDO/AM1/PM3/PM6_SP (and PM6_SP_STAR from parameter files), closed shell
+(scf_converger [0, alpha], [1] and [2] (DIIS), sp2) and unrestricted open shell (``UHF``: True
+with the Molecule's ``mult``; scf_converger [0, alpha] and [1], as the reference has neither
+open-shell DIIS nor SP2), learned parameters (values for any parameter; gradients for U_ss,
+U_pp, beta_s, beta_p), ``parameter_file_dir``, ``pair_outer_cutoff``, AM1-FS1 ``dispersion``,
+and the CIS / RPA excited states (``excited_states``: excitation energies, amplitudes,
+transition dipoles, oscillator strengths, orbital windows; with active_state > 0 the state's
+energy and relaxed forces; ``nonadiabatic`` couplings; ``do_all_forces``).  PM6 with d orbitals,
+scf_backward >= 1 and 2nd_grad raise NotImplementedError.
 """
 
 import copy

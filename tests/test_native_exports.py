@@ -35,3 +35,29 @@ def test_sp2_tc_work_size_is_host_computable():
     assert a > 32 * 100 * 100
     assert lib.seqm_sp2_tc_work_bytes(2 * 100 * 100, 2, 100) > a
     assert lib.seqm_sp2_tc_work_bytes(100 * 100, 1, 200) > a
+
+
+def test_batch_struct_layout_matches_header(tmp_path):
+    """The ctypes seqm_batch has the header's size and field offsets (gcc on a probe that
+    includes the header; no GPU): the binding and the library agree on the ABI."""
+    import shutil
+    import subprocess
+
+    import pytest
+
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    fields = [f[0] for f in native.SeqmBatch._fields_]
+    src = tmp_path / "probe.c"
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "pyseqm_gb300.h"', "int main(void) {",
+             '  printf("sizeof %zu\\n", sizeof(seqm_batch));']
+    lines += [f'  printf("{f} %zu\\n", offsetof(seqm_batch, {f}));' for f in fields]
+    lines += ["  return 0;", "}"]
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "probe"
+    subprocess.run(["gcc", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    out = dict(line.split() for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                       text=True).stdout.splitlines())
+    assert int(out["sizeof"]) == ctypes.sizeof(native.SeqmBatch)
+    for f in fields:
+        assert int(out[f]) == getattr(native.SeqmBatch, f).offset, f

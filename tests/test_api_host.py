@@ -225,3 +225,26 @@ def test_md_host_logic_matches_oracle():
     assert abs(float(lg.langevin_c1) - np.exp(-0.5 * dt / damp)) < 1e-15
     with pytest.raises(NotImplementedError):
         Molecular_Dynamics_Basic(s, output={"xyz": 10})
+
+
+def test_layout_edge_cases_match_the_oracle_parse():
+    """Single-atom molecules, hydrogen-only and hydrogen-free molecules, and a pair cutoff that
+    removes every pair of one molecule: the kept pairs in the reference's order equal the oracle
+    parser's, counts and offsets stay consistent."""
+    from pyseqm_gb300.layout import Layout
+
+    species = np.array([[6, 0, 0, 0], [1, 1, 0, 0], [8, 8, 0, 0], [7, 6, 1, 0], [8, 1, 1, 0]])
+    rng = np.random.default_rng(3)
+    coords = rng.normal(size=species.shape + (3,)) * 1.2
+    coords[2, 1] = coords[2, 0] + [6.0, 0.0, 0.0]  # the O2 pair lies beyond the 3 A cutoff
+    for cutoff in (None, 3.0):
+        L = Layout.from_padded(species, coords, "AM1", pair_cutoff=cutoff)
+        ref = O.parse(species, coords, cutoff=cutoff)
+        ri, rj = L.reference_pair_atoms()
+        np.testing.assert_array_equal(ri, ref["idxi"])
+        np.testing.assert_array_equal(rj, ref["idxj"])
+        assert L.nref == ref["idxi"].size
+        assert L.npairs == int(np.sum(L.natoms_m * (L.natoms_m - 1) // 2))
+        np.testing.assert_array_equal(L.norb, 4 * ref["nheavy"] + ref["nhyd"])
+        assert L.mat_off[-1] == int(np.sum(L.norb ** 2))
+    assert L.pair_skip is not None and L.pair_skip.sum() >= 1

@@ -165,3 +165,21 @@ def test_batch_independence():
         one = _run({"species_np": species[m:m + 1, :n], "coords_np": coords[m:m + 1, :n], "settings": s})
         assert abs(float(one["Etot"][0]) - float(full["Etot"][m])) < 1e-9
         assert int(one["iters"][0]) == int(full["iters"][m])
+
+
+def test_edge_case_molecules_match_oracle():
+    """A lone carbon atom (no pairs), H2 (hydrogen only), O2 (no hydrogens), HCN and water in one
+    batch: energies to 1e-6 eV against the oracle, all converged.  The atom and O2 fill one of
+    several degenerate orbitals, so only the energies are compared."""
+    from pyseqm_gb300.scf import run_energy
+
+    species = np.array([[6, 0, 0, 0], [1, 1, 0, 0], [8, 8, 0, 0], [7, 6, 1, 0], [8, 1, 1, 0]])
+    coords = np.zeros(species.shape + (3,))
+    coords[1, 1] = [0.74, 0, 0]
+    coords[2, 1] = [1.21, 0, 0]
+    coords[3, 1], coords[3, 2] = [1.16, 0, 0], [2.22, 0, 0]
+    coords[4, 1], coords[4, 2] = [0.957, 0, 0], [-0.24, 0.927, 0]
+    ref = O.single_point("AM1", species, coords, 1e-8, (1,))
+    out = run_energy(species, coords, "AM1", eps=1e-8, converger=(1,), device="cuda")
+    assert not out["notconverged"].any()
+    np.testing.assert_allclose(out["Etot"].cpu().numpy(), ref["Etot"], atol=1e-6, rtol=0)

@@ -149,7 +149,10 @@ int seqm_density_jacobi(const seqm_batch *b, const double *F, double *P, double 
  * and outputs as seqm_density_jacobi, minus `work`: the eigenvector scratch is a fixed
  * 16 MiB device array inside the library (held by every GPU that loads it, until exit).
  * Limit: sum of norb^2 over the batch <= SEQM_NOALLOC_JACOBI_DOUBLES, else SEQM_E_TOO_LARGE
- * and no launch.  Reads mat_off[nmol] back first, so it synchronises `stream` once.
+ * and no launch.  A batch whose b->max_norb is above 160 is rejected the same way, as a whole
+ * (seqm_density_jacobi instead skips such molecules with status -2 and solves the rest).
+ * Reads mat_off[nmol] back first and waits for that read, so every call synchronises
+ * `stream` once before it launches.
  * The first call on a device resolves the array's device address (cudaGetSymbolAddress)
  * with that device current; make that first call before any stream capture.
  * All calls share the array: calls that overlap on the GPU race. */

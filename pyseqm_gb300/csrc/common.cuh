@@ -4,6 +4,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+#include <mutex>
+
 #include "../../include/pyseqm_gb300.h"
 
 namespace seqm {
@@ -55,5 +58,28 @@ inline int launch_check() {
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? SEQM_OK : SEQM_E_CUDA;
 }
+
+// Dynamic shared-memory limit of one kernel, raised once per device to the largest size any
+// launch of that kernel asks for and never lowered.  The attribute belongs to the device and
+// the function, not to a stream or a thread: a caller that set it to its own size on every call
+// could have another host thread lower it between that set and its launch.
+struct SmemLimit {
+  std::atomic<bool> done[256] = {};
+  std::mutex mu;
+  template <typename Kern>
+  int ensure(Kern kern, size_t bytes) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return SEQM_E_CUDA;
+    if (dev < 0 || dev >= 256) return SEQM_E_ARG;
+    if (done[dev].load(std::memory_order_acquire)) return SEQM_OK;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!done[dev].load(std::memory_order_relaxed)) {
+      if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+        return SEQM_E_CUDA;
+      done[dev].store(true, std::memory_order_release);
+    }
+    return SEQM_OK;
+  }
+};
 
 }  // namespace seqm

@@ -361,6 +361,7 @@ __global__ void __launch_bounds__(NT_RED) k_energy_error(seqm_batch b, const dou
 // and rank 0 alone damps, clamps and renormalises the diagonal and writes it after
 // a cluster barrier, over the provisional values of the elementwise pass.
 constexpr int NT_MIX = 512, MIX_UNROLL = 4;
+constexpr size_t MIX_SMEM_MAX = 200 * 1024;  // diagonal history of molecules up to 12800 AOs
 __global__ void __launch_bounds__(NT_MIX) k_mix(seqm_batch b, double *__restrict__ P, const double *__restrict__ Pnew,
                                                 double *__restrict__ Pold, double *__restrict__ old2,
                                                 const int64_t *__restrict__ row_off, int32_t *__restrict__ kit,
@@ -555,9 +556,12 @@ extern "C" int seqm_mix(const seqm_batch *bp, double *P, const double *Pnew, dou
   seqm_batch b = *bp;
   if (b.nmol == 0) return SEQM_OK;
   size_t smem = linear ? 0 : (size_t)2 * b.max_norb * sizeof(double);
-  if (smem > 200 * 1024) return SEQM_E_TOO_LARGE;
-  if (smem > 48 * 1024 && cudaFuncSetAttribute(k_mix, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return SEQM_E_CUDA;
+  if (smem > MIX_SMEM_MAX) return SEQM_E_TOO_LARGE;
+  if (smem > 48 * 1024) {
+    static SmemLimit limit;
+    const int rc = limit.ensure(k_mix, MIX_SMEM_MAX);
+    if (rc != SEQM_OK) return rc;
+  }
   const int cs = mol_cluster(k_mix, b.max_norb);
   return launch_clusters(k_mix, cs, b.nmol, NT_MIX, smem, stream, b, P, Pnew, Pold, old2, mol_row_off, k, linear, alpha,
                          occupation, active, cs);

@@ -869,6 +869,9 @@ size_t jacobi_smem(int cap) {
   return bytes < 8 ? 8 : bytes;
 }
 
+// k_jacobi's shared-memory limit: set once per device to the largest class (JMAX_N)
+SmemLimit g_jacobi_smem;
+
 // threads of a CTA for count molecules of up to cap basis functions: at least one per rotation
 // pair (cap / 2 + 1) and enough warps for the products; small CTAs let several molecules share
 // an SM, which pays when the class fills the GPU; a class of fewer molecules than SMs keeps the
@@ -898,9 +901,8 @@ extern "C" int seqm_density_jacobi(const seqm_batch *bp, const double *F, double
   seqm_batch b = *bp;
   if (b.nmol == 0) return SEQM_OK;
   const int cap = b.max_norb > JMAX_N ? JMAX_N : b.max_norb;  // larger molecules are skipped (status -2)
-  if (cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jacobi_smem(cap)) !=
-      cudaSuccess)
-    return SEQM_E_CUDA;
+  const int rc0 = g_jacobi_smem.ensure(k_jacobi, jacobi_smem(JMAX_N));
+  if (rc0 != SEQM_OK) return rc0;
   if (b.nclass <= 0) {
     k_jacobi<<<b.nmol, NT_J, jacobi_smem(cap), (cudaStream_t)stream>>>(
         b, F, P, evals, evecs, work, mol_row_off, active, status, max_sweeps, warm, mixed_threshold, density_only, 0,
@@ -992,8 +994,8 @@ extern "C" int seqm_density_jacobi_noalloc(const seqm_batch *bp, const double *F
   int rc = jacobi_scratch_address(&work);
   if (rc != SEQM_OK) return rc;
   const size_t smem = jacobi_smem(b.max_norb);
-  if (cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return SEQM_E_CUDA;
+  rc = g_jacobi_smem.ensure(k_jacobi, jacobi_smem(JMAX_N));
+  if (rc != SEQM_OK) return rc;
   k_jacobi<<<b.nmol, NT_J, smem, s>>>(b, F, P, evals, evecs, work, mol_row_off, active, status, max_sweeps,
                                       nullptr, 0, 0, 0, b.max_norb);
   return launch_check();

@@ -483,8 +483,11 @@ extern "C" int seqm_density_sp2_tc(const seqm_batch *bp, const double *F, double
   k_tc_tile_offsets<<<1, 1024, 0, s>>>(b, xs_off);
   const int nb = (b.max_norb + TC_M - 1) / TC_M, nk = (b.max_norb + TC_KT - 1) / TC_KT;
   k_tc_split<<<dim3(nk, nb, b.nmol), 128, 0, s>>>(b, X, xs[0], xs[1], xs_off, st);
-  if (cudaFuncSetAttribute(k_tc_sp2_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM) != cudaSuccess)
-    return SEQM_E_CUDA;
+  {
+    static SmemLimit limit;
+    const int rc0 = limit.ensure(k_tc_sp2_step, TC_SMEM);
+    if (rc0 != SEQM_OK) return rc0;
+  }
   const dim3 grid((unsigned)(nb * (nb + 1) / 2), (unsigned)b.nmol);
   int rc = SEQM_OK, cur = 0;
   for (int it = 0; it < max_iter; ++it) {

@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this folder by running the PYSEQM reference.
 
 This script is the only place that executes the reference.  It needs a PYSEQM
-checkout (default /root/reference) and runs on the CPU in float64.  ``h5py`` is
+checkout, whose path is the one required argument, and runs on the CPU in float64.  ``h5py`` is
 only needed by the reference's MD module, so a stub stands in for it.
 
 Each fixture records the inputs (species, coordinates, seqm settings) and the
@@ -11,7 +11,7 @@ SCF loop count (calls of ``fock_restricted`` minus the one before and the one
 after the loop), per-molecule loop counts (each molecule run alone), and for the
 "stages" fixtures the hcore blocks and two-electron integrals.
 
-Usage:  python tests/golden/make_golden.py [/path/to/PYSEQM]
+Usage:  python tests/golden/make_golden.py /path/to/PYSEQM
 """
 
 import json
@@ -23,7 +23,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python make_golden.py <path to the PYSEQM source tree>")
+REF = sys.argv[1]
 # GOLDEN_ONLY=name1,name2 regenerates only those fixtures
 ONLY = set(filter(None, os.environ.get("GOLDEN_ONLY", "").split(",")))
 

@@ -90,3 +90,20 @@ def test_noalloc_rejects_batches_beyond_its_scratch():
     rc, P, *_ = _call("seqm_density_jacobi_noalloc", L, F, False)
     assert rc == native.SEQM_E_TOO_LARGE
     assert bool(torch.isnan(P).all())  # nothing was launched
+
+
+def test_noalloc_rejects_molecules_above_the_jacobi_limit():
+    """A batch holding one molecule above 160 AOs is refused as a whole before any launch."""
+    from pyseqm_gb300 import native, workloads
+    from pyseqm_gb300.layout import Layout
+
+    rng = np.random.default_rng(9)
+    mols = [workloads.alkane(2, rng, 0.03), workloads.water_cluster(30, rng)]  # 30 waters: 180 AOs
+    species, coords = workloads.pad_batch(mols)
+    L = Layout.from_padded(species, coords, "PM3").to_device("cuda")
+    assert L.max_norb > 160 and int(L.mat_off[-1]) <= 2**21
+    F = torch.zeros(int(L.mat_off[-1]), dtype=torch.float64, device="cuda")
+    rc, P, ev, vec, st = _call("seqm_density_jacobi_noalloc", L, F, False)
+    assert rc == native.SEQM_E_TOO_LARGE
+    assert bool(torch.isnan(P).all()) and bool(torch.isnan(ev).all()) and bool(torch.isnan(vec).all())
+    assert bool((st == 0).all())

@@ -29,7 +29,7 @@ JACOBI_MAX_N = 160
 
 
 class BatchSCF:
-    def __init__(self, layout: Layout, stream=None):
+    def __init__(self, layout: Layout, stream=None, jacobi_max_n=JACOBI_MAX_N):
         if layout.dev is None:
             raise ValueError("layout must be uploaded with to_device() first")
         self.L = layout
@@ -74,8 +74,12 @@ class BatchSCF:
         # molecules above the Jacobi limit take SP2: "fp64" (plain) or "tc" (tensor cores + FP64 McWeeny)
         self.large_density = "fp64"
         self.mcweeny_steps = 1  # FP64-accurate McWeeny steps after the tensor-core SP2 (and one FP32 step)
-        self.large_mask = torch.as_tensor((layout.norb > JACOBI_MAX_N).astype(np.uint8), device=dev)
-        self.n_large = int((layout.norb > JACOBI_MAX_N).sum())
+        # molecules above jacobi_max_n basis functions (at most the kernel's 160) take SP2
+        if not 0 <= int(jacobi_max_n) <= JACOBI_MAX_N:
+            raise ValueError(f"jacobi_max_n must lie in [0, {JACOBI_MAX_N}]")
+        self.jacobi_max_n = int(jacobi_max_n)
+        self.large_mask = torch.as_tensor((layout.norb > self.jacobi_max_n).astype(np.uint8), device=dev)
+        self.n_large = int((layout.norb > self.jacobi_max_n).sum())
         self.n_small = layout.nmol - self.n_large
         self.small_mask = 1 - self.large_mask
         # SP2 runs over a compact view of the large molecules when the batch also holds small ones
@@ -93,6 +97,18 @@ class BatchSCF:
         fma_newton = nsel * n * n + nsel * (n - nsel) * n + 0.5 * n * n * nsel
         self._fma = {k: torch.as_tensor(v, dtype=torch.float64, device=dev)
                      for k, v in (("newton", fma_newton), ("orth", 0.5 * n ** 3), ("final", 2.0 * n ** 3))}
+        # algorithmic units of the measurement: an eigensolve with vectors and the density,
+        # 9 n^3 + 2 n^2 nocc flops per molecule and density call (symmetric QR convention,
+        # independent of the sweeps taken); a Fock build, 8 (W_c + 3 N_blk) bytes per molecule
+        # (W_c = 100 XX + 10 XH + 1 HH integrals read, N_blk = 16 XX + 4 XH + 1 HH + 10 heavy + 1 H
+        # block elements of P read, of Hcore read and of F written)
+        nocc = layout.nocc.astype(np.float64)
+        self._eig_unit = torch.as_tensor(9.0 * n ** 3 + 2.0 * n * n * nocc, dtype=torch.float64, device=dev)
+        wc = 100.0 * layout.nxx_m + 10.0 * layout.nxh_m + layout.nhh_m
+        nblk = 16.0 * layout.nxx_m + 4.0 * layout.nxh_m + layout.nhh_m + 10.0 * layout.nheavy + layout.nhyd
+        self._fock_unit = torch.as_tensor(8.0 * (wc + 3.0 * nblk), dtype=torch.float64, device=dev)
+        self.profile_fock = False  # record CUDA events around every Fock build
+        self.fock_events = []
 
     # ------------------------------------------------------------------ calls
     def _s(self):
@@ -109,9 +125,18 @@ class BatchSCF:
 
     def fock(self, active=None):
         self.launches += 1
+        ev = None
+        if self.profile_fock:
+            stream = self.stream if self.stream is not None else torch.cuda.current_stream(self.L.device)
+            ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            unit = self._fock_unit if active is None else self._fock_unit * active[: self.L.nmol].double()
+            ev[0].record(stream)
         native.check(self.lib.seqm_fock(self.L.struct, native.ptr(self.P), native.ptr(self.H), native.ptr(self.w_xx),
                                         native.ptr(self.w_xh), native.ptr(self.w_hh), native.ptr(self.F),
                                         native.ptr(active), self._s()), "seqm_fock")
+        if ev is not None:
+            ev[1].record(stream)
+            self.fock_events.append((ev[0], ev[1], unit.sum()))
 
     def density(self, out, sp2=(False,), active=None, evecs=None, max_sweeps=50, density_only=False):
         if self.profile_density:
@@ -122,7 +147,10 @@ class BatchSCF:
             e0.record(stream)
             self._density(out, sp2, active, evecs, max_sweeps, density_only)
             e1.record(stream)
-            self.density_events.append((e0, e1, self._fp64_flops(act, int(density_only), evecs is not None)))
+            small = self.small_mask[: self.L.nmol].double() if self.n_large else 1.0
+            unit = self._eig_unit * small * (1.0 if act is None else act.double())
+            self.density_events.append((e0, e1, self._fp64_flops(act, int(density_only), evecs is not None),
+                                        unit.sum()))
             return
         self._density(out, sp2, active, evecs, max_sweeps, density_only)
 
@@ -147,7 +175,7 @@ class BatchSCF:
         nmol, max_norb, mol_norb, mol_nocc, mol_mat_off; the matrix offsets point into the
         full batch's matrices and end with the full size)."""
         L = self.L
-        idx = np.nonzero(L.norb > JACOBI_MAX_N)[0]
+        idx = np.nonzero(L.norb > self.jacobi_max_n)[0]
         dev = L.device
         v = dict(idx=torch.as_tensor(idx, dtype=torch.int64, device=dev),
                  norb=torch.as_tensor(L.norb[idx].astype(np.int32), device=dev),

@@ -94,6 +94,10 @@ typedef struct seqm_batch {
    * every term (integrals, Hcore block, core-core, gradients), as the reference drops it from its
    * pair list (basics.py:324-328); NULL: all pairs kept. */
   const uint8_t *pair_skip;
+  /* host value: mol_mat_off[nmol], the number of dense matrix elements of the batch (sum of
+   * norb^2), or 0 if the caller does not know it; entry points that size their scratch from it
+   * then read it back from the device and wait for that read. */
+  int64_t mat_total;
 } seqm_batch;
 
 /* Integrals + core Hamiltonian.  Replaces hcore(molecule) (seqm/seqm_functions/hcore.py:9-179),
@@ -118,7 +122,8 @@ int seqm_fock(const seqm_batch *b, const double *P, const double *H, const doubl
  * work: scratch of mat_off[nmol] doubles (unsorted eigenvector rows).
  * warm (NULL: cold start for all): molecules with warm[m] != 0 start from the orthonormal
  * rows already in `work` (the previous call's eigenvectors) and rotate A = V F V^T, which
- * converges in fewer sweeps when F changed little (successive SCF iterations); needs P.
+ * converges in fewer sweeps when F changed little (successive SCF iterations); needs P.  The
+ * call then sets warm[m] = 1 for every molecule it solves (its rows in `work` are valid).
  * mixed_threshold > 0 (needs P): molecules starting cold, or whose previous call (status[m]
  * on entry) took >= mixed_threshold sweeps, first sweep in FP32 (A and the rotation product
  * in shared memory), then lift the vectors to FP64 (one Newton-Schulz re-orthonormalisation)
@@ -140,7 +145,7 @@ int seqm_fock(const seqm_batch *b, const double *P, const double *H, const doubl
  * With size classes (b->nclass > 0) the molecules are processed by one launch per class. */
 int seqm_density_jacobi(const seqm_batch *b, const double *F, double *P, double *evals, double *evecs,
                         double *work, const int64_t *mol_row_off, const uint8_t *active, int32_t *status,
-                        int max_sweeps, const uint8_t *warm, int mixed_threshold, int density_only,
+                        int max_sweeps, uint8_t *warm, int mixed_threshold, int density_only,
                         void *stream);
 
 /* Allocation-free seqm_density_jacobi.  No counterpart in the reference: it exists for
@@ -165,10 +170,14 @@ int seqm_density_jacobi_noalloc(const seqm_batch *b, const double *F, double *P,
  * applied per molecule to its packed Fock matrix (eps clamped to [1e-7, 1e-3] as there).
  * work: SEQM_SP2_WORK_DOUBLES(T, nmol, max_norb) doubles with T = mat_off[nmol].
  * P = 2 X at convergence.  status[m]: SP2 steps taken, or -1 if max_iter was hit.
- * Synchronises the stream every 4 SP2 steps to test convergence. */
+ * Called on a stream that is not being captured, it synchronises the stream every 4 SP2 steps
+ * to test convergence.  Called while the stream is being captured into a CUDA graph, it adds
+ * the step loop to the graph as a conditional WHILE node whose last kernel ends the loop on the
+ * device once no molecule runs (at most max_iter trips), with no host synchronisation; give b
+ * its mat_total then, since a read-back of mol_mat_off cannot be captured. */
 #define SEQM_SP2_STATE 11
 #define SEQM_SP2_WORK_DOUBLES(T, nmol, maxn) \
-  (2 * (size_t)(T) + (SEQM_SP2_STATE + 2 * (size_t)(maxn)) * (size_t)(nmol) + 1)
+  (2 * (size_t)(T) + (SEQM_SP2_STATE + 2 * (size_t)(maxn)) * (size_t)(nmol) + 2)
 int seqm_density_sp2(const seqm_batch *b, const double *F, double *P, double *work, double eps,
                      const uint8_t *active, int32_t *status, int max_iter, void *stream);
 
@@ -182,7 +191,12 @@ int seqm_density_sp2(const seqm_batch *b, const double *F, double *P, double *wo
  * the trace error is below eps, or below 1e-2 and no longer improving (SP2.py:76-80).  No
  * counterpart of the mixed-precision form in the reference.  work: 256-byte aligned,
  * seqm_sp2_tc_work_bytes(mat_off[nmol], nmol, max_norb) bytes.  At most 65535 molecules.
- * status[m] = SP2 steps, -1 at the step cap.  Synchronises the stream every 4 SP2 steps. */
+ * status[m] = SP2 steps, -1 at the step cap, SEQM_E_CUDA if the product kernel gave up
+ * waiting on one of its barriers (it then releases its resources and returns; the call's return
+ * value says so too when the stream is not being captured).  On a stream that is not being captured it
+ * synchronises the stream every 4 SP2 steps; under CUDA graph capture the step loop becomes a
+ * conditional WHILE node ended on the device (two SP2 steps per trip, at most max_iter + 1
+ * steps), as seqm_density_sp2 describes. */
 size_t seqm_sp2_tc_work_bytes(int64_t total_matrix_elements, int nmol, int max_norb);
 int seqm_density_sp2_tc(const seqm_batch *b, const double *F, double *P, void *work, double eps,
                         const uint8_t *active, int32_t *status, int max_iter, int mcweeny_steps, void *stream);
@@ -207,6 +221,36 @@ int seqm_mix(const seqm_batch *b, double *P, const double *Pnew, double *Pold, d
 int seqm_energy_error(const seqm_batch *b, const double *P, const double *Pold, const double *H,
                       const double *F, double *Eelec, double *Eout, double *err, double *dm_err,
                       double *dm_el, uint8_t *active, double eps, const double *diis_err, void *stream);
+
+/* The rest of one SCF iteration after the density step, for the active molecules: mixing,
+ * Fock build of the mixed density, energy and convergence test, retirement of the molecules
+ * that pass it, and a count of those still active.  Replaces the body of the reference's
+ * iteration loop after its density step (scf_forward0 scf_loop.py:258-300, scf_forward1
+ * :505-598): P <- mix(P, Pnew) (seqm_mix), F <- F(P) (seqm_fock), Eelec and the test of
+ * get_error (seqm_energy_error), where the reference ends each iteration with a host read of
+ * the not-converged count (scf_loop.py:598, Nnot = int(notconverged.sum())); here the count goes
+ * to *nactive on the device (NULL: not counted) and no call synchronises the stream, so
+ * iterations can be queued ahead or captured in a CUDA graph.
+ * mixing: 0 linear (alpha), 1 adaptive, -1 none (P already mixed, e.g. by seqm_diis_mix; pass
+ * diis_err then).  Every pointer is device memory; the struct itself is read on the host. */
+typedef struct seqm_scf_state {
+  double *P;                /* [T] in: density; out: the mixed density */
+  const double *Pnew;       /* [T] the density step's output */
+  double *Pold;             /* [T] out: P before the mixing */
+  double *old2;             /* [sum norb] adaptive mixer's diagonal history (seqm_mix) */
+  const double *H;          /* [T] core Hamiltonian */
+  double *F;                /* [T] out: F(P) */
+  const double *w_xx, *w_xh, *w_hh;               /* integrals of seqm_hcore */
+  double *Eelec, *Eout, *err, *dm_err, *dm_el;    /* [nmol] as seqm_energy_error */
+  const int64_t *mol_row_off;                     /* [nmol+1] prefix sum of norb */
+  int32_t *iters;           /* [nmol] density steps per molecule (seqm_mix) */
+  uint8_t *active;          /* [nmol] in/out */
+  const double *diis_err;   /* [nmol] or NULL */
+  int32_t *nactive;         /* [1] out, or NULL */
+  int32_t mixing, pad_;
+  double alpha, occupation, eps;
+} seqm_scf_state;
+int seqm_scf_step(const seqm_batch *b, const seqm_scf_state *st, void *stream);
 
 /* Pulay DIIS converger (scf_converger [2]; scf_forward2, scf_loop.py:639-1132), per molecule.
  * state: SEQM_DIIS_STATE doubles per molecule (ring counter, stored count, reset flag, the

@@ -59,6 +59,20 @@ inline int launch_check() {
   return e == cudaSuccess ? SEQM_OK : SEQM_E_CUDA;
 }
 
+// mol_mat_off[nmol] (dense matrix elements of the batch): the host copy in the struct when the
+// caller filled it in, else read back from the device, which waits for the stream
+inline int batch_total(const seqm_batch &b, cudaStream_t s, int64_t *total) {
+  if (b.mat_total > 0) {
+    *total = b.mat_total;
+    return SEQM_OK;
+  }
+  *total = 0;
+  if (cudaMemcpyAsync(total, b.mol_mat_off + b.nmol, sizeof(int64_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return SEQM_E_CUDA;
+  return SEQM_OK;
+}
+
 // Dynamic shared-memory limit of one kernel, raised once per device to the largest size any
 // launch of that kernel asks for and never lowered.  The attribute belongs to the device and
 // the function, not to a stream or a thread: a caller that set it to its own size on every call

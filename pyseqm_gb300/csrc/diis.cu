@@ -235,9 +235,7 @@ __global__ void __launch_bounds__(EW_THREADS) k_diis_mix(seqm_batch b, double *_
 
 int64_t matrix_total(const seqm_batch &b, cudaStream_t s, int *rc) {
   int64_t total = 0;
-  if (cudaMemcpyAsync(&total, b.mol_mat_off + b.nmol, sizeof(int64_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-      cudaStreamSynchronize(s) != cudaSuccess)
-    *rc = SEQM_E_CUDA;
+  if (batch_total(b, s, &total) != SEQM_OK) *rc = SEQM_E_CUDA;
   return total;
 }
 

@@ -2,10 +2,12 @@
 //
 // Fock (fock.py:132-181): one warp per atom builds the atom's diagonal block
 // (Hcore + one-centre two-electron terms + Coulomb J gathered from all of the
-// atom's pairs; the lanes split the partners and a butterfly reduction combines
-// them), one thread per pair builds the off-diagonal block (Hcore + exchange K)
-// and its transpose.  Every element of F is written exactly once, there are no
-// atomics, and the result is bitwise symmetric.
+// atom's pairs; see fock_diag), one thread per pair builds the off-diagonal block
+// (Hcore + exchange K) and its transpose.  Every element of F is written exactly
+// once, there are no atomics, and the result is bitwise symmetric.  The build is
+// bound by the FP64 pipe (about 2 (456 XX + 36 XH + 3 HH) flops per pair against
+// 8 (100 XX + 10 XH + 1 HH) integral bytes): the mapping keeps every FP64
+// instruction's lanes busy and issues nothing in FP64 but the contractions.
 //
 // The energy / convergence test and the mixing run as thread-block clusters of
 // up to 16 CTAs per molecule (more CTAs for larger molecules); the energy sums are
@@ -41,7 +43,15 @@ __device__ __forceinline__ double warp_allsum(double v) {
   return v;
 }
 
-// diagonal block of atom a (fock.py:187-231 one-centre terms, :277-294 Coulomb), one warp
+// diagonal block of atom a (fock.py:187-231 one-centre terms, :277-294 Coulomb), one warp.
+//
+// A heavy atom's warp is three groups of ten lanes: lane k of group g accumulates output k of
+// the packed block (k10_row/k10_col order) over the partners q = g, g + 3, g + 6, ..., one
+// fused multiply-add per integral, and the three group sums are combined by two shuffles.
+// Every FP64 instruction of the warp thus carries 30 useful lanes: the Coulomb term is the
+// kernel's largest FP64 cost after the exchange blocks, and GB300's FP64 pipe, not memory,
+// bounds the Fock build.  A hydrogen's warp splits its partners over the lanes and sums with a
+// butterfly (one output).  The sums run in a fixed order, so the result is deterministic.
 __device__ __forceinline__ void fock_diag(const seqm_batch &b, int a, int lane, const double *__restrict__ P,
                                           const double *__restrict__ H, const double *__restrict__ w_xx,
                                           const double *__restrict__ w_xh, const double *__restrict__ w_hh,
@@ -56,86 +66,73 @@ __device__ __forceinline__ void fock_diag(const seqm_batch &b, int a, int lane, 
   const double gss = par(b, SEQM_P_GSS, a);
   if (la < nh) {
     const int o = 4 * la;
-    // Coulomb from the partners B (lanes take partners q = lane, lane + 32, ...): pairs where
-    // this atom is first contribute J_B = w . P_B, pairs where it is second P_B . w
-    double f[10];
-#pragma unroll
-    for (int k = 0; k < 10; ++k) f[k] = 0.0;
-    for (int q = lane; q < nat - 1; q += 32) {
+    const int g = lane / 10, k = lane - 10 * g;  // lanes 30, 31: g = 3, no partners
+    double f = 0.0;
+    for (int q = g; g < 3 && q < nat - 1; q += 3) {
       if (q < nh - 1) {
         const int j = q < la ? q : q + 1;
         double PB[10];
         packed_atom_density(Pm, norb, 4 * j, true, PB);
-        if (j > la) {
-          const double *w = w_xx + (size_t)100 * (xx0 + tri_index(la, j, nh));
+        if (j > la) {  // pair (A, B): row k of w, contiguous
+          const double2 *w2 = reinterpret_cast<const double2 *>(w_xx + (size_t)100 * (xx0 + tri_index(la, j, nh)) +
+                                                                10 * k);
 #pragma unroll
-          for (int k = 0; k < 10; ++k) {
-            double s = 0.0;
-#pragma unroll
-            for (int l = 0; l < 10; ++l) s += PB[l] * w[k * 10 + l];
-            f[k] += s;
+          for (int l = 0; l < 5; ++l) {
+            const double2 v = __ldg(w2 + l);
+            f = fma(v.x, PB[2 * l], f);
+            f = fma(v.y, PB[2 * l + 1], f);
           }
-        } else {
-          const double *w = w_xx + (size_t)100 * (xx0 + tri_index(j, la, nh));
+        } else {  // pair (B, A): column k of w
+          const double *w = w_xx + (size_t)100 * (xx0 + tri_index(j, la, nh)) + k;
 #pragma unroll
-          for (int l = 0; l < 10; ++l) {
-            double s = 0.0;
-#pragma unroll
-            for (int k = 0; k < 10; ++k) s += PB[k] * w[k * 10 + l];
-            f[l] += s;
-          }
+          for (int l = 0; l < 10; ++l) f = fma(PB[l], __ldg(w + 10 * l), f);
         }
       } else {
         const int h = q - (nh - 1), oh = 4 * nh + h;
-        const double *w = w_xh + (size_t)10 * (xh0 + la * ny + h);
-        const double ph = Pm[(size_t)oh * norb + oh];
-#pragma unroll
-        for (int k = 0; k < 10; ++k) f[k] += ph * w[k];
+        f = fma(Pm[(size_t)oh * norb + oh], __ldg(w_xh + (size_t)10 * (xh0 + la * ny + h) + k), f);
       }
     }
-#pragma unroll
-    for (int k = 0; k < 10; ++k) f[k] = warp_allsum(f[k]);
-    // one-centre terms (fock.py:187-231)
-    const double gsp = par(b, SEQM_P_GSP, a), gpp = par(b, SEQM_P_GPP, a);
-    const double gp2 = par(b, SEQM_P_GP2, a), hsp = par(b, SEQM_P_HSP, a);
-    double Pd[4][4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) Pd[r][c] = Pm[(size_t)(o + r) * norb + o + c];
-    const double f1 = gsp - 0.5 * hsp, f2 = 1.5 * hsp - 0.5 * gsp, f3 = 1.25 * gp2 - 0.25 * gpp,
-                 f4 = 0.75 * gpp - 1.25 * gp2;
-    const double Pss = Pd[0][0], Ppt = Pd[1][1] + Pd[2][2] + Pd[3][3];
-#pragma unroll
-    for (int k = 0; k < 10; ++k) {
+    const double f1 = __shfl_sync(0xffffffffu, f, (lane + 10) & 31);
+    const double f2 = __shfl_sync(0xffffffffu, f, (lane + 20) & 31);
+    if (lane < 10) {
+      const double J = (f + f1) + f2;
+      // one-centre terms (fock.py:187-231)
       const int r = k10_row(k), c = k10_col(k);
+      const double gsp = par(b, SEQM_P_GSP, a), gpp = par(b, SEQM_P_GPP, a);
+      const double gp2 = par(b, SEQM_P_GP2, a), hsp = par(b, SEQM_P_HSP, a);
+      const double c1 = gsp - 0.5 * hsp, c2 = 1.5 * hsp - 0.5 * gsp, c3 = 1.25 * gp2 - 0.25 * gpp,
+                   c4 = 0.75 * gpp - 1.25 * gp2;
+      const double Pss = Pm[(size_t)o * norb + o];
+      const double Ppt = Pm[(size_t)(o + 1) * norb + o + 1] + Pm[(size_t)(o + 2) * norb + o + 2] +
+                         Pm[(size_t)(o + 3) * norb + o + 3];
+      const double Prc = Pm[(size_t)(o + r) * norb + o + c];
       double oc;
-      if (r == 0 && c == 0) oc = 0.5 * Pss * gss + Ppt * f1;
-      else if (r == c) oc = Pss * f1 + 0.5 * Pd[r][r] * gpp + (Ppt - Pd[r][r]) * f3;
-      else if (r == 0) oc = Pd[0][c] * f2;
-      else oc = Pd[r][c] * f4;
-      if (lane == k) {
-        const double v = Hm[(size_t)(o + r) * norb + o + c] + oc + f[k];
-        Fm[(size_t)(o + r) * norb + o + c] = v;
-        Fm[(size_t)(o + c) * norb + o + r] = v;
-      }
+      if (r == 0 && c == 0) oc = 0.5 * Pss * gss + Ppt * c1;
+      else if (r == c) oc = Pss * c1 + 0.5 * Prc * gpp + (Ppt - Prc) * c3;
+      else if (r == 0) oc = Prc * c2;
+      else oc = Prc * c4;
+      const double v = Hm[(size_t)(o + r) * norb + o + c] + oc + J;
+      Fm[(size_t)(o + r) * norb + o + c] = v;
+      Fm[(size_t)(o + c) * norb + o + r] = v;
     }
   } else {
     const int h = la - nh, o = 3 * nh + la;
     double f = 0.0;
     for (int q = lane; q < nat - 1; q += 32) {
       if (q < nh) {
-        const double *w = w_xh + (size_t)10 * (xh0 + q * ny + h);
+        const double2 *w2 = reinterpret_cast<const double2 *>(w_xh + (size_t)10 * (xh0 + q * ny + h));
         double PB[10];
         packed_atom_density(Pm, norb, 4 * q, true, PB);
-        double s = 0.0;
 #pragma unroll
-        for (int k = 0; k < 10; ++k) s += PB[k] * w[k];
-        f += s;
+        for (int l = 0; l < 5; ++l) {
+          const double2 v = __ldg(w2 + l);
+          f = fma(v.x, PB[2 * l], f);
+          f = fma(v.y, PB[2 * l + 1], f);
+        }
       } else {
         const int g0 = q - nh, g = g0 < h ? g0 : g0 + 1, og = 4 * nh + g;
         const double w = w_hh[hh0 + (g < h ? tri_index(g, h, ny) : tri_index(h, g, ny))];
-        f += w * Pm[(size_t)og * norb + og];
+        f = fma(w, Pm[(size_t)og * norb + og], f);
       }
     }
     f = warp_allsum(f);
@@ -171,12 +168,20 @@ __global__ void __launch_bounds__(128) k_fock(seqm_batch b, const double *__rest
   const double *Pm = P + mo, *Hm = H + mo;
   double *Fm = F + mo;
   if (p < b.nxx) {
-    const double *w = w_xx + (size_t)100 * p;
+    // K(mu, nu) = sum_{l,s} (mu l | nu s) P_AB(l, s), F_AB = H_AB - K / 2 (the halving is exact)
+    const double2 *w2 = reinterpret_cast<const double2 *>(w_xx + (size_t)100 * p);
+    double w[100];
+#pragma unroll
+    for (int i = 0; i < 50; ++i) {
+      const double2 v = __ldg(w2 + i);
+      w[2 * i] = v.x;
+      w[2 * i + 1] = v.y;
+    }
     double Pp[4][4];
 #pragma unroll
     for (int l = 0; l < 4; ++l)
 #pragma unroll
-      for (int s = 0; s < 4; ++s) Pp[l][s] = -0.5 * Pm[(size_t)(oi + l) * norb + oj + s];
+      for (int s = 0; s < 4; ++s) Pp[l][s] = Pm[(size_t)(oi + l) * norb + oj + s];
 #pragma unroll
     for (int mu = 0; mu < 4; ++mu)
 #pragma unroll
@@ -185,8 +190,8 @@ __global__ void __launch_bounds__(128) k_fock(seqm_batch b, const double *__rest
 #pragma unroll
         for (int l = 0; l < 4; ++l)
 #pragma unroll
-          for (int s = 0; s < 4; ++s) k += w[kind(mu, l) * 10 + kind(nu, s)] * Pp[l][s];
-        double v = Hm[(size_t)(oi + mu) * norb + oj + nu] + k;
+          for (int s = 0; s < 4; ++s) k = fma(w[kind(mu, l) * 10 + kind(nu, s)], Pp[l][s], k);
+        const double v = fma(-0.5, k, Hm[(size_t)(oi + mu) * norb + oj + nu]);
         Fm[(size_t)(oi + mu) * norb + oj + nu] = v;
         Fm[(size_t)(oj + nu) * norb + oi + mu] = v;
       }
@@ -194,13 +199,13 @@ __global__ void __launch_bounds__(128) k_fock(seqm_batch b, const double *__rest
     const double *w = w_xh + (size_t)10 * (p - b.nxx);
     double Pp[4];
 #pragma unroll
-    for (int l = 0; l < 4; ++l) Pp[l] = -0.5 * Pm[(size_t)(oi + l) * norb + oj];
+    for (int l = 0; l < 4; ++l) Pp[l] = Pm[(size_t)(oi + l) * norb + oj];
 #pragma unroll
     for (int mu = 0; mu < 4; ++mu) {
       double k = 0.0;
 #pragma unroll
-      for (int l = 0; l < 4; ++l) k += w[kind(mu, l)] * Pp[l];
-      double v = Hm[(size_t)(oi + mu) * norb + oj] + k;
+      for (int l = 0; l < 4; ++l) k = fma(__ldg(w + kind(mu, l)), Pp[l], k);
+      const double v = fma(-0.5, k, Hm[(size_t)(oi + mu) * norb + oj]);
       Fm[(size_t)(oi + mu) * norb + oj] = v;
       Fm[(size_t)oj * norb + oi + mu] = v;
     }
@@ -262,7 +267,7 @@ __device__ double block_max(double v, double *red) {
 // so the result does not depend on cs.
 __device__ __forceinline__ void finish_error(const seqm_batch &b, int m, double e, double fro, double mx, double *Eelec,
                                         double *err, double *dm_err, double *dm_el, uint8_t *active, double eps,
-                                        const double *diis_err) {
+                                        const double *diis_err, int *nactive) {
   double de = e - Eelec[m];
   err[m] = de;
   // with DIIS, also max |F P - P F| > 50 eps (scf_loop.py:130-132)
@@ -274,6 +279,7 @@ __device__ __forceinline__ void finish_error(const seqm_batch &b, int m, double 
   bool nc = bad || dm_err[m] > eps * 2.0 || dm_el[m] > eps * 15.0;
   if (nc) Eelec[m] = e;
   if (active) active[m] = nc ? 1 : 0;
+  if (nc && nactive) atomicAdd(nactive, 1);
 }
 
 constexpr int NT_RED = 512, EE_SLICES = 16, EE_UNROLL = 4;
@@ -281,7 +287,8 @@ __global__ void __launch_bounds__(NT_RED) k_energy_error(seqm_batch b, const dou
                                                          const double *__restrict__ Pold, const double *__restrict__ H,
                                                          const double *__restrict__ F, double *Eelec, double *Eout,
                                                          double *err, double *dm_err, double *dm_el, uint8_t *active,
-                                                         double eps, const double *__restrict__ diis_err, int cs) {
+                                                         double eps, const double *__restrict__ diis_err,
+                                                         int *__restrict__ nactive, int cs) {
   __shared__ double wred[NT_RED / 32][3 * EE_SLICES];
   __shared__ double part[3 * EE_SLICES];
   cg::cluster_group cl = cg::this_cluster();
@@ -343,7 +350,7 @@ __global__ void __launch_bounds__(NT_RED) k_energy_error(seqm_batch b, const dou
     }
     e *= 0.5;
     Eout[m] = e;
-    if (Pold) finish_error(b, m, e, fro, mx, Eelec, err, dm_err, dm_el, active, eps, diis_err);
+    if (Pold) finish_error(b, m, e, fro, mx, Eelec, err, dm_err, dm_el, active, eps, diis_err, nactive);
   }
   cl.sync();  // the other CTAs' shared memory stays alive until rank 0 has read it
 }
@@ -546,7 +553,28 @@ extern "C" int seqm_energy_error(const seqm_batch *bp, const double *P, const do
   if (b.nmol == 0) return SEQM_OK;
   const int cs = mol_cluster(k_energy_error, b.max_norb);
   return launch_clusters(k_energy_error, cs, b.nmol, NT_RED, 0, stream, b, P, Pold, H, F, Eelec, Eout, err, dm_err,
-                         dm_el, active, eps, diis_err, cs);
+                         dm_el, active, eps, diis_err, (int *)nullptr, cs);
+}
+
+extern "C" int seqm_scf_step(const seqm_batch *bp, const seqm_scf_state *st, void *stream) {
+  if (!bp || !st || !st->P || !st->Pnew || !st->Pold || !st->H || !st->F || !st->active) return SEQM_E_ARG;
+  if (st->mixing < -1 || st->mixing > 1) return SEQM_E_ARG;
+  const seqm_batch &b = *bp;
+  if (b.nmol == 0) return SEQM_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = SEQM_OK;
+  if (st->mixing >= 0) {
+    rc = seqm_mix(bp, st->P, st->Pnew, st->Pold, st->old2, st->mol_row_off, st->iters, st->mixing == 0, st->alpha,
+                  st->occupation, st->active, stream);
+    if (rc != SEQM_OK) return rc;
+  }
+  rc = seqm_fock(bp, st->P, st->H, st->w_xx, st->w_xh, st->w_hh, st->F, st->active, stream);
+  if (rc != SEQM_OK) return rc;
+  if (st->nactive && cudaMemsetAsync(st->nactive, 0, sizeof(int32_t), s) != cudaSuccess) return SEQM_E_CUDA;
+  const int cs = mol_cluster(k_energy_error, b.max_norb);
+  return launch_clusters(k_energy_error, cs, b.nmol, NT_RED, 0, stream, b, (const double *)st->P,
+                         (const double *)st->Pold, st->H, (const double *)st->F, st->Eelec, st->Eout, st->err,
+                         st->dm_err, st->dm_el, st->active, st->eps, st->diis_err, (int *)st->nactive, cs);
 }
 
 extern "C" int seqm_mix(const seqm_batch *bp, double *P, const double *Pnew, double *Pold, double *old2,

@@ -620,7 +620,7 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
                                                  double *__restrict__ evals, double *__restrict__ evecs,
                                                  double *__restrict__ work, const int64_t *__restrict__ row_off,
                                                  const uint8_t *__restrict__ active, int32_t *__restrict__ status,
-                                                 int max_sweeps, const uint8_t *__restrict__ warm,
+                                                 int max_sweeps, uint8_t *__restrict__ warm,
                                                  int mixed_threshold, int density_only, int order_base, int cap) {
   extern __shared__ double A[];
   __shared__ JShared sh;
@@ -661,7 +661,8 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
     if (!is_warm) V[idx] = i == j ? 1.0 : 0.0;
     f2 += v * v;
   }
-  const double fro = sqrt(jblock_reduce(f2, sh.red, false));
+  const double fro = sqrt(jblock_reduce(f2, sh.red, false));  // every thread has read warm[m] here
+  if (warm != nullptr && tid == 0) warm[m] = 1;  // this call leaves valid eigenvector rows in work
   const double tol = 1.0e-13 * fro;
   const bool fp32_ok = mixed || (want_newton && mixed_threshold > 0);
   bool newton = false, a32_ready = false, a64_ready = false;
@@ -894,7 +895,7 @@ using namespace seqm;
 
 extern "C" int seqm_density_jacobi(const seqm_batch *bp, const double *F, double *P, double *evals, double *evecs,
                                    double *work, const int64_t *mol_row_off, const uint8_t *active, int32_t *status,
-                                   int max_sweeps, const uint8_t *warm, int mixed_threshold, int density_only,
+                                   int max_sweeps, uint8_t *warm, int mixed_threshold, int density_only,
                                    void *stream) {
   if (!bp || !work) return SEQM_E_ARG;
   if ((warm || mixed_threshold > 0) && !P) return SEQM_E_ARG;  // P's block is used as product scratch

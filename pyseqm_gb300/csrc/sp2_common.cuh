@@ -11,6 +11,8 @@
 
 #include <math.h>
 
+#include <tuple>
+
 #include "common.cuh"
 
 namespace seqm {
@@ -177,13 +179,14 @@ __global__ void k_sp2_check(seqm_batch b, double *__restrict__ st, double eps, i
   else atomicAdd(nrun, 1);
 }
 
-// status[m] = steps, or -1 if still running at the cap
+// status[m] = steps, or -1 if still running at the cap, or SEQM_E_CUDA if the step kernel
+// raised its error word (err, NULL: none)
 __global__ void k_sp2_status(int nmol, const double *__restrict__ st, const uint8_t *__restrict__ active,
-                             int32_t *__restrict__ status) {
+                             int32_t *__restrict__ status, const int *__restrict__ err) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= nmol || (active && !active[m])) return;
   const double *s = st + SP2_NS * m;
-  status[m] = s[S_RUN] != 0.0 ? -1 : (int)s[S_STEPS];
+  status[m] = (err && *err) ? SEQM_E_CUDA : s[S_RUN] != 0.0 ? -1 : (int)s[S_STEPS];
 }
 
 // elementwise P = c1 * A + c2 * A^T (FP64 out) for active molecules (A in T precision)
@@ -304,6 +307,79 @@ __global__ void __launch_bounds__(MW_THREADS) k_sym_gemm(seqm_batch b, const T *
     }
 }
 
+// ------------------------------------------------------------------ device-driven step loop
+// Loop counters of an SP2 call (int words of the driver's scratch): [0] molecules still running
+// after the last check (summed by k_sp2_check), [1] error word, [2] loop trips taken.
+enum { LC_RUN = 0, LC_ERR, LC_TRIPS, LC_WORDS };
+
+// End of one trip of the device-driven loop: the trip counts, the running count is consumed, and
+// the loop's condition (a CUDA graph WHILE node) stays set while molecules run, no error was
+// raised and fewer than max_trips trips were taken.
+__global__ void k_sp2_loop_tail(int *__restrict__ lc, cudaGraphConditionalHandle handle, int max_trips) {
+  const int run = lc[LC_RUN];
+  lc[LC_RUN] = 0;
+  const int trips = ++lc[LC_TRIPS];
+  cudaGraphSetConditional(handle, (run > 0 && lc[LC_ERR] == 0 && trips < max_trips) ? 1u : 0u);
+}
+
+// kernel node of `g` after `ndep` nodes: func<<<grid, block, smem>>>(args...), the arguments
+// converted to the kernel's parameter types and copied into the node
+template <typename... Params, typename... Args>
+cudaError_t add_kernel_node(cudaGraph_t g, cudaGraphNode_t *node, const cudaGraphNode_t *dep, size_t ndep,
+                            void (*func)(Params...), dim3 grid, dim3 block, size_t smem, Args... args) {
+  static_assert(sizeof...(Params) == sizeof...(Args), "argument count");
+  struct Pack {
+    std::tuple<Params...> v;
+  } pack{std::tuple<Params...>(args...)};
+  void *ptrs[sizeof...(Params) > 0 ? sizeof...(Params) : 1];
+  std::apply([&](auto &...e) {
+    int i = 0;
+    ((ptrs[i++] = (void *)&e), ...);
+  }, pack.v);
+  cudaKernelNodeParams p = {};
+  p.func = reinterpret_cast<void *>(func);
+  p.gridDim = grid;
+  p.blockDim = block;
+  p.sharedMemBytes = (unsigned)smem;
+  p.kernelParams = ptrs;
+  p.extra = nullptr;
+  return cudaGraphAddKernelNode(node, g, dep, ndep, &p);
+}
+
+// While `s` is being captured into a CUDA graph, append a WHILE node whose body is built by
+// body(graph, first_dependency_out...) and make the stream's next captured work depend on it.
+// The body must end with k_sp2_loop_tail(handle); the node runs the body at least once per graph
+// launch and again while the tail keeps the condition set, with no host involvement.
+// Returns cudaSuccess or the first failing call's error.
+template <typename BuildBody>
+cudaError_t capture_while_loop(cudaStream_t s, BuildBody build_body) {
+  cudaStreamCaptureStatus cs;
+  unsigned long long id = 0;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t *deps = nullptr;
+  const cudaGraphEdgeData *edges = nullptr;
+  size_t ndeps = 0;
+  cudaError_t e = cudaStreamGetCaptureInfo(s, &cs, &id, &g, &deps, &edges, &ndeps);
+  if (e != cudaSuccess) return e;
+  if (cs != cudaStreamCaptureStatusActive || g == nullptr) return cudaErrorStreamCaptureInvalidated;
+  cudaGraphConditionalHandle handle;
+  if ((e = cudaGraphConditionalHandleCreate(&handle, g, 1u, cudaGraphCondAssignDefault)) != cudaSuccess) return e;
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = handle;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t loop;
+  if ((e = cudaGraphAddNode(&loop, g, deps, edges, ndeps, &np)) != cudaSuccess) return e;
+  if ((e = build_body(np.conditional.phGraph_out[0], handle)) != cudaSuccess) return e;
+  return cudaStreamUpdateCaptureDependencies(s, &loop, nullptr, 1, cudaStreamSetCaptureDependencies);
+}
+
+inline bool stream_capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive;
+}
+
 // grid helpers
 inline dim3 ew_grid(const seqm_batch &b) {
   const size_t nn = (size_t)b.max_norb * b.max_norb;
@@ -315,10 +391,134 @@ inline dim3 gemm64_grid(const seqm_batch &b) {
   return dim3(t, t, (unsigned)b.nmol);
 }
 
-// McWeeny step X <- 3 X^2 - 2 X^3 written as X + D (I - 2X) with D = X^2 - X: X^2 in
-// FP64 gives D exactly, and the correction D (I - 2X), a product of a matrix of the size
+// ------------------------------------------------------------- FP64-accurate X^2 in FP32 pairs
+// GB300 issues FP32 at 64x its FP64 rate, so the one FP64-accurate product of a McWeeny step
+// is formed from FP32 pairs (double-float arithmetic; Dekker 1971, Knuth's TwoSum): X = Xh + Xl
+// with Xh = fl32(X), Xl = fl32(X - Xh) (|Xl| <= 2^-24 |X|), and per term
+//   Xh_ik Xh_kj = p + e exactly (p = fl32(product), e = fma(Xh_ik, Xh_kj, -p)),
+//   cross = Xh_ik Xl_kj + Xl_ik Xh_kj in FP32 (a term of relative size 2^-24),
+// the p's summed exactly into (s, c) by TwoSum and e + cross + the TwoSum errors summed in FP32
+// into c.  Xl Xl (2^-48) is dropped.  For |X| <= 1 with X^2 ~ X (a density) the result's error
+// is ~K 2^-48 at most (about 1e-11 for K = 6000, ~1e-13 typically), FP64 level for the
+// McWeeny correction D = X^2 - X.  About 13 FP32 instructions per term instead of one FP64 FMA.
+__global__ void __launch_bounds__(EW_THREADS) k_split_pair(seqm_batch b, const double *__restrict__ X,
+                                                           float *__restrict__ Xh, float *__restrict__ Xl,
+                                                           const uint8_t *__restrict__ active) {
+  const int m = blockIdx.y;
+  if (active && !active[m]) return;
+  const int n = b.mol_norb[m];
+  const size_t nn = (size_t)n * n, base = (size_t)blockIdx.x * EW_CHUNK;
+  if (base >= nn) return;
+  const size_t mo = b.mol_mat_off[m];
+  for (size_t idx = base + threadIdx.x; idx < nn && idx < base + EW_CHUNK; idx += EW_THREADS) {
+    const double x = X[mo + idx];
+    const float h = (float)x;
+    Xh[mo + idx] = h;
+    Xl[mo + idx] = (float)(x - (double)h);
+  }
+}
+
+// C = X X (symmetric X given as FP32 pairs, C in FP64): upper 64 x 64 output tiles with their
+// mirror, 256 threads of 4 x 4 outputs, 16-deep K slabs double-buffered in shared memory and
+// read along rows of X (symmetric), so every global load is coalesced.
+constexpr int DF_T = 64, DF_K = 16, DF_THREADS = 256;
+__device__ __forceinline__ void two_sum_acc(float &s, float &c, float p) {
+  const float t = s + p;
+  const float z = t - s;
+  c += (s - (t - z)) + (p - z);
+  s = t;
+}
+__global__ void __launch_bounds__(DF_THREADS) k_sym_gemm_pair(seqm_batch b, const float *__restrict__ Xh,
+                                                              const float *__restrict__ Xl, double *__restrict__ Cm,
+                                                              const uint8_t *__restrict__ active) {
+  const int m = blockIdx.z;
+  if (active && !active[m]) return;
+  const int n = b.mol_norb[m];
+  const int i0 = blockIdx.y * DF_T, j0 = blockIdx.x * DF_T;
+  if (i0 >= n || j0 >= n || blockIdx.y > blockIdx.x) return;
+  const size_t mo = b.mol_mat_off[m];
+  const float *H = Xh + mo, *L = Xl + mo;
+  __shared__ __align__(16) float Ah[2][DF_K][DF_T], Al[2][DF_K][DF_T], Bh[2][DF_K][DF_T], Bl[2][DF_K][DF_T];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  // slab loader: element e = threadIdx.x + 256 q (q = 0..3) of the 16 x 64 slab, row e / 64, col e % 64
+  float rah[4], ral[4], rbh[4], rbl[4];
+  auto load = [&](int k0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int e = threadIdx.x + DF_THREADS * q, kk = e >> 6, c = e & 63;
+      const bool kin = k0 + kk < n;
+      const size_t ra = (size_t)(k0 + kk) * n + i0 + c, rb = (size_t)(k0 + kk) * n + j0 + c;
+      const bool ina = kin && i0 + c < n, inb = kin && j0 + c < n;
+      rah[q] = ina ? H[ra] : 0.0f;
+      ral[q] = ina ? L[ra] : 0.0f;
+      rbh[q] = inb ? H[rb] : 0.0f;
+      rbl[q] = inb ? L[rb] : 0.0f;
+    }
+  };
+  auto store = [&](int buf) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int e = threadIdx.x + DF_THREADS * q, kk = e >> 6, c = e & 63;
+      Ah[buf][kk][c] = rah[q];
+      Al[buf][kk][c] = ral[q];
+      Bh[buf][kk][c] = rbh[q];
+      Bl[buf][kk][c] = rbl[q];
+    }
+  };
+  float s[4][4] = {}, c[4][4] = {};
+  load(0);
+  store(0);
+  __syncthreads();
+  int buf = 0;
+  for (int k0 = 0; k0 < n; k0 += DF_K) {
+    const bool more = k0 + DF_K < n;
+    if (more) load(k0 + DF_K);
+#pragma unroll 4
+    for (int kk = 0; kk < DF_K; ++kk) {
+      const float4 ah = *reinterpret_cast<const float4 *>(&Ah[buf][kk][4 * ty]);
+      const float4 al = *reinterpret_cast<const float4 *>(&Al[buf][kk][4 * ty]);
+      const float4 bh = *reinterpret_cast<const float4 *>(&Bh[buf][kk][4 * tx]);
+      const float4 bl = *reinterpret_cast<const float4 *>(&Bl[buf][kk][4 * tx]);
+      const float av[4] = {ah.x, ah.y, ah.z, ah.w}, alv[4] = {al.x, al.y, al.z, al.w};
+      const float bv[4] = {bh.x, bh.y, bh.z, bh.w}, blv[4] = {bl.x, bl.y, bl.z, bl.w};
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float p = av[r] * bv[q];
+          const float e = fmaf(av[r], bv[q], -p);
+          const float x = fmaf(av[r], blv[q], alv[r] * bv[q]);
+          two_sum_acc(s[r][q], c[r][q], p);
+          c[r][q] += e + x;
+        }
+    }
+    if (more) store(buf ^ 1);
+    __syncthreads();
+    buf ^= 1;
+  }
+  double *C = Cm + mo;
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int row = i0 + 4 * ty + r, col = j0 + 4 * tx + q;
+      if (row < n && col < n) {
+        const double v = (double)s[r][q] + (double)c[r][q];
+        C[(size_t)row * n + col] = v;
+        C[(size_t)col * n + row] = v;
+      }
+    }
+}
+
+inline dim3 pair_gemm_grid(const seqm_batch &b) {
+  const unsigned t = (unsigned)((b.max_norb + DF_T - 1) / DF_T);
+  return dim3(t, t, (unsigned)b.nmol);
+}
+
+// McWeeny step X <- 3 X^2 - 2 X^3 written as X + D (I - 2X) with D = X^2 - X: X^2 FP64-accurate
+// gives D exactly, and the correction D (I - 2X), a product of a matrix of the size
 // of the idempotency error, is formed in FP32 (relative error ~1e-7 of a term <= |D|),
-// so every step is FP64-accurate at one FP64 product instead of two.
+// so every step is FP64-accurate at one FP64-accurate product instead of two.
 // Df = float(Y - Z), Bf = float(I - 2 Z)
 __global__ void __launch_bounds__(EW_THREADS) k_mw_split(seqm_batch b, const double *__restrict__ Y,
                                                          const double *__restrict__ Z, float *__restrict__ Df,
@@ -368,11 +568,16 @@ __global__ void __launch_bounds__(EW_THREADS) k_mw_update(seqm_batch b, const do
 // McWeeny refinement of the density P (X = P/2), `steps` times.  Y, Z: FP64 scratch of the
 // batch's matrix size; Df, Bf: FP32 scratch of the same size (Y doubles as the FP32 product).
 inline void mcweeny(const seqm_batch &b, double *P, double *Y, double *Z, float *Df, float *Bf,
-                    const uint8_t *active, int steps, cudaStream_t s) {
+                    const uint8_t *active, int steps, cudaStream_t s, bool pair_product = false) {
   float *Cf = reinterpret_cast<float *>(Y);
   for (int k = 0; k < steps; ++k) {
     k_ew_axpby<<<ew_grid(b), EW_THREADS, 0, s>>>(b, 0.5, P, 0.0, nullptr, Z, active);        // Z = X
-    k_sym_gemm<double><<<gemm64_grid(b), MW_THREADS, 0, s>>>(b, Z, Z, Y, active, nullptr);    // Y = X^2 (FP64)
+    if (pair_product) {  // Y = X^2 from FP32 pairs (Df, Bf hold Xh, Xl until k_mw_split)
+      k_split_pair<<<ew_grid(b), EW_THREADS, 0, s>>>(b, Z, Df, Bf, active);
+      k_sym_gemm_pair<<<pair_gemm_grid(b), DF_THREADS, 0, s>>>(b, Df, Bf, Y, active);
+    } else {
+      k_sym_gemm<double><<<gemm64_grid(b), MW_THREADS, 0, s>>>(b, Z, Z, Y, active, nullptr);  // Y = X^2 (FP64)
+    }
     k_mw_split<<<ew_grid(b), EW_THREADS, 0, s>>>(b, Y, Z, Df, Bf, active);                   // D, I - 2X
     k_sym_gemm<float><<<gemm64_grid(b), MW_THREADS, 0, s>>>(b, Df, Bf, Cf, active, nullptr);  // D (I - 2X)
     k_mw_update<<<ew_grid(b), EW_THREADS, 0, s>>>(b, Z, Cf, P, active);                      // P = 2(X + ...)

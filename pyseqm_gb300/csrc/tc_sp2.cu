@@ -460,9 +460,7 @@ extern "C" int seqm_density_sp2_tc(const seqm_batch *bp, const double *F, double
   cudaStream_t s = (cudaStream_t)stream;
   eps = eps > 1.0e-3 ? 1.0e-3 : (eps < 1.0e-7 ? 1.0e-7 : eps);
   int64_t total = 0;
-  if (cudaMemcpyAsync(&total, b.mol_mat_off + b.nmol, sizeof(int64_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-      cudaStreamSynchronize(s) != cudaSuccess)
-    return SEQM_E_CUDA;
+  if (batch_total(b, s, &total) != SEQM_OK) return SEQM_E_CUDA;
   const TcWork w = tc_work_layout(total, b.nmol, b.max_norb);
   uint8_t *base = static_cast<uint8_t *>(work);
   float *X = reinterpret_cast<float *>(base + w.x);
@@ -475,7 +473,7 @@ extern "C" int seqm_density_sp2_tc(const seqm_batch *bp, const double *F, double
   int *cnt = reinterpret_cast<int *>(base + w.cnt);
   int64_t *xs_off = reinterpret_cast<int64_t *>(base + w.xs_off);
   uint8_t *xs[4] = {base + w.xs[0], base + w.xs[1], base + w.xs[2], base + w.xs[3]};  // hi, lo of two buffers
-  if (cudaMemsetAsync(cnt, 0, 2 * sizeof(int), s) != cudaSuccess) return SEQM_E_CUDA;
+  if (cudaMemsetAsync(cnt, 0, LC_WORDS * sizeof(int), s) != cudaSuccess) return SEQM_E_CUDA;
   k_sp2_rows<<<rows_grid(b), 256, 0, s>>>(b, F, rowlo, rowhi, active);
   k_sp2_bounds<<<b.nmol, 256, 0, s>>>(b, rowlo, rowhi, st, active);
   k_sp2_scale<float><<<ew_grid(b), EW_THREADS, 0, s>>>(b, F, X, st);
@@ -490,6 +488,28 @@ extern "C" int seqm_density_sp2_tc(const seqm_batch *bp, const double *F, double
   }
   const dim3 grid((unsigned)(nb * (nb + 1) / 2), (unsigned)b.nmol);
   int rc = SEQM_OK, cur = 0;
+  if (stream_capturing(s)) {
+    // inside a CUDA graph capture: the step loop becomes a WHILE node ended on the device; one
+    // trip takes two steps so that the split-tile buffers ping-pong back to where they started
+    // (a molecule that stops after the first step of a trip is skipped by the second)
+    const cudaError_t e = capture_while_loop(s, [&](cudaGraph_t body, cudaGraphConditionalHandle h) {
+      cudaGraphNode_t n[5];
+      cudaError_t r = cudaSuccess;
+      for (int half = 0; half < 2 && r == cudaSuccess; ++half) {
+        const int c = half;
+        r = add_kernel_node(body, &n[2 * half], half ? &n[1] : nullptr, half ? 1 : 0, k_tc_sp2_step, grid,
+                            dim3(TC_THREADS), TC_SMEM, b, X, (const uint8_t *)xs[2 * c], (const uint8_t *)xs[2 * c + 1],
+                            xs[2 - 2 * c], xs[3 - 2 * c], (const int64_t *)xs_off, st, cnt + LC_ERR);
+        if (r == cudaSuccess)
+          r = add_kernel_node(body, &n[2 * half + 1], &n[2 * half], 1, k_sp2_check, dim3((b.nmol + 127) / 128),
+                              dim3(128), 0, b, st, eps, 1, cnt + LC_RUN);
+      }
+      if (r == cudaSuccess)
+        r = add_kernel_node(body, &n[4], &n[3], 1, k_sp2_loop_tail, dim3(1), dim3(1), 0, cnt, h, (max_iter + 1) / 2);
+      return r;
+    });
+    if (e != cudaSuccess) return SEQM_E_CUDA;
+  } else
   for (int it = 0; it < max_iter; ++it) {
     if (cudaMemsetAsync(cnt, 0, sizeof(int), s) != cudaSuccess) { rc = SEQM_E_CUDA; break; }
     k_tc_sp2_step<<<grid, TC_THREADS, TC_SMEM, s>>>(b, X, xs[2 * cur], xs[2 * cur + 1], xs[2 - 2 * cur],
@@ -504,7 +524,7 @@ extern "C" int seqm_density_sp2_tc(const seqm_batch *bp, const double *F, double
     if (h[0] == 0) break;
   }
   if (rc != SEQM_OK) return rc;
-  if (status) k_sp2_status<<<(b.nmol + 127) / 128, 128, 0, s>>>(b.nmol, st, active, status);
+  if (status) k_sp2_status<<<(b.nmol + 127) / 128, 128, 0, s>>>(b.nmol, st, active, status, cnt + LC_ERR);
   // one FP32 McWeeny step X <- 3X^2 - 2X^3 takes the eigenvalues from the tensor-core level
   // (~1e-4 off 0/1 at the relaxed stop) to the FP32 accumulation level (~1e-6), so one
   // FP64-accurate step (mcweeny) then reaches ~1e-11
@@ -513,6 +533,6 @@ extern "C" int seqm_density_sp2_tc(const seqm_batch *bp, const double *F, double
   k_sym_gemm<float><<<gemm64_grid(b), MW_THREADS, 0, s>>>(b, X2, X, X3, active, nullptr);
   k_mw32<<<ew_grid(b), EW_THREADS, 0, s>>>(b, X2, X3, X, active);
   k_ew_sym<float><<<ew_grid(b), EW_THREADS, 0, s>>>(b, X, 1.0, 1.0, P, active);  // P = X + X^T
-  mcweeny(b, P, Y, Z, X, X2, active, mcweeny_steps, s);  // X, X2 are free after P = X + X^T
+  mcweeny(b, P, Y, Z, X, X2, active, mcweeny_steps, s, true);  // X, X2 are free after P = X + X^T
   return launch_check();
 }

@@ -197,6 +197,7 @@ class Layout:
             pair_zmax=self.pair_par[1] if self.pair_par is not None else -1, pad3_=0,
             mol_nsuper=d["nsuper"].data_ptr() if "nsuper" in d else None,
             pair_skip=d["pair_skip"].data_ptr() if "pair_skip" in d else None,
+            mat_total=int(self.mat_off[-1]),
         )
         set_size_classes(self._struct, self.norb[self.order] if self.nmol else np.zeros(0, np.int64))
         return self

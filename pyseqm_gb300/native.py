@@ -29,7 +29,7 @@ PAR = {n: i for i, n in enumerate(PAR_NAMES)}
 EXPORTS = ["seqm_hcore", "seqm_fock", "seqm_density_jacobi", "seqm_density_jacobi_noalloc", "seqm_density_sp2",
            "seqm_density_sp2_tc", "seqm_mix", "seqm_energy_error",
            "seqm_initial_density", "seqm_pair_sum", "seqm_energy_grad", "seqm_sp2_tc_work_bytes", "seqm_diis_init",
-           "seqm_diis_extrapolate", "seqm_diis_mix", "seqm_fock_u", "seqm_energy_error_u", "seqm_fock_general", "seqm_energy_grad_excited", "seqm_version"]
+           "seqm_diis_extrapolate", "seqm_diis_mix", "seqm_fock_u", "seqm_energy_error_u", "seqm_fock_general", "seqm_energy_grad_excited", "seqm_scf_step", "seqm_version"]
 DIIS_STATE = 124  # SEQM_DIIS_STATE
 
 _P = ctypes.c_void_p
@@ -49,8 +49,17 @@ class SeqmBatch(ctypes.Structure):
         ("nclass", ctypes.c_int32), ("pad2_", ctypes.c_int32), ("class_end", ctypes.c_int32 * MAX_CLASSES),
         ("class_norb", ctypes.c_int32 * MAX_CLASSES),
         ("pair_par", _P), ("pair_zmax", ctypes.c_int32), ("pad3_", ctypes.c_int32), ("mol_nsuper", _P),
-        ("pair_skip", _P),
+        ("pair_skip", _P), ("mat_total", ctypes.c_int64),
     ]
+
+
+class ScfState(ctypes.Structure):
+    """seqm_scf_state: device pointers and settings of one SCF iteration after the density step."""
+    _fields_ = [(n, _P) for n in ("P", "Pnew", "Pold", "old2", "H", "F", "w_xx", "w_xh", "w_hh", "Eelec", "Eout",
+                                  "err", "dm_err", "dm_el", "mol_row_off", "iters", "active", "diis_err",
+                                  "nactive")] + [
+        ("mixing", ctypes.c_int32), ("pad_", ctypes.c_int32), ("alpha", ctypes.c_double),
+        ("occupation", ctypes.c_double), ("eps", ctypes.c_double)]
 
 
 _lib = None
@@ -94,6 +103,7 @@ def load(path=None):
         "seqm_energy_error_u": [B, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, f64, _P],
         "seqm_fock_general": [B, i32, _P, _P, _P, _P, _P, ctypes.c_int64, _P, _P],
         "seqm_energy_grad_excited": [B, _P, _P, _P, _P, _P, _P, _P, _P],
+        "seqm_scf_step": [B, ctypes.POINTER(ScfState), _P],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

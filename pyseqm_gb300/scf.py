@@ -58,6 +58,8 @@ class BatchSCF:
         self.dm_el = torch.ones(max(1, nm), **f64)
         self.Enuc = torch.zeros(max(1, nm), **f64)
         self.active = torch.ones(max(1, nm), dtype=torch.uint8, device=dev)
+        self.nactive = torch.zeros(1, dtype=torch.int32, device=dev)  # molecules active after an iteration
+        self.h_nactive = torch.zeros(2, dtype=torch.int32, pin_memory=dev.type == "cuda")
         self.iters = torch.zeros(max(1, nm), dtype=torch.int32, device=dev)
         self.status = torch.zeros(max(1, nm), dtype=torch.int32, device=dev)
         # 1 once the molecule's eigenvector rows in `work` are valid (warm-started Jacobi)
@@ -208,7 +210,7 @@ class BatchSCF:
     def _sp2_fp64(self, out, eps, active, subset=False):
         b, nm, maxn, act, status = self._sp2_target(active, subset)
         T = int(self.L.mat_off[-1])
-        nd = 2 * T + (11 + 2 * maxn) * nm + 1  # SEQM_SP2_WORK_DOUBLES
+        nd = 2 * T + (11 + 2 * maxn) * nm + 2  # SEQM_SP2_WORK_DOUBLES
         if self.sp2_work is None or self.sp2_work.numel() < nd:
             self.sp2_work = torch.empty(nd, dtype=torch.float64, device=self.L.device)
         self.launches += 1
@@ -260,11 +262,7 @@ class BatchSCF:
                                                   self.mixed_threshold,
                                                   int(density_only) if self.first_order_density else 0,
                                                   self._s()),
-                     "seqm_density_jacobi")
-        if act_s is None:
-            self.warm.fill_(1)
-        else:
-            self.warm.bitwise_or_(act_s)
+                     "seqm_density_jacobi")  # sets warm[m] for the molecules it solved
 
     def energy_error(self, eps, first=False):
         self.launches += 1
@@ -314,6 +312,7 @@ class BatchSCF:
         self._sp2 = tuple(sp2)
         self._diis = int(converger[0]) == 2
         self._diis_err = None
+        self._state = self._scf_state()
         if self._diis:
             dev = L.device
             if self._diis_hist is None:
@@ -321,9 +320,23 @@ class BatchSCF:
                 self._diis_state = torch.empty(max(1, native.DIIS_STATE * L.nmol), dtype=torch.float64, device=dev)
                 self._diis_err_buf = torch.empty(max(1, L.nmol), dtype=torch.float64, device=dev)
             self._diis_err = self._diis_err_buf
+            self._state.diis_err = self._diis_err.data_ptr()
+            self._state.mixing = -1
             self.launches += 1
             native.check(self.lib.seqm_diis_init(b, native.ptr(self._diis_state), native.ptr(self._diis_err),
                                                  self._s()), "seqm_diis_init")
+
+    def _scf_state(self):
+        """seqm_scf_state of this solver's buffers and the current converger."""
+        st = native.ScfState()
+        for name in ("P", "Pnew", "Pold", "old2", "H", "F", "w_xx", "w_xh", "w_hh", "Eelec", "Eout", "err", "dm_err",
+                     "dm_el", "iters", "active", "nactive"):
+            setattr(st, name, getattr(self, name).data_ptr())
+        st.mol_row_off = self.L.dev["row_off"].data_ptr()
+        st.diis_err = None
+        st.mixing = 0 if self._linear else 1
+        st.alpha, st.occupation, st.eps = self._alpha, 2.0, self._eps
+        return st
 
     def step(self):
         """One SCF iteration of every still-active molecule (density, mixing, F(P), E(P), get_error);
@@ -338,32 +351,60 @@ class BatchSCF:
                                                         native.ptr(self._diis_err), native.ptr(self.active),
                                                         native.ptr(self.iters), self._s()), "seqm_diis_extrapolate")
         self.density(self.Pnew, self._sp2, active=self.active, density_only=True)
-        self.launches += 1
         if self._diis:
+            self.launches += 1
             native.check(self.lib.seqm_diis_mix(L.struct, native.ptr(self.P), native.ptr(self.Pnew),
                                                 native.ptr(self.Pold), native.ptr(self._diis_state),
                                                 native.ptr(self.active), self._s()), "seqm_diis_mix")
-        else:
-            native.check(self.lib.seqm_mix(L.struct, native.ptr(self.P), native.ptr(self.Pnew),
-                                           native.ptr(self.Pold), native.ptr(self.old2), native.ptr(L.dev["row_off"]),
-                                           native.ptr(self.iters), int(self._linear), self._alpha, 2.0,
-                                           native.ptr(self.active), self._s()), "seqm_mix")
-        self.fock(self.active)
-        self.energy_error(self._eps)
+        if self.profile_fock:
+            # the same kernels as seqm_scf_step, called one by one so that the Fock build is timed alone
+            if not self._diis:
+                self.launches += 1
+                native.check(self.lib.seqm_mix(L.struct, native.ptr(self.P), native.ptr(self.Pnew),
+                                               native.ptr(self.Pold), native.ptr(self.old2),
+                                               native.ptr(L.dev["row_off"]), native.ptr(self.iters), int(self._linear),
+                                               self._alpha, 2.0, native.ptr(self.active), self._s()), "seqm_mix")
+            self.fock(self.active)
+            self.energy_error(self._eps)
+            self.nactive.copy_(self.active[: L.nmol].sum())
+            return
+        # mixing, Fock build, energy and convergence test, count of the molecules still active
+        self.launches += 2 + (0 if self._diis else 1)
+        native.check(self.lib.seqm_scf_step(L.struct, ctypes.byref(self._state), self._s()), "seqm_scf_step")
 
     def max_loops(self, max_iter=MAX_ITER):
         """Iterations the reference's loop allows: MAX_ITER + 1 for linear mixing (scf_loop.py:250)
         and DIIS (:974), MAX_ITER adaptive (:505)."""
         return max_iter + 1 if (self._linear or self._diis) else max_iter
 
+    def iterate(self, max_iter=MAX_ITER):
+        """SCF iterations until no molecule is active or the cap.  The host keeps one iteration
+        queued ahead of the one whose active count it reads (copied to pinned memory behind each
+        iteration), so the GPU does not wait for the host between iterations; the iteration queued
+        after the last molecule retired finds nothing active and every kernel of it returns at
+        once.  Returns the per-molecule not-converged mask (host numpy)."""
+        stream = self.stream if self.stream is not None else torch.cuda.current_stream(self.L.device)
+        queued = []
+        for it in range(self.max_loops(max_iter)):
+            self.step()
+            slot = it & 1
+            self.h_nactive[slot].copy_(self.nactive[0], non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(stream)
+            queued.append((ev, slot))
+            if len(queued) == 2:
+                ev0, s0 = queued.pop(0)
+                ev0.synchronize()
+                if int(self.h_nactive[s0]) == 0:
+                    break
+        for ev, _ in queued:
+            ev.synchronize()
+        return self.active[: self.L.nmol].bool().cpu().numpy()
+
     def scf(self, eps, converger=(1,), sp2=(False,), P0=None, max_iter=MAX_ITER):
         """Run the SCF; returns the per-molecule not-converged mask (host numpy)."""
         self.start(eps, converger, sp2, P0)
-        for _ in range(self.max_loops(max_iter)):
-            self.step()
-            if int(self.active.sum()) == 0:
-                break
-        return self.active[: self.L.nmol].bool().cpu().numpy()
+        return self.iterate(max_iter)
 
     def resume(self, xyz, eps, converger=(1,), sp2=(False,), max_iter=MAX_ITER):
         """Next geometry of the same molecules (an MD step, cf. MolecularDynamics.py:815-825,
@@ -373,11 +414,7 @@ class BatchSCF:
         self.L.set_coordinates(xyz)
         self.hcore()
         self.start(eps, converger, sp2, P0=self.P, keep_warm=True)
-        for _ in range(self.max_loops(max_iter)):
-            self.step()
-            if int(self.active.sum()) == 0:
-                break
-        return self.active[: self.L.nmol].bool().cpu().numpy()
+        return self.iterate(max_iter)
 
     def final(self, want_vectors=True):
         """Fock matrix of the converged density, orbital energies / vectors, energies."""
@@ -465,10 +502,6 @@ class BatchUHF(BatchSCF):
                                                       int(density_only) if self.first_order_density else 0,
                                                       self._s()), "seqm_density_jacobi")
             Pn.mul_(0.5)
-            if active is None:
-                warm.fill_(1)
-            else:
-                warm.bitwise_or_(active)
 
     def start(self, eps, converger=(1,), sp2=(False,), P0=None, keep_warm=False):
         """P0: (Pa, Pb) packed spin densities, or None for half the restricted guess each."""
@@ -519,16 +552,13 @@ class BatchUHF(BatchSCF):
                                            self._alpha, 1.0, native.ptr(self.active), self._s()), "seqm_mix")
         self.fock(self.active)
         self.energy_error(self._eps)
+        self.nactive.copy_(self.active[: L.nmol].sum())
 
     def resume(self, xyz, eps, converger=(1,), sp2=(False,), max_iter=MAX_ITER):
         self.L.set_coordinates(xyz)
         self.hcore()
         self.start(eps, converger, sp2, P0=(self.P.clone(), self.Pb.clone()), keep_warm=True)
-        for _ in range(self.max_loops(max_iter)):
-            self.step()
-            if int(self.active.sum()) == 0:
-                break
-        return self.active[: self.L.nmol].bool().cpu().numpy()
+        return self.iterate(max_iter)
 
     def final(self, want_vectors=True):
         """Fock matrices of the converged spin densities, orbital energies (and vectors) per spin,

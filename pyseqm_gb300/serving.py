@@ -15,9 +15,10 @@ own, so the SP2 grids cover only their tiles.
 
 Two forms share the request format and the result record:
 
-* ``ServingLoop(form="serving")``: tensor-core SP2 with FP64 McWeeny refinement
+* ``ServingLoop(form="serving")``: tensor-core SP2 with FP64-accurate McWeeny refinement
   above the Jacobi limit, FP32-presweep + FP64 Jacobi below, continuous admission;
-  a Jacobi-sized cohort captures its SCF iteration once as a CUDA graph and replays it.
+  every cohort captures its SCF iteration once as a CUDA graph after its first iteration and
+  replays it (an SP2 cohort's step loop is a conditional node ended on the device).
 * ``ServingLoop(form="plain")``: FP64 kernels only, one batch at a time: the
   batch is everything that has arrived when the previous batch finished, solved
   to completion (its force requests, converged tighter, as a second solve)
@@ -111,7 +112,7 @@ class _Cohort:
 
     def __init__(self, reqs, method, eps, form, device, large, stream, graphs=False):
         self.reqs = reqs
-        self.graphs = graphs and not large  # the SP2 step loop synchronises with the host: not capturable
+        self.graphs = graphs
         self.graph = None
         self.method = method
         self.eps = eps
@@ -133,16 +134,6 @@ class _Cohort:
             s.hcore()
             s.start(self.eps, (1,))
             self.s = s
-            if self.graphs:
-                # one SCF iteration (density, mixing, Fock, energy + test) as a CUDA graph,
-                # replayed every iteration: the buffers and the retirement flags live on the device
-                self.graph = torch.cuda.CUDAGraph()
-                before = s.launches
-                with _CAPTURE_LOCK, torch.cuda.graph(self.graph, stream=self.stream,
-                                                     capture_error_mode="thread_local"):
-                    s.step()
-                self.graph_launches = s.launches - before
-                s.launches = before  # counted at every replay
             nm = self.L.nmol
             pin = dict(pin_memory=True)
             self.h_active = torch.empty(nm, dtype=torch.uint8, **pin)
@@ -163,6 +154,8 @@ class _Cohort:
                 s.launches += self.graph_launches
             else:
                 s.step()
+                if self.graphs:
+                    self._capture()
             self.iteration += 1
             self.h_active.copy_(s.active[:nm], non_blocking=True)
             self.h_E[0].copy_(s.Eout[:nm], non_blocking=True)
@@ -194,6 +187,20 @@ class _Cohort:
     def launches(self):
         return self.s.launches
 
+    def _capture(self):
+        """Record one SCF iteration (density step, mixing, Fock build, energy and test) as a CUDA
+        graph, replayed for every later iteration: buffers and retirement flags stay on the device,
+        and an SP2 density step's loop is a conditional node the device ends.  Capture follows the
+        first, eager iteration, which has set up everything done once (scratch buffers, kernel
+        attributes); capturing records the launches without running them."""
+        s = self.s
+        self.graph = torch.cuda.CUDAGraph()
+        before = s.launches
+        with _CAPTURE_LOCK, torch.cuda.graph(self.graph, stream=self.stream, capture_error_mode="thread_local"):
+            s.step()
+        self.graph_launches = s.launches - before
+        s.launches = before  # counted at every replay
+
     def _forces(self):
         """dE_tot/dR (natoms, 3) of the whole cohort at the current densities (host array)."""
         L, s = self.L, self.s
@@ -214,7 +221,7 @@ class _Cohort:
 class ServingLoop:
     """Request loop over one GPU (see the module docstring).
 
-    graphs: Jacobi-sized cohorts replay their SCF iteration as a CUDA graph (serving form);
+    graphs: every cohort replays its SCF iteration as a CUDA graph after the first (serving form);
     eps: SCF threshold (get_error) of energy requests; eps_forces: of force requests (forces
     are linear in the density error where the energy is quadratic, so they converge tighter
     and are admitted in cohorts of their own); budget_bytes: device memory the live cohorts

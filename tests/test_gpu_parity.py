@@ -183,3 +183,26 @@ def test_edge_case_molecules_match_oracle():
     out = run_energy(species, coords, "AM1", eps=1e-8, converger=(1,), device="cuda")
     assert not out["notconverged"].any()
     np.testing.assert_allclose(out["Etot"].cpu().numpy(), ref["Etot"], atol=1e-6, rtol=0)
+
+
+def test_scf_step_entry_matches_the_separate_calls():
+    """seqm_scf_step (mixing + Fock build + energy/test + active count in one call) against the
+    three entry points called one by one: the same kernels, so the same iterations and energies."""
+    from pyseqm_gb300 import workloads
+    from pyseqm_gb300.layout import Layout
+    from pyseqm_gb300.scf import BatchSCF
+
+    mols = workloads.mixed_batch(24, seed=11, alkane_range=(1, 10), water_range=(2, 12))
+    species, coords = workloads.pad_batch(mols)
+    L = Layout.from_padded(species, coords, "AM1").to_device("cuda")
+    out = []
+    for split in (False, True):
+        s = BatchSCF(L)
+        s.profile_fock = split
+        s.hcore()
+        assert not s.scf(1e-8, (1,)).any()
+        E, En = s.final(want_vectors=False)
+        out.append(((E + En).cpu().numpy(), s.iters[: L.nmol].cpu().numpy(), int(s.nactive[0])))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    assert out[0][2] == 0

@@ -56,12 +56,21 @@ def test_serving_within_tolerance_of_fp64(mix):
 
 
 def test_graph_replay_matches_eager_launches(mix):
-    """A Jacobi-sized cohort replaying its captured SCF iteration gives the eager results."""
-    mols = [m for m in _mols() if serving.norb_of(m[0]) <= 160]
+    """Cohorts replaying their captured SCF iteration give the eager results: Jacobi-sized ones
+    bit for bit (the same kernels in the same order), SP2-sized ones, whose captured step loop is
+    a conditional node ended on the device, to 1e-7 eV (their traces are summed with atomics, so
+    two eager runs differ at that level too)."""
+    mols = _mols()
     eager = serving.ServingLoop("PM3", eps=EPS, graphs=False).run(serving.make_requests(mols))
     graph = serving.ServingLoop("PM3", eps=EPS, graphs=True).run(serving.make_requests(mols))
-    for a, g in zip(eager, graph):
+    for m, a, g in zip(mols, eager, graph):
+        assert a.converged and g.converged
         assert a.iterations == g.iterations
-        assert a.Etot == g.Etot
+        if serving.norb_of(m[0]) > 160:
+            assert abs(a.Etot - g.Etot) <= 1e-7
+            if a.forces is not None:
+                np.testing.assert_allclose(a.forces, g.forces, atol=1e-5, rtol=0)
+            continue
+        assert a.Etot == g.Etot, (serving.norb_of(m[0]), a.Etot - g.Etot)
         if a.forces is not None:
             np.testing.assert_array_equal(a.forces, g.forces)

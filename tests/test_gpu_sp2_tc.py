@@ -63,3 +63,47 @@ def test_large_molecules_take_sp2_and_match_oracle(large):
     for m in (0, 2):
         assert int(L.norb[m]) > 160
         assert _idempotency(L, s.P, m) < 1e-9
+
+
+@pytest.mark.parametrize("large", ["tc", "fp64"])
+def test_captured_sp2_iteration_matches_eager(large):
+    """One SCF iteration of a batch of molecules above the Jacobi limit captured in a CUDA graph
+    (the SP2 step loop becomes a conditional WHILE node that the device ends, no host
+    synchronisation) and replayed to convergence gives the eager solve's iterations and
+    energies."""
+    from pyseqm_gb300 import workloads
+    from pyseqm_gb300.layout import Layout
+    from pyseqm_gb300.scf import BatchSCF
+
+    rng = np.random.default_rng(33)
+    mols = [workloads.water_cluster(30, rng), workloads.alkane(28, rng, 0.03), workloads.water_cluster(40, rng)]
+    species, coords = workloads.pad_batch(mols)
+    eps = SCF_EPS_MIXED if large == "tc" else 1e-7
+    L = Layout.from_padded(species, coords, "PM3").to_device("cuda")
+    eager = BatchSCF(L)
+    eager.large_density = large
+    eager.hcore()
+    assert not eager.scf(eps, (1,)).any()
+    E_eager = eager.final(want_vectors=False)
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        s = BatchSCF(L, stream=stream)
+        s.large_density = large
+        s.hcore()
+        s.start(eps, (1,))
+        s.step()  # eager first iteration: scratch buffers and kernel attributes
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            s.step()
+        for _ in range(200):
+            g.replay()
+            if not bool(s.active[: L.nmol].any()):
+                break
+        E = s.final(want_vectors=False)
+    torch.cuda.synchronize()
+    assert not bool(s.active[: L.nmol].any())
+    np.testing.assert_array_equal(s.iters[: L.nmol].cpu().numpy(), eager.iters[: L.nmol].cpu().numpy())
+    # the tensor-core form sums its traces with atomics: two eager solves differ at ~1e-9 eV too
+    np.testing.assert_allclose((E[0] + E[1]).cpu().numpy(), (E_eager[0] + E_eager[1]).cpu().numpy(),
+                               atol=1e-7 if large == "tc" else 1e-9, rtol=0)
+    assert bool((s.status[: L.nmol] > 0).all())

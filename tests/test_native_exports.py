@@ -61,3 +61,30 @@ def test_batch_struct_layout_matches_header(tmp_path):
     assert int(out["sizeof"]) == ctypes.sizeof(native.SeqmBatch)
     for f in fields:
         assert int(out[f]) == getattr(native.SeqmBatch, f).offset, f
+
+
+def test_scf_state_struct_layout_matches_header(tmp_path):
+    """The ctypes seqm_scf_state has the header's size and field offsets."""
+    import shutil
+    import subprocess
+
+    import pytest
+
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    fields = [f[0] for f in native.ScfState._fields_]
+    src = tmp_path / "probe.c"
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "pyseqm_gb300.h"', "int main(void) {",
+             '  printf("sizeof %zu\\n", sizeof(seqm_scf_state));']
+    lines += [f'  printf("{f} %zu\\n", offsetof(seqm_scf_state, {f}));' for f in fields]
+    lines += ["  return 0;", "}"]
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "probe"
+    subprocess.run(["gcc", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    out = dict(line.split() for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                       text=True).stdout.splitlines())
+    import ctypes as ct
+
+    assert int(out["sizeof"]) == ct.sizeof(native.ScfState)
+    for f in fields:
+        assert int(out[f]) == getattr(native.ScfState, f).offset, f

@@ -283,6 +283,7 @@ __device__ __forceinline__ void finish_error(const seqm_batch &b, int m, double 
 }
 
 constexpr int NT_RED = 512, EE_SLICES = 16, EE_UNROLL = 4;
+constexpr int EE_WARP_MAX = 160;  // larger molecules take the cluster kernel
 __global__ void __launch_bounds__(NT_RED) k_energy_error(seqm_batch b, const double *__restrict__ P,
                                                          const double *__restrict__ Pold, const double *__restrict__ H,
                                                          const double *__restrict__ F, double *Eelec, double *Eout,
@@ -295,6 +296,7 @@ __global__ void __launch_bounds__(NT_RED) k_energy_error(seqm_batch b, const dou
   const int m = blockIdx.x / cs, r = (int)cl.block_rank();
   if (!is_active(active, m)) return;  // uniform over the cluster
   const int norb = b.mol_norb[m];
+  if (norb <= EE_WARP_MAX) return;  // k_energy_error_warp's molecule
   const size_t mo = b.mol_mat_off[m], nn = (size_t)norb * norb;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // slices of this molecule: one per 8192 elements, at most EE_SLICES (a function of its size only)
@@ -355,6 +357,54 @@ __global__ void __launch_bounds__(NT_RED) k_energy_error(seqm_batch b, const dou
   cl.sync();  // the other CTAs' shared memory stays alive until rank 0 has read it
 }
 
+// Molecules of up to EE_WARP_MAX basis functions: one warp per molecule streams its n^2
+// elements (four independent loads per element, 32 B, coalesced across the lanes) and sums with
+// a butterfly; eight molecules per CTA.  A molecule's sums depend only on its own size, as in
+// the cluster kernel, which takes the larger molecules of the same batch.
+constexpr int EE_WARPS = 8, EE_WUNROLL = 4;
+__global__ void __launch_bounds__(32 * EE_WARPS) k_energy_error_warp(
+    seqm_batch b, const double *__restrict__ P, const double *__restrict__ Pold, const double *__restrict__ H,
+    const double *__restrict__ F, double *Eelec, double *Eout, double *err, double *dm_err, double *dm_el,
+    uint8_t *active, double eps, const double *__restrict__ diis_err, int *__restrict__ nactive) {
+  const int m = blockIdx.x * EE_WARPS + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (m >= b.nmol || !is_active(active, m)) return;  // uniform over the warp
+  const int n = b.mol_norb[m];
+  if (n > EE_WARP_MAX) return;
+  const size_t mo = b.mol_mat_off[m];
+  const int nn = n * n;
+  const double *Pm = P + mo, *Hm = H + mo, *Fm = F + mo, *Om = Pold ? Pold + mo : nullptr;
+  double e = 0.0, fro = 0.0, mx = 0.0;
+  for (int i = lane; i < nn; i += 32 * EE_WUNROLL) {
+    double pv[EE_WUNROLL], hf[EE_WUNROLL], po[EE_WUNROLL];
+#pragma unroll
+    for (int u = 0; u < EE_WUNROLL; ++u) {
+      const int j = i + 32 * u;
+      const bool in = j < nn;
+      pv[u] = in ? Pm[j] : 0.0;
+      hf[u] = in ? Hm[j] + Fm[j] : 0.0;
+      po[u] = (in && Om) ? Om[j] : pv[u];
+    }
+#pragma unroll
+    for (int u = 0; u < EE_WUNROLL; ++u) {
+      e = fma(pv[u], hf[u], e);
+      const double d = pv[u] - po[u];
+      fro = fma(d, d, fro);
+      mx = fmax(mx, fabs(d));
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    e += __shfl_xor_sync(0xffffffffu, e, o);
+    fro += __shfl_xor_sync(0xffffffffu, fro, o);
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  if (lane == 0) {
+    e *= 0.5;
+    Eout[m] = e;
+    if (Pold) finish_error(b, m, e, fro, mx, Eelec, err, dm_err, dm_el, active, eps, diis_err, nactive);
+  }
+}
+
 // ------------------------------------------------------------------ mixing
 // linear: P <- alpha P + (1 - alpha) Pnew (scf_loop.py:258-267);
 // adaptive (scf_loop.py:360-420): every third iteration extrapolate
@@ -368,6 +418,7 @@ __global__ void __launch_bounds__(NT_RED) k_energy_error(seqm_batch b, const dou
 // and rank 0 alone damps, clamps and renormalises the diagonal and writes it after
 // a cluster barrier, over the provisional values of the elementwise pass.
 constexpr int NT_MIX = 512, MIX_UNROLL = 4;
+constexpr int MIX_WARP_MAX = 160;  // molecules up to this size are mixed by k_mix_warp
 constexpr size_t MIX_SMEM_MAX = 200 * 1024;  // diagonal history of molecules up to 12800 AOs
 __global__ void __launch_bounds__(NT_MIX) k_mix(seqm_batch b, double *__restrict__ P, const double *__restrict__ Pnew,
                                                 double *__restrict__ Pold, double *__restrict__ old2,
@@ -380,6 +431,7 @@ __global__ void __launch_bounds__(NT_MIX) k_mix(seqm_batch b, double *__restrict
   const int m = blockIdx.x / cs, r = (int)cl.block_rank();
   if (!is_active(active, m)) return;  // uniform over the cluster
   const int n = b.mol_norb[m];
+  if (n <= MIX_WARP_MAX) return;  // k_mix_warp's molecule
   const int k = kit[m] + 1;  // 1-based iteration number of this molecule
   const size_t mo = b.mol_mat_off[m], nn = (size_t)n * n;
   const size_t i0 = (size_t)r * NT_MIX + threadIdx.x, step = (size_t)cs * NT_MIX;
@@ -484,6 +536,112 @@ __global__ void __launch_bounds__(NT_MIX) k_mix(seqm_batch b, double *__restrict
   }
 }
 
+// The same mixing for molecules of up to MIX_WARP_MAX basis functions, one warp per molecule
+// (eight per CTA): the lanes hold the diagonal (at most five elements each) in registers, every
+// sum of the adaptive step is a butterfly, and the elementwise update streams the molecule's
+// matrices with coalesced loads.  A molecule's arithmetic depends only on its own size.
+constexpr int MIX_WARPS = 8, MIX_DIAG = (MIX_WARP_MAX + 31) / 32;
+__global__ void __launch_bounds__(32 * MIX_WARPS) k_mix_warp(seqm_batch b, double *__restrict__ P,
+                                                             const double *__restrict__ Pnew, double *__restrict__ Pold,
+                                                             double *__restrict__ old2,
+                                                             const int64_t *__restrict__ row_off,
+                                                             int32_t *__restrict__ kit, int linear, double alpha,
+                                                             double occ, const uint8_t *__restrict__ active) {
+  const int m = blockIdx.x * MIX_WARPS + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (m >= b.nmol || !is_active(active, m)) return;  // uniform over the warp
+  const int n = b.mol_norb[m];
+  if (n > MIX_WARP_MAX) return;
+  const int k = kit[m] + 1;
+  const size_t mo = b.mol_mat_off[m];
+  const int nn = n * n;
+  double *Pm = P + mo, *Po = Pold + mo;
+  const double *Pn = Pnew + mo;
+  double dp[MIX_DIAG], dc[MIX_DIAG];
+  double fac = 0.0;
+  const bool third = !linear && (k % 3) == 0;
+  double *o2 = linear ? nullptr : old2 + row_off[m];
+  if (!linear) {
+    double num = 0.0, den = 0.0;
+#pragma unroll
+    for (int t = 0; t < MIX_DIAG; ++t) {
+      const int i = lane + 32 * t;
+      dp[t] = i < n ? Pm[(size_t)i * n + i] : 0.0;
+      dc[t] = i < n ? Pn[(size_t)i * n + i] : 0.0;
+      const double o2v = i < n ? o2[i] : 0.0;
+      const double d1 = dc[t] - dp[t], d2 = dc[t] - 2.0 * dp[t] + o2v;
+      num = fma(d1, d1, num);
+      den = fma(d2, d2, den);
+    }
+    if (third) {
+      num = warp_allsum(num);
+      den = warp_allsum(den);
+      fac = (den > 0.0 && num < 100.0 * den) ? sqrt(num / den) : 0.0;
+    }
+  }
+  __syncwarp();  // every lane has read its diagonal elements before any is overwritten
+  if (lane == 0) kit[m] = k;
+  const double oma = 1.0 - alpha;
+  for (int i = lane; i < nn; i += 32 * MIX_UNROLL) {
+    double pv[MIX_UNROLL], pn[MIX_UNROLL];
+#pragma unroll
+    for (int u = 0; u < MIX_UNROLL; ++u) {
+      const int j = i + 32 * u;
+      pv[u] = j < nn ? Pm[j] : 0.0;
+      pn[u] = j < nn ? Pn[j] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < MIX_UNROLL; ++u) {
+      const int j = i + 32 * u;
+      if (j < nn) {
+        Po[j] = pv[u];
+        Pm[j] = linear ? alpha * pv[u] + oma * pn[u] : (third ? (1.0 + fac) * pn[u] - fac * pv[u] : pn[u]);
+      }
+    }
+  }
+  if (linear) return;
+  __syncwarp();  // the provisional diagonal is written before the final one replaces it
+  // diagonal: damp, clamp, renormalise (as k_mix)
+  const double damp = k > 4 ? 0.05 : 1.0e10;
+  double di[MIX_DIAG], s0 = 0.0;
+#pragma unroll
+  for (int t = 0; t < MIX_DIAG; ++t) {
+    const int i = lane + 32 * t;
+    const double delta = dc[t] - dp[t];
+    const double v = fabs(delta) > damp ? dp[t] + (delta > 0.0 ? 1.0 : (delta < 0.0 ? -1.0 : 0.0)) * damp
+                                        : dc[t] + fac * delta;
+    di[t] = i < n ? fmin(fmax(v, 0.0), occ) : 0.0;
+    s0 += i < n ? dc[t] : 0.0;
+  }
+  double sum0 = warp_allsum(s0);
+  for (int pass = 0; pass < 20; ++pass) {
+    double s2 = 0.0;
+#pragma unroll
+    for (int t = 0; t < MIX_DIAG; ++t) s2 += di[t];
+    const double sum2 = warp_allsum(s2);
+    const double sum3 = sum2 > 1.0e-3 ? sum0 / sum2 : 0.0;
+    if (!(sum2 > 1.0e-3) || fabs(sum3 - 1.0) <= 1.0e-5) break;
+    double nfull = 0.0;
+#pragma unroll
+    for (int t = 0; t < MIX_DIAG; ++t) {
+      const int i = lane + 32 * t;
+      const double sc = fmax(di[t] * sum3, 0.0);
+      const bool full = sc > occ;
+      di[t] = i < n ? (full ? occ : sc) : 0.0;
+      nfull += (i < n && full) ? 1.0 : 0.0;
+    }
+    nfull = warp_allsum(nfull);
+    sum0 = sum0 - nfull * occ;
+  }
+#pragma unroll
+  for (int t = 0; t < MIX_DIAG; ++t) {
+    const int i = lane + 32 * t;
+    if (i < n) {
+      Pm[(size_t)i * n + i] = di[t];
+      o2[i] = dp[t];
+    }
+  }
+}
+
 // ----------------------------------------------------------- initial density
 __global__ void k_initial_density(seqm_batch b, double *__restrict__ P) {
   int a = blockIdx.x * blockDim.x + threadIdx.x;
@@ -535,6 +693,18 @@ static int launch_clusters(void (*kern)(Params...), int cs, int nmol, int nt, si
   return launch_check();
 }
 
+// energy + test of every molecule: the warp kernel for molecules up to EE_WARP_MAX basis
+// functions, the cluster kernel (launched only when the batch holds larger ones) for the rest
+template <typename... Args>
+int launch_energy_error(const seqm_batch &b, void *stream, int *nactive, Args... args) {
+  k_energy_error_warp<<<(b.nmol + EE_WARPS - 1) / EE_WARPS, 32 * EE_WARPS, 0, (cudaStream_t)stream>>>(b, args...,
+                                                                                                        nactive);
+  int rc = launch_check();
+  if (rc != SEQM_OK || b.max_norb <= EE_WARP_MAX) return rc;
+  const int cs = mol_cluster(k_energy_error, b.max_norb);
+  return launch_clusters(k_energy_error, cs, b.nmol, NT_RED, 0, stream, b, args..., nactive, cs);
+}
+
 extern "C" int seqm_fock(const seqm_batch *bp, const double *P, const double *H, const double *w_xx,
                          const double *w_xh, const double *w_hh, double *F, const uint8_t *active, void *stream) {
   if (!bp) return SEQM_E_ARG;
@@ -551,9 +721,8 @@ extern "C" int seqm_energy_error(const seqm_batch *bp, const double *P, const do
   if (!bp) return SEQM_E_ARG;
   seqm_batch b = *bp;
   if (b.nmol == 0) return SEQM_OK;
-  const int cs = mol_cluster(k_energy_error, b.max_norb);
-  return launch_clusters(k_energy_error, cs, b.nmol, NT_RED, 0, stream, b, P, Pold, H, F, Eelec, Eout, err, dm_err,
-                         dm_el, active, eps, diis_err, (int *)nullptr, cs);
+  return launch_energy_error(b, stream, (int *)nullptr, P, Pold, H, F, Eelec, Eout, err, dm_err, dm_el, active, eps,
+                             diis_err);
 }
 
 extern "C" int seqm_scf_step(const seqm_batch *bp, const seqm_scf_state *st, void *stream) {
@@ -571,10 +740,9 @@ extern "C" int seqm_scf_step(const seqm_batch *bp, const seqm_scf_state *st, voi
   rc = seqm_fock(bp, st->P, st->H, st->w_xx, st->w_xh, st->w_hh, st->F, st->active, stream);
   if (rc != SEQM_OK) return rc;
   if (st->nactive && cudaMemsetAsync(st->nactive, 0, sizeof(int32_t), s) != cudaSuccess) return SEQM_E_CUDA;
-  const int cs = mol_cluster(k_energy_error, b.max_norb);
-  return launch_clusters(k_energy_error, cs, b.nmol, NT_RED, 0, stream, b, (const double *)st->P,
-                         (const double *)st->Pold, st->H, (const double *)st->F, st->Eelec, st->Eout, st->err,
-                         st->dm_err, st->dm_el, st->active, st->eps, st->diis_err, (int *)st->nactive, cs);
+  return launch_energy_error(b, stream, (int *)st->nactive, (const double *)st->P, (const double *)st->Pold, st->H,
+                             (const double *)st->F, st->Eelec, st->Eout, st->err, st->dm_err, st->dm_el, st->active,
+                             st->eps, st->diis_err);
 }
 
 extern "C" int seqm_mix(const seqm_batch *bp, double *P, const double *Pnew, double *Pold, double *old2,
@@ -585,11 +753,15 @@ extern "C" int seqm_mix(const seqm_batch *bp, double *P, const double *Pnew, dou
   if (b.nmol == 0) return SEQM_OK;
   size_t smem = linear ? 0 : (size_t)2 * b.max_norb * sizeof(double);
   if (smem > MIX_SMEM_MAX) return SEQM_E_TOO_LARGE;
-  if (smem > 48 * 1024) {
+  if (smem > 0) {  // raised whatever the size: the kernel's static shared memory counts against the default 48 KB
     static SmemLimit limit;
     const int rc = limit.ensure(k_mix, MIX_SMEM_MAX);
     if (rc != SEQM_OK) return rc;
   }
+  k_mix_warp<<<(b.nmol + MIX_WARPS - 1) / MIX_WARPS, 32 * MIX_WARPS, 0, (cudaStream_t)stream>>>(
+      b, P, Pnew, Pold, old2, mol_row_off, k, linear, alpha, occupation, active);
+  const int rc = launch_check();
+  if (rc != SEQM_OK || b.max_norb <= MIX_WARP_MAX) return rc;
   const int cs = mol_cluster(k_mix, b.max_norb);
   return launch_clusters(k_mix, cs, b.nmol, NT_MIX, smem, stream, b, P, Pnew, Pold, old2, mol_row_off, k, linear, alpha,
                          occupation, active, cs);

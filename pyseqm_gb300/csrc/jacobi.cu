@@ -873,6 +873,32 @@ size_t jacobi_smem(int cap) {
 // k_jacobi's shared-memory limit: set once per device to the largest class (JMAX_N)
 SmemLimit g_jacobi_smem;
 
+// Side streams and events of the per-class launches, one set per host thread and device (a
+// caller's threads each keep their own, so concurrent calls never share an event).  Created on a
+// thread's first call with classes on a device; that call must not be under stream capture.
+struct ClassStreams {
+  cudaStream_t aux[SEQM_MAX_CLASSES - 1];
+  cudaEvent_t fork, join[SEQM_MAX_CLASSES - 1];
+};
+
+ClassStreams *class_streams() {
+  constexpr int MAX_DEV = 64;
+  thread_local ClassStreams sets[MAX_DEV];
+  thread_local bool made[MAX_DEV] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEV) return nullptr;
+  ClassStreams &cs = sets[dev];
+  if (!made[dev]) {
+    bool ok = cudaEventCreateWithFlags(&cs.fork, cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 0; ok && i < SEQM_MAX_CLASSES - 1; ++i)
+      ok = cudaStreamCreateWithFlags(&cs.aux[i], cudaStreamNonBlocking) == cudaSuccess &&
+           cudaEventCreateWithFlags(&cs.join[i], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) return nullptr;  // fall back to one stream (a partial set is left unused)
+    made[dev] = true;
+  }
+  return &cs;
+}
+
 // threads of a CTA for count molecules of up to cap basis functions: at least one per rotation
 // pair (cap / 2 + 1) and enough warps for the products; small CTAs let several molecules share
 // an SM, which pays when the class fills the GPU; a class of fewer molecules than SMs keeps the
@@ -911,23 +937,44 @@ extern "C" int seqm_density_jacobi(const seqm_batch *bp, const double *F, double
     return launch_check();
   }
   if (b.nclass > SEQM_MAX_CLASSES) return SEQM_E_ARG;
-  // one launch per size class (mol_order is by descending norb): CTA threads and shared memory
-  // sized for the class, so that several small molecules share an SM
   int start = 0;
   for (int c = 0; c < b.nclass; ++c) {
+    if (b.class_end[c] < start || b.class_end[c] > b.nmol) return SEQM_E_ARG;
+    start = b.class_end[c];
+  }
+  if (start != b.nmol) return SEQM_E_ARG;
+  // one launch per size class (mol_order is by descending norb): CTA threads and shared memory
+  // sized for the class, so that several small molecules share an SM.  The classes solve
+  // disjoint molecules, so classes after the first run on side streams forked from and joined
+  // back to `stream`: their CTAs fill the SMs the largest class leaves idle in its last wave.
+  cudaStream_t s = (cudaStream_t)stream;
+  ClassStreams *side = b.nclass > 1 ? class_streams() : nullptr;
+  if (side && cudaEventRecord(side->fork, s) != cudaSuccess) side = nullptr;
+  start = 0;
+  int rc = SEQM_OK;
+  for (int c = 0; c < b.nclass; ++c) {
     const int end = b.class_end[c];
-    if (end < start || end > b.nmol) return SEQM_E_ARG;
     const int ccap = b.class_norb[c] > cap ? cap : b.class_norb[c];
+    cudaStream_t cs = s;
+    if (side && c > 0) {
+      cs = side->aux[c - 1];
+      if (cudaStreamWaitEvent(cs, side->fork, 0) != cudaSuccess) { rc = SEQM_E_CUDA; break; }
+    }
     if (end > start && ccap > 0) {
-      k_jacobi<<<end - start, jacobi_threads(ccap, end - start), jacobi_smem(ccap), (cudaStream_t)stream>>>(
+      k_jacobi<<<end - start, jacobi_threads(ccap, end - start), jacobi_smem(ccap), cs>>>(
           b, F, P, evals, evecs, work, mol_row_off, active, status, max_sweeps, warm, mixed_threshold, density_only,
           start, ccap);
-      const int rc = launch_check();
-      if (rc != SEQM_OK) return rc;
+      rc = launch_check();
+      if (rc != SEQM_OK) break;
     }
     start = end;
   }
-  return start == b.nmol ? SEQM_OK : SEQM_E_ARG;
+  if (side)  // join every side stream that was forked, also after an error
+    for (int c = 1; c < b.nclass; ++c)
+      if (cudaEventRecord(side->join[c - 1], side->aux[c - 1]) != cudaSuccess ||
+          cudaStreamWaitEvent(s, side->join[c - 1], 0) != cudaSuccess)
+        rc = SEQM_E_CUDA;
+  return rc;
 }
 
 // ---------------------------------------------------------------------------

@@ -216,6 +216,40 @@ __global__ void __launch_bounds__(128) k_tc_split(seqm_batch b, const float *__r
   }
 }
 
+// Upper tile (tm <= tn) of linear index t in a grouped order: the tile columns are cut into bands
+// of TC_BAND columns and each band is walked row by row, so the CTAs resident at one time (two
+// per SM) read about TC_BAND + 300 / TC_BAND row blocks of split tiles, which stay in L2, where
+// a plain column-by-column walk cycles through every row block of a large molecule.
+// Returns false for t beyond the nb (nb + 1) / 2 tiles.
+constexpr int TC_BAND = 16;
+__device__ __forceinline__ bool upper_tile(int t, int nb, int &tm, int &tn) {
+  int base = 0;
+  for (int lo = 0; lo < nb; lo += TC_BAND) {
+    const int w = min(nb, lo + TC_BAND) - lo;
+    const int cnt = lo * w + w * (w + 1) / 2;  // rows above the band's diagonal block, then the block
+    if (t < base + cnt) {
+      int r = t - base;
+      if (r < lo * w) {
+        tm = r / w;
+        tn = lo + r % w;
+        return true;
+      }
+      r -= lo * w;
+      int row = lo, len = w;
+      while (r >= len) {
+        r -= len;
+        ++row;
+        --len;
+      }
+      tm = row;
+      tn = row + r;
+      return true;
+    }
+    base += cnt;
+  }
+  return false;
+}
+
 // One SP2 step of every running molecule: X' = X^2 or 2X - X^2 (see the file comment).
 // Grid: (upper tiles of the largest molecule, molecules); block: 128 threads.
 __global__ void __launch_bounds__(TC_THREADS) k_tc_sp2_step(seqm_batch b, float *__restrict__ X,
@@ -229,13 +263,8 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_sp2_step(seqm_batch b, float 
   if (s[S_RUN] == 0.0) return;
   const int n = b.mol_norb[m];
   const int nb = (n + TC_M - 1) / TC_M, nk = (n + TC_KT - 1) / TC_KT;
-  // upper tile (tm <= tn) from the linear index t = tn (tn + 1) / 2 + tm
-  const int t = blockIdx.x;
-  int tn = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
-  while ((tn + 1) * (tn + 2) / 2 <= t) ++tn;
-  while (tn * (tn + 1) / 2 > t) --tn;
-  const int tm = t - tn * (tn + 1) / 2;
-  if (tn >= nb) return;
+  int tm, tn;
+  if (!upper_tile(blockIdx.x, nb, tm, tn)) return;
 
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);

@@ -107,3 +107,22 @@ def test_captured_sp2_iteration_matches_eager(large):
     np.testing.assert_allclose((E[0] + E[1]).cpu().numpy(), (E_eager[0] + E_eager[1]).cpu().numpy(),
                                atol=1e-7 if large == "tc" else 1e-9, rtol=0)
     assert bool((s.status[: L.nmol] > 0).all())
+
+
+def test_mixing_at_the_48kb_shared_memory_edge():
+    """A 3072-AO molecule ((H2O)512): the adaptive mixer's diagonal history is exactly 48 KB of
+    dynamic shared memory, which with the kernel's static shared memory exceeds the default
+    limit; two SCF iterations run without a launch failure."""
+    from pyseqm_gb300 import workloads
+    from pyseqm_gb300.layout import Layout
+    from pyseqm_gb300.scf import BatchSCF
+
+    species, coords = workloads.pad_batch([workloads.big_water(seed=0, n_side=8)])
+    L = Layout.from_padded(species, coords, "PM3").to_device("cuda")
+    assert L.max_norb == 3072
+    s = BatchSCF(L)
+    s.large_density = "tc"
+    s.hcore()
+    s.scf(1e-5, (1,), max_iter=2)
+    torch.cuda.synchronize()
+    assert int(s.iters[0]) == 2 and bool(torch.isfinite(s.Eout[:1]).all())

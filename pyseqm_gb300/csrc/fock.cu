@@ -361,13 +361,20 @@ __global__ void __launch_bounds__(NT_RED) k_energy_error(seqm_batch b, const dou
 // elements (four independent loads per element, 32 B, coalesced across the lanes) and sums with
 // a butterfly; eight molecules per CTA.  A molecule's sums depend only on its own size, as in
 // the cluster kernel, which takes the larger molecules of the same batch.
-constexpr int EE_WARPS = 8, EE_WUNROLL = 4;
+constexpr int EE_WARPS = 8, EE_WUNROLL = 8;
+// molecule of warp w: the scheduling order (descending size) when the batch has one, so the
+// longest streams start first and the small molecules fill in behind them
+__device__ __forceinline__ int warp_molecule(const seqm_batch &b, int w) {
+  return b.nclass > 0 ? b.mol_order[w] : w;
+}
 __global__ void __launch_bounds__(32 * EE_WARPS) k_energy_error_warp(
     seqm_batch b, const double *__restrict__ P, const double *__restrict__ Pold, const double *__restrict__ H,
     const double *__restrict__ F, double *Eelec, double *Eout, double *err, double *dm_err, double *dm_el,
     uint8_t *active, double eps, const double *__restrict__ diis_err, int *__restrict__ nactive) {
-  const int m = blockIdx.x * EE_WARPS + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (m >= b.nmol || !is_active(active, m)) return;  // uniform over the warp
+  const int w = blockIdx.x * EE_WARPS + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (w >= b.nmol) return;
+  const int m = warp_molecule(b, w);
+  if (!is_active(active, m)) return;  // uniform over the warp
   const int n = b.mol_norb[m];
   if (n > EE_WARP_MAX) return;
   const size_t mo = b.mol_mat_off[m];
@@ -540,15 +547,17 @@ __global__ void __launch_bounds__(NT_MIX) k_mix(seqm_batch b, double *__restrict
 // (eight per CTA): the lanes hold the diagonal (at most five elements each) in registers, every
 // sum of the adaptive step is a butterfly, and the elementwise update streams the molecule's
 // matrices with coalesced loads.  A molecule's arithmetic depends only on its own size.
-constexpr int MIX_WARPS = 8, MIX_DIAG = (MIX_WARP_MAX + 31) / 32;
+constexpr int MIX_WARPS = 8, MIX_DIAG = (MIX_WARP_MAX + 31) / 32, MIX_WUNROLL = 8;
 __global__ void __launch_bounds__(32 * MIX_WARPS) k_mix_warp(seqm_batch b, double *__restrict__ P,
                                                              const double *__restrict__ Pnew, double *__restrict__ Pold,
                                                              double *__restrict__ old2,
                                                              const int64_t *__restrict__ row_off,
                                                              int32_t *__restrict__ kit, int linear, double alpha,
                                                              double occ, const uint8_t *__restrict__ active) {
-  const int m = blockIdx.x * MIX_WARPS + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (m >= b.nmol || !is_active(active, m)) return;  // uniform over the warp
+  const int w = blockIdx.x * MIX_WARPS + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (w >= b.nmol) return;
+  const int m = warp_molecule(b, w);
+  if (!is_active(active, m)) return;  // uniform over the warp
   const int n = b.mol_norb[m];
   if (n > MIX_WARP_MAX) return;
   const int k = kit[m] + 1;
@@ -581,16 +590,16 @@ __global__ void __launch_bounds__(32 * MIX_WARPS) k_mix_warp(seqm_batch b, doubl
   __syncwarp();  // every lane has read its diagonal elements before any is overwritten
   if (lane == 0) kit[m] = k;
   const double oma = 1.0 - alpha;
-  for (int i = lane; i < nn; i += 32 * MIX_UNROLL) {
-    double pv[MIX_UNROLL], pn[MIX_UNROLL];
+  for (int i = lane; i < nn; i += 32 * MIX_WUNROLL) {
+    double pv[MIX_WUNROLL], pn[MIX_WUNROLL];
 #pragma unroll
-    for (int u = 0; u < MIX_UNROLL; ++u) {
+    for (int u = 0; u < MIX_WUNROLL; ++u) {
       const int j = i + 32 * u;
       pv[u] = j < nn ? Pm[j] : 0.0;
       pn[u] = j < nn ? Pn[j] : 0.0;
     }
 #pragma unroll
-    for (int u = 0; u < MIX_UNROLL; ++u) {
+    for (int u = 0; u < MIX_WUNROLL; ++u) {
       const int j = i + 32 * u;
       if (j < nn) {
         Po[j] = pv[u];

@@ -537,20 +537,6 @@ __global__ void __launch_bounds__(EW_THREADS) k_mw_split(seqm_batch b, const dou
   }
 }
 
-// X = 3 X2 - 2 X3 (FP32 McWeeny step)
-__global__ void __launch_bounds__(EW_THREADS) k_mw32(seqm_batch b, const float *__restrict__ X2,
-                                                     const float *__restrict__ X3, float *__restrict__ X,
-                                                     const uint8_t *__restrict__ active) {
-  const int m = blockIdx.y;
-  if (active && !active[m]) return;
-  const int n = b.mol_norb[m];
-  const size_t nn = (size_t)n * n, base = (size_t)blockIdx.x * EW_CHUNK;
-  if (base >= nn) return;
-  const size_t mo = b.mol_mat_off[m];
-  for (size_t idx = base + threadIdx.x; idx < nn && idx < base + EW_CHUNK; idx += EW_THREADS)
-    X[mo + idx] = 3.0f * X2[mo + idx] - 2.0f * X3[mo + idx];
-}
-
 // P = 2 (Z + C)
 __global__ void __launch_bounds__(EW_THREADS) k_mw_update(seqm_batch b, const double *__restrict__ Z,
                                                           const float *__restrict__ C, double *__restrict__ P,

@@ -197,9 +197,9 @@ __global__ void __launch_bounds__(1024) k_tc_tile_offsets(seqm_batch b, int64_t 
 // split tiles of the FP32 X of running molecules: CTA (kb, rb, m) writes tile (rb, kb)
 __global__ void __launch_bounds__(128) k_tc_split(seqm_batch b, const float *__restrict__ X, uint8_t *__restrict__ Xh,
                                                   uint8_t *__restrict__ Xl, const int64_t *__restrict__ xs_off,
-                                                  const double *__restrict__ st) {
+                                                  const double *__restrict__ st, const uint8_t *__restrict__ active) {
   const int m = blockIdx.z;
-  if (st[SP2_NS * m + S_RUN] == 0.0) return;
+  if (st ? st[SP2_NS * m + S_RUN] == 0.0 : (active && !active[m])) return;  // running molecules, or active ones
   const int n = b.mol_norb[m];
   const int nb = (n + TC_M - 1) / TC_M, nk = (n + TC_KT - 1) / TC_KT;
   const int rb = blockIdx.y, kb = blockIdx.x;
@@ -252,15 +252,27 @@ __device__ __forceinline__ bool upper_tile(int t, int nb, int &tm, int &tn) {
 
 // One SP2 step of every running molecule: X' = X^2 or 2X - X^2 (see the file comment).
 // Grid: (upper tiles of the largest molecule, molecules); block: 128 threads.
-__global__ void __launch_bounds__(TC_THREADS) k_tc_sp2_step(seqm_batch b, float *__restrict__ X,
-                                                            const uint8_t *__restrict__ Xh,
-                                                            const uint8_t *__restrict__ Xl, uint8_t *__restrict__ Yh,
-                                                            uint8_t *__restrict__ Yl,
-                                                            const int64_t *__restrict__ xs_off,
-                                                            double *__restrict__ st, int *__restrict__ err) {
+// Operands and epilogue of a plain split product (PROD launches of k_tc_step): C = cY Y + cAB A B,
+// B's split tiles in Bh / Bl (A's are the kernel's Xh / Xl), Y an FP32 matrix (NULL: C = cAB A B);
+// A and B must commute (functions of one symmetric matrix), so that A B is symmetric and its upper
+// tiles with their mirrors are the whole product.
+struct TcProduct {
+  const uint8_t *Bh, *Bl;
+  const float *Y;
+  float cY, cAB;
+  const uint8_t *active;
+};
+
+template <bool PROD>
+__global__ void __launch_bounds__(TC_THREADS) k_tc_step(seqm_batch b, float *__restrict__ X,
+                                                        const uint8_t *__restrict__ Xh,
+                                                        const uint8_t *__restrict__ Xl, uint8_t *__restrict__ Yh,
+                                                        uint8_t *__restrict__ Yl,
+                                                        const int64_t *__restrict__ xs_off,
+                                                        double *__restrict__ st, int *__restrict__ err, TcProduct pp) {
   const int m = blockIdx.y;
   double *s = st + SP2_NS * m;
-  if (s[S_RUN] == 0.0) return;
+  if (PROD ? (pp.active && !pp.active[m]) : s[S_RUN] == 0.0) return;
   const int n = b.mol_norb[m];
   const int nb = (n + TC_M - 1) / TC_M, nk = (n + TC_KT - 1) / TC_KT;
   int tm, tn;
@@ -292,6 +304,8 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_sp2_step(seqm_batch b, float 
   const uint32_t tmem_d = tmem_base;
   const uint8_t *tiles_h = Xh + (size_t)xs_off[m] * SPLIT_TILE_BYTES;
   const uint8_t *tiles_l = Xl + (size_t)xs_off[m] * SPLIT_TILE_BYTES;
+  const uint8_t *btiles_h = PROD ? pp.Bh + (size_t)xs_off[m] * SPLIT_TILE_BYTES : tiles_h;
+  const uint8_t *btiles_l = PROD ? pp.Bl + (size_t)xs_off[m] * SPLIT_TILE_BYTES : tiles_l;
   const size_t rowA = (size_t)tm * nk * SPLIT_TILE_BYTES, rowB = (size_t)tn * nk * SPLIT_TILE_BYTES;
 
   if (threadIdx.x == 0) {
@@ -307,8 +321,8 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_sp2_step(seqm_batch b, float 
       mbar_expect_tx(&full[si], STAGE_BYTES);
       bulk_g2s(dst, tiles_h + rowA + ko, SPLIT_TILE_BYTES, &full[si]);
       bulk_g2s(dst + SPLIT_TILE_BYTES, tiles_l + rowA + ko, SPLIT_TILE_BYTES, &full[si]);
-      bulk_g2s(dst + 2 * SPLIT_TILE_BYTES, tiles_h + rowB + ko, SPLIT_TILE_BYTES, &full[si]);
-      bulk_g2s(dst + 3 * SPLIT_TILE_BYTES, tiles_l + rowB + ko, SPLIT_TILE_BYTES, &full[si]);
+      bulk_g2s(dst + 2 * SPLIT_TILE_BYTES, btiles_h + rowB + ko, SPLIT_TILE_BYTES, &full[si]);
+      bulk_g2s(dst + 3 * SPLIT_TILE_BYTES, btiles_l + rowB + ko, SPLIT_TILE_BYTES, &full[si]);
       sh_issued = kb + 1;
     }
   } else if (threadIdx.x == 32) {
@@ -349,18 +363,19 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_sp2_step(seqm_batch b, float 
     float *stg = reinterpret_cast<float *>(smem);  // 128 x EPI_LD staging; the stages are idle now
     const size_t mo = b.mol_mat_off[m];
     float *Xm = X + mo;
-    // old X tile into staging (coalesced rows)
+    // old X tile (a product: the Y tile) into staging (coalesced rows)
+    const float *Sm = PROD ? (pp.Y ? pp.Y + mo : nullptr) : Xm;
     for (int r = warp; r < TC_M; r += TC_THREADS / 32) {
       const int gr = tm * TC_M + r;
 #pragma unroll
       for (int c = lane; c < TC_N; c += 32) {
         const int gc = tn * TC_N + c;
-        stg[r * EPI_LD + c] = (gr < n && gc < n) ? Xm[(size_t)gr * n + gc] : 0.0f;
+        stg[r * EPI_LD + c] = (Sm && gr < n && gc < n) ? Sm[(size_t)gr * n + gc] : 0.0f;
       }
     }
     __syncthreads();
     // X' row by row: thread i owns accumulator row i (TMEM lane i)
-    const double nocc = (double)b.mol_nocc[m], t1 = s[S_T1], t2 = s[S_T2];
+    const double nocc = (double)b.mol_nocc[m], t1 = PROD ? 0.0 : s[S_T1], t2 = PROD ? 0.0 : s[S_T2];
     const bool sq = fabs(t2 - nocc) < fabs(2.0 * t1 - t2 - nocc);
     const int i = threadIdx.x, gi = tm * TC_M + i;
     // ||X'||_F^2 in FP32 per 32 columns, then FP64 (the sums of squares carry the tensor-core
@@ -375,7 +390,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_sp2_step(seqm_batch b, float 
       for (int j = 0; j < 32; ++j) {
         const int c = c0 + j;
         const float x = stg[i * EPI_LD + c];
-        float y = sq ? v[j] : 2.0f * x - v[j];
+        float y = PROD ? fmaf(pp.cAB, v[j], pp.cY * x) : (sq ? v[j] : 2.0f * x - v[j]);
         if (gi >= n || tn * TC_N + c >= n) y = 0.0f;  // keep the padding of the split tiles zero
         stg[i * EPI_LD + c] = y;
         q2 = fmaf(y, y, q2);
@@ -394,7 +409,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_sp2_step(seqm_batch b, float 
       red[1][warp] = f2;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (!PROD && threadIdx.x == 0) {  // (the barrier above also orders the staging rows)
       double a = 0.0, c = 0.0;
       for (int w = 0; w < TC_THREADS / 32; ++w) {
         a += red[0][w];
@@ -414,8 +429,9 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_sp2_step(seqm_batch b, float 
       }
     }
     // split tiles of X': tile (tm, 4 tn + q) and mirror tile (tn, 4 tm + q), 8 k per store
-    uint8_t *oh = Yh + (size_t)xs_off[m] * SPLIT_TILE_BYTES, *ol = Yl + (size_t)xs_off[m] * SPLIT_TILE_BYTES;
-    for (int g = threadIdx.x; g < TC_M * (TC_N / 8); g += TC_THREADS) {
+    uint8_t *oh = Yh ? Yh + (size_t)xs_off[m] * SPLIT_TILE_BYTES : nullptr;
+    uint8_t *ol = Yl ? Yl + (size_t)xs_off[m] * SPLIT_TILE_BYTES : nullptr;
+    for (int g = threadIdx.x; oh && g < TC_M * (TC_N / 8); g += TC_THREADS) {
       const int r = g >> 4, cg = (g & 15) * 8, q = cg / TC_KT, kc = cg % TC_KT;
       float v[8];
       const int kb1 = (tn * TC_N) / TC_KT + q;
@@ -509,10 +525,12 @@ extern "C" int seqm_density_sp2_tc(const seqm_batch *bp, const double *F, double
   k_sp2_start<<<(b.nmol + 127) / 128, 128, 0, s>>>(b, st);
   k_tc_tile_offsets<<<1, 1024, 0, s>>>(b, xs_off);
   const int nb = (b.max_norb + TC_M - 1) / TC_M, nk = (b.max_norb + TC_KT - 1) / TC_KT;
-  k_tc_split<<<dim3(nk, nb, b.nmol), 128, 0, s>>>(b, X, xs[0], xs[1], xs_off, st);
+  k_tc_split<<<dim3(nk, nb, b.nmol), 128, 0, s>>>(b, X, xs[0], xs[1], xs_off, st, nullptr);
   {
     static SmemLimit limit;
-    const int rc0 = limit.ensure(k_tc_sp2_step, TC_SMEM);
+    int rc0 = limit.ensure(k_tc_step<false>, TC_SMEM);
+    static SmemLimit limit_prod;
+    if (rc0 == SEQM_OK) rc0 = limit_prod.ensure(k_tc_step<true>, TC_SMEM);
     if (rc0 != SEQM_OK) return rc0;
   }
   const dim3 grid((unsigned)(nb * (nb + 1) / 2), (unsigned)b.nmol);
@@ -526,9 +544,9 @@ extern "C" int seqm_density_sp2_tc(const seqm_batch *bp, const double *F, double
       cudaError_t r = cudaSuccess;
       for (int half = 0; half < 2 && r == cudaSuccess; ++half) {
         const int c = half;
-        r = add_kernel_node(body, &n[2 * half], half ? &n[1] : nullptr, half ? 1 : 0, k_tc_sp2_step, grid,
+        r = add_kernel_node(body, &n[2 * half], half ? &n[1] : nullptr, half ? 1 : 0, k_tc_step<false>, grid,
                             dim3(TC_THREADS), TC_SMEM, b, X, (const uint8_t *)xs[2 * c], (const uint8_t *)xs[2 * c + 1],
-                            xs[2 - 2 * c], xs[3 - 2 * c], (const int64_t *)xs_off, st, cnt + LC_ERR);
+                            xs[2 - 2 * c], xs[3 - 2 * c], (const int64_t *)xs_off, st, cnt + LC_ERR, TcProduct{});
         if (r == cudaSuccess)
           r = add_kernel_node(body, &n[2 * half + 1], &n[2 * half], 1, k_sp2_check, dim3((b.nmol + 127) / 128),
                               dim3(128), 0, b, st, eps, 1, cnt + LC_RUN);
@@ -541,8 +559,8 @@ extern "C" int seqm_density_sp2_tc(const seqm_batch *bp, const double *F, double
   } else
   for (int it = 0; it < max_iter; ++it) {
     if (cudaMemsetAsync(cnt, 0, sizeof(int), s) != cudaSuccess) { rc = SEQM_E_CUDA; break; }
-    k_tc_sp2_step<<<grid, TC_THREADS, TC_SMEM, s>>>(b, X, xs[2 * cur], xs[2 * cur + 1], xs[2 - 2 * cur],
-                                                    xs[3 - 2 * cur], xs_off, st, cnt + 1);
+    k_tc_step<false><<<grid, TC_THREADS, TC_SMEM, s>>>(b, X, xs[2 * cur], xs[2 * cur + 1], xs[2 - 2 * cur],
+                                                    xs[3 - 2 * cur], xs_off, st, cnt + 1, TcProduct{});
     k_sp2_check<<<(b.nmol + 127) / 128, 128, 0, s>>>(b, st, eps, 1, cnt);
     cur ^= 1;
     if ((it + 1) % SP2_SYNC_EVERY != 0 && it + 1 < max_iter) continue;  // finished molecules skip the extra steps
@@ -553,15 +571,19 @@ extern "C" int seqm_density_sp2_tc(const seqm_batch *bp, const double *F, double
     if (h[0] == 0) break;
   }
   if (rc != SEQM_OK) return rc;
-  if (status) k_sp2_status<<<(b.nmol + 127) / 128, 128, 0, s>>>(b.nmol, st, active, status, cnt + LC_ERR);
   // one FP32 McWeeny step X <- 3X^2 - 2X^3 takes the eigenvalues from the tensor-core level
   // (~1e-4 off 0/1 at the relaxed stop) to the FP32 accumulation level (~1e-6), so one
-  // FP64-accurate step (mcweeny) then reaches ~1e-11
-  float *X3 = reinterpret_cast<float *>(Y);
-  k_sym_gemm<float><<<gemm64_grid(b), MW_THREADS, 0, s>>>(b, X, X, X2, active, nullptr);
-  k_sym_gemm<float><<<gemm64_grid(b), MW_THREADS, 0, s>>>(b, X2, X, X3, active, nullptr);
-  k_mw32<<<ew_grid(b), EW_THREADS, 0, s>>>(b, X2, X3, X, active);
+  // FP64-accurate step (mcweeny) then reaches ~1e-11.  Its two products run as split products
+  // on the tensor cores (FP32-level accuracy, like an FP32 CUDA-core product): X2 = X X with its
+  // split tiles, then X <- 3 X2 - 2 X2 X
+  k_tc_split<<<dim3(nk, nb, b.nmol), 128, 0, s>>>(b, X, xs[0], xs[1], xs_off, nullptr, active);
+  k_tc_step<true><<<grid, TC_THREADS, TC_SMEM, s>>>(b, X2, xs[0], xs[1], xs[2], xs[3], xs_off, st, cnt + LC_ERR,
+                                                   TcProduct{xs[0], xs[1], nullptr, 0.0f, 1.0f, active});
+  k_tc_step<true><<<grid, TC_THREADS, TC_SMEM, s>>>(b, X, xs[2], xs[3], nullptr, nullptr, xs_off, st, cnt + LC_ERR,
+                                                   TcProduct{xs[0], xs[1], X2, 3.0f, -2.0f, active});
   k_ew_sym<float><<<ew_grid(b), EW_THREADS, 0, s>>>(b, X, 1.0, 1.0, P, active);  // P = X + X^T
   mcweeny(b, P, Y, Z, X, X2, active, mcweeny_steps, s, true);  // X, X2 are free after P = X + X^T
+  // after the products, so that a product kernel that gave up waiting shows in status too
+  if (status) k_sp2_status<<<(b.nmol + 127) / 128, 128, 0, s>>>(b.nmol, st, active, status, cnt + LC_ERR);
   return launch_check();
 }

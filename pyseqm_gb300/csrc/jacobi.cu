@@ -912,7 +912,7 @@ int jacobi_threads(int cap, int count) {
       sms[dev].store(n, std::memory_order_relaxed);
     if (count < n) return NT_J;
   }
-  return cap > 96 ? 512 : cap > 64 ? 256 : cap > 32 ? 128 : 64;
+  return cap > 114 ? 512 : cap > 64 ? 256 : cap > 32 ? 128 : 64;
 }
 
 }  // namespace seqm

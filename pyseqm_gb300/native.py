@@ -36,7 +36,7 @@ _P = ctypes.c_void_p
 
 
 MAX_CLASSES = 4  # SEQM_MAX_CLASSES
-CLASS_BOUNDS = (96, 64, 32)  # size classes of per-molecule kernels: norb > 96, 65-96, 33-64, <= 32
+CLASS_BOUNDS = (114, 96, 64)  # size classes of per-molecule kernels: norb > 114, 97-114, 65-96, <= 64
 
 
 class SeqmBatch(ctypes.Structure):

@@ -187,10 +187,10 @@ def test_size_classes_of_scheduling_order():
     b = native.SeqmBatch()
     set_size_classes(b, np.array([144, 120, 97, 96, 70, 40, 33, 8, 6]))
     assert b.nclass == 4
-    assert list(b.class_end) == [3, 5, 7, 9]
-    assert list(b.class_norb) == [144, 96, 40, 8]
-    set_size_classes(b, np.array([60, 50, 12]))
-    assert b.nclass == 2 and list(b.class_end)[:2] == [2, 3] and list(b.class_norb)[:2] == [60, 12]
+    assert list(b.class_end) == [2, 3, 5, 9]
+    assert list(b.class_norb) == [144, 97, 96, 40]
+    set_size_classes(b, np.array([120, 60, 50, 12]))
+    assert b.nclass == 2 and list(b.class_end)[:2] == [1, 4] and list(b.class_norb)[:2] == [120, 60]
     set_size_classes(b, np.zeros(0, dtype=np.int64))
     assert b.nclass == 0
 

@@ -100,6 +100,13 @@ typedef struct seqm_batch {
   int64_t mat_total;
 } seqm_batch;
 
+/* Pair list of the batch on the device: pair_i[p], pair_j[p] (global atom indices, the
+ * layout's class segments, each row-major i < j inside its molecule) from the batch's atom and
+ * segment offsets and heavy-atom counts alone (b->pair_i / pair_j are not read).  Replaces the
+ * pair enumeration of Parser.forward (seqm/basics.py:313-342) for the unpadded layout; the
+ * caller then points b->pair_i / pair_j at the outputs. */
+int seqm_build_pairs(const seqm_batch *b, int32_t *pair_i, int32_t *pair_j, void *stream);
+
 /* Integrals + core Hamiltonian.  Replaces hcore(molecule) (seqm/seqm_functions/hcore.py:9-179),
  * which calls two_elec_two_center_int (two_elec_two_center_int.py:98-283) and
  * diatom_overlap_matrix_PM6_SP (diat_overlap_PM6_SP.py:6-444).  Writes the derived

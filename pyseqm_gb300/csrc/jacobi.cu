@@ -126,17 +126,103 @@ __device__ void tile_product_mnk(int M, int N, int K, LF L, RF R, OF out) {
   tile_product_mnk_t<double>(M, N, K, false, L, R, out);
 }
 
+// ------------------------------------------------- FP64-accurate products on the FP32 pipe
+// GB300 retires FP32 at ~64x its FP64 rate (and converts between them on the FP64 pipe), so
+// the density step's FP64-accurate products run as double-float arithmetic (Dekker 1971;
+// Knuth's TwoSum): each FP64 operand is split into FP32 hi + lo with integer instructions only,
+// each term a*b = p + e exactly (p = fl32(ah bh), e = fma(ah, bh, -p)) plus the FP32 cross terms
+// ah bl + al bh, the p's summed exactly into (s, c) by TwoSum and the rest into c.  Error
+// ~K 2^-48 relative at most (K the summation length), FP64 level for these products, at about
+// 13 FP32 and ~12 integer instructions per term instead of one FP64 FMA.
+
+// x = hi + lo, hi = x's sign, exponent and top 23 mantissa bits (truncated), lo = the remaining
+// 29 bits rounded to FP32 (together ~48 bits); integer instructions and one int-to-float
+// conversion, no FP64 pipe.  |x| below 2^-126 gives 0 (far below every term that matters here).
+__device__ __forceinline__ void split_f64(double x, float &hi, float &lo) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned int top = (unsigned int)(u >> 32), sign = top & 0x80000000u;
+  const int E = (int)((top >> 20) & 0x7FFu) - 1023 + 127;  // FP32 exponent field of x
+  if (E <= 0) { hi = 0.0f; lo = 0.0f; return; }
+  if (E >= 255) { hi = __double2float_rn(x); lo = 0.0f; return; }  // beyond FP32 range (not expected)
+  const unsigned long long m = u & 0xFFFFFFFFFFFFFull;
+  hi = __uint_as_float(sign | ((unsigned int)E << 23) | (unsigned int)(m >> 29));
+  const unsigned int r = (unsigned int)(m & 0x1FFFFFFFull);  // x - hi = r 2^(e - 1075)
+  const float scale = E > 52 ? __uint_as_float((unsigned int)(E - 52) << 23) : 0.0f;
+  const float l = __uint2float_rn(r) * scale;
+  lo = sign ? -l : l;
+}
+
+__device__ __forceinline__ void split_val(double x, float &hi, float &lo) { split_f64(x, hi, lo); }
+__device__ __forceinline__ void split_val(float x, float &hi, float &lo) {
+  hi = x;
+  lo = 0.0f;
+}
+
+__device__ __forceinline__ void two_sum_acc(float &s, float &c, float p) {
+  const float t = s + p;
+  const float z = t - s;
+  c += (s - (t - z)) + (p - z);
+  s = t;
+}
+
+// out(k, j) <- sum_l L(k, l) R(l, j) for k < M, j < N, l < K, 4x4 register tiles, FP64-accurate
+// from double-float arithmetic (above); L and R return doubles (split on load) or floats (exact
+// FP32 values, lo = 0: the terms are then exact before the summation); out receives a double.
+template <class LF, class RF, class OF>
+__device__ void tile_product_df(int M, int N, int K, bool upper_only, LF L, RF R, OF out) {
+  const int mt = (M + 3) >> 2, nt = (N + 3) >> 2;
+  for (int t = threadIdx.x; t < mt * nt; t += NTB) {
+    const int kb = t / nt, jb = t % nt;
+    if (upper_only && kb > jb) continue;
+    const int k0 = kb * 4, j0 = jb * 4;
+    float s[4][4] = {}, c[4][4] = {};
+    for (int l = 0; l < K; ++l) {
+      float ah[4], al[4], bh[4], bl[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        if (k0 + r < M) split_val(L(k0 + r, l), ah[r], al[r]);
+        else ah[r] = al[r] = 0.0f;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (j0 + q < N) split_val(R(l, j0 + q), bh[q], bl[q]);
+        else bh[q] = bl[q] = 0.0f;
+      }
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float p = ah[r] * bh[q];
+          const float e = fmaf(ah[r], bh[q], -p);
+          const float x = fmaf(ah[r], bl[q], al[r] * bh[q]);
+          two_sum_acc(s[r][q], c[r][q], p);
+          c[r][q] += e + x;
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (k0 + r < M && j0 + q < N) out(k0 + r, j0 + q, (double)s[r][q] + (double)c[r][q]);
+  }
+}
+
 // A (shared, holding F on entry) <- V F V^T; G (global n x n) is scratch
-__device__ void form_vfvt(double *A, int lda, const double *V, double *G, int n) {
-  tile_product(
-      n, false, [&](int k, int l) { return V[(size_t)k * n + l]; }, [&](int l, int j) { return A[l * lda + j]; },
-      [&](int k, int j, double v) { G[(size_t)k * n + j] = v; });
+// (pair: FP64-accurate double-float products on the FP32 pipe, else FP64 products)
+__device__ void form_vfvt(double *A, int lda, const double *V, double *G, int n, bool pair) {
+  auto L1 = [&](int k, int l) { return V[(size_t)k * n + l]; };
+  auto R1 = [&](int l, int j) { return A[l * lda + j]; };
+  auto O1 = [&](int k, int j, double v) { G[(size_t)k * n + j] = v; };
+  if (pair) tile_product_df(n, n, n, false, L1, R1, O1);
+  else tile_product(n, false, L1, R1, O1);
   __syncthreads();
-  tile_product(
-      n, true, [&](int k, int j) { return G[(size_t)k * n + j]; }, [&](int j, int l) { return V[(size_t)l * n + j]; },
-      [&](int k, int l, double v) {
-        if (k <= l) { A[k * lda + l] = v; A[l * lda + k] = v; }
-      });
+  auto L2 = [&](int k, int j) { return G[(size_t)k * n + j]; };
+  auto R2 = [&](int j, int l) { return V[(size_t)l * n + j]; };
+  auto O2 = [&](int k, int l, double v) {
+    if (k <= l) { A[k * lda + l] = v; A[l * lda + k] = v; }
+  };
+  if (pair) tile_product_df(n, n, n, true, L2, R2, O2);
+  else tile_product(n, true, L2, R2, O2);
   __syncthreads();
 }
 
@@ -399,8 +485,8 @@ __device__ int fp32_stage(double *A, int lda, double *V, double *G, const double
   __syncthreads();
   // V <- W V (warm) or W (cold), in FP64
   if (is_warm) {
-    tile_product(
-        n, false, [&](int k, int l) { return (double)W32[k * n + l]; }, [&](int l, int j) { return V[(size_t)l * n + j]; },
+    tile_product_df(
+        n, n, n, false, [&](int k, int l) { return W32[k * n + l]; }, [&](int l, int j) { return V[(size_t)l * n + j]; },
         [&](int k, int j, double v) { G[(size_t)k * n + j] = v; });
   } else {
     for (int idx = tid; idx < n * n; idx += NTB) G[idx] = (double)W32[idx];
@@ -412,8 +498,8 @@ __device__ int fp32_stage(double *A, int lda, double *V, double *G, const double
   // D = W W^T - I in FP64 from the FP32 W (exact products), stored as FP32 over the idle A32
   // (|D| ~ 1e-6, so FP32 keeps it to ~1e-13), and the small correction D V in FP32
   float *D32 = A32;
-  tile_product_t<double>(
-      n, true, [&](int k, int l) { return (double)W32[k * n + l]; }, [&](int l, int j) { return (double)W32[j * n + l]; },
+  tile_product_df(
+      n, n, n, true, [&](int k, int l) { return W32[k * n + l]; }, [&](int l, int j) { return W32[j * n + l]; },
       [&](int k, int j, double v) {
         if (k <= j) {
           const float d = (float)(v - (k == j ? 1.0 : 0.0));
@@ -432,7 +518,7 @@ __device__ int fp32_stage(double *A, int lda, double *V, double *G, const double
     A[i * lda + j] = Fm[idx];
   }
   __syncthreads();
-  form_vfvt(A, lda, V, G, n);
+  form_vfvt(A, lda, V, G, n, true);
   return s32;
 }
 
@@ -486,8 +572,8 @@ constexpr double EIG_PT_RATIO = 3.0e-3;  // largest coupling / splitting for sec
 // FP32 sweeps for the density-only step, without FP64 rotation work: A32 (float, overlaying
 // A) is swept to max |a_pq| <= tol32 with the rotations W (float, behind A32); dg / rank /
 // order take the swept diagonal; X = W V (warm) or W (cold) is formed in FP32 and stored in V,
-// so X holds FP32 values whose products are exact in FP64; D = X X^T - I is accumulated in
-// FP64 from X^T staged in shared memory (conflict-free rows) and kept as FP32 (|D| ~ 1e-6);
+// so X holds FP32 values whose products are exact; D = X X^T - I is summed to FP64 accuracy
+// (double-float) from X^T staged in shared memory (conflict-free rows) and kept as FP32 (|D| ~ 1e-6);
 // one Newton-Schulz step V <- X - D X / 2 (the small product D X in FP32) leaves the rows of V
 // orthonormal to ~1e-13.  G (floats): [X32 | V32, later D32].  Returns the FP32 sweeps taken.
 __device__ int fp32_sweeps_orth(double *A, int lda, double *V, double *G, int n, double tol32, bool is_warm,
@@ -519,14 +605,15 @@ __device__ int fp32_sweeps_orth(double *A, int lda, double *V, double *G, int n,
     }
   }
   __syncthreads();
-  double *XT = A;  // X^T, stride lda (A32 and W32 are no longer needed)
+  float *XT = A32;  // X^T as FP32, stride lda (A32 and W32 are no longer needed)
   for (int idx = tid; idx < n * n; idx += NTB) {
     int i = idx / n, j = idx - i * n;
-    XT[j * lda + i] = (double)X32[idx];
+    XT[j * lda + i] = X32[idx];
   }
   __syncthreads();
-  tile_product_t<double>(
-      n, true, [&](int k, int l) { return XT[l * lda + k]; }, [&](int l, int j) { return XT[l * lda + j]; },
+  // exact FP32 products summed to FP64 accuracy on the FP32 pipe
+  tile_product_df(
+      n, n, n, true, [&](int k, int l) { return XT[l * lda + k]; }, [&](int l, int j) { return XT[l * lda + j]; },
       [&](int k, int j, double v) {
         if (k <= j) {
           const float d = (float)(v - (k == j ? 1.0 : 0.0));
@@ -565,13 +652,13 @@ __device__ bool newton_density_ov(double *S, const double *V, const double *Fm, 
   float *V32 = reinterpret_cast<float *>(G);
   double *C1 = G + ((size_t)n * n + 1) / 2;  // after V32; ends at or before n^2 (nsel <= n / 2)
   for (int idx = threadIdx.x; idx < n * n; idx += NTB) V32[idx] = (float)V[idx];
-  tile_product_mnk(
-      nsel, n, n, [&](int i, int l) { return V[(size_t)order[s0 + i] * n + l]; },
+  tile_product_df(
+      nsel, n, n, false, [&](int i, int l) { return V[(size_t)order[s0 + i] * n + l]; },
       [&](int l, int j) { return Fm[(size_t)l * n + j]; }, [&](int i, int j, double v) { Gs[(size_t)j * nsel + i] = v; });
   __syncthreads();
   // a_st for t (rows, contiguous V_T rows broadcast) x s (columns of (V_S F)^T, contiguous)
-  tile_product_mnk(
-      ncomp, nsel, n, [&](int t, int l) { return V[(size_t)order[t0 + t] * n + l]; },
+  tile_product_df(
+      ncomp, nsel, n, false, [&](int t, int l) { return V[(size_t)order[t0 + t] * n + l]; },
       [&](int l, int i) { return Gs[(size_t)l * nsel + i]; },
       [&](int t, int i, double v) {
         const double d = dg[order[s0 + i]] - dg[order[t0 + t]];
@@ -604,7 +691,7 @@ __device__ bool newton_density_ov(double *S, const double *V, const double *Fm, 
       [&](int l, int k) { return C1_32[l * n + k]; },
       [&](int i, int k, float v) { U[(size_t)i * n + k] = C1[(size_t)i * n + k] - 0.5 * (double)v; });
   __syncthreads();
-  tile_product_mnk_t<double>(
+  tile_product_df(
       n, n, nsel, true, [&](int a, int k) { return U[(size_t)k * n + a]; },
       [&](int k, int c) { return U[(size_t)k * n + c]; },
       [&](int a, int c, double s) {
@@ -705,7 +792,7 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
       A[i * lda + j] = Fm[idx];
     }
     __syncthreads();
-    form_vfvt(A, lda, V, G, n);
+    form_vfvt(A, lda, V, G, n, true);
     a64_ready = true;
   } else if (density_only == 2 && evecs == nullptr && P != nullptr && fp32_ok) {
     // eigenvalues only: FP32 sweeps of the rotated F (warm) or F (cold), FP32 lift and
@@ -731,7 +818,7 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
       A[i * lda + j] = Fm[idx];
     }
     __syncthreads();
-    form_vfvt(A, lda, V, G, n);
+    form_vfvt(A, lda, V, G, n, true);
     a64_ready = true;
     newton = true;  // nearly diagonal: try the second-order eigenvalues first
   } else if (is_warm && want_newton && fp32_ok) {
@@ -746,7 +833,7 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
         A[i * lda + j] = Fm[idx];
       }
       __syncthreads();
-      form_vfvt(A, lda, V, G, n);
+      form_vfvt(A, lda, V, G, n, true);
       rank_diag(A, lda, n, dg, rank, order);
       newton = ov_theta(A, lda, n, nocc, dg, order, sh.red) <= NEWTON_THETA;
       if (!newton) {  // rare: back to F in A for the FP32 stage below
@@ -762,7 +849,7 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
       a32_ready = true;
     }
   } else if (is_warm) {
-    form_vfvt(A, lda, V, G, n);
+    form_vfvt(A, lda, V, G, n, fp32_ok);  // FP64 products when the FP32 stages are off
     if (want_newton) {
       rank_diag(A, lda, n, dg, rank, order);
       newton = ov_theta(A, lda, n, nocc, dg, order, sh.red) <= NEWTON_THETA;

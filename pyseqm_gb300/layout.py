@@ -15,6 +15,8 @@ convert per-molecule matrices to and from the reference's padded
 ``(nmol, 4*molsize, 4*molsize)`` layout (seqm/seqm_functions/pack.py:8-96).
 """
 
+import ctypes
+
 import numpy as np
 import torch
 
@@ -126,18 +128,10 @@ class Layout:
         L.hh_off = np.concatenate([[0], np.cumsum(L.nhh_m)])
         L.nxx, L.nxh, L.nhh = int(L.xx_off[-1]), int(L.xh_off[-1]), int(L.hh_off[-1])
         L.npairs = L.nxx + L.nxh + L.nhh
-        pi = np.empty(L.npairs, dtype=np.int64)
-        pj = np.empty(L.npairs, dtype=np.int64)
-        a0 = L.atom_off[:-1]
-        _group_fill([(pi[: L.nxx], a0), (pj[: L.nxx], a0)], L.xx_off, None, [nh],
-                    lambda n: np.triu_indices(n, 1))
-        _group_fill([(pi[L.nxx: L.nxx + L.nxh], a0), (pj[L.nxx: L.nxx + L.nxh], a0 + nh)], L.xh_off, None, [nh, ny],
-                    lambda a, b: (np.repeat(np.arange(a), b), np.tile(np.arange(b), a)))
-        _group_fill([(pi[L.nxx + L.nxh:], a0 + nh), (pj[L.nxx + L.nxh:], a0 + nh)], L.hh_off, None, [ny],
-                    lambda n: np.triu_indices(n, 1))
-        L.pair_i, L.pair_j = pi, pj
+        L._pairs = None  # host pair list, built on first use (to_device builds a CUDA batch's on the GPU)
         L.pair_skip = None
         if pair_cutoff is not None and L.npairs:
+            pi, pj = L.pair_i, L.pair_j
             d = L.xyz[pj] - L.xyz[pi]
             skip = np.sum(d * d, axis=1) >= float(pair_cutoff) ** 2
             if skip.any():
@@ -162,6 +156,32 @@ class Layout:
         L.par = par
         return L
 
+    # ------------------------------------------------------------------- pairs
+    def _host_pairs(self):
+        """Global atom indices of every pair in the class-segment order (what seqm_build_pairs
+        writes on the device): heavy-heavy and H-H row-major i < j, heavy-H by heavy atom then H."""
+        if self._pairs is None:
+            nh, ny = self.nheavy, self.nhyd
+            pi = np.empty(self.npairs, dtype=np.int64)
+            pj = np.empty(self.npairs, dtype=np.int64)
+            a0 = self.atom_off[:-1]
+            nxx, nxh = self.nxx, self.nxh
+            _group_fill([(pi[:nxx], a0), (pj[:nxx], a0)], self.xx_off, None, [nh], lambda n: np.triu_indices(n, 1))
+            _group_fill([(pi[nxx: nxx + nxh], a0), (pj[nxx: nxx + nxh], a0 + nh)], self.xh_off, None, [nh, ny],
+                        lambda a, b: (np.repeat(np.arange(a), b), np.tile(np.arange(b), a)))
+            _group_fill([(pi[nxx + nxh:], a0 + nh), (pj[nxx + nxh:], a0 + nh)], self.hh_off, None, [ny],
+                        lambda n: np.triu_indices(n, 1))
+            self._pairs = (pi, pj)
+        return self._pairs
+
+    @property
+    def pair_i(self):
+        return self._host_pairs()[0]
+
+    @property
+    def pair_j(self):
+        return self._host_pairs()[1]
+
     # ----------------------------------------------------------------- device
     def to_device(self, device="cuda"):
         i32 = lambda a: torch.as_tensor(np.asarray(a, dtype=np.int32), device=device)  # noqa: E731
@@ -173,8 +193,14 @@ class Layout:
             "xx_off": i32(self.xx_off), "xh_off": i32(self.xh_off), "hh_off": i32(self.hh_off),
             "order": i32(self.order), "Z": i32(self.Z), "atom_mol": i32(self.atom_mol),
             "xyz": f64(self.xyz.reshape(-1)), "par": f64(self.par.reshape(-1)),
-            "pair_i": i32(self.pair_i), "pair_j": i32(self.pair_j),
         }
+        # a CUDA batch whose host pair list was not needed builds it on the GPU (seqm_build_pairs)
+        on_gpu = torch.device(device).type == "cuda" and self._pairs is None
+        if on_gpu:
+            d["pair_i"] = torch.empty(max(1, self.npairs), dtype=torch.int32, device=device)
+            d["pair_j"] = torch.empty(max(1, self.npairs), dtype=torch.int32, device=device)
+        else:
+            d["pair_i"], d["pair_j"] = i32(self.pair_i), i32(self.pair_j)
         if self.uhf:
             d["nocc_a"], d["nocc_b"] = i32(self.nocc_a), i32(self.nocc_b)
         if self.pair_par is not None:
@@ -200,6 +226,13 @@ class Layout:
             mat_total=int(self.mat_off[-1]),
         )
         set_size_classes(self._struct, self.norb[self.order] if self.nmol else np.zeros(0, np.int64))
+        # bytes copied from the host (the pair list built on the GPU is not among them)
+        self.h2d_bytes = sum(int(t.numel() * t.element_size()) for k, t in d.items()
+                             if not (on_gpu and k in ("pair_i", "pair_j")))
+        if on_gpu and self.npairs:
+            stream = torch.cuda.current_stream(self.device).cuda_stream
+            native.check(native.load().seqm_build_pairs(self._struct, native.ptr(d["pair_i"]), native.ptr(d["pair_j"]),
+                                                        ctypes.c_void_p(stream)), "seqm_build_pairs")
         return self
 
     def set_coordinates(self, xyz_real):

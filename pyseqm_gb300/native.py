@@ -29,7 +29,7 @@ PAR = {n: i for i, n in enumerate(PAR_NAMES)}
 EXPORTS = ["seqm_hcore", "seqm_fock", "seqm_density_jacobi", "seqm_density_jacobi_noalloc", "seqm_density_sp2",
            "seqm_density_sp2_tc", "seqm_mix", "seqm_energy_error",
            "seqm_initial_density", "seqm_pair_sum", "seqm_energy_grad", "seqm_sp2_tc_work_bytes", "seqm_diis_init",
-           "seqm_diis_extrapolate", "seqm_diis_mix", "seqm_fock_u", "seqm_energy_error_u", "seqm_fock_general", "seqm_energy_grad_excited", "seqm_scf_step", "seqm_version"]
+           "seqm_diis_extrapolate", "seqm_diis_mix", "seqm_fock_u", "seqm_energy_error_u", "seqm_fock_general", "seqm_energy_grad_excited", "seqm_scf_step", "seqm_build_pairs", "seqm_version"]
 DIIS_STATE = 124  # SEQM_DIIS_STATE
 
 _P = ctypes.c_void_p
@@ -104,6 +104,7 @@ def load(path=None):
         "seqm_fock_general": [B, i32, _P, _P, _P, _P, _P, ctypes.c_int64, _P, _P],
         "seqm_energy_grad_excited": [B, _P, _P, _P, _P, _P, _P, _P, _P],
         "seqm_scf_step": [B, ctypes.POINTER(ScfState), _P],
+        "seqm_build_pairs": [B, _P, _P, _P],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

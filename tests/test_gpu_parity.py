@@ -206,3 +206,25 @@ def test_scf_step_entry_matches_the_separate_calls():
     np.testing.assert_array_equal(out[0][0], out[1][0])
     np.testing.assert_array_equal(out[0][1], out[1][1])
     assert out[0][2] == 0
+
+
+def test_device_pair_list_matches_host_enumeration():
+    """seqm_build_pairs on the GPU against the host enumeration of the same layout, on a batch
+    with single atoms, hydrogen-only and hydrogen-free molecules, and size classes of every kind."""
+    import torch
+
+    from pyseqm_gb300 import native, workloads
+    from pyseqm_gb300.layout import Layout
+
+    rng = np.random.default_rng(3)
+    mols = [workloads.alkane(k, rng, 0.03) for k in (1, 2, 9, 16)] + \
+           [workloads.water_cluster(k, rng) for k in (2, 7, 24)]
+    mols += [(np.array([8]), np.zeros((1, 3))), (np.array([1, 1]), np.array([[0.0, 0, 0], [0.74, 0, 0]])),
+             (np.array([8, 8]), np.array([[0.0, 0, 0], [1.21, 0, 0]]))]
+    species, coords = workloads.pad_batch(mols)
+    L = Layout.from_padded(species, coords, "AM1").to_device("cuda")
+    torch.cuda.synchronize()
+    dev_i, dev_j = L.dev["pair_i"][: L.npairs].cpu().numpy(), L.dev["pair_j"][: L.npairs].cpu().numpy()
+    np.testing.assert_array_equal(dev_i, L.pair_i)  # host enumeration, built on this access
+    np.testing.assert_array_equal(dev_j, L.pair_j)
+    assert native.load() is not None

@@ -308,16 +308,19 @@ def run_ours(args):
                                   "(SCF iterations 2 and 11: 404 / 280 MB for 52.7 % of the matrix elements), "
                                   "scaled to the batch and averaged over the 15 density calls of a solve",
                 "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (the measured-peaks file has no FP64 "
-                               "figure)",
+                               "figure); the unit counts FP64-accurate eigensolve work, which the kernel runs as FP32 "
+                               "sweeps, a first-order density step and double-float products on the FP32 pipe, so "
+                               "the fraction can exceed 1",
                 "algorithmic_unit": "9 n^3 + 2 n^2 nocc flops per molecule and density call (eigensolve with "
                                     "vectors, symmetric QR convention, + density), summed over the molecules "
                                     "each call solves",
                 "algorithmic_tflop": unit_jac / 1e12,
                 "executed_fp64": {"achieved": exec_jac / t_jac / 1e12 if t_jac else None,
                                   "frac": (exec_jac / t_jac / 1e12 / peak_fp64) if t_jac else None,
-                                  "what": "FP64 products the path executes: SCF step 2 (n^2 s + s (n - s) n + "
-                                          "n^2 s / 2), s = min(nocc, n - nocc), + n^3 after FP32 sweeps; final "
-                                          "eigenvalue step 4 n^3 (FP32 sweep work not counted)"},
+                                  "what": "FP64-accurate products the path executes (double-float on the FP32 "
+                                          "pipe), as FP64 flops: SCF step 2 (n^2 s + s (n - s) n + n^2 s / 2), "
+                                          "s = min(nocc, n - nocc), + n^3 after FP32 sweeps; final eigenvalue step "
+                                          "4 n^3 (FP32 sweep work not counted)"},
                 "launches": len(s.density_events), "avg_launch_ms": 1e3 * t_jac / max(1, len(s.density_events)),
                 "share_of_step_time": t_jac / elapsed}
     t_fock, unit_fock = _events_sum(s.fock_events)

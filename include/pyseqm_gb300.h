@@ -192,8 +192,10 @@ int seqm_density_sp2(const seqm_batch *b, const double *F, double *P, double *wo
  * accumulation in tensor memory; operands as pre-split tiles moved by bulk asynchronous
  * copies, the SP2 update fused into the product's epilogue), then one FP32 McWeeny step
  * X <- 3X^2 - 2X^3 of X = P/2 and mcweeny_steps FP64-accurate ones (X <- X + D (I - 2X),
- * D = X^2 - X, with X^2 in FP64 and the small correction product in FP32): idempotency
- * ~1e-11 after one, FP64 level after two.  Same purification and branch test as
+ * D = X^2 - X, with X^2 FP64-accurate from FP32 pairs and the small correction product on the
+ * tensor cores, D scaled per molecule into FP16's range): idempotency ~1e-11 after one, FP64
+ * level after two.  Molecules with active[m] == 2 (an SCF iteration that may keep the FP32-level
+ * density, see seqm_scf_step) take the FP32 McWeeny step only.  Same purification and branch test as
  * SP2.py:9-85 (the trace of X^2 for the test is ||X||_F^2 in FP64); a molecule stops when
  * the trace error is below eps, or below 1e-2 and no longer improving (SP2.py:76-80).  No
  * counterpart of the mixed-precision form in the reference.  work: 256-byte aligned,
@@ -239,7 +241,12 @@ int seqm_energy_error(const seqm_batch *b, const double *P, const double *Pold, 
  * to *nactive on the device (NULL: not counted) and no call synchronises the stream, so
  * iterations can be queued ahead or captured in a CUDA graph.
  * mixing: 0 linear (alpha), 1 adaptive, -1 none (P already mixed, e.g. by seqm_diis_mix; pass
- * diis_err then).  Every pointer is device memory; the struct itself is read on the host. */
+ * diis_err then).  Every pointer is device memory; the struct itself is read on the host.
+ * active[m]: 0 retired, 1 active, 2 active with a density from seqm_density_sp2_tc that skipped
+ * the FP64-accurate McWeeny step.  A molecule at 2 is never retired on that density: the test
+ * keeps it active and moves it to 1 (refined densities from then on) once |dE| < 1 eV or after
+ * 8 iterations (iters).  A caller that starts molecules at 2 saves that step's cost, about three
+ * times the rest of an iteration at thousands of basis functions, on the early iterations. */
 typedef struct seqm_scf_state {
   double *P;                /* [T] in: density; out: the mixed density */
   const double *Pnew;       /* [T] the density step's output */
@@ -251,7 +258,7 @@ typedef struct seqm_scf_state {
   double *Eelec, *Eout, *err, *dm_err, *dm_el;    /* [nmol] as seqm_energy_error */
   const int64_t *mol_row_off;                     /* [nmol+1] prefix sum of norb */
   int32_t *iters;           /* [nmol] density steps per molecule (seqm_mix) */
-  uint8_t *active;          /* [nmol] in/out */
+  uint8_t *active;          /* [nmol] in/out: 0, 1 or 2 (above) */
   const double *diis_err;   /* [nmol] or NULL */
   int32_t *nactive;         /* [1] out, or NULL */
   int32_t mixing, pad_;

@@ -260,14 +260,24 @@ __device__ double block_max(double v, double *red) {
 // not converged <=> |dE| > eps or ||dP||_F/(4 natoms + 9 nsuper) > 2 eps or max|dP| > 15 eps,
 // the density terms refreshed only when the energy test passes.
 //
+// active[m] == 2 marks a molecule whose density of this iteration came from the tensor-core SP2
+// without its FP64-accurate McWeeny step (that step costs about three times the rest of the
+// iteration at thousands of basis functions, and the SCF tolerates the FP32-level density while
+// the energy still moves by more than REFINE_DE).  Such a molecule is never retired on that
+// density; it turns to 1 (refined densities from the next iteration on) once |dE| < REFINE_DE or
+// after REFINE_ITERS iterations, and stays there.  The FP32-level density moves the energy by
+// ~1e-3 eV between iterations at 6000 basis functions, far below REFINE_DE.
+//
 // One cluster of cs CTAs per molecule.  The molecule's elements are cut into ns
 // interleaved slices (slice s: elements s*NT + t + k*ns*NT; ns grows with the
 // molecule's size up to EE_SLICES); CTA rank r sums the slices s with s % cs == r,
 // and rank 0 adds the slice sums in slice order through distributed shared memory,
 // so the result does not depend on cs.
+constexpr double REFINE_DE = 1.0;  // eV
+constexpr int REFINE_ITERS = 8;
 __device__ __forceinline__ void finish_error(const seqm_batch &b, int m, double e, double fro, double mx, double *Eelec,
                                         double *err, double *dm_err, double *dm_el, uint8_t *active, double eps,
-                                        const double *diis_err, int *nactive) {
+                                        const double *diis_err, int *nactive, const int32_t *kit) {
   double de = e - Eelec[m];
   err[m] = de;
   // with DIIS, also max |F P - P F| > 50 eps (scf_loop.py:130-132)
@@ -276,9 +286,13 @@ __device__ __forceinline__ void finish_error(const seqm_batch &b, int m, double 
     dm_err[m] = sqrt(fro) / dm_norm(b, m);
     dm_el[m] = mx;
   }
-  bool nc = bad || dm_err[m] > eps * 2.0 || dm_el[m] > eps * 15.0;
+  const uint8_t a = active ? active[m] : 1;
+  bool nc = bad || dm_err[m] > eps * 2.0 || dm_el[m] > eps * 15.0 || a == 2;
   if (nc) Eelec[m] = e;
-  if (active) active[m] = nc ? 1 : 0;
+  if (active) {
+    const bool keep_unrefined = a == 2 && !(fabs(de) < REFINE_DE) && !(kit && kit[m] >= REFINE_ITERS);
+    active[m] = !nc ? 0 : (keep_unrefined ? 2 : 1);
+  }
   if (nc && nactive) atomicAdd(nactive, 1);
 }
 
@@ -289,7 +303,8 @@ __global__ void __launch_bounds__(NT_RED) k_energy_error(seqm_batch b, const dou
                                                          const double *__restrict__ F, double *Eelec, double *Eout,
                                                          double *err, double *dm_err, double *dm_el, uint8_t *active,
                                                          double eps, const double *__restrict__ diis_err,
-                                                         int *__restrict__ nactive, int cs) {
+                                                         int *__restrict__ nactive,
+                                                         const int32_t *__restrict__ kit, int cs) {
   __shared__ double wred[NT_RED / 32][3 * EE_SLICES];
   __shared__ double part[3 * EE_SLICES];
   cg::cluster_group cl = cg::this_cluster();
@@ -352,7 +367,7 @@ __global__ void __launch_bounds__(NT_RED) k_energy_error(seqm_batch b, const dou
     }
     e *= 0.5;
     Eout[m] = e;
-    if (Pold) finish_error(b, m, e, fro, mx, Eelec, err, dm_err, dm_el, active, eps, diis_err, nactive);
+    if (Pold) finish_error(b, m, e, fro, mx, Eelec, err, dm_err, dm_el, active, eps, diis_err, nactive, kit);
   }
   cl.sync();  // the other CTAs' shared memory stays alive until rank 0 has read it
 }
@@ -370,7 +385,8 @@ __device__ __forceinline__ int warp_molecule(const seqm_batch &b, int w) {
 __global__ void __launch_bounds__(32 * EE_WARPS) k_energy_error_warp(
     seqm_batch b, const double *__restrict__ P, const double *__restrict__ Pold, const double *__restrict__ H,
     const double *__restrict__ F, double *Eelec, double *Eout, double *err, double *dm_err, double *dm_el,
-    uint8_t *active, double eps, const double *__restrict__ diis_err, int *__restrict__ nactive) {
+    uint8_t *active, double eps, const double *__restrict__ diis_err, int *__restrict__ nactive,
+    const int32_t *__restrict__ kit) {
   const int w = blockIdx.x * EE_WARPS + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (w >= b.nmol) return;
   const int m = warp_molecule(b, w);
@@ -408,7 +424,7 @@ __global__ void __launch_bounds__(32 * EE_WARPS) k_energy_error_warp(
   if (lane == 0) {
     e *= 0.5;
     Eout[m] = e;
-    if (Pold) finish_error(b, m, e, fro, mx, Eelec, err, dm_err, dm_el, active, eps, diis_err, nactive);
+    if (Pold) finish_error(b, m, e, fro, mx, Eelec, err, dm_err, dm_el, active, eps, diis_err, nactive, kit);
   }
 }
 
@@ -705,13 +721,13 @@ static int launch_clusters(void (*kern)(Params...), int cs, int nmol, int nt, si
 // energy + test of every molecule: the warp kernel for molecules up to EE_WARP_MAX basis
 // functions, the cluster kernel (launched only when the batch holds larger ones) for the rest
 template <typename... Args>
-int launch_energy_error(const seqm_batch &b, void *stream, int *nactive, Args... args) {
+int launch_energy_error(const seqm_batch &b, void *stream, int *nactive, const int32_t *kit, Args... args) {
   k_energy_error_warp<<<(b.nmol + EE_WARPS - 1) / EE_WARPS, 32 * EE_WARPS, 0, (cudaStream_t)stream>>>(b, args...,
-                                                                                                        nactive);
+                                                                                                        nactive, kit);
   int rc = launch_check();
   if (rc != SEQM_OK || b.max_norb <= EE_WARP_MAX) return rc;
   const int cs = mol_cluster(k_energy_error, b.max_norb);
-  return launch_clusters(k_energy_error, cs, b.nmol, NT_RED, 0, stream, b, args..., nactive, cs);
+  return launch_clusters(k_energy_error, cs, b.nmol, NT_RED, 0, stream, b, args..., nactive, kit, cs);
 }
 
 extern "C" int seqm_fock(const seqm_batch *bp, const double *P, const double *H, const double *w_xx,
@@ -730,8 +746,8 @@ extern "C" int seqm_energy_error(const seqm_batch *bp, const double *P, const do
   if (!bp) return SEQM_E_ARG;
   seqm_batch b = *bp;
   if (b.nmol == 0) return SEQM_OK;
-  return launch_energy_error(b, stream, (int *)nullptr, P, Pold, H, F, Eelec, Eout, err, dm_err, dm_el, active, eps,
-                             diis_err);
+  return launch_energy_error(b, stream, (int *)nullptr, (const int32_t *)nullptr, P, Pold, H, F, Eelec, Eout, err,
+                             dm_err, dm_el, active, eps, diis_err);
 }
 
 extern "C" int seqm_scf_step(const seqm_batch *bp, const seqm_scf_state *st, void *stream) {
@@ -749,9 +765,9 @@ extern "C" int seqm_scf_step(const seqm_batch *bp, const seqm_scf_state *st, voi
   rc = seqm_fock(bp, st->P, st->H, st->w_xx, st->w_xh, st->w_hh, st->F, st->active, stream);
   if (rc != SEQM_OK) return rc;
   if (st->nactive && cudaMemsetAsync(st->nactive, 0, sizeof(int32_t), s) != cudaSuccess) return SEQM_E_CUDA;
-  return launch_energy_error(b, stream, (int *)st->nactive, (const double *)st->P, (const double *)st->Pold, st->H,
-                             (const double *)st->F, st->Eelec, st->Eout, st->err, st->dm_err, st->dm_el, st->active,
-                             st->eps, st->diis_err);
+  return launch_energy_error(b, stream, (int *)st->nactive, (const int32_t *)st->iters, (const double *)st->P,
+                             (const double *)st->Pold, st->H, (const double *)st->F, st->Eelec, st->Eout, st->err,
+                             st->dm_err, st->dm_el, st->active, st->eps, st->diis_err);
 }
 
 extern "C" int seqm_mix(const seqm_batch *bp, double *P, const double *Pnew, double *Pold, double *old2,

@@ -25,6 +25,13 @@ constexpr int EW_THREADS = 256;
 constexpr int SP2_SYNC_EVERY = 4;
 constexpr int EW_CHUNK = EW_THREADS * 8;  // elements per CTA of an elementwise pass
 
+// row of element idx of an n x n matrix, and whether it lies on the diagonal: 32-bit division
+// (n^2 < 2^32 for every molecule a batch can hold), several times cheaper than a 64-bit one
+__device__ __forceinline__ uint32_t row_of(size_t idx, int n) { return (uint32_t)idx / (uint32_t)n; }
+__device__ __forceinline__ bool diagonal(size_t idx, int n) {
+  return (uint32_t)idx == row_of(idx, n) * (uint32_t)(n + 1);
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -106,13 +113,14 @@ __global__ void __launch_bounds__(EW_THREADS) k_sp2_scale(seqm_batch b, const do
   const int n = b.mol_norb[m];
   const size_t nn = (size_t)n * n, base = (size_t)blockIdx.x * EW_CHUNK;
   if (base >= nn) return;
-  const double h1 = s[S_H1], hN = s[S_HN];
+  const double h1 = s[S_H1], hN = s[S_HN], inv = 1.0 / (hN - h1);
   const size_t mo = b.mol_mat_off[m];
   double tr = 0.0, f2 = 0.0;
   for (size_t idx = base + threadIdx.x; idx < nn && idx < base + EW_CHUNK; idx += EW_THREADS) {
-    const size_t i = idx / n;
-    const bool d = idx == i * n + i;
-    const T v = (T)(((d ? hN : 0.0) - F[mo + idx]) / (hN - h1));
+    const bool d = diagonal(idx, n);
+    // the FP64 form divides as SP2.py:36-43 does; the FP32 iterate takes the reciprocal
+    const double a = (d ? hN : 0.0) - F[mo + idx];
+    const T v = (T)(sizeof(T) == 8 ? a / (hN - h1) : a * inv);
     X[mo + idx] = v;
     if (d) tr += (double)v;
     f2 += (double)v * (double)v;
@@ -151,8 +159,7 @@ __global__ void __launch_bounds__(EW_THREADS) k_sp2_step(seqm_batch b, T *__rest
     const T x = X[mo + idx], y = X2[mo + idx];
     const T v = sq ? y : (T)2 * x - y;
     X[mo + idx] = v;
-    const size_t i = idx / n;
-    if (idx == i * n + i) tr += (double)v;
+    if (diagonal(idx, n)) tr += (double)v;
     f2 += (double)v * (double)v;
   }
   cta_accumulate2(tr, f2, s + S_ACC_T);
@@ -200,7 +207,7 @@ __global__ void __launch_bounds__(EW_THREADS) k_ew_sym(seqm_batch b, const T *__
   if (base >= nn) return;
   const size_t mo = b.mol_mat_off[m];
   for (size_t idx = base + threadIdx.x; idx < nn && idx < base + EW_CHUNK; idx += EW_THREADS) {
-    const size_t i = idx / n, j = idx - i * n;
+    const size_t i = row_of(idx, n), j = idx - i * n;
     P[mo + idx] = c1 * (double)A[mo + idx] + c2 * (double)A[mo + j * n + i];
   }
 }
@@ -517,24 +524,32 @@ inline dim3 pair_gemm_grid(const seqm_batch &b) {
 
 // McWeeny step X <- 3 X^2 - 2 X^3 written as X + D (I - 2X) with D = X^2 - X: X^2 FP64-accurate
 // gives D exactly, and the correction D (I - 2X), a product of a matrix of the size
-// of the idempotency error, is formed in FP32 (relative error ~1e-7 of a term <= |D|),
+// of the idempotency error, is formed at FP32 level (relative error ~1e-7 of a term <= |D|),
 // so every step is FP64-accurate at one FP64-accurate product instead of two.
-// Df = float(Y - Z), Bf = float(I - 2 Z)
+// Df = float(Y - Z), Bf = float(I - 2 Z); with dmax, also max |Df| of each molecule (as the bits
+// of a non-negative float, which order like the unsigned integers)
 __global__ void __launch_bounds__(EW_THREADS) k_mw_split(seqm_batch b, const double *__restrict__ Y,
                                                          const double *__restrict__ Z, float *__restrict__ Df,
-                                                         float *__restrict__ Bf, const uint8_t *__restrict__ active) {
+                                                         float *__restrict__ Bf, const uint8_t *__restrict__ active,
+                                                         uint32_t *__restrict__ dmax = nullptr) {
   const int m = blockIdx.y;
   if (active && !active[m]) return;
   const int n = b.mol_norb[m];
   const size_t nn = (size_t)n * n, base = (size_t)blockIdx.x * EW_CHUNK;
   if (base >= nn) return;
   const size_t mo = b.mol_mat_off[m];
+  float mx = 0.0f;
   for (size_t idx = base + threadIdx.x; idx < nn && idx < base + EW_CHUNK; idx += EW_THREADS) {
-    const size_t i = idx / n;
     const double z = Z[mo + idx];
-    Df[mo + idx] = (float)(Y[mo + idx] - z);
-    Bf[mo + idx] = (float)((idx == i * n + i ? 1.0 : 0.0) - 2.0 * z);
+    const float d = (float)(Y[mo + idx] - z);
+    Df[mo + idx] = d;
+    Bf[mo + idx] = (float)((diagonal(idx, n) ? 1.0 : 0.0) - 2.0 * z);
+    mx = fmaxf(mx, fabsf(d));
   }
+  if (!dmax) return;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0 && mx > 0.0f) atomicMax(dmax + m, __float_as_uint(mx));
 }
 
 // P = 2 (Z + C)
@@ -549,25 +564,6 @@ __global__ void __launch_bounds__(EW_THREADS) k_mw_update(seqm_batch b, const do
   const size_t mo = b.mol_mat_off[m];
   for (size_t idx = base + threadIdx.x; idx < nn && idx < base + EW_CHUNK; idx += EW_THREADS)
     P[mo + idx] = 2.0 * (Z[mo + idx] + (double)C[mo + idx]);
-}
-
-// McWeeny refinement of the density P (X = P/2), `steps` times.  Y, Z: FP64 scratch of the
-// batch's matrix size; Df, Bf: FP32 scratch of the same size (Y doubles as the FP32 product).
-inline void mcweeny(const seqm_batch &b, double *P, double *Y, double *Z, float *Df, float *Bf,
-                    const uint8_t *active, int steps, cudaStream_t s, bool pair_product = false) {
-  float *Cf = reinterpret_cast<float *>(Y);
-  for (int k = 0; k < steps; ++k) {
-    k_ew_axpby<<<ew_grid(b), EW_THREADS, 0, s>>>(b, 0.5, P, 0.0, nullptr, Z, active);        // Z = X
-    if (pair_product) {  // Y = X^2 from FP32 pairs (Df, Bf hold Xh, Xl until k_mw_split)
-      k_split_pair<<<ew_grid(b), EW_THREADS, 0, s>>>(b, Z, Df, Bf, active);
-      k_sym_gemm_pair<<<pair_gemm_grid(b), DF_THREADS, 0, s>>>(b, Df, Bf, Y, active);
-    } else {
-      k_sym_gemm<double><<<gemm64_grid(b), MW_THREADS, 0, s>>>(b, Z, Z, Y, active, nullptr);  // Y = X^2 (FP64)
-    }
-    k_mw_split<<<ew_grid(b), EW_THREADS, 0, s>>>(b, Y, Z, Df, Bf, active);                   // D, I - 2X
-    k_sym_gemm<float><<<gemm64_grid(b), MW_THREADS, 0, s>>>(b, Df, Bf, Cf, active, nullptr);  // D (I - 2X)
-    k_mw_update<<<ew_grid(b), EW_THREADS, 0, s>>>(b, Z, Cf, P, active);                      // P = 2(X + ...)
-  }
 }
 
 }  // namespace

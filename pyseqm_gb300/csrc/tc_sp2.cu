@@ -194,16 +194,32 @@ __global__ void __launch_bounds__(1024) k_tc_tile_offsets(seqm_batch b, int64_t 
   if (threadIdx.x == 1023) xs_off[b.nmol] = part[1023];
 }
 
-// split tiles of the FP32 X of running molecules: CTA (kb, rb, m) writes tile (rb, kb)
+// Power-of-two exponent e of a molecule's operand scale: with dmax[m] = max |A| (float bits),
+// A 2^-e has its largest element in [0.5, 1), so a matrix of small elements (the McWeeny
+// correction D, ~1e-6) keeps FP16's 11 significant bits instead of falling into its subnormal
+// range.  No dmax or an all-zero matrix: e = 0.
+__device__ __forceinline__ int split_exp(const uint32_t *dmax, int m) {
+  if (!dmax) return 0;
+  const float mx = __uint_as_float(dmax[m]);
+  if (!(mx > 0.0f) || !(mx < INFINITY)) return 0;
+  int e = 0;
+  frexpf(mx, &e);
+  return e;
+}
+
+// split tiles of the FP32 X of running molecules (scaled by 2^-e of split_exp): CTA (kb, rb, m)
+// writes tile (rb, kb)
 __global__ void __launch_bounds__(128) k_tc_split(seqm_batch b, const float *__restrict__ X, uint8_t *__restrict__ Xh,
                                                   uint8_t *__restrict__ Xl, const int64_t *__restrict__ xs_off,
-                                                  const double *__restrict__ st, const uint8_t *__restrict__ active) {
+                                                  const double *__restrict__ st, const uint8_t *__restrict__ active,
+                                                  const uint32_t *__restrict__ dmax = nullptr) {
   const int m = blockIdx.z;
   if (st ? st[SP2_NS * m + S_RUN] == 0.0 : (active && !active[m])) return;  // running molecules, or active ones
   const int n = b.mol_norb[m];
   const int nb = (n + TC_M - 1) / TC_M, nk = (n + TC_KT - 1) / TC_KT;
   const int rb = blockIdx.y, kb = blockIdx.x;
   if (rb >= nb || kb >= nk) return;
+  const float scale = ldexpf(1.0f, -split_exp(dmax, m));
   const float *Xm = X + b.mol_mat_off[m];
   const size_t tile = (size_t)(xs_off[m] + (int64_t)rb * nk + kb) * SPLIT_TILE_BYTES;
   for (int g = threadIdx.x; g < TC_M * TC_KT / 8; g += 128) {
@@ -211,7 +227,7 @@ __global__ void __launch_bounds__(128) k_tc_split(seqm_batch b, const float *__r
     const int gr = rb * TC_M + row, gk = kb * TC_KT + kc;
     float v[8];
 #pragma unroll
-    for (int e = 0; e < 8; ++e) v[e] = (gr < n && gk + e < n) ? Xm[(size_t)gr * n + gk + e] : 0.0f;
+    for (int e = 0; e < 8; ++e) v[e] = (gr < n && gk + e < n) ? scale * Xm[(size_t)gr * n + gk + e] : 0.0f;
     split8(v, Xh + tile + tile_off(row, kc), Xl + tile + tile_off(row, kc));
   }
 }
@@ -255,12 +271,14 @@ __device__ __forceinline__ bool upper_tile(int t, int nb, int &tm, int &tn) {
 // Operands and epilogue of a plain split product (PROD launches of k_tc_step): C = cY Y + cAB A B,
 // B's split tiles in Bh / Bl (A's are the kernel's Xh / Xl), Y an FP32 matrix (NULL: C = cAB A B);
 // A and B must commute (functions of one symmetric matrix), so that A B is symmetric and its upper
-// tiles with their mirrors are the whole product.
+// tiles with their mirrors are the whole product.  A split with the scale of dmax (k_tc_split)
+// has cAB multiplied back by 2^e per molecule (exact).
 struct TcProduct {
   const uint8_t *Bh, *Bl;
   const float *Y;
   float cY, cAB;
   const uint8_t *active;
+  const uint32_t *dmax;
 };
 
 template <bool PROD>
@@ -376,6 +394,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_step(seqm_batch b, float *__r
     __syncthreads();
     // X' row by row: thread i owns accumulator row i (TMEM lane i)
     const double nocc = (double)b.mol_nocc[m], t1 = PROD ? 0.0 : s[S_T1], t2 = PROD ? 0.0 : s[S_T2];
+    const float cab = PROD ? ldexpf(pp.cAB, split_exp(pp.dmax, m)) : 0.0f;
     const bool sq = fabs(t2 - nocc) < fabs(2.0 * t1 - t2 - nocc);
     const int i = threadIdx.x, gi = tm * TC_M + i;
     // ||X'||_F^2 in FP32 per 32 columns, then FP64 (the sums of squares carry the tensor-core
@@ -390,7 +409,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_step(seqm_batch b, float *__r
       for (int j = 0; j < 32; ++j) {
         const int c = c0 + j;
         const float x = stg[i * EPI_LD + c];
-        float y = PROD ? fmaf(pp.cAB, v[j], pp.cY * x) : (sq ? v[j] : 2.0f * x - v[j]);
+        float y = PROD ? fmaf(cab, v[j], pp.cY * x) : (sq ? v[j] : 2.0f * x - v[j]);
         if (gi >= n || tn * TC_N + c >= n) y = 0.0f;  // keep the padding of the split tiles zero
         stg[i * EPI_LD + c] = y;
         q2 = fmaf(y, y, q2);
@@ -457,7 +476,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_step(seqm_batch b, float *__r
 
 // ----------------------------------------------------------------- work layout
 struct TcWork {
-  size_t x, x2, y, z, st, rowlo, rowhi, cnt, xs_off, xs[4], total;
+  size_t x, x2, y, z, st, rowlo, rowhi, cnt, xs_off, rmask, dmax, xs[4], total;
 };
 
 inline TcWork tc_work_layout(int64_t T, int nmol, int maxn) {
@@ -479,11 +498,44 @@ inline TcWork tc_work_layout(int64_t T, int nmol, int maxn) {
   w.rowhi = take(8 * nm * mx, 256);
   w.cnt = take(16, 256);
   w.xs_off = take(8 * (nm + 1), 256);
+  w.rmask = take(nm, 256);
+  w.dmax = take(4 * nm, 256);
   // sum over molecules of ceil(n/128) ceil(n/32) <= (T + nmol (159 maxn + 3937)) / 4096
   const size_t tiles = (t + nm * (159 * mx + 3937) + 4095) / 4096;
   for (int q = 0; q < 4; ++q) w.xs[q] = take(tiles * SPLIT_TILE_BYTES, 1024);
   w.total = o;
   return w;
+}
+
+// molecules whose density takes the FP64-accurate McWeeny step: active with value 1 (2 marks an
+// SCF iteration allowed to keep the FP32-level density; see the convergence test)
+__global__ void k_refine_mask(int nmol, const uint8_t *__restrict__ active, uint8_t *__restrict__ rmask) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < nmol) rmask[m] = active ? (active[m] == 1) : 1;
+}
+
+// FP64-accurate McWeeny step X <- X + D (I - 2X), D = X^2 - X (X = P/2), of the tensor-core form:
+// X^2 from FP32 pairs (k_sym_gemm_pair), the correction product as a split product on the tensor
+// cores with D scaled to FP16's range per molecule.  Buffers: Y, Z FP64 and Df, Bf FP32 of the
+// batch's matrix size (Y doubles as the FP32 correction), xs[0..3] split tiles.
+inline void mcweeny_tc(const seqm_batch &b, double *P, double *Y, double *Z, float *Df, float *Bf, uint8_t *const *xs,
+                       const int64_t *xs_off, double *st, int *err, uint32_t *dmax, const uint8_t *rmask, int steps,
+                       cudaStream_t s) {
+  float *Cf = reinterpret_cast<float *>(Y);
+  const int nb = (b.max_norb + TC_M - 1) / TC_M, nk = (b.max_norb + TC_KT - 1) / TC_KT;
+  const dim3 grid((unsigned)(nb * (nb + 1) / 2), (unsigned)b.nmol), split((unsigned)nk, (unsigned)nb, (unsigned)b.nmol);
+  for (int k = 0; k < steps; ++k) {
+    k_ew_axpby<<<ew_grid(b), EW_THREADS, 0, s>>>(b, 0.5, P, 0.0, nullptr, Z, rmask);  // Z = X
+    k_split_pair<<<ew_grid(b), EW_THREADS, 0, s>>>(b, Z, Df, Bf, rmask);
+    k_sym_gemm_pair<<<pair_gemm_grid(b), DF_THREADS, 0, s>>>(b, Df, Bf, Y, rmask);   // Y = X^2
+    cudaMemsetAsync(dmax, 0, sizeof(uint32_t) * b.nmol, s);
+    k_mw_split<<<ew_grid(b), EW_THREADS, 0, s>>>(b, Y, Z, Df, Bf, rmask, dmax);      // D, I - 2X, max |D|
+    k_tc_split<<<split, 128, 0, s>>>(b, Df, xs[0], xs[1], xs_off, nullptr, rmask, dmax);
+    k_tc_split<<<split, 128, 0, s>>>(b, Bf, xs[2], xs[3], xs_off, nullptr, rmask);
+    k_tc_step<true><<<grid, TC_THREADS, TC_SMEM, s>>>(b, Cf, xs[0], xs[1], nullptr, nullptr, xs_off, st, err,
+                                                     TcProduct{xs[2], xs[3], nullptr, 0.0f, 1.0f, rmask, dmax});
+    k_mw_update<<<ew_grid(b), EW_THREADS, 0, s>>>(b, Z, Cf, P, rmask);              // P = 2 (X + D (I - 2X))
+  }
 }
 
 }  // namespace seqm
@@ -582,7 +634,11 @@ extern "C" int seqm_density_sp2_tc(const seqm_batch *bp, const double *F, double
   k_tc_step<true><<<grid, TC_THREADS, TC_SMEM, s>>>(b, X, xs[2], xs[3], nullptr, nullptr, xs_off, st, cnt + LC_ERR,
                                                    TcProduct{xs[0], xs[1], X2, 3.0f, -2.0f, active});
   k_ew_sym<float><<<ew_grid(b), EW_THREADS, 0, s>>>(b, X, 1.0, 1.0, P, active);  // P = X + X^T
-  mcweeny(b, P, Y, Z, X, X2, active, mcweeny_steps, s, true);  // X, X2 are free after P = X + X^T
+  // FP64-accurate steps for the molecules that want them (X, X2 and the split tiles are free now)
+  uint8_t *rmask = base + w.rmask;
+  k_refine_mask<<<(b.nmol + 255) / 256, 256, 0, s>>>(b.nmol, active, rmask);
+  mcweeny_tc(b, P, Y, Z, X, X2, xs, xs_off, st, cnt + LC_ERR, reinterpret_cast<uint32_t *>(base + w.dmax), rmask,
+             mcweeny_steps, s);
   // after the products, so that a product kernel that gave up waiting shows in status too
   if (status) k_sp2_status<<<(b.nmol + 127) / 128, 128, 0, s>>>(b.nmol, st, active, status, cnt + LC_ERR);
   return launch_check();

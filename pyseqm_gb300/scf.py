@@ -76,6 +76,9 @@ class BatchSCF:
         # molecules above the Jacobi limit take SP2: "fp64" (plain) or "tc" (tensor cores + FP64 McWeeny)
         self.large_density = "fp64"
         self.mcweeny_steps = 1  # FP64-accurate McWeeny steps after the tensor-core SP2 (and one FP32 step)
+        # tensor-core SP2 molecules skip the FP64-accurate McWeeny step while their energy still moves
+        # by 1 eV or more per iteration (at most 8 iterations) and are never retired on such a density
+        self.refine_near_convergence = True
         # molecules above jacobi_max_n basis functions (at most the kernel's 160) take SP2
         if not 0 <= int(jacobi_max_n) <= JACOBI_MAX_N:
             raise ValueError(f"jacobi_max_n must lie in [0, {JACOBI_MAX_N}]")
@@ -302,6 +305,9 @@ class BatchSCF:
         self.dm_err.fill_(1.0)
         self.dm_el.fill_(1.0)
         self.active.fill_(1)
+        gated = self._refine_gated(sp2)
+        if gated is not None:
+            self.active[: L.nmol] += gated  # 2: the FP64-accurate McWeeny step may wait (see seqm_scf_step)
         self.iters.zero_()
         if not keep_warm:
             self.warm.zero_()
@@ -325,6 +331,17 @@ class BatchSCF:
             self.launches += 1
             native.check(self.lib.seqm_diis_init(b, native.ptr(self._diis_state), native.ptr(self._diis_err),
                                                  self._s()), "seqm_diis_init")
+
+    def _refine_gated(self, sp2):
+        """uint8 mask of the molecules whose tensor-core SP2 density may skip the FP64-accurate
+        McWeeny step early in the SCF (None: no molecule)."""
+        if not self.refine_near_convergence:
+            return None
+        if sp2[0]:
+            return self.large_mask.new_ones(self.L.nmol) if len(sp2) > 2 and sp2[2] == "tc" else None
+        if self.n_large and self.large_density == "tc":
+            return self.large_mask[: self.L.nmol]
+        return None
 
     def _scf_state(self):
         """seqm_scf_state of this solver's buffers and the current converger."""

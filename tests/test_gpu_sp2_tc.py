@@ -126,3 +126,36 @@ def test_mixing_at_the_48kb_shared_memory_edge():
     s.scf(1e-5, (1,), max_iter=2)
     torch.cuda.synchronize()
     assert int(s.iters[0]) == 2 and bool(torch.isfinite(s.Eout[:1]).all())
+
+
+def test_refinement_gate_matches_refining_every_iteration():
+    """(H2O)125 (750 AOs), tensor-core SP2: starting at active = 2, the early iterations keep the
+    FP32-level density (the FP64-accurate McWeeny step waits until |dE| < 1 eV) and the molecule
+    is never retired on such a density; the converged energy matches the run that refines every
+    iteration and the FP64 oracle, with idempotency at FP64 level."""
+    from pyseqm_gb300 import workloads
+    from pyseqm_gb300.layout import Layout
+    from pyseqm_gb300.scf import BatchSCF
+
+    species, coords = workloads.pad_batch([workloads.big_water(seed=3, n_side=5)])
+    L = Layout.from_padded(species, coords, "PM3").to_device("cuda")
+    out = {}
+    for gate in (True, False):
+        s = BatchSCF(L)
+        s.large_density = "tc"
+        s.refine_near_convergence = gate
+        s.hcore()
+        s.start(SCF_EPS_MIXED, (1,))
+        assert int(s.active[0]) == (2 if gate else 1)
+        s.step()
+        if gate:  # the first iteration moves the energy by far more than 1 eV
+            assert abs(float(s.err[0])) > 1.0 and int(s.active[0]) == 2
+        nc = s.iterate()
+        E, En = s.final(want_vectors=False)
+        assert not nc.any()
+        out[gate] = (float(E[0] + En[0]), int(s.iters[0]), _idempotency(L, s.P, 0))
+    (e1, it1, id1), (e0, it0, id0) = out[True], out[False]
+    assert abs(e1 - e0) < 5e-5 and abs(it1 - it0) <= 2
+    assert id1 < 1e-9 and id0 < 1e-9
+    ref = O.single_point("PM3", species, coords, 1e-8, (1,))
+    assert abs(e1 - float(ref["Etot"][0])) < TOL_E_MIXED

@@ -250,7 +250,7 @@ int seqm_energy_error(const seqm_batch *b, const double *P, const double *Pold, 
 typedef struct seqm_scf_state {
   double *P;                /* [T] in: density; out: the mixed density */
   const double *Pnew;       /* [T] the density step's output */
-  double *Pold;             /* [T] out: P before the mixing */
+  double *Pold;             /* [T] out: P before the mixing (unfused step; the fused one leaves it) */
   double *old2;             /* [sum norb] adaptive mixer's diagonal history (seqm_mix) */
   const double *H;          /* [T] core Hamiltonian */
   double *F;                /* [T] out: F(P) */
@@ -263,7 +263,15 @@ typedef struct seqm_scf_state {
   int32_t *nactive;         /* [1] out, or NULL */
   int32_t mixing, pad_;
   double alpha, occupation, eps;
+  double *scratch;          /* SEQM_SCF_SCRATCH_DOUBLES, or NULL (below) */
 } seqm_scf_state;
+/* With scratch != NULL and mixing >= 0 the step is fused: the mixer takes ||dP|| itself and leaves
+ * Pold untouched, the Fock build adds up P (H + F) per atom and per pair as it writes F, and one
+ * small kernel forms each molecule's energy from those sums in a fixed order and runs the test.
+ * No separate energy pass reads P, Pold, H and F again; the results equal the unfused step's to
+ * rounding.  Needs max_norb <= 12800.  Its size in doubles: */
+#define SEQM_SCF_SCRATCH_DOUBLES(nmol, natoms, npairs, sum_norb) \
+  (5 * (size_t)(nmol) + (size_t)(natoms) + (size_t)(npairs) + 4 * (size_t)(sum_norb))
 int seqm_scf_step(const seqm_batch *b, const seqm_scf_state *st, void *stream);
 
 /* Pulay DIIS converger (scf_converger [2]; scf_forward2, scf_loop.py:639-1132), per molecule.

@@ -54,6 +54,22 @@ __device__ __forceinline__ int find_mol(const int32_t *off, int nmol, int p) {
 // AO index of local atom la inside its molecule's packed basis (heavy: 4 per atom, H: 1)
 __device__ __forceinline__ int atom_ao(int la, int nheavy) { return la < nheavy ? 4 * la : 3 * nheavy + la; }
 
+// Exact j / d for 32-bit j without a division instruction (the 32-bit integer division goes through
+// conversions on a slow pipe): j / d = umulhi64(j, M) with M = ceil(2^64 / d), d >= 2 (the excess
+// j (M - 2^64/d) / 2^64 < 2^-32 never carries a fraction <= 1 - 1/d over an integer).
+struct FastDivU32 {
+  unsigned long long M;
+  uint32_t d;
+  __device__ explicit FastDivU32(uint32_t dv) : M(~0ULL / (unsigned long long)dv + 1), d(dv) {}
+  __device__ __forceinline__ uint32_t div(uint32_t j) const { return (uint32_t)__umul64hi((unsigned long long)j, M); }
+};
+// flat index j of an n x n matrix (n >= 1) lies on the diagonal: j is a multiple of n + 1
+struct DiagTest {
+  FastDivU32 q;
+  __device__ explicit DiagTest(int n) : q((uint32_t)(n + 1)) {}
+  __device__ __forceinline__ bool operator()(uint32_t j) const { return j == q.div(j) * q.d; }
+};
+
 inline int launch_check() {
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? SEQM_OK : SEQM_E_CUDA;

@@ -55,7 +55,7 @@ __device__ __forceinline__ double warp_allsum(double v) {
 __device__ __forceinline__ void fock_diag(const seqm_batch &b, int a, int lane, const double *__restrict__ P,
                                           const double *__restrict__ H, const double *__restrict__ w_xx,
                                           const double *__restrict__ w_xh, const double *__restrict__ w_hh,
-                                          double *__restrict__ F) {
+                                          double *__restrict__ F, double *__restrict__ epart) {
   const int m = b.atom_mol[a];
   const int a0 = b.mol_atom_off[m], nat = b.mol_atom_off[m + 1] - a0, nh = b.mol_nheavy[m], ny = nat - nh;
   const int norb = b.mol_norb[m], la = a - a0;
@@ -94,6 +94,7 @@ __device__ __forceinline__ void fock_diag(const seqm_batch &b, int a, int lane, 
     }
     const double f1 = __shfl_sync(0xffffffffu, f, (lane + 10) & 31);
     const double f2 = __shfl_sync(0xffffffffu, f, (lane + 20) & 31);
+    double ep = 0.0;
     if (lane < 10) {
       const double J = (f + f1) + f2;
       // one-centre terms (fock.py:187-231)
@@ -111,9 +112,15 @@ __device__ __forceinline__ void fock_diag(const seqm_batch &b, int a, int lane, 
       else if (r == c) oc = Pss * c1 + 0.5 * Prc * gpp + (Ppt - Prc) * c3;
       else if (r == 0) oc = Prc * c2;
       else oc = Prc * c4;
-      const double v = Hm[(size_t)(o + r) * norb + o + c] + oc + J;
+      const double h = Hm[(size_t)(o + r) * norb + o + c], v = h + oc + J;
       Fm[(size_t)(o + r) * norb + o + c] = v;
       Fm[(size_t)(o + c) * norb + o + r] = v;
+      ep = (r == c ? 1.0 : 2.0) * Prc * (h + v);  // both triangles of the block
+    }
+    if (epart) {  // sum P (H + F) over the block: lanes 0-9 hold the packed elements
+#pragma unroll
+      for (int o2 = 8; o2 > 0; o2 >>= 1) ep += __shfl_down_sync(0xffffffffu, ep, o2);
+      if (lane == 0) epart[a] = ep;
     }
   } else {
     const int h = la - nh, o = 3 * nh + la;
@@ -137,8 +144,10 @@ __device__ __forceinline__ void fock_diag(const seqm_batch &b, int a, int lane, 
     }
     f = warp_allsum(f);
     if (lane == 0) {
-      const double Pss = Pm[(size_t)o * norb + o];
-      Fm[(size_t)o * norb + o] = Hm[(size_t)o * norb + o] + 0.5 * Pss * gss + f;
+      const double Pss = Pm[(size_t)o * norb + o], h = Hm[(size_t)o * norb + o];
+      const double v = h + 0.5 * Pss * gss + f;
+      Fm[(size_t)o * norb + o] = v;
+      if (epart) epart[a] = Pss * (h + v);
     }
   }
 }
@@ -146,14 +155,14 @@ __device__ __forceinline__ void fock_diag(const seqm_batch &b, int a, int lane, 
 __global__ void __launch_bounds__(128) k_fock(seqm_batch b, const double *__restrict__ P, const double *__restrict__ H,
                                               const double *__restrict__ w_xx, const double *__restrict__ w_xh,
                                               const double *__restrict__ w_hh, double *__restrict__ F,
-                                              const uint8_t *__restrict__ active) {
+                                              const uint8_t *__restrict__ active, double *__restrict__ epart) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long ndiag = 32LL * b.natoms;  // one warp per atom; warps never straddle the two roles
   const int npairs = b.nxx + b.nxh + b.nhh;
   if (t < ndiag) {
     const int a = (int)(t >> 5);
     if (!is_active(active, b.atom_mol[a])) return;
-    fock_diag(b, a, (int)(t & 31), P, H, w_xx, w_xh, w_hh, F);
+    fock_diag(b, a, (int)(t & 31), P, H, w_xx, w_xh, w_hh, F, epart);
     return;
   }
   if (t - ndiag >= npairs) return;
@@ -167,6 +176,7 @@ __global__ void __launch_bounds__(128) k_fock(seqm_batch b, const double *__rest
   const size_t mo = b.mol_mat_off[m];
   const double *Pm = P + mo, *Hm = H + mo;
   double *Fm = F + mo;
+  double ep = 0.0;  // P (H + F) over the block and its transpose
   if (p < b.nxx) {
     // K(mu, nu) = sum_{l,s} (mu l | nu s) P_AB(l, s), F_AB = H_AB - K / 2 (the halving is exact)
     const double2 *w2 = reinterpret_cast<const double2 *>(w_xx + (size_t)100 * p);
@@ -191,9 +201,10 @@ __global__ void __launch_bounds__(128) k_fock(seqm_batch b, const double *__rest
         for (int l = 0; l < 4; ++l)
 #pragma unroll
           for (int s = 0; s < 4; ++s) k = fma(w[kind(mu, l) * 10 + kind(nu, s)], Pp[l][s], k);
-        const double v = fma(-0.5, k, Hm[(size_t)(oi + mu) * norb + oj + nu]);
+        const double h = Hm[(size_t)(oi + mu) * norb + oj + nu], v = fma(-0.5, k, h);
         Fm[(size_t)(oi + mu) * norb + oj + nu] = v;
         Fm[(size_t)(oj + nu) * norb + oi + mu] = v;
+        ep = fma(Pp[mu][nu], h + v, ep);
       }
   } else if (p < b.nxx + b.nxh) {
     const double *w = w_xh + (size_t)10 * (p - b.nxx);
@@ -205,15 +216,19 @@ __global__ void __launch_bounds__(128) k_fock(seqm_batch b, const double *__rest
       double k = 0.0;
 #pragma unroll
       for (int l = 0; l < 4; ++l) k = fma(__ldg(w + kind(mu, l)), Pp[l], k);
-      const double v = fma(-0.5, k, Hm[(size_t)(oi + mu) * norb + oj]);
+      const double h = Hm[(size_t)(oi + mu) * norb + oj], v = fma(-0.5, k, h);
       Fm[(size_t)(oi + mu) * norb + oj] = v;
       Fm[(size_t)oj * norb + oi + mu] = v;
+      ep = fma(Pp[mu], h + v, ep);
     }
   } else {
-    double v = Hm[(size_t)oi * norb + oj] + w_hh[p - b.nxx - b.nxh] * (-0.5 * Pm[(size_t)oi * norb + oj]);
+    const double h = Hm[(size_t)oi * norb + oj], pij = Pm[(size_t)oi * norb + oj];
+    const double v = h + w_hh[p - b.nxx - b.nxh] * (-0.5 * pij);
     Fm[(size_t)oi * norb + oj] = v;
     Fm[(size_t)oj * norb + oi] = v;
+    ep = pij * (h + v);
   }
+  if (epart) epart[(size_t)b.natoms + p] = 2.0 * ep;
 }
 
 // ---------------------------------------------------------------- block reductions
@@ -667,6 +682,452 @@ __global__ void __launch_bounds__(32 * MIX_WARPS) k_mix_warp(seqm_batch b, doubl
   }
 }
 
+// ----------------------------------------------------------- fused mixing (seqm_scf_step)
+// The mixing of seqm_scf_step takes the change of P itself instead of leaving Pold for a separate
+// energy pass.  Every update is P + c (Pnew - P) (linear: c = 1 - alpha; the adaptive
+// extrapolation: c = 1 + FAC; otherwise P = Pnew), so with d = Pnew - P formed once the new element
+// costs at most one FMA, and sum d^2 (times c^2) and max |d| (times |c|) give the ||dP|| terms of
+// the convergence test.  Adaptive mixing first runs k_mix_diag (warp per molecule up to
+// MIX_WARP_MAX basis functions, a CTA above): FAC from the diagonal history, the damped, clamped
+// and renormalised diagonal written to P with old2 and the iteration count, and the diagonal's
+// change and c left in the molecule's mixer slots; the streams then touch only the off-diagonal
+// elements and carry no serial tail.  Linear mixing streams every element.  Per molecule the
+// arithmetic depends only on its size.
+constexpr int MIX_SMALL = 64;
+// per-molecule mixer slots of the scratch: [0] sum d^2, [1] max |d| (diagonal, then all), [2] c
+constexpr int MIX_SLOTS = 4;
+// FP64 -> FP32 by truncation with integer instructions only (GB300 converts on its FP64 pipe):
+// sign, rebiased exponent, top 23 mantissa bits; |d| < 2^-126 gives 0.  For |d| <= 2 (density
+// elements and their changes) the exponent never overflows.
+__device__ __forceinline__ float f32_trunc(double d) {
+  const int hi = __double2hiint(d);
+  const unsigned lo = (unsigned)__double2loint(d);
+  const int e = ((hi >> 20) & 0x7ff) - 1023 + 127;
+  const unsigned bits = ((unsigned)hi & 0x80000000u) | ((unsigned)e << 23) | (((unsigned)hi & 0xfffffu) << 3) | (lo >> 29);
+  return e > 0 ? __uint_as_float(bits) : 0.0f;
+}
+
+// Diagonal step of adaptive mixing (scf_loop.py:360-420), one warp per molecule of up to
+// MIX_WARP_MAX basis functions (eight per CTA; each lane holds at most five diagonal elements).
+__global__ void __launch_bounds__(32 * MIX_WARPS) k_mix_diag_warp(seqm_batch b, double *__restrict__ P,
+                                                                  const double *__restrict__ Pnew,
+                                                                  double *__restrict__ old2,
+                                                                  const int64_t *__restrict__ row_off,
+                                                                  int32_t *__restrict__ kit, double occ,
+                                                                  const uint8_t *__restrict__ active,
+                                                                  double *__restrict__ ms) {
+  const int w = blockIdx.x * MIX_WARPS + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (w >= b.nmol) return;
+  const int m = warp_molecule(b, w);
+  if (!is_active(active, m)) return;  // uniform over the warp
+  const int n = b.mol_norb[m];
+  if (n > MIX_WARP_MAX) return;
+  const int k = kit[m] + 1;
+  double *Pm = P + b.mol_mat_off[m];
+  const double *Pn = Pnew + b.mol_mat_off[m];
+  double *o2 = old2 + row_off[m];
+  // slots a lane holds: the loops stop at the molecule's own count (uniform over the warp), as
+  // every FP64 instruction costs the FP64 pipe the same however few of its lanes work
+  const int nt = (n + 31) >> 5;
+  double dp[MIX_DIAG] = {}, dc[MIX_DIAG] = {}, num = 0.0, den = 0.0;
+#pragma unroll
+  for (int t = 0; t < MIX_DIAG; ++t) {
+    if (t >= nt) break;
+    const int i = lane + 32 * t;
+    dp[t] = i < n ? Pm[(size_t)i * n + i] : 0.0;
+    dc[t] = i < n ? Pn[(size_t)i * n + i] : 0.0;
+    const double o2v = i < n ? o2[i] : 0.0;
+    const double d1 = dc[t] - dp[t], d2 = dc[t] - 2.0 * dp[t] + o2v;
+    num = fma(d1, d1, num);
+    den = fma(d2, d2, den);
+  }
+  double fac = 0.0;
+  if (k % 3 == 0) {
+    num = warp_allsum(num);
+    den = warp_allsum(den);
+    fac = (den > 0.0 && num < 100.0 * den) ? sqrt(num / den) : 0.0;
+  }
+  const double damp = k > 4 ? 0.05 : 1.0e10;
+  double di[MIX_DIAG] = {}, s0 = 0.0;
+#pragma unroll
+  for (int t = 0; t < MIX_DIAG; ++t) {
+    if (t >= nt) break;
+    const int i = lane + 32 * t;
+    const double delta = dc[t] - dp[t];
+    const double v = fabs(delta) > damp ? dp[t] + (delta > 0.0 ? 1.0 : (delta < 0.0 ? -1.0 : 0.0)) * damp
+                                        : dc[t] + fac * delta;
+    di[t] = i < n ? fmin(fmax(v, 0.0), occ) : 0.0;
+    s0 += i < n ? dc[t] : 0.0;
+  }
+  double sum0 = warp_allsum(s0);
+  for (int pass = 0; pass < 20; ++pass) {
+    double s2 = 0.0;
+#pragma unroll
+    for (int t = 0; t < MIX_DIAG; ++t) {
+      if (t >= nt) break;
+      s2 += di[t];
+    }
+    const double sum2 = warp_allsum(s2);
+    const double sum3 = sum2 > 1.0e-3 ? sum0 / sum2 : 0.0;
+    if (!(sum2 > 1.0e-3) || fabs(sum3 - 1.0) <= 1.0e-5) break;
+    double nfull = 0.0;
+#pragma unroll
+    for (int t = 0; t < MIX_DIAG; ++t) {
+      if (t >= nt) break;
+      const int i = lane + 32 * t;
+      const double sc = fmax(di[t] * sum3, 0.0);
+      const bool full = sc > occ;
+      di[t] = i < n ? (full ? occ : sc) : 0.0;
+      nfull += (i < n && full) ? 1.0 : 0.0;
+    }
+    nfull = warp_allsum(nfull);
+    sum0 = sum0 - nfull * occ;
+  }
+  double dfro = 0.0, dmx = 0.0;
+#pragma unroll
+  for (int t = 0; t < MIX_DIAG; ++t) {
+    if (t >= nt) break;
+    const int i = lane + 32 * t;
+    if (i < n) {
+      Pm[(size_t)i * n + i] = di[t];
+      o2[i] = dp[t];
+      const double d = di[t] - dp[t];
+      dfro = fma(d, d, dfro);
+      dmx = fmax(dmx, fabs(d));
+    }
+  }
+  dfro = warp_allsum(dfro);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) dmx = fmax(dmx, __shfl_xor_sync(0xffffffffu, dmx, o));
+  if (lane == 0) {
+    kit[m] = k;
+    double *slot = ms + MIX_SLOTS * m;
+    slot[0] = dfro;
+    slot[1] = dmx;
+    slot[2] = k % 3 == 0 ? 1.0 + fac : 1.0;
+  }
+}
+
+// The same for molecules above MIX_WARP_MAX basis functions: one CTA per molecule, the new
+// diagonal kept in the molecule's scratch (L2-resident) through the renormalisation passes.
+constexpr int NT_MD = 512;
+// slice partials and scratch of molecule m in the 4 sum(norb) region (4 n doubles per molecule):
+// mixer slices (2 each) at [0, 2n), the new diagonal at [2n, 3n), energy slices at [3n, 4n)
+__device__ __forceinline__ double *mol_scratch(double *q, const int64_t *row_off, int m) { return q + 4 * row_off[m]; }
+
+__global__ void __launch_bounds__(NT_MD) k_mix_diag_cta(seqm_batch b, double *__restrict__ P,
+                                                        const double *__restrict__ Pnew, double *__restrict__ old2,
+                                                        const int64_t *__restrict__ row_off,
+                                                        int32_t *__restrict__ kit, double occ,
+                                                        const uint8_t *__restrict__ active, double *__restrict__ ms,
+                                                        double *__restrict__ q) {
+  __shared__ double red[NT_MD / 32];
+  const int m = blockIdx.x;
+  if (!is_active(active, m)) return;
+  const int n = b.mol_norb[m];
+  if (n <= MIX_WARP_MAX) return;
+  const int k = kit[m] + 1;
+  double *Pm = P + b.mol_mat_off[m];
+  const double *Pn = Pnew + b.mol_mat_off[m];
+  double *o2 = old2 + row_off[m];
+  double *di = mol_scratch(q, row_off, m) + 2 * (int64_t)n;
+  double fac = 0.0;
+  if (k % 3 == 0) {
+    double num = 0.0, den = 0.0;
+    for (int i = threadIdx.x; i < n; i += NT_MD) {
+      const double dp = Pm[(size_t)i * n + i], dc = Pn[(size_t)i * n + i];
+      const double d1 = dc - dp, d2 = dc - 2.0 * dp + o2[i];
+      num += d1 * d1;
+      den += d2 * d2;
+    }
+    num = block_sum<NT_MD>(num, red);
+    den = block_sum<NT_MD>(den, red);
+    fac = (den > 0.0 && num < 100.0 * den) ? sqrt(num / den) : 0.0;
+  }
+  const double damp = k > 4 ? 0.05 : 1.0e10;
+  double s0 = 0.0;
+  for (int i = threadIdx.x; i < n; i += NT_MD) {
+    const double dcv = Pn[(size_t)i * n + i], dpv = Pm[(size_t)i * n + i];
+    const double delta = dcv - dpv;
+    const double v =
+        fabs(delta) > damp ? dpv + (delta > 0.0 ? 1.0 : (delta < 0.0 ? -1.0 : 0.0)) * damp : dcv + fac * delta;
+    di[i] = fmin(fmax(v, 0.0), occ);
+    s0 += dcv;
+  }
+  double sum0 = block_sum<NT_MD>(s0, red);
+  for (int pass = 0; pass < 20; ++pass) {
+    double s2 = 0.0;
+    for (int i = threadIdx.x; i < n; i += NT_MD) s2 += di[i];
+    const double sum2 = block_sum<NT_MD>(s2, red);
+    const double sum3 = sum2 > 1.0e-3 ? sum0 / sum2 : 0.0;
+    if (!(sum2 > 1.0e-3) || fabs(sum3 - 1.0) <= 1.0e-5) break;
+    double nfull = 0.0;
+    for (int i = threadIdx.x; i < n; i += NT_MD) {
+      const double sc = fmax(di[i] * sum3, 0.0);
+      const bool full = sc > occ;
+      di[i] = full ? occ : sc;
+      nfull += full ? 1.0 : 0.0;
+    }
+    nfull = block_sum<NT_MD>(nfull, red);
+    sum0 = sum0 - nfull * occ;
+  }
+  double dfro = 0.0, dmx = 0.0;
+  for (int i = threadIdx.x; i < n; i += NT_MD) {
+    const double dpv = Pm[(size_t)i * n + i], d = di[i] - dpv;
+    Pm[(size_t)i * n + i] = di[i];
+    o2[i] = dpv;
+    dfro += d * d;
+    dmx = fmax(dmx, fabs(d));
+  }
+  dfro = block_sum<NT_MD>(dfro, red);
+  dmx = block_max<NT_MD>(dmx, red);
+  if (threadIdx.x == 0) {
+    kit[m] = k;
+    double *slot = ms + MIX_SLOTS * m;
+    slot[0] = dfro;
+    slot[1] = dmx;
+    slot[2] = k % 3 == 0 ? 1.0 + fac : 1.0;
+  }
+}
+
+// One thread's part of the fused stream: elements i0, i0 + STRIDE, ... below `end` (U at a time,
+// loads first) of an n x n matrix starting at element 0.  COPY: P = Pnew, else P + c d.  The
+// statistics of d run on the FP32 pipe from the integer-truncated f = fl32(d) rounded toward zero:
+// sum f^2 in FP32 (non-negative terms: relative error at most the thread's term count times 2^-24)
+// and max |f| (at most 2^-23 below max |d|), so an element costs one FP64 operation (d) when
+// copying and two otherwise.  Measured on GB300 over a 3 GB stream: 6.6 TB/s when copying and
+// 5.8 TB/s otherwise, where FP64 statistics or a 64-bit integer max took it to 3.6 TB/s.
+// SKIP_DIAG (adaptive mixing): the diagonal, written by k_mix_diag, is skipped; the thread's
+// (row, column) advance by the stride with integer adds only.
+template <bool COPY, bool SKIP_DIAG, int U, int STRIDE, typename Idx>
+__device__ __forceinline__ void fused_stream(double *__restrict__ Pm, const double *__restrict__ Pn, Idx i0, Idx end,
+                                             uint32_t n, double c, float &fro, float &mx) {
+  uint32_t row = 0, col = 0;
+  constexpr uint32_t S = (uint32_t)STRIDE;
+  const uint32_t drow = S / n, dcol = S % n;
+  if (SKIP_DIAG) {
+    row = (uint32_t)(i0 / n);
+    col = (uint32_t)(i0 % n);
+  }
+  for (Idx i = i0; i < end; i += (Idx)U * STRIDE) {
+    double *p = Pm + i;
+    const double *q = Pn + i;
+    const Idx rem = end - i;
+    double pv[U], pn[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      pv[u] = (Idx)(u * STRIDE) < rem ? p[u * STRIDE] : 0.0;
+      pn[u] = (Idx)(u * STRIDE) < rem ? q[u * STRIDE] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const bool diag = SKIP_DIAG && row == col;
+      if (SKIP_DIAG) {
+        col += dcol;
+        row += drow;
+        if (col >= n) {
+          col -= n;
+          ++row;
+        }
+      }
+      if ((Idx)(u * STRIDE) < rem && !diag) {
+        const double d = pn[u] - pv[u];
+        p[u * STRIDE] = COPY ? pn[u] : fma(c, d, pv[u]);
+        const float f = f32_trunc(d);
+        fro = fmaf(f, f, fro);
+        mx = fmaxf(mx, fabsf(f));
+      }
+    }
+  }
+}
+// the four forms of fused_stream, chosen by uniform flags
+template <int U, int STRIDE, typename Idx>
+__device__ __forceinline__ void fused_stream_any(bool copy, bool skip_diag, double *__restrict__ Pm,
+                                                 const double *__restrict__ Pn, Idx i0, Idx end, uint32_t n, double c,
+                                                 float &fro, float &mx) {
+  if (copy) {
+    if (skip_diag) fused_stream<true, true, U, STRIDE>(Pm, Pn, i0, end, n, c, fro, mx);
+    else fused_stream<true, false, U, STRIDE>(Pm, Pn, i0, end, n, c, fro, mx);
+  } else {
+    if (skip_diag) fused_stream<false, true, U, STRIDE>(Pm, Pn, i0, end, n, c, fro, mx);
+    else fused_stream<false, false, U, STRIDE>(Pm, Pn, i0, end, n, c, fro, mx);
+  }
+}
+// the mixer's ||dP|| terms of molecule m from the stream's sums and (adaptive) the diagonal's
+__device__ __forceinline__ void mix_finish(double *__restrict__ ms, int m, int linear, double c, bool copy,
+                                           double fro, double mx) {
+  double *slot = ms + MIX_SLOTS * m;
+  const double cc = copy ? 1.0 : c;
+  const double dfro = linear ? 0.0 : slot[0], dmx = linear ? 0.0 : slot[1];
+  slot[0] = fma(cc * cc, fro, dfro);
+  slot[1] = fmax(fabs(cc) * mx, dmx);
+}
+
+// The stream for molecules of up to MIX_WARP_MAX basis functions: G warps per molecule (G = 1:
+// eight molecules per CTA, n <= MIX_SMALL; G = 8: one molecule per CTA, larger n, so that its
+// stream keeps eight warps of loads in flight).
+template <int G>
+__global__ void __launch_bounds__(32 * MIX_WARPS) k_mix_fused(seqm_batch b, double *__restrict__ P,
+                                                              const double *__restrict__ Pnew,
+                                                              int32_t *__restrict__ kit, int linear, double alpha,
+                                                              const uint8_t *__restrict__ active,
+                                                              double *__restrict__ ms) {
+  static_assert(G == 1 || G == MIX_WARPS, "a molecule takes one warp or the whole CTA");
+  __shared__ double sfro[MIX_WARPS], smx[MIX_WARPS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w = blockIdx.x * (MIX_WARPS / G) + warp / G;  // the molecule's slot in the scheduling order
+  if (w >= b.nmol) return;
+  const int m = warp_molecule(b, w);
+  if (!is_active(active, m)) return;  // uniform over the group
+  const int n = b.mol_norb[m];
+  if (G == 1 ? n > MIX_SMALL : (n <= MIX_SMALL || n > MIX_WARP_MAX)) return;
+  const double c = linear ? 1.0 - alpha : ms[MIX_SLOTS * m + 2];
+  const bool copy = !linear && c == 1.0;
+  const size_t mo = b.mol_mat_off[m];
+  float fro32 = 0.0f, mx32 = 0.0f;
+  fused_stream_any<MIX_WUNROLL, 32 * G>(copy, !linear, P + mo, Pnew + mo, (warp % G) * 32 + lane, n * n,
+                                        (uint32_t)n, c, fro32, mx32);
+  double fro = warp_allsum((double)fro32), mx = (double)mx32;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (G > 1) {
+    if (lane == 0) {
+      sfro[warp] = fro;
+      smx[warp] = mx;
+    }
+    __syncthreads();  // every warp has read kit[m] and added its sums
+    if (warp != 0) return;
+    fro = 0.0;
+    mx = 0.0;
+    for (int g = 0; g < G; ++g) {
+      fro += sfro[g];
+      mx = fmax(mx, smx[g]);
+    }
+  }
+  if (lane == 0) {
+    mix_finish(ms, m, linear, c, copy, fro, mx);
+    if (linear) kit[m] += 1;  // (adaptive: k_mix_diag counted the iteration)
+  }
+}
+
+// The stream of a molecule above MIX_WARP_MAX basis functions over the whole GPU: CTA (m, s)
+// streams slice s (MG_SLICE elements), the slice sums go to the molecule's scratch, and its last
+// CTA to finish (a counter) adds them in slice order.
+constexpr int NT_MG = 512, MG_UNROLL = 4;
+constexpr size_t MG_SLICE = (size_t)1 << 17;
+__global__ void __launch_bounds__(NT_MG) k_mix_grid(seqm_batch b, double *__restrict__ P,
+                                                     const double *__restrict__ Pnew,
+                                                     const int64_t *__restrict__ row_off, int32_t *__restrict__ kit,
+                                                     int linear, double alpha, const uint8_t *__restrict__ active,
+                                                     double *__restrict__ ms, double *__restrict__ q,
+                                                     int *__restrict__ counter) {
+  __shared__ double red[NT_MG / 32];
+  __shared__ int last;
+  const int m = blockIdx.x;
+  if (!is_active(active, m)) return;
+  const int n = b.mol_norb[m];
+  if (n <= MIX_WARP_MAX) return;
+  const size_t nn = (size_t)n * n;
+  const int ns = (int)((nn + MG_SLICE - 1) / MG_SLICE), s = blockIdx.y;
+  if (s >= ns) return;
+  const double c = linear ? 1.0 - alpha : ms[MIX_SLOTS * m + 2];
+  const bool copy = !linear && c == 1.0;
+  const size_t mo = b.mol_mat_off[m];
+  double *qm = mol_scratch(q, row_off, m);
+  const size_t e0 = (size_t)s * MG_SLICE, e1 = e0 + MG_SLICE < nn ? e0 + MG_SLICE : nn;
+  float fro32 = 0.0f, mx32 = 0.0f;
+  fused_stream_any<MG_UNROLL, NT_MG>(copy, !linear, P + mo, Pnew + mo, e0 + threadIdx.x, e1, (uint32_t)n, c, fro32,
+                                     mx32);
+  const double fro = block_sum<NT_MG>((double)fro32, red);
+  const double mx = block_max<NT_MG>((double)mx32, red);
+  if (threadIdx.x == 0) {
+    qm[2 * s] = fro;
+    qm[2 * s + 1] = mx;
+    __threadfence();
+    last = atomicAdd(counter + m, 1) == ns - 1;
+  }
+  __syncthreads();
+  if (!last || threadIdx.x >= 32) return;
+  __threadfence();
+  // the slices in order: lane l sums slices l, l + 32, ..., then a butterfly
+  double f = 0.0, x = 0.0;
+  for (int t = threadIdx.x; t < ns; t += 32) {
+    f += __ldcg(qm + 2 * t);
+    x = fmax(x, __ldcg(qm + 2 * t + 1));
+  }
+  f = warp_allsum(f);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+  if (threadIdx.x == 0) {
+    mix_finish(ms, m, linear, c, copy, f, x);
+    if (linear) kit[m] += 1;
+  }
+}
+
+// Energy and convergence test of seqm_scf_step from the Fock build's partial sums of P (H + F)
+// (one per atom's diagonal block, one per pair's block with its transpose) and the mixer's
+// ||dP|| terms.  A molecule's partials are four contiguous runs (its atoms, XX, XH, HH pairs),
+// cut into slices of EF_SLICE entries; CTA (m, s), one warp, sums slice s, and a molecule with more
+// than one slice is finished by its last CTA (a counter), which adds the slice sums in slice order.
+// One warp per slice: GB300 issues an FP64 warp instruction at the same cost however few of its
+// lanes work, so a wide tree reduction per small molecule would cost more than the sums.
+constexpr int EF_THREADS = 32, EF_SLICE = 8192;
+__device__ __forceinline__ int64_t energy_partials(const seqm_batch &b, int m, int64_t base[4], int64_t len[4]) {
+  const int a0 = b.mol_atom_off[m];
+  base[0] = a0;
+  len[0] = b.mol_atom_off[m + 1] - a0;
+  base[1] = (int64_t)b.natoms + b.mol_xx_off[m];
+  len[1] = b.mol_xx_off[m + 1] - b.mol_xx_off[m];
+  base[2] = (int64_t)b.natoms + b.nxx + b.mol_xh_off[m];
+  len[2] = b.mol_xh_off[m + 1] - b.mol_xh_off[m];
+  base[3] = (int64_t)b.natoms + b.nxx + b.nxh + b.mol_hh_off[m];
+  len[3] = b.mol_hh_off[m + 1] - b.mol_hh_off[m];
+  return len[0] + len[1] + len[2] + len[3];
+}
+
+__global__ void __launch_bounds__(EF_THREADS) k_energy_finish(
+    seqm_batch b, const double *__restrict__ epart, const double *__restrict__ ms, double *__restrict__ q,
+    int *__restrict__ counter, const int64_t *__restrict__ row_off, double *Eelec, double *Eout, double *err,
+    double *dm_err, double *dm_el, uint8_t *active, double eps, int *__restrict__ nactive,
+    const int32_t *__restrict__ kit) {
+  const int m = blockIdx.x, lane = threadIdx.x;
+  if (!is_active(active, m)) return;
+  int64_t base[4], len[4];
+  const int64_t L = energy_partials(b, m, base, len);
+  const int ns = (int)((L + EF_SLICE - 1) / EF_SLICE), s = blockIdx.y;
+  if (s >= ns) return;
+  const int64_t v0 = (int64_t)s * EF_SLICE, v1 = v0 + EF_SLICE < L ? v0 + EF_SLICE : L;
+  double e = 0.0;
+  int64_t off = 0;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int64_t lo = v0 > off ? v0 : off, hi = v1 < off + len[r] ? v1 : off + len[r];
+    for (int64_t v = lo + lane; v < hi; v += 32) e += epart[base[r] + (v - off)];
+    off += len[r];
+  }
+  e = warp_allsum(e);
+  if (ns > 1) {
+    double *qe = mol_scratch(q, row_off, m) + 3 * (int64_t)b.mol_norb[m];
+    int last = 0;
+    if (lane == 0) {
+      qe[s] = e;
+      __threadfence();
+      last = atomicAdd(counter + m, 1) == ns - 1;
+    }
+    if (!__shfl_sync(0xffffffffu, last, 0)) return;
+    __threadfence();
+    e = 0.0;
+    for (int t = lane; t < ns; t += 32) e += __ldcg(qe + t);
+    e = warp_allsum(e);
+  }
+  if (lane == 0) {
+    e *= 0.5;
+    Eout[m] = e;
+    finish_error(b, m, e, ms[MIX_SLOTS * m], ms[MIX_SLOTS * m + 1], Eelec, err, dm_err, dm_el, active, eps, nullptr,
+                 nactive, kit);
+  }
+}
+
 // ----------------------------------------------------------- initial density
 __global__ void k_initial_density(seqm_batch b, double *__restrict__ P) {
   int a = blockIdx.x * blockDim.x + threadIdx.x;
@@ -736,7 +1197,8 @@ extern "C" int seqm_fock(const seqm_batch *bp, const double *P, const double *H,
   seqm_batch b = *bp;
   long long nt = 32LL * b.natoms + b.nxx + b.nxh + b.nhh;
   if (nt == 0) return SEQM_OK;
-  k_fock<<<(unsigned)((nt + 127) / 128), 128, 0, (cudaStream_t)stream>>>(b, P, H, w_xx, w_xh, w_hh, F, active);
+  k_fock<<<(unsigned)((nt + 127) / 128), 128, 0, (cudaStream_t)stream>>>(b, P, H, w_xx, w_xh, w_hh, F, active,
+                                                                          nullptr);
   return launch_check();
 }
 
@@ -750,12 +1212,58 @@ extern "C" int seqm_energy_error(const seqm_batch *bp, const double *P, const do
                              dm_err, dm_el, active, eps, diis_err);
 }
 
+// seqm_scf_step with a scratch buffer and mixing >= 0: mixing with the ||dP|| terms (adaptive: the
+// diagonal step first), Fock build with the energy partials, energy and test from those (no Pold,
+// no separate energy pass).  Scratch (doubles): mixer slots [MIX_SLOTS nmol], counters [2 nmol
+// int32], energy partials [natoms + npairs], per-molecule slices [4 sum(norb)].
+static int scf_step_fused(const seqm_batch &b, const seqm_scf_state *st, cudaStream_t s) {
+  if (!st->mol_row_off || !st->iters || (st->mixing == 1 && !st->old2)) return SEQM_E_ARG;
+  if (b.max_norb > 12800) return SEQM_E_TOO_LARGE;  // slices of a molecule fit its 4 norb scratch
+  const size_t nm = (size_t)b.nmol, npairs = (size_t)b.nxx + b.nxh + b.nhh;
+  double *ms = st->scratch;
+  int *counter = reinterpret_cast<int *>(ms + MIX_SLOTS * nm);  // mixer [nmol], energy [nmol]
+  double *epart = ms + (MIX_SLOTS + 1) * nm;
+  double *q = epart + (size_t)b.natoms + npairs;
+  const int linear = st->mixing == 0;
+  const bool large = b.max_norb > MIX_WARP_MAX;
+  const unsigned wgrid = (unsigned)((b.nmol + MIX_WARPS - 1) / MIX_WARPS);
+  if (cudaMemsetAsync(counter, 0, 2 * nm * sizeof(int), s) != cudaSuccess) return SEQM_E_CUDA;
+  if (!linear) {
+    k_mix_diag_warp<<<wgrid, 32 * MIX_WARPS, 0, s>>>(b, st->P, st->Pnew, st->old2, st->mol_row_off, st->iters,
+                                                     st->occupation, st->active, ms);
+    if (large)
+      k_mix_diag_cta<<<b.nmol, NT_MD, 0, s>>>(b, st->P, st->Pnew, st->old2, st->mol_row_off, st->iters,
+                                              st->occupation, st->active, ms, q);
+  }
+  k_mix_fused<1><<<wgrid, 32 * MIX_WARPS, 0, s>>>(b, st->P, st->Pnew, st->iters, linear, st->alpha, st->active, ms);
+  k_mix_fused<MIX_WARPS><<<b.nmol, 32 * MIX_WARPS, 0, s>>>(b, st->P, st->Pnew, st->iters, linear, st->alpha,
+                                                           st->active, ms);
+  if (large) {
+    const size_t nn = (size_t)b.max_norb * b.max_norb;
+    k_mix_grid<<<dim3((unsigned)b.nmol, (unsigned)((nn + MG_SLICE - 1) / MG_SLICE)), NT_MG, 0, s>>>(
+        b, st->P, st->Pnew, st->mol_row_off, st->iters, linear, st->alpha, st->active, ms, q, counter);
+  }
+  const long long nt = 32LL * b.natoms + (long long)npairs;
+  if (nt > 0)
+    k_fock<<<(unsigned)((nt + 127) / 128), 128, 0, s>>>(b, st->P, st->H, st->w_xx, st->w_xh, st->w_hh, st->F,
+                                                        st->active, epart);
+  if (st->nactive && cudaMemsetAsync(st->nactive, 0, sizeof(int32_t), s) != cudaSuccess) return SEQM_E_CUDA;
+  // slices of the largest molecule's partials: at most its atoms and their pairs, at most the batch's
+  const long long mx = b.max_norb, lmax_mol = mx + mx * (mx - 1) / 2, lmax_all = (long long)b.natoms + (long long)npairs;
+  const long long lmax = lmax_mol < lmax_all ? lmax_mol : lmax_all;
+  k_energy_finish<<<dim3((unsigned)b.nmol, (unsigned)((lmax + EF_SLICE - 1) / EF_SLICE)), EF_THREADS, 0, s>>>(
+      b, epart, ms, q, counter + nm, st->mol_row_off, st->Eelec, st->Eout, st->err, st->dm_err, st->dm_el,
+      st->active, st->eps, st->nactive, st->iters);
+  return launch_check();
+}
+
 extern "C" int seqm_scf_step(const seqm_batch *bp, const seqm_scf_state *st, void *stream) {
   if (!bp || !st || !st->P || !st->Pnew || !st->Pold || !st->H || !st->F || !st->active) return SEQM_E_ARG;
   if (st->mixing < -1 || st->mixing > 1) return SEQM_E_ARG;
   const seqm_batch &b = *bp;
   if (b.nmol == 0) return SEQM_OK;
   cudaStream_t s = (cudaStream_t)stream;
+  if (st->mixing >= 0 && st->scratch) return scf_step_fused(b, st, s);
   int rc = SEQM_OK;
   if (st->mixing >= 0) {
     rc = seqm_mix(bp, st->P, st->Pnew, st->Pold, st->old2, st->mol_row_off, st->iters, st->mixing == 0, st->alpha,

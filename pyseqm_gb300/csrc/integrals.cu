@@ -216,18 +216,38 @@ __global__ void k_hcore_diag(seqm_batch b, const double *__restrict__ w_xx, cons
   }
 }
 
-// per-molecule sum of a per-pair quantity (core-core energies), warp per molecule
-__global__ void k_pair_sum(seqm_batch b, const double *__restrict__ v, double *__restrict__ out) {
-  int m = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-  int lane = threadIdx.x & 31;
-  if (m >= b.nmol) return;
-  double s = 0.0;
-  for (int p = b.mol_xx_off[m] + lane; p < b.mol_xx_off[m + 1]; p += 32) s += v[p];
-  for (int p = b.mol_xh_off[m] + lane; p < b.mol_xh_off[m + 1]; p += 32) s += v[b.nxx + p];
-  for (int p = b.mol_hh_off[m] + lane; p < b.mol_hh_off[m + 1]; p += 32) s += v[b.nxx + b.nxh + p];
+// per-molecule sum of a per-pair quantity (core-core energies), one CTA per molecule: a molecule
+// of thousands of atoms has millions of pairs, which one warp would stream at a small fraction of
+// the bandwidth; each thread keeps PS_UNROLL independent sums, added in a fixed order
+constexpr int PS_THREADS = 1024, PS_UNROLL = 4;
+__global__ void __launch_bounds__(PS_THREADS) k_pair_sum(seqm_batch b, const double *__restrict__ v,
+                                                         double *__restrict__ out) {
+  __shared__ double red[PS_THREADS / 32];
+  const int m = blockIdx.x;
+  const int64_t base[3] = {b.mol_xx_off[m], (int64_t)b.nxx + b.mol_xh_off[m],
+                           (int64_t)b.nxx + b.nxh + b.mol_hh_off[m]};
+  const int64_t len[3] = {b.mol_xx_off[m + 1] - b.mol_xx_off[m], b.mol_xh_off[m + 1] - b.mol_xh_off[m],
+                          b.mol_hh_off[m + 1] - b.mol_hh_off[m]};
+  double s[PS_UNROLL] = {};
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (lane == 0) out[m] = s;
+  for (int r = 0; r < 3; ++r)
+    for (int64_t p = threadIdx.x; p < len[r]; p += PS_UNROLL * PS_THREADS) {
+#pragma unroll
+      for (int u = 0; u < PS_UNROLL; ++u) {
+        const int64_t q = p + (int64_t)u * PS_THREADS;
+        if (q < len[r]) s[u] += v[base[r] + q];
+      }
+    }
+  double t = (s[0] + s[1]) + (s[2] + s[3]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0;
+    for (int w = 0; w < PS_THREADS / 32; ++w) a += red[w];
+    out[m] = a;
+  }
 }
 
 }  // namespace seqm
@@ -269,6 +289,6 @@ extern "C" int seqm_pair_sum(const seqm_batch *bp, const double *pair_val, doubl
   if (!bp) return SEQM_E_ARG;
   seqm_batch b = *bp;
   if (b.nmol <= 0) return SEQM_OK;
-  k_pair_sum<<<(b.nmol + 7) / 8, 256, 0, (cudaStream_t)stream>>>(b, pair_val, mol_sum);
+  k_pair_sum<<<b.nmol, PS_THREADS, 0, (cudaStream_t)stream>>>(b, pair_val, mol_sum);
   return launch_check();
 }

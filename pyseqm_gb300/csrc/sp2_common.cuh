@@ -25,12 +25,6 @@ constexpr int EW_THREADS = 256;
 constexpr int SP2_SYNC_EVERY = 4;
 constexpr int EW_CHUNK = EW_THREADS * 8;  // elements per CTA of an elementwise pass
 
-// row of element idx of an n x n matrix, and whether it lies on the diagonal: 32-bit division
-// (n^2 < 2^32 for every molecule a batch can hold), several times cheaper than a 64-bit one
-__device__ __forceinline__ uint32_t row_of(size_t idx, int n) { return (uint32_t)idx / (uint32_t)n; }
-__device__ __forceinline__ bool diagonal(size_t idx, int n) {
-  return (uint32_t)idx == row_of(idx, n) * (uint32_t)(n + 1);
-}
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -115,9 +109,10 @@ __global__ void __launch_bounds__(EW_THREADS) k_sp2_scale(seqm_batch b, const do
   if (base >= nn) return;
   const double h1 = s[S_H1], hN = s[S_HN], inv = 1.0 / (hN - h1);
   const size_t mo = b.mol_mat_off[m];
+  const DiagTest diagonal(n);  // n^2 < 2^32 for every molecule a batch holds
   double tr = 0.0, f2 = 0.0;
   for (size_t idx = base + threadIdx.x; idx < nn && idx < base + EW_CHUNK; idx += EW_THREADS) {
-    const bool d = diagonal(idx, n);
+    const bool d = diagonal((uint32_t)idx);
     // the FP64 form divides as SP2.py:36-43 does; the FP32 iterate takes the reciprocal
     const double a = (d ? hN : 0.0) - F[mo + idx];
     const T v = (T)(sizeof(T) == 8 ? a / (hN - h1) : a * inv);
@@ -154,12 +149,13 @@ __global__ void __launch_bounds__(EW_THREADS) k_sp2_step(seqm_batch b, T *__rest
   const double nocc = (double)b.mol_nocc[m], t1 = s[S_T1], t2 = s[S_T2];
   const bool sq = fabs(t2 - nocc) < fabs(2.0 * t1 - t2 - nocc);
   const size_t mo = b.mol_mat_off[m];
+  const DiagTest diagonal(n);
   double tr = 0.0, f2 = 0.0;
   for (size_t idx = base + threadIdx.x; idx < nn && idx < base + EW_CHUNK; idx += EW_THREADS) {
     const T x = X[mo + idx], y = X2[mo + idx];
     const T v = sq ? y : (T)2 * x - y;
     X[mo + idx] = v;
-    if (diagonal(idx, n)) tr += (double)v;
+    if (diagonal((uint32_t)idx)) tr += (double)v;
     f2 += (double)v * (double)v;
   }
   cta_accumulate2(tr, f2, s + S_ACC_T);
@@ -206,8 +202,9 @@ __global__ void __launch_bounds__(EW_THREADS) k_ew_sym(seqm_batch b, const T *__
   const size_t nn = (size_t)n * n, base = (size_t)blockIdx.x * EW_CHUNK;
   if (base >= nn) return;
   const size_t mo = b.mol_mat_off[m];
+  const FastDivU32 row((uint32_t)n);
   for (size_t idx = base + threadIdx.x; idx < nn && idx < base + EW_CHUNK; idx += EW_THREADS) {
-    const size_t i = row_of(idx, n), j = idx - i * n;
+    const size_t i = row.div((uint32_t)idx), j = idx - i * n;
     P[mo + idx] = c1 * (double)A[mo + idx] + c2 * (double)A[mo + j * n + i];
   }
 }
@@ -401,13 +398,15 @@ inline dim3 gemm64_grid(const seqm_batch &b) {
 // ------------------------------------------------------------- FP64-accurate X^2 in FP32 pairs
 // GB300 issues FP32 at 64x its FP64 rate, so the one FP64-accurate product of a McWeeny step
 // is formed from FP32 pairs (double-float arithmetic; Dekker 1971, Knuth's TwoSum): X = Xh + Xl
-// with Xh = fl32(X), Xl = fl32(X - Xh) (|Xl| <= 2^-24 |X|), and per term
-//   Xh_ik Xh_kj = p + e exactly (p = fl32(product), e = fma(Xh_ik, Xh_kj, -p)),
-//   cross = Xh_ik Xl_kj + Xl_ik Xh_kj in FP32 (a term of relative size 2^-24),
-// the p's summed exactly into (s, c) by TwoSum and e + cross + the TwoSum errors summed in FP32
-// into c.  Xl Xl (2^-48) is dropped.  For |X| <= 1 with X^2 ~ X (a density) the result's error
-// is ~K 2^-48 at most (about 1e-11 for K = 6000, ~1e-13 typically), FP64 level for the
-// McWeeny correction D = X^2 - X.  About 13 FP32 instructions per term instead of one FP64 FMA.
+// with Xh = fl32(X), Xl = fl32(X - Xh) (|Xl| <= 2^-24 |X|), and
+//   X^2 = Xh Xh + (M + M^T) + Xl Xl,   M = Xh Xl  (X symmetric, so Xl Xh = M^T),
+// where per term Xh_ik Xh_kj = p + e exactly (p = fl32(product), e = fma(Xh_ik, Xh_kj, -p)) and
+// the p's are summed exactly into (s, c) by TwoSum, e and the TwoSum errors summed in FP32 into c
+// (10 FP32 instructions per term).  M, a product of relative size 2^-24, is formed on the tensor
+// cores as a split product of Xh and 2^24 Xl (error 2^-22 of a 2^-24 term) and added at the end;
+// Xl Xl (2^-48) is dropped.  For |X| <= 1 with X^2 ~ X (a density) the result's error is ~K 2^-48
+// at most (about 1e-11 for K = 6000, ~1e-13 typically), FP64 level for the McWeeny correction
+// D = X^2 - X.
 __global__ void __launch_bounds__(EW_THREADS) k_split_pair(seqm_batch b, const double *__restrict__ X,
                                                            float *__restrict__ Xh, float *__restrict__ Xl,
                                                            const uint8_t *__restrict__ active) {
@@ -425,9 +424,9 @@ __global__ void __launch_bounds__(EW_THREADS) k_split_pair(seqm_batch b, const d
   }
 }
 
-// C = X X (symmetric X given as FP32 pairs, C in FP64): upper 64 x 64 output tiles with their
-// mirror, 256 threads of 4 x 4 outputs, 16-deep K slabs double-buffered in shared memory and
-// read along rows of X (symmetric), so every global load is coalesced.
+// C = Xh Xh (double-float) + M + M^T (symmetric Xh, M in FP32, C in FP64): upper 64 x 64 output
+// tiles with their mirror, 256 threads of 4 x 4 outputs, 16-deep K slabs double-buffered in shared
+// memory and read along rows of Xh (symmetric), so every global load is coalesced.
 constexpr int DF_T = 64, DF_K = 16, DF_THREADS = 256;
 __device__ __forceinline__ void two_sum_acc(float &s, float &c, float p) {
   const float t = s + p;
@@ -436,7 +435,7 @@ __device__ __forceinline__ void two_sum_acc(float &s, float &c, float p) {
   s = t;
 }
 __global__ void __launch_bounds__(DF_THREADS) k_sym_gemm_pair(seqm_batch b, const float *__restrict__ Xh,
-                                                              const float *__restrict__ Xl, double *__restrict__ Cm,
+                                                              const float *__restrict__ M, double *__restrict__ Cm,
                                                               const uint8_t *__restrict__ active) {
   const int m = blockIdx.z;
   if (active && !active[m]) return;
@@ -444,22 +443,19 @@ __global__ void __launch_bounds__(DF_THREADS) k_sym_gemm_pair(seqm_batch b, cons
   const int i0 = blockIdx.y * DF_T, j0 = blockIdx.x * DF_T;
   if (i0 >= n || j0 >= n || blockIdx.y > blockIdx.x) return;
   const size_t mo = b.mol_mat_off[m];
-  const float *H = Xh + mo, *L = Xl + mo;
-  __shared__ __align__(16) float Ah[2][DF_K][DF_T], Al[2][DF_K][DF_T], Bh[2][DF_K][DF_T], Bl[2][DF_K][DF_T];
+  const float *H = Xh + mo;
+  __shared__ __align__(16) float Ah[2][DF_K][DF_T], Bh[2][DF_K][DF_T];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   // slab loader: element e = threadIdx.x + 256 q (q = 0..3) of the 16 x 64 slab, row e / 64, col e % 64
-  float rah[4], ral[4], rbh[4], rbl[4];
+  float rah[4], rbh[4];
   auto load = [&](int k0) {
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int e = threadIdx.x + DF_THREADS * q, kk = e >> 6, c = e & 63;
       const bool kin = k0 + kk < n;
       const size_t ra = (size_t)(k0 + kk) * n + i0 + c, rb = (size_t)(k0 + kk) * n + j0 + c;
-      const bool ina = kin && i0 + c < n, inb = kin && j0 + c < n;
-      rah[q] = ina ? H[ra] : 0.0f;
-      ral[q] = ina ? L[ra] : 0.0f;
-      rbh[q] = inb ? H[rb] : 0.0f;
-      rbl[q] = inb ? L[rb] : 0.0f;
+      rah[q] = (kin && i0 + c < n) ? H[ra] : 0.0f;
+      rbh[q] = (kin && j0 + c < n) ? H[rb] : 0.0f;
     }
   };
   auto store = [&](int buf) {
@@ -467,9 +463,7 @@ __global__ void __launch_bounds__(DF_THREADS) k_sym_gemm_pair(seqm_batch b, cons
     for (int q = 0; q < 4; ++q) {
       const int e = threadIdx.x + DF_THREADS * q, kk = e >> 6, c = e & 63;
       Ah[buf][kk][c] = rah[q];
-      Al[buf][kk][c] = ral[q];
       Bh[buf][kk][c] = rbh[q];
-      Bl[buf][kk][c] = rbl[q];
     }
   };
   float s[4][4] = {}, c[4][4] = {};
@@ -483,20 +477,16 @@ __global__ void __launch_bounds__(DF_THREADS) k_sym_gemm_pair(seqm_batch b, cons
 #pragma unroll 4
     for (int kk = 0; kk < DF_K; ++kk) {
       const float4 ah = *reinterpret_cast<const float4 *>(&Ah[buf][kk][4 * ty]);
-      const float4 al = *reinterpret_cast<const float4 *>(&Al[buf][kk][4 * ty]);
       const float4 bh = *reinterpret_cast<const float4 *>(&Bh[buf][kk][4 * tx]);
-      const float4 bl = *reinterpret_cast<const float4 *>(&Bl[buf][kk][4 * tx]);
-      const float av[4] = {ah.x, ah.y, ah.z, ah.w}, alv[4] = {al.x, al.y, al.z, al.w};
-      const float bv[4] = {bh.x, bh.y, bh.z, bh.w}, blv[4] = {bl.x, bl.y, bl.z, bl.w};
+      const float av[4] = {ah.x, ah.y, ah.z, ah.w}, bv[4] = {bh.x, bh.y, bh.z, bh.w};
 #pragma unroll
       for (int r = 0; r < 4; ++r)
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const float p = av[r] * bv[q];
           const float e = fmaf(av[r], bv[q], -p);
-          const float x = fmaf(av[r], blv[q], alv[r] * bv[q]);
           two_sum_acc(s[r][q], c[r][q], p);
-          c[r][q] += e + x;
+          c[r][q] += e;
         }
     }
     if (more) store(buf ^ 1);
@@ -504,13 +494,15 @@ __global__ void __launch_bounds__(DF_THREADS) k_sym_gemm_pair(seqm_batch b, cons
     buf ^= 1;
   }
   double *C = Cm + mo;
+  const float *Mm = M + mo;
 #pragma unroll
   for (int r = 0; r < 4; ++r)
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int row = i0 + 4 * ty + r, col = j0 + 4 * tx + q;
       if (row < n && col < n) {
-        const double v = (double)s[r][q] + (double)c[r][q];
+        const double cross = (double)Mm[(size_t)row * n + col] + (double)Mm[(size_t)col * n + row];
+        const double v = (double)s[r][q] + ((double)c[r][q] + cross);
         C[(size_t)row * n + col] = v;
         C[(size_t)col * n + row] = v;
       }
@@ -538,12 +530,13 @@ __global__ void __launch_bounds__(EW_THREADS) k_mw_split(seqm_batch b, const dou
   const size_t nn = (size_t)n * n, base = (size_t)blockIdx.x * EW_CHUNK;
   if (base >= nn) return;
   const size_t mo = b.mol_mat_off[m];
+  const DiagTest diagonal(n);
   float mx = 0.0f;
   for (size_t idx = base + threadIdx.x; idx < nn && idx < base + EW_CHUNK; idx += EW_THREADS) {
     const double z = Z[mo + idx];
     const float d = (float)(Y[mo + idx] - z);
     Df[mo + idx] = d;
-    Bf[mo + idx] = (float)((diagonal(idx, n) ? 1.0 : 0.0) - 2.0 * z);
+    Bf[mo + idx] = (float)((diagonal((uint32_t)idx) ? 1.0 : 0.0) - 2.0 * z);
     mx = fmaxf(mx, fabsf(d));
   }
   if (!dmax) return;

@@ -198,8 +198,8 @@ __global__ void __launch_bounds__(1024) k_tc_tile_offsets(seqm_batch b, int64_t 
 // A 2^-e has its largest element in [0.5, 1), so a matrix of small elements (the McWeeny
 // correction D, ~1e-6) keeps FP16's 11 significant bits instead of falling into its subnormal
 // range.  No dmax or an all-zero matrix: e = 0.
-__device__ __forceinline__ int split_exp(const uint32_t *dmax, int m) {
-  if (!dmax) return 0;
+__device__ __forceinline__ int split_exp(const uint32_t *dmax, int m, int fixed = 0) {
+  if (!dmax) return fixed;
   const float mx = __uint_as_float(dmax[m]);
   if (!(mx > 0.0f) || !(mx < INFINITY)) return 0;
   int e = 0;
@@ -207,19 +207,19 @@ __device__ __forceinline__ int split_exp(const uint32_t *dmax, int m) {
   return e;
 }
 
-// split tiles of the FP32 X of running molecules (scaled by 2^-e of split_exp): CTA (kb, rb, m)
-// writes tile (rb, kb)
+// split tiles of the FP32 X of running molecules (scaled by 2^-e of split_exp, or by 2^-fixed_exp
+// without dmax): CTA (kb, rb, m) writes tile (rb, kb)
 __global__ void __launch_bounds__(128) k_tc_split(seqm_batch b, const float *__restrict__ X, uint8_t *__restrict__ Xh,
                                                   uint8_t *__restrict__ Xl, const int64_t *__restrict__ xs_off,
                                                   const double *__restrict__ st, const uint8_t *__restrict__ active,
-                                                  const uint32_t *__restrict__ dmax = nullptr) {
+                                                  const uint32_t *__restrict__ dmax = nullptr, int fixed_exp = 0) {
   const int m = blockIdx.z;
   if (st ? st[SP2_NS * m + S_RUN] == 0.0 : (active && !active[m])) return;  // running molecules, or active ones
   const int n = b.mol_norb[m];
   const int nb = (n + TC_M - 1) / TC_M, nk = (n + TC_KT - 1) / TC_KT;
   const int rb = blockIdx.y, kb = blockIdx.x;
   if (rb >= nb || kb >= nk) return;
-  const float scale = ldexpf(1.0f, -split_exp(dmax, m));
+  const float scale = ldexpf(1.0f, -split_exp(dmax, m, fixed_exp));
   const float *Xm = X + b.mol_mat_off[m];
   const size_t tile = (size_t)(xs_off[m] + (int64_t)rb * nk + kb) * SPLIT_TILE_BYTES;
   for (int g = threadIdx.x; g < TC_M * TC_KT / 8; g += 128) {
@@ -272,13 +272,15 @@ __device__ __forceinline__ bool upper_tile(int t, int nb, int &tm, int &tn) {
 // B's split tiles in Bh / Bl (A's are the kernel's Xh / Xl), Y an FP32 matrix (NULL: C = cAB A B);
 // A and B must commute (functions of one symmetric matrix), so that A B is symmetric and its upper
 // tiles with their mirrors are the whole product.  A split with the scale of dmax (k_tc_split)
-// has cAB multiplied back by 2^e per molecule (exact).
+// has cAB multiplied back by 2^e per molecule (exact).  full: every tile of a general product of
+// two symmetric matrices (grid of nb^2 tiles per molecule, no mirrors).
 struct TcProduct {
   const uint8_t *Bh, *Bl;
   const float *Y;
   float cY, cAB;
   const uint8_t *active;
   const uint32_t *dmax;
+  int full;
 };
 
 template <bool PROD>
@@ -294,7 +296,15 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_step(seqm_batch b, float *__r
   const int n = b.mol_norb[m];
   const int nb = (n + TC_M - 1) / TC_M, nk = (n + TC_KT - 1) / TC_KT;
   int tm, tn;
-  if (!upper_tile(blockIdx.x, nb, tm, tn)) return;
+  const bool all_tiles = PROD && pp.full;
+  if (all_tiles) {
+    if ((int)blockIdx.x >= nb * nb) return;
+    tm = (int)blockIdx.x / nb;
+    tn = (int)blockIdx.x % nb;
+  } else if (!upper_tile(blockIdx.x, nb, tm, tn)) {
+    return;
+  }
+  const bool mirror = !all_tiles && tm != tn;
 
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
@@ -444,7 +454,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_step(seqm_batch b, float *__r
       for (int c = lane; c < TC_N; c += 32) {
         const int gc = tn * TC_N + c, gc2 = tm * TC_N + c;
         if (gr < n && gc < n) Xm[(size_t)gr * n + gc] = stg[r * EPI_LD + c];
-        if (tm != tn && gr2 < n && gc2 < n) Xm[(size_t)gr2 * n + gc2] = stg[c * EPI_LD + r];
+        if (mirror && gr2 < n && gc2 < n) Xm[(size_t)gr2 * n + gc2] = stg[c * EPI_LD + r];
       }
     }
     // split tiles of X': tile (tm, 4 tn + q) and mirror tile (tn, 4 tm + q), 8 k per store
@@ -515,18 +525,25 @@ __global__ void k_refine_mask(int nmol, const uint8_t *__restrict__ active, uint
 }
 
 // FP64-accurate McWeeny step X <- X + D (I - 2X), D = X^2 - X (X = P/2), of the tensor-core form:
-// X^2 from FP32 pairs (k_sym_gemm_pair), the correction product as a split product on the tensor
-// cores with D scaled to FP16's range per molecule.  Buffers: Y, Z FP64 and Df, Bf FP32 of the
-// batch's matrix size (Y doubles as the FP32 correction), xs[0..3] split tiles.
+// X^2 from FP32 pairs (k_sym_gemm_pair, its cross term Xh Xl a split product on the tensor cores),
+// the correction product as a split product on the tensor cores with D scaled to FP16's range per
+// molecule.  Buffers: Y, Z FP64 and Df, Bf FP32 of the batch's matrix size (Y doubles as the FP32
+// correction, Bf as the cross term once split), xs[0..3] split tiles.
 inline void mcweeny_tc(const seqm_batch &b, double *P, double *Y, double *Z, float *Df, float *Bf, uint8_t *const *xs,
                        const int64_t *xs_off, double *st, int *err, uint32_t *dmax, const uint8_t *rmask, int steps,
                        cudaStream_t s) {
   float *Cf = reinterpret_cast<float *>(Y);
   const int nb = (b.max_norb + TC_M - 1) / TC_M, nk = (b.max_norb + TC_KT - 1) / TC_KT;
   const dim3 grid((unsigned)(nb * (nb + 1) / 2), (unsigned)b.nmol), split((unsigned)nk, (unsigned)nb, (unsigned)b.nmol);
+  const dim3 grid_full((unsigned)(nb * nb), (unsigned)b.nmol);
   for (int k = 0; k < steps; ++k) {
     k_ew_axpby<<<ew_grid(b), EW_THREADS, 0, s>>>(b, 0.5, P, 0.0, nullptr, Z, rmask);  // Z = X
-    k_split_pair<<<ew_grid(b), EW_THREADS, 0, s>>>(b, Z, Df, Bf, rmask);
+    k_split_pair<<<ew_grid(b), EW_THREADS, 0, s>>>(b, Z, Df, Bf, rmask);             // Xh, Xl
+    k_tc_split<<<split, 128, 0, s>>>(b, Df, xs[0], xs[1], xs_off, nullptr, rmask);
+    k_tc_split<<<split, 128, 0, s>>>(b, Bf, xs[2], xs[3], xs_off, nullptr, rmask, nullptr, -24);  // 2^24 Xl
+    k_tc_step<true><<<grid_full, TC_THREADS, TC_SMEM, s>>>(b, Bf, xs[0], xs[1], nullptr, nullptr, xs_off, st, err,
+                                                          TcProduct{xs[2], xs[3], nullptr, 0.0f, 0x1p-24f, rmask,
+                                                                    nullptr, 1});  // Bf = M = Xh Xl
     k_sym_gemm_pair<<<pair_gemm_grid(b), DF_THREADS, 0, s>>>(b, Df, Bf, Y, rmask);   // Y = X^2
     cudaMemsetAsync(dmax, 0, sizeof(uint32_t) * b.nmol, s);
     k_mw_split<<<ew_grid(b), EW_THREADS, 0, s>>>(b, Y, Z, Df, Bf, rmask, dmax);      // D, I - 2X, max |D|

@@ -59,7 +59,12 @@ class ScfState(ctypes.Structure):
                                   "err", "dm_err", "dm_el", "mol_row_off", "iters", "active", "diis_err",
                                   "nactive")] + [
         ("mixing", ctypes.c_int32), ("pad_", ctypes.c_int32), ("alpha", ctypes.c_double),
-        ("occupation", ctypes.c_double), ("eps", ctypes.c_double)]
+        ("occupation", ctypes.c_double), ("eps", ctypes.c_double), ("scratch", _P)]
+
+
+def scf_scratch_doubles(nmol, natoms, npairs, sum_norb):
+    """SEQM_SCF_SCRATCH_DOUBLES: scratch of the fused seqm_scf_step."""
+    return 5 * nmol + natoms + npairs + 4 * sum_norb
 
 
 _lib = None

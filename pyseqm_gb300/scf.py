@@ -59,6 +59,9 @@ class BatchSCF:
         self.Enuc = torch.zeros(max(1, nm), **f64)
         self.active = torch.ones(max(1, nm), dtype=torch.uint8, device=dev)
         self.nactive = torch.zeros(1, dtype=torch.int32, device=dev)  # molecules active after an iteration
+        # scratch of the fused iteration (dP terms, energy partials of the Fock build, slice sums)
+        self.step_scratch = torch.empty(max(1, native.scf_scratch_doubles(nm, layout.natoms, layout.npairs, R)),
+                                        **f64)
         self.h_nactive = torch.zeros(2, dtype=torch.int32, pin_memory=dev.type == "cuda")
         self.iters = torch.zeros(max(1, nm), dtype=torch.int32, device=dev)
         self.status = torch.zeros(max(1, nm), dtype=torch.int32, device=dev)
@@ -350,6 +353,7 @@ class BatchSCF:
                      "dm_el", "iters", "active", "nactive"):
             setattr(st, name, getattr(self, name).data_ptr())
         st.mol_row_off = self.L.dev["row_off"].data_ptr()
+        st.scratch = self.step_scratch.data_ptr()
         st.diis_err = None
         st.mixing = 0 if self._linear else 1
         st.alpha, st.occupation, st.eps = self._alpha, 2.0, self._eps
@@ -385,8 +389,14 @@ class BatchSCF:
             self.energy_error(self._eps)
             self.nactive.copy_(self.active[: L.nmol].sum())
             return
-        # mixing, Fock build, energy and convergence test, count of the molecules still active
-        self.launches += 2 + (0 if self._diis else 1)
+        # mixing, Fock build, energy and convergence test, count of the molecules still active (fused:
+        # adaptive diagonal step(s), two mixer streams (+ the grid one), Fock build, energy finish;
+        # DIIS: Fock build, energy pass(es))
+        large = 1 if self.L.max_norb > 160 else 0
+        if self._diis:
+            self.launches += 2 + large
+        else:
+            self.launches += 4 + large + (0 if self._linear else 1 + large)
         native.check(self.lib.seqm_scf_step(L.struct, ctypes.byref(self._state), self._s()), "seqm_scf_step")
 
     def max_loops(self, max_iter=MAX_ITER):

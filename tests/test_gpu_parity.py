@@ -185,26 +185,35 @@ def test_edge_case_molecules_match_oracle():
     np.testing.assert_allclose(out["Etot"].cpu().numpy(), ref["Etot"], atol=1e-6, rtol=0)
 
 
-def test_scf_step_entry_matches_the_separate_calls():
-    """seqm_scf_step (mixing + Fock build + energy/test + active count in one call) against the
-    three entry points called one by one: the same kernels, so the same iterations and energies."""
+@pytest.mark.parametrize("case", ["mixed_adaptive", "mixed_linear", "water64_adaptive", "water64_linear"])
+def test_scf_step_entry_matches_the_separate_calls(case):
+    """seqm_scf_step (mixing with the ||dP|| terms, Fock build with the energy partials, energy
+    and test from those, active count) against the entry points called one by one (Pold stored,
+    a separate energy pass): the same SCF to rounding.  (H2O)64 (384 AOs) takes the grid mixer
+    over several slices and a multi-slice energy sum."""
     from pyseqm_gb300 import workloads
     from pyseqm_gb300.layout import Layout
     from pyseqm_gb300.scf import BatchSCF
 
-    mols = workloads.mixed_batch(24, seed=11, alkane_range=(1, 10), water_range=(2, 12))
+    if case.startswith("mixed"):
+        mols = workloads.mixed_batch(24, seed=11, alkane_range=(1, 10), water_range=(2, 12))
+        method = "AM1"
+    else:
+        mols = [workloads.big_water(seed=5, n_side=4), workloads.water_cluster(6, np.random.default_rng(2))]
+        method = "PM3"
+    converger = (0, 0.3) if case.endswith("linear") else (1,)
     species, coords = workloads.pad_batch(mols)
-    L = Layout.from_padded(species, coords, "AM1").to_device("cuda")
+    L = Layout.from_padded(species, coords, method).to_device("cuda")
     out = []
     for split in (False, True):
         s = BatchSCF(L)
         s.profile_fock = split
         s.hcore()
-        assert not s.scf(1e-8, (1,)).any()
+        assert not s.scf(1e-8, converger).any()
         E, En = s.final(want_vectors=False)
         out.append(((E + En).cpu().numpy(), s.iters[: L.nmol].cpu().numpy(), int(s.nactive[0])))
-    np.testing.assert_array_equal(out[0][0], out[1][0])
-    np.testing.assert_array_equal(out[0][1], out[1][1])
+    np.testing.assert_allclose(out[0][0], out[1][0], atol=1e-7, rtol=0)
+    assert np.abs(out[0][1] - out[1][1]).max() <= 1
     assert out[0][2] == 0
 
 

@@ -406,7 +406,7 @@ def run_ours(args):
         h2d = L.h2d_bytes
         d2h = 2 * 8 * args.nmol + 4 * args.nmol + args.nmol  # energies, iteration counts, flags
         e2e = {"value": args.nmol / dt, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-               "ms_per_step": 1e3 * dt, "includes": "host layout build (NumPy; the pair list is built on the GPU), H2D, hcore+SCF+energies, D2H"}
+               "ms_per_step": 1e3 * dt, "includes": "host layout build (NumPy; the pair list and the per-atom parameters are built on the GPU), H2D, hcore+SCF+energies, D2H"}
         assert not r["notconverged"].any()
     configs = {}
     if rank == 0:

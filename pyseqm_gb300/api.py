@@ -46,8 +46,11 @@ def _isolated_atom_energy(L):
     el = tables.elements()
     from .native import PAR
 
-    p = L.par
+    terms = (("U_ss", "ussc"), ("U_pp", "uppc"), ("g_ss", "gssc"), ("g_pp", "gppc"), ("g_sp", "gspc"),
+             ("g_p2", "gp2c"), ("h_sp", "hspc"))
     Z = L.Z
-    return (p[PAR["U_ss"]] * el["ussc"][Z] + p[PAR["U_pp"]] * el["uppc"][Z] + p[PAR["g_ss"]] * el["gssc"][Z]
-            + p[PAR["g_pp"]] * el["gppc"][Z] + p[PAR["g_sp"]] * el["gspc"][Z] + p[PAR["g_p2"]] * el["gp2c"][Z]
-            + p[PAR["h_sp"]] * el["hspc"][Z])
+    if not any(PAR[f] in L.learned for f, _ in terms):  # per element, then one gather
+        tab = L.par_table
+        per_el = sum(tab[PAR[f], : len(el[c])] * el[c] for f, c in terms)
+        return per_el[Z]
+    return sum(L.par_row(f) * el[c][Z] for f, c in terms)

@@ -138,23 +138,39 @@ class Layout:
                 L.pair_skip = skip
         L.order = np.argsort(-L.norb, kind="stable")
         L.max_norb = int(L.norb.max()) if L.nmol else 0
-        # per-atom parameters, structure of arrays
+        # per-atom parameters, structure of arrays: a per-element table (parameter slots x
+        # elements, small) whose column Z is each atom's, gathered where the parameters are used
+        # (on the device for a GPU batch, so the per-atom array is neither built on the host nor
+        # copied), and the learned per-atom overrides
         fields, rows = tables.method_table(method, param_dir)
-        if rows.shape[0] <= int(L.Z.max(initial=0)):  # elements past the file's last row: zeros
-            rows = np.vstack([rows, np.zeros((int(L.Z.max()) + 1 - rows.shape[0], rows.shape[1]))])
-        par = np.zeros((native.NPAR, L.natoms))
+        ne = max(rows.shape[0], len(el["tore"]), int(L.Z.max(initial=0)) + 1)  # past the file's rows: zeros
+        tab = np.zeros((native.NPAR, ne))
         for k, f in enumerate(fields):
-            par[native.PAR[f]] = rows[L.Z, k]
-        par[native.PAR["_tore"]] = el["tore"][L.Z]
-        par[native.PAR["_qn"]] = el["qn"][L.Z]
-        if learned:
-            for k, v in learned.items():
-                par[native.PAR[k]] = np.asarray(v, dtype=np.float64).reshape(-1)
+            tab[native.PAR[f], : rows.shape[0]] = rows[:, k]
+        tab[native.PAR["_tore"], : len(el["tore"])] = el["tore"]
+        tab[native.PAR["_qn"], : len(el["qn"])] = el["qn"]
         # the reference's Energy sets rho_core to zero for every method but PM6 with d orbitals
         # (basics.py:796-809), so the core-core term always takes rho0 here
-        par[native.PAR["rho_core"]] = 0.0
-        L.par = par
+        tab[native.PAR["rho_core"]] = 0.0
+        L.par_table = tab
+        L.learned = {native.PAR[k]: np.asarray(v, dtype=np.float64).reshape(-1) for k, v in (learned or {}).items()}
+        L._par = None
         return L
+
+    @property
+    def par(self):
+        """Per-atom parameters (NPAR x natoms), gathered on the host on first use."""
+        if self._par is None:
+            par = np.take(self.par_table, self.Z, axis=1)
+            for slot, v in self.learned.items():
+                par[slot] = v
+            self._par = par
+        return self._par
+
+    def par_row(self, name):
+        """One parameter of every atom (natoms,), without the full per-atom array."""
+        slot = native.PAR[name]
+        return self.learned[slot] if slot in self.learned else self.par_table[slot][self.Z]
 
     # ------------------------------------------------------------------- pairs
     def _host_pairs(self):
@@ -192,8 +208,15 @@ class Layout:
             "nocc": i32(self.nocc), "mat_off": i64(self.mat_off), "row_off": i64(self.row_off),
             "xx_off": i32(self.xx_off), "xh_off": i32(self.xh_off), "hh_off": i32(self.hh_off),
             "order": i32(self.order), "Z": i32(self.Z), "atom_mol": i32(self.atom_mol),
-            "xyz": f64(self.xyz.reshape(-1)), "par": f64(self.par.reshape(-1)),
+            "xyz": f64(self.xyz.reshape(-1)),
         }
+        # per-atom parameters gathered on the device from the element table (+ learned overrides)
+        tab = f64(self.par_table)
+        par = tab[:, d["Z"].long()]
+        for slot, v in self.learned.items():
+            par[slot] = f64(v)
+        d["par"] = par.reshape(-1).contiguous()
+        copied = int(tab.numel() * 8) + sum(int(v.size * 8) for v in self.learned.values())
         # a CUDA batch whose host pair list was not needed builds it on the GPU (seqm_build_pairs)
         on_gpu = torch.device(device).type == "cuda" and self._pairs is None
         if on_gpu:
@@ -226,9 +249,10 @@ class Layout:
             mat_total=int(self.mat_off[-1]),
         )
         set_size_classes(self._struct, self.norb[self.order] if self.nmol else np.zeros(0, np.int64))
-        # bytes copied from the host (the pair list built on the GPU is not among them)
-        self.h2d_bytes = sum(int(t.numel() * t.element_size()) for k, t in d.items()
-                             if not (on_gpu and k in ("pair_i", "pair_j")))
+        # bytes copied from the host (the pair list built on the GPU and the parameters gathered there
+        # are not among them; the element table and learned overrides are)
+        self.h2d_bytes = copied + sum(int(t.numel() * t.element_size()) for k, t in d.items()
+                                      if k != "par" and not (on_gpu and k in ("pair_i", "pair_j")))
         if on_gpu and self.npairs:
             stream = torch.cuda.current_stream(self.device).cuda_stream
             native.check(native.load().seqm_build_pairs(self._struct, native.ptr(d["pair_i"]), native.ptr(d["pair_j"]),

@@ -226,18 +226,19 @@ __device__ void form_vfvt(double *A, int lda, const double *V, double *G, int n,
   __syncthreads();
 }
 
-// A32 (float, shared, overlaying A) <- V F V^T in FP32, with F in A (FP64) on entry.  V and F
-// are converted once (G as floats: V32T = V^T in G[0, n^2), F32 in G[n^2, 2 n^2)) so that the
-// products run on FP32 operands (conversions to and from FP64 issue on the FP64 pipe) and every
-// operand row read across a warp is contiguous.  The product V F goes to the upper half of A's
-// space (T32).  Input to FP32 sweeps, which need no more precision.
-__device__ void form_vfvt32(double *A, int lda, const double *V, double *G, int n) {
-  float *V32T = reinterpret_cast<float *>(G), *F32 = V32T + (size_t)n * n;
-  float *A32 = reinterpret_cast<float *>(A), *T32 = A32 + (size_t)n * lda;
+// A32 (float, shared, overlaying A) <- V F V^T in FP32 from V and F (global, FP64).  Both
+// operands of the first product are converted once into A's shared space (F32 in the half A32
+// takes, V^T in the other) so that the products read FP32 operands from shared memory
+// (conversions to and from FP64 issue on the FP64 pipe); V F goes to G (global scratch, floats),
+// and V F V^T overwrites F32, which is dead by then.  A's FP64 contents are not used.  Input to
+// FP32 sweeps, which need no more precision.
+__device__ void form_vfvt32(double *A, int lda, const double *V, const double *Fm, double *G, int n) {
+  float *A32 = reinterpret_cast<float *>(A), *F32 = A32, *V32T = A32 + (size_t)n * lda;
+  float *T32 = reinterpret_cast<float *>(G);
   for (int idx = threadIdx.x; idx < n * n; idx += NTB) {
     const int i = idx / n, j = idx - i * n;
     V32T[j * n + i] = (float)V[idx];
-    F32[idx] = (float)A[i * lda + j];
+    F32[idx] = (float)Fm[idx];
   }
   __syncthreads();
   tile_product_t<float>(
@@ -760,7 +761,7 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
     // first-order density from the FP64 coupling block alone
     float *A32 = reinterpret_cast<float *>(A);
     if (is_warm) {
-      form_vfvt32(A, lda, V, G, n);
+      form_vfvt32(A, lda, V, Fm, G, n);
     } else {  // A (FP64) -> A32 in place, through G
       for (int idx = tid; idx < n * n; idx += NTB) {
         int i = idx / n, j = idx - i * n;
@@ -799,7 +800,7 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
     // re-orthonormalisation, then A = V F V^T in FP64 for the second-order eigenvalues below
     float *A32 = reinterpret_cast<float *>(A);
     if (is_warm) {
-      form_vfvt32(A, lda, V, G, n);
+      form_vfvt32(A, lda, V, Fm, G, n);
     } else {
       for (int idx = tid; idx < n * n; idx += NTB) {
         int i = idx / n, j = idx - i * n;
@@ -825,7 +826,7 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
     // rotate in FP32 first: if the occupied-virtual block is already small, the FP64
     // rotation and the first-order density follow; otherwise the FP32 sweeps start from it
     // and the FP64 rotation is skipped
-    form_vfvt32(A, lda, V, G, n);
+    form_vfvt32(A, lda, V, Fm, G, n);
     rank_diag(reinterpret_cast<const float *>(A), lda, n, dg, rank, order);
     if (ov_theta(reinterpret_cast<const float *>(A), lda, n, nocc, dg, order, sh.red) <= 0.5 * NEWTON_THETA) {
       for (int idx = tid; idx < n * n; idx += NTB) {
@@ -842,7 +843,7 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
           A[i * lda + j] = Fm[idx];
         }
         __syncthreads();
-        form_vfvt32(A, lda, V, G, n);
+        form_vfvt32(A, lda, V, Fm, G, n);
         a32_ready = true;
       }
     } else {

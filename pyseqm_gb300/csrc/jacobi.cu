@@ -28,6 +28,8 @@
 
 #include <atomic>
 
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace seqm {
@@ -188,15 +190,22 @@ __device__ void tile_product_df(int M, int N, int K, bool upper_only, LF L, RF R
         if (j0 + q < N) split_val(R(l, j0 + q), bh[q], bl[q]);
         else bh[q] = bl[q] = 0.0f;
       }
+      // exact FP32 operands (both lo parts zero) need no cross terms
+      constexpr bool exact = std::is_same<decltype(L(0, 0)), float>::value &&
+                             std::is_same<decltype(R(0, 0)), float>::value;
 #pragma unroll
       for (int r = 0; r < 4; ++r)
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const float p = ah[r] * bh[q];
           const float e = fmaf(ah[r], bh[q], -p);
-          const float x = fmaf(ah[r], bl[q], al[r] * bh[q]);
           two_sum_acc(s[r][q], c[r][q], p);
-          c[r][q] += e + x;
+          if (exact) {
+            c[r][q] += e;
+          } else {
+            const float x = fmaf(ah[r], bl[q], al[r] * bh[q]);
+            c[r][q] += e + x;
+          }
         }
     }
 #pragma unroll
@@ -404,60 +413,62 @@ __device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_swee
         __syncthreads();
         continue;
       }
-      // A <- J^T A J on 2x2 blocks (pair i rows, pair j cols, i <= j): block row i per warp,
-      // lanes along j; each block and its mirror written by one thread
-      for (int i = wid; i < np; i += NTB_W) {
-        const int fi = sh.rflag[i];
-        const int p = sh.rp[i], q = sh.rq[i];
-        const bool qv = q < n;
-        const T ci = rc[i], si = rs[i];
-        for (int j = i + lane; j < np; j += 32) {
-          const int fj = sh.rflag[j];
-          if (!(fi | fj)) continue;
-          if (j == i) {
-            const T t = rt[i], apq = A[p * lda + q];
-            A[p * lda + p] -= t * apq;
-            A[q * lda + q] += t * apq;
-            A[p * lda + q] = T(0);
-            A[q * lda + p] = T(0);
-            continue;
+      if constexpr (sizeof(T) == 8) {
+        // A <- J^T A J on 2x2 blocks (pair i rows, pair j cols, i <= j): block row i per warp,
+        // lanes along j; each block and its mirror written by one thread
+        for (int i = wid; i < np; i += NTB_W) {
+          const int fi = sh.rflag[i];
+          const int p = sh.rp[i], q = sh.rq[i];
+          const bool qv = q < n;
+          const T ci = rc[i], si = rs[i];
+          for (int j = i + lane; j < np; j += 32) {
+            const int fj = sh.rflag[j];
+            if (!(fi | fj)) continue;
+            if (j == i) {
+              const T t = rt[i], apq = A[p * lda + q];
+              A[p * lda + p] -= t * apq;
+              A[q * lda + q] += t * apq;
+              A[p * lda + q] = T(0);
+              A[q * lda + p] = T(0);
+              continue;
+            }
+            const int r = sh.rp[j], s = sh.rq[j];
+            const bool sv = s < n;
+            T x00 = A[p * lda + r];
+            T x01 = sv ? A[p * lda + s] : T(0);
+            T x10 = qv ? A[q * lda + r] : T(0);
+            T x11 = (qv && sv) ? A[q * lda + s] : T(0);
+            if (fi) {
+              T y00 = ci * x00 - si * x10, y10 = si * x00 + ci * x10;
+              T y01 = ci * x01 - si * x11, y11 = si * x01 + ci * x11;
+              x00 = y00; x10 = y10; x01 = y01; x11 = y11;
+            }
+            if (fj) {
+              const T c = rc[j], sn = rs[j];
+              T z00 = c * x00 - sn * x01, z01 = sn * x00 + c * x01;
+              T z10 = c * x10 - sn * x11, z11 = sn * x10 + c * x11;
+              x00 = z00; x01 = z01; x10 = z10; x11 = z11;
+            }
+            A[p * lda + r] = x00;
+            A[r * lda + p] = x00;
+            if (sv) { A[p * lda + s] = x01; A[s * lda + p] = x01; }
+            if (qv) { A[q * lda + r] = x10; A[r * lda + q] = x10; }
+            if (qv && sv) { A[q * lda + s] = x11; A[s * lda + q] = x11; }
           }
-          const int r = sh.rp[j], s = sh.rq[j];
-          const bool sv = s < n;
-          T x00 = A[p * lda + r];
-          T x01 = sv ? A[p * lda + s] : T(0);
-          T x10 = qv ? A[q * lda + r] : T(0);
-          T x11 = (qv && sv) ? A[q * lda + s] : T(0);
-          if (fi) {
-            T y00 = ci * x00 - si * x10, y10 = si * x00 + ci * x10;
-            T y01 = ci * x01 - si * x11, y11 = si * x01 + ci * x11;
-            x00 = y00; x10 = y10; x01 = y01; x11 = y11;
-          }
-          if (fj) {
-            const T c = rc[j], sn = rs[j];
-            T z00 = c * x00 - sn * x01, z01 = sn * x00 + c * x01;
-            T z10 = c * x10 - sn * x11, z11 = sn * x10 + c * x11;
-            x00 = z00; x01 = z01; x10 = z10; x11 = z11;
-          }
-          A[p * lda + r] = x00;
-          A[r * lda + p] = x00;
-          if (sv) { A[p * lda + s] = x01; A[s * lda + p] = x01; }
-          if (qv) { A[q * lda + r] = x10; A[r * lda + q] = x10; }
-          if (qv && sv) { A[q * lda + s] = x11; A[s * lda + q] = x11; }
         }
-      }
-      // eigenvector rows p,q: warp per pair, lanes along the row (coalesced / conflict-free)
-      for (int i = wid; i < np; i += NTB_W) {
-        if (!sh.rflag[i]) continue;
-        const T c = rc[i], sn = rs[i];
-        T *vp = V + (size_t)sh.rp[i] * n, *vq = V + (size_t)sh.rq[i] * n;
-        for (int k = lane; k < n; k += 32) {
-          const T a = vp[k], bq = vq[k];
-          vp[k] = c * a - sn * bq;
-          vq[k] = sn * a + c * bq;
+        // eigenvector rows p,q: warp per pair, lanes along the row (coalesced / conflict-free)
+        for (int i = wid; i < np; i += NTB_W) {
+          if (!sh.rflag[i]) continue;
+          const T c = rc[i], sn = rs[i];
+          T *vp = V + (size_t)sh.rp[i] * n, *vq = V + (size_t)sh.rq[i] * n;
+          for (int k = lane; k < n; k += 32) {
+            const T a = vp[k], bq = vq[k];
+            vp[k] = c * a - sn * bq;
+            vq[k] = sn * a + c * bq;
+          }
         }
+        __syncthreads();
       }
-      __syncthreads();
     }
   }
   return -1;
@@ -629,16 +640,16 @@ constexpr double EIG_PT_RATIO = 3.0e-3;  // largest coupling / splitting for sec
 // so X holds FP32 values whose products are exact; D = X X^T - I is summed to FP64 accuracy
 // (double-float) from X^T staged in shared memory (conflict-free rows) and kept as FP32 (|D| ~ 1e-6);
 // one Newton-Schulz step V <- X - D X / 2 (the small product D X in FP32) leaves the rows of V
-// orthonormal to ~1e-13.  G (floats): [X32 | V32, later D32].  Returns the FP32 sweeps taken.
+// orthonormal to ~1e-13.  G (floats): X32; shared: A32, then V (warm) for X = W V, then X^T, and
+// W32, then D.  Returns the FP32 sweeps taken.
 __device__ int fp32_sweeps_orth(double *A, int lda, double *V, double *G, int n, double tol32, bool is_warm,
                                 double *dg, int *rank, int *order, JShared &sh) {
   const int tid = threadIdx.x;
   float *A32 = reinterpret_cast<float *>(A), *W32 = A32 + (size_t)n * lda;
-  float *X32 = reinterpret_cast<float *>(G), *V32 = X32 + (size_t)n * n, *D32 = V32;
+  float *X32 = reinterpret_cast<float *>(G);
   for (int idx = tid; idx < n * n; idx += NTB) {
     int i = idx / n, j = idx - i * n;
     W32[idx] = i == j ? 1.0f : 0.0f;
-    if (is_warm) V32[idx] = (float)V[idx];
   }
   __syncthreads();
   int s32 = jacobi_solve<float>(A32, lda, W32, n, tol32, 20, sh);
@@ -646,6 +657,10 @@ __device__ int fp32_sweeps_orth(double *A, int lda, double *V, double *G, int n,
   __syncthreads();
   rank_diag(A32, lda, n, dg, rank, order);
   if (is_warm) {
+    // V in FP32 over the swept A32 (dead now), so that both operands of X = W V are in shared memory
+    float *V32 = A32;
+    for (int idx = tid; idx < n * n; idx += NTB) V32[idx] = (float)V[idx];
+    __syncthreads();
     tile_product_t<float>(
         n, false, [&](int k, int l) { return W32[k * n + l]; }, [&](int l, int j) { return V32[l * n + j]; },
         [&](int k, int j, float v) {
@@ -665,19 +680,21 @@ __device__ int fp32_sweeps_orth(double *A, int lda, double *V, double *G, int n,
     XT[j * lda + i] = X32[idx];
   }
   __syncthreads();
-  // exact FP32 products summed to FP64 accuracy on the FP32 pipe
+  // exact FP32 products summed to FP64 accuracy on the FP32 pipe; D over the dead W32, so that
+  // the correction D X reads both operands from shared memory (X as X^T's columns)
+  float *D32s = W32;
   tile_product_df(
       n, n, n, true, [&](int k, int l) { return XT[l * lda + k]; }, [&](int l, int j) { return XT[l * lda + j]; },
       [&](int k, int j, double v) {
         if (k <= j) {
           const float d = (float)(v - (k == j ? 1.0 : 0.0));
-          D32[k * n + j] = d;
-          D32[j * n + k] = d;
+          D32s[k * n + j] = d;
+          D32s[j * n + k] = d;
         }
       });
   __syncthreads();
   tile_product_t<float>(
-      n, false, [&](int k, int l) { return D32[k * n + l]; }, [&](int l, int j) { return X32[l * n + j]; },
+      n, false, [&](int k, int l) { return D32s[k * n + l]; }, [&](int l, int j) { return XT[j * lda + l]; },
       [&](int k, int j, float v) { V[(size_t)k * n + j] -= 0.5 * (double)v; });
   __syncthreads();
   return s32;

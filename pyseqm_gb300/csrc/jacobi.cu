@@ -178,6 +178,7 @@ __device__ void tile_product_df(int M, int N, int K, bool upper_only, LF L, RF R
     if (upper_only && kb > jb) continue;
     const int k0 = kb * 4, j0 = jb * 4;
     float s[4][4] = {}, c[4][4] = {};
+#pragma unroll 2
     for (int l = 0; l < K; ++l) {
       float ah[4], al[4], bh[4], bl[4];
 #pragma unroll

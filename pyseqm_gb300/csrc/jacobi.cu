@@ -70,6 +70,7 @@ __device__ void tile_product_t(int n, bool upper_only, LF L, RF R, OF out) {
     if (upper_only && kb > jb) continue;
     const int k0 = kb * 4, j0 = jb * 4;
     T acc[4][4] = {};
+#pragma unroll 2
     for (int l = 0; l < n; ++l) {
       T a[4], c[4];
 #pragma unroll
@@ -104,6 +105,7 @@ __device__ void tile_product_mnk_t(int M, int N, int K, bool upper_only, LF L, R
     if (upper_only && kb > jb) continue;
     const int k0 = kb * 4, j0 = jb * 4;
     T acc[4][4] = {};
+#pragma unroll 2
     for (int l = 0; l < K; ++l) {
       T a[4], c[4];
 #pragma unroll

@@ -52,10 +52,10 @@ WORKLOAD = {"workload": "AM1 batched single-point SCF, 4096 molecules 50/50 n-al
                             "coupling block and first-order density; FP64-accurate"}
 METRIC = "SCF solves/s"
 # DRAM bytes of one density call (all size-class launches) of the default workload, from ncu
-# captures of the norb > 114 class of the 2048-molecule batch (110 MB with FP32 sweeps, 80 MB for
+# captures of the norb > 114 class of the 2048-molecule batch (92 MB with FP32 sweeps, 74 MB for
 # a warm first-order step, for 37 % of that batch's matrix elements), scaled to the 4096-molecule
-# batch and averaged over the calls of a solve (ten with sweeps, four warm, one final)
-JACOBI_TRAFFIC_BYTES = 5.5e8
+# batch and weighted by the calls of a solve that take FP32 sweeps (73 %)
+JACOBI_TRAFFIC_BYTES = 4.7e8
 
 
 def _oracle_chunk(args):
@@ -314,8 +314,9 @@ def run_ours(args):
                 "bound": "fp64", "achieved": achieved, "peak": peak_fp64, "unit": "TFLOP/s",
                 "frac": (achieved / peak_fp64) if achieved else None, "traffic": JACOBI_TRAFFIC_BYTES,
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the norb > 114 class launch "
-                                  "of the 2048-molecule batch (110 MB with FP32 sweeps, 80 MB warm, for 37 % of its "
-                                  "matrix elements), scaled to this batch and averaged over a solve's density calls",
+                                  "of the 2048-molecule batch (92 MB with FP32 sweeps, 74 MB warm, for 37 % of its "
+                                  "matrix elements), scaled to this batch and weighted by the calls with sweeps "
+                                  "(73 %)",
                 "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (the measured-peaks file has no FP64 "
                                "figure); the unit counts FP64-accurate eigensolve work, which the kernel runs as FP32 "
                                "sweeps, a first-order density step and double-float products on the FP32 pipe, so "

@@ -157,6 +157,14 @@ __device__ __forceinline__ void split_f64(double x, float &hi, float &lo) {
 }
 
 __device__ __forceinline__ void split_val(double x, float &hi, float &lo) { split_f64(x, hi, lo); }
+// an operand already split into FP32 hi + lo (split once where it is produced)
+struct DFPair {
+  float h, l;
+};
+__device__ __forceinline__ void split_val(DFPair x, float &hi, float &lo) {
+  hi = x.h;
+  lo = x.l;
+}
 __device__ __forceinline__ void split_val(float x, float &hi, float &lo) {
   hi = x;
   lo = 0.0f;
@@ -712,28 +720,36 @@ __device__ int fp32_sweeps_orth(double *A, int lda, double *V, double *G, int n,
 // The products of small quantities (Theta V_T, Theta Theta^T, E C') run in FP32 on FP32
 // copies (rounding ~1e-7 of terms <= 1e-5); V_S F, the coupling block and U^T U in FP64.  The
 // diagonal dg only enters the denominators, where FP32 accuracy is enough.
-// Scratch: S (shared, >= n^2 doubles) = [V_S F, later U | Theta, later C'32 | E32 | Theta32];
-// G (global, n^2 doubles, P's block) = [V32 (floats) | C' (FP64)].  Returns false, with P
-// untouched, when the rotation is too large (or the gap not positive).
+// Scratch: S (shared, >= n^2 doubles) = [V_S F, later U (both as FP32 hi | lo) | Theta, later
+// C'32 | E32 | Theta32]; G (global, n^2 doubles, P's block) = [V hi (floats) | V lo, later C'
+// (FP64)].  Every operand of the double-float products is split into FP32 hi + lo once, where it
+// is produced (V on entry, V_S F and U by their products), instead of on each of the ~n/4 loads
+// by the register tiles.  Returns false, with P untouched, when the rotation is too large (or the
+// gap not positive).
 __device__ bool newton_density_ov(double *S, const double *V, const double *Fm, double *G, double *Pm, int n,
                                   int nocc, const double *dg, const int *order, double *red) {
   const bool use_occ = nocc <= n - nocc;
   const int nsel = use_occ ? nocc : n - nocc, ncomp = n - nsel;
   const int s0 = use_occ ? 0 : nocc, t0 = use_occ ? nocc : 0;
-  double *Gs = S, *Th = S + (size_t)nsel * n;  // Gs holds (V_S F)^T: n rows of nsel
+  const size_t sn = (size_t)nsel * n;
+  float *Gsh = reinterpret_cast<float *>(S), *Gsl = Gsh + sn;  // (V_S F)^T: n rows of nsel, split
+  double *Th = S + sn;
   float *E32 = reinterpret_cast<float *>(Th + (size_t)nsel * ncomp), *Th32 = E32 + (size_t)nsel * nsel;
   float *C1_32 = reinterpret_cast<float *>(Th);
-  float *V32 = reinterpret_cast<float *>(G);
-  double *C1 = G + ((size_t)n * n + 1) / 2;  // after V32; ends at or before n^2 (nsel <= n / 2)
-  for (int idx = threadIdx.x; idx < n * n; idx += NTB) V32[idx] = (float)V[idx];
+  float *Vh = reinterpret_cast<float *>(G), *Vl = Vh + (size_t)n * n;
+  double *C1 = G + ((size_t)n * n + 1) / 2;  // over V lo, dead by then; ends at or before n^2 (nsel <= n / 2)
+  for (int idx = threadIdx.x; idx < n * n; idx += NTB) split_f64(V[idx], Vh[idx], Vl[idx]);
+  __syncthreads();
+  auto Vrow = [&](int r, int l) { return DFPair{Vh[(size_t)r * n + l], Vl[(size_t)r * n + l]}; };
   tile_product_df(
-      nsel, n, n, false, [&](int i, int l) { return V[(size_t)order[s0 + i] * n + l]; },
-      [&](int l, int j) { return Fm[(size_t)l * n + j]; }, [&](int i, int j, double v) { Gs[(size_t)j * nsel + i] = v; });
+      nsel, n, n, false, [&](int i, int l) { return Vrow(order[s0 + i], l); },
+      [&](int l, int j) { return Fm[(size_t)l * n + j]; },
+      [&](int i, int j, double v) { split_f64(v, Gsh[(size_t)j * nsel + i], Gsl[(size_t)j * nsel + i]); });
   __syncthreads();
   // a_st for t (rows, contiguous V_T rows broadcast) x s (columns of (V_S F)^T, contiguous)
   tile_product_df(
-      ncomp, nsel, n, false, [&](int t, int l) { return V[(size_t)order[t0 + t] * n + l]; },
-      [&](int l, int i) { return Gs[(size_t)l * nsel + i]; },
+      ncomp, nsel, n, false, [&](int t, int l) { return Vrow(order[t0 + t], l); },
+      [&](int l, int i) { return DFPair{Gsh[(size_t)l * nsel + i], Gsl[(size_t)l * nsel + i]}; },
       [&](int t, int i, double v) {
         const double d = dg[order[s0 + i]] - dg[order[t0 + t]];
         Th[(size_t)i * ncomp + t] = d != 0.0 ? v / d : INFINITY;
@@ -747,27 +763,30 @@ __device__ bool newton_density_ov(double *S, const double *V, const double *Fm, 
   }
   mx = jblock_reduce(mx, red, true);  // synchronises: Th32 complete, Th no longer read
   if (!(mx <= NEWTON_THETA)) return false;
+  // products of small quantities in FP32 (V's hi part: V to 2^-23, on terms ~1e-5)
   tile_product_mnk_t<float>(
       nsel, n, ncomp, false, [&](int i, int t) { return Th32[i * ncomp + t]; },
-      [&](int t, int k) { return V32[order[t0 + t] * n + k]; },
+      [&](int t, int k) { return Vh[(size_t)order[t0 + t] * n + k]; },
       [&](int i, int k, float v) {
         const double c = V[(size_t)order[s0 + i] * n + k] + (double)v;
-        C1[(size_t)i * n + k] = c;
         C1_32[i * n + k] = (float)c;
+        C1[(size_t)i * n + k] = c;
       });
   tile_product_mnk_t<float>(
       nsel, nsel, ncomp, false, [&](int i, int t) { return Th32[i * ncomp + t]; },
       [&](int t, int j) { return Th32[j * ncomp + t]; }, [&](int i, int j, float v) { E32[i * nsel + j] = v; });
   __syncthreads();
-  double *U = Gs;  // V_S F is no longer needed
+  float *Uh = Gsh, *Ul = Gsl;  // V_S F is no longer needed
   tile_product_mnk_t<float>(
       nsel, n, nsel, false, [&](int i, int l) { return E32[i * nsel + l]; },
       [&](int l, int k) { return C1_32[l * n + k]; },
-      [&](int i, int k, float v) { U[(size_t)i * n + k] = C1[(size_t)i * n + k] - 0.5 * (double)v; });
+      [&](int i, int k, float v) {
+        split_f64(C1[(size_t)i * n + k] - 0.5 * (double)v, Uh[(size_t)i * n + k], Ul[(size_t)i * n + k]);
+      });
   __syncthreads();
   tile_product_df(
-      n, n, nsel, true, [&](int a, int k) { return U[(size_t)k * n + a]; },
-      [&](int k, int c) { return U[(size_t)k * n + c]; },
+      n, n, nsel, true, [&](int a, int k) { return DFPair{Uh[(size_t)k * n + a], Ul[(size_t)k * n + a]}; },
+      [&](int k, int c) { return DFPair{Uh[(size_t)k * n + c], Ul[(size_t)k * n + c]}; },
       [&](int a, int c, double s) {
         if (c < a) return;
         const double v = use_occ ? 2.0 * s : (a == c ? 2.0 : 0.0) - 2.0 * s;

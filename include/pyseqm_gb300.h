@@ -163,10 +163,11 @@ int seqm_density_jacobi(const seqm_batch *b, const double *F, double *P, double 
  * Limit: sum of norb^2 over the batch <= SEQM_NOALLOC_JACOBI_DOUBLES, else SEQM_E_TOO_LARGE
  * and no launch.  A batch whose b->max_norb is above 160 is rejected the same way, as a whole
  * (seqm_density_jacobi instead skips such molecules with status -2 and solves the rest).
- * Reads mat_off[nmol] back first and waits for that read, so every call synchronises
- * `stream` once before it launches.
+ * The size check takes b->mat_total; when that is 0 the call reads mat_off[nmol] back and waits
+ * for that read (it synchronises `stream` once, which a stream capture cannot hold).
  * The first call on a device resolves the array's device address (cudaGetSymbolAddress)
- * with that device current; make that first call before any stream capture.
+ * with that device current; make that first call before any stream capture.  Later calls with
+ * b->mat_total set can be captured.
  * All calls share the array: calls that overlap on the GPU race. */
 #define SEQM_NOALLOC_JACOBI_DOUBLES (1 << 21)
 int seqm_density_jacobi_noalloc(const seqm_batch *b, const double *F, double *P, double *evals, double *evecs,

@@ -720,43 +720,56 @@ __device__ int fp32_sweeps_orth(double *A, int lda, double *V, double *G, int n,
 // The products of small quantities (Theta V_T, Theta Theta^T, E C') run in FP32 on FP32
 // copies (rounding ~1e-7 of terms <= 1e-5); V_S F, the coupling block and U^T U in FP64.  The
 // diagonal dg only enters the denominators, where FP32 accuracy is enough.
-// Scratch: S (shared, >= n^2 doubles) = [V_S F, later U (both as FP32 hi | lo) | Theta, later
-// C'32 | E32 | Theta32]; G (global, n^2 doubles, P's block) = [V hi (floats) | V lo, later C'
-// (FP64)].  Every operand of the double-float products is split into FP32 hi + lo once, where it
-// is produced (V on entry, V_S F and U by their products), instead of on each of the ~n/4 loads
-// by the register tiles.  Returns false, with P untouched, when the rotation is too large (or the
-// gap not positive).
+// Every operand of the double-float products is split into FP32 hi + lo once, where it is
+// produced (F and V on entry, V_S F and U by their products), instead of on each of the ~n/4
+// loads by the register tiles.  Scratch, in doubles (sn = nsel n, tn = ncomp n, st = nsel ncomp;
+// S shared, >= n^2; G global, P's block, n^2):
+//   S: F split [0, n^2)                  -> V_T split [0, tn) | Theta [tn, tn + st), later C'32 |
+//                                           E32 [tn + st, tn + st + nsel^2 / 2); U split over V_T
+//   G: V_S split [0, sn), later Theta32 | V_S F split [sn, 2 sn), later C' (FP64); then P
+// (tn + st = n^2 - nsel^2, 2 sn <= n^2 as nsel <= n / 2).  Returns false, with P untouched, when
+// the rotation is too large (or the gap not positive).
 __device__ bool newton_density_ov(double *S, const double *V, const double *Fm, double *G, double *Pm, int n,
                                   int nocc, const double *dg, const int *order, double *red) {
   const bool use_occ = nocc <= n - nocc;
   const int nsel = use_occ ? nocc : n - nocc, ncomp = n - nsel;
   const int s0 = use_occ ? 0 : nocc, t0 = use_occ ? nocc : 0;
-  const size_t sn = (size_t)nsel * n;
-  float *Gsh = reinterpret_cast<float *>(S), *Gsl = Gsh + sn;  // (V_S F)^T: n rows of nsel, split
-  double *Th = S + sn;
-  float *E32 = reinterpret_cast<float *>(Th + (size_t)nsel * ncomp), *Th32 = E32 + (size_t)nsel * nsel;
-  float *C1_32 = reinterpret_cast<float *>(Th);
-  float *Vh = reinterpret_cast<float *>(G), *Vl = Vh + (size_t)n * n;
-  double *C1 = G + ((size_t)n * n + 1) / 2;  // over V lo, dead by then; ends at or before n^2 (nsel <= n / 2)
-  for (int idx = threadIdx.x; idx < n * n; idx += NTB) split_f64(V[idx], Vh[idx], Vl[idx]);
+  const size_t nn = (size_t)n * n, sn = (size_t)nsel * n, tn = (size_t)ncomp * n, st = (size_t)nsel * ncomp;
+  float *Fh = reinterpret_cast<float *>(S), *Fl = Fh + nn;
+  float *Vsh = reinterpret_cast<float *>(G), *Vsl = Vsh + sn;          // V_S rows, split
+  float *Gsh = reinterpret_cast<float *>(G + sn), *Gsl = Gsh + sn;    // (V_S F)^T: n rows of nsel, split
+  for (int idx = threadIdx.x; idx < n * n; idx += NTB) split_f64(Fm[idx], Fh[idx], Fl[idx]);
+  for (int idx = threadIdx.x; idx < (int)sn; idx += NTB) {
+    const int i = idx / n, l = idx - i * n;
+    split_f64(V[(size_t)order[s0 + i] * n + l], Vsh[idx], Vsl[idx]);
+  }
   __syncthreads();
-  auto Vrow = [&](int r, int l) { return DFPair{Vh[(size_t)r * n + l], Vl[(size_t)r * n + l]}; };
   tile_product_df(
-      nsel, n, n, false, [&](int i, int l) { return Vrow(order[s0 + i], l); },
-      [&](int l, int j) { return Fm[(size_t)l * n + j]; },
+      nsel, n, n, false, [&](int i, int l) { return DFPair{Vsh[(size_t)i * n + l], Vsl[(size_t)i * n + l]}; },
+      [&](int l, int j) { return DFPair{Fh[(size_t)l * n + j], Fl[(size_t)l * n + j]}; },
       [&](int i, int j, double v) { split_f64(v, Gsh[(size_t)j * nsel + i], Gsl[(size_t)j * nsel + i]); });
   __syncthreads();
-  // a_st for t (rows, contiguous V_T rows broadcast) x s (columns of (V_S F)^T, contiguous)
+  // F is dead: the V_T rows, split, over it
+  float *Vth = reinterpret_cast<float *>(S), *Vtl = Vth + tn;
+  double *Th = S + tn;
+  for (int idx = threadIdx.x; idx < (int)tn; idx += NTB) {
+    const int t = idx / n, l = idx - t * n;
+    split_f64(V[(size_t)order[t0 + t] * n + l], Vth[idx], Vtl[idx]);
+  }
+  __syncthreads();
+  // a_st for t (rows of V_T) x s (columns of (V_S F)^T, contiguous)
   tile_product_df(
-      ncomp, nsel, n, false, [&](int t, int l) { return Vrow(order[t0 + t], l); },
+      ncomp, nsel, n, false, [&](int t, int l) { return DFPair{Vth[(size_t)t * n + l], Vtl[(size_t)t * n + l]}; },
       [&](int l, int i) { return DFPair{Gsh[(size_t)l * nsel + i], Gsl[(size_t)l * nsel + i]}; },
       [&](int t, int i, double v) {
         const double d = dg[order[s0 + i]] - dg[order[t0 + t]];
         Th[(size_t)i * ncomp + t] = d != 0.0 ? v / d : INFINITY;
       });
   __syncthreads();
+  float *Th32 = reinterpret_cast<float *>(G);  // over the V_S split, dead now
+  float *E32 = reinterpret_cast<float *>(S + tn + st);
   double mx = 0.0;
-  for (int idx = threadIdx.x; idx < nsel * ncomp; idx += NTB) {
+  for (int idx = threadIdx.x; idx < (int)st; idx += NTB) {
     const double th = Th[idx], a = fabs(th);
     mx = fmax(mx, isnan(a) ? INFINITY : a);
     Th32[idx] = (float)th;
@@ -764,9 +777,11 @@ __device__ bool newton_density_ov(double *S, const double *V, const double *Fm, 
   mx = jblock_reduce(mx, red, true);  // synchronises: Th32 complete, Th no longer read
   if (!(mx <= NEWTON_THETA)) return false;
   // products of small quantities in FP32 (V's hi part: V to 2^-23, on terms ~1e-5)
+  float *C1_32 = reinterpret_cast<float *>(Th);  // Theta is dead
+  double *C1 = G + sn;                            // over the V_S F split, dead
   tile_product_mnk_t<float>(
       nsel, n, ncomp, false, [&](int i, int t) { return Th32[i * ncomp + t]; },
-      [&](int t, int k) { return Vh[(size_t)order[t0 + t] * n + k]; },
+      [&](int t, int k) { return Vth[(size_t)t * n + k]; },
       [&](int i, int k, float v) {
         const double c = V[(size_t)order[s0 + i] * n + k] + (double)v;
         C1_32[i * n + k] = (float)c;
@@ -776,7 +791,7 @@ __device__ bool newton_density_ov(double *S, const double *V, const double *Fm, 
       nsel, nsel, ncomp, false, [&](int i, int t) { return Th32[i * ncomp + t]; },
       [&](int t, int j) { return Th32[j * ncomp + t]; }, [&](int i, int j, float v) { E32[i * nsel + j] = v; });
   __syncthreads();
-  float *Uh = Gsh, *Ul = Gsl;  // V_S F is no longer needed
+  float *Uh = reinterpret_cast<float *>(S), *Ul = Uh + sn;  // over the V_T split, dead (sn <= tn)
   tile_product_mnk_t<float>(
       nsel, n, nsel, false, [&](int i, int l) { return E32[i * nsel + l]; },
       [&](int l, int k) { return C1_32[l * n + k]; },
@@ -1212,11 +1227,9 @@ extern "C" int seqm_density_jacobi_noalloc(const seqm_batch *bp, const double *F
   if (b.nmol == 0) return SEQM_OK;
   if (b.max_norb > JMAX_N) return SEQM_E_TOO_LARGE;
   cudaStream_t s = (cudaStream_t)stream;
-  // total dense-matrix size = mat_off[nmol] (device); one small read, then the size check
+  // total dense-matrix size: b.mat_total, or mat_off[nmol] read back (one small read), then the size check
   int64_t total = 0;
-  if (cudaMemcpyAsync(&total, b.mol_mat_off + b.nmol, sizeof(int64_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-      cudaStreamSynchronize(s) != cudaSuccess)
-    return SEQM_E_CUDA;
+  if (batch_total(b, s, &total) != SEQM_OK) return SEQM_E_CUDA;
   if (total < 0 || (size_t)total > NOALLOC_DOUBLES) return SEQM_E_TOO_LARGE;
   double *work = nullptr;
   int rc = jacobi_scratch_address(&work);

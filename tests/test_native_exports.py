@@ -88,3 +88,25 @@ def test_scf_state_struct_layout_matches_header(tmp_path):
     assert int(out["sizeof"]) == ct.sizeof(native.ScfState)
     for f in fields:
         assert int(out[f]) == getattr(native.ScfState, f).offset, f
+
+
+def test_scf_scratch_size_matches_header(tmp_path):
+    """native.scf_scratch_doubles (the fused iteration's scratch that BatchSCF allocates) agrees
+    with the header's SEQM_SCF_SCRATCH_DOUBLES for a few batch shapes."""
+    import shutil
+    import subprocess
+
+    import pytest
+
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    shapes = [(1, 3, 3, 7), (4096, 137263, 2905604, 369032), (2, 1, 0, 1)]
+    src = tmp_path / "scratch.c"
+    lines = ["#include <stdio.h>", '#include "pyseqm_gb300.h"', "int main(void) {"]
+    lines += [f'  printf("%zu\\n", (size_t)SEQM_SCF_SCRATCH_DOUBLES({a}, {b}, {c}, {d}));' for a, b, c, d in shapes]
+    lines += ["  return 0;", "}"]
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "scratch"
+    subprocess.run(["gcc", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert got == [native.scf_scratch_doubles(*s) for s in shapes]

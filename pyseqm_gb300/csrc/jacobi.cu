@@ -297,10 +297,14 @@ __device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_swee
   // the FP64 pipe), in the shared arrays' storage
   T *rc = reinterpret_cast<T *>(sh.rc), *rs = reinterpret_cast<T *>(sh.rs), *rt = reinterpret_cast<T *>(sh.rt);
   T *rdp = reinterpret_cast<T *>(sh.rdp), *rdq = reinterpret_cast<T *>(sh.rdq);  // rotated diagonal
+  // FP32 path: this warp's rotations of a step, slots wid, wid + warps, ... (<= 32 for every
+  // launch class: np <= 16 at 2 warps, <= 32 at 4, <= 80 at 8 or more)
+  const int nrot = np > wid ? (np - wid + NTB_W - 1) / NTB_W : 0;
   for (int sweep = 0; sweep <= max_sweeps; ++sweep) {
     if (offdiag_max(A, lda, n, sh.red) <= tol) return sweep;
     if (sweep == max_sweeps) break;
     for (int step = 0; step < nsteps; ++step) {
+      if constexpr (sizeof(T) == 8) {
       if (tid < np) {
         // round-robin partners of slot tid at this step (no integer division)
         int a = npad - 1, c = step;
@@ -337,87 +341,122 @@ __device__ int jacobi_solve(T *A, int lda, T *V, int n, double tol, int max_swee
         sh.rflag[tid] = fl;
       }
       __syncthreads();
+      }
       if constexpr (sizeof(T) == 4) {
         // FP32: A <- J^T A J as a row pass (rows p, q of A and of V, lanes along the rows) and a
         // column pass (columns p, q of A, lanes down the columns; the odd stride keeps them
-        // conflict-free); the pass writes the rotated 2x2 block exactly (a_pq = 0).  Above 96
-        // basis functions each lane loads all of its (at most JMAX_N / 32) elements of the two
-        // rows or columns before it stores any (the rows are disjoint, but only this order lets
-        // the loads overlap; measured 11-28 % faster there); smaller molecules, whose lanes hold
-        // at most three elements, keep the plain loop (the unrolled form was slower for them)
+        // conflict-free); the pass writes the rotated 2x2 block exactly (a_pq = 0).  Every warp
+        // computes the parameters of its own rotations (slots wid, wid + warps, ...; lane k the
+        // k-th) and hands them to its lanes by shuffles, so a step takes two barriers and no
+        // shared-memory round trip for them (a rotation's pivots lie in its own two rows, which no
+        // other warp touches before the row pass).  Above 96 basis functions each lane loads all
+        // of its (at most JMAX_N / 32) elements of the two rows or columns before it stores any
+        // (the rows are disjoint, but only this order lets the loads overlap; measured 11-28 %
+        // faster there); smaller molecules, whose lanes hold at most three elements, keep the
+        // plain loop (the unrolled form was slower for them)
         constexpr int KL = (JMAX_N + 31) / 32;
+        constexpr unsigned FULL = 0xffffffffu;
         const bool wide = n > 96;
-        for (int i = wid; i < np; i += NTB_W) {
-          if (!sh.rflag[i]) continue;
-          const T c = rc[i], sn = rs[i];
-          T *ap = A + sh.rp[i] * lda, *aq = A + sh.rq[i] * lda;
-          T *vp = V + (size_t)sh.rp[i] * n, *vq = V + (size_t)sh.rq[i] * n;
+        int mp = 0, mq = 0, mfl = 0;
+        T mc = 1, ms = 0, mdp = 0, mdq = 0;
+        if (lane < nrot) {
+          const int slot = wid + NTB_W * lane;
+          int a = npad - 1, c = step;
+          if (slot != 0) {
+            a = step + slot;
+            if (a >= npad - 1) a -= npad - 1;
+            c = step - slot;
+            if (c < 0) c += npad - 1;
+          }
+          mp = min(a, c);
+          mq = max(a, c);
+          if (mq < n) {
+            const T apq = A[mp * lda + mq], app = A[mp * lda + mp], aqq = A[mq * lda + mq];
+            if (fabs(apq) > ttol && (tratio == T(0) || fabs(apq) > tratio * fabs(aqq - app))) {
+              const T theta = (aqq - app) / (T(2) * apq);
+              T t = T(1) / (fabs(theta) + sqrt(theta * theta + T(1)));
+              if (theta < T(0)) t = -t;
+              mc = T(1) / sqrt(t * t + T(1));
+              ms = t * mc;
+              mdp = app - t * apq;
+              mdq = aqq + t * apq;
+              mfl = 1;
+            }
+          }
+        }
+        for (int k = 0; k < nrot; ++k) {
+          if (!__shfl_sync(FULL, mfl, k)) continue;  // uniform over the warp
+          const int p = __shfl_sync(FULL, mp, k), q = __shfl_sync(FULL, mq, k);
+          const T c = __shfl_sync(FULL, mc, k), sn = __shfl_sync(FULL, ms, k);
+          T *ap = A + p * lda, *aq = A + q * lda;
+          T *vp = V + (size_t)p * n, *vq = V + (size_t)q * n;
           if (wide) {
             T a[KL], b[KL], e[KL], f[KL];
 #pragma unroll
             for (int u = 0; u < KL; ++u) {
-              const int k = lane + 32 * u;
-              if (k < n) {
-                a[u] = ap[k];
-                b[u] = aq[k];
-                e[u] = vp[k];
-                f[u] = vq[k];
+              const int kk = lane + 32 * u;
+              if (kk < n) {
+                a[u] = ap[kk];
+                b[u] = aq[kk];
+                e[u] = vp[kk];
+                f[u] = vq[kk];
               }
             }
 #pragma unroll
             for (int u = 0; u < KL; ++u) {
-              const int k = lane + 32 * u;
-              if (k < n) {
-                ap[k] = c * a[u] - sn * b[u];
-                aq[k] = sn * a[u] + c * b[u];
-                vp[k] = c * e[u] - sn * f[u];
-                vq[k] = sn * e[u] + c * f[u];
+              const int kk = lane + 32 * u;
+              if (kk < n) {
+                ap[kk] = c * a[u] - sn * b[u];
+                aq[kk] = sn * a[u] + c * b[u];
+                vp[kk] = c * e[u] - sn * f[u];
+                vq[kk] = sn * e[u] + c * f[u];
               }
             }
           } else {
-            for (int k = lane; k < n; k += 32) {
-              const T a = ap[k], b = aq[k], e = vp[k], f = vq[k];
-              ap[k] = c * a - sn * b;
-              aq[k] = sn * a + c * b;
-              vp[k] = c * e - sn * f;
-              vq[k] = sn * e + c * f;
+            for (int kk = lane; kk < n; kk += 32) {
+              const T a = ap[kk], b = aq[kk], e = vp[kk], f = vq[kk];
+              ap[kk] = c * a - sn * b;
+              aq[kk] = sn * a + c * b;
+              vp[kk] = c * e - sn * f;
+              vq[kk] = sn * e + c * f;
             }
           }
         }
         __syncthreads();
-        for (int i = wid; i < np; i += NTB_W) {
-          if (!sh.rflag[i]) continue;
-          const T c = rc[i], sn = rs[i];
-          const int p = sh.rp[i], q = sh.rq[i];
+        for (int k = 0; k < nrot; ++k) {
+          if (!__shfl_sync(FULL, mfl, k)) continue;
+          const int p = __shfl_sync(FULL, mp, k), q = __shfl_sync(FULL, mq, k);
+          const T c = __shfl_sync(FULL, mc, k), sn = __shfl_sync(FULL, ms, k);
+          const T dp = __shfl_sync(FULL, mdp, k), dq = __shfl_sync(FULL, mdq, k);
           if (wide) {
             T a[KL], b[KL];
 #pragma unroll
             for (int u = 0; u < KL; ++u) {
-              const int k = lane + 32 * u;
-              if (k < n) {
-                a[u] = A[k * lda + p];
-                b[u] = A[k * lda + q];
+              const int kk = lane + 32 * u;
+              if (kk < n) {
+                a[u] = A[kk * lda + p];
+                b[u] = A[kk * lda + q];
               }
             }
 #pragma unroll
             for (int u = 0; u < KL; ++u) {
-              const int k = lane + 32 * u;
-              if (k < n) {
+              const int kk = lane + 32 * u;
+              if (kk < n) {
                 T xp = c * a[u] - sn * b[u], xq = sn * a[u] + c * b[u];
-                if (k == p) { xp = rdp[i]; xq = T(0); }
-                if (k == q) { xp = T(0); xq = rdq[i]; }
-                A[k * lda + p] = xp;
-                A[k * lda + q] = xq;
+                if (kk == p) { xp = dp; xq = T(0); }
+                if (kk == q) { xp = T(0); xq = dq; }
+                A[kk * lda + p] = xp;
+                A[kk * lda + q] = xq;
               }
             }
           } else {
-            for (int k = lane; k < n; k += 32) {
-              const T a = A[k * lda + p], b = A[k * lda + q];
+            for (int kk = lane; kk < n; kk += 32) {
+              const T a = A[kk * lda + p], b = A[kk * lda + q];
               T xp = c * a - sn * b, xq = sn * a + c * b;
-              if (k == p) { xp = rdp[i]; xq = T(0); }
-              if (k == q) { xp = T(0); xq = rdq[i]; }
-              A[k * lda + p] = xp;
-              A[k * lda + q] = xq;
+              if (kk == p) { xp = dp; xq = T(0); }
+              if (kk == q) { xp = T(0); xq = dq; }
+              A[kk * lda + p] = xp;
+              A[kk * lda + q] = xq;
             }
           }
         }

@@ -683,29 +683,25 @@ __device__ void newton_density(double *A, int lda, const double *V, double *G, d
 
 constexpr double NEWTON_THETA = 1.0e-5;  // largest occupied-virtual rotation the first-order density takes
 constexpr double EIG_PT_RATIO = 3.0e-3;  // largest coupling / splitting for second-order eigenvalues
+// a warm start whose largest occupied-virtual ratio |a_st| / gap is at most ROT_THETA takes one
+// rotation (rotate_orth) instead of FP32 sweeps, when its ||Theta||_F stays within ROT_NORM
+// (W = I + K + K^2 / 2 orthogonal to ||K||^4 / 4 <= 2.5e-9, which the lift's Newton-Schulz step removes)
+constexpr double ROT_THETA = 1.0e-3;
+constexpr double ROT_NORM = 1.0e-2;
+constexpr int ROT_ITERS = 3;  // fixed-point passes of the rotation's Sylvester equation
 
-// FP32 sweeps for the density-only step, without FP64 rotation work: A32 (float, overlaying
-// A) is swept to max |a_pq| <= tol32 with the rotations W (float, behind A32); dg / rank /
-// order take the swept diagonal; X = W V (warm) or W (cold) is formed in FP32 and stored in V,
-// so X holds FP32 values whose products are exact; D = X X^T - I is summed to FP64 accuracy
-// (double-float) from X^T staged in shared memory (conflict-free rows) and kept as FP32 (|D| ~ 1e-6);
-// one Newton-Schulz step V <- X - D X / 2 (the small product D X in FP32) leaves the rows of V
-// orthonormal to ~1e-13.  G (floats): X32; shared: A32, then V (warm) for X = W V, then X^T, and
-// W32, then D.  Returns the FP32 sweeps taken.
-__device__ int fp32_sweeps_orth(double *A, int lda, double *V, double *G, int n, double tol32, bool is_warm,
-                                double *dg, int *rank, int *order, JShared &sh) {
+// The lift of FP32 rotations W (float, rows of stride n behind A32 in shared memory, orthogonal
+// to FP32 accuracy) to FP64-orthonormal eigenvector rows, without FP64 rotation work:
+// X = W V (warm) or W (cold) is formed in FP32 and stored in V, so X holds FP32 values whose
+// products are exact; D = X X^T - I is summed to FP64 accuracy (double-float) from X^T staged in
+// shared memory (conflict-free rows) and kept as FP32 (|D| ~ 1e-6); one Newton-Schulz step
+// V <- X - D X / 2 (the small product D X in FP32) leaves the rows of V orthonormal to ~1e-13.
+// A32 is dead on entry.  G (floats): X32; shared: V (warm) over A32 for X = W V, then X^T, and
+// W32, then D.
+__device__ void lift_rotations(double *A, int lda, double *V, double *G, int n, bool is_warm) {
   const int tid = threadIdx.x;
   float *A32 = reinterpret_cast<float *>(A), *W32 = A32 + (size_t)n * lda;
   float *X32 = reinterpret_cast<float *>(G);
-  for (int idx = tid; idx < n * n; idx += NTB) {
-    int i = idx / n, j = idx - i * n;
-    W32[idx] = i == j ? 1.0f : 0.0f;
-  }
-  __syncthreads();
-  int s32 = jacobi_solve<float>(A32, lda, W32, n, tol32, 20, sh);
-  if (s32 < 0) s32 = 20;
-  __syncthreads();
-  rank_diag(A32, lda, n, dg, rank, order);
   if (is_warm) {
     // V in FP32 over the swept A32 (dead now), so that both operands of X = W V are in shared memory
     float *V32 = A32;
@@ -747,7 +743,123 @@ __device__ int fp32_sweeps_orth(double *A, int lda, double *V, double *G, int n,
       n, false, [&](int k, int l) { return D32s[k * n + l]; }, [&](int l, int j) { return XT[j * lda + l]; },
       [&](int k, int j, float v) { V[(size_t)k * n + j] -= 0.5 * (double)v; });
   __syncthreads();
+}
+
+// FP32 sweeps for the density-only step: A32 (float, overlaying A) is swept to
+// max |a_pq| <= tol32 with the rotations W (float, behind A32); dg / rank / order take the swept
+// diagonal; then the lift above.  Returns the FP32 sweeps taken.
+__device__ int fp32_sweeps_orth(double *A, int lda, double *V, double *G, int n, double tol32, bool is_warm,
+                                double *dg, int *rank, int *order, JShared &sh) {
+  float *A32 = reinterpret_cast<float *>(A), *W32 = A32 + (size_t)n * lda;
+  for (int idx = threadIdx.x; idx < n * n; idx += NTB) {
+    int i = idx / n, j = idx - i * n;
+    W32[idx] = i == j ? 1.0f : 0.0f;
+  }
+  __syncthreads();
+  int s32 = jacobi_solve<float>(A32, lda, W32, n, tol32, 20, sh);
+  if (s32 < 0) s32 = 20;
+  __syncthreads();
+  rank_diag(A32, lda, n, dg, rank, order);
+  lift_rotations(A, lda, V, G, n, is_warm);
   return s32;
+}
+
+// A warm start whose occupied-virtual block is small, brought to block-diagonal form by one
+// rotation instead of FP32 sweeps.  With S the smaller of the occupied / virtual sets (ranks from
+// dg, the diagonal of A32 = V F V^T) and T its complement, the rotation W = exp(K), K_st =
+// Theta_st = -K_ts, zeroes the S-T block of W A W^T to first order in Theta when
+//   Theta_st (d_s - d_t) = a_st + (Theta A'_TT)_st - (A'_SS Theta)_st   (A' without its diagonal d),
+// which ROT_ITERS fixed-point passes solve from Theta = 0 (the first gives the first-order
+// theta_st = a_st / (d_s - d_t); the others take in the couplings within the two blocks that
+// earlier rotations leave in a warm start); the S-T block left is of third order in Theta, next to
+// A32's FP32 rounding.  W = I + K + K^2 / 2 (K^2 = -Theta Theta^T on S x S, -Theta^T Theta on
+// T x T; W W^T - I = K^4 / 4) in FP32 in the sweeps' rotation buffer, then lift_rotations.  The
+// blocks within S and T stay as they are: the density needs the S subspace only.  Shared: A'_TT
+// and A'_SS (permuted to rank order) where W is formed afterwards; G (floats): Theta^T, Theta
+// Theta^T and Theta^T Theta in [0, n^2 - st), a_ST and two Theta buffers in [n^2, n^2 + 3 st)
+// (st = |S| |T| <= n^2 / 4).  Returns false, with A32 and V untouched, when ||Theta||_F exceeds
+// ROT_NORM (or is not finite) before or after the passes.
+__device__ bool rotate_orth(double *A, int lda, double *V, double *G, int n, int nocc, const double *dg,
+                            const int *rank, const int *order, double *red) {
+  const int tid = threadIdx.x;
+  const bool use_occ = nocc <= n - nocc;
+  const int nsel = use_occ ? nocc : n - nocc, ncomp = n - nsel;
+  const int s0 = use_occ ? 0 : nocc, t0 = use_occ ? nocc : 0;
+  const int st = nsel * ncomp;
+  const float *A32 = reinterpret_cast<const float *>(A);
+  float *W32 = reinterpret_cast<float *>(A) + (size_t)n * lda;
+  float *Att = W32, *Ass = W32 + ncomp * ncomp;  // ncomp^2 + nsel^2 <= n^2
+  float *Gf = reinterpret_cast<float *>(G);
+  float *ThT = Gf, *Qt = Gf + st, *Qs = Qt + ncomp * ncomp;  // st + ncomp^2 + nsel^2 = n^2 - st
+  float *Ast = Gf + (size_t)n * n, *cur = Ast + st, *nxt = cur + st;
+  const float rot_norm2 = (float)(ROT_NORM * ROT_NORM);
+  for (int idx = tid; idx < ncomp * ncomp; idx += NTB) {
+    const int u = idx / ncomp, t = idx - u * ncomp;
+    Att[idx] = u == t ? 0.0f : A32[order[t0 + u] * lda + order[t0 + t]];
+  }
+  for (int idx = tid; idx < nsel * nsel; idx += NTB) {
+    const int i = idx / nsel, j = idx - i * nsel;
+    Ass[idx] = i == j ? 0.0f : A32[order[s0 + i] * lda + order[s0 + j]];
+  }
+  double nrm = 0.0;
+  for (int idx = tid; idx < st; idx += NTB) {
+    const int i = idx / ncomp, t = idx - i * ncomp;
+    const int rs = order[s0 + i], rt = order[t0 + t];
+    const float a = A32[rs * lda + rt], th = a / (float)(dg[rs] - dg[rt]);
+    Ast[idx] = a;
+    cur[idx] = th;
+    nrm += (double)th * th;
+  }
+  nrm = jblock_reduce(nrm, red, false);  // synchronises: the gathered blocks and Theta complete
+  if (!(nrm <= rot_norm2)) return false;
+  for (int it = 1; it < ROT_ITERS; ++it) {
+    tile_product_mnk_t<float>(
+        nsel, ncomp, ncomp, false, [&](int i, int u) { return cur[i * ncomp + u]; },
+        [&](int u, int t) { return Att[u * ncomp + t]; },
+        [&](int i, int t, float v) { nxt[i * ncomp + t] = Ast[i * ncomp + t] + v; });
+    __syncthreads();
+    tile_product_mnk_t<float>(
+        nsel, ncomp, nsel, false, [&](int i, int j) { return Ass[i * nsel + j]; },
+        [&](int j, int t) { return cur[j * ncomp + t]; },
+        [&](int i, int t, float v) {
+          nxt[i * ncomp + t] = (nxt[i * ncomp + t] - v) / (float)(dg[order[s0 + i]] - dg[order[t0 + t]]);
+        });
+    __syncthreads();
+    float *sw = cur;
+    cur = nxt;
+    nxt = sw;
+  }
+  nrm = 0.0;
+  for (int idx = tid; idx < st; idx += NTB) {
+    const float th = cur[idx];
+    nrm += (double)th * th;
+    const int i = idx / ncomp, t = idx - i * ncomp;
+    ThT[t * nsel + i] = th;
+  }
+  nrm = jblock_reduce(nrm, red, false);  // synchronises: Theta^T complete
+  if (!(nrm <= rot_norm2)) return false;
+  tile_product_mnk_t<float>(
+      nsel, nsel, ncomp, false, [&](int i, int u) { return ThT[u * nsel + i]; },
+      [&](int u, int j) { return ThT[u * nsel + j]; }, [&](int i, int j, float v) { Qs[i * nsel + j] = v; });
+  tile_product_mnk_t<float>(
+      ncomp, ncomp, nsel, false, [&](int t, int i) { return cur[i * ncomp + t]; },
+      [&](int i, int u) { return cur[i * ncomp + u]; }, [&](int t, int u, float v) { Qt[t * ncomp + u] = v; });
+  __syncthreads();
+  for (int idx = tid; idx < n * n; idx += NTB) {  // A'_TT, A'_SS dead: W over them
+    const int r = idx / n, c = idx - r * n;
+    const int kr = rank[r], kc = rank[c];
+    const bool sr = (unsigned)(kr - s0) < (unsigned)nsel, sc = (unsigned)(kc - s0) < (unsigned)nsel;
+    const float dl = r == c ? 1.0f : 0.0f;
+    float w;
+    if (sr && !sc) w = cur[(kr - s0) * ncomp + (kc - t0)];
+    else if (!sr && sc) w = -cur[(kc - s0) * ncomp + (kr - t0)];
+    else if (sr) w = dl - 0.5f * Qs[(kr - s0) * nsel + (kc - s0)];
+    else w = dl - 0.5f * Qt[(kr - t0) * ncomp + (kc - t0)];
+    W32[idx] = w;
+  }
+  __syncthreads();
+  lift_rotations(A, lda, V, G, n, true);
+  return true;
 }
 
 // First-order density from orthonormal eigenvector rows V that nearly diagonalise F, with
@@ -921,9 +1033,23 @@ __global__ void __launch_bounds__(NT_J) k_jacobi(seqm_batch b, const double *__r
       __syncthreads();
     }
     rank_diag(A32, lda, n, dg, rank, order);
-    if (!is_warm || ov_theta(A32, lda, n, nocc, dg, order, sh.red) > 0.5 * NEWTON_THETA)
-      s32 = fp32_sweeps_orth(A, lda, V, G, n, 2.0e-7 * fro, is_warm, dg, rank, order, sh);
-    if (newton_density_ov(A, V, Fm, G, P + mo, n, nocc, dg, order, sh.red)) {
+    const double th32 = is_warm ? ov_theta(A32, lda, n, nocc, dg, order, sh.red) : INFINITY;
+    bool rotated = false;
+    if (th32 > 0.5 * NEWTON_THETA) {
+      // a small rotation in one step (reported as one FP32 sweep: its lift is the sweeps'),
+      // otherwise sweeps
+      rotated = th32 <= ROT_THETA && rotate_orth(A, lda, V, G, n, nocc, dg, rank, order, sh.red);
+      s32 = rotated ? 1 : fp32_sweeps_orth(A, lda, V, G, n, 2.0e-7 * fro, is_warm, dg, rank, order, sh);
+    }
+    bool done = newton_density_ov(A, V, Fm, G, P + mo, n, nocc, dg, order, sh.red);
+    if (!done && rotated) {  // the rotation left too large a coupling: sweeps from the rotated rows
+      __syncthreads();
+      form_vfvt32(A, lda, V, Fm, G, n);
+      rank_diag(A32, lda, n, dg, rank, order);
+      s32 = 1 + fp32_sweeps_orth(A, lda, V, G, n, 2.0e-7 * fro, true, dg, rank, order, sh);
+      done = newton_density_ov(A, V, Fm, G, P + mo, n, nocc, dg, order, sh.red);
+    }
+    if (done) {
       if (tid == 0 && status) status[m] = s32;
       if (evals) {  // diagonal estimates (FP32 accuracy); the final step computes the eigenvalues
         double *e = evals + row_off[m];

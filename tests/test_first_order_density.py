@@ -88,3 +88,77 @@ def test_fp32_sweeps_then_coupling_block_density(n, nocc):
     assert np.abs(P - P_exact).max() < 1e-9
     X2 = 0.5 * P
     assert np.abs(X2 @ X2 - X2).max() < 1e-12
+
+
+def _single_rotation(V, F, nocc, passes=3):
+    """rotate_orth restated: Theta from the fixed-point passes of the block Sylvester equation
+    on A32 = V F V^T (FP32), W = I + K + K^2 / 2 in FP32, then the lift of the FP32 sweeps
+    (X = W V in FP32, D = X X^T - I from exact products, one Newton-Schulz step)."""
+    n = F.shape[0]
+    f32 = np.float32
+    A32 = (V.astype(f32) @ F.astype(f32)) @ V.T.astype(f32)
+    A32 = np.triu(A32) + np.triu(A32, 1).T
+    dg = np.diag(A32).astype(np.float64)
+    order = np.argsort(dg, kind="stable")
+    use_occ = nocc <= n - nocc
+    S, T = (order[:nocc], order[nocc:]) if use_occ else (order[nocc:], order[:nocc])
+    a = A32[np.ix_(S, T)]
+    Att = A32[np.ix_(T, T)].copy()
+    Ass = A32[np.ix_(S, S)].copy()
+    np.fill_diagonal(Att, 0.0)
+    np.fill_diagonal(Ass, 0.0)
+    d = (dg[S][:, None] - dg[T][None, :]).astype(f32)
+    th = (a / d).astype(f32)
+    for _ in range(passes - 1):
+        th = ((a + th @ Att - Ass @ th) / d).astype(f32)
+    W = np.eye(n, dtype=f32)
+    W[np.ix_(S, S)] -= f32(0.5) * (th @ th.T)
+    W[np.ix_(T, T)] -= f32(0.5) * (th.T @ th)
+    W[np.ix_(S, T)] = th
+    W[np.ix_(T, S)] = -th.T
+    X = (W @ V.astype(f32)).astype(np.float64)
+    D = X @ X.T - np.eye(n)
+    V2 = X - 0.5 * (D.astype(f32) @ X.astype(f32)).astype(np.float64)
+    return V2, dg, float(np.sqrt((th.astype(np.float64) ** 2).sum()))
+
+
+@pytest.mark.parametrize("n,nocc", [(144, 96), (98, 49), (60, 20), (12, 8)])
+@pytest.mark.parametrize("dF", [1e-4, 1e-3])
+def test_single_rotation_then_coupling_block_density(n, nocc, dF):
+    """rotate_orth + newton_density_ov: a warm start (eigenvector rows of an earlier Fock matrix,
+    mixed within the occupied and the virtual blocks as earlier rotations leave them) whose
+    occupied-virtual ratio is <= 1e-3 is brought to block-diagonal form by one rotation in place
+    of FP32 sweeps; what coupling is left is at A32's FP32 rounding, the rows stay orthonormal to
+    FP64 accuracy, and the density is good to < 1e-8 (the parity bound is 1e-7)."""
+    from scipy.linalg import expm
+
+    rng = np.random.default_rng(3 * n + nocc)
+    Q, _ = np.linalg.qr(rng.normal(size=(n, n)))
+    ev = np.sort(np.r_[rng.uniform(-40, -10, nocc), rng.uniform(0, 30, n - nocc)])
+    F0 = (Q * ev) @ Q.T
+    F0 = 0.5 * (F0 + F0.T)
+    w0, C0 = np.linalg.eigh(F0)
+    K = rng.normal(size=(n, n)) * dF
+    K = K - K.T
+    M = np.zeros((n, n))
+    M[:nocc, :nocc] = K[:nocc, :nocc]
+    M[nocc:, nocc:] = K[nocc:, nocc:]
+    V = expm(M) @ C0.T  # rows: the occupied and virtual subspaces of F0, mixed within each
+    Pert = rng.normal(size=(n, n))
+    Pert = 0.5 * (Pert + Pert.T)
+    F = F0 + Pert * (10.0 * dF / np.abs(Pert).max())
+    w, C = np.linalg.eigh(F)
+    P_exact = 2.0 * C[:, :nocc] @ C[:, :nocc].T
+    A = V @ F @ V.T
+    dga = np.diag(A)
+    o = np.argsort(dga)
+    ratio = np.abs(A[np.ix_(o[nocc:], o[:nocc])]).max() / (dga[o[nocc]] - dga[o[nocc - 1]])
+    assert 5e-6 < ratio <= 1e-3  # the range the kernel takes this path for
+    V2, dg, norm = _single_rotation(V, F, nocc)
+    assert norm <= 1e-2  # ROT_NORM
+    assert np.abs(V2 @ V2.T - np.eye(n)).max() < 5e-13
+    P, theta = _ov_block_density(V2, F, nocc, dg)
+    assert theta <= 1e-6  # well inside the first-order density's 1e-5
+    assert np.abs(P - P_exact).max() < 1e-8
+    X2 = 0.5 * P
+    assert np.abs(X2 @ X2 - X2).max() < 1e-12

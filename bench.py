@@ -48,7 +48,8 @@ sys.path.insert(0, HERE)
 
 WORKLOAD = {"workload": "AM1 batched single-point SCF, 4096 molecules 50/50 n-alkanes C1-C16 / (H2O)2-24, seed 0",
             "method": "AM1", "nmol": 4096, "scf_eps": 1e-8, "scf_converger": [1], "seed": 0,
-            "density_step": "Jacobi for all molecules (norb <= 144): FP32 sweeps, FP64 orthonormalisation, "
+            "density_step": "Jacobi for all molecules (norb <= 144): FP32 sweeps (one FP32 rotation for a warm "
+                            "start whose occupied-virtual ratio is <= 1e-3), FP64 orthonormalisation, "
                             "coupling block and first-order density; FP64-accurate"}
 METRIC = "SCF solves/s"
 # DRAM bytes of one density call (all size-class launches) of the default workload, from ncu

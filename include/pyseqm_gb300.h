@@ -137,7 +137,8 @@ int seqm_fock(const seqm_batch *b, const double *P, const double *H, const doubl
  * and finish with FP64 sweeps; 0 = FP64 sweeps only.  The result is FP64-accurate either way.
  * density_only != 0 (an SCF iteration: needs P, evecs NULL): once A = V F V^T is nearly
  * diagonal (largest occupied-virtual element over the HOMO-LUMO gap of its diagonal <= 1e-5,
- * directly from a warm start or after the FP32 sweeps), P is formed from the first-order
+ * directly from a warm start, after one FP32 rotation of a warm start whose ratio is <= 1e-3,
+ * or after the FP32 sweeps), P is formed from the first-order
  * occupied-virtual rotation of the smaller set, re-orthonormalised (Loewdin), instead of
  * further FP64 sweeps; error second order in that ratio (<= ~1e-10 in P); evals are then the
  * diagonal of A.  density_only == 2 (evecs NULL: eigenvalues only, as the reference's final

@@ -164,8 +164,8 @@ class BatchSCF:
 
     def _fp64_flops(self, act, density_only, vectors):
         """FP64 flops of one Jacobi density call (device scalar), from the path each molecule
-        took: the status (sweeps) written by the call tells an SCF step with FP32 sweeps from one
-        without."""
+        took: the status (sweeps) written by the call tells an SCF step with FP32 sweeps (or the
+        single FP32 rotation, reported as one sweep: the same lift follows) from one without."""
         n = self.L.nmol
         if vectors or density_only == 0:
             fma = self._fma["final"] * 0  # eigenpairs for output: not counted

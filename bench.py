@@ -55,7 +55,8 @@ METRIC = "SCF solves/s"
 # DRAM bytes of one density call (all size-class launches) of the default workload, from ncu
 # captures of the norb > 114 class of the 2048-molecule batch (92 MB with FP32 sweeps, 74 MB for
 # a warm first-order step, for 37 % of that batch's matrix elements), scaled to the 4096-molecule
-# batch and weighted by the calls of a solve that take FP32 sweeps (73 %)
+# batch and weighted by the calls of a solve that take FP32 sweeps or the single FP32 rotation (73 %;
+# both end in the same lift of the rotations to FP64, which writes what the warm step does not)
 JACOBI_TRAFFIC_BYTES = 4.7e8
 
 

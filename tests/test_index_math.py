@@ -43,3 +43,22 @@ def test_diagonal_walk_of_the_fused_stream():
                     if col >= n:
                         col -= n
                         row += 1
+
+
+def test_single_rotation_scratch_fits():
+    """jacobi.cu rotate_orth: for every basis size the Jacobi step takes (<= 160) and every
+    occupation, its G scratch (Theta^T, Theta Theta^T and Theta^T Theta in [0, n^2 - st); a_ST and
+    two Theta buffers in [n^2, n^2 + 3 st), st = |S| |T|) fits P's n^2 doubles = 2 n^2 floats, and
+    the gathered A'_TT, A'_SS fit the n^2 floats of the sweeps' rotation buffer behind A32
+    (n lda floats) in the launch's cap lda doubles of shared memory."""
+    for n in range(2, 161):
+        lda = n | 1
+        for nocc in range(1, n):
+            use_occ = nocc <= n - nocc
+            nsel = nocc if use_occ else n - nocc
+            ncomp = n - nsel
+            st = nsel * ncomp
+            assert st + ncomp * ncomp + nsel * nsel == n * n - st
+            assert n * n + 3 * st <= 2 * n * n
+            assert ncomp * ncomp + nsel * nsel <= n * n
+            assert n * lda + n * n <= 2 * n * lda
